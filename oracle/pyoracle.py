@@ -1,0 +1,161 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes loader for the CPU oracle (oracle/fms_oracle.cpp).
+
+The oracle restates refeff's real-space FMS arithmetic on the CPU.  Only the
+tests, the smoke check and bench.py's CPU-baseline leg may load it; the product
+library never does.  ``mode=0`` is the f32-faithful restatement of the
+reference's Complex32 path, ``mode=1`` the FP64 oracle.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "build" / "liboracle_fms.so"
+
+F32, F64 = 0, 1
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with its Makefile (g++, OpenMP, -ffp-contract=off)."""
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < (HERE / "fms_oracle.cpp").stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(str(LIB_PATH))
+        _declare(_lib)
+    return _lib
+
+
+_p = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+
+
+def _declare(L):
+    sig = {
+        "oracle_sort_atoms_by_radius": [_i, _p, _p, _p],
+        "oracle_yprep_cluster": [_i, _i, _p, _p, C.c_float, _i, _p, _p, _p, _p, _p],
+        "oracle_sort_representative_atoms": [_i, _i, _i, _p, _p, _p],
+        "oracle_pair_polar_angles": [_i, _p, _p, _i, _p, _p],
+        "oracle_rotation_matrix": [_i, _i, _i, _d, _d, _i, _p],
+        "oracle_polynomials": [_i, _i, _i, _i, _p, _p],
+        "oracle_t_matrix_phase": [_i, _p, _p],
+        "oracle_prefactor": [_i, _p, _p, _d, _p],
+        "oracle_lu_factor_solve": [_i, _i, _p, _i, _p, _p, _p],
+        "oracle_fms_spectrum": [_i, _i, _p, _p, _i, _i, _i, _i, _i, _p, _d, _p, _d, _i, _p, _p, _p, _p, _i],
+        "oracle_driver_setup": [_i, _p, _i, _i, _i, _i, _p, _p, _p, _p, _p, _p, _i],
+        "oracle_fms_energy_intermediates": [_i, _i, _p, _p, _i, _i, _i, _i, _i, _p, _d, _p, _d, _p, _p, _d,
+                                            _p, _p, _p, _p, _p],
+        "oracle_lu_scattering_explicit": [_i, _i, _p, _i, _i, _i, _p, _p, _i, _i, _p, _p, _p, _p],
+        "oracle_iterative_system_explicit": [_i, _i, _p, _i, _p, _p, _d, _p],
+        "oracle_xgllm": [_i, _i, _i, _i, _i, _p, _p],
+        "oracle_t_matrix_element": [_i, _i, _i, _i, _i, _p, _p, _p, _i, _p],
+        "oracle_free_propagator_element": [_i, _i, _i, _p, _p, _p, _p, _d, _p, _p, _p, _p],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = _i
+    L.oracle_legendre_normalization.argtypes = [_i, _i]
+    L.oracle_legendre_normalization.restype = _d
+    L.oracle_spin_orbit_coefficient.argtypes = [_i, _i, _i, _i]
+    L.oracle_spin_orbit_coefficient.restype = _d
+
+
+def ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_p)
+
+
+def cbuf(values) -> np.ndarray:
+    """Complex array -> interleaved float64 buffer (C-contiguous copy, Fortran order preserved by caller)."""
+    a = np.asarray(values, dtype=np.complex128)
+    return np.ascontiguousarray(a.reshape(-1, order="F")).view(np.float64).copy()
+
+
+def from_cbuf(buf: np.ndarray, shape) -> np.ndarray:
+    return buf.view(np.complex128).reshape(shape, order="F")
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code: int):
+        super().__init__(f"oracle error code {code}")
+        self.code = code
+
+
+def check(rc: int):
+    if rc != 0:
+        raise OracleError(rc)
+
+
+def polynomials(lx, lmaxp1, mmaxp1, rho, mode=F32):
+    out = np.zeros(2 * (lx + 2) * (2 * lx + 3))
+    r = cbuf([rho])
+    check(lib().oracle_polynomials(mode, lx, lmaxp1, mmaxp1, ptr(r), ptr(out)))
+    return from_cbuf(out, (lx + 2, 2 * lx + 3))
+
+
+def rotation_matrix(lmax, mmax, beta, phi, forward, mode=F32):
+    d = 2 * lmax + 1
+    out = np.zeros(2 * d * d * (lmax + 1))
+    check(lib().oracle_rotation_matrix(mode, lmax, mmax, float(beta), float(phi), 1 if forward else 0, ptr(out)))
+    return from_cbuf(out, (d, d, lmax + 1))
+
+
+def fms_spectrum(positions, pots, lmaxph, wave_numbers, xphase, *, nsp=1, ispin=0, lfms=0, global_lmax=None,
+                 rdirec=1.0e6, sigsqr=None, sig2g=0.0, mode=F64, threads=1):
+    """Oracle scattering tables for every energy: array (E, C, C, npot) complex128.
+
+    wave_numbers: (E, nsp) complex; xphase: (E, nsp, 2L+1, npot) complex (FEFF xphase layout per energy).
+    """
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    pots = np.ascontiguousarray(pots, dtype=np.int32)
+    lmaxph = np.ascontiguousarray(lmaxph, dtype=np.int32)
+    npot = len(lmaxph)
+    L = int(lmaxph.max()) if global_lmax is None else int(global_lmax)
+    E = wave_numbers.shape[0]
+    k = cbuf(np.asarray(wave_numbers).reshape(E, nsp).T)  # (nsp, E) F-order == per-energy blocks of nsp
+    xp = np.ascontiguousarray(np.asarray(xphase, dtype=np.complex128).reshape(E, -1))
+    # per energy: (nsp, 2L+1, npot) column-major
+    xp_f = np.stack([np.asarray(xphase[e]).reshape(nsp, 2 * L + 1, npot).reshape(-1, order="F") for e in range(E)])
+    xpb = np.ascontiguousarray(xp_f).view(np.float64).copy()
+    del xp
+    Cc = nsp * (L + 1) ** 2
+    out = np.zeros(2 * E * Cc * Cc * npot)
+    status = np.zeros(E, dtype=np.int32)
+    sig = None if sigsqr is None else np.asfortranarray(sigsqr, dtype=np.float32)
+    rc = lib().oracle_fms_spectrum(mode, len(pots), ptr(positions), ptr(pots), nsp, ispin, lfms, npot - 1, L,
+                                   ptr(lmaxph), float(rdirec), ptr(sig), float(sig2g), E, ptr(k), ptr(xpb),
+                                   ptr(out), ptr(status), int(threads))
+    check(rc)
+    tabs = out.view(np.complex128).reshape(E, Cc * Cc * npot)
+    return np.stack([tabs[e].reshape((Cc, Cc, npot), order="F") for e in range(E)])
+
+
+def lu_factor_solve(A, B, mode=F64):
+    A = np.asarray(A, dtype=np.complex128)
+    B = np.asarray(B, dtype=np.complex128)
+    n, m = B.shape
+    a = cbuf(A)
+    b = cbuf(B)
+    piv = np.zeros(n, dtype=np.int64)
+    sp = np.zeros(1, dtype=np.int64)
+    rc = lib().oracle_lu_factor_solve(mode, n, ptr(a), m, ptr(b), ptr(piv), ptr(sp))
+    if rc != 0:
+        raise OracleError(rc)
+    return from_cbuf(a, (n, n)), from_cbuf(b, (n, m)), piv
+
+
+def threads_available() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)

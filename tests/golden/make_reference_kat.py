@@ -1,0 +1,265 @@
+"""Write tests/golden/reference_kat.json: the reference's known-answer vectors for the FMS path.
+
+The reference (refeff, Rust) cannot be built here, so its known-answer tests
+are the pin for the oracle.  Each entry below is transcribed from the
+reference's own #[test] functions and carries the file:line it came from.
+When the reference tree is present (``--reference DIR``), every number is
+checked to appear verbatim on its cited line, so the transcription can be
+audited; the JSON itself is what the tests read.
+
+Usage: python tests/golden/make_reference_kat.py [--reference /path/to/refeff]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import re
+from pathlib import Path
+
+FMS_TESTS = "crates/refeff-core/src/fms/tests"
+LINALG_TESTS = "crates/refeff-linalg/src/tests.rs"
+
+
+def c(re_, im_, src):
+    return {"value": [re_, im_], "src": src}
+
+
+def r(x, src):
+    return {"value": x, "src": src}
+
+
+KATS = {
+    "tolerance": {"complex32_abs": 2.0e-4, "f32_abs": 2.0e-6, "f64_abs": 1.0e-12,
+                  "src": f"{FMS_TESTS}/../tests.rs:228-247"},
+    # rehr_albers_polynomials(3, 4, 4, 1.25+0.4i); clm(il, im) zero-based.
+    "xclmz_lx3": {
+        "args": {"lx": 3, "lmaxp1": 4, "mmaxp1": 4, "rho": [1.25, 0.4]},
+        "entries": {
+            "0,0": c(1.0, 0.0, f"{FMS_TESTS}/mkgtr.rs:187"),
+            "1,0": c(1.2322206, 0.7256894, f"{FMS_TESTS}/mkgtr.rs:188"),
+            "3,0": c(-10.012509, 5.438266, f"{FMS_TESTS}/mkgtr.rs:189"),
+            "2,1": c(-2.1395304, 4.1993084, f"{FMS_TESTS}/mkgtr.rs:190"),
+            "3,2": c(-23.036537, -6.8588142, f"{FMS_TESTS}/mkgtr.rs:191"),
+            "4,3": c(8.928719, -161.62775, f"{FMS_TESTS}/mkgtr.rs:192"),
+        },
+        "sum": c(-58.983994, -154.61885, f"{FMS_TESTS}/mkgtr.rs:195"),
+        "nonzero": r(11, f"{FMS_TESTS}/mkgtr.rs:197"),
+    },
+    "xclmz_limited_m": {
+        "args": {"lx": 4, "lmaxp1": 3, "mmaxp1": 2, "rho": [-0.8, 1.1]},
+        "entries": {
+            "0,0": c(1.0, 0.0, f"{FMS_TESTS}/mkgtr.rs:207"),
+            "1,0": c(1.5945946, -0.4324324, f"{FMS_TESTS}/mkgtr.rs:208"),
+            "2,0": c(3.2834187, -2.840029, f"{FMS_TESTS}/mkgtr.rs:209"),
+            "1,1": c(0.5945946, -0.4324324, f"{FMS_TESTS}/mkgtr.rs:210"),
+            "2,1": c(2.7830534, -4.382761, f"{FMS_TESTS}/mkgtr.rs:211"),
+        },
+        "sum": c(9.255661, -8.087655, f"{FMS_TESTS}/mkgtr.rs:214"),
+        "nonzero": r(5, f"{FMS_TESTS}/mkgtr.rs:216"),
+    },
+    # fms_rotation_matrix(3, 3, 0.7, 1.1, Forward/Backward); entries keyed "m2,m1,l".
+    "rotxan": {
+        "args": {"lmax": 3, "mmax": 3, "beta": 0.7, "phi": 1.1},
+        "forward_sum": c(1.1595836, 0.2889818, f"{FMS_TESTS}/mkgtr.rs:257"),
+        "backward_sum": c(1.1595831, 0.28898174, f"{FMS_TESTS}/mkgtr.rs:261"),
+        "forward_nonzero": r(84, f"{FMS_TESTS}/mkgtr.rs:263"),
+        "backward_nonzero": r(84, f"{FMS_TESTS}/mkgtr.rs:264"),
+        "forward": {
+            "0,0,0": c(1.0, 0.0, f"{FMS_TESTS}/mkgtr.rs:266"),
+            "1,-1,1": c(-0.05333333, -0.10478719, f"{FMS_TESTS}/mkgtr.rs:269"),
+            "-1,1,1": c(-0.05333333, 0.10478719, f"{FMS_TESTS}/mkgtr.rs:273"),
+            "2,-1,2": c(-0.04457685, 0.061240695, f"{FMS_TESTS}/mkgtr.rs:277"),
+            "-2,1,3": c(0.11610273, 0.15950458, f"{FMS_TESTS}/mkgtr.rs:281"),
+            "3,3,3": c(0.67850935, 0.10838909, f"{FMS_TESTS}/mkgtr.rs:285"),
+        },
+        "backward": {
+            "2,-1,2": c(-0.034358274, -0.06750576, f"{FMS_TESTS}/mkgtr.rs:290"),
+            "-2,1,3": c(0.08948791, -0.17582226, f"{FMS_TESTS}/mkgtr.rs:294"),
+            "3,3,3": c(0.67850935, -0.10838909, f"{FMS_TESTS}/mkgtr.rs:298"),
+        },
+    },
+    # xgllm with xclm from rehr_albers_polynomials(3,4,4,1.25+0.4i).
+    "xgllm": {
+        "args": {"lx": 3, "rho": [1.25, 0.4]},
+        "cases": [
+            {"mu": 0, "l1": 2, "l2": 3, **c(415.5469, -1006.2809, f"{FMS_TESTS}/xgllm.rs:21")},
+            {"mu": 1, "l1": 2, "l2": 3, **c(-307.4973, 722.4695, f"{FMS_TESTS}/xgllm.rs:25")},
+            {"mu": 2, "l1": 2, "l2": 3, **c(115.08963, -235.94589, f"{FMS_TESTS}/xgllm.rs:29")},
+            {"mu": 2, "l1": 3, "l2": 1, **c(0.0, 0.0, f"{FMS_TESTS}/xgllm.rs:52")},
+        ],
+    },
+    # fms_pair_tables(2, 1.2+0.3i, atoms); polynomials indexed (m, l, atom2, atom1).
+    "pair_tables": {
+        "args": {"lmax": 2, "k": [1.2, 0.3],
+                 "positions": [[0.0, 0.0, 0.0], [1.0, 2.0, 2.0], [-1.0, 0.0, 0.5]]},
+        "rho": {
+            "0,1": c(3.6000001, 0.90000004, f"{FMS_TESTS}/pairs.rs:29"),
+            "0,2": c(1.3416408, 0.3354102, f"{FMS_TESTS}/pairs.rs:31"),
+            "1,2": c(3.8418748, 0.9604687, f"{FMS_TESTS}/pairs.rs:32"),
+        },
+        "poly_sum": c(8.870853, 26.772633, f"{FMS_TESTS}/pairs.rs:35"),
+        "poly_nonzero": r(36, f"{FMS_TESTS}/pairs.rs:37"),
+        "poly": {
+            "0,0,1,0": c(1.0, 0.0, f"{FMS_TESTS}/pairs.rs:38"),
+            "1,1,1,0": c(0.06535947, 0.2614379, f"{FMS_TESTS}/pairs.rs:41"),
+            "2,2,2,0": c(-1.384083, 0.7381776, f"{FMS_TESTS}/pairs.rs:45"),
+            "1,2,2,1": c(-0.15384735, 0.9149786, f"{FMS_TESTS}/pairs.rs:49"),
+            "1,1,0,0": c(0.0, 0.0, f"{FMS_TESTS}/pairs.rs:51"),
+        },
+    },
+    # fms_free_propagator_element: atoms (0,0,0),(1,2,2); k=1.2+0.3i; rotations (2,2,0.7,1.1);
+    # first (atom 1, l 2, m 1), second (atom 2, l 2, m -1); msd 0.05.
+    "free_propagator": {
+        "value": c(-0.13408086, 0.11388555, f"{FMS_TESTS}/pairs.rs:161"),
+        "matrix_0_1": c(-0.13408086, 0.11388555, f"{FMS_TESTS}/pairs.rs:365"),
+    },
+    "damping": {"src": f"{FMS_TESTS}/pairs.rs:167-183"},
+    "getang": {
+        "positions": [[0.0, 0.0, 0.0], [1.0, 2.0, 2.0], [0.0, 5.0e-8, 2.0e-7], [0.0, 2.0e-7, 0.0]],
+        "cases": [
+            {"i": 1, "j": 0, "theta": r(0.8410686, f"{FMS_TESTS}/cluster.rs:54"),
+             "phi": r(1.1071488, f"{FMS_TESTS}/cluster.rs:55")},
+            {"i": 3, "j": 2, "theta": r(2.4980915, f"{FMS_TESTS}/cluster.rs:58"),
+             "phi": r(1.5707964, f"{FMS_TESTS}/cluster.rs:59")},
+        ],
+    },
+    "athep": {
+        "positions": [[2.0, 0.0, 0.0], [0.0, 0.0, 0.0], [-1.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 2.0, 0.0]],
+        "potentials": [1, 0, 2, 3, 4],
+        "sorted_potentials": r([0, 2, 3, 1, 4], f"{FMS_TESTS}/cluster.rs:29-32"),
+        "keys": [r(2.0e-6, f"{FMS_TESTS}/cluster.rs:36"), r(1.000003, f"{FMS_TESTS}/cluster.rs:37"),
+                 r(1.000004, f"{FMS_TESTS}/cluster.rs:38"), r(4.000001, f"{FMS_TESTS}/cluster.rs:39"),
+                 r(4.000005, f"{FMS_TESTS}/cluster.rs:40")],
+    },
+    "sortat": {
+        "positions": [[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [2.0, 0.0, 0.0], [3.0, 0.0, 0.0], [4.0, 0.0, 0.0],
+                      [5.0, 0.0, 0.0]],
+        "potentials": [0, 2, 1, 3, 2, 1],
+        "representatives": r([0, 1, 2, 3], f"{FMS_TESTS}/cluster.rs:96"),
+        "sorted_potentials": r([0, 1, 2, 3, 2, 1], f"{FMS_TESTS}/cluster.rs:97-100"),
+        "position_1": r([2.0, 0.0, 0.0], f"{FMS_TESTS}/cluster.rs:101"),
+        "position_2": r([1.0, 0.0, 0.0], f"{FMS_TESTS}/cluster.rs:102"),
+        "position_3": r([3.0, 0.0, 0.0], f"{FMS_TESTS}/cluster.rs:103"),
+    },
+    "yprep": {
+        "positions": [[2.0, 0.0, 0.0], [1.0, 1.0, 0.0], [1.0, 3.0, 0.0], [4.0, 1.0, 0.0], [1.0, 1.0, 1.0]],
+        "potentials": [1, 0, 2, 1, 2], "radius": 2.1, "capacity": 3,
+        "central_atom": r(1, f"{FMS_TESTS}/cluster.rs:126"),
+        "untruncated": r(4, f"{FMS_TESTS}/cluster.rs:127"),
+        "potentials_out": r([0, 2, 1], f"{FMS_TESTS}/cluster.rs:129-136"),
+        "positions_out": r([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0], [1.0, -1.0, 0.0]], f"{FMS_TESTS}/cluster.rs:137-139"),
+    },
+    # reference_phase_shifts(): shape (2 spins, 5 signed l, 2 potentials).
+    "t_matrix": {
+        "phases": {"0,4,1": [0.2, 0.05], "0,0,1": [-0.1, 0.03], "1,4,1": [0.15, -0.02], "1,0,1": [0.07, 0.04]},
+        "phases_src": f"{FMS_TESTS}/../tests.rs:62-69",
+        "non_spin": c(0.17618014, 0.08329478, f"{FMS_TESTS}/t_matrix.rs:46"),
+        "spin_orbit_diagonal": c(0.06828813, 0.06537849, f"{FMS_TESTS}/t_matrix.rs:49"),
+        "spin_mixing": c(-0.08796438, -0.0011440981, f"{FMS_TESTS}/t_matrix.rs:51"),
+    },
+    # reference_gglu_inputs(8) with construct_state_kets(2, [0], [1], 1).
+    "gglu": {
+        "inputs_src": f"{FMS_TESTS}/../tests.rs:71-90",
+        "system_sum": c(8.10728, -0.54295987, f"{FMS_TESTS}/solvers.rs:319"),
+        "scattering_sum": c(-2.9443204, 4.7994013, f"{FMS_TESTS}/solvers.rs:323"),
+        "scattering": {
+            "0,0,0": c(-0.0077970205, -0.0032442866, f"{FMS_TESTS}/solvers.rs:327"),
+            "1,3,0": c(-0.06596742, 0.04409315, f"{FMS_TESTS}/solvers.rs:331"),
+            "6,7,0": c(-0.0962859, 0.14052007, f"{FMS_TESTS}/solvers.rs:335"),
+        },
+    },
+    "iterative_system": {
+        "sum": c(7.9095793, -0.5169, f"{FMS_TESTS}/solvers.rs:20"),
+        "entries": {
+            "0,0": c(1.0, 0.0, f"{FMS_TESTS}/solvers.rs:22"),
+            "1,3": c(0.0014, -0.0031999997, f"{FMS_TESTS}/solvers.rs:23"),
+            "4,5": c(0.0012300003, -0.011239999, f"{FMS_TESTS}/solvers.rs:26"),
+            "6,7": c(0.0017899997, -0.0209, f"{FMS_TESTS}/solvers.rs:28"),
+        },
+        "cutoff_toler2": 0.09,
+        "cutoff_sum": c(7.9228334, -0.47112507, f"{FMS_TESTS}/solvers.rs:40"),
+        "cutoff_entries": {
+            "1,3": c(0.0, 0.0, f"{FMS_TESTS}/solvers.rs:42"),
+            "4,5": c(0.0012300003, -0.011239999, f"{FMS_TESTS}/solvers.rs:45"),
+        },
+    },
+    # complex32 cgetrf/cgetrs known answer (3x3, two right-hand sides).
+    "cgetrf": {
+        "matrix": [[[0.0, 0.0], [2.0, -1.0], [-1.0, 0.5]],
+                   [[3.0, 2.0], [-1.0, 0.0], [4.0, -1.0]],
+                   [[1.0, -3.0], [0.5, 2.0], [2.0, 0.0]]],
+        "rhs": [[[1.0, 0.5], [-2.0, 1.0]], [[0.0, -1.0], [3.0, 0.0]], [[2.0, 2.0], [-1.0, -0.5]]],
+        "pivots_one_based": r([2, 2, 3], f"{LINALG_TESTS}:170"),
+        "factors": r([[[3.0, 2.0], [-1.0, 0.0], [4.0, -1.0]],
+                      [[0.0, 0.0], [2.0, -1.0], [-1.0, 0.5]],
+                      [[-0.23076928, -0.8461538], [-0.12307697, 0.5153847], [3.9038463, 3.730769]]],
+                     f"{LINALG_TESTS}:172-190"),
+        "solution": r([[[-0.23347072, 0.43198672], [-0.13470735, -0.2801319]],
+                       [[0.60016483, 0.28161582], [-0.7983512, 0.2161583]],
+                       [[0.6003297, -0.2367683], [0.4032976, 0.43231657]]],
+                      f"{LINALG_TESTS}:193-208"),
+    },
+    "driver_setup": {
+        "potentials": [1, 0, 2], "raw_lmax": [-1, 5, 1], "global_lmax": 2, "max_potential": 2,
+        "potential_lmax": r([2, 2, 1], f"{FMS_TESTS}/driver.rs:30"),
+        "range": r([1, 1], f"{FMS_TESTS}/driver.rs:31-32"),
+        "representative_offsets": r([9, 0, 18], f"{FMS_TESTS}/driver.rs:33-36"),
+        "state_count": r(22, f"{FMS_TESTS}/driver.rs:37"),
+    },
+}
+
+
+def _numbers_in(obj):
+    if isinstance(obj, dict):
+        if "value" in obj and "src" in obj:
+            yield obj["value"], obj["src"]
+        for v in obj.values():
+            if isinstance(v, (dict, list)):
+                yield from _numbers_in(v)
+    elif isinstance(obj, list):
+        for v in obj:
+            yield from _numbers_in(v)
+
+
+def _flatten(v):
+    if isinstance(v, list):
+        for x in v:
+            yield from _flatten(x)
+    else:
+        yield v
+
+
+def audit(reference: Path) -> int:
+    """Check that each transcribed number appears in the cited lines (underscores removed)."""
+    bad = 0
+    for value, src in _numbers_in(KATS):
+        path, _, span = src.rpartition(":")
+        lo, _, hi = span.partition("-")
+        lines = (reference / path).resolve().read_text().splitlines()
+        text = " ".join(lines[int(lo) - 1:int(hi or lo)]).replace("_", "")
+        tokens = [float(t) for t in re.findall(r"-?\d+\.?\d*(?:e-?\d+)?", text)]
+        for x in _flatten(value):
+            if isinstance(x, bool) or x == 0:
+                continue  # zeros are implied by Complex32::new(0.0, 0.0) or 0.0 literals
+            if not any(abs(t - x) <= 1e-9 * max(1.0, abs(x)) or abs(abs(t) - abs(x)) <= 1e-9 * max(1.0, abs(x))
+                       for t in tokens):
+                print(f"not found: {x} at {src}")
+                bad += 1
+    return bad
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", type=Path, default=None)
+    args = ap.parse_args()
+    out = Path(__file__).with_name("reference_kat.json")
+    out.write_text(json.dumps(KATS, indent=1) + "\n")
+    print(f"wrote {out}")
+    if args.reference is not None:
+        bad = audit(args.reference)
+        print("audit:", "ok" if bad == 0 else f"{bad} number(s) not found")
+        raise SystemExit(1 if bad else 0)
+
+
+if __name__ == "__main__":
+    main()
