@@ -1,0 +1,213 @@
+/*
+ * refeff_fms.h -- C ABI of the GB300 (sm_103a) full-multiple-scattering path.
+ *
+ * This library replaces the real-space FMS hot path of refeff (a Rust port of
+ * FEFF10): the per-energy G0 / T assembly and the dense complex solve that
+ * crates/refeff-engine/src/fms.rs hands to refeff-core and refeff-linalg.
+ * A Rust caller binds these entry points through a thin FFI crate; the
+ * signatures use plain C types only (no CUDA or torch types).
+ *
+ * Conventions
+ *  - Complex numbers are two consecutive doubles (re, im): refeff_complex128.
+ *  - Arrays are column-major ("Fortran order"), exactly like the reference's
+ *    ndarray `.f()` tables.  Indices are zero-based.
+ *  - Every entry point returns a refeff_fms_status; 0 is success.  Nothing
+ *    aborts or throws across the ABI.  refeff_fms_last_error() returns a
+ *    human-readable message for the last failure on a context.
+ *  - The caller owns every host buffer; the library owns device memory and
+ *    streams inside the context and plan handles.  Handles are not
+ *    thread-safe: use one context per host thread (the reference configures
+ *    faer's parallelism process-wide, docs/EMBEDDING_ROADMAP.md:88-92).
+ *  - Lengths are Angstrom, wave numbers Angstrom^-1, sigma^2 Angstrom^2
+ *    (crates/refeff-core/src/fms/internals/geometry.rs:19-24).
+ */
+#ifndef REFEFF_FMS_H
+#define REFEFF_FMS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define REFEFF_FMS_ABI_VERSION 1
+
+typedef struct {
+  double re;
+  double im;
+} refeff_complex128;
+
+/* Status codes.  They map onto the reference error variants the FMS path can
+ * raise: crates/refeff-core/src/fms/types.rs:832 (FmsError) and
+ * crates/refeff-linalg/src/error.rs (LinalgError::SingularMatrix). */
+typedef enum {
+  REFEFF_FMS_OK = 0,
+  REFEFF_FMS_ERR_INVALID_ARGUMENT = 1,       /* null pointer, bad count, bad enum */
+  REFEFF_FMS_ERR_EMPTY_CLUSTER = 2,          /* FmsError::EmptyCluster */
+  REFEFF_FMS_ERR_POTENTIAL_OUT_OF_RANGE = 3, /* FmsError::PotentialOutOfRange */
+  REFEFF_FMS_ERR_MISSING_REPRESENTATIVE = 4, /* FmsError::MissingRepresentativePotential */
+  REFEFF_FMS_ERR_INVALID_ANGULAR_LIMIT = 5,  /* FmsError::InvalidAngularLimit */
+  REFEFF_FMS_ERR_NONFINITE_INPUT = 6,        /* NonFiniteWaveNumber / NonFinitePhaseShift / NonFiniteRho */
+  REFEFF_FMS_ERR_NONFINITE_COORDINATE = 7,   /* FmsError::NonFiniteCoordinate */
+  REFEFF_FMS_ERR_ZERO_RHO = 8,               /* FmsError::ZeroRho */
+  REFEFF_FMS_ERR_SINGULAR_MATRIX = 9,        /* LinalgError::SingularMatrix { pivot } */
+  REFEFF_FMS_ERR_NOT_CONVERGED = 10,         /* refinement did not reach its tolerance */
+  REFEFF_FMS_ERR_DUPLICATE_ABSORBER = 11,    /* FmsError::DuplicateAbsorber */
+  REFEFF_FMS_ERR_MISSING_CENTRAL_ATOM = 12,  /* FmsError::MissingCentralAtom */
+  REFEFF_FMS_ERR_UNSUPPORTED = 13,           /* valid input outside this library's scope */
+  REFEFF_FMS_ERR_CUDA = 14,                  /* CUDA runtime error (message in last_error) */
+  REFEFF_FMS_ERR_OUT_OF_MEMORY = 15,
+  REFEFF_FMS_ERR_INVALID_TOLERANCE = 16,     /* FmsError::InvalidTolerance */
+  REFEFF_FMS_ERR_INVALID_CLUSTER_RADIUS = 17 /* FmsError::InvalidClusterRadius */
+} refeff_fms_status;
+
+/* Solver forms for the dense system (I - G0 T) X = G0[:, absorber]. */
+typedef enum {
+  /* Plain FP64 blocked LU.  The drop-in for minv = 0 (FEFF gglu,
+   * crates/refeff-core/src/fms/solvers.rs:366-484). */
+  REFEFF_FMS_FORM_FP64_LU = 0,
+  /* Complex FP32 LU, then FP64 iterative refinement of the full solution
+   * against the FP64 system until the residual meets the plan tolerance. */
+  REFEFF_FMS_FORM_FP32_REFINED = 1
+} refeff_fms_form;
+
+typedef struct refeff_fms_context refeff_fms_context;
+typedef struct refeff_fms_plan refeff_fms_plan;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Create a context on CUDA device `device` (one GPU per context). */
+int refeff_fms_context_create(int device, refeff_fms_context** out);
+void refeff_fms_context_destroy(refeff_fms_context* ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char* refeff_fms_last_error(const refeff_fms_context* ctx);
+int refeff_fms_abi_version(void);
+/* Total GPU kernel launches issued by this library in the process so far
+ * (launches replayed inside CUDA graphs included). */
+unsigned long long refeff_fms_kernel_launches(void);
+
+/* ---- cluster preparation (host) -------------------------------------- */
+
+/* FEFF yprep + sortat for one absorber: replaces fms_yprep_cluster
+ * (crates/refeff-core/src/fms/cluster.rs:10-84) followed by
+ * sort_representative_atoms (cluster.rs:115-195), as called from
+ * fms_atoms_from_geom (crates/refeff-engine/src/fms.rs:4286-4322) and
+ * build_fms_source_outputs (fms.rs:3578-3580).
+ * positions_xyz: n_rows x 3 floats (row-major x,y,z); potentials: n_rows ints.
+ * out_*: capacity n_rows.  The absorber ends up first, at the origin. */
+int refeff_fms_yprep_cluster(int central_potential, int max_potential, int n_rows, const int* potentials,
+                             const float* positions_xyz, float cluster_radius, int cluster_capacity,
+                             float* out_positions_xyz, int* out_potentials, int* out_count);
+
+/* ---- plan ------------------------------------------------------------- */
+
+/* Energy-independent inputs; replaces FmsRealSpacePlanInput
+ * (crates/refeff-core/src/fms/types.rs:166, driver.rs:105-140). */
+typedef struct {
+  int n_atoms;                      /* prepared cluster (absorber first) */
+  const float* positions_xyz;       /* n_atoms x 3, Angstrom */
+  const int* potentials;            /* n_atoms */
+  int spin_channels;                /* nsp: 1 or 2 */
+  int spin_selector;                /* global.inp ispin */
+  int lfms;                         /* 0: absorber potential only; else all potentials */
+  int minv;                         /* FEFF minv (0 = LU); others are solved with LU too */
+  int max_potential;                /* nph */
+  int global_lmax;                  /* max over lmaxph */
+  const int* raw_potential_lmax;    /* lmaxph(0..nph), clamped like clamp_fms_lipotx */
+  float direct_cutoff;              /* rdirec, Angstrom */
+  const float* mean_square_displacements; /* N x N column-major [atom2 + N*atom1], or NULL */
+  float sig2g;                      /* used for every i != j pair when the table is NULL */
+  float convergence_tolerance;      /* toler1 (iterative forms) */
+  float zero_tolerance;             /* toler2 */
+} refeff_fms_plan_input;
+
+int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* input,
+                                      refeff_fms_plan** out);
+void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan);
+
+/* Sizes of a plan: state count n, channel count C = nsp (L+1)^2 of the
+ * scattering table, absorber block width m, potential count. */
+int refeff_fms_plan_query(const refeff_fms_plan* plan, int* n_states, int* channel_count, int* absorber_block,
+                          int* n_potentials);
+
+/* Tuning: energies solved per device batch (0 = automatic from free memory)
+ * and the refinement limits of REFEFF_FMS_FORM_FP32_REFINED. */
+int refeff_fms_plan_set_batch(refeff_fms_plan* plan, int max_batch);
+int refeff_fms_plan_set_refinement(refeff_fms_plan* plan, int max_iterations, double tolerance);
+
+/* Per-phase device time (CUDA events on the solve stream) of the spectrum
+ * calls made while profiling is on, accumulated in milliseconds:
+ *   0 system build (G0, T, I - G0 T)   1 LU elimination
+ *   2 triangular sweeps                3 FP64 residuals
+ *   4 absorber extraction / small solves
+ * Profiling runs batches without graph replay; enabling it resets the sums. */
+#define REFEFF_FMS_PHASES 5
+int refeff_fms_plan_set_profiling(refeff_fms_plan* plan, int enable);
+int refeff_fms_plan_phase_times(const refeff_fms_plan* plan, double* ms_out, int n_phases);
+
+/* ---- spectrum --------------------------------------------------------- */
+
+/* Per-energy inputs; replaces FmsRealSpaceEnergyPoint (types.rs).
+ * wave_numbers: n_energies x nsp (energy-major).
+ * phase_shifts: n_energies blocks, each the FEFF xphase(spin, l + L, pot)
+ *   table of shape (nsp, 2L+1, npot) in column-major order
+ *   (built by fms_phase_shifts_for_energy, crates/refeff-engine/src/fms.rs:5002-5054). */
+typedef struct {
+  int n_energies;
+  const refeff_complex128* wave_numbers;
+  const refeff_complex128* phase_shifts;
+} refeff_fms_energy_points;
+
+typedef struct {
+  double seconds;               /* wall time of the call */
+  int refinement_iterations;    /* max over energies (FP32_REFINED) */
+  double residual_max;          /* max relative residual after refinement */
+  int energies_failed;          /* energies with a non-zero status */
+} refeff_fms_report;
+
+/* fms_real_space_spectrum (crates/refeff-core/src/fms/driver.rs:231-239):
+ * solves every energy point and writes the scattering table of each, shape
+ * (C, C, npot) column-major, C = nsp (L+1)^2 (FmsLuResult::scattering,
+ * solvers.rs:415-471): entry (row, col, pot) = X[offset(pot) + row, col] with
+ * X = (I - G0 T)^-1 G0[:, offset(pot) : offset(pot) + ipart].
+ * status_out (optional): one refeff_fms_status per energy (the reference
+ * returns Vec<Result<..>>).  Host buffers; the call copies inputs to the GPU
+ * and results back. */
+int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                   refeff_fms_form form, refeff_complex128* scattering_out, int32_t* status_out,
+                                   refeff_fms_report* report);
+
+/* Same solve for inputs already resident in device memory (same layouts as
+ * above, device pointers); writes only the absorber block per energy:
+ * d_gg_out = n_energies x (m x m) complex128.  `stream` is a cudaStream_t
+ * (NULL = the context stream).  Asynchronous: synchronise the stream before
+ * reading results. */
+int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies, const void* d_wave_numbers,
+                                          const void* d_phase_shifts, refeff_fms_form form, void* d_gg_out,
+                                          int32_t* d_status, void* stream);
+
+/* FEFF gg section for one energy (fms_gg_section_values,
+ * crates/refeff-engine/src/fms.rs:2004-2047): the absorber block widened to
+ * the output spin capacity nspu (>= nsp) of .dimensions.dat; out is
+ * (nspu (lmax0+1)^2)^2 complex, column-major, zero-padded. */
+int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_complex128* scattering, int nspu,
+                          refeff_complex128* out);
+
+/* ---- dense solve (refeff-linalg boundary) ----------------------------- */
+
+/* Batched dense complex solve A X = B, replacing complex32_faer_lu_factor +
+ * complex32_faer_lu_solve (crates/refeff-linalg/src/lu.rs:385-397, 474-490)
+ * for `batch` independent systems.  A: batch x (n x n), B/X: batch x (n x m),
+ * column-major host buffers; X may alias B.  status_out (optional, batch
+ * entries) reports REFEFF_FMS_ERR_SINGULAR_MATRIX with pivot_out (1-based
+ * first zero pivot, optional). */
+int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, int m, int batch, const refeff_complex128* A,
+                                    const refeff_complex128* B, refeff_complex128* X, refeff_fms_form form,
+                                    int32_t* status_out, int32_t* pivot_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REFEFF_FMS_H */

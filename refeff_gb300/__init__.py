@@ -1,0 +1,26 @@
+"""GB300-native (sm_103a) implementation of refeff's real-space FMS hot path.
+
+The compute lives in librefeff_fms.so (CUDA kernels + C ABI, include/refeff_fms.h);
+this package is the Python mirror of the reference interface used by tests and
+benchmarks.  There is no CPU fallback.
+"""
+from .fms import (  # noqa: F401
+    FORM_FP32_REFINED,
+    FORM_FP64_LU,
+    Context,
+    FmsError,
+    FmsRealSpacePlan,
+    complex_lu_solve_batched,
+    fms_real_space_plan,
+    fms_real_space_spectrum,
+    fms_real_space_spectrum_device,
+    fms_yprep_cluster,
+    gg_section,
+    load,
+)
+
+__all__ = [
+    "FORM_FP32_REFINED", "FORM_FP64_LU", "Context", "FmsError", "FmsRealSpacePlan", "complex_lu_solve_batched",
+    "fms_real_space_plan", "fms_real_space_spectrum", "fms_real_space_spectrum_device", "fms_yprep_cluster",
+    "gg_section", "load",
+]

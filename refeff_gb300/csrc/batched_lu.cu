@@ -1,0 +1,764 @@
+// Batched blocked complex LU (partial pivoting, pivot norm |re|+|im| as in
+// crates/refeff-linalg/src/lu.rs:337-345, 612-614) on augmented systems
+// [A | B], batched over energy points, and the triangular sweeps that reuse
+// the factors (crates/refeff-linalg/src/lu.rs:400-529 solve semantics).
+//
+// One elimination step k (panel width NB):
+//   panel_kernel      the (n-k) x NB panel lives in the distributed shared
+//                     memory of a thread-block cluster (rows split across the
+//                     CTAs); one cluster barrier per column: local arg-max,
+//                     cluster arg-max over DSMEM, pivot row read over DSMEM,
+//                     rank-1 update of the CTA's own rows.  Rows are not moved
+//                     while the panel is factored; the permutation is applied
+//                     when the panel is written back, and its row moves are
+//                     stored per panel.
+//   rhs_lower_kernel  applies the panel's row moves to the trailing columns and
+//                     solves U12 = L11^-1 A12 (one warp per column).
+//   gemm_update       A22 -= L21 U12 on the trailing block (B included).
+// Columns left of the panel are never permuted.  A later forward sweep
+// applies each panel's moves to the new right-hand side just before that
+// panel's L columns, which is the same permutation order the elimination saw.
+#include <cooperative_groups.h>
+#include <climits>
+#include "cplx.cuh"
+#include "batched_lu.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace rfx {
+
+constexpr int kPanelThreads = 256;
+
+template <typename T, int NB>
+static size_t panel_smem_bytes(int rpc_max, int n) {
+  size_t b = size_t(NB) * rpc_max * sizeof(cplx<T>);  // panel
+  b += NB * sizeof(cplx<T>);                          // pivot row copy
+  b += 2 * 16;                                        // arg-max slots
+  b += size_t(rpc_max) * sizeof(int);                 // done flags
+  b += 2 * size_t(n) * sizeof(int);                   // row2pos / pos2row (rank 0)
+  b += 64;                                            // scratch
+  return (b + 15) / 16 * 16;
+}
+
+template <typename T>
+struct alignas(16) ArgSlot {
+  T val;
+  int row;
+};
+
+template <typename T>
+__device__ __forceinline__ void argmax_merge(T& v, int& r, T ov, int orow) {
+  if (ov > v || (ov == v && orow < r)) { v = ov; r = orow; }
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, int k, cplx<T>* __restrict__ M,
+                                                              LuWork w, int rpc_max) {
+  using C = cplx<T>;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CL = int(cluster.num_blocks());
+  const int rank = int(cluster.block_rank());
+  const int b = blockIdx.y;
+  const int n = lay.n;
+  const int R = n - k;
+  const int kb = min(NB, R);
+  const int panel = k / NB;
+  const int rpc = (R + CL - 1) / CL;
+  const int row_lo = rank * rpc;
+  const int nloc = max(0, min(R, row_lo + rpc) - row_lo);
+  const int tid = threadIdx.x, nthr = blockDim.x, lane = tid & 31, wid = tid >> 5;
+
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* pan = reinterpret_cast<C*>(smraw);
+  C* urow = pan + size_t(NB) * rpc_max;
+  ArgSlot<T>* slot = reinterpret_cast<ArgSlot<T>*>(urow + NB);
+  int* done = reinterpret_cast<int*>(slot + 2);
+  int* row2pos = done + rpc_max;
+  int* pos2row = row2pos + n;
+  int* scratch = pos2row + n;  // [0] winner row, [2] move count
+  __shared__ T red_v[kPanelThreads / 32];
+  __shared__ int red_r[kPanelThreads / 32];
+  __shared__ T win_v;
+
+  C* Mb = M + size_t(b) * lay.stride;
+  for (int idx = tid; idx < nloc * kb; idx += nthr) {
+    const int r = idx % nloc, c = idx / nloc;
+    pan[size_t(c) * rpc_max + r] = Mb[size_t(k + row_lo + r) + size_t(lay.lda) * (k + c)];
+  }
+  for (int r = tid; r < nloc; r += nthr) done[r] = 0;
+  if (rank == 0) {
+    for (int q = tid; q < R; q += nthr) { row2pos[q] = q; pos2row[q] = q; }
+    if (tid == 0) scratch[2] = 0;
+  }
+  __syncthreads();
+
+  for (int j = 0; j < kb; ++j) {
+    // local arg-max of column j over rows not yet used as pivots
+    T best = T(-1);
+    int brow = INT_MAX;
+    for (int r = tid; r < nloc; r += nthr) {
+      if (done[r]) continue;
+      T v = cabs1(pan[size_t(j) * rpc_max + r]);
+      if (!(v >= T(0))) v = T(0);  // a NaN entry competes as zero, so a valid row is always chosen
+      argmax_merge(best, brow, v, row_lo + r);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_down_sync(0xffffffffu, best, off);
+      const int orow = __shfl_down_sync(0xffffffffu, brow, off);
+      argmax_merge(best, brow, ov, orow);
+    }
+    if (lane == 0) { red_v[wid] = best; red_r[wid] = brow; }
+    __syncthreads();
+    if (tid == 0) {
+      T v = red_v[0];
+      int r = red_r[0];
+      for (int q = 1; q < nthr / 32; ++q) argmax_merge(v, r, red_v[q], red_r[q]);
+      slot[j & 1].val = v;
+      slot[j & 1].row = r;
+    }
+    cluster.sync();
+    // cluster arg-max over DSMEM
+    if (wid == 0) {
+      T v = T(-1);
+      int r = INT_MAX;
+      if (lane < CL) {
+        const ArgSlot<T>* rs = cluster.map_shared_rank(slot, lane);
+        v = rs[j & 1].val;
+        r = rs[j & 1].row;
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const T ov = __shfl_down_sync(0xffffffffu, v, off);
+        const int orow = __shfl_down_sync(0xffffffffu, r, off);
+        argmax_merge(v, r, ov, orow);
+      }
+      if (lane == 0) { scratch[0] = r; win_v = v; }
+    }
+    __syncthreads();
+    const int wrow = scratch[0];
+    const int owner = wrow / rpc, lr = wrow % rpc;
+    const C* opan = cluster.map_shared_rank(pan, owner);
+    for (int c = j + tid; c < kb; c += nthr) urow[c] = opan[size_t(c) * rpc_max + lr];
+    if (rank == owner && tid == 0) done[lr] = 1;
+    if (rank == 0 && tid == 0) {
+      const int q = row2pos[wrow];
+      const int pj = pos2row[j];
+      pos2row[j] = wrow;
+      pos2row[q] = pj;
+      row2pos[wrow] = j;
+      row2pos[pj] = q;
+      w.ipiv[size_t(b) * n + k + j] = k + q;
+      if (!(win_v > T(0))) {
+        atomicMax(w.status + b, int(kDevSingular));
+        atomicCAS(w.info + b, 0, k + j + 1);
+      }
+    }
+    __syncthreads();
+    // multipliers and rank-1 update of own rows
+    const C pv = urow[j];
+    const bool zero_pivot = !(cabs1(pv) > T(0));
+    for (int r = tid; r < nloc; r += nthr) {
+      if (done[r]) continue;
+      C l = pan[size_t(j) * rpc_max + r];
+      l = zero_pivot ? mk<T>(T(0), T(0)) : cdiv(l, pv);
+      pan[size_t(j) * rpc_max + r] = l;
+      for (int c = j + 1; c < kb; ++c) cfms(pan[size_t(c) * rpc_max + r], l, urow[c]);
+    }
+  }
+  cluster.sync();
+  // write back in pivoted order; rank 0 publishes the row moves of this panel
+  const int* r2p0 = cluster.map_shared_rank(row2pos, 0);
+  for (int idx = tid; idx < nloc * kb; idx += nthr) {
+    const int r = idx % nloc, c = idx / nloc;
+    const int dst = k + r2p0[row_lo + r];
+    Mb[size_t(dst) + size_t(lay.lda) * (k + c)] = pan[size_t(c) * rpc_max + r];
+  }
+  if (rank == 0) {
+    int2* pm = w.perm + (size_t(b) * w.npanels + panel) * (2 * NB);
+    for (int q = tid; q < R; q += nthr) {
+      if (pos2row[q] != q) {
+        const int si = atomicAdd(&scratch[2], 1);
+        if (si < 2 * NB) pm[si] = make_int2(k + q, k + pos2row[q]);
+      }
+    }
+    __syncthreads();
+    if (tid == 0) w.nperm[size_t(b) * w.npanels + panel] = min(scratch[2], 2 * NB);
+  }
+  cluster.sync();
+}
+
+// One warp per column in [c_begin, c_end): apply the panel's row moves, then
+// solve the panel rows with the unit lower L11.
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, int c_begin, int c_end,
+                                                        cplx<T>* __restrict__ M, LuWork w, const int* skip) {
+  using C = cplx<T>;
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  __shared__ C L11[NB][NB + 1];
+  const int n = lay.n;
+  const int kb = min(NB, n - k);
+  const int panel = k / NB;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  C* Mb = M + size_t(b) * lay.stride;
+  for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+    const int r = idx % kb, c = idx / kb;
+    L11[r][c] = Mb[size_t(k + r) + size_t(lay.lda) * (k + c)];
+  }
+  __syncthreads();
+  const int col = c_begin + blockIdx.x * (blockDim.x / 32) + wid;
+  if (col >= c_end) return;
+  C* colp = Mb + size_t(lay.lda) * col;
+  const size_t pidx = size_t(b) * w.npanels + panel;
+  const int np = w.nperm[pidx];
+  const int2* pm = w.perm + pidx * (2 * NB);
+  constexpr int kMoves = (2 * NB + 31) / 32;
+  C v[kMoves];
+  int dst[kMoves];
+#pragma unroll
+  for (int t = 0; t < kMoves; ++t) {
+    const int i = lane + 32 * t;
+    dst[t] = -1;
+    if (i < np) { const int2 mv = pm[i]; dst[t] = mv.x; v[t] = colp[mv.y]; }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < kMoves; ++t)
+    if (dst[t] >= 0) colp[dst[t]] = v[t];
+  __syncwarp();
+  constexpr int kRows = (NB + 31) / 32;
+  C x[kRows];
+#pragma unroll
+  for (int t = 0; t < kRows; ++t) {
+    const int i = lane + 32 * t;
+    x[t] = i < kb ? colp[k + i] : mk<T>(T(0), T(0));
+  }
+  for (int p = 0; p < kb; ++p) {
+    const int owner_t = p >> 5, owner_l = p & 31;
+    C xp = mk<T>(T(0), T(0));
+#pragma unroll
+    for (int t = 0; t < kRows; ++t) {
+      const T re = __shfl_sync(0xffffffffu, x[t].x, owner_l);
+      const T im = __shfl_sync(0xffffffffu, x[t].y, owner_l);
+      if (t == owner_t) { xp.x = re; xp.y = im; }
+    }
+#pragma unroll
+    for (int t = 0; t < kRows; ++t) {
+      const int i = lane + 32 * t;
+      if (i > p && i < kb) cfms(x[t], L11[i][p], xp);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kRows; ++t) {
+    const int i = lane + 32 * t;
+    if (i < kb) colp[k + i] = x[t];
+  }
+}
+
+// One warp per RHS column: X[k:k+kb] = U11^-1 Y[k:k+kb] (bottom-up).
+template <typename T, int NB>
+__global__ void __launch_bounds__(256) rhs_upper_kernel(BatchLayout lay, int k, cplx<T>* __restrict__ M,
+                                                        const int* skip) {
+  using C = cplx<T>;
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  __shared__ C U11[NB][NB + 1];
+  const int n = lay.n;
+  const int kb = min(NB, n - k);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  C* Mb = M + size_t(b) * lay.stride;
+  for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+    const int r = idx % kb, c = idx / kb;
+    U11[r][c] = Mb[size_t(k + r) + size_t(lay.lda) * (k + c)];
+  }
+  __syncthreads();
+  const int col = n + blockIdx.x * (blockDim.x / 32) + wid;
+  if (col >= n + lay.m) return;
+  C* colp = Mb + size_t(lay.lda) * col;
+  constexpr int kRows = (NB + 31) / 32;
+  C x[kRows];
+#pragma unroll
+  for (int t = 0; t < kRows; ++t) {
+    const int i = lane + 32 * t;
+    x[t] = i < kb ? colp[k + i] : mk<T>(T(0), T(0));
+  }
+  for (int p = kb - 1; p >= 0; --p) {
+    const int owner_t = p >> 5, owner_l = p & 31;
+#pragma unroll
+    for (int t = 0; t < kRows; ++t)
+      if (t == owner_t && lane == owner_l) {
+        const C d = U11[p][p];
+        x[t] = (d.x == T(0) && d.y == T(0)) ? mk<T>(T(0), T(0)) : cdiv(x[t], d);
+      }
+    C xp = mk<T>(T(0), T(0));
+#pragma unroll
+    for (int t = 0; t < kRows; ++t) {
+      const T re = __shfl_sync(0xffffffffu, x[t].x, owner_l);
+      const T im = __shfl_sync(0xffffffffu, x[t].y, owner_l);
+      if (t == owner_t) { xp.x = re; xp.y = im; }
+    }
+#pragma unroll
+    for (int t = 0; t < kRows; ++t) {
+      const int i = lane + 32 * t;
+      if (i < p) cfms(x[t], U11[i][p], xp);
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kRows; ++t) {
+    const int i = lane + 32 * t;
+    if (i < kb) colp[k + i] = x[t];
+  }
+}
+
+// C[r_begin:r_end, c_begin:c_end] -= M[rows, ka:ka+kb] * M[ka:ka+kb, cols]
+// Thread tile TM x TN complex, CTA tile (16*TM) x (16*TN), 256 threads.
+template <typename T, int TM, int TN, int KMAX>
+__global__ void __launch_bounds__(256) gemm_update_kernel(BatchLayout lay, int r_begin, int r_end, int c_begin,
+                                                          int c_end, int ka, int kb, cplx<T>* __restrict__ M,
+                                                          const int* skip) {
+  using C = cplx<T>;
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  const int b = blockIdx.z;
+  if (skip && skip[b]) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* As = reinterpret_cast<C*>(smraw);   // [KMAX][BM]
+  C* Bs = As + KMAX * BM;                // [KMAX][BN]
+  const int r0 = r_begin + blockIdx.x * BM;
+  const int c0 = c_begin + blockIdx.y * BN;
+  if (r0 >= r_end || c0 >= c_end) return;
+  C* Mb = M + size_t(b) * lay.stride;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < kb * BM; idx += 256) {
+    const int r = idx % BM, kk = idx / BM;
+    As[kk * BM + r] = (r0 + r < r_end) ? Mb[size_t(r0 + r) + size_t(lay.lda) * (ka + kk)] : mk<T>(T(0), T(0));
+  }
+  for (int idx = tid; idx < kb * BN; idx += 256) {
+    const int kk = idx % kb, c = idx / kb;
+    Bs[kk * BN + c] = (c0 + c < c_end) ? Mb[size_t(ka + kk) + size_t(lay.lda) * (c0 + c)] : mk<T>(T(0), T(0));
+  }
+  __syncthreads();
+  const int tx = tid & 15, ty = tid >> 4;
+  C acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int jj = 0; jj < TN; ++jj) acc[i][jj] = mk<T>(T(0), T(0));
+  for (int kk = 0; kk < kb; ++kk) {
+    C a[TM], bb[TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) a[i] = As[kk * BM + ty + 16 * i];
+#pragma unroll
+    for (int jj = 0; jj < TN; ++jj) bb[jj] = Bs[kk * BN + tx + 16 * jj];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int jj = 0; jj < TN; ++jj) cfma(acc[i][jj], a[i], bb[jj]);
+  }
+#pragma unroll
+  for (int jj = 0; jj < TN; ++jj) {
+    const int c = c0 + tx + 16 * jj;
+    if (c >= c_end) continue;
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+      const int r = r0 + ty + 16 * i;
+      if (r >= r_end) continue;
+      C* p = Mb + size_t(r) + size_t(lay.lda) * c;
+      C v = *p;
+      v.x -= acc[i][jj].x;
+      v.y -= acc[i][jj].y;
+      *p = v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void absorber_solve_kernel(BatchLayout lay, const cplx<T>* __restrict__ M, double2* __restrict__ gg,
+                                      const int* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  double2* U = reinterpret_cast<double2*>(smraw);  // m x m
+  const int b = blockIdx.x;
+  const int n = lay.n, m = lay.m, r0 = n - m;
+  const cplx<T>* Mb = M + size_t(b) * lay.stride;
+  for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+    const int r = idx % m, c = idx / m;
+    const cplx<T> u = Mb[size_t(r0 + r) + size_t(lay.lda) * (r0 + c)];
+    U[r + m * c] = make_double2(double(u.x), double(u.y));
+  }
+  __syncthreads();
+  const int c = threadIdx.x;
+  if (c >= m) return;
+  double2* out = gg + size_t(b) * m * m + size_t(m) * c;
+  for (int r = 0; r < m; ++r) {
+    const cplx<T> y = Mb[size_t(r0 + r) + size_t(lay.lda) * (n + c)];
+    out[r] = make_double2(double(y.x), double(y.y));
+  }
+  const bool bad = status && status[b] != kDevOk;
+  for (int r = m - 1; r >= 0; --r) {
+    double2 v = out[r];
+    for (int p = r + 1; p < m; ++p) cfms(v, U[r + m * p], out[p]);
+    const double2 d = U[r + m * r];
+    out[r] = (bad || (d.x == 0.0 && d.y == 0.0)) ? make_double2(0.0, 0.0) : cdiv(v, d);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 refinement kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double v) {
+  atomicMax(p, static_cast<unsigned long long>(__double_as_longlong(v)));
+}
+
+// R = B - A X for 64 rows per CTA, all m columns; K loop in chunks of 32.
+__global__ void __launch_bounds__(256) residual_kernel(BatchLayout lay, const double2* __restrict__ M64,
+                                                       const double2* __restrict__ X64, double2* __restrict__ R,
+                                                       unsigned long long* rnorm, unsigned long long* bnorm,
+                                                       const int* skip) {
+  constexpr int BR = 64, BK = 16, kMaxM = 64;
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  __shared__ double2 As[BK][BR];
+  __shared__ double2 Xs[BK][kMaxM];
+  const int n = lay.n, m = lay.m;
+  const int r0 = blockIdx.x * BR;
+  const double2* A = M64 + size_t(b) * lay.stride;
+  const double2* X = X64 + size_t(b) * lay.lda * m;
+  double2* Rb = R + size_t(b) * lay.lda * m;
+  const int tid = threadIdx.x;
+  const int row = tid % BR, cg0 = tid / BR;  // column group 0..3
+  constexpr int kCols = kMaxM / 4;
+  double2 acc[kCols];
+#pragma unroll
+  for (int q = 0; q < kCols; ++q) acc[q] = make_double2(0.0, 0.0);
+  for (int k0 = 0; k0 < n; k0 += BK) {
+    const int kk_n = min(BK, n - k0);
+    __syncthreads();
+    for (int idx = tid; idx < BK * BR; idx += 256) {
+      const int r = idx % BR, kk = idx / BR;
+      As[kk][r] = (r0 + r < n && kk < kk_n) ? A[size_t(r0 + r) + size_t(lay.lda) * (k0 + kk)] : make_double2(0.0, 0.0);
+    }
+    for (int idx = tid; idx < BK * m; idx += 256) {
+      const int kk = idx % BK, c = idx / BK;
+      Xs[kk][c] = kk < kk_n ? X[size_t(k0 + kk) + size_t(lay.lda) * c] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kk_n; ++kk) {
+      const double2 a = As[kk][row];
+#pragma unroll
+      for (int q = 0; q < kCols; ++q) {
+        const int c = cg0 + 4 * q;
+        if (c < m) cfma(acc[q], a, Xs[kk][c]);
+      }
+    }
+  }
+  double rmax = 0.0, bmax = 0.0;
+  const bool row_ok = r0 + row < n;
+#pragma unroll
+  for (int q = 0; q < kCols; ++q) {
+    const int c = cg0 + 4 * q;
+    if (c >= m || !row_ok) continue;
+    const double2 bv = A[size_t(r0 + row) + size_t(lay.lda) * (n + c)];
+    const double2 rv = make_double2(bv.x - acc[q].x, bv.y - acc[q].y);
+    Rb[size_t(r0 + row) + size_t(lay.lda) * c] = rv;
+    rmax = fmax(rmax, cabs1(rv));
+    bmax = fmax(bmax, cabs1(bv));
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    rmax = fmax(rmax, __shfl_down_sync(0xffffffffu, rmax, off));
+    bmax = fmax(bmax, __shfl_down_sync(0xffffffffu, bmax, off));
+  }
+  if ((tid & 31) == 0) {
+    atomic_max_nonneg(rnorm + b, rmax);
+    atomic_max_nonneg(bnorm + b, bmax);
+  }
+}
+
+__global__ void refine_check_kernel(int batch, const unsigned long long* rnorm, const unsigned long long* bnorm,
+                                    double tol, int* converged) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  const double r = __longlong_as_double(static_cast<long long>(rnorm[b]));
+  const double bn = __longlong_as_double(static_cast<long long>(bnorm[b]));
+  if (r <= tol * bn) converged[b] = 1;
+}
+
+__device__ __forceinline__ double norm_scale(const unsigned long long* rnorm, int b) {
+  const double r = __longlong_as_double(static_cast<long long>(rnorm[b]));
+  return r > 0.0 ? r : 1.0;
+}
+
+__global__ void residual_to_rhs32_kernel(BatchLayout lay, const double2* __restrict__ R,
+                                         const unsigned long long* rnorm, float2* __restrict__ M32, const int* skip) {
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  const int n = lay.n, m = lay.m;
+  const double inv = 1.0 / norm_scale(rnorm, b);
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n * m; idx += gridDim.x * blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    const double2 v = R[size_t(b) * lay.lda * m + size_t(r) + size_t(lay.lda) * c];
+    M32[size_t(b) * lay.stride + size_t(r) + size_t(lay.lda) * (n + c)] = make_float2(float(v.x * inv), float(v.y * inv));
+  }
+}
+
+__global__ void accumulate_correction_kernel(BatchLayout lay, const float2* __restrict__ M32,
+                                             const unsigned long long* rnorm, double2* __restrict__ X64, int init,
+                                             const int* skip) {
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  const int n = lay.n, m = lay.m;
+  const double sc = init ? 1.0 : norm_scale(rnorm, b);
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n * m; idx += gridDim.x * blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    const float2 d = M32[size_t(b) * lay.stride + size_t(r) + size_t(lay.lda) * (n + c)];
+    double2& x = X64[size_t(b) * lay.lda * m + size_t(r) + size_t(lay.lda) * c];
+    if (init) x = make_double2(double(d.x), double(d.y));
+    else { x.x += double(d.x) * sc; x.y += double(d.y) * sc; }
+  }
+}
+
+__global__ void extract_absorber_kernel(BatchLayout lay, const double2* __restrict__ X64, double2* __restrict__ gg) {
+  const int b = blockIdx.x;
+  const int n = lay.n, m = lay.m;
+  for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+    const int r = idx % m, c = idx / m;
+    gg[size_t(b) * m * m + idx] = X64[size_t(b) * lay.lda * m + size_t(n - m + r) + size_t(lay.lda) * c];
+  }
+}
+
+__global__ void copy_rhs64_kernel(BatchLayout lay, const double2* __restrict__ M64, double2* __restrict__ X64) {
+  const int b = blockIdx.y;
+  const int n = lay.n, m = lay.m;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n * m; idx += gridDim.x * blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    X64[size_t(b) * lay.lda * m + size_t(r) + size_t(lay.lda) * c] =
+        M64[size_t(b) * lay.stride + size_t(r) + size_t(lay.lda) * (n + c)];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <typename T>
+PanelConfig choose_panel(int n) {
+  PanelConfig pc;
+  const size_t budget = 200 * 1024;
+  for (int nb : {(sizeof(T) == 4 && n >= 512) ? 64 : 32, 32}) {
+    for (int cl = 1; cl <= 16; cl *= 2) {
+      const int rpc = (n + cl - 1) / cl;
+      const size_t b = nb == 64 ? panel_smem_bytes<T, 64>(rpc, n) : panel_smem_bytes<T, 32>(rpc, n);
+      if (b <= budget) {
+        pc.nb = nb;
+        pc.cluster = cl;
+        pc.rpc_max = rpc;
+        pc.smem = int(b);
+        return pc;
+      }
+    }
+  }
+  pc.cluster = 0;  // too large for one cluster
+  return pc;
+}
+
+template <typename T, int NB>
+static cudaError_t launch_panel(const PanelConfig& pc, const BatchLayout& lay, int batch, int k, cplx<T>* M,
+                                const LuWork& w, cudaStream_t s) {
+  auto kern = panel_kernel<T, NB>;
+  // Attributes are raised once to the largest request (before any stream capture).
+  static int smem_set = 0;
+  static bool nonportable_set = false;
+  cudaError_t err;
+  if (pc.smem > smem_set) {
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, pc.smem);
+    if (err != cudaSuccess) return err;
+    smem_set = pc.smem;
+  }
+  if (pc.cluster > 8 && !nonportable_set) {
+    err = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (err != cudaSuccess) return err;
+    nonportable_set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(pc.cluster), unsigned(batch), 1);
+  cfg.blockDim = dim3(kPanelThreads, 1, 1);
+  cfg.dynamicSmemBytes = size_t(pc.smem);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = unsigned(pc.cluster);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  count_launch();
+  return cudaLaunchKernelEx(&cfg, kern, lay, k, M, w, pc.rpc_max);
+}
+
+template <typename T, int NB>
+static void launch_rhs_lower(const BatchLayout& lay, int batch, int k, int c_begin, int c_end, cplx<T>* M,
+                             const LuWork& w, const int* skip, cudaStream_t s) {
+  const int ncols = c_end - c_begin;
+  if (ncols <= 0) return;
+  dim3 grid(unsigned((ncols + 7) / 8), unsigned(batch));
+  count_launch();
+  rhs_lower_kernel<T, NB><<<grid, 256, 0, s>>>(lay, k, c_begin, c_end, M, w, skip);
+}
+
+template <typename T, int TM, int TN, int KMAX>
+static void launch_gemm(const BatchLayout& lay, int batch, int r_begin, int r_end, int c_begin, int c_end, int ka,
+                        int kb, cplx<T>* M, const int* skip, cudaStream_t s) {
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  const int rows = r_end - r_begin, cols = c_end - c_begin;
+  if (rows <= 0 || cols <= 0 || kb <= 0) return;
+  const size_t smem = size_t(KMAX) * (BM + BN) * sizeof(cplx<T>);
+  auto kern = gemm_update_kernel<T, TM, TN, KMAX>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    attr_set = true;
+  }
+  dim3 grid(unsigned((rows + BM - 1) / BM), unsigned((cols + BN - 1) / BN), unsigned(batch));
+  count_launch();
+  kern<<<grid, 256, smem, s>>>(lay, r_begin, r_end, c_begin, c_end, ka, kb, M, skip);
+}
+
+template <typename T>
+static void gemm_any(int nb, const BatchLayout& lay, int batch, int r_begin, int r_end, int c_begin, int c_end, int ka,
+                     int kb, cplx<T>* M, const int* skip, cudaStream_t s) {
+  // Skinny right-hand sides (m columns) use a narrow tile.
+  const bool skinny = (c_end - c_begin) <= 32;
+  if (sizeof(T) == 8) {
+    if (skinny) {
+      if (nb == 64) launch_gemm<T, 4, 2, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+      else launch_gemm<T, 4, 2, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+    } else {
+      if (nb == 64) launch_gemm<T, 4, 4, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+      else launch_gemm<T, 4, 4, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+    }
+  } else {
+    if (skinny) {
+      if (nb == 64) launch_gemm<T, 8, 2, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+      else launch_gemm<T, 8, 2, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+    } else {
+      if (nb == 64) launch_gemm<T, 8, 4, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+      else launch_gemm<T, 8, 4, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+    }
+  }
+}
+
+template <typename T>
+cudaError_t lu_eliminate(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const LuWork& w,
+                         cudaStream_t s) {
+  const int n = lay.n, col_end = lay.n + lay.m;
+  if (pc.cluster <= 0 || w.nb != pc.nb) return cudaErrorInvalidValue;
+  for (int k = 0; k < n; k += pc.nb) {
+    const int kb = min(pc.nb, n - k);
+    cudaError_t err;
+    if (pc.nb == 64) {
+      err = launch_panel<T, 64>(pc, lay, batch, k, M, w, s);
+      if (err != cudaSuccess) return err;
+      launch_rhs_lower<T, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
+    } else {
+      err = launch_panel<T, 32>(pc, lay, batch, k, M, w, s);
+      if (err != cudaSuccess) return err;
+      launch_rhs_lower<T, 32>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
+    }
+    gemm_any<T>(pc.nb, lay, batch, k + kb, n, k + kb, col_end, k, kb, M, nullptr, s);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+void lu_forward_rhs(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const LuWork& w,
+                    const int* skip, cudaStream_t s) {
+  const int n = lay.n, col_end = lay.n + lay.m;
+  for (int k = 0; k < n; k += pc.nb) {
+    const int kb = min(pc.nb, n - k);
+    if (pc.nb == 64) launch_rhs_lower<T, 64>(lay, batch, k, n, col_end, M, w, skip, s);
+    else launch_rhs_lower<T, 32>(lay, batch, k, n, col_end, M, w, skip, s);
+    gemm_any<T>(pc.nb, lay, batch, k + kb, n, n, col_end, k, kb, M, skip, s);
+  }
+}
+
+template <typename T>
+void lu_backward_rhs(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const int* skip,
+                     cudaStream_t s) {
+  const int n = lay.n, col_end = lay.n + lay.m;
+  const int last = ((n - 1) / pc.nb) * pc.nb;
+  dim3 grid(unsigned((lay.m + 7) / 8), unsigned(batch));
+  for (int k = last; k >= 0; k -= pc.nb) {
+    const int kb = min(pc.nb, n - k);
+    count_launch();
+    if (pc.nb == 64) rhs_upper_kernel<T, 64><<<grid, 256, 0, s>>>(lay, k, M, skip);
+    else rhs_upper_kernel<T, 32><<<grid, 256, 0, s>>>(lay, k, M, skip);
+    gemm_any<T>(pc.nb, lay, batch, 0, k, n, col_end, k, kb, M, skip, s);
+  }
+}
+
+template <typename T>
+void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, double2* gg, const int* status,
+                           cudaStream_t s) {
+  const int threads = ((lay.m + 31) / 32) * 32;
+  const size_t smem = size_t(lay.m) * lay.m * sizeof(double2);
+  count_launch();
+  absorber_solve_kernel<T><<<unsigned(batch), threads, smem, s>>>(lay, M, gg, status);
+}
+
+void launch_residual(const BatchLayout& lay, int batch, const double2* M64, const double2* X64, double2* R,
+                     unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
+                     cudaStream_t s) {
+  dim3 grid(unsigned((lay.n + 63) / 64), unsigned(batch));
+  count_launch();
+  residual_kernel<<<grid, 256, 0, s>>>(lay, M64, X64, R, rnorm_bits, bnorm_bits, skip);
+}
+
+void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
+                         double tol, int* converged, cudaStream_t s) {
+  count_launch();
+  refine_check_kernel<<<unsigned((batch + 127) / 128), 128, 0, s>>>(batch, rnorm_bits, bnorm_bits, tol, converged);
+}
+
+void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,
+                              const unsigned long long* rnorm_bits, float2* M32, const int* skip, cudaStream_t s) {
+  dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
+  count_launch();
+  residual_to_rhs32_kernel<<<grid, 256, 0, s>>>(lay, R, rnorm_bits, M32, skip);
+}
+
+void launch_accumulate_correction(const BatchLayout& lay, int batch, const float2* M32,
+                                  const unsigned long long* rnorm_bits, double2* X64, bool init, const int* skip,
+                                  cudaStream_t s) {
+  dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
+  count_launch();
+  accumulate_correction_kernel<<<grid, 256, 0, s>>>(lay, M32, rnorm_bits, X64, init ? 1 : 0, skip);
+}
+
+void launch_extract_absorber(const BatchLayout& lay, int batch, const double2* X64, double2* gg, cudaStream_t s) {
+  count_launch();
+  extract_absorber_kernel<<<unsigned(batch), 256, 0, s>>>(lay, X64, gg);
+}
+
+void launch_copy_rhs64(const BatchLayout& lay, int batch, const double2* M64, double2* X64, cudaStream_t s) {
+  dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
+  count_launch();
+  copy_rhs64_kernel<<<grid, 256, 0, s>>>(lay, M64, X64);
+}
+
+template PanelConfig choose_panel<double>(int);
+template PanelConfig choose_panel<float>(int);
+template cudaError_t lu_eliminate<double>(const PanelConfig&, const BatchLayout&, int, double2*, const LuWork&,
+                                          cudaStream_t);
+template cudaError_t lu_eliminate<float>(const PanelConfig&, const BatchLayout&, int, float2*, const LuWork&,
+                                         cudaStream_t);
+template void lu_forward_rhs<double>(const PanelConfig&, const BatchLayout&, int, double2*, const LuWork&, const int*,
+                                     cudaStream_t);
+template void lu_forward_rhs<float>(const PanelConfig&, const BatchLayout&, int, float2*, const LuWork&, const int*,
+                                    cudaStream_t);
+template void lu_backward_rhs<double>(const PanelConfig&, const BatchLayout&, int, double2*, const int*,
+                                      cudaStream_t);
+template void lu_backward_rhs<float>(const PanelConfig&, const BatchLayout&, int, float2*, const int*, cudaStream_t);
+template void launch_absorber_solve<double>(const BatchLayout&, int, const double2*, double2*, const int*,
+                                            cudaStream_t);
+template void launch_absorber_solve<float>(const BatchLayout&, int, const float2*, double2*, const int*,
+                                           cudaStream_t);
+
+}  // namespace rfx

@@ -1,0 +1,78 @@
+// Batched blocked complex LU with partial pivoting on augmented systems
+// [A | B] (column-major, B in columns n .. n+m-1 of the same buffer), and the
+// blocked triangular sweeps that reuse the stored factors.
+#pragma once
+#include <cuda_runtime.h>
+#include "cplx.cuh"
+#include "fms_plan.cuh"
+
+namespace rfx {
+
+// Panel geometry picked on the host for a given n / precision.
+struct PanelConfig {
+  int nb = 32;       // panel width
+  int cluster = 1;   // CTAs per matrix (thread-block cluster)
+  int rpc_max = 0;   // rows per CTA at k = 0
+  int smem = 0;      // dynamic smem bytes per CTA
+};
+
+template <typename T> PanelConfig choose_panel(int n);
+
+inline int panel_count(int n, int nb) { return (n + nb - 1) / nb; }
+
+struct LuWork {
+  int* ipiv = nullptr;    // [batch][n]  LAPACK-style: row k+j was swapped with row ipiv
+  int2* perm = nullptr;   // [batch][npanels][2*nb] (dst, src) row moves per panel
+  int* nperm = nullptr;   // [batch][npanels]
+  int* status = nullptr;  // [batch] DevStatus (max-reduced)
+  int* info = nullptr;    // [batch] first zero pivot (1-based, 0 = none)
+  int npanels = 0;
+  int nb = 0;
+};
+
+// Elimination of the whole augmented system: after it, columns [0, n) hold
+// L\U and columns [n, n+m) hold Y = L^-1 P B.
+template <typename T>
+cudaError_t lu_eliminate(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const LuWork& w,
+                         cudaStream_t s);
+
+// Forward sweep on the right-hand-side columns [n, n+m) only (new RHS):
+// Y = L^-1 P R with the stored per-panel row moves.
+// `skip` (nullable, per matrix): matrices with skip[b] != 0 are left untouched.
+template <typename T>
+void lu_forward_rhs(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const LuWork& w,
+                    const int* skip, cudaStream_t s);
+
+// Backward sweep on the RHS columns: X = U^-1 Y (in place).
+template <typename T>
+void lu_backward_rhs(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const int* skip,
+                     cudaStream_t s);
+
+// gg from the eliminated [U | Y]: solve U[n-m:, n-m:] X = Y[n-m:, :] (m x m,
+// upper triangular) and write X (FP64, column-major m x m) per matrix.
+template <typename T>
+void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, double2* gg, const int* status,
+                           cudaStream_t s);
+
+// FP64 refinement helpers.  X64 and R are n x m per matrix with leading
+// dimension lay.lda and matrix stride lay.lda * m.
+// R = B64 - A64 * X64 and per matrix rnorm = max |R|, bnorm = max |B| (|re|+|im|);
+// matrices with skip[b] != 0 are left untouched (norms included).
+void launch_residual(const BatchLayout& lay, int batch, const double2* M64, const double2* X64, double2* R,
+                     unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip, cudaStream_t s);
+// converged[b] |= (rnorm <= tol * bnorm); iterations[b] counts refinement steps taken.
+void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
+                         double tol, int* converged, cudaStream_t s);
+// RHS columns of M32 <- float(R / rnorm_b)
+void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,
+                              const unsigned long long* rnorm_bits, float2* M32, const int* skip, cudaStream_t s);
+// X64 += D32 * rnorm_b (D32 = RHS columns of M32); with init, X64 = D32.
+void launch_accumulate_correction(const BatchLayout& lay, int batch, const float2* M32,
+                                  const unsigned long long* rnorm_bits, double2* X64, bool init, const int* skip,
+                                  cudaStream_t s);
+// gg (m x m per matrix) = rows [n-m, n) of X64
+void launch_extract_absorber(const BatchLayout& lay, int batch, const double2* X64, double2* gg, cudaStream_t s);
+// X64 = RHS columns of M64 (for the FP64 full solve)
+void launch_copy_rhs64(const BatchLayout& lay, int batch, const double2* M64, double2* X64, cudaStream_t s);
+
+}  // namespace rfx

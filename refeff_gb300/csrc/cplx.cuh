@@ -1,0 +1,51 @@
+// Complex arithmetic for the FMS kernels, templated on the real type.
+// Plain (naive) formulas, matching the num-complex semantics the reference
+// uses (no Annex-G special cases); the kernels never rely on inf/NaN rules.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace rfx {
+
+template <typename R> struct cplx_t;
+template <> struct cplx_t<double> { using type = double2; };
+template <> struct cplx_t<float> { using type = float2; };
+template <typename R> using cplx = typename cplx_t<R>::type;
+
+template <typename R> __host__ __device__ __forceinline__ cplx<R> mk(R re, R im) { cplx<R> z; z.x = re; z.y = im; return z; }
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename C> __host__ __device__ __forceinline__ C cneg(C a) { a.x = -a.x; a.y = -a.y; return a; }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+template <typename C, typename R> __host__ __device__ __forceinline__ C cscale(C a, R s) { a.x *= s; a.y *= s; return a; }
+// acc += a*b with fused multiply-adds (the device path is allowed to contract).
+template <typename C> __device__ __forceinline__ void cfma(C& acc, C a, C b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(a.y, b.x, acc.y);
+}
+// acc -= a*b
+template <typename C> __device__ __forceinline__ void cfms(C& acc, C a, C b) {
+  acc.x = fma(-a.x, b.x, acc.x); acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(-a.x, b.y, acc.y); acc.y = fma(-a.y, b.x, acc.y);
+}
+template <typename C> __host__ __device__ __forceinline__ C cdiv(C a, C b) {
+  auto n = b.x * b.x + b.y * b.y;
+  C r; r.x = (a.x * b.x + a.y * b.y) / n; r.y = (a.y * b.x - a.x * b.y) / n; return r;
+}
+template <typename C> __host__ __device__ __forceinline__ auto cabs1(C a) -> decltype(a.x) {
+  return fabs(a.x) + fabs(a.y);
+}
+template <typename C> __host__ __device__ __forceinline__ bool cfinite(C a) { return isfinite(a.x) && isfinite(a.y); }
+
+__device__ __forceinline__ double2 cexp(double2 a) {
+  double s, c; sincos(a.y, &s, &c); double r = exp(a.x); return make_double2(r * c, r * s);
+}
+__device__ __forceinline__ float2 cexp(float2 a) {
+  float s, c; sincosf(a.y, &s, &c); float r = expf(a.x); return make_float2(r * c, r * s);
+}
+
+template <typename Dst, typename Src> __device__ __forceinline__ Dst ccast(Src s) { Dst d; d.x = s.x; d.y = s.y; return d; }
+
+}  // namespace rfx

@@ -1,0 +1,910 @@
+// Host runtime behind include/refeff_fms.h: context, cluster preparation,
+// plan construction (energy-independent tables resident in HBM), batched
+// execution of the FMS solve on the GPU (captured as CUDA graphs), and the
+// dense batched solve.
+//
+// Reference interfaces replaced here:
+//   fms_yprep_cluster / sort_representative_atoms  crates/refeff-core/src/fms/cluster.rs:10-195
+//   fms_real_space_plan / fms_driver_setup         crates/refeff-core/src/fms/driver.rs:4-140
+//   construct_state_kets_with_limit                crates/refeff-core/src/state.rs:97-148
+//   fms_real_space_spectrum                        crates/refeff-core/src/fms/driver.rs:231-239
+//   fms_gg_section_values                          crates/refeff-engine/src/fms.rs:2004-2047
+//   complex32_faer_lu_factor / _solve              crates/refeff-linalg/src/lu.rs:385-490
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/refeff_fms.h"
+#include "batched_lu.cuh"
+#include "cplx.cuh"
+#include "fms_plan.cuh"
+
+using namespace rfx;
+
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+}
+
+void rfx::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+extern "C" unsigned long long refeff_fms_kernel_launches(void) { return g_launches.load(); }
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct refeff_fms_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int sm_count = 0;
+};
+
+namespace {
+
+int fail(refeff_fms_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return code;
+}
+
+int cuda_fail(refeff_fms_context* ctx, cudaError_t err, const char* where) {
+  const int code = (err == cudaErrorMemoryAllocation) ? REFEFF_FMS_ERR_OUT_OF_MEMORY : REFEFF_FMS_ERR_CUDA;
+  return fail(ctx, code, std::string(where) + ": " + cudaGetErrorString(err));
+}
+
+#define RF_CUDA(ctx, expr)                                   \
+  do {                                                       \
+    cudaError_t rf_err_ = (expr);                            \
+    if (rf_err_ != cudaSuccess) return cuda_fail(ctx, rf_err_, #expr); \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
+    cudaError_t e = alloc(count);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+};
+
+struct Atom {
+  float pos[3];
+  int pot;
+};
+
+// athep radial sort (crates/refeff-core/src/fms/internals/geometry.rs:30-36,
+// cluster.rs:91-107): stable sort by r^2 + (index+1)*1e-6 in f64.
+void athep_sort(std::vector<Atom>& atoms) {
+  std::vector<std::pair<double, size_t>> keyed(atoms.size());
+  for (size_t i = 0; i < atoms.size(); ++i) {
+    const double x = atoms[i].pos[0], y = atoms[i].pos[1], z = atoms[i].pos[2];
+    keyed[i] = {x * x + y * y + z * z + (double(i) + 1.0) * 1.0e-6, i};
+  }
+  std::stable_sort(keyed.begin(), keyed.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  std::vector<Atom> out(atoms.size());
+  for (size_t i = 0; i < atoms.size(); ++i) out[i] = atoms[keyed[i].second];
+  atoms.swap(out);
+}
+
+bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+}  // namespace
+
+extern "C" int refeff_fms_abi_version(void) { return REFEFF_FMS_ABI_VERSION; }
+
+extern "C" int refeff_fms_context_create(int device, refeff_fms_context** out) {
+  if (!out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || device < 0 || device >= count) return REFEFF_FMS_ERR_CUDA;
+  auto* ctx = new refeff_fms_context();
+  ctx->device = device;
+  if ((e = cudaSetDevice(device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete ctx;
+    return REFEFF_FMS_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  *out = ctx;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" void refeff_fms_context_destroy(refeff_fms_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+}
+
+extern "C" const char* refeff_fms_last_error(const refeff_fms_context* ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+// ---------------------------------------------------------------------------
+// cluster preparation (FEFF yprep + sortat)
+// ---------------------------------------------------------------------------
+extern "C" int refeff_fms_yprep_cluster(int central_potential, int max_potential, int n_rows, const int* potentials,
+                                        const float* positions_xyz, float cluster_radius, int cluster_capacity,
+                                        float* out_positions_xyz, int* out_potentials, int* out_count) {
+  if (n_rows <= 0 || !potentials || !positions_xyz || !out_positions_xyz || !out_potentials || !out_count)
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (!std::isfinite(cluster_radius) || cluster_radius < 0.0f) return REFEFF_FMS_ERR_INVALID_CLUSTER_RADIUS;
+  if (cluster_capacity <= 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  // cluster.rs:34-50: first atom with the central potential; duplicate absorbers rejected
+  long central = -1;
+  for (int i = 0; i < n_rows; ++i) {
+    if (potentials[i] == central_potential) {
+      if (central_potential == 0 && central >= 0) return REFEFF_FMS_ERR_DUPLICATE_ABSORBER;
+      if (central < 0) central = i;
+    }
+  }
+  if (central < 0) return REFEFF_FMS_ERR_MISSING_CENTRAL_ATOM;
+  const float* c = positions_xyz + 3 * central;
+  if (!finite3(c)) return REFEFF_FMS_ERR_NONFINITE_COORDINATE;
+  std::vector<Atom> atoms(static_cast<size_t>(n_rows));
+  for (int i = 0; i < n_rows; ++i) {
+    for (int a = 0; a < 3; ++a) atoms[size_t(i)].pos[a] = positions_xyz[3 * i + a] - c[a];
+    if (!finite3(atoms[size_t(i)].pos)) return REFEFF_FMS_ERR_NONFINITE_COORDINATE;
+    atoms[size_t(i)].pot = potentials[i];
+  }
+  athep_sort(atoms);
+  const float r2 = cluster_radius * cluster_radius;
+  size_t first_outside = atoms.size();
+  for (size_t i = 0; i < atoms.size(); ++i) {
+    const float* p = atoms[i].pos;
+    if (p[0] * p[0] + p[1] * p[1] + p[2] * p[2] > r2) { first_outside = i; break; }
+  }
+  const size_t untruncated = first_outside == 0 ? atoms.size() : first_outside;
+  atoms.resize(std::min(untruncated, size_t(cluster_capacity)));
+  // sortat (cluster.rs:115-195): representatives of each potential into the prefix
+  if (central_potential < 0 || central_potential > max_potential) return REFEFF_FMS_ERR_POTENTIAL_OUT_OF_RANGE;
+  for (auto& a : atoms)
+    if (a.pot < 0 || a.pot > max_potential) return REFEFF_FMS_ERR_POTENTIAL_OUT_OF_RANGE;
+  std::vector<long> rep(size_t(max_potential) + 1, -1);
+  rep[size_t(central_potential)] = 0;
+  for (int p = 0; p <= max_potential; ++p) {
+    if (p == central_potential) continue;
+    for (size_t i = 1; i < atoms.size(); ++i)
+      if (atoms[i].pot == p) { rep[size_t(p)] = long(i); break; }
+  }
+  for (int p = 0; p <= max_potential; ++p) {
+    const long point = rep[size_t(p)];
+    if (point < 0 || point <= p) continue;
+    std::swap(atoms[size_t(p)], atoms[size_t(point)]);
+    for (int q = p + 1; q <= max_potential; ++q)
+      if (rep[size_t(q)] == p) rep[size_t(q)] = point;
+    rep[size_t(p)] = p;
+  }
+  const size_t prefix = std::min(atoms.size(), size_t(max_potential) + 1);
+  for (int p = 0; p <= max_potential; ++p) {
+    const long point = rep[size_t(p)];
+    if (point < 0) continue;
+    long last = -1;
+    for (size_t i = 0; i < prefix; ++i)
+      if (atoms[i].pot == p) last = long(i);
+    if (last >= 0 && last != point) {
+      float tmp[3];
+      std::memcpy(tmp, atoms[size_t(last)].pos, sizeof tmp);
+      std::memcpy(atoms[size_t(last)].pos, atoms[size_t(point)].pos, sizeof tmp);
+      std::memcpy(atoms[size_t(point)].pos, tmp, sizeof tmp);
+      rep[size_t(p)] = last;
+    }
+  }
+  for (size_t i = 0; i < atoms.size(); ++i) {
+    std::memcpy(out_positions_xyz + 3 * i, atoms[i].pos, 3 * sizeof(float));
+    out_potentials[i] = atoms[i].pot;
+  }
+  *out_count = int(atoms.size());
+  return REFEFF_FMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plan
+// ---------------------------------------------------------------------------
+namespace {
+
+// FEFF's associated-Legendre normalization (crates/refeff-core/src/angular/harmonics.rs:51-75).
+double xnlm_value(int l, int m) {
+  if (m > l) return 0.0;
+  double den = 1.0;
+  for (int k = l - m + 1; k <= l + m; ++k) den *= double(k);
+  return std::sqrt(double(2 * l + 1) / den);
+}
+
+// Doubled-argument Wigner 3j by the Racah sum over log-factorials and the
+// t3jp / t3jm coefficients (crates/refeff-core/src/angular/coupling.rs:4-40).
+double wigner3j_doubled(int j1, int j2, int j3, int m1, int m2) {
+  const int m3 = -m1 - m2;
+  if (std::abs(m1) + std::abs(m2) == 0 && (j1 + j2 + j3) % 4 != 0) return 0.0;
+  int v[12] = {j1 + j2 - j3, j2 + j3 - j1, j3 + j1 - j2, j1 + m1, j1 - m1, j2 + m2,
+               j2 - m2,      j3 + m3,      j3 - m3,      j1 + j2 + j3 + 2, j2 - j3 - m1, j1 - j3 + m2};
+  for (int i = 0; i < 12; ++i) {
+    if (i < 10 && v[i] < 0) return 0.0;
+    v[i] /= 2;
+  }
+  double lf[64];
+  lf[0] = 0.0;
+  for (int i = 1; i < 64; ++i) lf[i] = lf[i - 1] + std::log(double(i));
+  const int kmin = std::max(std::max(v[10], v[11]), 0), kmax = std::min(std::min(v[0], v[4]), v[5]);
+  if (kmin > kmax) return 0.0;
+  double sign = (kmin % 2 == 0) ? 1.0 : -1.0;
+  double c = -lf[v[9]];
+  for (int i = 0; i < 9; ++i) c += lf[v[i]];
+  c /= 2.0;
+  double coef = 0.0;
+  for (int k = kmin; k <= kmax; ++k) {
+    coef += sign * std::exp(c - (lf[k] + lf[v[0] - k] + lf[v[4] - k] + lf[v[5] - k] + lf[k - v[10]] + lf[k - v[11]]));
+    sign = -sign;
+  }
+  if ((j1 - j2 - m3) % 4 != 0) coef = -coef;
+  return coef;
+}
+
+double so_coefficient(bool plus, int l, int m, int spin) {
+  const int j1 = 2 * l, j2 = 1, j3 = plus ? j1 + 1 : j1 - 1, m1 = 2 * m, m2 = 2 * spin - 3;
+  const int phase = (j2 - j1 - m1 - m2) / 2;
+  return ((phase % 2 == 0) ? 1.0 : -1.0) * std::sqrt(double(j3 + 1)) * wigner3j_doubled(j1, j2, j3, m1, m2);
+}
+
+}  // namespace
+
+struct Workspace {
+  int batch = 0;
+  bool fp32 = false;
+  BatchLayout lay;
+  PanelConfig pc64, pc32;
+  DevBuf<double2> M64;
+  DevBuf<float2> M32;
+  DevBuf<double2> X64, R;
+  DevBuf<unsigned long long> rnorm, bnorm;
+  DevBuf<int> converged;
+  DevBuf<int> ipiv, nperm, status, info;
+  DevBuf<int2> perm;
+  // staging so that a captured graph can be replayed on every batch
+  DevBuf<double2> k_stage, x_stage, gg_stage;
+  std::map<int, cudaGraphExec_t> graphs;  // key: form
+  std::map<int, unsigned long long> graph_launches;  // kernel launches per replay
+  void drop_graphs() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    graphs.clear();
+  }
+  ~Workspace() { drop_graphs(); }
+};
+
+struct refeff_fms_plan {
+  refeff_fms_context* ctx = nullptr;
+  int N = 0, L = 0, nsp = 1, ispin = 0, npot = 0, lfms = 0, minv = 0;
+  int n = 0, m = 0, C = 0, abs_pot = 0, abs_lmax = 0;
+  std::vector<int> pot_lmax;
+  std::vector<long> rep_offsets;  // reference state order
+  int max_batch = 0;
+  int refine_iters = 4;
+  double refine_tol = 1.0e-14;
+  // device tables
+  PlanDev P;
+  DevBuf<float> d_pos;
+  DevBuf<int> d_atom_pot, d_atom_off, d_atom_lmax;
+  DevBuf<double> d_sigsqr, d_dist, d_phi, d_dsmall, d_xnlm, d_t3p, d_t3m;
+  DevBuf<double2> d_k_all, d_x_all, d_gg_all;
+  DevBuf<int> d_status_all;
+  Workspace ws;
+  bool profiling = false;
+  double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0};
+  size_t xph_per_energy() const { return size_t(nsp) * size_t(2 * L + 1) * size_t(npot); }
+};
+
+extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* in,
+                                                 refeff_fms_plan** out) {
+  if (!ctx || !in || !out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  ctx->last_error.clear();
+  if (in->n_atoms <= 0) return fail(ctx, REFEFF_FMS_ERR_EMPTY_CLUSTER, "empty cluster");
+  if (!in->positions_xyz || !in->potentials || !in->raw_potential_lmax)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "null plan input array");
+  if (in->spin_channels < 1 || in->spin_channels > 2)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "spin_channels must be 1 or 2");
+  if (in->max_potential < 0) return fail(ctx, REFEFF_FMS_ERR_POTENTIAL_OUT_OF_RANGE, "negative max_potential");
+  if (in->global_lmax < 0 || in->global_lmax > kMaxL)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ANGULAR_LIMIT, "global_lmax outside 0..6");
+  if (!std::isfinite(in->direct_cutoff) || in->direct_cutoff < 0.0f)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "invalid direct cutoff");
+  if (!std::isfinite(in->zero_tolerance) || in->zero_tolerance < 0.0f)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_TOLERANCE, "invalid toler2");
+  auto plan = std::make_unique<refeff_fms_plan>();
+  refeff_fms_plan& p = *plan;
+  p.ctx = ctx;
+  p.N = in->n_atoms;
+  p.L = in->global_lmax;
+  p.nsp = in->spin_channels;
+  p.ispin = in->spin_selector;
+  p.npot = in->max_potential + 1;
+  p.lfms = in->lfms;
+  p.minv = in->minv;
+  const int N = p.N, L = p.L, nsp = p.nsp;
+  // driver.rs:25-31, validation.rs:69-75: clamp lipotx
+  p.pot_lmax.resize(size_t(p.npot));
+  for (int q = 0; q < p.npot; ++q) {
+    const int v = in->raw_potential_lmax[q];
+    p.pot_lmax[size_t(q)] = v < 0 ? L : std::min(v, L);
+  }
+  std::vector<int> atom_pot(static_cast<size_t>(N));
+  for (int a = 0; a < N; ++a) {
+    const int pot = in->potentials[a];
+    if (pot < 0 || pot > in->max_potential)
+      return fail(ctx, REFEFF_FMS_ERR_POTENTIAL_OUT_OF_RANGE, "atom " + std::to_string(a) + " potential out of range");
+    if (!finite3(in->positions_xyz + 3 * a)) return fail(ctx, REFEFF_FMS_ERR_NONFINITE_COORDINATE, "non-finite coordinate");
+    atom_pot[size_t(a)] = pot;
+  }
+  // state kets (state.rs:97-148) in reference order: offsets per potential
+  p.rep_offsets.assign(size_t(p.npot), -1);
+  std::vector<int> ref_off(static_cast<size_t>(N) + 1, 0);
+  for (int a = 0; a < N; ++a) {
+    const int pot = atom_pot[size_t(a)];
+    if (p.rep_offsets[size_t(pot)] < 0) p.rep_offsets[size_t(pot)] = ref_off[size_t(a)];
+    const int lm = std::min(L, p.pot_lmax[size_t(pot)]);
+    ref_off[size_t(a) + 1] = ref_off[size_t(a)] + nsp * (lm + 1) * (lm + 1);
+  }
+  p.n = ref_off[size_t(N)];
+  p.abs_pot = atom_pot[0];
+  p.abs_lmax = std::min(L, p.pot_lmax[size_t(p.abs_pot)]);
+  p.m = nsp * (p.abs_lmax + 1) * (p.abs_lmax + 1);
+  p.C = nsp * (L + 1) * (L + 1);
+  // driver.rs:36-60: active potential range must have representatives
+  const int pstart = p.lfms == 0 ? p.abs_pot : 0, pend = p.lfms == 0 ? p.abs_pot : in->max_potential;
+  for (int q = pstart; q <= pend; ++q)
+    if (p.rep_offsets[size_t(q)] < 0)
+      return fail(ctx, REFEFF_FMS_ERR_MISSING_REPRESENTATIVE, "no atom for potential " + std::to_string(q));
+  if (p.lfms != 0)
+    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "lfms != 0 (all-potential FMS) is not supported by this library");
+  if (N < 2) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "a single-atom cluster has no scattering");
+
+  // device atom order: reference atom 0 (absorber) last
+  auto dev = [N](int a) { return a == 0 ? N - 1 : a - 1; };
+  std::vector<float> pos(static_cast<size_t>(3 * N));
+  std::vector<int> dpot(static_cast<size_t>(N)), doff(static_cast<size_t>(N) + 1, 0), dlmax(static_cast<size_t>(N));
+  for (int a = 0; a < N; ++a) {
+    const int d = dev(a);
+    std::memcpy(&pos[size_t(3 * d)], in->positions_xyz + 3 * a, 3 * sizeof(float));
+    dpot[size_t(d)] = atom_pot[size_t(a)];
+    dlmax[size_t(d)] = std::min(L, p.pot_lmax[size_t(atom_pot[size_t(a)])]);
+  }
+  for (int d = 0; d < N; ++d) doff[size_t(d) + 1] = doff[size_t(d)] + nsp * (dlmax[size_t(d)] + 1) * (dlmax[size_t(d)] + 1);
+  // sigma^2 table, device order [a2 + N a1] (engine/fms.rs:4394-4426)
+  std::vector<double> sig(static_cast<size_t>(N) * N, 0.0);
+  for (int a1 = 0; a1 < N; ++a1)
+    for (int a2 = 0; a2 < N; ++a2) {
+      if (a1 == a2) continue;
+      const float v = in->mean_square_displacements ? in->mean_square_displacements[size_t(a2) + size_t(N) * a1] : in->sig2g;
+      if (!std::isfinite(v)) return fail(ctx, REFEFF_FMS_ERR_NONFINITE_INPUT, "non-finite mean-square displacement");
+      sig[size_t(dev(a2)) + size_t(N) * dev(a1)] = double(v);
+    }
+  // xnlm narrowed to f32 like the reference (pairs.rs:678)
+  std::vector<double> xnlm(static_cast<size_t>((L + 1) * (L + 1)), 0.0);
+  for (int l = 0; l <= L; ++l)
+    for (int mu = 0; mu <= l; ++mu) xnlm[size_t(mu + (L + 1) * l)] = double(float(xnlm_value(l, mu)));
+  const int D = 2 * L + 1;
+  std::vector<double> t3p(size_t(L + 1) * D * 2, 0.0), t3m(size_t(L + 1) * D * 2, 0.0);
+  for (int l = 0; l <= L; ++l)
+    for (int mm = -l; mm <= l; ++mm)
+      for (int s = 1; s <= 2; ++s) {
+        const size_t idx = size_t(l) + size_t(L + 1) * (size_t(mm + L) + size_t(D) * size_t(s - 1));
+        t3p[idx] = double(float(so_coefficient(true, l, mm, s)));
+        t3m[idx] = double(float(so_coefficient(false, l, mm, s)));
+      }
+
+  RF_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const int ds = 2 * (L + 1) * (2 * L + 1) * (2 * L + 3) / 3;
+  RF_CUDA(ctx, p.d_pos.upload(pos.data(), pos.size(), s));
+  RF_CUDA(ctx, p.d_atom_pot.upload(dpot.data(), dpot.size(), s));
+  RF_CUDA(ctx, p.d_atom_off.upload(doff.data(), doff.size(), s));
+  RF_CUDA(ctx, p.d_atom_lmax.upload(dlmax.data(), dlmax.size(), s));
+  RF_CUDA(ctx, p.d_sigsqr.upload(sig.data(), sig.size(), s));
+  RF_CUDA(ctx, p.d_xnlm.upload(xnlm.data(), xnlm.size(), s));
+  RF_CUDA(ctx, p.d_t3p.upload(t3p.data(), t3p.size(), s));
+  RF_CUDA(ctx, p.d_t3m.upload(t3m.data(), t3m.size(), s));
+  RF_CUDA(ctx, p.d_dist.alloc(size_t(N) * N));
+  RF_CUDA(ctx, p.d_phi.alloc(size_t(N) * N));
+  RF_CUDA(ctx, p.d_dsmall.alloc(size_t(N) * N * ds));
+  PlanDev& P = p.P;
+  P.N = N; P.L = L; P.nsp = nsp; P.ispin = p.ispin; P.npot = p.npot; P.n = p.n; P.m = p.m; P.ds = ds;
+  P.pos = p.d_pos.p; P.atom_pot = p.d_atom_pot.p; P.atom_off = p.d_atom_off.p; P.atom_lmax = p.d_atom_lmax.p;
+  P.sigsqr = p.d_sigsqr.p; P.pair_dist = p.d_dist.p; P.pair_phi = p.d_phi.p; P.pair_dsmall = p.d_dsmall.p;
+  P.xnlm = p.d_xnlm.p; P.t3p = p.d_t3p.p; P.t3m = p.d_t3m.p;
+  P.rdirec2 = double(in->direct_cutoff) * double(in->direct_cutoff);
+  launch_plan_geometry(P, s);
+  RF_CUDA(ctx, cudaGetLastError());
+  RF_CUDA(ctx, cudaStreamSynchronize(s));
+  *out = plan.release();
+  return REFEFF_FMS_OK;
+}
+
+extern "C" void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan) {
+  if (!plan) return;
+  cudaSetDevice(plan->ctx->device);
+  cudaStreamSynchronize(plan->ctx->stream);
+  delete plan;
+}
+
+extern "C" int refeff_fms_plan_set_profiling(refeff_fms_plan* plan, int enable) {
+  if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->profiling = enable != 0;
+  for (double& v : plan->phase_ms) v = 0.0;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_phase_times(const refeff_fms_plan* plan, double* ms_out, int n_phases) {
+  if (!plan || !ms_out || n_phases < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < n_phases && i < REFEFF_FMS_PHASES; ++i) ms_out[i] = plan->phase_ms[i];
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_query(const refeff_fms_plan* plan, int* n_states, int* channel_count, int* absorber_block,
+                                     int* n_potentials) {
+  if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (n_states) *n_states = plan->n;
+  if (channel_count) *channel_count = plan->C;
+  if (absorber_block) *absorber_block = plan->m;
+  if (n_potentials) *n_potentials = plan->npot;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_set_batch(refeff_fms_plan* plan, int max_batch) {
+  if (!plan || max_batch < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->max_batch = max_batch;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_set_refinement(refeff_fms_plan* plan, int max_iterations, double tolerance) {
+  if (!plan || max_iterations < 0 || !(tolerance > 0.0)) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->refine_iters = max_iterations;
+  plan->refine_tol = tolerance;
+  plan->ws.drop_graphs();
+  return REFEFF_FMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batched execution
+// ---------------------------------------------------------------------------
+namespace {
+
+BatchLayout make_layout(int n, int m) {
+  BatchLayout lay;
+  lay.n = n;
+  lay.m = m;
+  lay.lda = (n + 31) / 32 * 32;
+  lay.stride = size_t(lay.lda) * size_t(n + m);
+  return lay;
+}
+
+size_t bytes_per_system(const BatchLayout& lay, bool fp32) {
+  size_t b = lay.stride * sizeof(double2);
+  if (fp32) b += lay.stride * sizeof(float2) + 2 * size_t(lay.lda) * lay.m * sizeof(double2);
+  return b;
+}
+
+int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32) {
+  const BatchLayout lay = make_layout(n, m);
+  if (ws.batch >= batch && ws.lay.n == n && ws.lay.m == m && (ws.fp32 || !fp32)) return REFEFF_FMS_OK;
+  ws.drop_graphs();
+  ws.batch = std::max(batch, ws.lay.n == n && ws.lay.m == m ? ws.batch : 0);
+  ws.fp32 = fp32 || (ws.lay.n == n && ws.lay.m == m && ws.fp32);
+  ws.lay = lay;
+  const int B = ws.batch;
+  ws.pc64 = choose_panel<double>(n);
+  ws.pc32 = choose_panel<float>(n);
+  if (ws.pc64.cluster <= 0 || (ws.fp32 && ws.pc32.cluster <= 0))
+    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "system too large for the cluster panel factorization");
+  const int nb_min = std::min(ws.pc64.nb, ws.pc32.nb);
+  const int nb_max = std::max(ws.pc64.nb, ws.pc32.nb);
+  const int npanels = panel_count(n, nb_min);
+  RF_CUDA(ctx, ws.M64.alloc(size_t(B) * lay.stride));
+  if (ws.fp32) {
+    RF_CUDA(ctx, ws.M32.alloc(size_t(B) * lay.stride));
+    RF_CUDA(ctx, ws.X64.alloc(size_t(B) * lay.lda * m));
+    RF_CUDA(ctx, ws.R.alloc(size_t(B) * lay.lda * m));
+    RF_CUDA(ctx, ws.rnorm.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.bnorm.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.converged.alloc(size_t(B)));
+  }
+  RF_CUDA(ctx, ws.ipiv.alloc(size_t(B) * n));
+  RF_CUDA(ctx, ws.perm.alloc(size_t(B) * npanels * 2 * nb_max));
+  RF_CUDA(ctx, ws.nperm.alloc(size_t(B) * npanels));
+  RF_CUDA(ctx, ws.status.alloc(size_t(B)));
+  RF_CUDA(ctx, ws.info.alloc(size_t(B)));
+  return REFEFF_FMS_OK;
+}
+
+LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
+  LuWork w;
+  w.ipiv = ws.ipiv.p;
+  w.perm = ws.perm.p;
+  w.nperm = ws.nperm.p;
+  w.status = ws.status.p;
+  w.info = ws.info.p;
+  w.nb = pc.nb;
+  w.npanels = panel_count(ws.lay.n, pc.nb);
+  return w;
+}
+
+using Spans = std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>>;
+
+// Refinement of X64 for [A64 | B64] in M64 with the FP32 factors in M32
+// (eliminated; RHS columns of M32 hold Y32).  Leaves converged flags and
+// final residual norms in the workspace.  With `spans`, events bracket the
+// sweeps (phase 2) and the residuals (phase 3).
+cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStream_t s, Spans* spans = nullptr) {
+  const BatchLayout& lay = ws.lay;
+  const LuWork w32 = lu_work(ws, ws.pc32);
+  auto span = [&](int phase, auto&& fn) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (spans) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+    fn();
+    if (spans) {
+      cudaEventRecord(b, s);
+      spans->push_back({phase, {a, b}});
+    }
+  };
+  span(2, [&] {
+    lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, nullptr, s);
+    launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, true, nullptr, s);
+  });
+  cudaMemsetAsync(ws.converged.p, 0, size_t(batch) * sizeof(int), s);
+  for (int it = 0; it <= iters; ++it) {
+    span(3, [&] {
+      cudaMemsetAsync(ws.rnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
+      cudaMemsetAsync(ws.bnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
+      launch_residual(lay, batch, ws.M64.p, ws.X64.p, ws.R.p, ws.rnorm.p, ws.bnorm.p, nullptr, s);
+      launch_refine_check(batch, ws.rnorm.p, ws.bnorm.p, tol, ws.converged.p, s);
+    });
+    if (it == iters) break;
+    span(2, [&] {
+      launch_residual_to_rhs32(lay, batch, ws.R.p, ws.rnorm.p, ws.M32.p, ws.converged.p, s);
+      lu_forward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, w32, ws.converged.p, s);
+      lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, ws.converged.p, s);
+      launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, false, ws.converged.p, s);
+    });
+  }
+  return cudaGetLastError();
+}
+
+__global__ void convert_to_f32_kernel(BatchLayout lay, const double2* __restrict__ M64, float2* __restrict__ M32) {
+  const int b = blockIdx.y;
+  const size_t total = lay.stride;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+    const double2 v = M64[size_t(b) * lay.stride + i];
+    M32[size_t(b) * lay.stride + i] = make_float2(float(v.x), float(v.y));
+  }
+}
+
+__global__ void status_not_converged_kernel(int batch, const int* converged, int* status) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch && !converged[b] && status[b] == kDevOk) status[b] = kDevNotConverged;
+}
+
+// One batch of energies from the staging buffers (k_stage, x_stage) into gg_stage/status.
+// With profiling on, CUDA events bracket each phase (see refeff_fms_plan_phase_times).
+cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, cudaStream_t s) {
+  Workspace& ws = p.ws;
+  const BatchLayout& lay = ws.lay;
+  cudaMemsetAsync(ws.status.p, 0, size_t(batch) * sizeof(int), s);
+  cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s);
+  const bool prof = p.profiling;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
+  auto tick = [&](int phase, auto&& fn) -> cudaError_t {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (prof) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+    cudaError_t e = fn();
+    if (prof) {
+      cudaEventRecord(b, s);
+      spans.push_back({phase, {a, b}});
+    }
+    return e;
+  };
+  cudaError_t e = cudaSuccess;
+  if (form == REFEFF_FMS_FORM_FP64_LU) {
+    tick(0, [&] {
+      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, nullptr, ws.status.p, s);
+      return cudaGetLastError();
+    });
+    e = tick(1, [&] { return lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s); });
+    if (e != cudaSuccess) return e;
+    tick(4, [&] {
+      launch_absorber_solve<double>(lay, batch, ws.M64.p, ws.gg_stage.p, ws.status.p, s);
+      return cudaGetLastError();
+    });
+  } else {
+    tick(0, [&] {
+      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, ws.M32.p, ws.status.p, s);
+      return cudaGetLastError();
+    });
+    e = tick(1, [&] { return lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s); });
+    if (e != cudaSuccess) return e;
+    e = refine_fp32(ws, batch, p.refine_iters, p.refine_tol, s, prof ? &spans : nullptr);
+    if (e != cudaSuccess) return e;
+    tick(4, [&] {
+      count_launch();
+      status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
+      launch_extract_absorber(lay, batch, ws.X64.p, ws.gg_stage.p, s);
+      return cudaGetLastError();
+    });
+  }
+  if (prof) {
+    cudaStreamSynchronize(s);
+    for (auto& sp : spans) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, sp.second.first, sp.second.second);
+      p.phase_ms[sp.first] += ms;
+      cudaEventDestroy(sp.second.first);
+      cudaEventDestroy(sp.second.second);
+    }
+  }
+  return cudaGetLastError();
+}
+
+int map_status(int dev) {
+  switch (dev) {
+    case kDevOk: return REFEFF_FMS_OK;
+    case kDevSingular: return REFEFF_FMS_ERR_SINGULAR_MATRIX;
+    case kDevNonfinite: return REFEFF_FMS_ERR_NONFINITE_INPUT;
+    case kDevZeroRho: return REFEFF_FMS_ERR_ZERO_RHO;
+    case kDevNotConverged: return REFEFF_FMS_ERR_NOT_CONVERGED;
+    default: return REFEFF_FMS_ERR_CUDA;
+  }
+}
+
+int pick_batch(refeff_fms_plan& p, int E, bool fp32) {
+  if (p.max_batch > 0) return std::min(E, p.max_batch);
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const BatchLayout lay = make_layout(p.n, p.m);
+  const size_t per = bytes_per_system(lay, fp32);
+  const size_t budget = size_t(double(free_b) * 0.5);
+  int b = int(std::max<size_t>(1, budget / std::max<size_t>(per, 1)));
+  b = std::min(b, 256);
+  return std::min(E, b);
+}
+
+// Solve E energies whose inputs are already on the device (d_k: E*nsp, d_x:
+// E*xph); writes d_gg (E*m*m) and d_status (E).  Uses graph replay per batch.
+int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
+                          double2* d_gg, int* d_status, cudaStream_t s) {
+  refeff_fms_context* ctx = p.ctx;
+  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
+  const int B = pick_batch(p, E, fp32);
+  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, fp32);
+  if (rc) return rc;
+  Workspace& ws = p.ws;
+  const size_t xph = p.xph_per_energy();
+  RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
+  RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
+  RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.m * p.m));
+  for (int e0 = 0; e0 < E; e0 += B) {
+    const int nb = std::min(B, E - e0);
+    RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, d_k + size_t(e0) * p.nsp, size_t(nb) * p.nsp * sizeof(double2),
+                                 cudaMemcpyDeviceToDevice, s));
+    RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
+                                 cudaMemcpyDeviceToDevice, s));
+    if (nb == B && !p.profiling) {
+      const int key = int(form);
+      auto it = ws.graphs.find(key);
+      if (it == ws.graphs.end()) {
+        // first run un-captured (sets kernel attributes), then capture
+        cudaError_t e = run_fms_batch(p, nb, form, s);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch");
+        cudaGraph_t g = nullptr;
+        RF_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const unsigned long long before = g_launches.load();
+        e = run_fms_batch(p, nb, form, s);
+        ws.graph_launches[key] = g_launches.load() - before;
+        cudaError_t e2 = cudaStreamEndCapture(s, &g);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch capture");
+        if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "end capture");
+        cudaGraphExec_t ge = nullptr;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
+        ws.graphs[key] = ge;
+      } else {
+        RF_CUDA(ctx, cudaGraphLaunch(it->second, s));
+        g_launches.fetch_add(ws.graph_launches[key], std::memory_order_relaxed);
+      }
+    } else {
+      cudaError_t e = run_fms_batch(p, nb, form, s);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch");
+    }
+    RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.m * p.m, ws.gg_stage.p, size_t(nb) * p.m * p.m * sizeof(double2),
+                                 cudaMemcpyDeviceToDevice, s));
+    RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+  }
+  return REFEFF_FMS_OK;
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies, const void* d_wave_numbers,
+                                                     const void* d_phase_shifts, refeff_fms_form form, void* d_gg_out,
+                                                     int32_t* d_status, void* stream) {
+  if (!plan || n_energies < 0 || (n_energies > 0 && (!d_wave_numbers || !d_phase_shifts || !d_gg_out || !d_status)))
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
+    return fail(plan->ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
+  if (n_energies == 0) return REFEFF_FMS_OK;
+  RF_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : plan->ctx->stream;
+  return solve_device_energies(*plan, n_energies, static_cast<const double2*>(d_wave_numbers),
+                               static_cast<const double2*>(d_phase_shifts), form, static_cast<double2*>(d_gg_out),
+                               d_status, s);
+}
+
+extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                              refeff_fms_form form, refeff_complex128* scattering_out,
+                                              int32_t* status_out, refeff_fms_report* report) {
+  if (!plan || !points || !scattering_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  refeff_fms_context* ctx = plan->ctx;
+  ctx->last_error.clear();
+  const auto t0 = std::chrono::steady_clock::now();
+  const int E = points->n_energies;
+  if (E < 0 || (E > 0 && (!points->wave_numbers || !points->phase_shifts)))
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "invalid energy points");
+  if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
+  refeff_fms_plan& p = *plan;
+  const size_t C = size_t(p.C), tab = C * C * size_t(p.npot);
+  std::memset(scattering_out, 0, size_t(E) * tab * sizeof(refeff_complex128));
+  if (E == 0) return REFEFF_FMS_OK;
+  RF_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const size_t xph = p.xph_per_energy();
+  RF_CUDA(ctx, p.d_k_all.upload(reinterpret_cast<const double2*>(points->wave_numbers), size_t(E) * p.nsp, s));
+  RF_CUDA(ctx, p.d_x_all.upload(reinterpret_cast<const double2*>(points->phase_shifts), size_t(E) * xph, s));
+  RF_CUDA(ctx, p.d_gg_all.alloc(size_t(E) * p.m * p.m));
+  RF_CUDA(ctx, p.d_status_all.alloc(size_t(E)));
+  int rc = solve_device_energies(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
+  if (rc) return rc;
+  std::vector<double2> gg(size_t(E) * p.m * p.m);
+  std::vector<int> st(static_cast<size_t>(E));
+  RF_CUDA(ctx, cudaMemcpyAsync(gg.data(), p.d_gg_all.p, gg.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(ctx, cudaMemcpyAsync(st.data(), p.d_status_all.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(ctx, cudaStreamSynchronize(s));
+  int failed = 0;
+  for (int e = 0; e < E; ++e) {
+    const int code = map_status(st[size_t(e)]);
+    if (status_out) status_out[e] = code;
+    if (code != REFEFF_FMS_OK) ++failed;
+    refeff_complex128* outp = scattering_out + size_t(e) * tab;
+    for (int c = 0; c < p.m; ++c)
+      for (int r = 0; r < p.m; ++r) {
+        const double2 v = gg[size_t(e) * p.m * p.m + size_t(r) + size_t(p.m) * c];
+        outp[size_t(r) + C * (size_t(c) + C * size_t(p.abs_pot))] = {v.x, v.y};
+      }
+  }
+  if (report) {
+    report->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    report->energies_failed = failed;
+    report->refinement_iterations = form == REFEFF_FMS_FORM_FP32_REFINED ? p.refine_iters : 0;
+    report->residual_max = 0.0;
+  }
+  if (failed) {
+    for (int e = 0; e < E; ++e)
+      if (map_status(st[size_t(e)]) != REFEFF_FMS_OK)
+        return fail(ctx, map_status(st[size_t(e)]), "failed to solve FMS energy section " + std::to_string(e + 1));
+  }
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_complex128* scattering, int nspu,
+                                     refeff_complex128* out) {
+  if (!plan || !scattering || !out || nspu < plan->nsp) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  const int ang = (plan->abs_lmax + 1) * (plan->abs_lmax + 1);
+  const int active = ang * plan->nsp, outc = ang * nspu;
+  const size_t C = size_t(plan->C);
+  for (int i = 0; i < outc * outc; ++i) out[i] = {0.0, 0.0};
+  for (int c = 0; c < active; ++c)
+    for (int r = 0; r < active; ++r)
+      out[size_t(r) + size_t(outc) * c] = scattering[size_t(r) + C * (size_t(c) + C * size_t(plan->abs_pot))];
+  return REFEFF_FMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dense batched solve
+// ---------------------------------------------------------------------------
+extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, int m, int batch,
+                                               const refeff_complex128* A, const refeff_complex128* B,
+                                               refeff_complex128* X, refeff_fms_form form, int32_t* status_out,
+                                               int32_t* pivot_out) {
+  if (!ctx || n <= 0 || m <= 0 || m > 64 || batch <= 0 || !A || !B || !X) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
+  ctx->last_error.clear();
+  RF_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
+  Workspace ws;
+  int rc = ensure_workspace(ctx, ws, n, m, batch, fp32);
+  if (rc) return rc;
+  const BatchLayout& lay = ws.lay;
+  RF_CUDA(ctx, cudaMemsetAsync(ws.M64.p, 0, size_t(batch) * lay.stride * sizeof(double2), s));
+  for (int b = 0; b < batch; ++b) {
+    RF_CUDA(ctx, cudaMemcpy2DAsync(ws.M64.p + size_t(b) * lay.stride, size_t(lay.lda) * sizeof(double2),
+                                   A + size_t(b) * n * n, size_t(n) * sizeof(double2), size_t(n) * sizeof(double2), size_t(n),
+                                   cudaMemcpyHostToDevice, s));
+    RF_CUDA(ctx, cudaMemcpy2DAsync(ws.M64.p + size_t(b) * lay.stride + size_t(lay.lda) * n,
+                                   size_t(lay.lda) * sizeof(double2), B + size_t(b) * n * m, size_t(n) * sizeof(double2),
+                                   size_t(n) * sizeof(double2), size_t(m), cudaMemcpyHostToDevice, s));
+  }
+  RF_CUDA(ctx, cudaMemsetAsync(ws.status.p, 0, size_t(batch) * sizeof(int), s));
+  RF_CUDA(ctx, cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s));
+  if (!fp32) {
+    cudaError_t e = lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<double>");
+    lu_backward_rhs<double>(ws.pc64, lay, batch, ws.M64.p, nullptr, s);
+    RF_CUDA(ctx, ws.X64.alloc(size_t(batch) * lay.lda * m));
+    launch_copy_rhs64(lay, batch, ws.M64.p, ws.X64.p, s);
+  } else {
+    dim3 grid(64, unsigned(batch));
+    count_launch();
+    convert_to_f32_kernel<<<grid, 256, 0, s>>>(lay, ws.M64.p, ws.M32.p);
+    cudaError_t e = lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<float>");
+    // M32's RHS columns hold Y32; refinement uses the FP64 copy in M64
+    e = refine_fp32(ws, batch, 6, 1.0e-14, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "refine");
+    count_launch();
+    status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
+  }
+  RF_CUDA(ctx, cudaGetLastError());
+  for (int b = 0; b < batch; ++b)
+    RF_CUDA(ctx, cudaMemcpy2DAsync(X + size_t(b) * n * m, size_t(n) * sizeof(double2), ws.X64.p + size_t(b) * lay.lda * m,
+                                   size_t(lay.lda) * sizeof(double2), size_t(n) * sizeof(double2), size_t(m),
+                                   cudaMemcpyDeviceToHost, s));
+  std::vector<int> st(static_cast<size_t>(batch)), info(static_cast<size_t>(batch));
+  RF_CUDA(ctx, cudaMemcpyAsync(st.data(), ws.status.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(ctx, cudaMemcpyAsync(info.data(), ws.info.p, info.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(ctx, cudaStreamSynchronize(s));
+  int first_bad = REFEFF_FMS_OK;
+  for (int b = 0; b < batch; ++b) {
+    const int code = map_status(st[size_t(b)]);
+    if (status_out) status_out[b] = code;
+    if (pivot_out) pivot_out[b] = info[size_t(b)];
+    if (code != REFEFF_FMS_OK && first_bad == REFEFF_FMS_OK) first_bad = code;
+  }
+  if (first_bad != REFEFF_FMS_OK) return fail(ctx, first_bad, "batched solve: at least one system failed");
+  return REFEFF_FMS_OK;
+}

@@ -1,0 +1,71 @@
+// Device-side plan of one FMS cluster (energy independent) and the launch
+// entry points of the FMS kernels.
+//
+// Device state order: atoms are stored with the absorber (reference atom 0)
+// moved to the END, so its states are the last m rows/columns of every
+// system matrix.  Within an atom the reference order is kept
+// (l = 0..lmax, m = -l..l, spin innermost; crates/refeff-core/src/state.rs:97-148).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+
+namespace rfx {
+
+constexpr int kMaxL = 6;          // largest global lmax the kernels accept
+constexpr int kBuildRowAtoms = 16;  // row atoms per build CTA
+
+struct PlanDev {
+  int N = 0;        // atoms
+  int L = 0;        // global lmax
+  int nsp = 1;      // spin channels
+  int ispin = 0;    // spin selector (global.inp ispin)
+  int npot = 0;     // potentials
+  int n = 0;        // states
+  int m = 0;        // absorber block width (states of the absorber atom)
+  int ds = 0;       // small-d doubles per ordered pair (forward + backward)
+  const float* pos = nullptr;        // [N][3] device order
+  const int* atom_pot = nullptr;     // [N]
+  const int* atom_off = nullptr;     // [N+1] first state of each atom (device order)
+  const int* atom_lmax = nullptr;    // [N] per-atom l cutoff
+  const double* sigsqr = nullptr;    // [N*N] (a2 + N*a1), device order
+  double* pair_dist = nullptr;       // [N*N] (j + N*i), |R_i - R_j|        (written by launch_plan_geometry)
+  double* pair_phi = nullptr;        // [N*N] azimuth of R_i - R_j           (written by launch_plan_geometry)
+  double* pair_dsmall = nullptr;     // [N*N][ds] Wigner small-d tables      (written by launch_plan_geometry)
+  const double* xnlm = nullptr;      // [(L+1)*(L+1)] xnlm(mu, l) at mu + (L+1)*l
+  const double* t3p = nullptr;       // spin-orbit coefficients [l + (L+1)*((m+L) + (2L+1)*(s-1))]
+  const double* t3m = nullptr;
+  double rdirec2 = 0.0;              // direct-cutoff radius squared (Angstrom^2)
+};
+
+// Per-batch matrix layout: [A | B] with A n x n and B n x m (column-major,
+// leading dimension lda, matrix stride `stride` elements).
+struct BatchLayout {
+  int n = 0, m = 0, lda = 0;
+  size_t stride = 0;
+};
+
+// status codes written by kernels (per matrix)
+enum DevStatus : int {
+  kDevOk = 0,
+  kDevSingular = 1,      // exact zero pivot (info = 1 + pivot index in the aux word)
+  kDevNonfinite = 2,     // non-finite wave number / phase / rho
+  kDevZeroRho = 3,
+  kDevNotConverged = 4,
+  kDevTimeout = 5,
+};
+
+// Every kernel launch of the library calls this first; the total (including
+// launches replayed inside CUDA graphs) is reported by refeff_fms_kernel_launches.
+void count_launch();
+
+// ---- geometry (once per plan) ----
+void launch_plan_geometry(const PlanDev& P, cudaStream_t s);
+
+// ---- system build (per energy batch) ----
+// k: [E][nsp] double2; xphase: [E][nsp*(2L+1)*npot] double2 (column-major (nsp, 2L+1, npot)).
+// Writes A (= I - G0 T) and B (= G0[:, absorber]) into M64 (and a float copy into M32 if non-null).
+void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
+                         double2* M64, float2* M32, int* status, cudaStream_t s);
+
+}  // namespace rfx

@@ -1,0 +1,417 @@
+// FMS system assembly on the GPU: pair geometry (once per cluster) and the
+// fused G0 / T / (I - G0 T) build (once per energy batch).
+//
+// Reference arithmetic followed here:
+//   getang            crates/refeff-core/src/fms/cluster.rs:201-241
+//   rotxan small-d    crates/refeff-core/src/fms/internals/rotation.rs:3-125
+//   xclmz polynomials crates/refeff-core/src/fms/polynomial.rs:8-83
+//   xgllm             crates/refeff-core/src/fms/xgllm.rs:9-57
+//   G0 element        crates/refeff-core/src/fms/pairs.rs:242-323, 413-460
+//   prefactor         crates/refeff-core/src/fms/internals/geometry.rs:14-28
+//   T table           crates/refeff-core/src/fms/t_matrix.rs:10-190
+//   A = I - G0 T      crates/refeff-core/src/fms/internals/linear.rs:102-135
+// All of it is evaluated in FP64.  Rotation tables depend only on geometry,
+// so they are computed once per plan and stay resident in HBM; the Hankel
+// polynomial and the propagator prefactor depend on the energy and are
+// recomputed per (pair, energy) inside the build kernel, next to the store.
+#include "cplx.cuh"
+#include "fms_plan.cuh"
+
+namespace rfx {
+
+__host__ __device__ constexpr int dsmall_per_dir(int L) { return (L + 1) * (2 * L + 1) * (2 * L + 3) / 3; }
+__device__ __forceinline__ int lblock_offset(int l) { return l * (2 * l - 1) * (2 * l + 1) / 3; }
+
+// ---------------------------------------------------------------------------
+// Pair geometry: one thread per ordered pair (i, j), i != j, device order.
+// The small-d recursion keeps two levels in registers/local memory.
+// ---------------------------------------------------------------------------
+template <int L>
+__device__ void rotxan_small_d(double beta, double* out /* dsmall_per_dir(L) */) {
+  constexpr int D0 = 2 * L + 3;  // indices 1..2L+1 used
+  double bufa[D0 * D0], bufb[D0 * D0];
+  double* prev = bufa;
+  double* cur = bufb;
+  auto at = [](double* b, int n, int m) -> double& { return b[n + D0 * m]; };
+  const int ndm = 2 * L + 1;  // lxp1 + mxp1 - 1 with mmax = lmax
+  const double xc = cos(beta / 2.0), xs = sin(beta / 2.0), s = sin(beta);
+  // level il = 1
+  for (int q = 0; q < D0 * D0; ++q) cur[q] = 0.0;
+  at(cur, 1, 1) = 1.0;
+  out[0] = 1.0;
+  if (L >= 1) {
+    double* t = prev; prev = cur; cur = t;
+    for (int q = 0; q < D0 * D0; ++q) cur[q] = 0.0;
+    at(cur, 1, 1) = xc * xc;
+    at(cur, 1, 2) = s / sqrt(2.0);
+    at(cur, 1, 3) = xs * xs;
+    at(cur, 2, 1) = -at(cur, 1, 2);
+    at(cur, 2, 2) = cos(beta);
+    at(cur, 2, 3) = at(cur, 1, 2);
+    at(cur, 3, 1) = at(cur, 1, 3);
+    at(cur, 3, 2) = -at(cur, 2, 3);
+    at(cur, 3, 3) = at(cur, 1, 1);
+    // drix(m2, m1, l=1) = dri0(2, m1+2, m2+2) stored at [(m2+1)*3 + (m1+1)]
+    for (int m2 = -1; m2 <= 1; ++m2)
+      for (int m1 = -1; m1 <= 1; ++m1) out[1 + (m2 + 1) * 3 + (m1 + 1)] = at(cur, m1 + 2, m2 + 2);
+  }
+  for (int l = 3; l <= L + 1; ++l) {
+    double* t = prev; prev = cur; cur = t;
+    for (int q = 0; q < D0 * D0; ++q) cur[q] = 0.0;
+    int ln = min(2 * l - 1, ndm), lm = min(2 * l - 3, ndm);
+    for (int n = 1; n <= ln; ++n) {
+      for (int m = 1; m <= lm; ++m) {
+        double t1 = double((2 * l - 1 - n) * (2 * l - 2 - n));
+        double tt = double((2 * l - 1 - m) * (2 * l - 2 - m));
+        double f1 = sqrt(t1 / tt);
+        double f2 = sqrt(double((2 * l - 1 - n) * (n - 1)) / tt);
+        double f3 = sqrt(double((n - 2) * (n - 1)) / tt);
+        double dlnm = f1 * xc * xc * at(prev, n, m);
+        if (n > 1) dlnm -= f2 * s * at(prev, n - 1, m);
+        if (n > 2) dlnm += f3 * xs * xs * at(prev, n - 2, m);
+        at(cur, n, m) = dlnm;
+        if (n > 2 * l - 3) at(cur, m, n) = (((n - m) & 1) == 0 ? 1.0 : -1.0) * dlnm;
+      }
+      if (n > 2 * l - 3) {
+        at(cur, 2 * l - 2, 2 * l - 2) = at(cur, 2, 2);
+        at(cur, 2 * l - 1, 2 * l - 2) = -at(cur, 1, 2);
+        at(cur, 2 * l - 2, 2 * l - 1) = -at(cur, 2, 1);
+        at(cur, 2 * l - 1, 2 * l - 1) = at(cur, 1, 1);
+      }
+    }
+    const int lo = l - 1;  // angular momentum of this level
+    const int w = 2 * lo + 1;
+    double* o = out + lblock_offset(lo);
+    for (int m2 = -lo; m2 <= lo; ++m2)
+      for (int m1 = -lo; m1 <= lo; ++m1) o[(m2 + lo) * w + (m1 + lo)] = at(cur, m1 + l, m2 + l);
+  }
+}
+
+template <int L>
+__global__ void plan_geometry_kernel(PlanDev P) {
+  const int N = P.N;
+  const int64_t idx = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= int64_t(N) * N) return;
+  const int j = int(idx % N), i = int(idx / N);  // pair (row atom i, column atom j) stored at j + N*i
+  const float* pi = P.pos + 3 * i;
+  const float* pj = P.pos + 3 * j;
+  double x = double(pi[0]) - double(pj[0]);
+  double y = double(pi[1]) - double(pj[1]);
+  double z = double(pi[2]) - double(pj[2]);
+  double r = sqrt(x * x + y * y + z * z);
+  double* dsm = P.pair_dsmall + size_t(idx) * P.ds;
+  P.pair_dist[idx] = r;
+  if (i == j) {
+    P.pair_phi[idx] = 0.0;
+    for (int q = 0; q < P.ds; ++q) dsm[q] = 0.0;
+    return;
+  }
+  // getang with FEFF's single-precision threshold
+  const double tiny = double(1.0e-7f);
+  const double half_pi = 1.57079632679489661923;
+  double phi;
+  if (fabs(x) < tiny) phi = fabs(y) < tiny ? 0.0 : (y > tiny ? half_pi : -half_pi);
+  else phi = atan2(y, x);
+  double theta;
+  if (r <= tiny) theta = 0.0;
+  else if (z <= -r) theta = 3.14159265358979323846;
+  else if (z < r) theta = acos(z / r);
+  else theta = 0.0;
+  P.pair_phi[idx] = phi;
+  rotxan_small_d<L>(theta, dsm);                        // forward, beta
+  rotxan_small_d<L>(-theta, dsm + dsmall_per_dir(L));   // backward, -beta
+}
+
+void launch_plan_geometry(const PlanDev& P, cudaStream_t s) {
+  const int64_t pairs = int64_t(P.N) * P.N;
+  const int threads = 64;
+  const unsigned blocks = unsigned((pairs + threads - 1) / threads);
+  switch (P.L) {
+    case 0: count_launch(); plan_geometry_kernel<0><<<blocks, threads, 0, s>>>(P); break;
+    case 1: count_launch(); plan_geometry_kernel<1><<<blocks, threads, 0, s>>>(P); break;
+    case 2: count_launch(); plan_geometry_kernel<2><<<blocks, threads, 0, s>>>(P); break;
+    case 3: count_launch(); plan_geometry_kernel<3><<<blocks, threads, 0, s>>>(P); break;
+    case 4: count_launch(); plan_geometry_kernel<4><<<blocks, threads, 0, s>>>(P); break;
+    case 5: count_launch(); plan_geometry_kernel<5><<<blocks, threads, 0, s>>>(P); break;
+    case 6: count_launch(); plan_geometry_kernel<6><<<blocks, threads, 0, s>>>(P); break;
+    default: break;  // rejected on the host
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Build kernel: CTA = (column atom j, chunk of kBuildRowAtoms row atoms, energy).
+// ---------------------------------------------------------------------------
+struct BuildSmem {
+  // offsets in doubles from the dynamic smem base
+  int tcol0, tcol1, colinfo, rowinfo, pref, eph, g, dsm, clm, flag;
+  int total_bytes;
+};
+
+__host__ __device__ inline BuildSmem build_smem_layout(int L, int nsp, int ds) {
+  BuildSmem b{};
+  const int L1 = L + 1;
+  const int ncol_max = nsp * L1 * L1;
+  const int RA = kBuildRowAtoms;
+  int o = 0;
+  b.tcol0 = o; o += 2 * ncol_max;
+  b.tcol1 = o; o += 2 * ncol_max;
+  b.colinfo = o; o += 2 * ncol_max;            // int4 per column (as 2 doubles)
+  b.rowinfo = o; o += 2 * RA * ncol_max;       // int4 per row
+  b.pref = o; o += 2 * RA * nsp;
+  b.eph = o; o += 2 * RA * (4 * L + 1);
+  b.g = o; o += 2 * RA * nsp * L1 * L1 * L1;
+  b.dsm = o; o += RA * ds;
+  b.clm = o; o += 2 * RA * nsp * (L + 2) * L1;
+  b.flag = o; o += RA;                          // one int per pair (stored in a double slot)
+  b.total_bytes = o * int(sizeof(double));
+  return b;
+}
+
+__device__ __forceinline__ double2 t_phase(double2 d) {
+  // (exp(2 i d) - 1) / (2 i), crates/refeff-core/src/fms/internals/t_matrix.rs:38-41
+  double2 e = cexp(make_double2(-2.0 * d.y, 2.0 * d.x));
+  double2 num = make_double2(e.x - 1.0, e.y);
+  return make_double2(num.y / 2.0, -num.x / 2.0);
+}
+
+__device__ __forceinline__ double so_coef(const PlanDev& P, const double* tab, int l, int m, int s) {
+  return tab[l + (P.L + 1) * ((m + P.L) + (2 * P.L + 1) * (s - 1))];
+}
+
+template <bool kMirror32>
+__global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const double2* __restrict__ kE,
+                                                           const double2* __restrict__ xph, BatchLayout lay,
+                                                           double2* __restrict__ M64, float2* __restrict__ M32,
+                                                           int* __restrict__ status) {
+  extern __shared__ double sm[];
+  const int L = P.L, L1 = L + 1, nsp = P.nsp, N = P.N;
+  const int j = blockIdx.x;
+  const int i0 = blockIdx.y * kBuildRowAtoms;
+  const int e = blockIdx.z;
+  const int i1 = min(i0 + kBuildRowAtoms, N);
+  const int RA = i1 - i0;
+  const int cj0 = P.atom_off[j], ncol = P.atom_off[j + 1] - cj0;
+  const int r0 = P.atom_off[i0], nrow = P.atom_off[i1] - r0;
+  const BuildSmem lay_s = build_smem_layout(L, nsp, P.ds);
+  double2* tcol0 = reinterpret_cast<double2*>(sm + lay_s.tcol0);
+  double2* tcol1 = reinterpret_cast<double2*>(sm + lay_s.tcol1);
+  int4* colinfo = reinterpret_cast<int4*>(sm + lay_s.colinfo);
+  int4* rowinfo = reinterpret_cast<int4*>(sm + lay_s.rowinfo);
+  double2* pref = reinterpret_cast<double2*>(sm + lay_s.pref);
+  double2* eph = reinterpret_cast<double2*>(sm + lay_s.eph);
+  double2* gtab = reinterpret_cast<double2*>(sm + lay_s.g);
+  double* dsm = sm + lay_s.dsm;
+  double2* clm = reinterpret_cast<double2*>(sm + lay_s.clm);
+  int* flag = reinterpret_cast<int*>(sm + lay_s.flag);
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int D = 2 * L + 1;
+  const double2* xe = xph + size_t(e) * size_t(nsp) * D * P.npot;
+  const double2* ke = kE + size_t(e) * nsp;
+  const int potj = P.atom_pot[j];
+  auto phase = [&](int s, int l) { return xe[(s - 1) + nsp * ((l + L) + D * potj)]; };
+
+  // ---- columns of atom j: state decode and compact T (t_matrix.rs:149-190) ----
+  for (int q = tid; q < ncol; q += nthr) {
+    const int s = q % nsp + 1, lm = q / nsp;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) ++l;
+    const int m = lm - l * l - l;
+    int partner = -1, mp = 0, sp = 0;
+    if (nsp == 2) {
+      if (s == 1 && m > -l) { partner = q - 1; mp = m - 1; sp = 2; }
+      if (s == 2 && m < l) { partner = q + 1; mp = m + 1; sp = 1; }
+    }
+    colinfo[q] = make_int4(l, m, s, partner);
+    double2 t0, t1 = make_double2(0.0, 0.0);
+    const double2 dm = phase(s, l);
+    if (!cfinite(dm) || !cfinite(phase(s, -l))) atomicMax(status + e, int(kDevNonfinite));
+    if (nsp == 1 && P.ispin == 0) {
+      t0 = t_phase(dm);
+    } else {
+      const int cs = nsp == 1 ? (P.ispin > 0 ? 2 : 1) : s;
+      const double mi = so_coef(P, P.t3m, l, m, cs), pl = so_coef(P, P.t3p, l, m, cs);
+      const double2 a = t_phase(dm), b = t_phase(phase(s, -l));
+      t0 = make_double2(a.x * (mi * mi) + b.x * (pl * pl), a.y * (mi * mi) + b.y * (pl * pl));
+      if (partner >= 0) {
+        const double mf = so_coef(P, P.t3m, l, m, s), ms = so_coef(P, P.t3m, l, mp, sp);
+        const double pf = so_coef(P, P.t3p, l, m, s), ps = so_coef(P, P.t3p, l, mp, sp);
+        const double2 a2 = t_phase(phase(sp, l)), b2 = t_phase(phase(sp, -l));
+        const double2 mph = make_double2((a.x + a2.x) * 0.5, (a.y + a2.y) * 0.5);
+        const double2 pph = make_double2((b.x + b2.x) * 0.5, (b.y + b2.y) * 0.5);
+        t1 = make_double2(mph.x * mf * ms + pph.x * pf * ps, mph.y * mf * ms + pph.y * pf * ps);
+      }
+    }
+    tcol0[q] = t0;
+    tcol1[q] = t1;
+  }
+  // ---- rows of the chunk ----
+  for (int rr = tid; rr < nrow; rr += nthr) {
+    const int r = r0 + rr;
+    int p = 0;
+    while (P.atom_off[i0 + p + 1] <= r) ++p;
+    const int q = r - P.atom_off[i0 + p];
+    const int s = q % nsp + 1, lm = q / nsp;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) ++l;
+    rowinfo[rr] = make_int4(p, l, lm - l * l - l, s);
+  }
+  // ---- per pair: small-d tables (resident, from the plan) ----
+  for (int t = tid; t < RA * P.ds; t += nthr) {
+    const int p = t / P.ds, q = t % P.ds;
+    dsm[t] = P.pair_dsmall[(size_t(j) + size_t(N) * (i0 + p)) * P.ds + q];
+  }
+  // ---- per pair: azimuth phases e^{i m (phi - pi)}, m in [-2L, 2L] ----
+  for (int t = tid; t < RA * (4 * L + 1); t += nthr) {
+    const int p = t / (4 * L + 1), mm = t % (4 * L + 1) - 2 * L;
+    const double ang = double(mm) * (P.pair_phi[size_t(j) + size_t(N) * (i0 + p)] - 3.14159265358979323846);
+    double sn, cs;
+    sincos(ang, &sn, &cs);
+    eph[t] = make_double2(cs, sn);
+  }
+  // ---- per (pair, spin): rho, prefactor, Hankel polynomial table ----
+  const int rows = L + 2;
+  for (int t = tid; t < RA * nsp; t += nthr) {
+    const int p = t / nsp, s = t % nsp;
+    const int i = i0 + p;
+    const size_t pij = size_t(j) + size_t(N) * i;
+    const double dist = P.pair_dist[pij];
+    int ok = (i != j) && (dist * dist <= P.rdirec2);
+    const double2 k = ke[s];
+    if (!cfinite(k)) { atomicMax(status + e, int(kDevNonfinite)); ok = 0; }
+    double2* c = clm + size_t(t) * rows * L1;
+    if (ok) {
+      const double2 rho = make_double2(k.x * dist, k.y * dist);
+      if (rho.x == 0.0 && rho.y == 0.0) { atomicMax(status + e, int(kDevZeroRho)); ok = 0; }
+      else {
+        const double msd = P.sigsqr[size_t(j) + size_t(N) * i];
+        // e^{i rho} / rho * e^{-msd k^2}
+        const double2 ph = cdiv(cexp(make_double2(-rho.y, rho.x)), rho);
+        const double2 k2 = cmul(k, k);
+        const double2 damp = cexp(make_double2(-msd * k2.x, -msd * k2.y));
+        pref[t] = cmul(ph, damp);
+        // xclmz recursion, clm(il, im) at c[il + rows*im]
+        const double2 z = cdiv(make_double2(0.0, -1.0), rho);
+        const double2 one = make_double2(1.0, 0.0);
+        for (int q = 0; q < rows * L1; ++q) c[q] = make_double2(0.0, 0.0);
+        c[0] = one;
+        if (L >= 1) c[1] = csub(one, z);
+        for (int il = 2; il <= L; ++il) {
+          const double2 f = cscale(z, double(2 * il - 1));
+          c[il] = csub(c[il - 2], cmul(f, c[il - 1]));
+        }
+        double2 cmm = one;
+        for (int im = 2; im <= L1; ++im) {
+          const int mmm = im - 1;
+          cmm = cmul(cneg(cmm), cscale(z, double(2 * mmm - 1)));
+          c[(im - 1) + rows * (im - 1)] = cmm;
+          const double2 oz = csub(one, cscale(z, double(im)));
+          c[im + rows * (im - 1)] = cmul(cscale(cmm, double(2 * im - 1)), oz);
+          for (int il = im + 1; il <= L; ++il) {
+            const double2 f = cscale(z, double(2 * il - 1));
+            c[il + rows * (im - 1)] =
+                csub(c[(il - 2) + rows * (im - 1)], cmul(f, cadd(c[(il - 1) + rows * (im - 1)], c[(il - 1) + rows * (im - 2)])));
+          }
+        }
+      }
+    }
+    if (s == 0) flag[p] = ok;
+  }
+  __syncthreads();
+  // ---- z-axis propagator g(l1, l2, mu) per (pair, spin) (xgllm) ----
+  const int gsz = L1 * L1 * L1;
+  for (int t = tid; t < RA * nsp * gsz; t += nthr) {
+    const int ps = t / gsz, rem = t % gsz;
+    const int p = ps / nsp;
+    const int l1 = rem % L1, l2 = (rem / L1) % L1, mu = rem / (L1 * L1);
+    double2 g = make_double2(0.0, 0.0);
+    if (flag[p] && mu <= l1 && mu <= l2) {
+      const double2* c = clm + size_t(ps) * rows * L1;
+      const double n1 = P.xnlm[mu + L1 * l1], n2 = P.xnlm[mu + L1 * l2];
+      const double w = double(2 * l1 + 1);
+      const double sgn = (mu & 1) ? -1.0 : 1.0;
+      const int numax = min(l1, l2 - mu);
+      for (int nu = 0; nu <= numax; ++nu) {
+        const double2 cl1 = c[l1 + rows * nu];
+        const double2 cl2 = c[l2 + rows * (mu + nu)];
+        const double2 gamtl = make_double2(w * cl1.x / n1, w * cl1.y / n1);
+        const double2 gam = make_double2(cl2.x * (sgn * n2), cl2.y * (sgn * n2));
+        g = cadd(g, cmul(gamtl, gam));
+      }
+    }
+    gtab[t] = g;
+  }
+  __syncthreads();
+
+  // ---- elements: rows fastest (coalesced column-major stores) ----
+  const int dpd = P.ds / 2;
+  const bool absorber_col = (j == N - 1);
+  const size_t base = size_t(e) * lay.stride;
+  auto g0 = [&](int p, int l1, int m1, int s1, int l2, int m2, int s2) -> double2 {
+    if (s1 != s2 || !flag[p]) return make_double2(0.0, 0.0);
+    const double* tf = dsm + size_t(p) * P.ds + lblock_offset(l2);          // forward (beta), l2 block
+    const double* tb = dsm + size_t(p) * P.ds + dpd + lblock_offset(l1);    // backward (-beta), l1 block
+    const double2* gg = gtab + size_t(p * nsp + (s1 - 1)) * gsz;
+    const int w1 = 2 * l1 + 1, w2 = 2 * l2 + 1;
+    double sx = 0.0, sy = 0.0;
+    for (int mu = -l1; mu <= l1; ++mu) {
+      const int amu = mu < 0 ? -mu : mu;
+      if (amu > l2) continue;
+      const double dd = tb[(mu + l1) * w1 + (m1 + l1)] * tf[(m2 + l2) * w2 + (mu + l2)];
+      const double2 gv = gg[l1 + L1 * (l2 + L1 * amu)];
+      sx = fma(dd, gv.x, sx);
+      sy = fma(dd, gv.y, sy);
+    }
+    const double2 ph = eph[p * (4 * L + 1) + (m2 - m1 + 2 * L)];
+    return cmul(pref[p * nsp + (s1 - 1)], cmul(ph, make_double2(sx, sy)));
+  };
+  const int total = nrow * ncol;
+  for (int idx = tid; idx < total; idx += nthr) {
+    const int rr = idx % nrow, cc = idx / nrow;
+    const int4 ri = rowinfo[rr];
+    const int4 ci = colinfo[cc];
+    const int r = r0 + rr, c = cj0 + cc;
+    double2 a = make_double2(0.0, 0.0), gcol = make_double2(0.0, 0.0);
+    if (i0 + ri.x != j) {
+      gcol = g0(ri.x, ri.y, ri.z, ri.w, ci.x, ci.y, ci.z);
+      a = cneg(cmul(gcol, tcol0[cc]));
+      if (ci.w >= 0) {
+        const int4 pi = colinfo[ci.w];
+        const double2 gp = g0(ri.x, ri.y, ri.z, ri.w, pi.x, pi.y, pi.z);
+        a = csub(a, cmul(gp, tcol1[cc]));
+      }
+    }
+    if (r == c) a.x += 1.0;
+    M64[base + size_t(r) + size_t(lay.lda) * c] = a;
+    if (kMirror32) M32[base + size_t(r) + size_t(lay.lda) * c] = make_float2(float(a.x), float(a.y));
+    if (absorber_col) {
+      const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + cc);
+      M64[bi] = gcol;
+      if (kMirror32) M32[bi] = make_float2(float(gcol.x), float(gcol.y));
+    }
+  }
+}
+
+void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
+                         double2* M64, float2* M32, int* status, cudaStream_t s) {
+  const BuildSmem b = build_smem_layout(P.L, P.nsp, P.ds);
+  dim3 grid(unsigned(P.N), unsigned((P.N + kBuildRowAtoms - 1) / kBuildRowAtoms), unsigned(E));
+  // raised once to the largest request (before any stream capture)
+  static int smem_true = 0, smem_false = 0;
+  if (M32) {
+    if (b.total_bytes > smem_true) {
+      cudaFuncSetAttribute(build_system_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
+      smem_true = b.total_bytes;
+    }
+    count_launch();
+    build_system_kernel<true><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, M32, status);
+  } else {
+    if (b.total_bytes > smem_false) {
+      cudaFuncSetAttribute(build_system_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
+      smem_false = b.total_bytes;
+    }
+    count_launch();
+    build_system_kernel<false><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, nullptr, status);
+  }
+}
+
+}  // namespace rfx

@@ -1,0 +1,304 @@
+"""Python mirror of refeff's real-space FMS interface, bound to the C ABI of
+include/refeff_fms.h (librefeff_fms.so, built for sm_103a).
+
+Names follow the reference:
+  fms_yprep_cluster        crates/refeff-core/src/fms/cluster.rs:10-195 (with sortat)
+  fms_real_space_plan      crates/refeff-core/src/fms/driver.rs:105-140
+  fms_real_space_spectrum  crates/refeff-core/src/fms/driver.rs:231-239
+  complex_lu_solve_batched crates/refeff-linalg/src/lu.rs:385-490 (faer c32 LU factor + solve)
+Errors raise FmsError carrying the library status code (the reference
+returns Result<_, FmsError>).  There is no CPU fallback: if the CUDA library
+cannot be loaded, or no GPU is present, the calls fail.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+FORM_FP64_LU = 0
+FORM_FP32_REFINED = 1
+
+STATUS_NAMES = {
+    0: "OK", 1: "InvalidArgument", 2: "EmptyCluster", 3: "PotentialOutOfRange", 4: "MissingRepresentativePotential",
+    5: "InvalidAngularLimit", 6: "NonFiniteInput", 7: "NonFiniteCoordinate", 8: "ZeroRho", 9: "SingularMatrix",
+    10: "NotConverged", 11: "DuplicateAbsorber", 12: "MissingCentralAtom", 13: "Unsupported", 14: "Cuda",
+    15: "OutOfMemory", 16: "InvalidTolerance", 17: "InvalidClusterRadius",
+}
+
+
+class FmsError(RuntimeError):
+    def __init__(self, code: int, message: str = ""):
+        name = STATUS_NAMES.get(code, f"status {code}")
+        super().__init__(f"{name}: {message}" if message else name)
+        self.code = code
+        self.name = name
+
+
+_lib = None
+_p = C.c_void_p
+_i = C.c_int
+
+
+class _PlanInput(C.Structure):
+    _fields_ = [
+        ("n_atoms", C.c_int), ("positions_xyz", _p), ("potentials", _p), ("spin_channels", C.c_int),
+        ("spin_selector", C.c_int), ("lfms", C.c_int), ("minv", C.c_int), ("max_potential", C.c_int),
+        ("global_lmax", C.c_int), ("raw_potential_lmax", _p), ("direct_cutoff", C.c_float),
+        ("mean_square_displacements", _p), ("sig2g", C.c_float), ("convergence_tolerance", C.c_float),
+        ("zero_tolerance", C.c_float),
+    ]
+
+
+class _EnergyPoints(C.Structure):
+    _fields_ = [("n_energies", C.c_int), ("wave_numbers", _p), ("phase_shifts", _p)]
+
+
+class _Report(C.Structure):
+    _fields_ = [("seconds", C.c_double), ("refinement_iterations", C.c_int), ("residual_max", C.c_double),
+                ("energies_failed", C.c_int)]
+
+
+def header_functions() -> list[str]:
+    """Names of every function declared in include/refeff_fms.h."""
+    text = (Path(__file__).resolve().parents[1] / "include" / "refeff_fms.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w ]*?[\s\*]+(refeff_\w+)\s*\(", text, flags=re.M)
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load librefeff_fms.so (building it with nvcc if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not path.exists():
+        if not build_if_missing:
+            raise FmsError(14, f"{path} is not built")
+        _build.build()
+    lib = C.CDLL(str(path))
+    sig = {
+        "refeff_fms_abi_version": ([], _i),
+        "refeff_fms_kernel_launches": ([], C.c_ulonglong),
+        "refeff_fms_context_create": ([_i, _p], _i),
+        "refeff_fms_context_destroy": ([_p], None),
+        "refeff_fms_last_error": ([_p], C.c_char_p),
+        "refeff_fms_yprep_cluster": ([_i, _i, _i, _p, _p, C.c_float, _i, _p, _p, _p], _i),
+        "refeff_fms_real_space_plan_create": ([_p, _p, _p], _i),
+        "refeff_fms_real_space_plan_destroy": ([_p], None),
+        "refeff_fms_plan_query": ([_p, _p, _p, _p, _p], _i),
+        "refeff_fms_plan_set_batch": ([_p, _i], _i),
+        "refeff_fms_plan_set_refinement": ([_p, _i, C.c_double], _i),
+        "refeff_fms_plan_set_profiling": ([_p, _i], _i),
+        "refeff_fms_plan_phase_times": ([_p, _p, _i], _i),
+        "refeff_fms_real_space_spectrum": ([_p, _p, _i, _p, _p, _p], _i),
+        "refeff_fms_real_space_spectrum_device": ([_p, _i, _p, _p, _i, _p, _p, _p], _i),
+        "refeff_fms_gg_section": ([_p, _p, _i, _p], _i),
+        "refeff_complex_lu_solve_batched": ([_p, _i, _i, _i, _p, _p, _p, _i, _p, _p], _i),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_p)
+
+
+def fms_yprep_cluster(positions, potentials, *, central_potential=0, max_potential=None, cluster_radius,
+                      cluster_capacity=None):
+    """FEFF yprep + sortat on the host library: absorber first, at the origin."""
+    lib = load()
+    pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+    pots = np.ascontiguousarray(potentials, dtype=np.int32)
+    n = len(pots)
+    maxp = int(pots.max()) if max_potential is None else int(max_potential)
+    cap = n if cluster_capacity is None else int(cluster_capacity)
+    out_pos = np.zeros_like(pos)
+    out_pot = np.zeros_like(pots)
+    cnt = np.zeros(1, np.int32)
+    rc = lib.refeff_fms_yprep_cluster(int(central_potential), maxp, n, _ptr(pots), _ptr(pos), float(cluster_radius),
+                                      cap, _ptr(out_pos), _ptr(out_pot), _ptr(cnt))
+    if rc:
+        raise FmsError(rc)
+    return out_pos[: cnt[0]].copy(), out_pot[: cnt[0]].copy()
+
+
+class Context:
+    """One CUDA device, one stream (refeff_fms_context)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = _p()
+        rc = self._lib.refeff_fms_context_create(int(device), C.byref(h))
+        if rc:
+            raise FmsError(rc, "cannot create a CUDA context (no GPU?)")
+        self.handle = h
+
+    def last_error(self) -> str:
+        return self._lib.refeff_fms_last_error(self.handle).decode()
+
+    def check(self, rc: int):
+        if rc:
+            raise FmsError(rc, self.last_error())
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.refeff_fms_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class PlanShape:
+    n_states: int
+    channel_count: int
+    absorber_block: int
+    n_potentials: int
+
+
+class FmsRealSpacePlan:
+    """Energy-independent FMS plan resident on the GPU (FmsRealSpacePlan)."""
+
+    def __init__(self, ctx: Context, handle, inputs: dict):
+        self.ctx = ctx
+        self.handle = handle
+        self.inputs = inputs
+        n, c, m, npot = (C.c_int() for _ in range(4))
+        ctx.check(ctx._lib.refeff_fms_plan_query(handle, C.byref(n), C.byref(c), C.byref(m), C.byref(npot)))
+        self.shape = PlanShape(n.value, c.value, m.value, npot.value)
+
+    def set_batch(self, max_batch: int):
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_batch(self.handle, int(max_batch)))
+
+    def set_refinement(self, max_iterations: int, tolerance: float):
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_refinement(self.handle, int(max_iterations), float(tolerance)))
+
+    def set_profiling(self, enable: bool):
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_profiling(self.handle, 1 if enable else 0))
+
+    PHASES = ("build", "eliminate", "sweeps", "residual", "extract")
+
+    def phase_times(self) -> dict:
+        out = np.zeros(len(self.PHASES))
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_phase_times(self.handle, _ptr(out), len(out)))
+        return dict(zip(self.PHASES, out.tolist()))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx._lib.refeff_fms_real_space_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fms_real_space_plan(ctx: Context, positions, potentials, raw_potential_lmax, *, spin_channels=1, spin_selector=0,
+                        lfms=0, minv=0, global_lmax=None, direct_cutoff=1.0e6, mean_square_displacements=None,
+                        sig2g=0.0, convergence_tolerance=1.0e-3, zero_tolerance=0.0) -> FmsRealSpacePlan:
+    pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+    pots = np.ascontiguousarray(potentials, dtype=np.int32)
+    lmax = np.ascontiguousarray(raw_potential_lmax, dtype=np.int32)
+    L = int(lmax.max()) if global_lmax is None else int(global_lmax)
+    msd = None if mean_square_displacements is None else np.asfortranarray(mean_square_displacements, dtype=np.float32)
+    inp = _PlanInput(len(pots), _ptr(pos), _ptr(pots), int(spin_channels), int(spin_selector), int(lfms), int(minv),
+                     len(lmax) - 1, L, _ptr(lmax), float(direct_cutoff), _ptr(msd), float(sig2g),
+                     float(convergence_tolerance), float(zero_tolerance))
+    h = _p()
+    ctx.check(ctx._lib.refeff_fms_real_space_plan_create(ctx.handle, C.byref(inp), C.byref(h)))
+    return FmsRealSpacePlan(ctx, h, dict(positions=pos, potentials=pots, lmaxph=lmax, nsp=int(spin_channels),
+                                          L=L, npot=len(lmax)))
+
+
+def fms_real_space_spectrum(plan: FmsRealSpacePlan, wave_numbers, phase_shifts, form=FORM_FP64_LU,
+                            raise_on_error=True):
+    """Scattering tables (E, C, C, npot) complex128 and per-energy status codes.
+
+    wave_numbers: (E, nsp) complex; phase_shifts: (E, nsp, 2L+1, npot) complex (FEFF xphase per energy).
+    """
+    nsp, L, npot = plan.inputs["nsp"], plan.inputs["L"], plan.inputs["npot"]
+    k = np.ascontiguousarray(np.asarray(wave_numbers, dtype=np.complex128).reshape(-1, nsp))
+    E = k.shape[0]
+    ph = np.asarray(phase_shifts, dtype=np.complex128).reshape(E, nsp, 2 * L + 1, npot)
+    xp = np.ascontiguousarray(np.stack([ph[e].reshape(-1, order="F") for e in range(E)])) if E else \
+        np.zeros((0,), np.complex128)
+    Cc = plan.shape.channel_count
+    out = np.zeros(E * Cc * Cc * npot, dtype=np.complex128)
+    status = np.zeros(E, dtype=np.int32)
+    pts = _EnergyPoints(E, _ptr(k), _ptr(xp))
+    rep = _Report()
+    rc = plan.ctx._lib.refeff_fms_real_space_spectrum(plan.handle, C.byref(pts), int(form), _ptr(out), _ptr(status),
+                                                      C.byref(rep))
+    if rc and (raise_on_error or rc not in (9, 10, 6, 8)):
+        raise FmsError(rc, plan.ctx.last_error())
+    tabs = out.reshape(E, Cc * Cc * npot)
+    scat = np.stack([tabs[e].reshape((Cc, Cc, npot), order="F") for e in range(E)]) if E else \
+        np.zeros((0, Cc, Cc, npot), np.complex128)
+    return scat, status
+
+
+def fms_real_space_spectrum_device(plan: FmsRealSpacePlan, d_k: int, d_phase: int, n_energies: int, d_gg: int,
+                                   d_status: int, form=FORM_FP64_LU, stream: int = 0):
+    """Device-pointer variant (pointers as ints, e.g. torch tensor .data_ptr())."""
+    rc = plan.ctx._lib.refeff_fms_real_space_spectrum_device(plan.handle, int(n_energies), _p(d_k), _p(d_phase),
+                                                             int(form), _p(d_gg), _p(d_status),
+                                                             _p(stream) if stream else None)
+    if rc:
+        raise FmsError(rc, plan.ctx.last_error())
+
+
+def gg_section(plan: FmsRealSpacePlan, scattering_table, nspu: int | None = None):
+    nsp = plan.inputs["nsp"]
+    nspu = nsp if nspu is None else int(nspu)
+    tab = np.asfortranarray(scattering_table, dtype=np.complex128)
+    lmax0 = int(round((plan.shape.absorber_block // nsp) ** 0.5)) - 1
+    w = nspu * (lmax0 + 1) ** 2
+    out = np.zeros(w * w, dtype=np.complex128)
+    flat = np.ascontiguousarray(tab.reshape(-1, order="F"))
+    rc = plan.ctx._lib.refeff_fms_gg_section(plan.handle, _ptr(flat), nspu, _ptr(out))
+    if rc:
+        raise FmsError(rc)
+    return out.reshape((w, w), order="F")
+
+
+def complex_lu_solve_batched(ctx: Context, A, B, form=FORM_FP64_LU):
+    """Solve A[b] X[b] = B[b] for a batch (batch, n, n) / (batch, n, m) complex; returns X, status, pivot."""
+    A = np.asarray(A, dtype=np.complex128)
+    B = np.asarray(B, dtype=np.complex128)
+    if A.ndim == 2:
+        A = A[None]
+    if B.ndim == 2:
+        B = B[None]
+    batch, n, _ = A.shape
+    m = B.shape[2]
+    a = np.ascontiguousarray(np.stack([A[i].reshape(-1, order="F") for i in range(batch)]))
+    b = np.ascontiguousarray(np.stack([B[i].reshape(-1, order="F") for i in range(batch)]))
+    x = np.zeros_like(b)
+    st = np.zeros(batch, np.int32)
+    piv = np.zeros(batch, np.int32)
+    rc = ctx._lib.refeff_complex_lu_solve_batched(ctx.handle, n, m, batch, _ptr(a), _ptr(b), _ptr(x), int(form),
+                                                  _ptr(st), _ptr(piv))
+    X = np.stack([x[i].reshape((n, m), order="F") for i in range(batch)])
+    if rc and rc not in (9, 10):
+        raise FmsError(rc, ctx.last_error())
+    return X, st, piv

@@ -1,0 +1,222 @@
+"""GPU parity of the FMS path against the CPU oracle, through the C ABI.
+
+Tolerances (relative, Frobenius norm of the absorber block per energy):
+  plain FP64 LU           <= 1e-10 versus the FP64 oracle
+  FP32 LU + refinement    <= 1e-6  versus the FP64 oracle (the chosen-form gate)
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from refeff_gb300 import fms, workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-10
+TOL_CHOSEN = 1e-6
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return fms.Context(0)
+
+
+def rel_err(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def absorber_blocks(scat, m, abs_pot=0):
+    return scat[:, :m, :m, abs_pot]
+
+
+def run_pair(ctx, cl, grid, form, nsp=1, ispin=0, energies=None, **plan_kw):
+    sl = slice(None) if energies is None else energies
+    k = grid.wave_numbers[sl]
+    ph = grid.phase_shifts[sl]
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph, spin_channels=nsp,
+                                   spin_selector=ispin, **plan_kw)
+    gpu, status = fms.fms_real_space_spectrum(plan, k, ph, form)
+    ref = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, k, ph, nsp=nsp, ispin=ispin, mode=po.F64,
+                          threads=po.threads_available(), **{kk: v for kk, v in plan_kw.items()
+                                                            if kk in ("rdirec", "sig2g", "sigsqr")})
+    return plan, gpu, ref, status
+
+
+@pytest.mark.parametrize("n,m", [(5, 1), (33, 4), (100, 16), (300, 16)])
+def test_dense_lu_fp64_matches_numpy(ctx, n, m):
+    rng = np.random.default_rng(n)
+    A = rng.normal(size=(3, n, n)) + 1j * rng.normal(size=(3, n, n)) + 4 * np.sqrt(n) * np.eye(n)
+    B = rng.normal(size=(3, n, m)) + 1j * rng.normal(size=(3, n, m))
+    X, st, _ = fms.complex_lu_solve_batched(ctx, A, B, fms.FORM_FP64_LU)
+    assert (st == 0).all()
+    for b in range(3):
+        assert rel_err(X[b], np.linalg.solve(A[b], B[b])) < 1e-12
+
+
+def test_dense_lu_fp64_matches_oracle_pivoting(ctx):
+    """A matrix that needs row exchanges in every panel (small diagonal)."""
+    rng = np.random.default_rng(11)
+    n, m = 150, 3
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A[np.diag_indices(n)] *= 1e-3
+    B = rng.normal(size=(n, m)) + 0j
+    X, st, _ = fms.complex_lu_solve_batched(ctx, A, B, fms.FORM_FP64_LU)
+    _, Xo, _ = po.lu_factor_solve(A, B, po.F64)
+    assert st[0] == 0
+    assert rel_err(X[0], Xo) < 1e-10
+
+
+@pytest.mark.parametrize("n", [64, 257])
+def test_dense_lu_fp32_refined(ctx, n):
+    rng = np.random.default_rng(n + 1)
+    A = rng.normal(size=(2, n, n)) + 1j * rng.normal(size=(2, n, n)) + 3 * np.sqrt(n) * np.eye(n)
+    B = rng.normal(size=(2, n, 16)) + 1j * rng.normal(size=(2, n, 16))
+    X, st, _ = fms.complex_lu_solve_batched(ctx, A, B, fms.FORM_FP32_REFINED)
+    assert (st == 0).all()
+    for b in range(2):
+        assert rel_err(X[b], np.linalg.solve(A[b], B[b])) < 1e-11
+
+
+def test_dense_lu_singular_reports_pivot(ctx):
+    n = 40
+    rng = np.random.default_rng(5)
+    A = rng.normal(size=(n, n)) + 0j
+    A[:, 7] = 0.0  # exactly singular: a zero column
+    B = np.ones((n, 2), np.complex128)
+    X, st, piv = fms.complex_lu_solve_batched(ctx, A, B, fms.FORM_FP64_LU)
+    assert st[0] == 9  # SingularMatrix
+    assert piv[0] == 8  # 1-based first zero pivot
+    assert np.isfinite(X).all()
+
+
+def test_fms_small_cluster_fp64(ctx):
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=6)
+    plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP64_LU)
+    assert (status == 0).all()
+    m = plan.shape.absorber_block
+    assert np.abs(gpu[:, m:, :, :]).max() == 0 and np.abs(gpu[:, :, m:, :]).max() == 0
+    for e in range(gpu.shape[0]):
+        assert rel_err(gpu[e], ref[e]) < TOL_FP64, e
+
+
+def test_fms_small_cluster_fp32_refined(ctx):
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=6)
+    plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP32_REFINED)
+    assert (status == 0).all()
+    for e in range(gpu.shape[0]):
+        assert rel_err(gpu[e], ref[e]) < TOL_CHOSEN, e
+
+
+def test_fms_config0_subset_both_forms(ctx):
+    """fcc Cu <= 4.5 A (43 atoms, n = 688): 8 energies across the grid."""
+    cl, grid = wl.config0()
+    sel = np.linspace(0, 99, 8).astype(int)
+    plan, gpu64, ref, st64 = run_pair(ctx, cl, grid, fms.FORM_FP64_LU, energies=sel)
+    assert plan.shape.n_states == 688 and plan.shape.absorber_block == 16
+    gpu32, st32 = fms.fms_real_space_spectrum(plan, grid.wave_numbers[sel], grid.phase_shifts[sel],
+                                              fms.FORM_FP32_REFINED)
+    assert (st64 == 0).all() and (st32 == 0).all()
+    for e in range(len(sel)):
+        assert rel_err(gpu64[e], ref[e]) < TOL_FP64, e
+        assert rel_err(gpu32[e], ref[e]) < TOL_CHOSEN, e
+
+
+def test_fms_reference_precision_agreement(ctx):
+    """The reference computes in Complex32: the f32-faithful oracle sits within f32 error of the GPU FP64 path."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=4, seed=3)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    gpu, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    f32 = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts, mode=po.F32)
+    for e in range(gpu.shape[0]):
+        assert rel_err(gpu[e], f32[e]) < 1e-3
+
+
+def test_fms_spin_orbit_two_spins(ctx):
+    """nsp = 2 with distinct j = l -/+ 1/2 phase shifts: compact T with the spin-flip partner band."""
+    cl, grid = wl.small_cluster(2.6, lmax=2, n_energies=3, seed=9, nsp=2)
+    rng = np.random.default_rng(1)
+    ph = grid.phase_shifts.copy()
+    L = cl.global_lmax
+    ph[:, :, :L, :] *= 1.0 + 0.2 * rng.random(ph[:, :, :L, :].shape)  # -l slots differ from +l
+    ph[:, 1] *= 0.9
+    grid.phase_shifts = ph
+    plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP64_LU, nsp=2)
+    assert (status == 0).all()
+    for e in range(gpu.shape[0]):
+        assert rel_err(gpu[e], ref[e]) < TOL_FP64, e
+
+
+def test_fms_spin_selector_one_spin(ctx):
+    cl, grid = wl.small_cluster(2.6, lmax=2, n_energies=3, seed=10)
+    ph = grid.phase_shifts.copy()
+    ph[:, :, :cl.global_lmax, :] *= 0.8
+    grid.phase_shifts = ph
+    plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP64_LU, ispin=1)
+    assert (status == 0).all()
+    for e in range(gpu.shape[0]):
+        assert rel_err(gpu[e], ref[e]) < TOL_FP64, e
+
+
+def test_fms_debye_damping_and_cutoff(ctx):
+    cl, grid = wl.small_cluster(3.7, lmax=2, n_energies=3, seed=12)
+    plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP64_LU, direct_cutoff=3.0, sig2g=0.004)
+    ref2 = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts,
+                           rdirec=3.0, sig2g=0.004, mode=po.F64)
+    for e in range(gpu.shape[0]):
+        assert rel_err(gpu[e], ref2[e]) < TOL_FP64, e
+
+
+def test_fms_nonfinite_phase_flags_only_that_energy(ctx):
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=4, seed=13)
+    ph = grid.phase_shifts.copy()
+    ph[2, 0, cl.global_lmax + 1, 1] = np.nan
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    gpu, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers, ph, raise_on_error=False)
+    assert status[2] == 6 and (status[[0, 1, 3]] == 0).all()
+    ref = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers[[0, 1, 3]],
+                          grid.phase_shifts[[0, 1, 3]], mode=po.F64)
+    for i, e in enumerate([0, 1, 3]):
+        assert rel_err(gpu[e], ref[i]) < TOL_FP64
+
+
+def test_fms_batching_is_invariant(ctx):
+    """Results do not depend on how energies are split into device batches (graph replay included)."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=11, seed=14)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    full, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    plan.set_batch(4)
+    split, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    again, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    assert np.array_equal(split, again)
+    assert rel_err(split, full) < 1e-13
+
+
+def test_device_pointer_entry_point(ctx):
+    torch = pytest.importorskip("torch")
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=5, seed=15)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    host, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    E, m = 5, plan.shape.absorber_block
+    L, npot = cl.global_lmax, len(cl.lmaxph)
+    k = torch.from_numpy(np.ascontiguousarray(grid.wave_numbers)).cuda()
+    xp = np.ascontiguousarray(np.stack([grid.phase_shifts[e].reshape(-1, order="F") for e in range(E)]))
+    x = torch.from_numpy(xp).cuda()
+    gg = torch.zeros((E, m * m), dtype=torch.complex128, device="cuda")
+    st = torch.zeros(E, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    fms.fms_real_space_spectrum_device(plan, k.data_ptr(), x.data_ptr(), E, gg.data_ptr(), st.data_ptr())
+    torch.cuda.synchronize()
+    dev = gg.cpu().numpy().reshape(E, m, m).transpose(0, 2, 1)  # column-major blocks
+    assert (st.cpu().numpy() == 0).all()
+    assert rel_err(dev, host[:, :m, :m, 0]) < 1e-14
+
+
+def test_gg_section_pads_to_output_spin_capacity(ctx):
+    cl, grid = wl.small_cluster(2.6, lmax=2, n_energies=1, seed=16)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    scat, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    sec = fms.gg_section(plan, scat[0], nspu=2)
+    m = plan.shape.absorber_block
+    assert sec.shape == (2 * m, 2 * m)
+    assert np.array_equal(sec[:m, :m], scat[0, :m, :m, 0])
+    assert np.abs(sec[m:, :]).max() == 0 and np.abs(sec[:, m:]).max() == 0

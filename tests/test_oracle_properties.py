@@ -1,0 +1,78 @@
+"""Independent cross-checks of the FP64 oracle (no GPU): its LU against LAPACK
+(numpy), and its scattering tables against a direct solve built from its own
+G0 / T intermediates."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from refeff_gb300 import workloads as wl
+
+
+def test_fp64_lu_matches_lapack():
+    rng = np.random.default_rng(0)
+    n, m = 120, 5
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    B = rng.normal(size=(n, m)) + 1j * rng.normal(size=(n, m))
+    _, X, _ = po.lu_factor_solve(A, B, po.F64)
+    ref = np.linalg.solve(A, B)
+    assert np.linalg.norm(X - ref) / np.linalg.norm(ref) < 1e-12
+
+
+def _intermediates(cl, k, ph, nsp=1, mode=po.F64):
+    L = cl.global_lmax
+    npot = len(cl.lmaxph)
+    n = np.zeros(1, np.int32)
+    args = [mode, cl.n_atoms, po.ptr(cl.positions), po.ptr(cl.potentials), nsp, 0, 0, npot - 1, L,
+            po.ptr(cl.lmaxph), 1.0e6, None, 0.0]
+    kb = po.cbuf(k)
+    xb = po.cbuf(np.asarray(ph).reshape(nsp, 2 * L + 1, npot))
+    po.check(po.lib().oracle_fms_energy_intermediates(*args, po.ptr(kb), po.ptr(xb), 0.0, po.ptr(n), None, None, None,
+                                                      None))
+    ns = int(n[0])
+    g0 = np.zeros(2 * ns * ns)
+    t = np.zeros(2 * nsp * ns)
+    a = np.zeros(2 * ns * ns)
+    po.check(po.lib().oracle_fms_energy_intermediates(*args, po.ptr(kb), po.ptr(xb), 0.0, po.ptr(n), po.ptr(g0),
+                                                      po.ptr(t), po.ptr(a), None))
+    return po.from_cbuf(g0, (ns, ns)), po.from_cbuf(t, (nsp, ns)), po.from_cbuf(a, (ns, ns))
+
+
+def test_oracle_scattering_equals_direct_solve():
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=2)
+    scat = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts, mode=po.F64)
+    for e in range(2):
+        g0, t, a = _intermediates(cl, grid.wave_numbers[e], grid.phase_shifts[e])
+        n = g0.shape[0]
+        assert np.allclose(a, np.eye(n) - g0 * t[0][None, :], atol=0, rtol=1e-15)
+        m = 9
+        x = np.linalg.solve(a, g0[:, :m])
+        assert np.linalg.norm(scat[e, :m, :m, 0] - x[:m]) / np.linalg.norm(x[:m]) < 1e-12
+
+
+def test_g0_same_atom_blocks_vanish_and_spin_structure():
+    cl, grid = wl.small_cluster(2.6, lmax=2, n_energies=1, nsp=2)
+    g0, t, a = _intermediates(cl, grid.wave_numbers[0], grid.phase_shifts[0], nsp=2)
+    per_atom = 2 * 9
+    for at in range(cl.n_atoms):
+        s = slice(at * per_atom, (at + 1) * per_atom)
+        assert np.abs(g0[s, s]).max() == 0
+    # cross-spin couplings vanish: states alternate spin 1, 2
+    assert np.abs(g0[0::2, 1::2]).max() == 0 and np.abs(g0[1::2, 0::2]).max() == 0
+
+
+def test_f32_faithful_and_fp64_agree_to_single_precision():
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=3, seed=4)
+    a = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts, mode=po.F32)
+    b = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts, mode=po.F64)
+    for e in range(3):
+        assert np.linalg.norm(a[e] - b[e]) / np.linalg.norm(b[e]) < 1e-3
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_g0_reciprocity(seed):
+    """Free propagator reciprocity G0(i l m, j l' m') = (-1)^(l+l') G0(j l' m', i l m) up to the m phase convention:
+    magnitudes of the s-s couplings are symmetric and depend only on distance."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=1, seed=seed)
+    g0, _, _ = _intermediates(cl, grid.wave_numbers[0], grid.phase_shifts[0])
+    ss = g0[0::9, 0::9]
+    assert np.allclose(np.abs(ss), np.abs(ss.T), rtol=1e-12, atol=0)
