@@ -161,9 +161,10 @@ typedef struct {
 
 typedef struct {
   double seconds;               /* wall time of the call */
-  int refinement_iterations;    /* max over energies (FP32_REFINED) */
-  double residual_max;          /* max relative residual after refinement */
+  int refinement_iterations;    /* max corrections over energies (FP32_REFINED) */
+  double residual_max;          /* max relative residual ||b - A x|| / ||b|| after refinement */
   int energies_failed;          /* energies with a non-zero status */
+  int fp64_fallbacks;           /* energies re-solved with the FP64 LU because refinement missed */
 } refeff_fms_report;
 
 /* fms_real_space_spectrum (crates/refeff-core/src/fms/driver.rs:231-239):
@@ -186,6 +187,13 @@ int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energ
 int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies, const void* d_wave_numbers,
                                           const void* d_phase_shifts, refeff_fms_form form, void* d_gg_out,
                                           int32_t* d_status, void* stream);
+
+/* Per-energy outcome of the last refeff_fms_real_space_spectrum call with
+ * REFEFF_FMS_FORM_FP32_REFINED: final relative residual (max-norm, FP64),
+ * corrections applied, and whether the energy was re-solved with the FP64 LU
+ * because the residual missed the tolerance (each pointer optional). */
+int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int n_energies, double* rel_residual,
+                                     int* iterations, int* fp64_fallback);
 
 /* FEFF gg section for one energy (fms_gg_section_values,
  * crates/refeff-engine/src/fms.rs:2004-2047): the absorber block widened to

@@ -472,12 +472,15 @@ __global__ void __launch_bounds__(256) residual_kernel(BatchLayout lay, const do
 }
 
 __global__ void refine_check_kernel(int batch, const unsigned long long* rnorm, const unsigned long long* bnorm,
-                                    double tol, int* converged) {
+                                    double tol, int* converged, int* iters, double* relres, int count_step) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch) return;
+  if (b >= batch || converged[b]) return;  // a converged system keeps its last residual
   const double r = __longlong_as_double(static_cast<long long>(rnorm[b]));
   const double bn = __longlong_as_double(static_cast<long long>(bnorm[b]));
-  if (r <= tol * bn) converged[b] = 1;
+  const double rel = bn > 0.0 ? r / bn : r;
+  relres[b] = rel;
+  if (rel <= tol) converged[b] = 1;
+  else if (count_step) iters[b] += 1;
 }
 
 __device__ __forceinline__ double norm_scale(const unsigned long long* rnorm, int b) {
@@ -712,9 +715,10 @@ void launch_residual(const BatchLayout& lay, int batch, const double2* M64, cons
 }
 
 void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
-                         double tol, int* converged, cudaStream_t s) {
+                         double tol, int* converged, int* iters, double* relres, bool count_step, cudaStream_t s) {
   count_launch();
-  refine_check_kernel<<<unsigned((batch + 127) / 128), 128, 0, s>>>(batch, rnorm_bits, bnorm_bits, tol, converged);
+  refine_check_kernel<<<unsigned((batch + 127) / 128), 128, 0, s>>>(batch, rnorm_bits, bnorm_bits, tol, converged, iters,
+                                                                      relres, count_step ? 1 : 0);
 }
 
 void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,

@@ -60,9 +60,10 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
 // matrices with skip[b] != 0 are left untouched (norms included).
 void launch_residual(const BatchLayout& lay, int batch, const double2* M64, const double2* X64, double2* R,
                      unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip, cudaStream_t s);
-// converged[b] |= (rnorm <= tol * bnorm); iterations[b] counts refinement steps taken.
+// For systems not yet converged: relres[b] = rnorm / bnorm, converged[b] = (relres <= tol);
+// when count_step, a failed check adds one to iters[b] (a correction follows).
 void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
-                         double tol, int* converged, cudaStream_t s);
+                         double tol, int* converged, int* iters, double* relres, bool count_step, cudaStream_t s);
 // RHS columns of M32 <- float(R / rnorm_b)
 void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,
                               const unsigned long long* rnorm_bits, float2* M32, const int* skip, cudaStream_t s);

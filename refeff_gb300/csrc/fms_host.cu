@@ -285,7 +285,8 @@ struct Workspace {
   DevBuf<float2> M32;
   DevBuf<double2> X64, R;
   DevBuf<unsigned long long> rnorm, bnorm;
-  DevBuf<int> converged;
+  DevBuf<int> converged, iters;
+  DevBuf<double> relres;
   DevBuf<int> ipiv, nperm, status, info;
   DevBuf<int2> perm;
   // staging so that a captured graph can be replayed on every batch
@@ -306,8 +307,15 @@ struct refeff_fms_plan {
   std::vector<int> pot_lmax;
   std::vector<long> rep_offsets;  // reference state order
   int max_batch = 0;
-  int refine_iters = 4;
-  double refine_tol = 1.0e-14;
+  int refine_iters = 10;
+  double refine_tol = 1.0e-12;
+  // per-energy refinement outcome of the last spectrum call (FP32_REFINED)
+  DevBuf<double> d_relres_all;
+  DevBuf<int> d_iters_all;
+  std::vector<double> last_relres;
+  std::vector<int> last_iters;
+  std::vector<int> last_fallback;  // energies re-solved with the FP64 LU after refinement missed
+  int last_fallbacks = 0;
   // device tables
   PlanDev P;
   DevBuf<float> d_pos;
@@ -534,6 +542,8 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
     RF_CUDA(ctx, ws.rnorm.alloc(size_t(B)));
     RF_CUDA(ctx, ws.bnorm.alloc(size_t(B)));
     RF_CUDA(ctx, ws.converged.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.iters.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.relres.alloc(size_t(B)));
   }
   RF_CUDA(ctx, ws.ipiv.alloc(size_t(B) * n));
   RF_CUDA(ctx, ws.perm.alloc(size_t(B) * npanels * 2 * nb_max));
@@ -582,12 +592,13 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
     launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, true, nullptr, s);
   });
   cudaMemsetAsync(ws.converged.p, 0, size_t(batch) * sizeof(int), s);
+  cudaMemsetAsync(ws.iters.p, 0, size_t(batch) * sizeof(int), s);
   for (int it = 0; it <= iters; ++it) {
     span(3, [&] {
       cudaMemsetAsync(ws.rnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
       cudaMemsetAsync(ws.bnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
-      launch_residual(lay, batch, ws.M64.p, ws.X64.p, ws.R.p, ws.rnorm.p, ws.bnorm.p, nullptr, s);
-      launch_refine_check(batch, ws.rnorm.p, ws.bnorm.p, tol, ws.converged.p, s);
+      launch_residual(lay, batch, ws.M64.p, ws.X64.p, ws.R.p, ws.rnorm.p, ws.bnorm.p, ws.converged.p, s);
+      launch_refine_check(batch, ws.rnorm.p, ws.bnorm.p, tol, ws.converged.p, ws.iters.p, ws.relres.p, it < iters, s);
     });
     if (it == iters) break;
     span(2, [&] {
@@ -715,6 +726,10 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
   RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
   RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.m * p.m));
+  if (fp32) {
+    RF_CUDA(ctx, p.d_relres_all.alloc(size_t(E)));
+    RF_CUDA(ctx, p.d_iters_all.alloc(size_t(E)));
+  }
   for (int e0 = 0; e0 < E; e0 += B) {
     const int nb = std::min(B, E - e0);
     RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, d_k + size_t(e0) * p.nsp, size_t(nb) * p.nsp * sizeof(double2),
@@ -752,6 +767,41 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
     RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.m * p.m, ws.gg_stage.p, size_t(nb) * p.m * p.m * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
     RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    if (fp32) {
+      RF_CUDA(ctx, cudaMemcpyAsync(p.d_relres_all.p + e0, ws.relres.p, size_t(nb) * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, s));
+      RF_CUDA(ctx, cudaMemcpyAsync(p.d_iters_all.p + e0, ws.iters.p, size_t(nb) * sizeof(int),
+                                   cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  if (!fp32) return REFEFF_FMS_OK;
+  // Energies whose refinement missed the tolerance are solved again with the
+  // plain FP64 LU (same inputs), so every returned block meets the FP64 bar.
+  std::vector<int> st(static_cast<size_t>(E));
+  RF_CUDA(ctx, cudaMemcpyAsync(st.data(), d_status, size_t(E) * sizeof(int), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(ctx, cudaStreamSynchronize(s));
+  std::vector<int> redo;
+  for (int e = 0; e < E; ++e)
+    if (st[size_t(e)] == kDevNotConverged) redo.push_back(e);
+  p.last_fallback = redo;
+  p.last_fallbacks = int(redo.size());
+  for (size_t r0 = 0; r0 < redo.size(); r0 += size_t(B)) {
+    const int nb = int(std::min(redo.size() - r0, size_t(B)));
+    for (int i = 0; i < nb; ++i) {
+      const int e = redo[r0 + size_t(i)];
+      RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p + size_t(i) * p.nsp, d_k + size_t(e) * p.nsp, p.nsp * sizeof(double2),
+                                   cudaMemcpyDeviceToDevice, s));
+      RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p + size_t(i) * xph, d_x + size_t(e) * xph, xph * sizeof(double2),
+                                   cudaMemcpyDeviceToDevice, s));
+    }
+    cudaError_t e = run_fms_batch(p, nb, REFEFF_FMS_FORM_FP64_LU, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fp64 fallback batch");
+    for (int i = 0; i < nb; ++i) {
+      const int en = redo[r0 + size_t(i)];
+      RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(en) * p.m * p.m, ws.gg_stage.p + size_t(i) * p.m * p.m,
+                                   size_t(p.m) * p.m * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+      RF_CUDA(ctx, cudaMemcpyAsync(d_status + en, ws.status.p + i, sizeof(int), cudaMemcpyDeviceToDevice, s));
+    }
   }
   return REFEFF_FMS_OK;
 }
@@ -802,6 +852,15 @@ extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refef
   std::vector<int> st(static_cast<size_t>(E));
   RF_CUDA(ctx, cudaMemcpyAsync(gg.data(), p.d_gg_all.p, gg.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), p.d_status_all.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
+  p.last_relres.assign(fp32 ? size_t(E) : 0, 0.0);
+  p.last_iters.assign(fp32 ? size_t(E) : 0, 0);
+  if (fp32) {
+    RF_CUDA(ctx, cudaMemcpyAsync(p.last_relres.data(), p.d_relres_all.p, size_t(E) * sizeof(double),
+                                 cudaMemcpyDeviceToHost, s));
+    RF_CUDA(ctx, cudaMemcpyAsync(p.last_iters.data(), p.d_iters_all.p, size_t(E) * sizeof(int), cudaMemcpyDeviceToHost,
+                                 s));
+  }
   RF_CUDA(ctx, cudaStreamSynchronize(s));
   int failed = 0;
   for (int e = 0; e < E; ++e) {
@@ -818,14 +877,34 @@ extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refef
   if (report) {
     report->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     report->energies_failed = failed;
-    report->refinement_iterations = form == REFEFF_FMS_FORM_FP32_REFINED ? p.refine_iters : 0;
+    report->refinement_iterations = 0;
     report->residual_max = 0.0;
+    for (int e = 0; e < int(p.last_iters.size()); ++e) {
+      report->refinement_iterations = std::max(report->refinement_iterations, p.last_iters[size_t(e)]);
+      report->residual_max = std::max(report->residual_max, p.last_relres[size_t(e)]);
+    }
+    report->fp64_fallbacks = fp32 ? p.last_fallbacks : 0;
   }
   if (failed) {
     for (int e = 0; e < E; ++e)
       if (map_status(st[size_t(e)]) != REFEFF_FMS_OK)
         return fail(ctx, map_status(st[size_t(e)]), "failed to solve FMS energy section " + std::to_string(e + 1));
   }
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int n_energies, double* rel_residual,
+                                                int* iterations, int* fp64_fallback) {
+  if (!plan || n_energies < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  const int have = int(plan->last_iters.size());
+  for (int e = 0; e < n_energies; ++e) {
+    if (rel_residual) rel_residual[e] = e < have ? plan->last_relres[size_t(e)] : 0.0;
+    if (iterations) iterations[e] = e < have ? plan->last_iters[size_t(e)] : 0;
+    if (fp64_fallback) fp64_fallback[e] = 0;
+  }
+  if (fp64_fallback)
+    for (int e : plan->last_fallback)
+      if (e < n_energies) fp64_fallback[e] = 1;
   return REFEFF_FMS_OK;
 }
 

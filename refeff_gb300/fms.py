@@ -61,7 +61,7 @@ class _EnergyPoints(C.Structure):
 
 class _Report(C.Structure):
     _fields_ = [("seconds", C.c_double), ("refinement_iterations", C.c_int), ("residual_max", C.c_double),
-                ("energies_failed", C.c_int)]
+                ("energies_failed", C.c_int), ("fp64_fallbacks", C.c_int)]
 
 
 def header_functions() -> list[str]:
@@ -103,6 +103,7 @@ def load(build_if_missing: bool = True):
         "refeff_fms_real_space_spectrum": ([_p, _p, _i, _p, _p, _p], _i),
         "refeff_fms_real_space_spectrum_device": ([_p, _i, _p, _p, _i, _p, _p, _p], _i),
         "refeff_fms_gg_section": ([_p, _p, _i, _p], _i),
+        "refeff_fms_plan_refinement_stats": ([_p, _i, _p, _p, _p], _i),
         "refeff_complex_lu_solve_batched": ([_p, _i, _i, _i, _p, _p, _p, _i, _p, _p], _i),
     }
     for name, (args, res) in sig.items():
@@ -193,6 +194,15 @@ class FmsRealSpacePlan:
 
     def set_profiling(self, enable: bool):
         self.ctx.check(self.ctx._lib.refeff_fms_plan_set_profiling(self.handle, 1 if enable else 0))
+
+    def refinement_stats(self, n_energies: int):
+        """(relative residual, corrections, FP64 fallback flag) per energy of the last FP32_REFINED call."""
+        rel = np.zeros(n_energies)
+        its = np.zeros(n_energies, np.int32)
+        fb = np.zeros(n_energies, np.int32)
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_refinement_stats(self.handle, int(n_energies), _ptr(rel),
+                                                                       _ptr(its), _ptr(fb)))
+        return rel, its, fb
 
     PHASES = ("build", "eliminate", "sweeps", "residual", "extract")
 

@@ -66,7 +66,7 @@ def test_dense_lu_fp64_matches_oracle_pivoting(ctx):
     assert rel_err(X[0], Xo) < 1e-10
 
 
-@pytest.mark.parametrize("n", [64, 257])
+@pytest.mark.parametrize("n", [64, 257, 700, 1100])
 def test_dense_lu_fp32_refined(ctx, n):
     rng = np.random.default_rng(n + 1)
     A = rng.normal(size=(2, n, n)) + 1j * rng.normal(size=(2, n, n)) + 3 * np.sqrt(n) * np.eye(n)
@@ -94,7 +94,8 @@ def test_fms_small_cluster_fp64(ctx):
     plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP64_LU)
     assert (status == 0).all()
     m = plan.shape.absorber_block
-    assert np.abs(gpu[:, m:, :, :]).max() == 0 and np.abs(gpu[:, :, m:, :]).max() == 0
+    assert np.count_nonzero(gpu[:, m:, :, :]) == 0 and np.count_nonzero(gpu[:, :, m:, :]) == 0
+    assert np.count_nonzero(gpu[:, :, :, 1]) == 0  # only the absorber potential is solved (lfms = 0)
     for e in range(gpu.shape[0]):
         assert rel_err(gpu[e], ref[e]) < TOL_FP64, e
 
@@ -119,6 +120,35 @@ def test_fms_config0_subset_both_forms(ctx):
     for e in range(len(sel)):
         assert rel_err(gpu64[e], ref[e]) < TOL_FP64, e
         assert rel_err(gpu32[e], ref[e]) < TOL_CHOSEN, e
+
+
+def test_fms_config1_sample_against_oracle(ctx):
+    """fcc Cu <= 7.5 A (141 atoms, n = 2256, two-level cluster panels): 4 energies against the FP64 oracle."""
+    cl, grid = wl.config1()
+    sel = np.array([0, 36, 120, 199])
+    plan, gpu64, ref, st64 = run_pair(ctx, cl, grid, fms.FORM_FP64_LU, energies=sel)
+    assert plan.shape.n_states == 2256
+    gpu32, st32 = fms.fms_real_space_spectrum(plan, grid.wave_numbers[sel], grid.phase_shifts[sel],
+                                              fms.FORM_FP32_REFINED)
+    assert (st64 == 0).all() and (st32 == 0).all()
+    for e in range(len(sel)):
+        assert rel_err(gpu64[e], ref[e]) < TOL_FP64, e
+        assert rel_err(gpu32[e], ref[e]) < TOL_CHOSEN, e
+
+
+def test_refinement_stats_and_fallback(ctx):
+    """An unattainable tolerance forces every energy through the FP64 fallback; results stay at the FP64 bar."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=3, seed=21)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    ok, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts, fms.FORM_FP32_REFINED)
+    rel, its, fb = plan.refinement_stats(3)
+    assert (rel <= 1e-12).all() and (fb == 0).all()
+    plan.set_refinement(1, 1e-300)
+    forced, st = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts, fms.FORM_FP32_REFINED)
+    rel, its, fb = plan.refinement_stats(3)
+    assert (fb == 1).all() and (st == 0).all()
+    ref64, _ = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts, fms.FORM_FP64_LU)
+    assert rel_err(forced, ref64) < 1e-15
 
 
 def test_fms_reference_precision_agreement(ctx):
