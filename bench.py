@@ -189,7 +189,10 @@ def ours(args, world, rank, local):
     d_x = torch.from_numpy(x_h).cuda()
     d_gg = {f: torch.zeros((E, m * m), dtype=torch.complex128, device="cuda") for f in (0, 1)}
     d_st = torch.zeros(E, dtype=torch.int32, device="cuda")
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the library launches on it and the timing events are recorded on it.
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
 
     def step(form):
         fms.fms_real_space_spectrum_device(plan, d_k.data_ptr(), d_x.data_ptr(), E, d_gg[form].data_ptr(),

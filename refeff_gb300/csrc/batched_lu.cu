@@ -407,56 +407,71 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double 
   atomicMax(p, static_cast<unsigned long long>(__double_as_longlong(v)));
 }
 
-// R = B - A X for 64 rows per CTA, all m columns; K loop in chunks of 32.
-__global__ void __launch_bounds__(256) residual_kernel(BatchLayout lay, const double2* __restrict__ M64,
-                                                       const double2* __restrict__ X64, double2* __restrict__ R,
-                                                       unsigned long long* rnorm, unsigned long long* bnorm,
-                                                       const int* skip) {
-  constexpr int BR = 64, BK = 16, kMaxM = 64;
+// R = B - A X.  A and B are stored as hi/lo float pairs (float4 per complex
+// entry, exact to about 2^-48) and X in FP64; the products are accumulated in
+// double-float on the FP32 pipes (GB300's FP64 rate is a small fraction of its
+// FP32 rate).  CTA: 32 rows x all m columns (8 column groups); K in chunks of 32.
+constexpr int kResRows = 32, kResK = 32, kResMaxM = 64, kResGroups = 8;
+__global__ void __launch_bounds__(256) residual_split_kernel(BatchLayout lay, const float4* __restrict__ Ms,
+                                                             const double2* __restrict__ X64, double2* __restrict__ R,
+                                                             unsigned long long* rnorm, unsigned long long* bnorm,
+                                                             const int* skip) {
+  constexpr int BR = kResRows, BK = kResK, kCols = kResMaxM / kResGroups;
   const int b = blockIdx.y;
   if (skip && skip[b]) return;
-  __shared__ double2 As[BK][BR];
-  __shared__ double2 Xs[BK][kMaxM];
+  extern __shared__ float4 sm4[];
+  float4* As = sm4;            // [BK][BR]
+  float4* Xs = sm4 + BK * BR;  // [BK][kResMaxM] x split as (hi.re, hi.im, lo.re, lo.im)
   const int n = lay.n, m = lay.m;
   const int r0 = blockIdx.x * BR;
-  const double2* A = M64 + size_t(b) * lay.stride;
+  const float4* A = Ms + size_t(b) * lay.stride;
   const double2* X = X64 + size_t(b) * lay.lda * m;
   double2* Rb = R + size_t(b) * lay.lda * m;
   const int tid = threadIdx.x;
-  const int row = tid % BR, cg0 = tid / BR;  // column group 0..3
-  constexpr int kCols = kMaxM / 4;
-  double2 acc[kCols];
+  const int row = tid % BR, cg0 = tid / BR;
+  df accr[kCols], acci[kCols];
 #pragma unroll
-  for (int q = 0; q < kCols; ++q) acc[q] = make_double2(0.0, 0.0);
+  for (int q = 0; q < kCols; ++q) { accr[q] = {0.f, 0.f}; acci[q] = {0.f, 0.f}; }
   for (int k0 = 0; k0 < n; k0 += BK) {
     const int kk_n = min(BK, n - k0);
     __syncthreads();
     for (int idx = tid; idx < BK * BR; idx += 256) {
       const int r = idx % BR, kk = idx / BR;
-      As[kk][r] = (r0 + r < n && kk < kk_n) ? A[size_t(r0 + r) + size_t(lay.lda) * (k0 + kk)] : make_double2(0.0, 0.0);
+      As[kk * BR + r] = (r0 + r < n && kk < kk_n) ? A[size_t(r0 + r) + size_t(lay.lda) * (k0 + kk)]
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     for (int idx = tid; idx < BK * m; idx += 256) {
       const int kk = idx % BK, c = idx / BK;
-      Xs[kk][c] = kk < kk_n ? X[size_t(k0 + kk) + size_t(lay.lda) * c] : make_double2(0.0, 0.0);
+      Xs[kk * kResMaxM + c] = kk < kk_n ? split_hi_lo(X[size_t(k0 + kk) + size_t(lay.lda) * c])
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
     for (int kk = 0; kk < kk_n; ++kk) {
-      const double2 a = As[kk][row];
+      const float4 a = As[kk * BR + row];
 #pragma unroll
       for (int q = 0; q < kCols; ++q) {
-        const int c = cg0 + 4 * q;
-        if (c < m) cfma(acc[q], a, Xs[kk][c]);
+        const int c = cg0 + kResGroups * q;
+        if (c >= m) continue;
+        const float4 x = Xs[kk * kResMaxM + c];
+        df_mac(accr[q], a.x, a.z, x.x, x.z);    // re += a.re x.re
+        df_mac(accr[q], -a.y, -a.w, x.y, x.w);  // re -= a.im x.im
+        df_mac(acci[q], a.x, a.z, x.y, x.w);    // im += a.re x.im
+        df_mac(acci[q], a.y, a.w, x.x, x.z);    // im += a.im x.re
       }
     }
+#pragma unroll
+    for (int q = 0; q < kCols; ++q) { df_renorm(accr[q]); df_renorm(acci[q]); }
   }
   double rmax = 0.0, bmax = 0.0;
   const bool row_ok = r0 + row < n;
 #pragma unroll
   for (int q = 0; q < kCols; ++q) {
-    const int c = cg0 + 4 * q;
+    const int c = cg0 + kResGroups * q;
     if (c >= m || !row_ok) continue;
-    const double2 bv = A[size_t(r0 + row) + size_t(lay.lda) * (n + c)];
-    const double2 rv = make_double2(bv.x - acc[q].x, bv.y - acc[q].y);
+    const double2 bv = join_hi_lo(A[size_t(r0 + row) + size_t(lay.lda) * (n + c)]);
+    const double ax = double(accr[q].hi) + double(accr[q].lo);
+    const double ay = double(acci[q].hi) + double(acci[q].lo);
+    const double2 rv = make_double2(bv.x - ax, bv.y - ay);
     Rb[size_t(r0 + row) + size_t(lay.lda) * c] = rv;
     rmax = fmax(rmax, cabs1(rv));
     bmax = fmax(bmax, cabs1(bv));
@@ -534,6 +549,23 @@ __global__ void copy_rhs64_kernel(BatchLayout lay, const double2* __restrict__ M
     X64[size_t(b) * lay.lda * m + size_t(r) + size_t(lay.lda) * c] =
         M64[size_t(b) * lay.stride + size_t(r) + size_t(lay.lda) * (n + c)];
   }
+}
+
+// In place: M (double2 per entry) -> hi/lo float4 per entry, and M32 <- hi.
+__global__ void split_system_kernel(BatchLayout lay, double2* __restrict__ M, float2* __restrict__ M32) {
+  const int b = blockIdx.y;
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < lay.stride; i += size_t(gridDim.x) * blockDim.x) {
+    const size_t g = size_t(b) * lay.stride + i;
+    const float4 v = split_hi_lo(M[g]);
+    reinterpret_cast<float4*>(M)[g] = v;
+    M32[g] = make_float2(v.x, v.y);
+  }
+}
+
+void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* M32, cudaStream_t s) {
+  dim3 grid(256, unsigned(batch));
+  count_launch();
+  split_system_kernel<<<grid, 256, 0, s>>>(lay, M, M32);
 }
 
 // ---------------------------------------------------------------------------
@@ -706,12 +738,18 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
   absorber_solve_kernel<T><<<unsigned(batch), threads, smem, s>>>(lay, M, gg, status);
 }
 
-void launch_residual(const BatchLayout& lay, int batch, const double2* M64, const double2* X64, double2* R,
+void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, double2* R,
                      unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
                      cudaStream_t s) {
-  dim3 grid(unsigned((lay.n + 63) / 64), unsigned(batch));
+  constexpr size_t smem = size_t(kResK) * (kResRows + kResMaxM) * sizeof(float4);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(residual_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    attr_set = true;
+  }
+  dim3 grid(unsigned((lay.n + kResRows - 1) / kResRows), unsigned(batch));
   count_launch();
-  residual_kernel<<<grid, 256, 0, s>>>(lay, M64, X64, R, rnorm_bits, bnorm_bits, skip);
+  residual_split_kernel<<<grid, 256, smem, s>>>(lay, Ms, X64, R, rnorm_bits, bnorm_bits, skip);
 }
 
 void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,

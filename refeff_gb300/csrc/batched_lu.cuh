@@ -56,10 +56,14 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
 
 // FP64 refinement helpers.  X64 and R are n x m per matrix with leading
 // dimension lay.lda and matrix stride lay.lda * m.
-// R = B64 - A64 * X64 and per matrix rnorm = max |R|, bnorm = max |B| (|re|+|im|);
-// matrices with skip[b] != 0 are left untouched (norms included).
-void launch_residual(const BatchLayout& lay, int batch, const double2* M64, const double2* X64, double2* R,
+// The FP64 system [A | B] of the refined form is stored as hi/lo float pairs
+// (float4 per entry, see split_hi_lo).
+// R = B - A * X64 (double-float accumulation) and per matrix rnorm = max |R|,
+// bnorm = max |B| (|re|+|im|); matrices with skip[b] != 0 are left untouched.
+void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, double2* R,
                      unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip, cudaStream_t s);
+// In place: M (double2 entries) -> hi/lo float4 entries, M32 <- hi (for the dense solve API).
+void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* M32, cudaStream_t s);
 // For systems not yet converged: relres[b] = rnorm / bnorm, converged[b] = (relres <= tol);
 // when count_step, a failed check adds one to iters[b] (a correction follows).
 void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,

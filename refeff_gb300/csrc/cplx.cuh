@@ -48,4 +48,39 @@ __device__ __forceinline__ float2 cexp(float2 a) {
 
 template <typename Dst, typename Src> __device__ __forceinline__ Dst ccast(Src s) { Dst d; d.x = s.x; d.y = s.y; return d; }
 
+// Complex double -> (hi.re, hi.im, lo.re, lo.im) with hi = fl32(v), lo = fl32(v - hi):
+// hi + lo carries v to about 2^-48 relative.
+__device__ __forceinline__ float4 split_hi_lo(double2 v) {
+  const float hr = float(v.x), hi = float(v.y);
+  return make_float4(hr, hi, float(v.x - double(hr)), float(v.y - double(hi)));
+}
+__device__ __forceinline__ double2 join_hi_lo(float4 s) {
+  return make_double2(double(s.x) + double(s.z), double(s.y) + double(s.w));
+}
+
+// ---- double-float (FP32 pair) arithmetic on the FP32 pipes ----
+// Error-free transforms after Dekker / Knuth: two_prod via FMA, two_sum.
+struct df { float hi, lo; };
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// acc += (ah + al) * (xh + xl), dropping al*xl (below 2^-48 relative).
+__device__ __forceinline__ void df_mac(df& acc, float ah, float al, float xh, float xl) {
+  const float p = ah * xh;
+  float e = fmaf(ah, xh, -p);
+  e = fmaf(ah, xl, e);
+  e = fmaf(al, xh, e);
+  float s, t;
+  df_two_sum(acc.hi, p, s, t);
+  acc.hi = s;
+  acc.lo += t + e;
+}
+__device__ __forceinline__ void df_renorm(df& a) {
+  const float s = a.hi + a.lo;
+  a.lo = a.lo - (s - a.hi);
+  a.hi = s;
+}
+
 }  // namespace rfx

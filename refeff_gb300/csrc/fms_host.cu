@@ -597,7 +597,8 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
     span(3, [&] {
       cudaMemsetAsync(ws.rnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
       cudaMemsetAsync(ws.bnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
-      launch_residual(lay, batch, ws.M64.p, ws.X64.p, ws.R.p, ws.rnorm.p, ws.bnorm.p, ws.converged.p, s);
+      launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.R.p, ws.rnorm.p,
+                      ws.bnorm.p, ws.converged.p, s);
       launch_refine_check(batch, ws.rnorm.p, ws.bnorm.p, tol, ws.converged.p, ws.iters.p, ws.relres.p, it < iters, s);
     });
     if (it == iters) break;
@@ -609,15 +610,6 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
     });
   }
   return cudaGetLastError();
-}
-
-__global__ void convert_to_f32_kernel(BatchLayout lay, const double2* __restrict__ M64, float2* __restrict__ M32) {
-  const int b = blockIdx.y;
-  const size_t total = lay.stride;
-  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
-    const double2 v = M64[size_t(b) * lay.stride + i];
-    M32[size_t(b) * lay.stride + i] = make_float2(float(v.x), float(v.y));
-  }
 }
 
 __global__ void status_not_converged_kernel(int batch, const int* converged, int* status) {
@@ -957,12 +949,10 @@ extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, i
     RF_CUDA(ctx, ws.X64.alloc(size_t(batch) * lay.lda * m));
     launch_copy_rhs64(lay, batch, ws.M64.p, ws.X64.p, s);
   } else {
-    dim3 grid(64, unsigned(batch));
-    count_launch();
-    convert_to_f32_kernel<<<grid, 256, 0, s>>>(lay, ws.M64.p, ws.M32.p);
+    launch_split_system(lay, batch, ws.M64.p, ws.M32.p, s);
     cudaError_t e = lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<float>");
-    // M32's RHS columns hold Y32; refinement uses the FP64 copy in M64
+    // M32's RHS columns hold Y32; refinement uses the hi/lo split system in M64
     e = refine_fp32(ws, batch, 6, 1.0e-14, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "refine");
     count_launch();

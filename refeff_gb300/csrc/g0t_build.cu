@@ -381,12 +381,25 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
       }
     }
     if (r == c) a.x += 1.0;
-    M64[base + size_t(r) + size_t(lay.lda) * c] = a;
-    if (kMirror32) M32[base + size_t(r) + size_t(lay.lda) * c] = make_float2(float(a.x), float(a.y));
+    const size_t ai = base + size_t(r) + size_t(lay.lda) * c;
+    if (kMirror32) {
+      // FP32 form: the FP64 system is kept as an exact-to-2^-48 hi/lo float pair
+      // (same 16 bytes per entry) for the refinement residual; hi is the LU copy.
+      const float4 sa = split_hi_lo(a);
+      reinterpret_cast<float4*>(M64)[ai] = sa;
+      M32[ai] = make_float2(sa.x, sa.y);
+    } else {
+      M64[ai] = a;
+    }
     if (absorber_col) {
       const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + cc);
-      M64[bi] = gcol;
-      if (kMirror32) M32[bi] = make_float2(float(gcol.x), float(gcol.y));
+      if (kMirror32) {
+        const float4 sb = split_hi_lo(gcol);
+        reinterpret_cast<float4*>(M64)[bi] = sb;
+        M32[bi] = make_float2(sb.x, sb.y);
+      } else {
+        M64[bi] = gcol;
+      }
     }
   }
 }
