@@ -132,7 +132,11 @@ int refeff_fms_plan_query(const refeff_fms_plan* plan, int* n_states, int* chann
                           int* n_potentials);
 
 /* Tuning: energies solved per device batch (0 = automatic from free memory)
- * and the refinement limits of REFEFF_FMS_FORM_FP32_REFINED. */
+ * and the refinement limits of REFEFF_FMS_FORM_FP32_REFINED: at most
+ * max_iterations corrections; an energy has converged when its last
+ * correction satisfies max|d| <= tolerance * max|x| (default 10, 1e-8).
+ * Energies that reach the limit, or whose corrections stop halving, are
+ * solved again with the FP64 LU. */
 int refeff_fms_plan_set_batch(refeff_fms_plan* plan, int max_batch);
 int refeff_fms_plan_set_refinement(refeff_fms_plan* plan, int max_iterations, double tolerance);
 
@@ -189,9 +193,10 @@ int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies,
                                           int32_t* d_status, void* stream);
 
 /* Per-energy outcome of the last refeff_fms_real_space_spectrum call with
- * REFEFF_FMS_FORM_FP32_REFINED: final relative residual (max-norm, FP64),
+ * REFEFF_FMS_FORM_FP32_REFINED: relative residual max|b - A x| / max|b| of
+ * the last residual evaluated (the one that produced the final correction),
  * corrections applied, and whether the energy was re-solved with the FP64 LU
- * because the residual missed the tolerance (each pointer optional). */
+ * because refinement did not converge (each pointer optional). */
 int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int n_energies, double* rel_residual,
                                      int* iterations, int* fp64_fallback);
 

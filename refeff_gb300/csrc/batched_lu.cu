@@ -486,18 +486,6 @@ __global__ void __launch_bounds__(256) residual_split_kernel(BatchLayout lay, co
   }
 }
 
-__global__ void refine_check_kernel(int batch, const unsigned long long* rnorm, const unsigned long long* bnorm,
-                                    double tol, int* converged, int* iters, double* relres, int count_step) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch || converged[b]) return;  // a converged system keeps its last residual
-  const double r = __longlong_as_double(static_cast<long long>(rnorm[b]));
-  const double bn = __longlong_as_double(static_cast<long long>(bnorm[b]));
-  const double rel = bn > 0.0 ? r / bn : r;
-  relres[b] = rel;
-  if (rel <= tol) converged[b] = 1;
-  else if (count_step) iters[b] += 1;
-}
-
 __device__ __forceinline__ double norm_scale(const unsigned long long* rnorm, int b) {
   const double r = __longlong_as_double(static_cast<long long>(rnorm[b]));
   return r > 0.0 ? r : 1.0;
@@ -518,18 +506,50 @@ __global__ void residual_to_rhs32_kernel(BatchLayout lay, const double2* __restr
 
 __global__ void accumulate_correction_kernel(BatchLayout lay, const float2* __restrict__ M32,
                                              const unsigned long long* rnorm, double2* __restrict__ X64, int init,
-                                             const int* skip) {
+                                             const int* skip, unsigned long long* dnorm, unsigned long long* xnorm) {
   const int b = blockIdx.y;
   if (skip && skip[b]) return;
   const int n = lay.n, m = lay.m;
   const double sc = init ? 1.0 : norm_scale(rnorm, b);
+  double dmax = 0.0, xmax = 0.0;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n * m; idx += gridDim.x * blockDim.x) {
     const int r = idx % n, c = idx / n;
     const float2 d = M32[size_t(b) * lay.stride + size_t(r) + size_t(lay.lda) * (n + c)];
     double2& x = X64[size_t(b) * lay.lda * m + size_t(r) + size_t(lay.lda) * c];
-    if (init) x = make_double2(double(d.x), double(d.y));
-    else { x.x += double(d.x) * sc; x.y += double(d.y) * sc; }
+    const double2 dd = make_double2(double(d.x) * sc, double(d.y) * sc);
+    if (init) x = dd;
+    else { x.x += dd.x; x.y += dd.y; }
+    dmax = fmax(dmax, cabs1(dd));
+    xmax = fmax(xmax, cabs1(x));
   }
+  if (!dnorm) return;
+  for (int off = 16; off > 0; off >>= 1) {
+    dmax = fmax(dmax, __shfl_down_sync(0xffffffffu, dmax, off));
+    xmax = fmax(xmax, __shfl_down_sync(0xffffffffu, xmax, off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_nonneg(dnorm + b, dmax);
+    atomic_max_nonneg(xnorm + b, xmax);
+  }
+}
+
+// Stopping rule of the refinement, per system not yet finished (done == 0):
+// record relres = |r| / |b| of this step's residual and count the step; stop
+// with done = 1 when the correction is small, |d| <= tol |x| (the solution is
+// then accurate to about cond * eps32 * tol), or with done = 2 when the
+// corrections stop shrinking (|d| > 0.5 |d_prev|): such systems go to the FP64 LU.
+__global__ void ir_check_kernel(int batch, const unsigned long long* rnorm, const unsigned long long* bnorm,
+                                const unsigned long long* dnorm, const unsigned long long* xnorm, double tol,
+                                int* done, int* iters, double* relres, double* dprev) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch || done[b]) return;
+  auto v = [](const unsigned long long* p, int i) { return __longlong_as_double(static_cast<long long>(p[i])); };
+  const double r = v(rnorm, b), bn = v(bnorm, b), d = v(dnorm, b), x = v(xnorm, b);
+  relres[b] = bn > 0.0 ? r / bn : r;
+  const int it = iters[b]++;
+  if (d <= tol * x) done[b] = 1;
+  else if (it > 0 && d > 0.5 * dprev[b]) done[b] = 2;
+  dprev[b] = d;
 }
 
 __global__ void extract_absorber_kernel(BatchLayout lay, const double2* __restrict__ X64, double2* __restrict__ gg) {
@@ -752,13 +772,6 @@ void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const 
   residual_split_kernel<<<grid, 256, smem, s>>>(lay, Ms, X64, R, rnorm_bits, bnorm_bits, skip);
 }
 
-void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
-                         double tol, int* converged, int* iters, double* relres, bool count_step, cudaStream_t s) {
-  count_launch();
-  refine_check_kernel<<<unsigned((batch + 127) / 128), 128, 0, s>>>(batch, rnorm_bits, bnorm_bits, tol, converged, iters,
-                                                                      relres, count_step ? 1 : 0);
-}
-
 void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,
                               const unsigned long long* rnorm_bits, float2* M32, const int* skip, cudaStream_t s) {
   dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
@@ -768,10 +781,19 @@ void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* 
 
 void launch_accumulate_correction(const BatchLayout& lay, int batch, const float2* M32,
                                   const unsigned long long* rnorm_bits, double2* X64, bool init, const int* skip,
-                                  cudaStream_t s) {
+                                  unsigned long long* dnorm_bits, unsigned long long* xnorm_bits, cudaStream_t s) {
   dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
   count_launch();
-  accumulate_correction_kernel<<<grid, 256, 0, s>>>(lay, M32, rnorm_bits, X64, init ? 1 : 0, skip);
+  accumulate_correction_kernel<<<grid, 256, 0, s>>>(lay, M32, rnorm_bits, X64, init ? 1 : 0, skip, dnorm_bits,
+                                                    xnorm_bits);
+}
+
+void launch_ir_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
+                     const unsigned long long* dnorm_bits, const unsigned long long* xnorm_bits, double tol,
+                     int* done, int* iters, double* relres, double* dprev, cudaStream_t s) {
+  count_launch();
+  ir_check_kernel<<<unsigned((batch + 127) / 128), 128, 0, s>>>(batch, rnorm_bits, bnorm_bits, dnorm_bits, xnorm_bits,
+                                                                tol, done, iters, relres, dprev);
 }
 
 void launch_extract_absorber(const BatchLayout& lay, int batch, const double2* X64, double2* gg, cudaStream_t s) {

@@ -64,17 +64,18 @@ void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const 
                      unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip, cudaStream_t s);
 // In place: M (double2 entries) -> hi/lo float4 entries, M32 <- hi (for the dense solve API).
 void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* M32, cudaStream_t s);
-// For systems not yet converged: relres[b] = rnorm / bnorm, converged[b] = (relres <= tol);
-// when count_step, a failed check adds one to iters[b] (a correction follows).
-void launch_refine_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
-                         double tol, int* converged, int* iters, double* relres, bool count_step, cudaStream_t s);
 // RHS columns of M32 <- float(R / rnorm_b)
 void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,
                               const unsigned long long* rnorm_bits, float2* M32, const int* skip, cudaStream_t s);
 // X64 += D32 * rnorm_b (D32 = RHS columns of M32); with init, X64 = D32.
+// When dnorm/xnorm are given, max |correction| and max |X| are accumulated per matrix.
 void launch_accumulate_correction(const BatchLayout& lay, int batch, const float2* M32,
                                   const unsigned long long* rnorm_bits, double2* X64, bool init, const int* skip,
-                                  cudaStream_t s);
+                                  unsigned long long* dnorm_bits, unsigned long long* xnorm_bits, cudaStream_t s);
+// Refinement stopping rule (see ir_check_kernel): done[b] = 1 converged, 2 stalled.
+void launch_ir_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
+                     const unsigned long long* dnorm_bits, const unsigned long long* xnorm_bits, double tol,
+                     int* done, int* iters, double* relres, double* dprev, cudaStream_t s);
 // gg (m x m per matrix) = rows [n-m, n) of X64
 void launch_extract_absorber(const BatchLayout& lay, int batch, const double2* X64, double2* gg, cudaStream_t s);
 // X64 = RHS columns of M64 (for the FP64 full solve)

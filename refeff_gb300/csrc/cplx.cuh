@@ -66,7 +66,9 @@ __device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e)
   const float bb = s - a;
   e = (a - (s - bb)) + (b - bb);
 }
-// acc += (ah + al) * (xh + xl), dropping al*xl (below 2^-48 relative).
+// acc += (ah + al) * (xh + xl), dropping al*xl (below 2^-48 relative); the
+// result is renormalised (|lo| <= ulp(hi)/2) so that every step adds an error
+// of about 2^-48 |acc| only.
 __device__ __forceinline__ void df_mac(df& acc, float ah, float al, float xh, float xl) {
   const float p = ah * xh;
   float e = fmaf(ah, xh, -p);
@@ -74,8 +76,9 @@ __device__ __forceinline__ void df_mac(df& acc, float ah, float al, float xh, fl
   e = fmaf(al, xh, e);
   float s, t;
   df_two_sum(acc.hi, p, s, t);
-  acc.hi = s;
-  acc.lo += t + e;
+  t += acc.lo + e;
+  acc.hi = s + t;
+  acc.lo = t - (acc.hi - s);
 }
 __device__ __forceinline__ void df_renorm(df& a) {
   const float s = a.hi + a.lo;

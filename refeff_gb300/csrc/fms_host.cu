@@ -284,7 +284,8 @@ struct Workspace {
   DevBuf<double2> M64;
   DevBuf<float2> M32;
   DevBuf<double2> X64, R;
-  DevBuf<unsigned long long> rnorm, bnorm;
+  DevBuf<unsigned long long> rnorm, bnorm, dnorm, xnorm;
+  DevBuf<double> dprev;
   DevBuf<int> converged, iters;
   DevBuf<double> relres;
   DevBuf<int> ipiv, nperm, status, info;
@@ -308,7 +309,7 @@ struct refeff_fms_plan {
   std::vector<long> rep_offsets;  // reference state order
   int max_batch = 0;
   int refine_iters = 10;
-  double refine_tol = 1.0e-12;
+  double refine_tol = 1.0e-8;  // stop when max|correction| <= tol * max|x|
   // per-energy refinement outcome of the last spectrum call (FP32_REFINED)
   DevBuf<double> d_relres_all;
   DevBuf<int> d_iters_all;
@@ -541,6 +542,9 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
     RF_CUDA(ctx, ws.R.alloc(size_t(B) * lay.lda * m));
     RF_CUDA(ctx, ws.rnorm.alloc(size_t(B)));
     RF_CUDA(ctx, ws.bnorm.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.dnorm.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.xnorm.alloc(size_t(B)));
+    RF_CUDA(ctx, ws.dprev.alloc(size_t(B)));
     RF_CUDA(ctx, ws.converged.alloc(size_t(B)));
     RF_CUDA(ctx, ws.iters.alloc(size_t(B)));
     RF_CUDA(ctx, ws.relres.alloc(size_t(B)));
@@ -567,9 +571,11 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
 
 using Spans = std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>>;
 
-// Refinement of X64 for [A64 | B64] in M64 with the FP32 factors in M32
-// (eliminated; RHS columns of M32 hold Y32).  Leaves converged flags and
-// final residual norms in the workspace.  With `spans`, events bracket the
+// Iterative refinement of X64 for the split system [A | B] in M64 with the
+// FP32 factors in M32 (eliminated; RHS columns of M32 hold Y32).  Each step:
+// r = b - A x (double-float), d = LU^-1 r (FP32), x += d; stop per system when
+// |d| <= tol |x| (converged[b] = 1) or when |d| stops halving (converged[b] = 2,
+// handed to the FP64 LU by the caller).  With `spans`, events bracket the
 // sweeps (phase 2) and the residuals (phase 3).
 cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStream_t s, Spans* spans = nullptr) {
   const BatchLayout& lay = ws.lay;
@@ -587,26 +593,30 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
       spans->push_back({phase, {a, b}});
     }
   };
+  const size_t nb8 = size_t(batch) * sizeof(unsigned long long);
   span(2, [&] {
     lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, nullptr, s);
-    launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, true, nullptr, s);
+    launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, true, nullptr, nullptr, nullptr, s);
   });
   cudaMemsetAsync(ws.converged.p, 0, size_t(batch) * sizeof(int), s);
   cudaMemsetAsync(ws.iters.p, 0, size_t(batch) * sizeof(int), s);
-  for (int it = 0; it <= iters; ++it) {
+  for (int it = 0; it < iters; ++it) {
     span(3, [&] {
-      cudaMemsetAsync(ws.rnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
-      cudaMemsetAsync(ws.bnorm.p, 0, size_t(batch) * sizeof(unsigned long long), s);
+      cudaMemsetAsync(ws.rnorm.p, 0, nb8, s);
+      cudaMemsetAsync(ws.bnorm.p, 0, nb8, s);
       launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.R.p, ws.rnorm.p,
                       ws.bnorm.p, ws.converged.p, s);
-      launch_refine_check(batch, ws.rnorm.p, ws.bnorm.p, tol, ws.converged.p, ws.iters.p, ws.relres.p, it < iters, s);
     });
-    if (it == iters) break;
     span(2, [&] {
+      cudaMemsetAsync(ws.dnorm.p, 0, nb8, s);
+      cudaMemsetAsync(ws.xnorm.p, 0, nb8, s);
       launch_residual_to_rhs32(lay, batch, ws.R.p, ws.rnorm.p, ws.M32.p, ws.converged.p, s);
       lu_forward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, w32, ws.converged.p, s);
       lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, ws.converged.p, s);
-      launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, false, ws.converged.p, s);
+      launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, false, ws.converged.p, ws.dnorm.p,
+                                   ws.xnorm.p, s);
+      launch_ir_check(batch, ws.rnorm.p, ws.bnorm.p, ws.dnorm.p, ws.xnorm.p, tol, ws.converged.p, ws.iters.p,
+                      ws.relres.p, ws.dprev.p, s);
     });
   }
   return cudaGetLastError();
@@ -614,7 +624,7 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
 
 __global__ void status_not_converged_kernel(int batch, const int* converged, int* status) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < batch && !converged[b] && status[b] == kDevOk) status[b] = kDevNotConverged;
+  if (b < batch && converged[b] != 1 && status[b] == kDevOk) status[b] = kDevNotConverged;
 }
 
 // One batch of energies from the staging buffers (k_stage, x_stage) into gg_stage/status.
@@ -953,7 +963,7 @@ extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, i
     cudaError_t e = lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<float>");
     // M32's RHS columns hold Y32; refinement uses the hi/lo split system in M64
-    e = refine_fp32(ws, batch, 6, 1.0e-14, s);
+    e = refine_fp32(ws, batch, 10, 1.0e-10, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "refine");
     count_launch();
     status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
