@@ -87,6 +87,18 @@ int refeff_fms_abi_version(void);
  * (launches replayed inside CUDA graphs included). */
 unsigned long long refeff_fms_kernel_launches(void);
 
+/* Context options; they apply to plans created and dense solves started
+ * after the call.
+ *   REFEFF_FMS_OPT_TENSOR_CORES: 1 (default) runs the trailing updates of the
+ *     FP32 LU on the tcgen05 tensor cores (split TF32, FP32 accumulation);
+ *     0 runs them on the CUDA cores.
+ *   REFEFF_FMS_OPT_DENSE_REFINEMENT: corrections allowed in
+ *     refeff_complex_lu_solve_batched with REFEFF_FMS_FORM_FP32_REFINED
+ *     (default 10; 0 returns the plain FP32 LU solution, flagged NOT_CONVERGED). */
+#define REFEFF_FMS_OPT_TENSOR_CORES 1
+#define REFEFF_FMS_OPT_DENSE_REFINEMENT 2
+int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
+
 /* ---- cluster preparation (host) -------------------------------------- */
 
 /* FEFF yprep + sortat for one absorber: replaces fms_yprep_cluster

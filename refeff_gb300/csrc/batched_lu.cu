@@ -715,6 +715,14 @@ cudaError_t lu_eliminate(const PanelConfig& pc, const BatchLayout& lay, int batc
       if (err != cudaSuccess) return err;
       launch_rhs_lower<T, 32>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
     }
+    if constexpr (sizeof(T) == 4) {
+      if (w.tc_images) {
+        tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        continue;
+      }
+    }
     gemm_any<T>(pc.nb, lay, batch, k + kb, n, k + kb, col_end, k, kb, M, nullptr, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;

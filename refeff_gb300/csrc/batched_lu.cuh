@@ -20,7 +20,17 @@ template <typename T> PanelConfig choose_panel(int n);
 
 inline int panel_count(int n, int nb) { return (n + nb - 1) / nb; }
 
+// Tensor-core trailing update (tc_update.cu) for the FP32 elimination.
+constexpr int kTcBM = 128, kTcBN = 48;
+// bytes of the operand tile images for a batch of systems of order n with m right-hand sides
+size_t tc_image_bytes(int n, int m, int batch);
+// C -= L21 U12 for elimination step k with tcgen05 MMAs (split TF32, FP32 accumulation).
+void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int col_end, float2* M, uint8_t* images,
+                        int* err_flag, const int* skip, cudaStream_t s);
+
 struct LuWork {
+  uint8_t* tc_images = nullptr;  // operand images for the tensor-core update (FP32 only); null = CUDA cores
+  int* tc_err = nullptr;         // set when a tensor-core wait timed out
   int* ipiv = nullptr;    // [batch][n]  LAPACK-style: row k+j was swapped with row ipiv
   int2* perm = nullptr;   // [batch][npanels][2*nb] (dst, src) row moves per panel
   int* nperm = nullptr;   // [batch][npanels]

@@ -44,7 +44,21 @@ struct refeff_fms_context {
   cudaStream_t stream = nullptr;
   std::string last_error;
   int sm_count = 0;
+  int use_tensor_cores = 1;  // FP32 trailing updates on tcgen05 (REFEFF_FMS_OPT_TENSOR_CORES)
+  int dense_refinement = 10; // corrections of the dense FP32 solve (REFEFF_FMS_OPT_DENSE_REFINEMENT)
 };
+
+extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value) {
+  if (!ctx) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  switch (option) {
+    case REFEFF_FMS_OPT_TENSOR_CORES: ctx->use_tensor_cores = value != 0; return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_DENSE_REFINEMENT:
+      if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+      ctx->dense_refinement = int(value);
+      return REFEFF_FMS_OK;
+    default: return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+}
 
 namespace {
 
@@ -289,6 +303,9 @@ struct Workspace {
   DevBuf<int> converged, iters;
   DevBuf<double> relres;
   DevBuf<int> ipiv, nperm, status, info;
+  bool use_tc = false;               // FP32 trailing update on the tensor cores
+  DevBuf<uint8_t> tc_images;         // operand images of the tensor-core update
+  DevBuf<int> tc_err;                // set by a tensor-core wait that timed out
   DevBuf<int2> perm;
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
@@ -554,6 +571,12 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
   RF_CUDA(ctx, ws.nperm.alloc(size_t(B) * npanels));
   RF_CUDA(ctx, ws.status.alloc(size_t(B)));
   RF_CUDA(ctx, ws.info.alloc(size_t(B)));
+  ws.use_tc = ws.fp32 && ctx->use_tensor_cores != 0;
+  if (ws.use_tc) {
+    RF_CUDA(ctx, ws.tc_images.alloc(tc_image_bytes(n, m, B)));
+    RF_CUDA(ctx, ws.tc_err.alloc(1));
+    RF_CUDA(ctx, cudaMemset(ws.tc_err.p, 0, sizeof(int)));
+  }
   return REFEFF_FMS_OK;
 }
 
@@ -566,6 +589,10 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
   w.info = ws.info.p;
   w.nb = pc.nb;
   w.npanels = panel_count(ws.lay.n, pc.nb);
+  if (&pc == &ws.pc32 && ws.use_tc) {
+    w.tc_images = ws.tc_images.p;
+    w.tc_err = ws.tc_err.p;
+  }
   return w;
 }
 
@@ -781,7 +808,17 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
   // plain FP64 LU (same inputs), so every returned block meets the FP64 bar.
   std::vector<int> st(static_cast<size_t>(E));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), d_status, size_t(E) * sizeof(int), cudaMemcpyDeviceToHost, s));
+  int tc_timeout = 0;
+  if (ws.use_tc) RF_CUDA(ctx, cudaMemcpyAsync(&tc_timeout, ws.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaStreamSynchronize(s));
+  if (tc_timeout) {
+    // A tensor-core wait gave up: the update of that batch is incomplete, so
+    // every FP32 result is redone on the FP64 LU below.
+    for (auto& v : st)
+      if (v == kDevOk) v = kDevNotConverged;
+    RF_CUDA(ctx, cudaMemsetAsync(ws.tc_err.p, 0, sizeof(int), s));
+    ctx->last_error = "tensor-core update timed out; energies re-solved with the FP64 LU";
+  }
   std::vector<int> redo;
   for (int e = 0; e < E; ++e)
     if (st[size_t(e)] == kDevNotConverged) redo.push_back(e);
@@ -963,7 +1000,7 @@ extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, i
     cudaError_t e = lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<float>");
     // M32's RHS columns hold Y32; refinement uses the hi/lo split system in M64
-    e = refine_fp32(ws, batch, 10, 1.0e-10, s);
+    e = refine_fp32(ws, batch, ctx->dense_refinement, 1.0e-10, s);  // 0 corrections: the FP32 LU solution
     if (e != cudaSuccess) return cuda_fail(ctx, e, "refine");
     count_launch();
     status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
@@ -976,7 +1013,10 @@ extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, i
   std::vector<int> st(static_cast<size_t>(batch)), info(static_cast<size_t>(batch));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), ws.status.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaMemcpyAsync(info.data(), ws.info.p, info.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+  int tc_timeout = 0;
+  if (ws.use_tc) RF_CUDA(ctx, cudaMemcpyAsync(&tc_timeout, ws.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaStreamSynchronize(s));
+  if (tc_timeout) return fail(ctx, REFEFF_FMS_ERR_CUDA, "tensor-core update timed out");
   int first_bad = REFEFF_FMS_OK;
   for (int b = 0; b < batch; ++b) {
     const int code = map_status(st[size_t(b)]);

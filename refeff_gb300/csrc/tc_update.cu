@@ -1,0 +1,309 @@
+// Tensor-core (tcgen05, sm_103a) trailing update of the FP32 LU:
+//     C[r, c] -= sum_k A[r, k] B[k, c]      (complex, K = panel width <= 64)
+// with A = L21 (rows below the panel) and B = U12 (panel rows, trailing columns).
+//
+// Each complex product is formed from real TF32 MMAs with FP32 accumulation in
+// tensor memory, using a two-term split x = hi + lo (hi = tf32(x), lo =
+// tf32(x - hi)) and the three products hi*hi + hi*lo + lo*hi, which keeps the
+// update at about FP32 accuracy:
+//     Cr += Ar Br + Ai (-Bi)        Ci += Ar Bi + Ai Br
+// The operands are first written by tc_split_* into tile images that are
+// already in the UMMA shared-memory layout (K-major, 128-byte rows, 128-byte
+// swizzle), so the update kernel moves them with plain cp.async.bulk copies
+// completed on an mbarrier.  One CTA (4 warps) computes a 128 x 48 complex
+// tile: thread 0 issues copies and MMAs, all warps run the epilogue
+// (tcgen05.ld from TMEM, C read-modify-write, coalesced along the rows).
+// Every wait on an mbarrier is bounded; on timeout the kernel records an error
+// flag, skips the epilogue, frees its tensor memory and returns.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "cplx.cuh"
+#include "batched_lu.cuh"
+
+namespace rfx {
+
+namespace {
+
+constexpr int BM = kTcBM;         // 128 rows per tile (MMA M)
+constexpr int BN = kTcBN;         // 48 columns per tile (MMA N)
+constexpr int KC = 32;            // K elements per chunk: 32 x 4 B = one 128-byte swizzle row
+constexpr int A_PLANE = BM * 128; // bytes per A plane per chunk (16 KB)
+constexpr int B_PLANE = BN * 128; // bytes per B plane per chunk (6 KB)
+constexpr int A_PLANES = 4;       // re_hi, re_lo, im_hi, im_lo
+constexpr int B_PLANES = 6;       // re_hi, re_lo, im_hi, im_lo, -im_hi, -im_lo
+constexpr int SMEM_OPS = A_PLANES * A_PLANE + B_PLANES * B_PLANE;  // 100 KB
+constexpr int SMEM_BYTES = SMEM_OPS + 1024 + 64;                      // + alignment slack + barriers
+constexpr uint32_t TMEM_COLS = 128;  // Cr at column 0, Ci at column 64
+constexpr long long kWaitLimit = 1LL << 26;
+
+__device__ __forceinline__ uint32_t tf32_bits(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// Byte offset of element (row, k) (k < 32, 4 bytes) in a K-major tile with
+// 128-byte rows and the 128-byte swizzle (16-byte chunk index XOR row % 8).
+__device__ __forceinline__ int sw128_offset(int row, int k) {
+  return row * 128 + ((((k >> 2) ^ (row & 7))) << 4) + ((k & 3) << 2);
+}
+
+__device__ __forceinline__ void split4(float2 v, uint32_t out[4]) {
+  const uint32_t rh = tf32_bits(v.x), ih = tf32_bits(v.y);
+  out[0] = rh;
+  out[1] = tf32_bits(v.x - __uint_as_float(rh));
+  out[2] = ih;
+  out[3] = tf32_bits(v.y - __uint_as_float(ih));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+  // start address >> 4 (14 bits), LBO = 1 (unused for swizzled K-major), SBO = 1024 B (8-row groups),
+  // descriptor version 1, base offset 0, layout type 2 = 128-byte swizzle.
+  return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) |
+         (uint64_t(2) << 61);
+}
+
+// kind::tf32, D = F32, A = B = TF32, both K-major, N = BN, M = BM.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// operand images: A[b][bm][chunk][plane] (16 KB), B[b][bn][chunk][plane] (6 KB)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k, int kb, const float2* __restrict__ M,
+                                                         uint8_t* __restrict__ img, int nbm) {
+  const int bm = blockIdx.x >> 1, chunk = blockIdx.x & 1, b = blockIdx.y;
+  const int n = lay.n;
+  const int r0 = k + kb + bm * BM;
+  const float2* Mb = M + size_t(b) * lay.stride;
+  uint8_t* base = img + ((size_t(b) * nbm + bm) * 2 + chunk) * size_t(A_PLANES) * A_PLANE;
+  for (int e = threadIdx.x; e < BM * KC; e += blockDim.x) {
+    const int r = e % BM, kk = e / BM;
+    const int kcol = chunk * KC + kk;
+    float2 v = make_float2(0.f, 0.f);
+    if (r0 + r < n && kcol < kb) v = Mb[size_t(r0 + r) + size_t(lay.lda) * (k + kcol)];
+    uint32_t s[4];
+    split4(v, s);
+    const int off = sw128_offset(r, kk);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) *reinterpret_cast<uint32_t*>(base + size_t(p) * A_PLANE + off) = s[p];
+  }
+}
+
+__global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k, int kb, int col_end,
+                                                         const float2* __restrict__ M, uint8_t* __restrict__ img,
+                                                         int nbn) {
+  const int bn = blockIdx.x >> 1, chunk = blockIdx.x & 1, b = blockIdx.y;
+  const int c0 = k + kb + bn * BN;
+  const float2* Mb = M + size_t(b) * lay.stride;
+  uint8_t* base = img + ((size_t(b) * nbn + bn) * 2 + chunk) * size_t(B_PLANES) * B_PLANE;
+  for (int e = threadIdx.x; e < BN * KC; e += blockDim.x) {
+    const int kk = e % KC, c = e / KC;
+    const int krow = chunk * KC + kk;
+    float2 v = make_float2(0.f, 0.f);
+    if (c0 + c < col_end && krow < kb) v = Mb[size_t(k + krow) + size_t(lay.lda) * (c0 + c)];
+    uint32_t s[4];
+    split4(v, s);
+    const int off = sw128_offset(c, kk);
+#pragma unroll
+    for (int p = 0; p < 4; ++p) *reinterpret_cast<uint32_t*>(base + size_t(p) * B_PLANE + off) = s[p];
+    *reinterpret_cast<uint32_t*>(base + size_t(4) * B_PLANE + off) = s[2] ^ 0x80000000u;  // -im_hi
+    *reinterpret_cast<uint32_t*>(base + size_t(5) * B_PLANE + off) = s[3] ^ 0x80000000u;  // -im_lo
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the update
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, int kb, int col_end,
+                                                        float2* __restrict__ M, const uint8_t* __restrict__ aimg,
+                                                        const uint8_t* __restrict__ bimg, int nbm, int nbn,
+                                                        int* __restrict__ err_flag, const int* skip) {
+  const int bm = blockIdx.x, bn = blockIdx.y, b = blockIdx.z;
+  if (skip && skip[b]) return;
+  const int n = lay.n;
+  const int r0 = k + kb + bm * BM, c0 = k + kb + bn * BN;
+  if (r0 >= n || c0 >= col_end) return;
+  extern __shared__ uint8_t smraw[];
+  const uint32_t raw = smem_u32(smraw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t* const gbase = smraw + (sbase - raw);
+  const uint32_t sA = sbase;
+  const uint32_t sB = sbase + A_PLANES * A_PLANE;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + SMEM_OPS);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + SMEM_OPS + 16);
+  int* shared_err = reinterpret_cast<int*>(gbase + SMEM_OPS + 20);
+  const uint32_t bar_load = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    mbar_init(bar_load, 1);
+    mbar_init(bar_mma, 1);
+    *shared_err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tmem_r = tmem, tmem_i = tmem + 64;
+
+  const int nchunks = kb > KC ? 2 : 1;
+  if (tid == 0) {
+    int bad = 0;
+    const uint8_t* ab = aimg + (size_t(b) * nbm + bm) * 2 * size_t(A_PLANES) * A_PLANE;
+    const uint8_t* bb = bimg + (size_t(b) * nbn + bn) * 2 * size_t(B_PLANES) * B_PLANE;
+    for (int ch = 0; ch < nchunks && !bad; ++ch) {
+      mbar_expect_tx(bar_load, uint32_t(SMEM_OPS));
+      const uint8_t* ach = ab + size_t(ch) * A_PLANES * A_PLANE;
+      const uint8_t* bch = bb + size_t(ch) * B_PLANES * B_PLANE;
+      for (int p = 0; p < A_PLANES; ++p) bulk_copy(sA + p * A_PLANE, ach + size_t(p) * A_PLANE, A_PLANE, bar_load);
+      for (int p = 0; p < B_PLANES; ++p) bulk_copy(sB + p * B_PLANE, bch + size_t(p) * B_PLANE, B_PLANE, bar_load);
+      if (!mbar_wait(bar_load, uint32_t(ch & 1))) { bad = 1; break; }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int ks = 0; ks < KC / 8; ++ks) {
+        const uint32_t koff = uint32_t(ks * 32);  // 8 tf32 = 32 bytes along the swizzled row
+        auto ad = [&](int p) { return umma_desc_sw128(sA + p * A_PLANE + koff); };
+        auto bd = [&](int p) { return umma_desc_sw128(sB + p * B_PLANE + koff); };
+        const uint32_t acc0 = (ch == 0 && ks == 0) ? 0u : 1u;
+        // Cr += Ar Br + Ai (-Bi)
+        mma_tf32(tmem_r, ad(0), bd(0), acc0);
+        mma_tf32(tmem_r, ad(0), bd(1), 1u);
+        mma_tf32(tmem_r, ad(1), bd(0), 1u);
+        mma_tf32(tmem_r, ad(2), bd(4), 1u);
+        mma_tf32(tmem_r, ad(2), bd(5), 1u);
+        mma_tf32(tmem_r, ad(3), bd(4), 1u);
+        // Ci += Ar Bi + Ai Br
+        mma_tf32(tmem_i, ad(0), bd(2), acc0);
+        mma_tf32(tmem_i, ad(0), bd(3), 1u);
+        mma_tf32(tmem_i, ad(1), bd(2), 1u);
+        mma_tf32(tmem_i, ad(2), bd(0), 1u);
+        mma_tf32(tmem_i, ad(2), bd(1), 1u);
+        mma_tf32(tmem_i, ad(3), bd(0), 1u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_mma)
+                   : "memory");
+      if (!mbar_wait(bar_mma, uint32_t(ch & 1))) { bad = 1; break; }
+    }
+    if (bad) {
+      *shared_err = 1;
+      atomicExch(err_flag, 1);
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (*shared_err == 0) {
+    const int row = r0 + warp * 32 + lane;
+    const uint32_t lane_off = uint32_t(warp * 32) << 16;
+    float2* Mb = M + size_t(b) * lay.stride;
+#pragma unroll
+    for (int part = 0; part < BN / 16; ++part) {
+      uint32_t cr[16], ci[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(cr[0]), "=r"(cr[1]), "=r"(cr[2]), "=r"(cr[3]), "=r"(cr[4]), "=r"(cr[5]), "=r"(cr[6]), "=r"(cr[7]),
+            "=r"(cr[8]), "=r"(cr[9]), "=r"(cr[10]), "=r"(cr[11]), "=r"(cr[12]), "=r"(cr[13]), "=r"(cr[14]),
+            "=r"(cr[15])
+          : "r"(tmem_r + lane_off + uint32_t(part * 16)));
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(ci[0]), "=r"(ci[1]), "=r"(ci[2]), "=r"(ci[3]), "=r"(ci[4]), "=r"(ci[5]), "=r"(ci[6]), "=r"(ci[7]),
+            "=r"(ci[8]), "=r"(ci[9]), "=r"(ci[10]), "=r"(ci[11]), "=r"(ci[12]), "=r"(ci[13]), "=r"(ci[14]),
+            "=r"(ci[15])
+          : "r"(tmem_i + lane_off + uint32_t(part * 16)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < n) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = c0 + part * 16 + j;
+          if (col < col_end) {
+            float2* p = Mb + size_t(row) + size_t(lay.lda) * col;
+            float2 v = *p;
+            v.x -= __uint_as_float(cr[j]);
+            v.y -= __uint_as_float(ci[j]);
+            *p = v;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+size_t tc_image_bytes(int n, int m, int batch) {
+  const int nbm = (n + BM - 1) / BM, nbn = (n + m + BN - 1) / BN;
+  return size_t(batch) * 2 * (size_t(nbm) * A_PLANES * A_PLANE + size_t(nbn) * B_PLANES * B_PLANE);
+}
+
+void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int col_end, float2* M, uint8_t* images,
+                        int* err_flag, const int* skip, cudaStream_t s) {
+  const int rows = lay.n - (k + kb), cols = col_end - (k + kb);
+  if (rows <= 0 || cols <= 0 || kb <= 0) return;
+  const int nbm_all = (lay.n + BM - 1) / BM, nbn_all = (lay.n + lay.m + BN - 1) / BN;
+  uint8_t* aimg = images;
+  uint8_t* bimg = images + size_t(batch) * 2 * size_t(nbm_all) * A_PLANES * A_PLANE;
+  const int nbm = (rows + BM - 1) / BM, nbn = (cols + BN - 1) / BN;
+  count_launch();
+  tc_split_a_kernel<<<dim3(unsigned(2 * nbm), unsigned(batch)), 256, 0, s>>>(lay, k, kb, M, aimg, nbm_all);
+  count_launch();
+  tc_split_b_kernel<<<dim3(unsigned(2 * nbn), unsigned(batch)), 256, 0, s>>>(lay, k, kb, col_end, M, bimg, nbn_all);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    attr = true;
+  }
+  count_launch();
+  tc_update_kernel<<<dim3(unsigned(nbm), unsigned(nbn), unsigned(batch)), 128, SMEM_BYTES, s>>>(
+      lay, k, kb, col_end, M, aimg, bimg, nbm_all, nbn_all, err_flag, skip);
+}
+
+}  // namespace rfx

@@ -89,6 +89,7 @@ def load(build_if_missing: bool = True):
     sig = {
         "refeff_fms_abi_version": ([], _i),
         "refeff_fms_kernel_launches": ([], C.c_ulonglong),
+        "refeff_fms_context_set_option": ([_p, _i, C.c_longlong], _i),
         "refeff_fms_context_create": ([_i, _p], _i),
         "refeff_fms_context_destroy": ([_p], None),
         "refeff_fms_last_error": ([_p], C.c_char_p),
@@ -147,6 +148,13 @@ class Context:
         if rc:
             raise FmsError(rc, "cannot create a CUDA context (no GPU?)")
         self.handle = h
+
+    OPT_TENSOR_CORES = 1
+    OPT_DENSE_REFINEMENT = 2
+
+    def set_option(self, option: int, value: int):
+        """Context option (applies to plans / dense solves started afterwards)."""
+        self.check(self._lib.refeff_fms_context_set_option(self.handle, int(option), int(value)))
 
     def last_error(self) -> str:
         return self._lib.refeff_fms_last_error(self.handle).decode()

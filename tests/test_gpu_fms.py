@@ -77,6 +77,27 @@ def test_dense_lu_fp32_refined(ctx, n):
         assert rel_err(X[b], np.linalg.solve(A[b], B[b])) < 1e-11
 
 
+@pytest.mark.parametrize("n,m", [(130, 3), (700, 16), (1100, 25)])
+def test_tensor_core_update_matches_cuda_cores(n, m):
+    """FP32 LU without refinement: tcgen05 split-TF32 trailing updates against the CUDA-core updates."""
+    rng = np.random.default_rng(n + m)
+    A = rng.normal(size=(2, n, n)) + 1j * rng.normal(size=(2, n, n)) + 3 * np.sqrt(n) * np.eye(n)
+    B = rng.normal(size=(2, n, m)) + 1j * rng.normal(size=(2, n, m))
+    out = {}
+    for tc in (0, 1):
+        c = fms.Context(0)
+        c.set_option(c.OPT_TENSOR_CORES, tc)
+        c.set_option(c.OPT_DENSE_REFINEMENT, 0)
+        out[tc], st, _ = fms.complex_lu_solve_batched(c, A, B, fms.FORM_FP32_REFINED)
+        assert (st == 10).all()  # no refinement: flagged NOT_CONVERGED by design
+        c.close()
+    for b in range(2):
+        ref = np.linalg.solve(A[b], B[b])
+        assert rel_err(out[0][b], ref) < 1e-5
+        assert rel_err(out[1][b], ref) < 1e-5
+        assert rel_err(out[1][b], out[0][b]) < 1e-5
+
+
 def test_dense_lu_singular_reports_pivot(ctx):
     n = 40
     rng = np.random.default_rng(5)
