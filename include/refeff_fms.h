@@ -219,6 +219,34 @@ int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int n_energies
 int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_complex128* scattering, int nspu,
                           refeff_complex128* out);
 
+/* ---- FEFF file seam (module-level drop-in) ---------------------------- */
+
+/* The `fms` stage on a FEFF work directory, replacing the generation path of
+ * run_fms_in_dir (crates/refeff-engine/src/fms.rs:1102-1127, 1141-1219,
+ * 3549-3695): reads fms.inp, global.inp, phase.bin, geom.dat and the optional
+ * .dimensions.dat, solves every energy on the GPU, and writes gg.bin and
+ * gg.dat (byte-compatible sectioned text, io/gg_dat.rs:174-233) and log3.dat
+ * (fms.rs:5995-6058).  Supported: idwopt < 0 (uniform sig2g), save_gg_slice
+ * off; anything else returns REFEFF_FMS_ERR_UNSUPPORTED. */
+int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir, refeff_fms_form form, refeff_fms_report* report);
+
+/* gg.dat / gg.bin writer (gg_dat_bytes, crates/refeff-io/src/gg_dat.rs:174-202):
+ * n_sections square dim x dim complex blocks (column-major), section numbers
+ * 1..n, every value as Fortran E20.10 (crates/refeff-io/src/format.rs:174-209).
+ * Host only; needs no GPU. */
+int refeff_fms_write_gg_dat(const char* path, int n_sections, int dim, const refeff_complex128* values);
+
+/* phase.bin reader (crates/refeff-io/src/phase_bin/parse.rs:18-130, PAD
+ * decoding crates/refeff-io/src/pad.rs:102-127).  Host only.
+ * dims: spin count, energy count, potential count (nph + 1), largest lmax.
+ * read: energy grid (ne), reference energy (ne x nsp, energy fastest), lmax per
+ * potential, and phase shifts (ne, 2*lmax_max+1, nsp, npot) column-major with
+ * the signed-l axis centred on lmax_max (zero outside a potential's lmax);
+ * any output pointer may be NULL. */
+int refeff_fms_phase_bin_dims(const char* path, int* nsp, int* ne, int* npot, int* lmax_max);
+int refeff_fms_phase_bin_read(const char* path, refeff_complex128* energy_grid, refeff_complex128* reference_energy,
+                              int* potential_lmax, refeff_complex128* phase_shifts);
+
 /* ---- dense solve (refeff-linalg boundary) ----------------------------- */
 
 /* Batched dense complex solve A X = B, replacing complex32_faer_lu_factor +

@@ -1,0 +1,244 @@
+"""TEST INFRASTRUCTURE ONLY: FEFF handoff files for the file-seam tests.
+
+Restates, independently of the product, the reference's writers for the
+files the `fms` stage reads (phase.bin with its PAD encoding, fms.inp,
+global.inp, geom.dat) and the gg.dat text it writes, so that tests can build
+FEFF work directories and check the product's gg.bin / gg.dat byte for byte.
+
+  PAD encode/decode   crates/refeff-io/src/pad.rs:33-127
+  Fortran E20.10      crates/refeff-io/src/format.rs:164-209
+  gg.dat text         crates/refeff-io/src/gg_dat.rs:155-233
+  phase.bin text      crates/refeff-io/src/phase_bin/render.rs:14-99
+  fms.inp text        crates/refeff-io/src/fms_input.rs:214-246
+  global.inp text     crates/refeff-io/src/global_input.rs:108-190
+  geom.dat text       crates/refeff-io/src/structure_output.rs:204-223
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+
+import numpy as np
+
+IOFF, IBASE, IHUGE, IBAS2 = 37, 90, 38, 45
+TENLOG = 2.3025850929940455
+
+
+def powi(a: float, b: int) -> float:
+    """Integer power by repeated squaring (what the reference's powi lowers to)."""
+    recip = b < 0
+    r = 1.0
+    while True:
+        if b & 1:
+            r *= a
+        b = int(b / 2)  # truncation toward zero, like C integer division
+        if b == 0:
+            break
+        a *= a
+    return 1.0 / r if recip else r
+
+
+def _trunc(x: float) -> int:
+    return int(x)  # Rust `as i32` truncates toward zero
+
+
+def pad_encode(value: float, npack: int) -> str:
+    huge = powi(10.0, IHUGE)
+    tiny = 1.0 / huge
+    out = [ord(" ")] * npack
+    xsave = min(max(value, -huge), huge)
+    isgn = 1 if xsave > 0.0 else 0
+    xwork = abs(xsave)
+    iexp = 0
+    if tiny < xwork < huge:
+        iexp = 1 + _trunc(math.log(xwork) / TENLOG)
+    elif xwork >= huge:
+        iexp = IHUGE
+        xwork = 1.0
+    elif xwork <= tiny:
+        xwork = 0.0
+    xwork /= powi(10.0, iexp)
+    while True:
+        if xwork >= 1.0:
+            xwork *= 0.1
+            iexp += 1
+        elif xwork <= 0.099999999994:
+            xwork *= 10.0
+            iexp -= 1
+        if xwork < 1.0:
+            break
+    itmp = _trunc(float(IBAS2) * xwork)
+    out[0] = iexp + IOFF + IBAS2
+    out[1] = 2 * itmp + isgn + IOFF
+    xwork = xwork * float(IBAS2) - float(itmp)
+    for slot in range(2, npack):
+        itmp = _trunc(float(IBASE) * xwork + 1.0e-9)
+        out[slot] = itmp + IOFF
+        xwork = xwork * float(IBASE) - float(itmp)
+    if xwork >= 0.5:
+        rounded = itmp + IOFF + 1
+        if rounded <= 126:
+            out[npack - 1] = rounded
+        elif out[npack - 2] < 126:
+            out[npack - 2] += 1
+            out[npack - 1] = 37
+    return bytes(out).decode("ascii")
+
+
+def pad_decode(s: str, npack: int) -> float:
+    b = s.encode("ascii")
+    iexp = b[0] - IOFF - IBAS2
+    second = b[1] - IOFF
+    isgn = (second % 2) * 2 - 1
+    itmp = second // 2
+    base = float(IBASE)
+    total = float(itmp) / powi(base, 2)
+    for i in range(npack - 1, 1, -1):
+        total += float(b[i] - IOFF) / powi(base, i + 1)
+    return 2.0 * float(isgn) * float(IBASE) * total * powi(10.0, iexp)
+
+
+def encode_reals(values, npack: int) -> str:
+    out, payload = [], ""
+    maxp = 82 - npack + 1
+    for i, v in enumerate(values):
+        payload += pad_encode(float(v), npack)
+        if len(payload) >= maxp or i == len(values) - 1:
+            out.append("!" + payload)
+            payload = ""
+    return "".join(line + "\n" for line in out)
+
+
+def encode_complex(values, npack: int) -> str:
+    out, payload = [], ""
+    maxp = 82 - 2 * npack + 1
+    for i, v in enumerate(values):
+        payload += pad_encode(float(v.real), npack) + pad_encode(float(v.imag), npack)
+        if len(payload) >= maxp or i == len(values) - 1:
+            out.append("$" + payload)
+            payload = ""
+    return "".join(line + "\n" for line in out)
+
+
+def fortran_exp(value: float, width: int = 20, precision: int = 10, min_exp_width: int = 2) -> str:
+    exponent = 0 if value == 0.0 else math.floor(math.log10(abs(value))) + 1
+    mantissa = value if value == 0.0 else value / powi(10.0, exponent)
+    m = f"{mantissa:.{precision}f}"
+    digits = str(abs(exponent))
+    ew = max(len(digits), min_exp_width)
+    field = len(m) + 2 + ew
+    return " " * max(0, width - field) + m + "E" + ("-" if exponent < 0 else "+") + digits.zfill(ew)
+
+
+def gg_dat_text(sections) -> str:
+    """sections: list of square complex arrays (row, column)."""
+    out = []
+    for number, sec in enumerate(sections, start=1):
+        r, c = sec.shape
+        out.append(f"#SN#   Section: {number:4d}\n")
+        out.append("#DF# This section written in txt.\n#H#\n")
+        out.append(f"#DT# 2D complex array with sizes {r:4d}{c:4d}\n")
+        out.append("#H# File is organized as follows:  Array(1,i)     Array(1,i+1)    Array(1,i+2)  . . .\n")
+        out.append("#H#                                Array(2,i)\n")
+        out.append("#H#                                     .\n" * 3)
+        for row in range(r):
+            out.append("".join(fortran_exp(float(v.real)) + " " + fortran_exp(float(v.imag)) for v in sec[row]) + "\n")
+    return "".join(out)
+
+
+def parse_gg_dat(text: str):
+    sections, cur, dim = [], [], 0
+    for line in text.splitlines():
+        if line.startswith("#DT#"):
+            dim = int(line[-8:-4])
+            cur = []
+        elif line.startswith("#"):
+            continue
+        elif line.strip():
+            vals = [float(line[i:i + 20]) for i in range(0, len(line), 41)]
+            ims = [float(line[i + 21:i + 41]) for i in range(0, len(line), 41)]
+            cur.append(np.array(vals) + 1j * np.array(ims))
+            if len(cur) == dim:
+                sections.append(np.array(cur))
+    return sections
+
+
+def phase_bin_text(*, nsp, energy_grid, reference_energy, potentials, pad_width=8, transition_count=8,
+                   edge=8979.0) -> str:
+    """potentials: list of (lmax, iz, label, phase array (ne, 2lmax+1, nsp))."""
+    ne = len(energy_grid)
+    hdr = [nsp, ne, ne, 0, len(potentials) - 1, 1, 1, pad_width, transition_count, transition_count, 1]
+    out = "".join(f" {v:>4d}" for v in hdr) + "\n"
+    out += encode_reals([1.2, 0.0, edge], pad_width)
+    out += encode_complex(list(energy_grid), pad_width)
+    eref = np.asarray(reference_energy).reshape(ne, nsp)
+    out += encode_complex([eref[e, s] for s in range(nsp) for e in range(ne)], pad_width)
+    for lmax, iz, label, ph in potentials:
+        out += f" {lmax:>3d} {iz:>3d} {label:<6s}\n"
+        for s in range(nsp):
+            out += encode_complex([ph[e, l, s] for e in range(ne) for l in range(2 * lmax + 1)], pad_width)
+    rkk = [complex(0.2 + 0.03 * e + 0.015 * t, -0.01 * t) for s in range(nsp) for t in range(transition_count)
+           for e in range(ne)]
+    out += encode_complex(rkk, pad_width)
+    return out
+
+
+def fms_inp_text(*, lmaxph, rfms2, rdirec, toler1=1e-3, toler2=1e-3, idwopt=-1, sig2g=0.0, minv=0, mfms=1,
+                 do_fms=0, save_gg_slice=False) -> str:
+    def i4(vals):
+        return "".join(f"{v:4d}" for v in vals)
+    return ("mfms, idwopt, minv\n" + i4([mfms, idwopt, minv]) + "\n"
+            "rfms2, rdirec, toler1, toler2\n" + f"{rfms2:13.5f}{rdirec:13.5f}{toler1:13.5f}{toler2:13.5f}\n"
+            "tk, thetad, sig2g\n" + f"{0.0:13.5f}{0.0:13.5f}{sig2g:13.5f}\n"
+            " lmaxph(0:nph)\n" + i4(lmaxph) + "\n"
+            " the number of decomposi\n" + f"{-1:5d}\n"
+            " save_gg_slice\n" + ("T" if save_gg_slice else "F") + "\n"
+            "do_fms\n" + i4([do_fms]) + "\n")
+
+
+def global_inp_text(ispin: int = 0) -> str:
+    return (" nabs, iphabs - CFAVERAGE data\n" + f"{1:8d}{0:8d}{0.0:13.5f}\n"
+            " ipol, ispin, le2, elpty, angks, l2lp, do_nrixs, ldecmx, lj\n"
+            + f"{0:5d}{ispin:5d}{0:5d}{0.0:12.4f}{0.0:12.4f}{0:5d}{0:5d}{0:5d}{0:5d}\n"
+            "evec\t\t  xivec \t   spvec\n" + "".join(f"{a:13.5f}{b:13.5f}{c:13.5f}\n" for a, b, c in
+                                                  [(0, 1, 0), (0, 0, 0), (1, 0, 1)]))
+
+
+def geom_dat_text(positions, potentials) -> str:
+    nph = int(max(potentials))
+    out = f"nat, nph = {len(potentials):5d}{nph:5d}\n"
+    out += "".join(f"{i + 1:5d}" for i in range(nph + 1)) + "\n"
+    out += " iat     x       y        z       iph  \n " + "-" * 71 + "\n"
+    for i, (p, ip) in enumerate(zip(positions, potentials)):
+        out += f"{i + 1:4d}{p[0]:13.5f}{p[1]:13.5f}{p[2]:13.5f}{int(ip):4d}{0:4d}\n"
+    return out
+
+
+def write_workdir(path: Path, *, positions, potentials, lmaxph, energy_grid, phase_potentials, nsp=1, ispin=0,
+                  rfms2=100.0, rdirec=100.0, sig2g=0.0, do_fms=0, nspu=None):
+    path.mkdir(parents=True, exist_ok=True)
+    ne = len(energy_grid)
+    (path / "phase.bin").write_text(phase_bin_text(nsp=nsp, energy_grid=energy_grid,
+                                                   reference_energy=np.zeros((ne, nsp), complex),
+                                                   potentials=phase_potentials))
+    (path / "fms.inp").write_text(fms_inp_text(lmaxph=lmaxph, rfms2=rfms2, rdirec=rdirec, sig2g=sig2g,
+                                               do_fms=do_fms))
+    (path / "global.inp").write_text(global_inp_text(ispin))
+    (path / "geom.dat").write_text(geom_dat_text(positions, potentials))
+    if nspu is not None:
+        (path / ".dimensions.dat").write_text(f"{300:12d}{max(lmaxph):12d}{len(lmaxph) - 1:12d}{nspu:12d}\n")
+
+
+def reference_engine_fixture(path: Path):
+    """The reference engine's FMS source fixture (crates/refeff-engine/src/fms/tests.rs:2501-2525, 2821-2875):
+    two atoms 1.4 A apart, two energies, two potentials with lmax 2, lmaxph [1, 1], rfms2 3, rdirec 5."""
+    grid = [complex(1.0, 0.02), complex(1.4, 0.03)]
+    pots = []
+    for p in range(2):
+        ph = np.zeros((2, 5, 1), complex)
+        for e in range(2):
+            for sl in range(5):
+                ph[e, sl, 0] = complex(0.03 * (p + 1) + 0.01 * e + 0.02 * sl, 0.004 * (sl + 1))
+        pots.append((2, 29, "Cu", ph))
+    write_workdir(path, positions=[[0, 0, 0], [1.4, 0, 0]], potentials=[0, 1], lmaxph=[1, 1], energy_grid=grid,
+                  phase_potentials=pots, rfms2=3.0, rdirec=5.0)

@@ -19,7 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "build"
 LIB = BUILD / "librefeff_fms.so"
-SOURCES = ["g0t_build.cu", "batched_lu.cu", "tc_update.cu", "fms_host.cu"]
+SOURCES = ["g0t_build.cu", "batched_lu.cu", "tc_update.cu", "fms_host.cu", "fms_files.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -48,7 +48,7 @@ def _compile(src: Path, obj: Path, verbose: bool) -> None:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
-    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "refeff_fms.h"]
+    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "refeff_fms.h"]
     newest = max(p.stat().st_mtime for p in deps)
     if not force and LIB.exists() and LIB.stat().st_mtime >= newest:
         return LIB

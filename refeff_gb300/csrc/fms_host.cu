@@ -25,6 +25,7 @@
 #include "batched_lu.cuh"
 #include "cplx.cuh"
 #include "fms_plan.cuh"
+#include "host_internal.h"
 
 using namespace rfx;
 
@@ -47,6 +48,10 @@ struct refeff_fms_context {
   int use_tensor_cores = 1;  // FP32 trailing updates on tcgen05 (REFEFF_FMS_OPT_TENSOR_CORES)
   int dense_refinement = 10; // corrections of the dense FP32 solve (REFEFF_FMS_OPT_DENSE_REFINEMENT)
 };
+
+void rfx::set_last_error(refeff_fms_context* ctx, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+}
 
 extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value) {
   if (!ctx) return REFEFF_FMS_ERR_INVALID_ARGUMENT;

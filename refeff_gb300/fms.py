@@ -106,6 +106,10 @@ def load(build_if_missing: bool = True):
         "refeff_fms_gg_section": ([_p, _p, _i, _p], _i),
         "refeff_fms_plan_refinement_stats": ([_p, _i, _p, _p, _p], _i),
         "refeff_complex_lu_solve_batched": ([_p, _i, _i, _i, _p, _p, _p, _i, _p, _p], _i),
+        "refeff_fms_run_dir": ([_p, C.c_char_p, _i, _p], _i),
+        "refeff_fms_write_gg_dat": ([C.c_char_p, _i, _i, _p], _i),
+        "refeff_fms_phase_bin_dims": ([C.c_char_p, _p, _p, _p, _p], _i),
+        "refeff_fms_phase_bin_read": ([C.c_char_p, _p, _p, _p, _p], _i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -320,3 +324,50 @@ def complex_lu_solve_batched(ctx: Context, A, B, form=FORM_FP64_LU):
     if rc and rc not in (9, 10):
         raise FmsError(rc, ctx.last_error())
     return X, st, piv
+
+
+def run_fms_in_dir(ctx: Context, work_dir, form=FORM_FP64_LU) -> dict:
+    """The `fms` stage on a FEFF work directory (run_fms_in_dir, crates/refeff-engine/src/fms.rs:1102-1127):
+    reads fms.inp, global.inp, phase.bin, geom.dat (and .dimensions.dat if present) and writes gg.bin, gg.dat
+    and log3.dat.  Returns the run report as a dict."""
+    rep = _Report()
+    rc = ctx._lib.refeff_fms_run_dir(ctx.handle, str(work_dir).encode(), int(form), C.byref(rep))
+    if rc:
+        raise FmsError(rc, ctx.last_error())
+    return {"seconds": rep.seconds, "refinement_iterations": rep.refinement_iterations,
+            "residual_max": rep.residual_max, "energies_failed": rep.energies_failed,
+            "fp64_fallbacks": rep.fp64_fallbacks}
+
+
+def write_gg_dat(path, sections) -> None:
+    """Write square complex sections (n, dim, dim) as FEFF gg.dat text (crates/refeff-io/src/gg_dat.rs:174-202)."""
+    lib = load()
+    sec = np.asarray(sections, dtype=np.complex128)
+    n, dim, _ = sec.shape
+    flat = np.ascontiguousarray(np.stack([sec[i].reshape(-1, order="F") for i in range(n)])) if n else \
+        np.zeros(0, np.complex128)
+    rc = lib.refeff_fms_write_gg_dat(str(path).encode(), n, dim, _ptr(flat))
+    if rc:
+        raise FmsError(rc, f"cannot write {path}")
+
+
+def read_phase_bin(path) -> dict:
+    """Decode a FEFF phase.bin (crates/refeff-io/src/phase_bin/parse.rs:18-130).
+
+    Returns energy_grid (ne,), reference_energy (ne, nsp), potential_lmax (npot,) and phase_shifts
+    (ne, 2*lmax_max+1, nsp, npot) with the signed-l axis centred on lmax_max."""
+    lib = load()
+    nsp, ne, npot, lm = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    rc = lib.refeff_fms_phase_bin_dims(str(path).encode(), C.byref(nsp), C.byref(ne), C.byref(npot), C.byref(lm))
+    if rc:
+        raise FmsError(rc, f"cannot read {path}")
+    nsp, ne, npot, lm = nsp.value, ne.value, npot.value, lm.value
+    grid = np.zeros(ne, np.complex128)
+    eref = np.zeros(ne * nsp, np.complex128)
+    lmax = np.zeros(npot, np.int32)
+    ph = np.zeros(ne * (2 * lm + 1) * nsp * npot, np.complex128)
+    rc = lib.refeff_fms_phase_bin_read(str(path).encode(), _ptr(grid), _ptr(eref), _ptr(lmax), _ptr(ph))
+    if rc:
+        raise FmsError(rc, f"cannot read {path}")
+    return {"energy_grid": grid, "reference_energy": eref.reshape((ne, nsp), order="F"), "potential_lmax": lmax,
+            "phase_shifts": ph.reshape((ne, 2 * lm + 1, nsp, npot), order="F")}
