@@ -12,7 +12,8 @@
 // swizzle), so the update kernel moves them with plain cp.async.bulk copies
 // completed on an mbarrier.  One CTA (4 warps) computes a 128 x 48 complex
 // tile: thread 0 issues copies and MMAs, all warps run the epilogue
-// (tcgen05.ld from TMEM, C read-modify-write, coalesced along the rows).
+// (C prefetched into registers at entry, tcgen05.ld from TMEM, subtract and
+// store, coalesced along the rows).
 // Every wait on an mbarrier is bounded; on timeout the kernel records an error
 // flag, skips the epilogue, frees its tensor memory and returns.
 #include <cuda_runtime.h>
@@ -184,6 +185,17 @@ __global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, 
   const uint32_t bar_load = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
+  // Every thread owns one row of the tile: its 48 C values are loaded now, so
+  // that their memory latency overlaps the operand copies and the MMAs.
+  const int row = r0 + warp * 32 + lane;
+  float2* Mb = M + size_t(b) * lay.stride;
+  float2 cv[BN];
+#pragma unroll
+  for (int j = 0; j < BN; ++j) {
+    const int col = c0 + j;
+    cv[j] = (row < n && col < col_end) ? Mb[size_t(row) + size_t(lay.lda) * col] : make_float2(0.f, 0.f);
+  }
+
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(TMEM_COLS));
@@ -246,9 +258,7 @@ __global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, 
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (*shared_err == 0) {
-    const int row = r0 + warp * 32 + lane;
     const uint32_t lane_off = uint32_t(warp * 32) << 16;
-    float2* Mb = M + size_t(b) * lay.stride;
 #pragma unroll
     for (int part = 0; part < BN / 16; ++part) {
       uint32_t cr[16], ci[16];
@@ -270,11 +280,10 @@ __global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, 
         for (int j = 0; j < 16; ++j) {
           const int col = c0 + part * 16 + j;
           if (col < col_end) {
-            float2* p = Mb + size_t(row) + size_t(lay.lda) * col;
-            float2 v = *p;
+            float2 v = cv[part * 16 + j];
             v.x -= __uint_as_float(cr[j]);
             v.y -= __uint_as_float(ci[j]);
-            *p = v;
+            Mb[size_t(row) + size_t(lay.lda) * col] = v;
           }
         }
       }
