@@ -59,7 +59,8 @@ typedef enum {
   REFEFF_FMS_ERR_CUDA = 14,                  /* CUDA runtime error (message in last_error) */
   REFEFF_FMS_ERR_OUT_OF_MEMORY = 15,
   REFEFF_FMS_ERR_INVALID_TOLERANCE = 16,     /* FmsError::InvalidTolerance */
-  REFEFF_FMS_ERR_INVALID_CLUSTER_RADIUS = 17 /* FmsError::InvalidClusterRadius */
+  REFEFF_FMS_ERR_INVALID_CLUSTER_RADIUS = 17, /* FmsError::InvalidClusterRadius */
+  REFEFF_FMS_ERR_SCRATCH_LIMIT = 18           /* request exceeds REFEFF_FMS_NOALLOC_SCRATCH_BYTES */
 } refeff_fms_status;
 
 /* Solver forms for the dense system (I - G0 T) X = G0[:, absorber]. */
@@ -258,6 +259,37 @@ int refeff_fms_phase_bin_read(const char* path, refeff_complex128* energy_grid, 
 int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, int m, int batch, const refeff_complex128* A,
                                     const refeff_complex128* B, refeff_complex128* X, refeff_fms_form form,
                                     int32_t* status_out, int32_t* pivot_out);
+
+/* ---- allocation-free dense solve ---------------------------------------- */
+
+/* Device scratch reserved for refeff_complex_lu_solve_device_noalloc: one
+ * static device array per device of this many bytes (24 MiB). */
+#define REFEFF_FMS_NOALLOC_SCRATCH_BYTES (24u * 1024u * 1024u)
+
+/* No counterpart in the reference: an allocation-free variant of
+ * refeff_complex_lu_solve_batched (FP64 LU form) for callers that must not
+ * allocate device memory -- a host whose device memory is fully reserved by
+ * its own pool, or a multi-stream pipeline that cannot take the implicit
+ * device-wide synchronisation of cudaFree.  Same elimination and results;
+ * its scratch (padded systems, pivots, row moves, status words) is a static
+ * device array of REFEFF_FMS_NOALLOC_SCRATCH_BYTES, never cudaMalloc.
+ *
+ * d_A: batch x (n x n), d_B / d_X: batch x (n x m), column-major device
+ * buffers (d_X must not overlap d_A or d_B); d_status / d_pivot (optional,
+ * device, batch entries) receive the per-system status code and 1-based
+ * first zero pivot.  Runs asynchronously on `stream` (NULL = legacy default
+ * stream) on the calling thread's current device; results are ready when
+ * the stream reaches them.  The scratch needed is about
+ * batch * roundup(n, 32) * (n + m) * 16 bytes plus small pivot tables (one
+ * system of n = 1200, m = 16 fits); a larger request returns
+ * REFEFF_FMS_ERR_SCRATCH_LIMIT before anything runs.  m <= 64.
+ * First call on each device: looks up the array's address
+ * (cudaGetSymbolAddress) with that device current; make it before any
+ * stream capture.  The array is shared by all calls on a device: calls whose
+ * GPU work overlaps race on it, so order them on one stream or with events. */
+int refeff_complex_lu_solve_device_noalloc(int n, int m, int batch, const refeff_complex128* d_A,
+                                           const refeff_complex128* d_B, refeff_complex128* d_X, int32_t* d_status,
+                                           int32_t* d_pivot, void* stream);
 
 #ifdef __cplusplus
 }

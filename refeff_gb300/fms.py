@@ -28,7 +28,7 @@ STATUS_NAMES = {
     0: "OK", 1: "InvalidArgument", 2: "EmptyCluster", 3: "PotentialOutOfRange", 4: "MissingRepresentativePotential",
     5: "InvalidAngularLimit", 6: "NonFiniteInput", 7: "NonFiniteCoordinate", 8: "ZeroRho", 9: "SingularMatrix",
     10: "NotConverged", 11: "DuplicateAbsorber", 12: "MissingCentralAtom", 13: "Unsupported", 14: "Cuda",
-    15: "OutOfMemory", 16: "InvalidTolerance", 17: "InvalidClusterRadius",
+    15: "OutOfMemory", 16: "InvalidTolerance", 17: "InvalidClusterRadius", 18: "ScratchLimit",
 }
 
 
@@ -371,3 +371,20 @@ def read_phase_bin(path) -> dict:
         raise FmsError(rc, f"cannot read {path}")
     return {"energy_grid": grid, "reference_energy": eref.reshape((ne, nsp), order="F"), "potential_lmax": lmax,
             "phase_shifts": ph.reshape((ne, 2 * lm + 1, nsp, npot), order="F")}
+
+
+NOALLOC_SCRATCH_BYTES = 24 * 1024 * 1024
+
+
+def complex_lu_solve_device_noalloc(n: int, m: int, batch: int, d_A: int, d_B: int, d_X: int, d_status: int = 0,
+                                    d_pivot: int = 0, stream: int = 0) -> None:
+    """Allocation-free FP64 batched solve on device pointers (ints, e.g. torch ``.data_ptr()``), asynchronous on
+    ``stream``; scratch is the library's static device array (NOALLOC_SCRATCH_BYTES).  No reference counterpart."""
+    lib = load()
+    fn = lib.refeff_complex_lu_solve_device_noalloc
+    fn.argtypes = [_i, _i, _i, _p, _p, _p, _p, _p, _p]
+    fn.restype = _i
+    rc = fn(int(n), int(m), int(batch), _p(d_A), _p(d_B), _p(d_X), _p(d_status) if d_status else None,
+            _p(d_pivot) if d_pivot else None, _p(stream) if stream else None)
+    if rc:
+        raise FmsError(rc, "allocation-free dense solve")
