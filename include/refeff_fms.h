@@ -248,6 +248,61 @@ int refeff_fms_phase_bin_dims(const char* path, int* nsp, int* ne, int* npot, in
 int refeff_fms_phase_bin_read(const char* path, refeff_complex128* energy_grid, refeff_complex128* reference_energy,
                               int* potential_lmax, refeff_complex128* phase_shifts);
 
+/* ---- MKGTR: gg -> trace spectrum ---------------------------------------- */
+
+/* FEFF transition B matrix (bcoef; transition_b_matrix,
+ * crates/refeff-core/src/angular/transition.rs:9-73), host only, FP64.
+ * polarization_tensor: 3 x 3 complex, row-major (rows m = -1, 0, 1), may be
+ * NULL when polarization == 0.  bmat_out (optional): (2L+1, 2, 8, 2L+1, 2, 8)
+ * complex column-major, indexed [m2+L, s2, k2, m1+L, s1, k1] with transitions
+ * zero-based; lind_out / kiind_out (optional): 8 orbital momenta (-1 = unused)
+ * and final-state kappas. */
+int refeff_fms_transition_matrix(int lmax, int initial_kappa, int polarization,
+                                 const refeff_complex128* polarization_tensor, int multipole, int trace_orbital,
+                                 int spin, int spin_channels, double spin_vector_angle, refeff_complex128* bmat_out,
+                                 int32_t* lind_out, int32_t* kiind_out);
+
+/* MKGTR trace on the GPU (mkgtr_green_trace, crates/refeff-core/src/fms/mkgtr.rs:790-952):
+ * traces[sp + n_spectra*e] = sum over transitions k1,k2 (lind >= 0), spins s1,s2 < active_spin_channels and
+ * m1, m2 of gg[e]((l1^2+l1+m1) nsp + s1, (l2^2+l2+m2) nsp + s2) * bmat[sp](m2,s2,k2,m1,s1,k1)
+ * * rkk[e,k1,s1] * rkk[e,k2,s2].  lind: n_spectra x 8, bmat: n_spectra blocks as from
+ * refeff_fms_transition_matrix with `lmax`.  Host buffers: gg (E, dim, dim) column-major per
+ * energy, rkk (E, 8, rkk_spins) column-major, traces (n_spectra, E). */
+int refeff_fms_mkgtr_trace(refeff_fms_context* ctx, int n_energies, int dim, int active_spin_channels, int lmax,
+                           int n_spectra, const int32_t* lind, const refeff_complex128* bmat,
+                           const refeff_complex128* gg, const refeff_complex128* rkk, int rkk_spins,
+                           refeff_complex128* traces);
+
+/* The same on device buffers, fusable after refeff_fms_real_space_spectrum_device: gg[e](r, c) =
+ * d_gg[e*gg_energy_stride + r + gg_ld*c] (the scattering tables with gg_ld = C and energy stride
+ * C*C*npot), d_rkk (E, 8, active spins) column-major, d_traces (n_spectra, E).  Synchronises
+ * `stream` (NULL = the context's stream) before returning. */
+int refeff_fms_mkgtr_trace_device(refeff_fms_context* ctx, int n_energies, int dim, int active_spin_channels,
+                                  int lmax, int n_spectra, const int32_t* lind, const refeff_complex128* bmat,
+                                  const refeff_complex128* d_gg, long long gg_ld, long long gg_energy_stride,
+                                  const refeff_complex128* d_rkk, refeff_complex128* d_traces, void* stream);
+
+/* The `mkgtr` stage on a FEFF work directory (run_mkgtr_in_dir + the ordinary
+ * MKGTR outputs, crates/refeff-engine/src/fms.rs:559-600, 5255-5332, 5528-5608):
+ * reads fms.inp, global.inp, phase.bin and gg.bin (else gg.dat); when fms.bin
+ * or gtr.dat is missing, writes both (fms.bin PAD text, io/fms_bin.rs:77-98;
+ * gtr.dat, io/gtr_dat.rs:60-71) from the GPU trace; then makes sure log3.dat
+ * carries the MKGTR lines (fms.rs:5941-5963).  NRIXS (do_nrixs = 1) and EELS
+ * (eels.inp) projections return REFEFF_FMS_ERR_UNSUPPORTED.  *written (optional)
+ * receives the number of trace files written. */
+int refeff_fms_run_mkgtr_dir(refeff_fms_context* ctx, const char* work_dir, int* written);
+
+/* fms.bin writer (fms_bin_string, crates/refeff-io/src/fms_bin.rs:77-98): title
+ * "FMS rfms=%7.4f", counts ne ne1 ne3 nph npadx 0 in I7, then one '$' PAD block
+ * (pad.rs:142-161) per spectrum of traces (n_spectra x ne, column-major).
+ * Host only. */
+int refeff_fms_write_fms_bin(const char* path, double cluster_radius, int ne, int ne1, int ne3, int nph, int pad_width,
+                             int n_spectra, const refeff_complex128* traces);
+
+/* gtr.dat writer (gtr_dat_string, crates/refeff-io/src/gtr_dat.rs:60-71): per
+ * energy Re E, Im E, Re gtr, Im gtr as F13.6.  Host only. */
+int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* energy, const refeff_complex128* trace);
+
 /* ---- dense solve (refeff-linalg boundary) ----------------------------- */
 
 /* Batched dense complex solve A X = B, replacing complex32_faer_lu_factor +

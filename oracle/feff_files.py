@@ -12,6 +12,8 @@ FEFF work directories and check the product's gg.bin / gg.dat byte for byte.
   fms.inp text        crates/refeff-io/src/fms_input.rs:214-246
   global.inp text     crates/refeff-io/src/global_input.rs:108-190
   geom.dat text       crates/refeff-io/src/structure_output.rs:204-223
+  fms.bin text        crates/refeff-io/src/fms_bin.rs:77-98
+  gtr.dat text        crates/refeff-io/src/gtr_dat.rs:60-71
 """
 from __future__ import annotations
 
@@ -196,12 +198,69 @@ def fms_inp_text(*, lmaxph, rfms2, rdirec, toler1=1e-3, toler2=1e-3, idwopt=-1, 
             "do_fms\n" + i4([do_fms]) + "\n")
 
 
-def global_inp_text(ispin: int = 0) -> str:
-    return (" nabs, iphabs - CFAVERAGE data\n" + f"{1:8d}{0:8d}{0.0:13.5f}\n"
-            " ipol, ispin, le2, elpty, angks, l2lp, do_nrixs, ldecmx, lj\n"
-            + f"{0:5d}{ispin:5d}{0:5d}{0.0:12.4f}{0.0:12.4f}{0:5d}{0:5d}{0:5d}{0:5d}\n"
-            "evec\t\t  xivec \t   spvec\n" + "".join(f"{a:13.5f}{b:13.5f}{c:13.5f}\n" for a, b, c in
-                                                  [(0, 1, 0), (0, 0, 0), (1, 0, 1)]))
+def global_inp_text(ispin: int = 0, *, ipol: int = 0, le2: int = 0, elpty: float = 0.0, angks: float = 0.0,
+                    do_nrixs: int = 0, polarization_tensor=None) -> str:
+    """global.inp (crates/refeff-io/src/global_input.rs:108-190) with one q vector; polarization_tensor is 3x3
+    complex (rows m = -1, 0, 1), written as 3 rows of 6 F13.5 fields."""
+    ptz = np.zeros((3, 3), complex) if polarization_tensor is None else np.asarray(polarization_tensor, complex)
+    out = " nabs, iphabs - CFAVERAGE data\n" + f"{1:8d}{0:8d}{0.0:13.5f}\n"
+    out += " ipol, ispin, le2, elpty, angks, l2lp, do_nrixs, ldecmx, lj\n"
+    out += f"{ipol:5d}{ispin:5d}{le2:5d}{elpty:12.4f}{angks:12.4f}{0:5d}{do_nrixs:5d}{-1:5d}{0:5d}\n"
+    out += "evec\t\t  xivec \t   spvec\n"
+    out += "".join(f"{a:13.5f}{b:13.5f}{c:13.5f}\n" for a, b, c in [(0, 1, 0), (0, 0, 0), (1, 0, 1)])
+    out += " polarization tensor \n"
+    for r in range(3):
+        out += "".join(f"{v:13.5f}" for z in ptz[r] for v in (z.real, z.imag)) + "\n"
+    out += "evnorm, xivnorm, spvnorm - only used for nrixs\n" + f"{0.0:13.5f}{0.0:13.5f}{0.0:13.5f}\n"
+    out += "nq,    imdff,   qaverage,   mixdff\n" + f"{1:12d}{0:12d} F F\n"
+    out += " q-vectors : qx, qy, qz, q(norm), weight, qcosth, qsinth, qcosfi, qsinfi\n"
+    out += "".join(f"{v:13.5f}" for v in [0, 0, 0, 0, 1, 0, 1, 0, 0, 1]) + "\n"
+    return out
+
+
+def fms_bin_text(traces, *, cluster_radius, ne1=None, ne3=0, nph, pad_width=8) -> str:
+    """fms.bin (crates/refeff-io/src/fms_bin.rs:77-98); traces (n_spectra, ne)."""
+    tr = np.asarray(traces, complex)
+    ne = tr.shape[1]
+    counts = [ne, ne if ne1 is None else ne1, ne3, nph, pad_width, 0]
+    out = f"FMS rfms={cluster_radius:7.4f}\n" + "".join(f" {c:>7d}" for c in counts) + "\n"
+    for row in tr:
+        out += encode_complex(list(row), pad_width)
+    return out
+
+
+def parse_fms_bin(text: str):
+    """Title radius, counts and the decoded spectra (n_spectra, ne) of an fms.bin."""
+    lines = text.splitlines()
+    radius = float(lines[0].split("=")[1])
+    counts = [int(x) for x in lines[1].split()]
+    ne, npad = counts[0], counts[4]
+    vals = []
+    for line in lines[2:]:
+        p = line[1:]
+        for k in range(0, len(p), 2 * npad):
+            vals.append(complex(pad_decode(p[k:k + npad], npad), pad_decode(p[k + npad:k + 2 * npad], npad)))
+    return radius, counts, np.array(vals).reshape(-1, ne) if ne else np.zeros((0, 0), complex)
+
+
+def gtr_dat_text(energy, trace) -> str:
+    """gtr.dat (crates/refeff-io/src/gtr_dat.rs:60-71)."""
+    return "".join(f"{e.real:13.6f}{e.imag:13.6f}{t.real:13.6f}{t.imag:13.6f}\n" for e, t in zip(energy, trace))
+
+
+def read_rkk(phase_bin: str, *, nsp, ne, ntrans=8):
+    """The q = 0 transition moments (ne, ntrans, nsp) of a phase.bin written by phase_bin_text: the last block."""
+    lines = phase_bin.splitlines()
+    npad = int(lines[0].split()[7])
+    per_line = (82 - 2 * npad + 1 + 2 * npad - 1) // (2 * npad)
+    count = ne * ntrans * nsp
+    nlines = -(-count // per_line)
+    vals = []
+    for line in lines[-nlines:]:
+        p = line[1:]
+        for k in range(0, len(p), 2 * npad):
+            vals.append(complex(pad_decode(p[k:k + npad], npad), pad_decode(p[k + npad:k + 2 * npad], npad)))
+    return np.array(vals[:count]).reshape((ne, ntrans, nsp), order="F")
 
 
 def geom_dat_text(positions, potentials) -> str:
@@ -215,7 +274,7 @@ def geom_dat_text(positions, potentials) -> str:
 
 
 def write_workdir(path: Path, *, positions, potentials, lmaxph, energy_grid, phase_potentials, nsp=1, ispin=0,
-                  rfms2=100.0, rdirec=100.0, sig2g=0.0, do_fms=0, nspu=None):
+                  rfms2=100.0, rdirec=100.0, sig2g=0.0, do_fms=0, nspu=None, global_kw=None):
     path.mkdir(parents=True, exist_ok=True)
     ne = len(energy_grid)
     (path / "phase.bin").write_text(phase_bin_text(nsp=nsp, energy_grid=energy_grid,
@@ -223,15 +282,16 @@ def write_workdir(path: Path, *, positions, potentials, lmaxph, energy_grid, pha
                                                    potentials=phase_potentials))
     (path / "fms.inp").write_text(fms_inp_text(lmaxph=lmaxph, rfms2=rfms2, rdirec=rdirec, sig2g=sig2g,
                                                do_fms=do_fms))
-    (path / "global.inp").write_text(global_inp_text(ispin))
+    (path / "global.inp").write_text(global_inp_text(ispin, **(global_kw or {})))
     (path / "geom.dat").write_text(geom_dat_text(positions, potentials))
     if nspu is not None:
         (path / ".dimensions.dat").write_text(f"{300:12d}{max(lmaxph):12d}{len(lmaxph) - 1:12d}{nspu:12d}\n")
 
 
 def reference_engine_fixture(path: Path):
-    """The reference engine's FMS source fixture (crates/refeff-engine/src/fms/tests.rs:2501-2525, 2821-2875):
-    two atoms 1.4 A apart, two energies, two potentials with lmax 2, lmaxph [1, 1], rfms2 3, rdirec 5."""
+    """The reference engine's FMS source fixture (crates/refeff-engine/src/fms/tests.rs:2381-2421, 2501-2525,
+    2821-2875): two atoms 1.4 A apart, two energies, two potentials with lmax 2, lmaxph [1, 1], rfms2 3, rdirec 5,
+    K edge (ihole 1), isotropic global.inp (ipol 0, ispin 0, le2 0, polarization tensor diag(1/3))."""
     grid = [complex(1.0, 0.02), complex(1.4, 0.03)]
     pots = []
     for p in range(2):
@@ -241,4 +301,5 @@ def reference_engine_fixture(path: Path):
                 ph[e, sl, 0] = complex(0.03 * (p + 1) + 0.01 * e + 0.02 * sl, 0.004 * (sl + 1))
         pots.append((2, 29, "Cu", ph))
     write_workdir(path, positions=[[0, 0, 0], [1.4, 0, 0]], potentials=[0, 1], lmaxph=[1, 1], energy_grid=grid,
-                  phase_potentials=pots, rfms2=3.0, rdirec=5.0)
+                  phase_potentials=pots, rfms2=3.0, rdirec=5.0,
+                  global_kw={"polarization_tensor": np.eye(3) / 3.0})

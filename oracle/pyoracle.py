@@ -24,7 +24,8 @@ _lib = None
 
 def build(force: bool = False) -> Path:
     """Compile the oracle with its Makefile (g++, OpenMP, -ffp-contract=off)."""
-    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < (HERE / "fms_oracle.cpp").stat().st_mtime:
+    newest = max((HERE / f).stat().st_mtime for f in ("fms_oracle.cpp", "mkgtr_oracle.cpp", "Makefile"))
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < newest:
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB_PATH
 
@@ -63,6 +64,8 @@ def _declare(L):
         "oracle_xgllm": [_i, _i, _i, _i, _i, _p, _p],
         "oracle_t_matrix_element": [_i, _i, _i, _i, _i, _p, _p, _p, _i, _p],
         "oracle_free_propagator_element": [_i, _i, _i, _p, _p, _p, _p, _d, _p, _p, _p, _p],
+        "oracle_transition_b_matrix": [_i, _i, _i, _p, _i, _i, _i, _i, _d, _p, _p, _p],
+        "oracle_mkgtr_trace": [_i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -72,6 +75,10 @@ def _declare(L):
     L.oracle_legendre_normalization.restype = _d
     L.oracle_spin_orbit_coefficient.argtypes = [_i, _i, _i, _i]
     L.oracle_spin_orbit_coefficient.restype = _d
+    L.oracle_wigner_3j.argtypes = [_i, _i, _i, _i, _i, _i]
+    L.oracle_wigner_3j.restype = _d
+    L.oracle_wigner_rotation.argtypes = [_d, _i, _i, _i, _i]
+    L.oracle_wigner_rotation.restype = _d
 
 
 def ptr(a: np.ndarray | None):
@@ -159,3 +166,36 @@ def lu_factor_solve(A, B, mode=F64):
 
 def threads_available() -> int:
     return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def transition_b_matrix(*, lmax, initial_kappa, polarization, polarization_tensor, multipole, trace_orbital=False,
+                        spin=1, spin_channels=1, spin_vector_angle=0.0):
+    """FEFF bcoef (crates/refeff-core/src/angular/transition.rs:9-73): returns (bmat, lind, kiind) with bmat of
+    shape (2L+1, 2, 8, 2L+1, 2, 8) indexed [m2+L, s2, k2, m1+L, s1, k1] (transitions zero-based)."""
+    ML = 2 * lmax + 1
+    out = np.zeros(2 * ML * 2 * 8 * ML * 2 * 8)
+    ptz = np.ascontiguousarray(np.asarray(polarization_tensor, dtype=np.complex128).reshape(3, 3)).view(np.float64)
+    lind = np.zeros(8, np.int32)
+    kiind = np.zeros(8, np.int32)
+    check(lib().oracle_transition_b_matrix(int(lmax), int(initial_kappa), int(polarization), ptr(ptz),
+                                           int(multipole), int(bool(trace_orbital)), int(spin), int(spin_channels),
+                                           float(spin_vector_angle), ptr(out), ptr(lind), ptr(kiind)))
+    bm = out.view(np.complex128).reshape((ML, 2, 8, ML, 2, 8), order="F")
+    return bm, lind, kiind
+
+
+def mkgtr_trace(gg, bmats, lind, rkk, *, nsp, lmax):
+    """getgtr trace (crates/refeff-core/src/fms/mkgtr.rs:790-952): gg (E, dim, dim), bmats list of (2L+1,2,8,2L+1,2,8),
+    lind list of 8-int arrays, rkk (E, 8, nsp_rkk) -> traces (nspec, E)."""
+    gg = np.asarray(gg, np.complex128)
+    E, dim, _ = gg.shape
+    g = np.ascontiguousarray(np.stack([gg[e].reshape(-1, order="F") for e in range(E)])).view(np.float64)
+    b = np.ascontiguousarray(np.concatenate([np.asarray(x, np.complex128).reshape(-1, order="F") for x in bmats]))
+    li = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int32) for x in lind]))
+    rk = np.asarray(rkk, np.complex128)
+    r = np.ascontiguousarray(rk.reshape(-1, order="F")).view(np.float64)
+    nspec = len(bmats)
+    out = np.zeros(2 * nspec * E)
+    check(lib().oracle_mkgtr_trace(E, dim, int(nsp), int(lmax), nspec, ptr(li), ptr(b.view(np.float64)), ptr(g),
+                                   ptr(r), int(rk.shape[2]), ptr(out)))
+    return out.view(np.complex128).reshape((nspec, E), order="F")

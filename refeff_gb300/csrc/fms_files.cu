@@ -230,6 +230,8 @@ struct PadCursor {
 
 struct PhaseBin {
   int nsp = 0, ne = 0, npot = 0, npad = 0;
+  int ne1 = 0, ne3 = 0, ihole = 0, ntrans = 8, nq = 1;
+  std::vector<refeff_complex128> rkk;   // q = 0 transition moments (energy, transition, spin), energy fastest
   std::vector<refeff_complex128> em;    // ne
   std::vector<refeff_complex128> eref;  // ne x nsp, energy fastest
   std::vector<int> lmax;                // per potential
@@ -249,8 +251,14 @@ int read_phase_bin(const std::string& path, PhaseBin& pb, std::string& err) {
     if (!parse_int(h[i], v[i])) { err = "bad phase.bin header field " + h[i]; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
   pb.nsp = int(v[0]);
   pb.ne = int(v[1]);
+  pb.ne1 = int(v[2]);
+  pb.ne3 = int(v[3]);
   pb.npot = int(v[4]) + 1;
+  pb.ihole = int(v[5]);
   pb.npad = int(v[7]);
+  if (h.size() >= 10) pb.ntrans = int(v[9]);  // indmax (parse.rs:31-46)
+  if (h.size() == 11) pb.nq = int(v[10]);
+  if (pb.ntrans < 0 || pb.nq < 1) { err = "phase.bin transition counts out of range"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
   if (pb.nsp < 1 || pb.nsp > 2 || pb.ne < 0 || pb.npot < 1 || pb.npad <= 2) { err = "phase.bin header out of range"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
   PadCursor cur{lines, 1, ""};
   std::vector<double> dum;
@@ -278,6 +286,14 @@ int read_phase_bin(const std::string& path, PhaseBin& pb, std::string& err) {
       for (int e = 0; e < pb.ne; ++e)
         for (int l = 0; l < lc; ++l) tab[size_t(e) + size_t(pb.ne) * (size_t(l) + size_t(lc) * s)] = blk[idx++];
     }
+  }
+  // transition moments, one block per q (parse.rs:88-100, 156-180): spin outer,
+  // transition, energy inner -- the order of the (energy, transition, spin)
+  // column-major table kept here for q = 0
+  for (int q = 0; q < pb.nq; ++q) {
+    std::vector<refeff_complex128> blk;
+    if (!cur.complex_block(pb.npad, size_t(pb.ne) * pb.ntrans * pb.nsp, blk)) { err = cur.error; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+    if (q == 0) pb.rkk = std::move(blk);
   }
   return REFEFF_FMS_OK;
 }
@@ -479,6 +495,7 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   FmsInp fi;
   int rc = parse_fms_inp(dir + "fms.inp", fi, err);
   if (rc) { set_error(ctx, err); return rc; }
+  if (fi.mfms == 0) return REFEFF_FMS_OK;  // fms_enabled (fms.rs:633-635): the stage is off
   PhaseBin pb;
   rc = read_phase_bin(dir + "phase.bin", pb, err);
   if (rc) { set_error(ctx, err); return rc; }
@@ -643,5 +660,296 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
     set_error(ctx, "cannot write log3.dat");
     return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   }
+  return REFEFF_FMS_OK;
+}
+
+// ===========================================================================
+// MKGTR stage: gg.bin + phase.bin + global.inp -> fms.bin, gtr.dat, log3.dat
+// ===========================================================================
+namespace {
+
+// PAD encoding of one value in `npack` characters (pad.rs:33-93): base-90
+// digits offset by 37, a decimal exponent byte and a sign folded into the
+// second byte, round-half-up in the last digit.
+std::string pad_encode(double value, int npack) {
+  const double huge = powi_squaring(10.0, 38), tiny = 1.0 / huge;
+  std::string out(size_t(npack), ' ');
+  const double xsave = value < -huge ? -huge : (value > huge ? huge : value);
+  const int isgn = xsave > 0.0 ? 1 : 0;
+  double xwork = std::fabs(xsave);
+  int iexp = 0;
+  if (xwork < huge && xwork > tiny) iexp = 1 + int(std::log(xwork) / 2.3025850929940455);
+  else if (xwork >= huge) { iexp = 38; xwork = 1.0; }
+  else if (xwork <= tiny) xwork = 0.0;
+  xwork /= powi_squaring(10.0, iexp);
+  do {
+    if (xwork >= 1.0) { xwork *= 0.1; ++iexp; }
+    else if (xwork <= 0.099999999994) { xwork *= 10.0; --iexp; }
+  } while (xwork >= 1.0);
+  int itmp = int(double(kPadHalf) * xwork);
+  out[0] = char(iexp + kPadOff + kPadHalf);
+  out[1] = char(2 * itmp + isgn + kPadOff);
+  xwork = xwork * double(kPadHalf) - double(itmp);
+  for (int i = 2; i < npack; ++i) {
+    itmp = int(double(kPadBase) * xwork + 1.0e-9);
+    out[size_t(i)] = char(itmp + kPadOff);
+    xwork = xwork * double(kPadBase) - double(itmp);
+  }
+  if (xwork >= 0.5) {
+    const int up = itmp + kPadOff + 1;
+    if (up <= 126) out[size_t(npack) - 1] = char(up);
+    else if (static_cast<unsigned char>(out[size_t(npack) - 2]) < 126) {
+      out[size_t(npack) - 2] = char(static_cast<unsigned char>(out[size_t(npack) - 2]) + 1);
+      out[size_t(npack) - 1] = char(37);
+    }
+  }
+  return out;
+}
+
+// '$' lines of complex PAD pairs, flushed once the payload reaches 82 - 2 npack + 1 (pad.rs:142-161).
+std::string pad_complex_lines(const refeff_complex128* v, size_t n, int npack) {
+  std::string out, payload;
+  const size_t maxp = size_t(82 - 2 * npack + 1);
+  for (size_t i = 0; i < n; ++i) {
+    payload += pad_encode(v[i].re, npack);
+    payload += pad_encode(v[i].im, npack);
+    if (payload.size() >= maxp || i + 1 == n) {
+      out += '$';
+      out += payload;
+      out += '\n';
+      payload.clear();
+    }
+  }
+  return out;
+}
+
+struct GlobalInp {
+  int ipol = 0, ispin = 0, le2 = 0, do_nrixs = 0;
+  double elpty = 0.0, angks = 0.0;
+  double ptz[3][6] = {};
+};
+
+// global.inp control line and polarization tensor (global_input.rs:314-345).
+int parse_global_inp(const std::string& path, GlobalInp& g, std::string& err) {
+  std::string text;
+  if (!read_file(path, text)) { err = "cannot read " + path; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+  const auto L = split_lines(text);
+  bool ctl = false, pol = false;
+  for (size_t i = 0; i + 1 < L.size(); ++i) {
+    const std::string h = trim(L[i]);
+    if (!ctl && h == "ipol, ispin, le2, elpty, angks, l2lp, do_nrixs, ldecmx, lj") {
+      const auto fs = fields(L[i + 1]);
+      double x[7];
+      if (fs.size() < 7) { err = "global.inp: short control line"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+      for (int k = 0; k < 7; ++k)
+        if (!parse_double(fs[size_t(k)], x[k])) { err = "global.inp: bad control value"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+      g.ipol = int(x[0]); g.ispin = int(x[1]); g.le2 = int(x[2]); g.elpty = x[3]; g.angks = x[4]; g.do_nrixs = int(x[6]);
+      ctl = true;
+    } else if (!pol && h == "polarization tensor") {
+      if (i + 3 >= L.size()) { err = "global.inp: polarization tensor truncated"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+      for (int r = 0; r < 3; ++r) {
+        const auto fs = fields(L[i + 1 + size_t(r)]);
+        if (fs.size() < 6) { err = "global.inp: short polarization row"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+        for (int c = 0; c < 6; ++c)
+          if (!parse_double(fs[size_t(c)], g.ptz[r][c])) { err = "global.inp: bad polarization value"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+      }
+      pol = true;
+    }
+  }
+  if (!ctl || !pol) { err = "global.inp: control line or polarization tensor missing"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+  return REFEFF_FMS_OK;
+}
+
+// gg.bin / gg.dat sections (gg_dat.rs:92-150): '#' header lines, '#DT#' sizes,
+// then rows of (re, im) pairs.
+int parse_gg_sections(const std::string& path, int& dim, std::vector<refeff_complex128>& vals, int& count,
+                      std::string& err) {
+  std::string text;
+  if (!read_file(path, text)) { err = "cannot read " + path; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+  const auto L = split_lines(text);
+  dim = -1;
+  count = 0;
+  vals.clear();
+  int rows = 0, cols = 0, got = 0;
+  bool open = false;
+  for (const auto& line : L) {
+    const std::string t = trim(line);
+    if (t.empty()) continue;
+    if (t[0] == '#') {
+      if (t.compare(0, 4, "#SN#") == 0) {
+        if (open && got != rows) { err = "gg section ended early"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+        open = true; rows = cols = got = 0;
+        ++count;
+      } else if (t.compare(0, 4, "#DT#") == 0) {
+        const auto fs = fields(t);
+        long long r = 0, c = 0;
+        if (fs.size() < 2 || !parse_int(fs[fs.size() - 2], r) || !parse_int(fs[fs.size() - 1], c) || r <= 0 || r != c) {
+          err = "gg sections must be nonempty square matrices";
+          return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+        }
+        rows = int(r); cols = int(c);
+        if (dim < 0) dim = rows;
+        if (dim != rows) { err = "gg section shapes differ"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+        vals.resize(size_t(count) * dim * dim);
+      }
+      continue;
+    }
+    if (!open || rows == 0 || got >= rows) { err = "gg data row outside a section"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+    const auto fs = fields(t);
+    if (fs.size() != size_t(2 * cols)) { err = "gg row has the wrong number of values"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+    refeff_complex128* sec = vals.data() + size_t(count - 1) * dim * dim;
+    for (int c = 0; c < cols; ++c) {
+      refeff_complex128 v;
+      if (!parse_double(fs[size_t(2 * c)], v.re) || !parse_double(fs[size_t(2 * c + 1)], v.im)) {
+        err = "bad gg value";
+        return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+      }
+      sec[size_t(got) + size_t(dim) * c] = v;
+    }
+    ++got;
+  }
+  if (count == 0 || dim <= 0 || got != rows) { err = "gg file holds no complete section"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+  return REFEFF_FMS_OK;
+}
+
+// core_hole_quantum_numbers (crates/refeff-core/src/core_hole.rs:66-83): FEFF hole index -> kappa.
+bool core_hole_kappa(int ihole, int& kappa) {
+  switch (ihole) {
+    case 1: case 2: case 5: case 10: case 17: case 24: case 29: kappa = -1; return true;
+    case 3: case 6: case 11: case 18: case 25: case 30: kappa = 1; return true;
+    case 4: case 7: case 12: case 19: case 26: kappa = -2; return true;
+    case 8: case 13: case 20: case 27: kappa = 2; return true;
+    case 9: case 14: case 21: case 28: kappa = -3; return true;
+    case 15: case 22: kappa = 3; return true;
+    case 16: case 23: kappa = -4; return true;
+    default: return false;
+  }
+}
+
+bool file_exists(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  return bool(f);
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_write_fms_bin(const char* path, double cluster_radius, int ne, int ne1, int ne3, int nph,
+                                        int pad_width, int n_spectra, const refeff_complex128* traces) {
+  if (!path || ne < 0 || ne1 < 0 || ne3 < 0 || nph < 0 || pad_width <= 2 || pad_width > 40 || n_spectra < 0 ||
+      (n_spectra > 0 && ne > 0 && !traces))
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  // fms_bin_string (fms_bin.rs:77-98): title, six counts in I7 (nip declared 0), one PAD block per spectrum
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "FMS rfms=%7.4f\n", cluster_radius);
+  std::string out = buf;
+  const long long counts[6] = {ne, ne1, ne3, nph, pad_width, 0};
+  for (long long c : counts) {
+    std::snprintf(buf, sizeof buf, " %7lld", c);
+    out += buf;
+  }
+  out += '\n';
+  for (int sp = 0; sp < n_spectra; ++sp) {
+    std::vector<refeff_complex128> row(static_cast<size_t>(ne));
+    for (int e = 0; e < ne; ++e) row[size_t(e)] = traces[size_t(sp) + size_t(n_spectra) * e];
+    out += pad_complex_lines(row.data(), row.size(), pad_width);
+  }
+  return write_file_atomic(path, out) ? REFEFF_FMS_OK : REFEFF_FMS_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* energy,
+                                        const refeff_complex128* trace) {
+  if (!path || ne < 0 || (ne > 0 && (!energy || !trace))) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  // gtr_dat_string (gtr_dat.rs:60-71): four F13.6 fields per energy
+  std::string out;
+  char buf[128];
+  for (int e = 0; e < ne; ++e) {
+    std::snprintf(buf, sizeof buf, "%13.6f%13.6f%13.6f%13.6f\n", energy[e].re, energy[e].im, trace[e].re, trace[e].im);
+    out += buf;
+  }
+  return write_file_atomic(path, out) ? REFEFF_FMS_OK : REFEFF_FMS_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int refeff_fms_run_mkgtr_dir(refeff_fms_context* ctx, const char* work_dir, int* written) {
+  if (!ctx || !work_dir) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (written) *written = 0;
+  const std::string dir = std::string(work_dir) + "/";
+  std::string err;
+  FmsInp fi;
+  int rc = parse_fms_inp(dir + "fms.inp", fi, err);
+  if (rc) { set_error(ctx, err); return rc; }
+  if (fi.mfms == 0) return REFEFF_FMS_OK;  // fms_enabled (fms.rs:633-635)
+  const std::string gg_path = file_exists(dir + "gg.bin") ? dir + "gg.bin" : dir + "gg.dat";
+  if (!file_exists(gg_path)) { set_error(ctx, "MKGTR requires gg.bin or gg.dat from the FMS stage"); return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+  if (!file_exists(dir + "phase.bin") || !file_exists(dir + "global.inp")) return REFEFF_FMS_OK;
+  GlobalInp gi;
+  rc = parse_global_inp(dir + "global.inp", gi, err);
+  if (rc) { set_error(ctx, err); return rc; }
+  if (gi.do_nrixs == 1) { set_error(ctx, "NRIXS (JAS) MKGTR projections are not supported"); return REFEFF_FMS_ERR_UNSUPPORTED; }
+  if (file_exists(dir + "eels.inp")) { set_error(ctx, "EELS MKGTR projections are not supported"); return REFEFF_FMS_ERR_UNSUPPORTED; }
+  int produced = 0;
+  if (!file_exists(dir + "fms.bin") || !file_exists(dir + "gtr.dat")) {
+    PhaseBin pb;
+    rc = read_phase_bin(dir + "phase.bin", pb, err);
+    if (rc) { set_error(ctx, err); return rc; }
+    int dim = 0, count = 0;
+    std::vector<refeff_complex128> gg;
+    rc = parse_gg_sections(gg_path, dim, gg, count, err);
+    if (rc) { set_error(ctx, err); return rc; }
+    if (count != pb.ne) { set_error(ctx, "gg section count does not match the phase.bin energy count"); return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+    // green_functions_from_gg (fms.rs:5883-5918): the cached values narrowed to complex64
+    for (auto& v : gg) {
+      const float re = float(v.re), im = float(v.im);
+      if (!std::isfinite(v.re) || !std::isfinite(v.im) || !std::isfinite(re) || !std::isfinite(im)) {
+        set_error(ctx, "non-finite gg value");
+        return REFEFF_FMS_ERR_NONFINITE_INPUT;
+      }
+      v = {double(re), double(im)};
+    }
+    if (fi.lmaxph.empty() || fi.lmaxph[0] < 0) { set_error(ctx, "fms.inp lmaxph(0) must be nonnegative"); return REFEFF_FMS_ERR_INVALID_ANGULAR_LIMIT; }
+    const int lmax = fi.lmaxph[0];
+    const int active = (gi.ispin == 1 || gi.ispin == -1) ? pb.nsp : 1;  // active_spin_channels (fms.rs:5860-5869)
+    int kappa = 0;
+    if (!core_hole_kappa(pb.ihole, kappa)) { set_error(ctx, "phase.bin ihole has no core-hole kappa"); return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+    if (pb.ntrans < 8) { set_error(ctx, "phase.bin carries fewer than 8 transition moments"); return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+    refeff_complex128 ptz[9];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) ptz[3 * r + c] = {gi.ptz[r][2 * c], gi.ptz[r][2 * c + 1]};
+    const int nm = 2 * lmax + 1;
+    std::vector<refeff_complex128> bmat(size_t(nm) * 2 * 8 * nm * 2 * 8);
+    int32_t lind[8], kiind[8];
+    rc = rfx::mkgtr_transition_matrix(lmax, kappa, gi.ipol, ptz, gi.le2, 0, gi.ispin, pb.nsp, gi.angks, bmat.data(),
+                                      lind, kiind);
+    if (rc) { set_error(ctx, "transition matrix"); return rc; }
+    // rkk (energy, transition, spin) with the first 8 transitions
+    std::vector<refeff_complex128> rkk(size_t(pb.ne) * 8 * pb.nsp);
+    for (int sp = 0; sp < pb.nsp; ++sp)
+      for (int k = 0; k < 8; ++k)
+        for (int e = 0; e < pb.ne; ++e)
+          rkk[size_t(e) + size_t(pb.ne) * (size_t(k) + 8 * size_t(sp))] =
+              pb.rkk[size_t(e) + size_t(pb.ne) * (size_t(k) + size_t(pb.ntrans) * sp)];
+    std::vector<refeff_complex128> traces(size_t(pb.ne));
+    rc = refeff_fms_mkgtr_trace(ctx, pb.ne, dim, active, lmax, 1, lind, bmat.data(), gg.data(), rkk.data(), pb.nsp,
+                                traces.data());
+    if (rc) return rc;
+    if (refeff_fms_write_fms_bin((dir + "fms.bin").c_str(), fi.rfms2, pb.ne, pb.ne1, pb.ne3, pb.npot - 1, pb.npad, 1,
+                                 traces.data()) != REFEFF_FMS_OK ||
+        refeff_fms_write_gtr_dat((dir + "gtr.dat").c_str(), pb.ne, pb.em.data(), traces.data()) != REFEFF_FMS_OK) {
+      set_error(ctx, "cannot write fms.bin / gtr.dat");
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+    produced = 2;
+  }
+  // ensure_mkgtr_module_log (fms.rs:5941-5963)
+  std::string log;
+  if (!read_file(dir + "log3.dat", log))
+    log = "FMS calculation of full Green's function ...\nFEFF-serial using 1 thread.\nDone with module: FMS.\n";
+  if (log.find("Done with module: MKGTR.") == std::string::npos) {
+    log += "\nMKGTR: Tracing over Green's function ...\nDone with module: MKGTR.\n";
+    if (!write_file_atomic(dir + "log3.dat", log)) {
+      set_error(ctx, "cannot write log3.dat");
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+  }
+  if (written) *written = produced;
   return REFEFF_FMS_OK;
 }

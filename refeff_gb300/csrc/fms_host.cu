@@ -53,6 +53,9 @@ void rfx::set_last_error(refeff_fms_context* ctx, const std::string& msg) {
   if (ctx) ctx->last_error = msg;
 }
 
+int rfx::context_device(const refeff_fms_context* ctx) { return ctx->device; }
+cudaStream_t rfx::context_stream(const refeff_fms_context* ctx) { return ctx->stream; }
+
 extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value) {
   if (!ctx) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   switch (option) {

@@ -110,6 +110,13 @@ def load(build_if_missing: bool = True):
         "refeff_fms_write_gg_dat": ([C.c_char_p, _i, _i, _p], _i),
         "refeff_fms_phase_bin_dims": ([C.c_char_p, _p, _p, _p, _p], _i),
         "refeff_fms_phase_bin_read": ([C.c_char_p, _p, _p, _p, _p], _i),
+        "refeff_fms_transition_matrix": ([_i, _i, _i, _p, _i, _i, _i, _i, C.c_double, _p, _p, _p], _i),
+        "refeff_fms_mkgtr_trace": ([_p, _i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p], _i),
+        "refeff_fms_mkgtr_trace_device": ([_p, _i, _i, _i, _i, _i, _p, _p, _p, C.c_longlong, C.c_longlong, _p, _p,
+                                           _p], _i),
+        "refeff_fms_run_mkgtr_dir": ([_p, C.c_char_p, _p], _i),
+        "refeff_fms_write_fms_bin": ([C.c_char_p, C.c_double, _i, _i, _i, _i, _i, _i, _p], _i),
+        "refeff_fms_write_gtr_dat": ([C.c_char_p, _i, _p, _p], _i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -388,3 +395,88 @@ def complex_lu_solve_device_noalloc(n: int, m: int, batch: int, d_A: int, d_B: i
             _p(d_pivot) if d_pivot else None, _p(stream) if stream else None)
     if rc:
         raise FmsError(rc, "allocation-free dense solve")
+
+
+def transition_matrix(*, lmax, initial_kappa, polarization, polarization_tensor=None, multipole=1,
+                      trace_orbital=False, spin=1, spin_channels=1, spin_vector_angle=0.0):
+    """FEFF bcoef (transition_b_matrix, crates/refeff-core/src/angular/transition.rs:9-73).
+
+    Returns (bmat, lind, kiind); bmat has shape (2L+1, 2, 8, 2L+1, 2, 8) indexed [m2+L, s2, k2, m1+L, s1, k1]."""
+    lib = load()
+    ML = 2 * lmax + 1
+    out = np.zeros(ML * 2 * 8 * ML * 2 * 8, np.complex128)
+    ptz = None if polarization_tensor is None else np.ascontiguousarray(
+        np.asarray(polarization_tensor, np.complex128).reshape(3, 3))
+    lind = np.zeros(8, np.int32)
+    kiind = np.zeros(8, np.int32)
+    rc = lib.refeff_fms_transition_matrix(int(lmax), int(initial_kappa), int(polarization), _ptr(ptz), int(multipole),
+                                          int(bool(trace_orbital)), int(spin), int(spin_channels),
+                                          float(spin_vector_angle), _ptr(out), _ptr(lind), _ptr(kiind))
+    if rc:
+        raise FmsError(rc, "transition matrix")
+    return out.reshape((ML, 2, 8, ML, 2, 8), order="F"), lind, kiind
+
+
+def mkgtr_trace(ctx: Context, gg, bmats, linds, rkk, *, active_spin_channels, lmax):
+    """getgtr trace on the GPU (crates/refeff-core/src/fms/mkgtr.rs:790-952).
+
+    gg (E, dim, dim), bmats / linds one per spectrum, rkk (E, 8, nsp) -> traces (n_spectra, E)."""
+    gg = np.asarray(gg, np.complex128)
+    E, dim, _ = gg.shape
+    g = np.ascontiguousarray(np.stack([gg[e].reshape(-1, order="F") for e in range(E)]))
+    b = np.ascontiguousarray(np.concatenate([np.asarray(x, np.complex128).reshape(-1, order="F") for x in bmats]))
+    li = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int32) for x in linds]))
+    rk = np.asarray(rkk, np.complex128)
+    r = np.ascontiguousarray(rk.reshape(-1, order="F"))
+    nspec = len(bmats)
+    out = np.zeros(nspec * E, np.complex128)
+    rc = ctx._lib.refeff_fms_mkgtr_trace(ctx.handle, E, dim, int(active_spin_channels), int(lmax), nspec, _ptr(li),
+                                         _ptr(b), _ptr(g), _ptr(r), int(rk.shape[2]), _ptr(out))
+    if rc:
+        raise FmsError(rc, ctx.last_error())
+    return out.reshape((nspec, E), order="F")
+
+
+def mkgtr_trace_device(ctx: Context, n_energies, dim, active_spin_channels, lmax, bmats, linds, d_gg: int, gg_ld,
+                       gg_energy_stride, d_rkk: int, d_traces: int, stream: int = 0):
+    """Device-pointer trace (pointers as ints), reading gg[e](r, c) = d_gg[e*stride + r + ld*c]."""
+    b = np.ascontiguousarray(np.concatenate([np.asarray(x, np.complex128).reshape(-1, order="F") for x in bmats]))
+    li = np.ascontiguousarray(np.concatenate([np.asarray(x, np.int32) for x in linds]))
+    rc = ctx._lib.refeff_fms_mkgtr_trace_device(ctx.handle, int(n_energies), int(dim), int(active_spin_channels),
+                                                int(lmax), len(bmats), _ptr(li), _ptr(b), _p(d_gg), int(gg_ld),
+                                                int(gg_energy_stride), _p(d_rkk), _p(d_traces),
+                                                _p(stream) if stream else None)
+    if rc:
+        raise FmsError(rc, ctx.last_error())
+
+
+def run_mkgtr_in_dir(ctx: Context, work_dir) -> int:
+    """The `mkgtr` stage on a FEFF work directory (run_mkgtr_in_dir, crates/refeff-engine/src/fms.rs:559-632):
+    gg.bin + phase.bin + global.inp -> fms.bin, gtr.dat, log3.dat.  Returns the number of trace files written."""
+    n = C.c_int()
+    rc = ctx._lib.refeff_fms_run_mkgtr_dir(ctx.handle, str(work_dir).encode(), C.byref(n))
+    if rc:
+        raise FmsError(rc, ctx.last_error())
+    return n.value
+
+
+def write_fms_bin(path, traces, *, cluster_radius, ne1=None, ne3=0, nph, pad_width=8) -> None:
+    """FEFF fms.bin text (crates/refeff-io/src/fms_bin.rs:77-98); traces (n_spectra, ne)."""
+    lib = load()
+    tr = np.asarray(traces, np.complex128)
+    nspec, ne = tr.shape
+    flat = np.ascontiguousarray(tr.reshape(-1, order="F"))
+    rc = lib.refeff_fms_write_fms_bin(str(path).encode(), float(cluster_radius), ne, ne if ne1 is None else int(ne1),
+                                      int(ne3), int(nph), int(pad_width), nspec, _ptr(flat))
+    if rc:
+        raise FmsError(rc, f"cannot write {path}")
+
+
+def write_gtr_dat(path, energy, trace) -> None:
+    """FEFF gtr.dat text (crates/refeff-io/src/gtr_dat.rs:60-71)."""
+    lib = load()
+    e = np.ascontiguousarray(energy, np.complex128)
+    t = np.ascontiguousarray(trace, np.complex128)
+    rc = lib.refeff_fms_write_gtr_dat(str(path).encode(), len(e), _ptr(e), _ptr(t))
+    if rc:
+        raise FmsError(rc, f"cannot write {path}")
