@@ -88,6 +88,8 @@ enum : int {
   ERR_MISSING_REPRESENTATIVE = -9,
   ERR_CENTRAL_MISMATCH = -10,
   ERR_INVALID_ARGUMENT = -11,
+  ERR_BREAKDOWN = -12,       // FmsError::IterativeSolverBreakdown
+  ERR_NO_CONVERGENCE = -13,  // FmsError::IterativeSolverNoConvergence
 };
 
 struct Atom {
@@ -822,6 +824,375 @@ inline void iterative_system_matrix(const Plan<R>& P, const std::vector<cx<R>>& 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Iterative FMS solvers (minv != 0).  crates/refeff-core/src/fms/solvers.rs:10-78,
+// 225-357 and internals/iterative.rs:24-612, with the vector helpers of
+// internals/linear.rs:3-101.  Each solver returns the solution of W x = e_src.
+// ---------------------------------------------------------------------------
+template <typename R>
+inline cx<R> conj(cx<R> a) { return {a.re, -a.im}; }
+
+// num-complex sqrt: special cases on the axes, else the polar form.
+template <typename R>
+inline cx<R> csqrt(cx<R> z) {
+  if (z.im == R(0)) {
+    if (!std::signbit(z.re)) return {std::sqrt(z.re), z.im};
+    const R r = std::sqrt(-z.re);
+    return {R(0), std::signbit(z.im) ? -r : r};
+  }
+  if (z.re == R(0)) {
+    const R x = std::sqrt(std::fabs(z.im) / R(2));
+    return {x, std::signbit(z.im) ? -x : x};
+  }
+  const R r = std::hypot(z.re, z.im), th = std::atan2(z.im, z.re);
+  const R sr = std::sqrt(r), h = th / R(2);
+  return {sr * std::cos(h), sr * std::sin(h)};
+}
+
+template <typename R>
+inline cx<R> cdot(const std::vector<cx<R>>& a, const std::vector<cx<R>>& b) {
+  cx<R> s;
+  for (size_t i = 0; i < a.size(); ++i) s = s + conj(a[i]) * b[i];
+  return s;
+}
+
+template <typename R>
+inline std::vector<cx<R>> matvec(const std::vector<cx<R>>& W, const std::vector<cx<R>>& v) {
+  const size_t n = v.size();
+  std::vector<cx<R>> y(n);
+  for (size_t c = 0; c < n; ++c)
+    for (size_t r = 0; r < n; ++r) y[r] += W[r + n * c] * v[c];
+  return y;
+}
+
+template <typename R>
+inline std::vector<cx<R>> adj_matvec(const std::vector<cx<R>>& W, const std::vector<cx<R>>& v) {
+  const size_t n = v.size();
+  std::vector<cx<R>> y(n);
+  for (size_t c = 0; c < n; ++c)
+    for (size_t r = 0; r < n; ++r) y[c] += conj(W[r + n * c]) * v[r];
+  return y;
+}
+
+template <typename R>
+inline bool within(const std::vector<cx<R>>& v, R tol) {
+  for (const auto& x : v)
+    if (!(std::fabs(x.re) <= tol && std::fabs(x.im) <= tol)) return false;
+  return true;
+}
+
+struct Breakdown {};
+template <typename R> inline void nz(cx<R> v) { if (is_zero(v)) throw Breakdown{}; }
+template <typename R> inline cx<R> cdivc(cx<R> a, cx<R> b) { nz(b); return a / b; }
+template <typename R> inline R pos(R v) { if (!(std::isfinite(v) && v > R(0))) throw Breakdown{}; return v; }
+template <typename R> inline R nonneg(R v) { if (!(std::isfinite(v) && v >= R(0))) throw Breakdown{}; return v; }
+template <typename R> inline R scaled(R tol, R scale) {
+  const R s = tol * scale;
+  if (!(std::isfinite(s) && s >= R(0))) throw Breakdown{};
+  return s;
+}
+
+// FEFF ggbi: one BiCGSTAB step that returns after the first update.
+template <typename R>
+int bicgstab(const std::vector<cx<R>>& W, size_t src, R tol, std::vector<cx<R>>& x, int& ord) {
+  ord = 0;
+  const size_t n = x.size();
+  const cx<R> zero;
+  std::fill(x.begin(), x.end(), zero);
+  std::vector<cx<R>> r(n);
+  r[src] = cx<R>(R(1), R(0));
+  if (within(r, tol)) return OK;
+  std::vector<cx<R>> p = r, a = matvec(W, p);
+  ++ord;
+  cx<R> aa = cdot(a, a), wa = cdot(r, a), aw = conj(wa), ww = cdot(r, r);
+  nz(aa);
+  nz(ww);
+  const cx<R> dd = aa * ww - aw * wa;
+  const cx<R> sdd = cdivc(cdivc(dd, aa), ww);
+  std::vector<cx<R>> y(n);
+  if (cnorm(sdd) < R(1.0e-8)) {
+    for (size_t i = 0; i < n; ++i) y[i] = r[i] / ww;
+  } else {
+    nz(dd);
+    ww = (ww - aw) / dd;
+    aa = (wa - aa) / dd;
+    for (size_t i = 0; i < n; ++i) y[i] = r[i] * aa + a[i] * ww;
+  }
+  const cx<R> del = cdot(y, r), delp = cdot(y, a);
+  const cx<R> omega = cdivc(del, delp);
+  std::vector<cx<R>> sv(n);
+  for (size_t i = 0; i < n; ++i) sv[i] = r[i] - omega * a[i];
+  if (within(sv, tol)) {
+    for (size_t i = 0; i < n; ++i) x[i] += omega * p[i];
+    return OK;
+  }
+  const std::vector<cx<R>> as = matvec(W, sv);
+  ++ord;
+  const cx<R> a2 = cdot(as, as), w2 = cdot(as, sv);
+  const cx<R> chi = cdivc(w2, a2);
+  for (size_t i = 0; i < n; ++i) x[i] += omega * p[i] + chi * sv[i];
+  return OK;
+}
+
+// FEFF ggrm: two-sided Lanczos recursion with restarts.
+template <typename R>
+int recursion(const std::vector<cx<R>>& W, size_t src, R tol, std::vector<cx<R>>& x, int& ord) {
+  ord = 0;
+  const size_t n = x.size();
+  const cx<R> zero, one(R(1), R(0));
+  std::fill(x.begin(), x.end(), zero);
+  for (int restart = 0; restart < 128; ++restart) {
+    std::vector<cx<R>> r = restart > 0 ? matvec(W, x) : std::vector<cx<R>>(n);
+    r[src] -= one;
+    std::vector<cx<R>> xket(n);
+    for (size_t i = 0; i < n; ++i) xket[i] = -r[i];
+    const cx<R> rn = cdot(xket, xket);
+    if (is_zero(rn)) return OK;
+    const R xf = R(1) / pos(rn.re);
+    std::vector<cx<R>> xbra(n);
+    for (size_t i = 0; i < n; ++i) xbra[i] = xket[i] * xf;
+    std::vector<cx<R>> tket = matvec(W, xket);
+    ++ord;
+    cx<R> aa = cdot(xbra, tket), aac = conj(aa), bb, bbc, betac = aa;
+    nz(betac);
+    cx<R> yy = one;
+    std::vector<cx<R>> xketp(n), xbrap(n), z = xket, sv = tket;
+    for (size_t i = 0; i < n; ++i) x[i] += z[i] / betac;
+    for (size_t i = 0; i < n; ++i) r[i] += sv[i] / betac;
+    for (int it = 0; it < 100; ++it) {
+      for (size_t i = 0; i < n; ++i) tket[i] -= aa * xket[i] + bb * xketp[i];
+      std::vector<cx<R>> tbra = adj_matvec(W, xbra);
+      for (size_t i = 0; i < n; ++i) tbra[i] -= aac * xbra[i] + bbc * xbrap[i];
+      const cx<R> rnorm = cdot(tbra, tket);
+      if (is_zero(rnorm)) return OK;
+      bb = csqrt(rnorm);
+      bbc = conj(bb);
+      nz(bb);
+      nz(bbc);
+      xketp = xket;
+      xbrap = xbra;
+      for (size_t i = 0; i < n; ++i) xket[i] = tket[i] / bb;
+      for (size_t i = 0; i < n; ++i) xbra[i] = tbra[i] / bbc;
+      tket = matvec(W, xket);
+      ++ord;
+      aa = cdot(xbra, tket);
+      aac = conj(aa);
+      const cx<R> alphac = cdivc(bb, betac);
+      for (size_t i = 0; i < n; ++i) {
+        z[i] = xket[i] - alphac * z[i];
+        sv[i] = tket[i] - alphac * sv[i];
+      }
+      betac = aa - alphac * bb;
+      nz(betac);
+      yy = -alphac * yy;
+      const cx<R> gamma = cdivc(yy, betac);
+      for (size_t i = 0; i < n; ++i) {
+        x[i] += gamma * z[i];
+        r[i] += gamma * sv[i];
+      }
+      if (within(r, tol)) return OK;
+    }
+  }
+  return ERR_NO_CONVERGENCE;
+}
+
+// FEFF gggm: Graves-Morris on W = T G0 (no identity), restarted.
+template <typename R>
+int graves_morris(const std::vector<cx<R>>& W, size_t src, R tol, std::vector<cx<R>>& x, int& ord) {
+  ord = 0;
+  const size_t n = x.size();
+  const cx<R> zero, one(R(1), R(0));
+  std::fill(x.begin(), x.end(), zero);
+  std::vector<cx<R>> b(n), x0(n);
+  cx<R> q0 = one;
+  b[src] = one;
+  for (int restart = 0; restart < 128; ++restart) {
+    if (restart > 0) {
+      nz(q0);
+      for (size_t i = 0; i < n; ++i) x[i] += x0[i] / q0;
+      const std::vector<cx<R>> av = matvec(W, x);
+      for (size_t i = 0; i < n; ++i) b[i] = av[i] - x[i];
+      b[src] += one;
+    }
+    std::vector<cx<R>> r0 = b;
+    std::fill(x0.begin(), x0.end(), zero);
+    std::vector<cx<R>> x1 = b, r1 = matvec(W, b);
+    ++ord;
+    cx<R> ww = cdot(r0, r0), aa = cdot(r1, r1);
+    const cx<R> wa = cdot(r0, r1), aw = conj(wa);
+    nz(aa);
+    nz(ww);
+    const cx<R> dd = aa * ww - aw * wa;
+    const cx<R> sdd = cdivc(cdivc(dd, aa), ww);
+    std::vector<cx<R>> wv(n);
+    if (cnorm(sdd) < R(1.0e-8)) {
+      for (size_t i = 0; i < n; ++i) wv[i] = r0[i] / ww;
+    } else {
+      nz(dd);
+      ww = (ww - aw) / dd;
+      aa = (wa - aa) / dd;
+      for (size_t i = 0; i < n; ++i) wv[i] = r0[i] * aa + r1[i] * ww;
+    }
+    cx<R> e0 = cdot(wv, r0), e1 = cdot(wv, r1);
+    q0 = one;
+    cx<R> q1 = one;
+    for (int it = 0; it < 10; ++it) {
+      R t1 = scaled(tol, cnorm(q1) / R(10));
+      if (within(r1, t1)) {
+        nz(q1);
+        for (size_t i = 0; i < n; ++i) x[i] += x1[i] / q1;
+        return OK;
+      }
+      const cx<R> alpha = cdivc(e1, e0);
+      std::vector<cx<R>> t0(n);
+      for (size_t i = 0; i < n; ++i) t0[i] = r1[i] - alpha * r0[i];
+      const std::vector<cx<R>> tv = matvec(W, t0);
+      ++ord;
+      const cx<R> wa2 = cdot(t0, tv), ww2 = cdot(t0, t0), aa2 = cdot(tv, tv), aw2 = conj(wa2);
+      const cx<R> theta = cdivc(wa2 - aa2, ww2 - aw2);
+      for (size_t i = 0; i < n; ++i) r0[i] = tv[i] - theta * t0[i];
+      const cx<R> d1 = one - theta;
+      for (size_t i = 0; i < n; ++i) x0[i] = t0[i] + d1 * (x1[i] - alpha * x0[i]);
+      q0 = d1 * (q1 - alpha * q0);
+      R t0l = scaled(tol, cnorm(q0));
+      if (within(r0, t0l)) {
+        nz(q0);
+        for (size_t i = 0; i < n; ++i) x[i] += x0[i] / q0;
+        return OK;
+      }
+      e0 = cdot(wv, r0);
+      const cx<R> beta = cdivc(e0, e1);
+      for (size_t i = 0; i < n; ++i) t0[i] = r0[i] - beta * r1[i];
+      const std::vector<cx<R>> av = matvec(W, t0);
+      ++ord;
+      const cx<R> d2 = beta * theta;
+      for (size_t i = 0; i < n; ++i) r1[i] = av[i] + d2 * r1[i];
+      e1 = cdot(wv, r1);
+      const cx<R> d3 = beta * (one - theta);
+      for (size_t i = 0; i < n; ++i) x1[i] = x0[i] - d3 * x1[i] + t0[i];
+      q1 = q0 - (one - theta) * beta * q1;
+    }
+  }
+  return ERR_NO_CONVERGENCE;
+}
+
+// FEFF ggtf: transpose-free QMR, 21 half-steps per restart.
+template <typename R>
+int tfqmr(const std::vector<cx<R>>& W, size_t src, R tol, std::vector<cx<R>>& x, int& ord) {
+  ord = 0;
+  const size_t n = x.size();
+  const cx<R> zero;
+  std::fill(x.begin(), x.end(), zero);
+  std::vector<cx<R>> a(n);
+  for (int restart = 0; restart < 128; ++restart) {
+    if (restart > 0) a = matvec(W, x);
+    std::vector<cx<R>> u(n);
+    for (size_t i = 0; i < n; ++i) u[i] = -a[i];
+    u[src] += cx<R>(R(1), R(0));
+    a = matvec(W, u);
+    ++ord;
+    std::vector<cx<R>> w = u, v = a, d(n);
+    const cx<R> aa0 = cdot(u, u);
+    nz(aa0);
+    R tau = std::sqrt(pos(aa0.re));
+    R nu = R(0);
+    cx<R> eta, alpha, rho(R(1), R(0));
+    std::vector<cx<R>> rv(n);
+    for (size_t i = 0; i < n; ++i) rv[i] = u[i] / aa0;
+    for (int nit = 0; nit <= 20; ++nit) {
+      if (nit % 2 == 0) alpha = cdivc(rho, cdot(rv, v));
+      else {
+        a = matvec(W, u);
+        ++ord;
+      }
+      for (size_t i = 0; i < n; ++i) w[i] -= alpha * a[i];
+      const cx<R> f = cdivc(eta * (nu * nu), alpha);
+      const std::vector<cx<R>> dp = d;
+      for (size_t i = 0; i < n; ++i) d[i] = u[i] + f * dp[i];
+      const cx<R> wn = cdot(w, w);
+      const R norm = std::sqrt(nonneg(wn.re));
+      nu = norm / tau;
+      const R cm = R(1) / std::sqrt(R(1) + nu * nu);
+      tau *= nu * cm;
+      eta = alpha * (cm * cm);
+      for (size_t i = 0; i < n; ++i) x[i] += eta * d[i];
+      const R err = tau * std::sqrt((R(1) + R(nit)) / R(n)) * R(10);
+      if (std::fabs(err) < tol) return OK;
+      if (nit % 2 != 0) {
+        const cx<R> prho = rho;
+        rho = cdot(rv, w);
+        const cx<R> beta = cdivc(rho, prho);
+        for (size_t i = 0; i < n; ++i) u[i] = w[i] + beta * u[i];
+        for (size_t i = 0; i < n; ++i) v[i] = beta * (a[i] + beta * v[i]);
+        a = matvec(W, u);
+        ++ord;
+        for (size_t i = 0; i < n; ++i) v[i] += a[i];
+      } else {
+        for (size_t i = 0; i < n; ++i) u[i] -= alpha * v[i];
+      }
+    }
+  }
+  return ERR_NO_CONVERGENCE;
+}
+
+// fms_iterative_scattering_with_system (iterative.rs:38-179): absorber-range
+// potentials, every source column of the representative block, gg = G0 x rows.
+template <typename R>
+inline int iterative_scattering(const Plan<R>& P, const std::vector<cx<R>>& g0, const std::vector<cx<R>>& t, int minv,
+                                R toler1, R toler2, std::vector<cx<R>>& scat, std::vector<cx<R>>* system_out = nullptr,
+                                int* order_out = nullptr) {
+  const size_t n = P.n();
+  std::vector<cx<R>> W(n * n);
+  if (minv == 3) {
+    // fms_graves_morris_system_matrix: + T G0, no identity
+    for (size_t c = 0; c < n; ++c)
+      for (size_t r = 0; r < n; ++r) {
+        const cx<R> g = g0[r + n * c];
+        if (cnorm(g) > toler2) W[r + n * c] += cx<R>(R(1), R(0)) * t[size_t(P.nsp) * r] * g;
+        if (P.nsp == 2) {
+          const long partner = spin_partner_index(P.kets[r], long(r), long(n));
+          if (partner >= 0) {
+            const cx<R> gf = g0[size_t(partner) + n * c];
+            if (cnorm(gf) > toler2) W[r + n * c] += cx<R>(R(1), R(0)) * t[1 + 2 * size_t(partner)] * gf;
+          }
+        }
+      }
+  } else {
+    iterative_system_matrix(P, g0, t, toler2, W);
+  }
+  const size_t C = size_t(P.nsp) * size_t((P.L + 1) * (P.L + 1));
+  scat.assign(C * C * size_t(P.npot), cx<R>());
+  if (system_out) *system_out = W;
+  std::vector<cx<R>> x(n);
+  int ord = 0;
+  for (int p = P.pot_start; p <= P.pot_end; ++p) {
+    const int lm = std::min(P.pot_lmax[size_t(p)], P.L);
+    const size_t ipart = size_t(P.nsp) * size_t((lm + 1) * (lm + 1));
+    const size_t off = size_t(P.rep_offsets[size_t(p)]);
+    for (size_t c = 0; c < ipart; ++c) {
+      int rc;
+      try {
+        switch (minv) {
+          case 1: rc = bicgstab(W, off + c, toler1, x, ord); break;
+          case 2: rc = recursion(W, off + c, toler1, x, ord); break;
+          case 3: rc = graves_morris(W, off + c, toler1, x, ord); break;
+          default: rc = tfqmr(W, off + c, toler1, x, ord); break;
+        }
+      } catch (const Breakdown&) {
+        rc = ERR_BREAKDOWN;
+      }
+      if (rc != OK) return rc;
+      for (size_t r = 0; r < ipart; ++r) {
+        cx<R> v;
+        for (size_t s = 0; s < n; ++s) v = v + g0[off + r + n * s] * x[s];
+        scat[r + C * (c + C * size_t(p))] = v;
+      }
+      if (order_out) *order_out = ord;
+    }
+  }
+  return OK;
+}
+
 }  // namespace oracle
 
 // ===========================================================================
@@ -1002,6 +1373,49 @@ int oracle_fms_spectrum(int mode, int n_atoms, const float* positions, const int
   return mode == 0 ? run(float(0)) : run(double(0));
 }
 
+// Iterative forms (minv != 0) of oracle_fms_spectrum: toler1 = convergence,
+// toler2 = G0 drop tolerance, both narrowed to f32 like the reference.
+int oracle_fms_spectrum_iterative(int mode, int minv, double toler1, double toler2, int n_atoms, const float* positions,
+                                  const int* pots, int nsp, int ispin, int lfms, int max_potential, int global_lmax,
+                                  const int* lmaxph, double rdirec, const float* sigsqr, double sig2g, int n_energies,
+                                  const double* wave_numbers, const double* xphase, double* scattering_out,
+                                  int* status_out, int n_threads) {
+  std::vector<Atom> atoms(static_cast<size_t>(n_atoms));
+  for (int i = 0; i < n_atoms; ++i) { std::memcpy(atoms[size_t(i)].pos, positions + 3 * i, 12); atoms[size_t(i)].pot = pots[i]; }
+  auto run = [&](auto tag) -> int {
+    using R = decltype(tag);
+    Plan<R> P;
+    int rc = make_plan<R>(P, atoms.data(), n_atoms, nsp, ispin, lfms, max_potential, global_lmax, lmaxph, R(float(rdirec)),
+                          sigsqr, float(sig2g));
+    if (rc) return rc;
+    const size_t C = size_t(P.nsp) * size_t((P.L + 1) * (P.L + 1));
+    const size_t scat_sz = C * C * size_t(P.npot);
+    const size_t xph_sz = size_t(P.nsp) * size_t(2 * P.L + 1) * size_t(P.npot);
+    int first_error = OK;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads > 0 ? n_threads : 1)
+    for (int e = 0; e < n_energies; ++e) {
+      std::vector<cx<R>> k(static_cast<size_t>(P.nsp)), xp(xph_sz), g0, t, scat;
+      for (int s = 0; s < P.nsp; ++s) k[size_t(s)] = ld<R>(wave_numbers + 2 * (size_t(e) * size_t(P.nsp) + size_t(s)));
+      for (size_t i = 0; i < xph_sz; ++i) xp[i] = ld<R>(xphase + 2 * (size_t(e) * xph_sz + i));
+      int erc = free_propagator_matrix(P, k.data(), g0);
+      if (erc == OK) {
+        t_matrix_table(P, xp.data(), t);
+        erc = iterative_scattering(P, g0, t, minv, R(float(toler1)), R(float(toler2)), scat);
+      }
+      if (status_out) status_out[e] = erc;
+      if (erc != OK) {
+#pragma omp critical
+        if (first_error == OK) first_error = erc;
+        continue;
+      }
+      if (scattering_out)
+        for (size_t i = 0; i < scat_sz; ++i) st(scattering_out + 2 * (size_t(e) * scat_sz + i), scat[i]);
+    }
+    return first_error;
+  };
+  return mode == 0 ? run(float(0)) : run(double(0));
+}
+
 // fms_driver_setup for the known-answer test (driver.rs:4-65): returns the
 // clamped potential lmax, active potential range, representative offsets and kets.
 int oracle_driver_setup(int n_atoms, const int* pots, int nsp, int lfms, int max_potential, int global_lmax,
@@ -1106,6 +1520,39 @@ int oracle_lu_scattering_explicit(int mode, int n, const int* kets4, int nsp, in
       for (size_t i = 0; i < A.size(); ++i) st(system_out + 2 * i, A[i]);
     long sp = -1;
     int rc = lu_scattering(P, g0, t, scat, &sp);
+    if (rc) return rc;
+    for (size_t i = 0; i < scat.size(); ++i) st(scat_out + 2 * i, scat[i]);
+    return OK;
+  };
+  return mode == 0 ? run(float(0)) : run(double(0));
+}
+
+// Iterative forms on explicit G0 / T tables (the reference's solver tests):
+// system matrix, scattering table and the last solve's multiple-scattering order.
+int oracle_iterative_scattering_explicit(int mode, int minv, int n, const int* kets4, int nsp, int global_lmax, int npot,
+                                         const int* pot_lmax, const long* rep_offsets, int pot_start, int pot_end,
+                                         const double* g0_in, const double* t_in, double toler1, double toler2,
+                                         double* system_out, double* scat_out, int* order_out) {
+  auto run = [&](auto tag) -> int {
+    using R = decltype(tag);
+    Plan<R> P;
+    P.nsp = nsp;
+    P.L = global_lmax;
+    P.npot = npot;
+    P.pot_lmax.assign(pot_lmax, pot_lmax + npot);
+    P.rep_offsets.assign(rep_offsets, rep_offsets + npot);
+    P.pot_start = pot_start;
+    P.pot_end = pot_end;
+    P.kets.resize(size_t(n));
+    for (int i = 0; i < n; ++i) P.kets[size_t(i)] = {kets4[4 * i], kets4[4 * i + 1], kets4[4 * i + 2], kets4[4 * i + 3]};
+    for (int p = pot_start; p <= pot_end; ++p)
+      if (p < 0 || p >= npot || P.rep_offsets[size_t(p)] < 0) return ERR_MISSING_REPRESENTATIVE;
+    std::vector<cx<R>> g0(size_t(n) * size_t(n)), t(size_t(nsp) * size_t(n)), W, scat;
+    for (size_t i = 0; i < g0.size(); ++i) g0[i] = ld<R>(g0_in + 2 * i);
+    for (size_t i = 0; i < t.size(); ++i) t[i] = ld<R>(t_in + 2 * i);
+    int rc = iterative_scattering(P, g0, t, minv, R(float(toler1)), R(float(toler2)), scat, &W, order_out);
+    if (system_out)
+      for (size_t i = 0; i < W.size(); ++i) st(system_out + 2 * i, W[i]);
     if (rc) return rc;
     for (size_t i = 0; i < scat.size(); ++i) st(scat_out + 2 * i, scat[i]);
     return OK;

@@ -65,6 +65,10 @@ def _declare(L):
         "oracle_t_matrix_element": [_i, _i, _i, _i, _i, _p, _p, _p, _i, _p],
         "oracle_free_propagator_element": [_i, _i, _i, _p, _p, _p, _p, _d, _p, _p, _p, _p],
         "oracle_transition_b_matrix": [_i, _i, _i, _p, _i, _i, _i, _i, _d, _p, _p, _p],
+        "oracle_iterative_scattering_explicit": [_i, _i, _i, _p, _i, _i, _i, _p, _p, _i, _i, _p, _p, _d, _d, _p, _p,
+                                                 _p],
+        "oracle_fms_spectrum_iterative": [_i, _i, _d, _d, _i, _p, _p, _i, _i, _i, _i, _i, _p, _d, _p, _d, _i, _p, _p,
+                                          _p, _p, _i],
         "oracle_mkgtr_trace": [_i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p],
     }
     for name, args in sig.items():
@@ -148,6 +152,35 @@ def fms_spectrum(positions, pots, lmaxph, wave_numbers, xphase, *, nsp=1, ispin=
     check(rc)
     tabs = out.view(np.complex128).reshape(E, Cc * Cc * npot)
     return np.stack([tabs[e].reshape((Cc, Cc, npot), order="F") for e in range(E)])
+
+
+def fms_spectrum_iterative(positions, pots, lmaxph, wave_numbers, xphase, *, minv, toler1=1e-3, toler2=1e-3, nsp=1,
+                           ispin=0, lfms=0, global_lmax=None, rdirec=1.0e6, sigsqr=None, sig2g=0.0, mode=F64,
+                           threads=1, raise_on_error=True):
+    """Oracle scattering tables of the iterative forms (minv 1 ggbi, 2 ggrm, 3 gggm, else ggtf): (E, C, C, npot);
+    with raise_on_error=False returns (tables, per-energy status)."""
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    pots = np.ascontiguousarray(pots, dtype=np.int32)
+    lmaxph = np.ascontiguousarray(lmaxph, dtype=np.int32)
+    npot = len(lmaxph)
+    L = int(lmaxph.max()) if global_lmax is None else int(global_lmax)
+    E = wave_numbers.shape[0]
+    k = cbuf(np.asarray(wave_numbers).reshape(E, nsp).T)
+    xp_f = np.stack([np.asarray(xphase[e]).reshape(nsp, 2 * L + 1, npot).reshape(-1, order="F") for e in range(E)])
+    xpb = np.ascontiguousarray(xp_f).view(np.float64).copy()
+    Cc = nsp * (L + 1) ** 2
+    out = np.zeros(2 * E * Cc * Cc * npot)
+    status = np.zeros(E, dtype=np.int32)
+    sig = None if sigsqr is None else np.asfortranarray(sigsqr, dtype=np.float32)
+    rc = lib().oracle_fms_spectrum_iterative(mode, int(minv), float(toler1), float(toler2), len(pots), ptr(positions),
+                                             ptr(pots), nsp, ispin, lfms, npot - 1, L, ptr(lmaxph), float(rdirec),
+                                             ptr(sig), float(sig2g), E, ptr(k), ptr(xpb), ptr(out), ptr(status),
+                                             int(threads))
+    if raise_on_error:
+        check(rc)
+    tabs = out.view(np.complex128).reshape(E, Cc * Cc * npot)
+    res = np.stack([tabs[e].reshape((Cc, Cc, npot), order="F") for e in range(E)])
+    return res if raise_on_error else (res, status)
 
 
 def lu_factor_solve(A, B, mode=F64):

@@ -168,6 +168,47 @@ KATS = {
             "6,7,0": c(-0.0962859, 0.14052007, f"{FMS_TESTS}/solvers.rs:335"),
         },
     },
+    # iterative forms on reference_gglu_inputs(8), toler1 = 1e-5, toler2 = 0 (solvers.rs:73-292).
+    "ggbi": {
+        "order": r(2, f"{FMS_TESTS}/solvers.rs:97"),
+        "system_sum": c(7.9095793, -0.5169, f"{FMS_TESTS}/solvers.rs:100"),
+        "scattering_sum": c(-2.9492176, 4.806942, f"{FMS_TESTS}/solvers.rs:104"),
+        "scattering": {
+            "0,0,0": c(-0.007855818, -0.0032014623, f"{FMS_TESTS}/solvers.rs:108"),
+            "1,3,0": c(-0.066029795, 0.044123195, f"{FMS_TESTS}/solvers.rs:112"),
+            "6,7,0": c(-0.096492656, 0.1408408, f"{FMS_TESTS}/solvers.rs:116"),
+        },
+    },
+    "ggrm": {
+        "order": r(3, f"{FMS_TESTS}/solvers.rs:174"),
+        "system_sum": c(7.9095793, -0.5169, f"{FMS_TESTS}/solvers.rs:177"),
+        "scattering_sum": c(-2.944324, 4.799402, f"{FMS_TESTS}/solvers.rs:181"),
+        "scattering": {
+            "0,0,0": c(-0.007797021, -0.0032442873, f"{FMS_TESTS}/solvers.rs:185"),
+            "1,3,0": c(-0.06596752, 0.044093154, f"{FMS_TESTS}/solvers.rs:189"),
+            "6,7,0": c(-0.09628572, 0.14052017, f"{FMS_TESTS}/solvers.rs:193"),
+        },
+    },
+    "gggm": {
+        "order": r(4, f"{FMS_TESTS}/solvers.rs:222"),
+        "system_sum": c(0.09041999, 0.5169, f"{FMS_TESTS}/solvers.rs:225"),
+        "scattering_sum": c(-2.9443216, 4.799405, f"{FMS_TESTS}/solvers.rs:229"),
+        "scattering": {
+            "0,0,0": c(-0.0077970494, -0.003244209, f"{FMS_TESTS}/solvers.rs:233"),
+            "1,3,0": c(-0.06596747, 0.044093188, f"{FMS_TESTS}/solvers.rs:237"),
+            "6,7,0": c(-0.096285895, 0.14052008, f"{FMS_TESTS}/solvers.rs:241"),
+        },
+    },
+    "ggtf": {
+        "order": r(4, f"{FMS_TESTS}/solvers.rs:270"),
+        "system_sum": c(7.9095793, -0.5169, f"{FMS_TESTS}/solvers.rs:273"),
+        "scattering_sum": c(-2.9443207, 4.7994027, f"{FMS_TESTS}/solvers.rs:277"),
+        "scattering": {
+            "0,0,0": c(-0.0077970214, -0.0032442873, f"{FMS_TESTS}/solvers.rs:281"),
+            "1,3,0": c(-0.06596743, 0.044093173, f"{FMS_TESTS}/solvers.rs:285"),
+            "6,7,0": c(-0.09628591, 0.1405201, f"{FMS_TESTS}/solvers.rs:289"),
+        },
+    },
     "iterative_system": {
         "sum": c(7.9095793, -0.5169, f"{FMS_TESTS}/solvers.rs:20"),
         "entries": {

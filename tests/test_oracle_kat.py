@@ -403,3 +403,26 @@ def test_state_kets_order():
                                           po.ptr(ns), po.ptr(k4), 16))
     assert ns[0] == 8
     assert k4[:16].reshape(4, 4)[:, 3].tolist() == [1, 2, 1, 2]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("minv,key", [(1, "ggbi"), (2, "ggrm"), (3, "gggm"), (4, "ggtf")])
+def test_iterative_scattering_forms(mode, minv, key):
+    """ggbi / ggrm / gggm / ggtf on reference_gglu_inputs(8), toler1 1e-5, toler2 0 (solvers.rs:73-292)."""
+    k = KAT[key]
+    ks = kets(2, [0], [1], 1)
+    g0, t = gglu_inputs(len(ks))
+    n = len(ks)
+    sysm = np.zeros(2 * n * n)
+    scat = np.zeros(2 * 8 * 8 * 1)
+    order = np.zeros(1, np.int32)
+    po.check(po.lib().oracle_iterative_scattering_explicit(
+        mode, minv, n, po.ptr(ks), 2, 1, 1, po.ptr(np.array([1], np.int32)), po.ptr(np.array([0], np.int64)), 0, 0,
+        po.ptr(po.cbuf(g0)), po.ptr(po.cbuf(t)), 1.0e-5, 0.0, po.ptr(sysm), po.ptr(scat), po.ptr(order)))
+    A = po.from_cbuf(sysm, (n, n))
+    S = po.from_cbuf(scat, (8, 8, 1))
+    assert int(order[0]) == k["order"]["value"]
+    assert_c(A.sum(), k["system_sum"])
+    assert_c(S.sum(), k["scattering_sum"])
+    for key_, e in k["scattering"].items():
+        assert_c(S[tuple(map(int, key_.split(",")))], e)
