@@ -60,10 +60,14 @@ typedef enum {
   REFEFF_FMS_ERR_OUT_OF_MEMORY = 15,
   REFEFF_FMS_ERR_INVALID_TOLERANCE = 16,     /* FmsError::InvalidTolerance */
   REFEFF_FMS_ERR_INVALID_CLUSTER_RADIUS = 17, /* FmsError::InvalidClusterRadius */
-  REFEFF_FMS_ERR_SCRATCH_LIMIT = 18           /* request exceeds REFEFF_FMS_NOALLOC_SCRATCH_BYTES */
+  REFEFF_FMS_ERR_SCRATCH_LIMIT = 18,          /* request exceeds REFEFF_FMS_NOALLOC_SCRATCH_BYTES */
+  REFEFF_FMS_ERR_ITERATIVE_BREAKDOWN = 19     /* FmsError::IterativeSolverBreakdown (minv != 0) */
 } refeff_fms_status;
 
 /* Solver forms for the dense system (I - G0 T) X = G0[:, absorber]. */
+/* For a plan with minv != 0 (the FEFF iterative forms, solvers.rs:225-357)
+ * the form picks the arithmetic of the iterative solve instead: FP64_LU runs it
+ * in FP64, FP32_REFINED in complex FP32 like the reference (no refinement). */
 typedef enum {
   /* Plain FP64 blocked LU.  The drop-in for minv = 0 (FEFF gglu,
    * crates/refeff-core/src/fms/solvers.rs:366-484). */
@@ -124,7 +128,7 @@ typedef struct {
   int spin_channels;                /* nsp: 1 or 2 */
   int spin_selector;                /* global.inp ispin */
   int lfms;                         /* 0: absorber potential only; else all potentials */
-  int minv;                         /* FEFF minv (0 = LU); others are solved with LU too */
+  int minv;                         /* FEFF minv: 0 LU, 1 ggbi, 2 ggrm (recursion), 3 gggm, other ggtf (TFQMR) */
   int max_potential;                /* nph */
   int global_lmax;                  /* max over lmaxph */
   const int* raw_potential_lmax;    /* lmaxph(0..nph), clamped like clamp_fms_lipotx */

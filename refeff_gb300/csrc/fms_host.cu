@@ -26,6 +26,7 @@
 #include "cplx.cuh"
 #include "fms_plan.cuh"
 #include "host_internal.h"
+#include "iterative.cuh"
 
 using namespace rfx;
 
@@ -306,6 +307,7 @@ struct Workspace {
   DevBuf<double2> M64;
   DevBuf<float2> M32;
   DevBuf<double2> X64, R;
+  DevBuf<double2> t_tab, grow, iter_scratch;  // iterative forms (minv != 0)
   DevBuf<unsigned long long> rnorm, bnorm, dnorm, xnorm;
   DevBuf<double> dprev;
   DevBuf<int> converged, iters;
@@ -349,6 +351,8 @@ struct refeff_fms_plan {
   DevBuf<double> d_sigsqr, d_dist, d_phi, d_dsmall, d_xnlm, d_t3p, d_t3m;
   DevBuf<double2> d_k_all, d_x_all, d_gg_all;
   DevBuf<int> d_status_all;
+  DevBuf<int> d_partner;  // spin partner per state, device order (-1 none)
+  double toler1 = 0.0, toler2 = 0.0;  // iterative forms: convergence and G0 drop tolerances (f32 values)
   Workspace ws;
   bool profiling = false;
   double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0};
@@ -372,6 +376,8 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
     return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "invalid direct cutoff");
   if (!std::isfinite(in->zero_tolerance) || in->zero_tolerance < 0.0f)
     return fail(ctx, REFEFF_FMS_ERR_INVALID_TOLERANCE, "invalid toler2");
+  if (in->minv != 0 && (!std::isfinite(in->convergence_tolerance) || in->convergence_tolerance < 0.0f))
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_TOLERANCE, "invalid toler1");
   auto plan = std::make_unique<refeff_fms_plan>();
   refeff_fms_plan& p = *plan;
   p.ctx = ctx;
@@ -382,6 +388,8 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   p.npot = in->max_potential + 1;
   p.lfms = in->lfms;
   p.minv = in->minv;
+  p.toler1 = double(in->convergence_tolerance);
+  p.toler2 = double(in->zero_tolerance);
   const int N = p.N, L = p.L, nsp = p.nsp;
   // driver.rs:25-31, validation.rs:69-75: clamp lipotx
   p.pot_lmax.resize(size_t(p.npot));
@@ -465,6 +473,21 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   RF_CUDA(ctx, p.d_xnlm.upload(xnlm.data(), xnlm.size(), s));
   RF_CUDA(ctx, p.d_t3p.upload(t3p.data(), t3p.size(), s));
   RF_CUDA(ctx, p.d_t3m.upload(t3m.data(), t3m.size(), s));
+  {
+    // fms_spin_partner_index (internals/linear.rs:163-201): (l, m, 1) <-> (l, m - 1, 2)
+    std::vector<int> partner(static_cast<size_t>(p.n), -1);
+    for (int d = 0; d < N; ++d)
+      for (int q = 0; q < doff[size_t(d) + 1] - doff[size_t(d)]; ++q) {
+        if (nsp != 2) break;
+        const int sp = q % 2 + 1, lm = q / 2;
+        int l = 0;
+        while ((l + 1) * (l + 1) <= lm) ++l;
+        const int m = lm - l * l - l;
+        if (sp == 1 && m > -l) partner[size_t(doff[size_t(d)] + q)] = doff[size_t(d)] + q - 1;
+        if (sp == 2 && m < l) partner[size_t(doff[size_t(d)] + q)] = doff[size_t(d)] + q + 1;
+      }
+    RF_CUDA(ctx, p.d_partner.upload(partner.data(), partner.size(), s));
+  }
   RF_CUDA(ctx, p.d_dist.alloc(size_t(N) * N));
   RF_CUDA(ctx, p.d_phi.alloc(size_t(N) * N));
   RF_CUDA(ctx, p.d_dsmall.alloc(size_t(N) * N * ds));
@@ -686,7 +709,21 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     return e;
   };
   cudaError_t e = cudaSuccess;
-  if (form == REFEFF_FMS_FORM_FP64_LU) {
+  if (p.minv != 0) {
+    // FEFF iterative forms: G0 and the per-state T table, then one CTA per
+    // (energy, absorber column) runs the minv solver on W = I - T G0
+    tick(0, [&] {
+      launch_build_g0(p.P, batch, ws.k_stage.p, lay, ws.M64.p, ws.status.p, s);
+      launch_t_table(p.P, batch, ws.x_stage.p, ws.t_tab.p, ws.status.p, s);
+      return cudaGetLastError();
+    });
+    e = tick(1, [&] {
+      return launch_iterative(form == REFEFF_FMS_FORM_FP64_LU, p.minv, lay, batch, ws.M64.p, ws.M32.p, ws.t_tab.p,
+                              p.d_partner.p, p.toler1, p.toler2, ws.grow.p, ws.iter_scratch.p, ws.gg_stage.p,
+                              ws.status.p, s);
+    });
+    if (e != cudaSuccess) return e;
+  } else if (form == REFEFF_FMS_FORM_FP64_LU) {
     tick(0, [&] {
       launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, nullptr, ws.status.p, s);
       return cudaGetLastError();
@@ -733,6 +770,7 @@ int map_status(int dev) {
     case kDevNonfinite: return REFEFF_FMS_ERR_NONFINITE_INPUT;
     case kDevZeroRho: return REFEFF_FMS_ERR_ZERO_RHO;
     case kDevNotConverged: return REFEFF_FMS_ERR_NOT_CONVERGED;
+    case kDevBreakdown: return REFEFF_FMS_ERR_ITERATIVE_BREAKDOWN;
     default: return REFEFF_FMS_ERR_CUDA;
   }
 }
@@ -763,7 +801,13 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
   RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
   RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.m * p.m));
-  if (fp32) {
+  const bool refined = fp32 && p.minv == 0;  // refinement statistics and the FP64 fallback
+  if (p.minv != 0) {
+    RF_CUDA(ctx, ws.t_tab.alloc(size_t(ws.batch) * p.n * 2));
+    RF_CUDA(ctx, ws.grow.alloc(size_t(ws.batch) * p.m * p.n));
+    RF_CUDA(ctx, ws.iter_scratch.alloc(size_t(ws.batch) * p.m * kIterVectors * p.n));
+  }
+  if (refined) {
     RF_CUDA(ctx, p.d_relres_all.alloc(size_t(E)));
     RF_CUDA(ctx, p.d_iters_all.alloc(size_t(E)));
   }
@@ -804,14 +848,14 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
     RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.m * p.m, ws.gg_stage.p, size_t(nb) * p.m * p.m * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
     RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, s));
-    if (fp32) {
+    if (refined) {
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_relres_all.p + e0, ws.relres.p, size_t(nb) * sizeof(double),
                                    cudaMemcpyDeviceToDevice, s));
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_iters_all.p + e0, ws.iters.p, size_t(nb) * sizeof(int),
                                    cudaMemcpyDeviceToDevice, s));
     }
   }
-  if (!fp32) return REFEFF_FMS_OK;
+  if (!refined) return REFEFF_FMS_OK;
   // Energies whose refinement missed the tolerance are solved again with the
   // plain FP64 LU (same inputs), so every returned block meets the FP64 bar.
   std::vector<int> st(static_cast<size_t>(E));
@@ -899,7 +943,7 @@ extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refef
   std::vector<int> st(static_cast<size_t>(E));
   RF_CUDA(ctx, cudaMemcpyAsync(gg.data(), p.d_gg_all.p, gg.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), p.d_status_all.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
-  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
+  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED && p.minv == 0;  // refinement statistics exist
   p.last_relres.assign(fp32 ? size_t(E) : 0, 0.0);
   p.last_iters.assign(fp32 ? size_t(E) : 0, 0);
   if (fp32) {

@@ -53,6 +53,7 @@ enum DevStatus : int {
   kDevZeroRho = 3,
   kDevNotConverged = 4,
   kDevTimeout = 5,
+  kDevBreakdown = 6,     // iterative solver breakdown (zero divisor)
 };
 
 // Every kernel launch of the library calls this first; the total (including
@@ -67,5 +68,10 @@ void launch_plan_geometry(const PlanDev& P, cudaStream_t s);
 // Writes A (= I - G0 T) and B (= G0[:, absorber]) into M64 (and a float copy into M32 if non-null).
 void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
                          double2* M64, float2* M32, int* status, cudaStream_t s);
+// Plain free propagator G0 (FP64, device state order) into G0[e * lay.stride + r + lay.lda * c].
+void launch_build_g0(const PlanDev& P, int E, const double2* k, const BatchLayout& lay, double2* G0, int* status,
+                     cudaStream_t s);
+// T table per state: t[(e * n + state) * 2 + band], band 0 = T(0, .), 1 = T(1, .).
+void launch_t_table(const PlanDev& P, int E, const double2* xphase, double2* t, int* status, cudaStream_t s);
 
 }  // namespace rfx

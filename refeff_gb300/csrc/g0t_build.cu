@@ -178,7 +178,69 @@ __device__ __forceinline__ double so_coef(const PlanDev& P, const double* tab, i
   return tab[l + (P.L + 1) * ((m + P.L) + (2 * P.L + 1) * (s - 1))];
 }
 
-template <bool kMirror32>
+// Compact T of one state (l, m, spin s) of an atom with potential `pot`
+// (fms_t_matrix_element, t_matrix.rs:10-143): t0 = T(0, state); t1 = T(1,
+// state), the spin-flip coupling to the partner (l, m -+ 1, other spin) when
+// nsp = 2.  Returns false when a phase shift it reads is not finite.
+__device__ inline bool state_t_matrix(const PlanDev& P, const double2* xe, int pot, int l, int m, int s, double2& t0,
+                                      double2& t1) {
+  const int nsp = P.nsp, L = P.L, D = 2 * L + 1;
+  auto phase = [&](int sp, int ll) { return xe[(sp - 1) + nsp * ((ll + L) + D * pot)]; };
+  t1 = make_double2(0.0, 0.0);
+  const double2 dm = phase(s, l);
+  const bool finite = cfinite(dm) && cfinite(phase(s, -l));
+  if (nsp == 1 && P.ispin == 0) {
+    t0 = t_phase(dm);
+    return finite;
+  }
+  int mp = 0, sp = 0;
+  bool has_partner = false;
+  if (nsp == 2) {
+    if (s == 1 && m > -l) { mp = m - 1; sp = 2; has_partner = true; }
+    if (s == 2 && m < l) { mp = m + 1; sp = 1; has_partner = true; }
+  }
+  const int cs = nsp == 1 ? (P.ispin > 0 ? 2 : 1) : s;
+  const double mi = so_coef(P, P.t3m, l, m, cs), pl = so_coef(P, P.t3p, l, m, cs);
+  const double2 a = t_phase(dm), b = t_phase(phase(s, -l));
+  t0 = make_double2(a.x * (mi * mi) + b.x * (pl * pl), a.y * (mi * mi) + b.y * (pl * pl));
+  if (has_partner) {
+    const double mf = so_coef(P, P.t3m, l, m, s), ms = so_coef(P, P.t3m, l, mp, sp);
+    const double pf = so_coef(P, P.t3p, l, m, s), ps = so_coef(P, P.t3p, l, mp, sp);
+    const double2 a2 = t_phase(phase(sp, l)), b2 = t_phase(phase(sp, -l));
+    const double2 mph = make_double2((a.x + a2.x) * 0.5, (a.y + a2.y) * 0.5);
+    const double2 pph = make_double2((b.x + b2.x) * 0.5, (b.y + b2.y) * 0.5);
+    t1 = make_double2(mph.x * mf * ms + pph.x * pf * ps, mph.y * mf * ms + pph.y * pf * ps);
+  }
+  return finite;
+}
+
+// Per-state T table for the iterative forms: t[e][2 * state + band] in
+// device state order (band 0 = T(0, state), band 1 = T(1, state)).
+__global__ void t_table_kernel(PlanDev P, const double2* __restrict__ xph, double2* __restrict__ t,
+                               int* __restrict__ status) {
+  const int a = blockIdx.x, e = blockIdx.y, nsp = P.nsp;
+  const int D = 2 * P.L + 1;
+  const double2* xe = xph + size_t(e) * size_t(nsp) * D * P.npot;
+  const int off = P.atom_off[a], cnt = P.atom_off[a + 1] - off, pot = P.atom_pot[a];
+  for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+    const int s = q % nsp + 1, lm = q / nsp;
+    int l = 0;
+    while ((l + 1) * (l + 1) <= lm) ++l;
+    double2 t0, t1;
+    if (!state_t_matrix(P, xe, pot, l, lm - l * l - l, s, t0, t1)) atomicMax(status + e, int(kDevNonfinite));
+    t[(size_t(e) * P.n + off + q) * 2] = t0;
+    t[(size_t(e) * P.n + off + q) * 2 + 1] = t1;
+  }
+}
+
+void launch_t_table(const PlanDev& P, int E, const double2* xphase, double2* t, int* status, cudaStream_t s) {
+  count_launch();
+  t_table_kernel<<<dim3(unsigned(P.N), unsigned(E)), 64, 0, s>>>(P, xphase, t, status);
+}
+
+// kMode 0: FP64 system [A | B]; 1: the same as hi/lo float pairs plus the FP32
+// copy; 2: the plain free propagator G0 (FP64, n x n, for the iterative forms).
+template <int kMode>
 __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const double2* __restrict__ kE,
                                                            const double2* __restrict__ xph, BatchLayout lay,
                                                            double2* __restrict__ M64, float2* __restrict__ M32,
@@ -205,10 +267,9 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
   int* flag = reinterpret_cast<int*>(sm + lay_s.flag);
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int D = 2 * L + 1;
-  const double2* xe = xph + size_t(e) * size_t(nsp) * D * P.npot;
+  const double2* xe = kMode == 2 ? nullptr : xph + size_t(e) * size_t(nsp) * D * P.npot;
   const double2* ke = kE + size_t(e) * nsp;
   const int potj = P.atom_pot[j];
-  auto phase = [&](int s, int l) { return xe[(s - 1) + nsp * ((l + L) + D * potj)]; };
 
   // ---- columns of atom j: state decode and compact T (t_matrix.rs:149-190) ----
   for (int q = tid; q < ncol; q += nthr) {
@@ -216,31 +277,14 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     int l = 0;
     while ((l + 1) * (l + 1) <= lm) ++l;
     const int m = lm - l * l - l;
-    int partner = -1, mp = 0, sp = 0;
+    int partner = -1;
     if (nsp == 2) {
-      if (s == 1 && m > -l) { partner = q - 1; mp = m - 1; sp = 2; }
-      if (s == 2 && m < l) { partner = q + 1; mp = m + 1; sp = 1; }
+      if (s == 1 && m > -l) partner = q - 1;
+      if (s == 2 && m < l) partner = q + 1;
     }
     colinfo[q] = make_int4(l, m, s, partner);
-    double2 t0, t1 = make_double2(0.0, 0.0);
-    const double2 dm = phase(s, l);
-    if (!cfinite(dm) || !cfinite(phase(s, -l))) atomicMax(status + e, int(kDevNonfinite));
-    if (nsp == 1 && P.ispin == 0) {
-      t0 = t_phase(dm);
-    } else {
-      const int cs = nsp == 1 ? (P.ispin > 0 ? 2 : 1) : s;
-      const double mi = so_coef(P, P.t3m, l, m, cs), pl = so_coef(P, P.t3p, l, m, cs);
-      const double2 a = t_phase(dm), b = t_phase(phase(s, -l));
-      t0 = make_double2(a.x * (mi * mi) + b.x * (pl * pl), a.y * (mi * mi) + b.y * (pl * pl));
-      if (partner >= 0) {
-        const double mf = so_coef(P, P.t3m, l, m, s), ms = so_coef(P, P.t3m, l, mp, sp);
-        const double pf = so_coef(P, P.t3p, l, m, s), ps = so_coef(P, P.t3p, l, mp, sp);
-        const double2 a2 = t_phase(phase(sp, l)), b2 = t_phase(phase(sp, -l));
-        const double2 mph = make_double2((a.x + a2.x) * 0.5, (a.y + a2.y) * 0.5);
-        const double2 pph = make_double2((b.x + b2.x) * 0.5, (b.y + b2.y) * 0.5);
-        t1 = make_double2(mph.x * mf * ms + pph.x * pf * ps, mph.y * mf * ms + pph.y * pf * ps);
-      }
-    }
+    double2 t0 = make_double2(0.0, 0.0), t1 = t0;
+    if (kMode != 2 && !state_t_matrix(P, xe, potj, l, m, s, t0, t1)) atomicMax(status + e, int(kDevNonfinite));
     tcol0[q] = t0;
     tcol1[q] = t1;
   }
@@ -374,15 +418,19 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     if (i0 + ri.x != j) {
       gcol = g0(ri.x, ri.y, ri.z, ri.w, ci.x, ci.y, ci.z);
       a = cneg(cmul(gcol, tcol0[cc]));
-      if (ci.w >= 0) {
+      if (kMode != 2 && ci.w >= 0) {
         const int4 pi = colinfo[ci.w];
         const double2 gp = g0(ri.x, ri.y, ri.z, ri.w, pi.x, pi.y, pi.z);
         a = csub(a, cmul(gp, tcol1[cc]));
       }
     }
-    if (r == c) a.x += 1.0;
     const size_t ai = base + size_t(r) + size_t(lay.lda) * c;
-    if (kMirror32) {
+    if (kMode == 2) {
+      M64[ai] = gcol;
+      continue;
+    }
+    if (r == c) a.x += 1.0;
+    if (kMode == 1) {
       // FP32 form: the FP64 system is kept as an exact-to-2^-48 hi/lo float pair
       // (same 16 bytes per entry) for the refinement residual; hi is the LU copy.
       const float4 sa = split_hi_lo(a);
@@ -393,7 +441,7 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     }
     if (absorber_col) {
       const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + cc);
-      if (kMirror32) {
+      if (kMode == 1) {
         const float4 sb = split_hi_lo(gcol);
         reinterpret_cast<float4*>(M64)[bi] = sb;
         M32[bi] = make_float2(sb.x, sb.y);
@@ -404,27 +452,29 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
   }
 }
 
-void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
-                         double2* M64, float2* M32, int* status, cudaStream_t s) {
+template <int kMode>
+static void launch_build_mode(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
+                              double2* M64, float2* M32, int* status, cudaStream_t s) {
   const BuildSmem b = build_smem_layout(P.L, P.nsp, P.ds);
   dim3 grid(unsigned(P.N), unsigned((P.N + kBuildRowAtoms - 1) / kBuildRowAtoms), unsigned(E));
-  // raised once to the largest request (before any stream capture)
-  static int smem_true = 0, smem_false = 0;
-  if (M32) {
-    if (b.total_bytes > smem_true) {
-      cudaFuncSetAttribute(build_system_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
-      smem_true = b.total_bytes;
-    }
-    count_launch();
-    build_system_kernel<true><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, M32, status);
-  } else {
-    if (b.total_bytes > smem_false) {
-      cudaFuncSetAttribute(build_system_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
-      smem_false = b.total_bytes;
-    }
-    count_launch();
-    build_system_kernel<false><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, nullptr, status);
+  static int smem_set = 0;  // raised once to the largest request (before any stream capture)
+  if (b.total_bytes > smem_set) {
+    cudaFuncSetAttribute(build_system_kernel<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
+    smem_set = b.total_bytes;
   }
+  count_launch();
+  build_system_kernel<kMode><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, M32, status);
+}
+
+void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
+                         double2* M64, float2* M32, int* status, cudaStream_t s) {
+  if (M32) launch_build_mode<1>(P, E, k, xphase, lay, M64, M32, status, s);
+  else launch_build_mode<0>(P, E, k, xphase, lay, M64, nullptr, status, s);
+}
+
+void launch_build_g0(const PlanDev& P, int E, const double2* k, const BatchLayout& lay, double2* G0, int* status,
+                     cudaStream_t s) {
+  launch_build_mode<2>(P, E, k, nullptr, lay, G0, nullptr, status, s);
 }
 
 }  // namespace rfx

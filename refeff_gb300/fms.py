@@ -29,6 +29,7 @@ STATUS_NAMES = {
     5: "InvalidAngularLimit", 6: "NonFiniteInput", 7: "NonFiniteCoordinate", 8: "ZeroRho", 9: "SingularMatrix",
     10: "NotConverged", 11: "DuplicateAbsorber", 12: "MissingCentralAtom", 13: "Unsupported", 14: "Cuda",
     15: "OutOfMemory", 16: "InvalidTolerance", 17: "InvalidClusterRadius", 18: "ScratchLimit",
+    19: "IterativeSolverBreakdown",
 }
 
 
@@ -278,7 +279,7 @@ def fms_real_space_spectrum(plan: FmsRealSpacePlan, wave_numbers, phase_shifts, 
     rep = _Report()
     rc = plan.ctx._lib.refeff_fms_real_space_spectrum(plan.handle, C.byref(pts), int(form), _ptr(out), _ptr(status),
                                                       C.byref(rep))
-    if rc and (raise_on_error or rc not in (9, 10, 6, 8)):
+    if rc and (raise_on_error or rc not in (9, 10, 6, 8, 19)):
         raise FmsError(rc, plan.ctx.last_error())
     tabs = out.reshape(E, Cc * Cc * npot)
     scat = np.stack([tabs[e].reshape((Cc, Cc, npot), order="F") for e in range(E)]) if E else \
