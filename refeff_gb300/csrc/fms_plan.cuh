@@ -31,8 +31,10 @@ struct PlanDev {
   const double* sigsqr = nullptr;    // [N*N] (a2 + N*a1), device order
   double* pair_dist = nullptr;       // [N*N] (j + N*i), |R_i - R_j|        (written by launch_plan_geometry)
   double* pair_phi = nullptr;        // [N*N] azimuth of R_i - R_j           (written by launch_plan_geometry)
+  double2* pair_eph = nullptr;       // [N*N*(4L+1)] e^{i mm (phi - pi)}, mm in [-2L, 2L] (launch_plan_geometry)
   double* pair_dsmall = nullptr;     // [N*N][ds] Wigner small-d tables      (written by launch_plan_geometry)
   const double* xnlm = nullptr;      // [(L+1)*(L+1)] xnlm(mu, l) at mu + (L+1)*l
+  const double* xnlm_w = nullptr;    // [(L+1)*(L+1)] (2l+1) / xnlm(mu, l), same index
   const double* t3p = nullptr;       // spin-orbit coefficients [l + (L+1)*((m+L) + (2L+1)*(s-1))]
   const double* t3m = nullptr;
   double rdirec2 = 0.0;              // direct-cutoff radius squared (Angstrom^2)

@@ -101,9 +101,12 @@ __global__ void plan_geometry_kernel(PlanDev P) {
   double r = sqrt(x * x + y * y + z * z);
   double* dsm = P.pair_dsmall + size_t(idx) * P.ds;
   P.pair_dist[idx] = r;
+  const int ne = 4 * L + 1;
+  double2* eph = P.pair_eph + size_t(idx) * ne;
   if (i == j) {
     P.pair_phi[idx] = 0.0;
     for (int q = 0; q < P.ds; ++q) dsm[q] = 0.0;
+    for (int q = 0; q < ne; ++q) eph[q] = make_double2(0.0, 0.0);
     return;
   }
   // getang with FEFF's single-precision threshold
@@ -118,6 +121,12 @@ __global__ void plan_geometry_kernel(PlanDev P) {
   else if (z < r) theta = acos(z / r);
   else theta = 0.0;
   P.pair_phi[idx] = phi;
+  // azimuth phases e^{i mm (phi - pi)} of the G0 element, energy independent
+  for (int mm = -2 * L; mm <= 2 * L; ++mm) {
+    double sn, cs;
+    sincos(double(mm) * (phi - 3.14159265358979323846), &sn, &cs);
+    eph[mm + 2 * L] = make_double2(cs, sn);
+  }
   rotxan_small_d<L>(theta, dsm);                        // forward, beta
   rotxan_small_d<L>(-theta, dsm + dsmall_per_dir(L));   // backward, -beta
 }
@@ -289,28 +298,38 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     tcol1[q] = t1;
   }
   // ---- rows of the chunk ----
-  for (int rr = tid; rr < nrow; rr += nthr) {
-    const int r = r0 + rr;
-    int p = 0;
-    while (P.atom_off[i0 + p + 1] <= r) ++p;
-    const int q = r - P.atom_off[i0 + p];
-    const int s = q % nsp + 1, lm = q / nsp;
-    int l = 0;
-    while ((l + 1) * (l + 1) <= lm) ++l;
-    rowinfo[rr] = make_int4(p, l, lm - l * l - l, s);
+  // Rows are visited grouped by (l, spin), then atom and m, so that the lanes
+  // of a warp share l1 and the spin: the mu loop below has one trip count per
+  // warp and no lane idles on a spin mismatch.
+  // rowinfo[v] = (atom << 2 | spin, l, m, row offset in the chunk).
+  for (int v = tid; v < nrow; v += nthr) {
+    int l = 0, w = v, cnt = 0;
+    for (;; ++l) {
+      cnt = 0;
+      for (int p = 0; p < RA; ++p) cnt += P.atom_lmax[i0 + p] >= l;
+      const int group = cnt * (2 * l + 1) * nsp;
+      if (w < group) break;
+      w -= group;
+    }
+    const int per_spin = cnt * (2 * l + 1);
+    const int sp = w / per_spin + 1;
+    w %= per_spin;
+    int k = w / (2 * l + 1), p = 0;
+    for (;; ++p)
+      if (P.atom_lmax[i0 + p] >= l && k-- == 0) break;
+    const int m = w % (2 * l + 1) - l;
+    const int rr = P.atom_off[i0 + p] - r0 + (l * l + (m + l)) * nsp + (sp - 1);
+    rowinfo[v] = make_int4((p << 2) | sp, l, m, rr);
   }
   // ---- per pair: small-d tables (resident, from the plan) ----
   for (int t = tid; t < RA * P.ds; t += nthr) {
     const int p = t / P.ds, q = t % P.ds;
     dsm[t] = P.pair_dsmall[(size_t(j) + size_t(N) * (i0 + p)) * P.ds + q];
   }
-  // ---- per pair: azimuth phases e^{i m (phi - pi)}, m in [-2L, 2L] ----
+  // ---- per pair: azimuth phases e^{i m (phi - pi)}, m in [-2L, 2L] (resident, from the plan) ----
   for (int t = tid; t < RA * (4 * L + 1); t += nthr) {
-    const int p = t / (4 * L + 1), mm = t % (4 * L + 1) - 2 * L;
-    const double ang = double(mm) * (P.pair_phi[size_t(j) + size_t(N) * (i0 + p)] - 3.14159265358979323846);
-    double sn, cs;
-    sincos(ang, &sn, &cs);
-    eph[t] = make_double2(cs, sn);
+    const int p = t / (4 * L + 1), q = t % (4 * L + 1);
+    eph[t] = P.pair_eph[(size_t(j) + size_t(N) * (i0 + p)) * (4 * L + 1) + q];
   }
   // ---- per (pair, spin): rho, prefactor, Hankel polynomial table ----
   const int rows = L + 2;
@@ -370,17 +389,17 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     double2 g = make_double2(0.0, 0.0);
     if (flag[p] && mu <= l1 && mu <= l2) {
       const double2* c = clm + size_t(ps) * rows * L1;
-      const double n1 = P.xnlm[mu + L1 * l1], n2 = P.xnlm[mu + L1 * l2];
-      const double w = double(2 * l1 + 1);
+      const double wn1 = P.xnlm_w[mu + L1 * l1], n2 = P.xnlm[mu + L1 * l2];
       const double sgn = (mu & 1) ? -1.0 : 1.0;
       const int numax = min(l1, l2 - mu);
       for (int nu = 0; nu <= numax; ++nu) {
         const double2 cl1 = c[l1 + rows * nu];
         const double2 cl2 = c[l2 + rows * (mu + nu)];
-        const double2 gamtl = make_double2(w * cl1.x / n1, w * cl1.y / n1);
+        const double2 gamtl = make_double2(cl1.x * wn1, cl1.y * wn1);  // (2 l1 + 1) c / xnlm
         const double2 gam = make_double2(cl2.x * (sgn * n2), cl2.y * (sgn * n2));
         g = cadd(g, cmul(gamtl, gam));
       }
+      g = cmul(pref[ps], g);  // the pair prefactor e^{i rho}/rho e^{-msd k^2}, folded in once per table entry
     }
     gtab[t] = g;
   }
@@ -395,32 +414,32 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     const double* tf = dsm + size_t(p) * P.ds + lblock_offset(l2);          // forward (beta), l2 block
     const double* tb = dsm + size_t(p) * P.ds + dpd + lblock_offset(l1);    // backward (-beta), l1 block
     const double2* gg = gtab + size_t(p * nsp + (s1 - 1)) * gsz;
-    const int w1 = 2 * l1 + 1, w2 = 2 * l2 + 1;
+    const int w1 = 2 * l1 + 1, w2 = 2 * l2 + 1, mn = min(l1, l2);
     double sx = 0.0, sy = 0.0;
-    for (int mu = -l1; mu <= l1; ++mu) {
+    for (int mu = -mn; mu <= mn; ++mu) {
       const int amu = mu < 0 ? -mu : mu;
-      if (amu > l2) continue;
       const double dd = tb[(mu + l1) * w1 + (m1 + l1)] * tf[(m2 + l2) * w2 + (mu + l2)];
       const double2 gv = gg[l1 + L1 * (l2 + L1 * amu)];
       sx = fma(dd, gv.x, sx);
       sy = fma(dd, gv.y, sy);
     }
     const double2 ph = eph[p * (4 * L + 1) + (m2 - m1 + 2 * L)];
-    return cmul(pref[p * nsp + (s1 - 1)], cmul(ph, make_double2(sx, sy)));
+    return cmul(ph, make_double2(sx, sy));
   };
   const int total = nrow * ncol;
   for (int idx = tid; idx < total; idx += nthr) {
-    const int rr = idx % nrow, cc = idx / nrow;
-    const int4 ri = rowinfo[rr];
+    const int v = idx % nrow, cc = idx / nrow;
+    const int4 ri = rowinfo[v];
     const int4 ci = colinfo[cc];
-    const int r = r0 + rr, c = cj0 + cc;
+    const int rp = ri.x >> 2, rs = ri.x & 3;
+    const int r = r0 + ri.w, c = cj0 + cc;
     double2 a = make_double2(0.0, 0.0), gcol = make_double2(0.0, 0.0);
-    if (i0 + ri.x != j) {
-      gcol = g0(ri.x, ri.y, ri.z, ri.w, ci.x, ci.y, ci.z);
+    if (i0 + rp != j) {
+      gcol = g0(rp, ri.y, ri.z, rs, ci.x, ci.y, ci.z);
       a = cneg(cmul(gcol, tcol0[cc]));
       if (kMode != 2 && ci.w >= 0) {
         const int4 pi = colinfo[ci.w];
-        const double2 gp = g0(ri.x, ri.y, ri.z, ri.w, pi.x, pi.y, pi.z);
+        const double2 gp = g0(rp, ri.y, ri.z, rs, pi.x, pi.y, pi.z);
         a = csub(a, cmul(gp, tcol1[cc]));
       }
     }
