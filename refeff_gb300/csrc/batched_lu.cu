@@ -410,28 +410,49 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double 
 // R = B - A X.  A and B are stored as hi/lo float pairs (float4 per complex
 // entry, exact to about 2^-48) and X in FP64; the products are accumulated in
 // double-float on the FP32 pipes (GB300's FP64 rate is a small fraction of its
-// FP32 rate).  CTA: 32 rows x all m columns (8 column groups); K in chunks of 32.
-constexpr int kResRows = 32, kResK = 32, kResMaxM = 64, kResGroups = 8;
-__global__ void __launch_bounds__(256) residual_split_kernel(BatchLayout lay, const float4* __restrict__ Ms,
-                                                             const double2* __restrict__ X64, double2* __restrict__ R,
-                                                             unsigned long long* rnorm, unsigned long long* bnorm,
-                                                             const int* skip) {
-  constexpr int BR = kResRows, BK = kResK, kCols = kResMaxM / kResGroups;
+// FP32 rate).
+//
+// x (FP64) -> (hi.re, hi.im, lo.re, lo.im) once per residual, so that the
+// residual CTAs read a ready split instead of each converting all of x.
+__global__ void split_x_kernel(BatchLayout lay, const double2* __restrict__ X64, float4* __restrict__ Xs,
+                               const int* skip) {
   const int b = blockIdx.y;
   if (skip && skip[b]) return;
-  extern __shared__ float4 sm4[];
-  float4* As = sm4;            // [BK][BR]
-  float4* Xs = sm4 + BK * BR;  // [BK][kResMaxM] x split as (hi.re, hi.im, lo.re, lo.im)
+  const size_t base = size_t(b) * lay.lda * lay.m;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < lay.n * lay.m; idx += gridDim.x * blockDim.x) {
+    const int r = idx % lay.n, c = idx / lay.n;
+    const size_t i = base + size_t(r) + size_t(lay.lda) * c;
+    Xs[i] = split_hi_lo(X64[i]);
+  }
+}
+
+// r = b - A x in double-float: 64 rows per CTA, each thread two rows (r, r + 32)
+// and kCols right-hand sides (columns cg, cg + 8, ...), so that every a and x
+// value read from shared memory feeds several complex MACs.
+constexpr int kRdRows = 64, kRdK = 32, kRdGroups = 8;
+
+template <int kCols>
+__global__ void __launch_bounds__(256) residual_df_kernel(BatchLayout lay, const float4* __restrict__ Ms,
+                                                          const float4* __restrict__ Xsp, double2* __restrict__ R,
+                                                          unsigned long long* rnorm, unsigned long long* bnorm,
+                                                          const int* skip) {
+  constexpr int BR = kRdRows, BK = kRdK, XW = kCols * kRdGroups;
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  extern __shared__ float4 rd_sm[];
+  float4* As = rd_sm;            // [BK][BR]
+  float4* Xs = rd_sm + BK * BR;  // [BK][XW]
   const int n = lay.n, m = lay.m;
   const int r0 = blockIdx.x * BR;
   const float4* A = Ms + size_t(b) * lay.stride;
-  const double2* X = X64 + size_t(b) * lay.lda * m;
+  const float4* X = Xsp + size_t(b) * lay.lda * m;
   double2* Rb = R + size_t(b) * lay.lda * m;
-  const int tid = threadIdx.x;
-  const int row = tid % BR, cg0 = tid / BR;
-  df accr[kCols], acci[kCols];
+  const int tid = threadIdx.x, rp = tid & 31, cg = tid >> 5;
+  df acc[2][kCols][2];
 #pragma unroll
-  for (int q = 0; q < kCols; ++q) { accr[q] = {0.f, 0.f}; acci[q] = {0.f, 0.f}; }
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int q = 0; q < kCols; ++q) acc[h][q][0] = acc[h][q][1] = {0.f, 0.f};
   for (int k0 = 0; k0 < n; k0 += BK) {
     const int kk_n = min(BK, n - k0);
     __syncthreads();
@@ -440,41 +461,44 @@ __global__ void __launch_bounds__(256) residual_split_kernel(BatchLayout lay, co
       As[kk * BR + r] = (r0 + r < n && kk < kk_n) ? A[size_t(r0 + r) + size_t(lay.lda) * (k0 + kk)]
                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int idx = tid; idx < BK * m; idx += 256) {
+    for (int idx = tid; idx < BK * XW; idx += 256) {
       const int kk = idx % BK, c = idx / BK;
-      Xs[kk * kResMaxM + c] = kk < kk_n ? split_hi_lo(X[size_t(k0 + kk) + size_t(lay.lda) * c])
-                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+      Xs[kk * XW + c] = (kk < kk_n && c < m) ? X[size_t(k0 + kk) + size_t(lay.lda) * c] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
     for (int kk = 0; kk < kk_n; ++kk) {
-      const float4 a = As[kk * BR + row];
+      const float4 a0 = As[kk * BR + rp], a1 = As[kk * BR + rp + 32];
 #pragma unroll
       for (int q = 0; q < kCols; ++q) {
-        const int c = cg0 + kResGroups * q;
-        if (c >= m) continue;
-        const float4 x = Xs[kk * kResMaxM + c];
-        df_mac(accr[q], a.x, a.z, x.x, x.z);    // re += a.re x.re
-        df_mac(accr[q], -a.y, -a.w, x.y, x.w);  // re -= a.im x.im
-        df_mac(acci[q], a.x, a.z, x.y, x.w);    // im += a.re x.im
-        df_mac(acci[q], a.y, a.w, x.x, x.z);    // im += a.im x.re
+        const float4 x = Xs[kk * XW + cg + kRdGroups * q];
+        df_mac(acc[0][q][0], a0.x, a0.z, x.x, x.z);    // re += a.re x.re
+        df_mac(acc[0][q][0], -a0.y, -a0.w, x.y, x.w);  // re -= a.im x.im
+        df_mac(acc[0][q][1], a0.x, a0.z, x.y, x.w);    // im += a.re x.im
+        df_mac(acc[0][q][1], a0.y, a0.w, x.x, x.z);    // im += a.im x.re
+        df_mac(acc[1][q][0], a1.x, a1.z, x.x, x.z);
+        df_mac(acc[1][q][0], -a1.y, -a1.w, x.y, x.w);
+        df_mac(acc[1][q][1], a1.x, a1.z, x.y, x.w);
+        df_mac(acc[1][q][1], a1.y, a1.w, x.x, x.z);
       }
     }
-#pragma unroll
-    for (int q = 0; q < kCols; ++q) { df_renorm(accr[q]); df_renorm(acci[q]); }
   }
   double rmax = 0.0, bmax = 0.0;
-  const bool row_ok = r0 + row < n;
 #pragma unroll
-  for (int q = 0; q < kCols; ++q) {
-    const int c = cg0 + kResGroups * q;
-    if (c >= m || !row_ok) continue;
-    const double2 bv = join_hi_lo(A[size_t(r0 + row) + size_t(lay.lda) * (n + c)]);
-    const double ax = double(accr[q].hi) + double(accr[q].lo);
-    const double ay = double(acci[q].hi) + double(acci[q].lo);
-    const double2 rv = make_double2(bv.x - ax, bv.y - ay);
-    Rb[size_t(r0 + row) + size_t(lay.lda) * c] = rv;
-    rmax = fmax(rmax, cabs1(rv));
-    bmax = fmax(bmax, cabs1(bv));
+  for (int h = 0; h < 2; ++h) {
+    const int row = r0 + rp + 32 * h;
+    if (row >= n) continue;
+#pragma unroll
+    for (int q = 0; q < kCols; ++q) {
+      const int c = cg + kRdGroups * q;
+      if (c >= m) continue;
+      const double2 bv = join_hi_lo(A[size_t(row) + size_t(lay.lda) * (n + c)]);
+      const double ax = double(acc[h][q][0].hi) + double(acc[h][q][0].lo);
+      const double ay = double(acc[h][q][1].hi) + double(acc[h][q][1].lo);
+      const double2 rv = make_double2(bv.x - ax, bv.y - ay);
+      Rb[size_t(row) + size_t(lay.lda) * c] = rv;
+      rmax = fmax(rmax, cabs1(rv));
+      bmax = fmax(bmax, cabs1(bv));
+    }
   }
   for (int off = 16; off > 0; off >>= 1) {
     rmax = fmax(rmax, __shfl_down_sync(0xffffffffu, rmax, off));
@@ -766,18 +790,32 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
   absorber_solve_kernel<T><<<unsigned(batch), threads, smem, s>>>(lay, M, gg, status);
 }
 
-void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, double2* R,
-                     unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
-                     cudaStream_t s) {
-  constexpr size_t smem = size_t(kResK) * (kResRows + kResMaxM) * sizeof(float4);
+template <int kCols>
+static void launch_residual_df(const BatchLayout& lay, int batch, const float4* Ms, const float4* Xs, double2* R,
+                               unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
+                               cudaStream_t s) {
+  constexpr size_t smem = size_t(kRdK) * (kRdRows + kCols * kRdGroups) * sizeof(float4);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(residual_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaFuncSetAttribute(residual_df_kernel<kCols>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     attr_set = true;
   }
-  dim3 grid(unsigned((lay.n + kResRows - 1) / kResRows), unsigned(batch));
+  dim3 grid(unsigned((lay.n + kRdRows - 1) / kRdRows), unsigned(batch));
   count_launch();
-  residual_split_kernel<<<grid, 256, smem, s>>>(lay, Ms, X64, R, rnorm_bits, bnorm_bits, skip);
+  residual_df_kernel<kCols><<<grid, 256, smem, s>>>(lay, Ms, Xs, R, rnorm_bits, bnorm_bits, skip);
+}
+
+void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
+                     double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
+                     cudaStream_t s) {
+  {
+    dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
+    count_launch();
+    split_x_kernel<<<grid, 256, 0, s>>>(lay, X64, Xsplit, skip);
+  }
+  if (lay.m <= 16) launch_residual_df<2>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else if (lay.m <= 32) launch_residual_df<4>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else launch_residual_df<8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
 }
 
 void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,

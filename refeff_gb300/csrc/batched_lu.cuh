@@ -70,8 +70,9 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
 // (float4 per entry, see split_hi_lo).
 // R = B - A * X64 (double-float accumulation) and per matrix rnorm = max |R|,
 // bnorm = max |B| (|re|+|im|); matrices with skip[b] != 0 are left untouched.
-void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, double2* R,
-                     unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip, cudaStream_t s);
+void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
+                     double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
+                     cudaStream_t s);
 // In place: M (double2 entries) -> hi/lo float4 entries, M32 <- hi (for the dense solve API).
 void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* M32, cudaStream_t s);
 // RHS columns of M32 <- float(R / rnorm_b)

@@ -307,6 +307,7 @@ struct Workspace {
   DevBuf<double2> M64;
   DevBuf<float2> M32;
   DevBuf<double2> X64, R;
+  DevBuf<float4> Xsplit;  // x as hi/lo float pairs for the residual
   DevBuf<double2> t_tab, grow, iter_scratch;  // iterative forms (minv != 0)
   DevBuf<unsigned long long> rnorm, bnorm, dnorm, xnorm;
   DevBuf<double> dprev;
@@ -596,6 +597,7 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
     RF_CUDA(ctx, ws.M32.alloc(size_t(B) * lay.stride));
     RF_CUDA(ctx, ws.X64.alloc(size_t(B) * lay.lda * m));
     RF_CUDA(ctx, ws.R.alloc(size_t(B) * lay.lda * m));
+    RF_CUDA(ctx, ws.Xsplit.alloc(size_t(B) * lay.lda * m));
     RF_CUDA(ctx, ws.rnorm.alloc(size_t(B)));
     RF_CUDA(ctx, ws.bnorm.alloc(size_t(B)));
     RF_CUDA(ctx, ws.dnorm.alloc(size_t(B)));
@@ -670,7 +672,7 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
     span(3, [&] {
       cudaMemsetAsync(ws.rnorm.p, 0, nb8, s);
       cudaMemsetAsync(ws.bnorm.p, 0, nb8, s);
-      launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.R.p, ws.rnorm.p,
+      launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.Xsplit.p, ws.R.p, ws.rnorm.p,
                       ws.bnorm.p, ws.converged.p, s);
     });
     span(2, [&] {
