@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
 
 // One warp per column in [c_begin, c_end): apply the panel's row moves, then
 // solve the panel rows with the unit lower L11.
-template <typename T, int NB>
+template <typename T, int NB, bool kSolve = true>
 __global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, int c_begin, int c_end,
                                                         cplx<T>* __restrict__ M, LuWork w, const int* skip) {
   using C = cplx<T>;
@@ -225,6 +225,7 @@ __global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, 
   for (int t = 0; t < kMoves; ++t)
     if (dst[t] >= 0) colp[dst[t]] = v[t];
   __syncwarp();
+  if (!kSolve) return;
   constexpr int kRows = (NB + 31) / 32;
   C x[kRows];
 #pragma unroll
@@ -636,6 +637,26 @@ PanelConfig choose_panel(int n) {
   return pc;
 }
 
+// Panel configuration for a fixed panel width (the 32-column inner panels).
+template <typename T>
+PanelConfig choose_panel_nb(int n, int nb) {
+  PanelConfig pc;
+  const size_t budget = 200 * 1024;
+  for (int cl = 1; cl <= 16; cl *= 2) {
+    const int rpc = (n + cl - 1) / cl;
+    const size_t b = nb == 64 ? panel_smem_bytes<T, 64>(rpc, n) : panel_smem_bytes<T, 32>(rpc, n);
+    if (b <= budget) {
+      pc.nb = nb;
+      pc.cluster = cl;
+      pc.rpc_max = rpc;
+      pc.smem = int(b);
+      return pc;
+    }
+  }
+  pc.cluster = 0;
+  return pc;
+}
+
 template <typename T, int NB>
 static cudaError_t launch_panel(const PanelConfig& pc, const BatchLayout& lay, int batch, int k, cplx<T>* M,
                                 const LuWork& w, cudaStream_t s) {
@@ -670,14 +691,51 @@ static cudaError_t launch_panel(const PanelConfig& pc, const BatchLayout& lay, i
   return cudaLaunchKernelEx(&cfg, kern, lay, k, M, w, pc.rpc_max);
 }
 
-template <typename T, int NB>
+template <typename T, int NB, bool kSolve = true>
 static void launch_rhs_lower(const BatchLayout& lay, int batch, int k, int c_begin, int c_end, cplx<T>* M,
                              const LuWork& w, const int* skip, cudaStream_t s) {
   const int ncols = c_end - c_begin;
   if (ncols <= 0) return;
   dim3 grid(unsigned((ncols + 7) / 8), unsigned(batch));
   count_launch();
-  rhs_lower_kernel<T, NB><<<grid, 256, 0, s>>>(lay, k, c_begin, c_end, M, w, skip);
+  rhs_lower_kernel<T, NB, kSolve><<<grid, 256, 0, s>>>(lay, k, c_begin, c_end, M, w, skip);
+}
+
+// Composes the row moves of the two inner panels of an outer block into one
+// gather list: after both, row d holds the original row f(d), f = src0(src1(d)).
+__global__ void compose_moves_kernel(int batch, int n, int k, LuWork w_out, LuWork w_in, int two) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  const int p0 = k / 32;
+  const int2* m0 = w_in.perm + (size_t(b) * w_in.npanels + p0) * 64;
+  const int n0 = w_in.nperm[size_t(b) * w_in.npanels + p0];
+  const int2* m1 = two ? w_in.perm + (size_t(b) * w_in.npanels + p0 + 1) * 64 : nullptr;
+  const int n1 = two ? w_in.nperm[size_t(b) * w_in.npanels + p0 + 1] : 0;
+  int2* out = w_out.perm + (size_t(b) * w_out.npanels + k / 64) * 128;
+  auto src0 = [&](int x) {
+    for (int i = 0; i < n0; ++i)
+      if (m0[i].x == x) return m0[i].y;
+    return x;
+  };
+  auto src1 = [&](int x) {
+    for (int i = 0; i < n1; ++i)
+      if (m1[i].x == x) return m1[i].y;
+    return x;
+  };
+  int cnt = 0;
+  for (int i = 0; i < n0; ++i) {  // rows moved by the first panel
+    const int d = m0[i].x, f = src0(src1(d));
+    if (f != d && cnt < 128) out[cnt++] = make_int2(d, f);
+  }
+  for (int i = 0; i < n1; ++i) {  // rows moved only by the second panel
+    const int d = m1[i].x;
+    bool seen = false;
+    for (int q = 0; q < n0; ++q) seen |= m0[q].x == d;
+    if (seen) continue;
+    const int f = src0(src1(d));
+    if (f != d && cnt < 128) out[cnt++] = make_int2(d, f);
+  }
+  w_out.nperm[size_t(b) * w_out.npanels + k / 64] = cnt;
 }
 
 template <typename T, int TM, int TN, int KMAX>
@@ -722,11 +780,60 @@ static void gemm_any(int nb, const BatchLayout& lay, int batch, int r_begin, int
   }
 }
 
+// FP32 tensor-core elimination with two-level blocking: each 64-column outer
+// block is factored as two 32-column cluster panels (half the on-chip panel
+// footprint, so twice the matrices resident per wave); the second inner
+// panel's row moves are applied to the first panel's L columns, the two move
+// lists are composed, and the trailing matrix gets one K = 64 tensor-core
+// update per outer block.
+static cudaError_t lu_eliminate_two_level(const BatchLayout& lay, int batch, float2* M, const LuWork& w,
+                                          cudaStream_t s) {
+  const int n = lay.n, col_end = lay.n + lay.m;
+  static int cached_n = -1;
+  static PanelConfig pin;
+  if (cached_n != n) {
+    pin = choose_panel_nb<float>(n, 32);
+    cached_n = n;
+  }
+  if (pin.cluster <= 0 || w.nb != 64) return cudaErrorInvalidValue;
+  LuWork wi = w;
+  wi.perm = w.perm_in;
+  wi.nperm = w.nperm_in;
+  wi.nb = 32;
+  wi.npanels = panel_count(n, 32);
+  for (int k = 0; k < n; k += 64) {
+    const int kb = min(64, n - k);
+    const int kb0 = min(32, kb);
+    const bool two = kb > 32;
+    cudaError_t err = launch_panel<float, 32>(pin, lay, batch, k, M, wi, s);
+    if (err != cudaSuccess) return err;
+    if (two) {
+      // second inner panel's columns: moves + L11 of the first, then its rank-32 update
+      launch_rhs_lower<float, 32>(lay, batch, k, k + kb0, k + kb, M, wi, nullptr, s);
+      gemm_any<float>(32, lay, batch, k + kb0, n, k + kb0, k + kb, k, kb0, M, nullptr, s);
+      err = launch_panel<float, 32>(pin, lay, batch, k + kb0, M, wi, s);
+      if (err != cudaSuccess) return err;
+      // the second panel's row moves on the first panel's L columns
+      launch_rhs_lower<float, 32, false>(lay, batch, k + kb0, k, k + kb0, M, wi, nullptr, s);
+    }
+    count_launch();
+    compose_moves_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, n, k, w, wi, two ? 1 : 0);
+    launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
+    tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return err;
+  }
+  return cudaSuccess;
+}
+
 template <typename T>
 cudaError_t lu_eliminate(const PanelConfig& pc, const BatchLayout& lay, int batch, cplx<T>* M, const LuWork& w,
                          cudaStream_t s) {
   const int n = lay.n, col_end = lay.n + lay.m;
   if (pc.cluster <= 0 || w.nb != pc.nb) return cudaErrorInvalidValue;
+  if constexpr (sizeof(T) == 4) {
+    if (w.tc_images && w.perm_in && pc.nb == 64) return lu_eliminate_two_level(lay, batch, M, w, s);
+  }
   for (int k = 0; k < n; k += pc.nb) {
     const int kb = min(pc.nb, n - k);
     cudaError_t err;

@@ -36,6 +36,11 @@ struct LuWork {
   int* nperm = nullptr;   // [batch][npanels]
   int* status = nullptr;  // [batch] DevStatus (max-reduced)
   int* info = nullptr;    // [batch] first zero pivot (1-based, 0 = none)
+  // Two-level FP32 elimination (tensor-core path): row moves of the 32-column
+  // inner panels, [batch][ceil(n/32)][64] and [batch][ceil(n/32)]; the outer
+  // 64-column blocks keep their composed moves in perm / nperm.
+  int2* perm_in = nullptr;
+  int* nperm_in = nullptr;
   int npanels = 0;
   int nb = 0;
 };

@@ -318,6 +318,8 @@ struct Workspace {
   DevBuf<uint8_t> tc_images;         // operand images of the tensor-core update
   DevBuf<int> tc_err;                // set by a tensor-core wait that timed out
   DevBuf<int2> perm;
+  DevBuf<int2> perm_in;              // row moves of the 32-column inner panels (two-level FP32 LU)
+  DevBuf<int> nperm_in;
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
   std::map<int, cudaGraphExec_t> graphs;  // key: form
@@ -614,6 +616,8 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
   RF_CUDA(ctx, ws.info.alloc(size_t(B)));
   ws.use_tc = ws.fp32 && ctx->use_tensor_cores != 0;
   if (ws.use_tc) {
+    RF_CUDA(ctx, ws.perm_in.alloc(size_t(B) * panel_count(n, 32) * 64));
+    RF_CUDA(ctx, ws.nperm_in.alloc(size_t(B) * panel_count(n, 32)));
     RF_CUDA(ctx, ws.tc_images.alloc(tc_image_bytes(n, m, B)));
     RF_CUDA(ctx, ws.tc_err.alloc(1));
     RF_CUDA(ctx, cudaMemset(ws.tc_err.p, 0, sizeof(int)));
@@ -633,6 +637,8 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
   if (&pc == &ws.pc32 && ws.use_tc) {
     w.tc_images = ws.tc_images.p;
     w.tc_err = ws.tc_err.p;
+    w.perm_in = ws.perm_in.p;
+    w.nperm_in = ws.nperm_in.p;
   }
   return w;
 }
