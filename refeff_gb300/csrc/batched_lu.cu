@@ -703,39 +703,42 @@ static void launch_rhs_lower(const BatchLayout& lay, int batch, int k, int c_beg
 
 // Composes the row moves of the two inner panels of an outer block into one
 // gather list: after both, row d holds the original row f(d), f = src0(src1(d)).
-__global__ void compose_moves_kernel(int batch, int n, int k, LuWork w_out, LuWork w_in, int two) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch) return;
+// One CTA of 128 threads per matrix, both lists in shared memory.
+__global__ void __launch_bounds__(128) compose_moves_kernel(int n, int k, LuWork w_out, LuWork w_in, int two) {
+  const int b = blockIdx.x;
+  __shared__ int2 m0[64], m1[64];
+  __shared__ int cnt;
   const int p0 = k / 32;
-  const int2* m0 = w_in.perm + (size_t(b) * w_in.npanels + p0) * 64;
   const int n0 = w_in.nperm[size_t(b) * w_in.npanels + p0];
-  const int2* m1 = two ? w_in.perm + (size_t(b) * w_in.npanels + p0 + 1) * 64 : nullptr;
   const int n1 = two ? w_in.nperm[size_t(b) * w_in.npanels + p0 + 1] : 0;
+  const int t = threadIdx.x;
+  if (t < n0) m0[t] = w_in.perm[(size_t(b) * w_in.npanels + p0) * 64 + t];
+  if (t < n1) m1[t] = w_in.perm[(size_t(b) * w_in.npanels + p0 + 1) * 64 + t];
+  if (t == 0) cnt = 0;
+  __syncthreads();
   int2* out = w_out.perm + (size_t(b) * w_out.npanels + k / 64) * 128;
-  auto src0 = [&](int x) {
-    for (int i = 0; i < n0; ++i)
-      if (m0[i].x == x) return m0[i].y;
-    return x;
-  };
-  auto src1 = [&](int x) {
-    for (int i = 0; i < n1; ++i)
-      if (m1[i].x == x) return m1[i].y;
-    return x;
-  };
-  int cnt = 0;
-  for (int i = 0; i < n0; ++i) {  // rows moved by the first panel
-    const int d = m0[i].x, f = src0(src1(d));
-    if (f != d && cnt < 128) out[cnt++] = make_int2(d, f);
+  // thread t < 64 handles the first list's destinations, t >= 64 the second's
+  int d = -1;
+  if (t < 64) {
+    if (t < n0) d = m0[t].x;
+  } else if (t - 64 < n1) {
+    d = m1[t - 64].x;
+    for (int q = 0; q < n0; ++q)
+      if (m0[q].x == d) d = -1;  // already handled with the first list
   }
-  for (int i = 0; i < n1; ++i) {  // rows moved only by the second panel
-    const int d = m1[i].x;
-    bool seen = false;
-    for (int q = 0; q < n0; ++q) seen |= m0[q].x == d;
-    if (seen) continue;
-    const int f = src0(src1(d));
-    if (f != d && cnt < 128) out[cnt++] = make_int2(d, f);
+  if (d >= 0) {
+    int f = d;
+    for (int q = 0; q < n1; ++q)
+      if (m1[q].x == f) { f = m1[q].y; break; }
+    for (int q = 0; q < n0; ++q)
+      if (m0[q].x == f) { f = m0[q].y; break; }
+    if (f != d) {
+      const int slot = atomicAdd(&cnt, 1);
+      if (slot < 128) out[slot] = make_int2(d, f);
+    }
   }
-  w_out.nperm[size_t(b) * w_out.npanels + k / 64] = cnt;
+  __syncthreads();
+  if (t == 0) w_out.nperm[size_t(b) * w_out.npanels + k / 64] = min(cnt, 128);
 }
 
 template <typename T, int TM, int TN, int KMAX>
@@ -817,7 +820,7 @@ static cudaError_t lu_eliminate_two_level(const BatchLayout& lay, int batch, flo
       launch_rhs_lower<float, 32, false>(lay, batch, k + kb0, k, k + kb0, M, wi, nullptr, s);
     }
     count_launch();
-    compose_moves_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, n, k, w, wi, two ? 1 : 0);
+    compose_moves_kernel<<<batch, 128, 0, s>>>(n, k, w, wi, two ? 1 : 0);
     launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
     tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
     err = cudaGetLastError();
