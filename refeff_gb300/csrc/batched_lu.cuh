@@ -75,6 +75,13 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
 // (float4 per entry, see split_hi_lo).
 // R = B - A * X64 (double-float accumulation) and per matrix rnorm = max |R|,
 // bnorm = max |B| (|re|+|im|); matrices with skip[b] != 0 are left untouched.
+// Whole forward / backward sweeps of the right-hand-side columns in one launch
+// (sweeps.cu); false when the right-hand sides do not fit in shared memory,
+// in which case nothing was launched.
+bool fused_forward_sweep(int nb, const BatchLayout& lay, int batch, float2* M, const LuWork& w, const int* skip,
+                         cudaStream_t s);
+bool fused_backward_sweep(int nb, const BatchLayout& lay, int batch, float2* M, const int* skip, cudaStream_t s);
+
 void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
                      double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
                      cudaStream_t s);

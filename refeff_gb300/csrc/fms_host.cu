@@ -668,8 +668,17 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
     }
   };
   const size_t nb8 = size_t(batch) * sizeof(unsigned long long);
+  // fused one-CTA-per-(matrix, column group) sweeps when the right-hand sides fit in shared memory
+  auto forward = [&](const int* skip) {
+    if (!fused_forward_sweep(ws.pc32.nb, lay, batch, ws.M32.p, w32, skip, s))
+      lu_forward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, w32, skip, s);
+  };
+  auto backward = [&](const int* skip) {
+    if (!fused_backward_sweep(ws.pc32.nb, lay, batch, ws.M32.p, skip, s))
+      lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, skip, s);
+  };
   span(2, [&] {
-    lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, nullptr, s);
+    backward(nullptr);
     launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, true, nullptr, nullptr, nullptr, s);
   });
   cudaMemsetAsync(ws.converged.p, 0, size_t(batch) * sizeof(int), s);
@@ -685,8 +694,8 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
       cudaMemsetAsync(ws.dnorm.p, 0, nb8, s);
       cudaMemsetAsync(ws.xnorm.p, 0, nb8, s);
       launch_residual_to_rhs32(lay, batch, ws.R.p, ws.rnorm.p, ws.M32.p, ws.converged.p, s);
-      lu_forward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, w32, ws.converged.p, s);
-      lu_backward_rhs<float>(ws.pc32, lay, batch, ws.M32.p, ws.converged.p, s);
+      forward(ws.converged.p);
+      backward(ws.converged.p);
       launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, false, ws.converged.p, ws.dnorm.p,
                                    ws.xnorm.p, s);
       launch_ir_check(batch, ws.rnorm.p, ws.bnorm.p, ws.dnorm.p, ws.xnorm.p, tol, ws.converged.p, ws.iters.p,
