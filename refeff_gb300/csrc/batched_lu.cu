@@ -30,14 +30,29 @@ namespace rfx {
 constexpr int kPanelThreads = 256;
 
 template <typename T, int NB>
-static size_t panel_smem_bytes(int rpc_max, int n) {
+static size_t panel_smem_bytes(int rpc_max, int n, bool pos_global) {
   size_t b = size_t(NB) * rpc_max * sizeof(cplx<T>);  // panel
   b += NB * sizeof(cplx<T>);                          // pivot row copy
   b += 2 * 16;                                        // arg-max slots
   b += size_t(rpc_max) * sizeof(int);                 // done flags
-  b += 2 * size_t(n) * sizeof(int);                   // row2pos / pos2row (rank 0)
+  if (!pos_global) b += 2 * size_t(n) * sizeof(int);  // row2pos / pos2row (rank 0)
   b += 64;                                            // scratch
   return (b + 15) / 16 * 16;
+}
+
+static size_t panel_smem_any(int elem, int nb, int rpc, int n, bool pos_global) {
+  if (elem == 8) {
+    switch (nb) {
+      case 64: return panel_smem_bytes<float, 64>(rpc, n, pos_global);
+      case 32: return panel_smem_bytes<float, 32>(rpc, n, pos_global);
+      default: return panel_smem_bytes<float, 16>(rpc, n, pos_global);
+    }
+  }
+  switch (nb) {
+    case 32: return panel_smem_bytes<double, 32>(rpc, n, pos_global);
+    case 16: return panel_smem_bytes<double, 16>(rpc, n, pos_global);
+    default: return panel_smem_bytes<double, 8>(rpc, n, pos_global);
+  }
 }
 
 template <typename T>
@@ -73,9 +88,11 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
   C* urow = pan + size_t(NB) * rpc_max;
   ArgSlot<T>* slot = reinterpret_cast<ArgSlot<T>*>(urow + NB);
   int* done = reinterpret_cast<int*>(slot + 2);
-  int* row2pos = done + rpc_max;
+  // row-position bookkeeping (rank 0): shared memory, or global scratch for large n
+  const bool pos_global = w.pos_scratch != nullptr;
+  int* row2pos = pos_global ? w.pos_scratch + size_t(b) * 2 * n : done + rpc_max;
   int* pos2row = row2pos + n;
-  int* scratch = pos2row + n;  // [0] winner row, [2] move count
+  int* scratch = pos_global ? done + rpc_max : pos2row + n;  // [0] winner row, [2] move count
   __shared__ T red_v[kPanelThreads / 32];
   __shared__ int red_r[kPanelThreads / 32];
   __shared__ T win_v;
@@ -166,7 +183,7 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
   }
   cluster.sync();
   // write back in pivoted order; rank 0 publishes the row moves of this panel
-  const int* r2p0 = cluster.map_shared_rank(row2pos, 0);
+  const int* r2p0 = pos_global ? row2pos : cluster.map_shared_rank(row2pos, 0);
   for (int idx = tid; idx < nloc * kb; idx += nthr) {
     const int r = idx % nloc, c = idx / nloc;
     const int dst = k + r2p0[row_lo + r];
@@ -616,44 +633,50 @@ void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// First panel configuration of width nb that fits the shared-memory budget:
+// smallest cluster with the bookkeeping in shared memory, else with it in
+// global scratch.
+static bool fit_panel(int elem, int nb, int n, int& cluster, int& rpc, int& smem, int& pos_global) {
+  const size_t budget = 200 * 1024;
+  for (int g = 0; g < 2; ++g)
+    for (int cl = 1; cl <= 16; cl *= 2) {
+      const int r = (n + cl - 1) / cl;
+      const size_t bsz = panel_smem_any(elem, nb, r, n, g == 1);
+      if (bsz <= budget) {
+        cluster = cl;
+        rpc = r;
+        smem = int(bsz);
+        pos_global = g;
+        return true;
+      }
+    }
+  return false;
+}
+
 template <typename T>
 PanelConfig choose_panel(int n) {
   PanelConfig pc;
-  const size_t budget = 200 * 1024;
-  for (int nb : {(sizeof(T) == 4 && n >= 512) ? 64 : 32, 32}) {
-    for (int cl = 1; cl <= 16; cl *= 2) {
-      const int rpc = (n + cl - 1) / cl;
-      const size_t b = nb == 64 ? panel_smem_bytes<T, 64>(rpc, n) : panel_smem_bytes<T, 32>(rpc, n);
-      if (b <= budget) {
-        pc.nb = nb;
-        pc.cluster = cl;
-        pc.rpc_max = rpc;
-        pc.smem = int(b);
+  pc.cluster = 0;
+  if (sizeof(T) == 4 && n >= 512) {
+    // two-level: 64-column blocks of 32- or 16-column cluster panels
+    for (int iw : {32, 16})
+      if (fit_panel(8, iw, n, pc.inner_cluster, pc.inner_rpc, pc.inner_smem, pc.inner_pos_global)) {
+        pc.nb = 64;
+        pc.inner_nb = iw;
+        pc.cluster = pc.inner_cluster;
+        pc.pos_global = pc.inner_pos_global;
         return pc;
       }
-    }
+    return pc;
   }
-  pc.cluster = 0;  // too large for one cluster
-  return pc;
-}
-
-// Panel configuration for a fixed panel width (the 32-column inner panels).
-template <typename T>
-PanelConfig choose_panel_nb(int n, int nb) {
-  PanelConfig pc;
-  const size_t budget = 200 * 1024;
-  for (int cl = 1; cl <= 16; cl *= 2) {
-    const int rpc = (n + cl - 1) / cl;
-    const size_t b = nb == 64 ? panel_smem_bytes<T, 64>(rpc, n) : panel_smem_bytes<T, 32>(rpc, n);
-    if (b <= budget) {
+  const int elem = int(sizeof(cplx<T>));
+  const int widths[3] = {32, 16, sizeof(T) == 4 ? 16 : 8};
+  for (int nb : widths)
+    if (fit_panel(elem, nb, n, pc.cluster, pc.rpc_max, pc.smem, pc.pos_global)) {
       pc.nb = nb;
-      pc.cluster = cl;
-      pc.rpc_max = rpc;
-      pc.smem = int(b);
       return pc;
     }
-  }
-  pc.cluster = 0;
+  pc.cluster = 0;  // too large for one cluster
   return pc;
 }
 
@@ -701,37 +724,39 @@ static void launch_rhs_lower(const BatchLayout& lay, int batch, int k, int c_beg
   rhs_lower_kernel<T, NB, kSolve><<<grid, 256, 0, s>>>(lay, k, c_begin, c_end, M, w, skip);
 }
 
-// Composes the row moves of the two inner panels of an outer block into one
-// gather list: after both, row d holds the original row f(d), f = src0(src1(d)).
-// One CTA of 128 threads per matrix, both lists in shared memory.
-__global__ void __launch_bounds__(128) compose_moves_kernel(int n, int k, LuWork w_out, LuWork w_in, int two) {
+// Composes the row moves of the P inner panels of an outer block into one
+// gather list: after all of them, row d holds the original row
+// f(d) = src_0(src_1(...src_{P-1}(d))).  One CTA of 128 threads per matrix,
+// the lists in shared memory (P * 2 * IW <= 128 entries).
+__global__ void __launch_bounds__(128) compose_moves_kernel(int k, int iw, int P, LuWork w_out, LuWork w_in) {
   const int b = blockIdx.x;
-  __shared__ int2 m0[64], m1[64];
+  __shared__ int2 mv[128];
+  __shared__ int cntl[4];
   __shared__ int cnt;
-  const int p0 = k / 32;
-  const int n0 = w_in.nperm[size_t(b) * w_in.npanels + p0];
-  const int n1 = two ? w_in.nperm[size_t(b) * w_in.npanels + p0 + 1] : 0;
+  const int per = 2 * iw, p0 = k / iw;
   const int t = threadIdx.x;
-  if (t < n0) m0[t] = w_in.perm[(size_t(b) * w_in.npanels + p0) * 64 + t];
-  if (t < n1) m1[t] = w_in.perm[(size_t(b) * w_in.npanels + p0 + 1) * 64 + t];
+  if (t < P) cntl[t] = w_in.nperm[size_t(b) * w_in.npanels + p0 + t];
   if (t == 0) cnt = 0;
   __syncthreads();
+  {
+    const int p = t / per, e = t % per;
+    if (p < P && e < cntl[p]) mv[t] = w_in.perm[(size_t(b) * w_in.npanels + p0 + p) * per + e];
+  }
+  __syncthreads();
   int2* out = w_out.perm + (size_t(b) * w_out.npanels + k / 64) * 128;
-  // thread t < 64 handles the first list's destinations, t >= 64 the second's
+  const int p = t / per, e = t % per;
   int d = -1;
-  if (t < 64) {
-    if (t < n0) d = m0[t].x;
-  } else if (t - 64 < n1) {
-    d = m1[t - 64].x;
-    for (int q = 0; q < n0; ++q)
-      if (m0[q].x == d) d = -1;  // already handled with the first list
+  if (p < P && e < cntl[p]) {
+    d = mv[t].x;
+    for (int q = 0; q < p && d >= 0; ++q)  // a row moved by an earlier panel is handled there
+      for (int x = 0; x < cntl[q]; ++x)
+        if (mv[q * per + x].x == d) { d = -1; break; }
   }
   if (d >= 0) {
     int f = d;
-    for (int q = 0; q < n1; ++q)
-      if (m1[q].x == f) { f = m1[q].y; break; }
-    for (int q = 0; q < n0; ++q)
-      if (m0[q].x == f) { f = m0[q].y; break; }
+    for (int q = P - 1; q >= 0; --q)
+      for (int x = 0; x < cntl[q]; ++x)
+        if (mv[q * per + x].x == f) { f = mv[q * per + x].y; break; }
     if (f != d) {
       const int slot = atomicAdd(&cnt, 1);
       if (slot < 128) out[slot] = make_int2(d, f);
@@ -762,68 +787,95 @@ static void launch_gemm(const BatchLayout& lay, int batch, int r_begin, int r_en
 template <typename T>
 static void gemm_any(int nb, const BatchLayout& lay, int batch, int r_begin, int r_end, int c_begin, int c_end, int ka,
                      int kb, cplx<T>* M, const int* skip, cudaStream_t s) {
-  // Skinny right-hand sides (m columns) use a narrow tile.
+  // Skinny right-hand sides (m columns) use a narrow tile; KMAX = panel width.
   const bool skinny = (c_end - c_begin) <= 32;
+#define RFX_GEMM(TM, TN, K) launch_gemm<T, TM, TN, K>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s)
   if (sizeof(T) == 8) {
-    if (skinny) {
-      if (nb == 64) launch_gemm<T, 4, 2, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
-      else launch_gemm<T, 4, 2, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
-    } else {
-      if (nb == 64) launch_gemm<T, 4, 4, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
-      else launch_gemm<T, 4, 4, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+    switch (nb) {
+      case 64: skinny ? RFX_GEMM(4, 2, 64) : RFX_GEMM(4, 4, 64); break;
+      case 32: skinny ? RFX_GEMM(4, 2, 32) : RFX_GEMM(4, 4, 32); break;
+      case 16: skinny ? RFX_GEMM(4, 2, 16) : RFX_GEMM(4, 4, 16); break;
+      default: skinny ? RFX_GEMM(4, 2, 8) : RFX_GEMM(4, 4, 8); break;
     }
   } else {
-    if (skinny) {
-      if (nb == 64) launch_gemm<T, 8, 2, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
-      else launch_gemm<T, 8, 2, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
-    } else {
-      if (nb == 64) launch_gemm<T, 8, 4, 64>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
-      else launch_gemm<T, 8, 4, 32>(lay, batch, r_begin, r_end, c_begin, c_end, ka, kb, M, skip, s);
+    switch (nb) {
+      case 64: skinny ? RFX_GEMM(8, 2, 64) : RFX_GEMM(8, 4, 64); break;
+      case 32: skinny ? RFX_GEMM(8, 2, 32) : RFX_GEMM(8, 4, 32); break;
+      default: skinny ? RFX_GEMM(8, 2, 16) : RFX_GEMM(8, 4, 16); break;
     }
+  }
+#undef RFX_GEMM
+}
+
+template <typename T, bool kSolve = true>
+static void rhs_lower_any(int nb, const BatchLayout& lay, int batch, int k, int c_begin, int c_end, cplx<T>* M,
+                          const LuWork& w, const int* skip, cudaStream_t s) {
+  switch (nb) {
+    case 64: launch_rhs_lower<T, 64, kSolve>(lay, batch, k, c_begin, c_end, M, w, skip, s); break;
+    case 32: launch_rhs_lower<T, 32, kSolve>(lay, batch, k, c_begin, c_end, M, w, skip, s); break;
+    case 16: launch_rhs_lower<T, 16, kSolve>(lay, batch, k, c_begin, c_end, M, w, skip, s); break;
+    default:
+      if constexpr (sizeof(T) == 8) launch_rhs_lower<T, 8, kSolve>(lay, batch, k, c_begin, c_end, M, w, skip, s);
+      break;
   }
 }
 
-// FP32 tensor-core elimination with two-level blocking: each 64-column outer
-// block is factored as two 32-column cluster panels (half the on-chip panel
-// footprint, so twice the matrices resident per wave); the second inner
-// panel's row moves are applied to the first panel's L columns, the two move
-// lists are composed, and the trailing matrix gets one K = 64 tensor-core
-// update per outer block.
-static cudaError_t lu_eliminate_two_level(const BatchLayout& lay, int batch, float2* M, const LuWork& w,
-                                          cudaStream_t s) {
-  const int n = lay.n, col_end = lay.n + lay.m;
-  static int cached_n = -1;
-  static PanelConfig pin;
-  if (cached_n != n) {
-    pin = choose_panel_nb<float>(n, 32);
-    cached_n = n;
+// Cluster panel of width nb: FP32 uses 32 / 16, FP64 32 / 16 / 8.
+template <typename T>
+static cudaError_t panel_any(const PanelConfig& pc, int nb, const BatchLayout& lay, int batch, int k, cplx<T>* M,
+                             const LuWork& w, cudaStream_t s) {
+  if (nb == 32) return launch_panel<T, 32>(pc, lay, batch, k, M, w, s);
+  if (nb == 16) return launch_panel<T, 16>(pc, lay, batch, k, M, w, s);
+  if constexpr (sizeof(T) == 8) {
+    if (nb == 8) return launch_panel<T, 8>(pc, lay, batch, k, M, w, s);
   }
-  if (pin.cluster <= 0 || w.nb != 64) return cudaErrorInvalidValue;
+  return cudaErrorInvalidValue;
+}
+
+// FP32 elimination with two-level blocking: each 64-column outer block is
+// factored as P = 64 / IW cluster panels of width IW (32, or 16 for large n),
+// which keeps the on-chip panel footprint small enough for many matrices per
+// wave; inside the block each panel updates the block's remaining columns
+// (rank-IW), and its row moves are applied to the earlier panels' L columns,
+// so that the block's L is in one row order.  The panels' moves are composed,
+// and the trailing matrix (right-hand sides included) gets one K = 64 update:
+// on the tensor cores when operand images are available, else on CUDA cores.
+static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayout& lay, int batch, float2* M,
+                                          const LuWork& w, cudaStream_t s) {
+  const int n = lay.n, col_end = lay.n + lay.m, iw = pc.inner_nb;
+  if (pc.nb != 64 || w.nb != 64 || (iw != 32 && iw != 16) || !w.perm_in) return cudaErrorInvalidValue;
+  PanelConfig pin;
+  pin.nb = iw;
+  pin.cluster = pc.inner_cluster;
+  pin.rpc_max = pc.inner_rpc;
+  pin.smem = pc.inner_smem;
+  pin.pos_global = pc.inner_pos_global;
   LuWork wi = w;
   wi.perm = w.perm_in;
   wi.nperm = w.nperm_in;
-  wi.nb = 32;
-  wi.npanels = panel_count(n, 32);
+  wi.nb = iw;
+  wi.npanels = panel_count(n, iw);
+  if (!pin.pos_global) wi.pos_scratch = nullptr;
   for (int k = 0; k < n; k += 64) {
     const int kb = min(64, n - k);
-    const int kb0 = min(32, kb);
-    const bool two = kb > 32;
-    cudaError_t err = launch_panel<float, 32>(pin, lay, batch, k, M, wi, s);
-    if (err != cudaSuccess) return err;
-    if (two) {
-      // second inner panel's columns: moves + L11 of the first, then its rank-32 update
-      launch_rhs_lower<float, 32>(lay, batch, k, k + kb0, k + kb, M, wi, nullptr, s);
-      gemm_any<float>(32, lay, batch, k + kb0, n, k + kb0, k + kb, k, kb0, M, nullptr, s);
-      err = launch_panel<float, 32>(pin, lay, batch, k + kb0, M, wi, s);
+    int P = 0;
+    for (int ki = k; ki < k + kb; ki += iw, ++P) {
+      const int kbi = min(iw, k + kb - ki);
+      cudaError_t err = panel_any<float>(pin, iw, lay, batch, ki, M, wi, s);
       if (err != cudaSuccess) return err;
-      // the second panel's row moves on the first panel's L columns
-      launch_rhs_lower<float, 32, false>(lay, batch, k + kb0, k, k + kb0, M, wi, nullptr, s);
+      if (ki > k) rhs_lower_any<float, false>(iw, lay, batch, ki, k, ki, M, wi, nullptr, s);  // moves on earlier L
+      if (ki + kbi < k + kb) {
+        // the block's remaining columns: this panel's moves and L11, then its rank-IW update
+        rhs_lower_any<float>(iw, lay, batch, ki, ki + kbi, k + kb, M, wi, nullptr, s);
+        gemm_any<float>(iw, lay, batch, ki + kbi, n, ki + kbi, k + kb, ki, kbi, M, nullptr, s);
+      }
     }
     count_launch();
-    compose_moves_kernel<<<batch, 128, 0, s>>>(n, k, w, wi, two ? 1 : 0);
+    compose_moves_kernel<<<batch, 128, 0, s>>>(k, iw, P, w, wi);
     launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
-    tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
-    err = cudaGetLastError();
+    if (w.tc_images) tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
+    else gemm_any<float>(64, lay, batch, k + kb, n, k + kb, col_end, k, kb, M, nullptr, s);
+    cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
   return cudaSuccess;
@@ -835,20 +887,15 @@ cudaError_t lu_eliminate(const PanelConfig& pc, const BatchLayout& lay, int batc
   const int n = lay.n, col_end = lay.n + lay.m;
   if (pc.cluster <= 0 || w.nb != pc.nb) return cudaErrorInvalidValue;
   if constexpr (sizeof(T) == 4) {
-    if (w.tc_images && w.perm_in && pc.nb == 64) return lu_eliminate_two_level(lay, batch, M, w, s);
+    if (pc.inner_nb) return lu_eliminate_two_level(pc, lay, batch, M, w, s);
   }
+  LuWork wl = w;
+  if (!pc.pos_global) wl.pos_scratch = nullptr;
   for (int k = 0; k < n; k += pc.nb) {
     const int kb = min(pc.nb, n - k);
-    cudaError_t err;
-    if (pc.nb == 64) {
-      err = launch_panel<T, 64>(pc, lay, batch, k, M, w, s);
-      if (err != cudaSuccess) return err;
-      launch_rhs_lower<T, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
-    } else {
-      err = launch_panel<T, 32>(pc, lay, batch, k, M, w, s);
-      if (err != cudaSuccess) return err;
-      launch_rhs_lower<T, 32>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
-    }
+    cudaError_t err = panel_any<T>(pc, pc.nb, lay, batch, k, M, wl, s);
+    if (err != cudaSuccess) return err;
+    rhs_lower_any<T>(pc.nb, lay, batch, k, k + kb, col_end, M, wl, nullptr, s);
     if constexpr (sizeof(T) == 4) {
       if (w.tc_images) {
         tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
@@ -870,8 +917,7 @@ void lu_forward_rhs(const PanelConfig& pc, const BatchLayout& lay, int batch, cp
   const int n = lay.n, col_end = lay.n + lay.m;
   for (int k = 0; k < n; k += pc.nb) {
     const int kb = min(pc.nb, n - k);
-    if (pc.nb == 64) launch_rhs_lower<T, 64>(lay, batch, k, n, col_end, M, w, skip, s);
-    else launch_rhs_lower<T, 32>(lay, batch, k, n, col_end, M, w, skip, s);
+    rhs_lower_any<T>(pc.nb, lay, batch, k, n, col_end, M, w, skip, s);
     gemm_any<T>(pc.nb, lay, batch, k + kb, n, n, col_end, k, kb, M, skip, s);
   }
 }
@@ -885,8 +931,14 @@ void lu_backward_rhs(const PanelConfig& pc, const BatchLayout& lay, int batch, c
   for (int k = last; k >= 0; k -= pc.nb) {
     const int kb = min(pc.nb, n - k);
     count_launch();
-    if (pc.nb == 64) rhs_upper_kernel<T, 64><<<grid, 256, 0, s>>>(lay, k, M, skip);
-    else rhs_upper_kernel<T, 32><<<grid, 256, 0, s>>>(lay, k, M, skip);
+    switch (pc.nb) {
+      case 64: rhs_upper_kernel<T, 64><<<grid, 256, 0, s>>>(lay, k, M, skip); break;
+      case 32: rhs_upper_kernel<T, 32><<<grid, 256, 0, s>>>(lay, k, M, skip); break;
+      case 16: rhs_upper_kernel<T, 16><<<grid, 256, 0, s>>>(lay, k, M, skip); break;
+      default:
+        if constexpr (sizeof(T) == 8) rhs_upper_kernel<T, 8><<<grid, 256, 0, s>>>(lay, k, M, skip);
+        break;
+    }
     gemm_any<T>(pc.nb, lay, batch, 0, k, n, col_end, k, kb, M, skip, s);
   }
 }

@@ -10,10 +10,13 @@ namespace rfx {
 
 // Panel geometry picked on the host for a given n / precision.
 struct PanelConfig {
-  int nb = 32;       // panel width
+  int nb = 32;       // panel width (the outer block width of a two-level elimination)
   int cluster = 1;   // CTAs per matrix (thread-block cluster)
   int rpc_max = 0;   // rows per CTA at k = 0
   int smem = 0;      // dynamic smem bytes per CTA
+  int pos_global = 0;  // row-position bookkeeping in global scratch (large n) instead of shared memory
+  // two-level elimination (FP32, nb = 64): the cluster panels are inner_nb wide
+  int inner_nb = 0, inner_cluster = 0, inner_rpc = 0, inner_smem = 0, inner_pos_global = 0;
 };
 
 template <typename T> PanelConfig choose_panel(int n);
@@ -36,11 +39,14 @@ struct LuWork {
   int* nperm = nullptr;   // [batch][npanels]
   int* status = nullptr;  // [batch] DevStatus (max-reduced)
   int* info = nullptr;    // [batch] first zero pivot (1-based, 0 = none)
-  // Two-level FP32 elimination (tensor-core path): row moves of the 32-column
-  // inner panels, [batch][ceil(n/32)][64] and [batch][ceil(n/32)]; the outer
-  // 64-column blocks keep their composed moves in perm / nperm.
+  // Two-level FP32 elimination: row moves of the inner panels (width IW = 32 or
+  // 16), [batch][ceil(n/IW)][2 IW] and [batch][ceil(n/IW)]; the outer 64-column
+  // blocks keep their composed moves in perm / nperm.
   int2* perm_in = nullptr;
   int* nperm_in = nullptr;
+  // row-position bookkeeping of the panel kernel when it does not fit in
+  // shared memory: [batch][2n] ints (row2pos, pos2row)
+  int* pos_scratch = nullptr;
   int npanels = 0;
   int nb = 0;
 };

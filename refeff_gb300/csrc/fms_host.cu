@@ -318,8 +318,9 @@ struct Workspace {
   DevBuf<uint8_t> tc_images;         // operand images of the tensor-core update
   DevBuf<int> tc_err;                // set by a tensor-core wait that timed out
   DevBuf<int2> perm;
-  DevBuf<int2> perm_in;              // row moves of the 32-column inner panels (two-level FP32 LU)
+  DevBuf<int2> perm_in;              // row moves of the inner panels (two-level FP32 LU)
   DevBuf<int> nperm_in;
+  DevBuf<int> pos_scratch;           // panel row-position bookkeeping for large n
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
   std::map<int, cudaGraphExec_t> graphs;  // key: form
@@ -609,6 +610,11 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
     RF_CUDA(ctx, ws.iters.alloc(size_t(B)));
     RF_CUDA(ctx, ws.relres.alloc(size_t(B)));
   }
+  if (ws.pc64.pos_global || (ws.fp32 && ws.pc32.pos_global)) RF_CUDA(ctx, ws.pos_scratch.alloc(size_t(B) * 2 * n));
+  if (ws.fp32 && ws.pc32.inner_nb) {
+    RF_CUDA(ctx, ws.perm_in.alloc(size_t(B) * panel_count(n, ws.pc32.inner_nb) * 2 * ws.pc32.inner_nb));
+    RF_CUDA(ctx, ws.nperm_in.alloc(size_t(B) * panel_count(n, ws.pc32.inner_nb)));
+  }
   RF_CUDA(ctx, ws.ipiv.alloc(size_t(B) * n));
   RF_CUDA(ctx, ws.perm.alloc(size_t(B) * npanels * 2 * nb_max));
   RF_CUDA(ctx, ws.nperm.alloc(size_t(B) * npanels));
@@ -616,8 +622,6 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
   RF_CUDA(ctx, ws.info.alloc(size_t(B)));
   ws.use_tc = ws.fp32 && ctx->use_tensor_cores != 0;
   if (ws.use_tc) {
-    RF_CUDA(ctx, ws.perm_in.alloc(size_t(B) * panel_count(n, 32) * 64));
-    RF_CUDA(ctx, ws.nperm_in.alloc(size_t(B) * panel_count(n, 32)));
     RF_CUDA(ctx, ws.tc_images.alloc(tc_image_bytes(n, m, B)));
     RF_CUDA(ctx, ws.tc_err.alloc(1));
     RF_CUDA(ctx, cudaMemset(ws.tc_err.p, 0, sizeof(int)));
@@ -634,11 +638,14 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
   w.info = ws.info.p;
   w.nb = pc.nb;
   w.npanels = panel_count(ws.lay.n, pc.nb);
+  w.pos_scratch = ws.pos_scratch.p;
+  if (&pc == &ws.pc32) {
+    w.perm_in = ws.perm_in.p;
+    w.nperm_in = ws.nperm_in.p;
+  }
   if (&pc == &ws.pc32 && ws.use_tc) {
     w.tc_images = ws.tc_images.p;
     w.tc_err = ws.tc_err.p;
-    w.perm_in = ws.perm_in.p;
-    w.nperm_in = ws.nperm_in.p;
   }
   return w;
 }

@@ -114,7 +114,7 @@ extern "C" int refeff_complex_lu_solve_device_noalloc(int n, int m, int batch, c
   lay.lda = (n + 31) / 32 * 32;
   lay.stride = size_t(lay.lda) * size_t(n + m);
   const PanelConfig pc = choose_panel<double>(n);
-  if (pc.cluster <= 0) return REFEFF_FMS_ERR_UNSUPPORTED;
+  if (pc.cluster <= 0 || pc.pos_global) return REFEFF_FMS_ERR_UNSUPPORTED;
   const int npanels = panel_count(n, pc.nb);
   // scratch carve-up, each piece 256-byte aligned
   const size_t off_ipiv = align256(size_t(batch) * lay.stride * sizeof(double2));

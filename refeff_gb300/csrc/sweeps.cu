@@ -201,7 +201,8 @@ template <int NB, int CG>
 bool launch_sweep_cg(bool forward, const BatchLayout& lay, int batch, float2* M, const LuWork* w, const int* skip,
                      cudaStream_t s) {
   const size_t smem = SweepSmem<NB, CG>::bytes(lay.n);
-  if (smem > kSwSmemBudget) return false;
+  // each column group streams the whole triangle: decline narrow groups for many columns
+  if (smem > kSwSmemBudget || CG < (lay.m < 4 ? lay.m : 4)) return false;
   static size_t set_f = 0, set_b = 0;  // raised once to the largest request (before any stream capture)
   size_t& set = forward ? set_f : set_b;
   if (smem > set) {
