@@ -209,6 +209,17 @@ int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies,
                                           const void* d_phase_shifts, refeff_fms_form form, void* d_gg_out,
                                           int32_t* d_status, void* stream);
 
+/* Many clusters in one call (the batched form of fms_real_space_spectrum over
+ * several plans, crates/refeff-core/src/fms/driver.rs:231-239): plans[i] with
+ * points[i] writes scattering_out[i] (and status_out[i] when status_out is not
+ * NULL), all plans of the same context.  Every plan's device work is put in
+ * flight on a small pool of streams before any completes, so small clusters
+ * overlap; the return code is the first failure, the report sums over plans. */
+int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int n_plans, refeff_fms_plan* const* plans,
+                                         const refeff_fms_energy_points* points, refeff_fms_form form,
+                                         refeff_complex128* const* scattering_out, int32_t* const* status_out,
+                                         refeff_fms_report* report);
+
 /* Per-energy outcome of the last refeff_fms_real_space_spectrum call with
  * REFEFF_FMS_FORM_FP32_REFINED: relative residual max|b - A x| / max|b| of
  * the last residual evaluated (the one that produced the final correction),

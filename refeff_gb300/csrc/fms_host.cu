@@ -48,6 +48,7 @@ struct refeff_fms_context {
   int sm_count = 0;
   int use_tensor_cores = 1;  // FP32 trailing updates on tcgen05 (REFEFF_FMS_OPT_TENSOR_CORES)
   int dense_refinement = 10; // corrections of the dense FP32 solve (REFEFF_FMS_OPT_DENSE_REFINEMENT)
+  std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
 };
 
 void rfx::set_last_error(refeff_fms_context* ctx, const std::string& msg) {
@@ -163,6 +164,10 @@ extern "C" void refeff_fms_context_destroy(refeff_fms_context* ctx) {
   if (ctx->stream) {
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+  }
+  for (cudaStream_t q : ctx->pool) {
+    cudaStreamSynchronize(q);
+    cudaStreamDestroy(q);
   }
   delete ctx;
 }
@@ -821,7 +826,7 @@ int pick_batch(refeff_fms_plan& p, int E, bool fp32) {
 
 // Solve E energies whose inputs are already on the device (d_k: E*nsp, d_x:
 // E*xph); writes d_gg (E*m*m) and d_status (E).  Uses graph replay per batch.
-int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
+int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
                           double2* d_gg, int* d_status, cudaStream_t s) {
   refeff_fms_context* ctx = p.ctx;
   const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
@@ -887,6 +892,18 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
                                    cudaMemcpyDeviceToDevice, s));
     }
   }
+  return REFEFF_FMS_OK;
+}
+
+// Completion of solve_device_energies_enqueue: waits for the stream, then
+// re-solves with the FP64 LU the energies whose refinement missed.
+int solve_device_energies_finish(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x,
+                                 refeff_fms_form form, double2* d_gg, int* d_status, cudaStream_t s) {
+  refeff_fms_context* ctx = p.ctx;
+  Workspace& ws = p.ws;
+  const bool refined = form == REFEFF_FMS_FORM_FP32_REFINED && p.minv == 0;
+  const int B = ws.batch;
+  const size_t xph = p.xph_per_energy();
   if (!refined) return REFEFF_FMS_OK;
   // Energies whose refinement missed the tolerance are solved again with the
   // plain FP64 LU (same inputs), so every returned block meets the FP64 bar.
@@ -929,6 +946,13 @@ int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const d
   return REFEFF_FMS_OK;
 }
 
+int solve_device_energies(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
+                          double2* d_gg, int* d_status, cudaStream_t s) {
+  const int rc = solve_device_energies_enqueue(p, E, d_k, d_x, form, d_gg, d_status, s);
+  if (rc) return rc;
+  return solve_device_energies_finish(p, E, d_k, d_x, form, d_gg, d_status, s);
+}
+
 }  // namespace
 
 extern "C" int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies, const void* d_wave_numbers,
@@ -946,30 +970,40 @@ extern "C" int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int 
                                d_status, s);
 }
 
-extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
-                                              refeff_fms_form form, refeff_complex128* scattering_out,
-                                              int32_t* status_out, refeff_fms_report* report) {
-  if (!plan || !points || !scattering_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
-  refeff_fms_context* ctx = plan->ctx;
-  ctx->last_error.clear();
-  const auto t0 = std::chrono::steady_clock::now();
+namespace {
+
+// Host-buffer spectrum in two halves, so that several plans can have their
+// device work in flight at once: begin validates, uploads and enqueues on
+// stream s; end waits, runs the FP64 fallback, downloads and scatters.
+int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
+                   refeff_complex128* scattering_out, cudaStream_t s) {
+  refeff_fms_context* ctx = p.ctx;
+  if (!points || !scattering_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   const int E = points->n_energies;
   if (E < 0 || (E > 0 && (!points->wave_numbers || !points->phase_shifts)))
     return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "invalid energy points");
   if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
     return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
-  refeff_fms_plan& p = *plan;
   const size_t C = size_t(p.C), tab = C * C * size_t(p.npot);
   std::memset(scattering_out, 0, size_t(E) * tab * sizeof(refeff_complex128));
   if (E == 0) return REFEFF_FMS_OK;
   RF_CUDA(ctx, cudaSetDevice(ctx->device));
-  cudaStream_t s = ctx->stream;
   const size_t xph = p.xph_per_energy();
   RF_CUDA(ctx, p.d_k_all.upload(reinterpret_cast<const double2*>(points->wave_numbers), size_t(E) * p.nsp, s));
   RF_CUDA(ctx, p.d_x_all.upload(reinterpret_cast<const double2*>(points->phase_shifts), size_t(E) * xph, s));
   RF_CUDA(ctx, p.d_gg_all.alloc(size_t(E) * p.m * p.m));
   RF_CUDA(ctx, p.d_status_all.alloc(size_t(E)));
-  int rc = solve_device_energies(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
+  return solve_device_energies_enqueue(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
+}
+
+int spectrum_end(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
+                 refeff_complex128* scattering_out, int32_t* status_out, int* failed_out, cudaStream_t s) {
+  refeff_fms_context* ctx = p.ctx;
+  const int E = points->n_energies;
+  *failed_out = 0;
+  if (E == 0) return REFEFF_FMS_OK;
+  const size_t C = size_t(p.C), tab = C * C * size_t(p.npot);
+  int rc = solve_device_energies_finish(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
   if (rc) return rc;
   std::vector<double2> gg(size_t(E) * p.m * p.m);
   std::vector<int> st(static_cast<size_t>(E));
@@ -985,11 +1019,11 @@ extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refef
                                  s));
   }
   RF_CUDA(ctx, cudaStreamSynchronize(s));
-  int failed = 0;
+  int failed = 0, first_bad = -1;
   for (int e = 0; e < E; ++e) {
     const int code = map_status(st[size_t(e)]);
     if (status_out) status_out[e] = code;
-    if (code != REFEFF_FMS_OK) ++failed;
+    if (code != REFEFF_FMS_OK && failed++ == 0) first_bad = e;
     refeff_complex128* outp = scattering_out + size_t(e) * tab;
     for (int c = 0; c < p.m; ++c)
       for (int r = 0; r < p.m; ++r) {
@@ -997,23 +1031,85 @@ extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refef
         outp[size_t(r) + C * (size_t(c) + C * size_t(p.abs_pot))] = {v.x, v.y};
       }
   }
-  if (report) {
-    report->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    report->energies_failed = failed;
-    report->refinement_iterations = 0;
-    report->residual_max = 0.0;
-    for (int e = 0; e < int(p.last_iters.size()); ++e) {
-      report->refinement_iterations = std::max(report->refinement_iterations, p.last_iters[size_t(e)]);
-      report->residual_max = std::max(report->residual_max, p.last_relres[size_t(e)]);
-    }
-    report->fp64_fallbacks = fp32 ? p.last_fallbacks : 0;
-  }
-  if (failed) {
-    for (int e = 0; e < E; ++e)
-      if (map_status(st[size_t(e)]) != REFEFF_FMS_OK)
-        return fail(ctx, map_status(st[size_t(e)]), "failed to solve FMS energy section " + std::to_string(e + 1));
-  }
+  *failed_out = failed;
+  if (failed)
+    return fail(ctx, map_status(st[size_t(first_bad)]),
+                "failed to solve FMS energy section " + std::to_string(first_bad + 1));
   return REFEFF_FMS_OK;
+}
+
+void fill_report(refeff_fms_report* report, const std::vector<refeff_fms_plan*>& plans, refeff_fms_form form,
+                 int failed, std::chrono::steady_clock::time_point t0) {
+  if (!report) return;
+  report->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  report->energies_failed = failed;
+  report->refinement_iterations = 0;
+  report->residual_max = 0.0;
+  report->fp64_fallbacks = 0;
+  for (const refeff_fms_plan* p : plans) {
+    for (size_t e = 0; e < p->last_iters.size(); ++e) {
+      report->refinement_iterations = std::max(report->refinement_iterations, p->last_iters[e]);
+      report->residual_max = std::max(report->residual_max, p->last_relres[e]);
+    }
+    if (form == REFEFF_FMS_FORM_FP32_REFINED && p->minv == 0) report->fp64_fallbacks += p->last_fallbacks;
+  }
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                              refeff_fms_form form, refeff_complex128* scattering_out,
+                                              int32_t* status_out, refeff_fms_report* report) {
+  if (!plan || !points || !scattering_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  refeff_fms_context* ctx = plan->ctx;
+  ctx->last_error.clear();
+  const auto t0 = std::chrono::steady_clock::now();
+  int rc = spectrum_begin(*plan, points, form, scattering_out, ctx->stream);
+  if (rc) return rc;
+  int failed = 0;
+  rc = spectrum_end(*plan, points, form, scattering_out, status_out, &failed, ctx->stream);
+  fill_report(report, {plan}, form, failed, t0);
+  return rc;
+}
+
+extern "C" int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int n_plans, refeff_fms_plan* const* plans,
+                                                    const refeff_fms_energy_points* points, refeff_fms_form form,
+                                                    refeff_complex128* const* scattering_out,
+                                                    int32_t* const* status_out, refeff_fms_report* report) {
+  if (!ctx || n_plans < 0 || (n_plans > 0 && (!plans || !points || !scattering_out)))
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  ctx->last_error.clear();
+  for (int i = 0; i < n_plans; ++i)
+    if (!plans[i] || plans[i]->ctx != ctx || !scattering_out[i])
+      return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "plan " + std::to_string(i) + " is null or of another context");
+  for (int i = 0; i < n_plans; ++i)
+    for (int j = 0; j < i; ++j)
+      if (plans[i] == plans[j]) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "a plan appears twice");
+  const auto t0 = std::chrono::steady_clock::now();
+  RF_CUDA(ctx, cudaSetDevice(ctx->device));
+  constexpr int kStreams = 4;
+  while (int(ctx->pool.size()) < kStreams) {
+    cudaStream_t q = nullptr;
+    RF_CUDA(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    ctx->pool.push_back(q);
+  }
+  // every plan's work in flight first (round-robin over the streams), then completion
+  int rc = REFEFF_FMS_OK;
+  int begun = 0;
+  for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun)
+    rc = spectrum_begin(*plans[begun], &points[begun], form, scattering_out[begun], ctx->pool[size_t(begun % kStreams)]);
+  int failed = 0, first_rc = rc;
+  for (int i = 0; i < begun; ++i) {
+    int f = 0;
+    const int r = rc == REFEFF_FMS_OK ? spectrum_end(*plans[i], &points[i], form, scattering_out[i],
+                                                     status_out ? status_out[i] : nullptr, &f,
+                                                     ctx->pool[size_t(i % kStreams)])
+                                      : (cudaStreamSynchronize(ctx->pool[size_t(i % kStreams)]), REFEFF_FMS_OK);
+    failed += f;
+    if (first_rc == REFEFF_FMS_OK) first_rc = r;
+  }
+  fill_report(report, std::vector<refeff_fms_plan*>(plans, plans + begun), form, failed, t0);
+  return first_rc;
 }
 
 extern "C" int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int n_energies, double* rel_residual,

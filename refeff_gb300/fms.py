@@ -118,6 +118,7 @@ def load(build_if_missing: bool = True):
         "refeff_fms_run_mkgtr_dir": ([_p, C.c_char_p, _p], _i),
         "refeff_fms_write_fms_bin": ([C.c_char_p, C.c_double, _i, _i, _i, _i, _i, _i, _p], _i),
         "refeff_fms_write_gtr_dat": ([C.c_char_p, _i, _p, _p], _i),
+        "refeff_fms_real_space_spectrum_multi": ([_p, _i, _p, _p, _i, _p, _p, _p], _i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -481,3 +482,39 @@ def write_gtr_dat(path, energy, trace) -> None:
     rc = lib.refeff_fms_write_gtr_dat(str(path).encode(), len(e), _ptr(e), _ptr(t))
     if rc:
         raise FmsError(rc, f"cannot write {path}")
+
+
+def fms_real_space_spectrum_multi(plans, wave_numbers, phase_shifts, form=FORM_FP64_LU, raise_on_error=True):
+    """Many clusters in one call (refeff_fms_real_space_spectrum_multi): plans[i] with wave_numbers[i]
+    (E_i, nsp) and phase_shifts[i] (E_i, nsp, 2L+1, npot); returns lists of scattering tables and statuses."""
+    if not plans:
+        return [], []
+    ctx = plans[0].ctx
+    keep, outs, sts = [], [], []
+    pts = (_EnergyPoints * len(plans))()
+    for i, plan in enumerate(plans):
+        nsp, L, npot = plan.inputs["nsp"], plan.inputs["L"], plan.inputs["npot"]
+        k = np.ascontiguousarray(np.asarray(wave_numbers[i], dtype=np.complex128).reshape(-1, nsp))
+        E = k.shape[0]
+        ph = np.asarray(phase_shifts[i], dtype=np.complex128).reshape(E, nsp, 2 * L + 1, npot)
+        xp = np.ascontiguousarray(np.stack([ph[e].reshape(-1, order="F") for e in range(E)])) if E else \
+            np.zeros((0,), np.complex128)
+        Cc = plan.shape.channel_count
+        outs.append(np.zeros(E * Cc * Cc * npot, dtype=np.complex128))
+        sts.append(np.zeros(E, dtype=np.int32))
+        keep += [k, xp]
+        pts[i] = _EnergyPoints(E, _ptr(k), _ptr(xp))
+    hs = (_p * len(plans))(*[p.handle for p in plans])
+    op = (_p * len(plans))(*[_ptr(o) for o in outs])
+    sp = (_p * len(plans))(*[_ptr(x) for x in sts])
+    rep = _Report()
+    rc = ctx._lib.refeff_fms_real_space_spectrum_multi(ctx.handle, len(plans), hs, pts, int(form), op, sp, C.byref(rep))
+    if rc and (raise_on_error or rc not in (9, 10, 6, 8, 19)):
+        raise FmsError(rc, ctx.last_error())
+    tables = []
+    for plan, o, x in zip(plans, outs, sts):
+        Cc, npot, E = plan.shape.channel_count, plan.inputs["npot"], len(x)
+        t = o.reshape(E, Cc * Cc * npot)
+        tables.append(np.stack([t[e].reshape((Cc, Cc, npot), order="F") for e in range(E)]) if E else
+                      np.zeros((0, Cc, Cc, npot), np.complex128))
+    return tables, sts

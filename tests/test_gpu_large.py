@@ -56,3 +56,30 @@ def test_config4_n15000_refined_matches_fp64(ctx):
         blk = g64[e, :m, :m, 0]
         assert np.abs(blk).max() > 0
         assert rel_err(g32[e, :m, :m, 0], blk) < TOL_CHOSEN, e
+
+
+def test_config2_many_clusters_in_one_call(ctx):
+    """config 2: 32 seeded displaced fcc clusters (n from 9*43 to 16*141), 150 energies each; here every
+    cluster with 4 energies through one multi-cluster call, checked against one call per plan (same kernels,
+    so equal to rounding) and the smallest clusters against the FP64 oracle."""
+    from oracle import pyoracle as po
+    cases = wl.config2()
+    sel = np.array([0, 50, 100, 149])
+    plans = [fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph) for cl, _ in cases]
+    ks = [g.wave_numbers[sel] for _, g in cases]
+    phs = [g.phase_shifts[sel] for _, g in cases]
+    for form, tol in ((fms.FORM_FP64_LU, 1e-10), (fms.FORM_FP32_REFINED, 1e-6)):
+        tables, sts = fms.fms_real_space_spectrum_multi(plans, ks, phs, form)
+        assert all((s == 0).all() for s in sts)
+        for i in (0, 13, 31):
+            single, _ = fms.fms_real_space_spectrum(plans[i], ks[i], phs[i], form)
+            m = plans[i].shape.absorber_block
+            assert rel_err(tables[i][:, :m, :m, 0], single[:, :m, :m, 0]) < 1e-12
+        small = sorted(range(len(cases)), key=lambda i: plans[i].shape.n_states)[:2]
+        for i in small:
+            cl, _ = cases[i]
+            ref = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, ks[i], phs[i], mode=po.F64,
+                                  threads=po.threads_available())
+            m = plans[i].shape.absorber_block
+            for e in range(len(sel)):
+                assert rel_err(tables[i][e, :m, :m, 0], ref[e, :m, :m, 0]) < tol, (i, e)
