@@ -61,7 +61,9 @@ typedef enum {
   REFEFF_FMS_ERR_INVALID_TOLERANCE = 16,     /* FmsError::InvalidTolerance */
   REFEFF_FMS_ERR_INVALID_CLUSTER_RADIUS = 17, /* FmsError::InvalidClusterRadius */
   REFEFF_FMS_ERR_SCRATCH_LIMIT = 18,          /* request exceeds REFEFF_FMS_NOALLOC_SCRATCH_BYTES */
-  REFEFF_FMS_ERR_ITERATIVE_BREAKDOWN = 19     /* FmsError::IterativeSolverBreakdown (minv != 0) */
+  REFEFF_FMS_ERR_ITERATIVE_BREAKDOWN = 19,    /* FmsError::IterativeSolverBreakdown (minv != 0) */
+  REFEFF_FMS_ERR_DEBYE = 20                   /* DebyeError::IntegrationDidNotConverge / NonFiniteOutput, or a
+                                                 pair sigma^2 that fails narrow_nonnegative_f64_to_f32 */
 } refeff_fms_status;
 
 /* Solver forms for the dense system (I - G0 T) X = G0[:, absorber]. */
@@ -141,6 +143,28 @@ typedef struct {
 
 int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* input,
                                       refeff_fms_plan** out);
+
+/* The pair mean-square displacement table that feeds
+ * refeff_fms_plan_input.mean_square_displacements, computed on the GPU.
+ * Replaces fms_mean_square_displacements_with_metadata
+ * (crates/refeff-engine/src/fms.rs:4345-4433) for idwopt < 0 (sig2g for every
+ * i != j pair), 0 (correlated Debye: corrfn/sigms on the path atom1 -> atom2
+ * -> atom1, crates/refeff-core/src/debye/models.rs:88-271) and 3 (classical
+ * Debye: corrfn2/sigcl); other idwopt values return UNSUPPORTED.
+ *   positions_xyz, potentials: the prepared cluster (refeff_fms_yprep_cluster)
+ *   atomic_numbers: per potential 0..n_potentials-1 (phase.bin potential headers)
+ *   temperature, debye_temperature: fms.inp tk, thetad (K)
+ *   average_norman_radius: phase.bin rnrmav (Bohr)
+ *   table_out: n_atoms x n_atoms floats, [atom2 + N*atom1], host memory
+ *   debye_term_out: optional n_atoms x n_atoms doubles, the Debye term before
+ *                   sig2g is added and the sum narrowed (NULL to skip)
+ * Errors: INVALID_ARGUMENT (tk < 0, thetad <= 0, rnrmav <= 0, atomic number
+ * outside 1..139, two atoms at one position), POTENTIAL_OUT_OF_RANGE,
+ * NONFINITE_COORDINATE, DEBYE. */
+int refeff_fms_debye_sigma2_table(refeff_fms_context* ctx, int idwopt, int n_atoms, const float* positions_xyz,
+                                  const int* potentials, int n_potentials, const int* atomic_numbers,
+                                  double temperature, double debye_temperature, double average_norman_radius,
+                                  float sig2g, float* table_out, double* debye_term_out);
 void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan);
 
 /* Sizes of a plan: state count n, channel count C = nsp (L+1)^2 of the

@@ -186,12 +186,12 @@ def phase_bin_text(*, nsp, energy_grid, reference_energy, potentials, pad_width=
 
 
 def fms_inp_text(*, lmaxph, rfms2, rdirec, toler1=1e-3, toler2=1e-3, idwopt=-1, sig2g=0.0, minv=0, mfms=1,
-                 do_fms=0, save_gg_slice=False) -> str:
+                 do_fms=0, save_gg_slice=False, tk=0.0, thetad=0.0) -> str:
     def i4(vals):
         return "".join(f"{v:4d}" for v in vals)
     return ("mfms, idwopt, minv\n" + i4([mfms, idwopt, minv]) + "\n"
             "rfms2, rdirec, toler1, toler2\n" + f"{rfms2:13.5f}{rdirec:13.5f}{toler1:13.5f}{toler2:13.5f}\n"
-            "tk, thetad, sig2g\n" + f"{0.0:13.5f}{0.0:13.5f}{sig2g:13.5f}\n"
+            "tk, thetad, sig2g\n" + f"{tk:13.5f}{thetad:13.5f}{sig2g:13.5f}\n"
             " lmaxph(0:nph)\n" + i4(lmaxph) + "\n"
             " the number of decomposi\n" + f"{-1:5d}\n"
             " save_gg_slice\n" + ("T" if save_gg_slice else "F") + "\n"
@@ -274,14 +274,15 @@ def geom_dat_text(positions, potentials) -> str:
 
 
 def write_workdir(path: Path, *, positions, potentials, lmaxph, energy_grid, phase_potentials, nsp=1, ispin=0,
-                  rfms2=100.0, rdirec=100.0, sig2g=0.0, do_fms=0, nspu=None, global_kw=None):
+                  rfms2=100.0, rdirec=100.0, sig2g=0.0, do_fms=0, nspu=None, global_kw=None, idwopt=-1, tk=0.0,
+                  thetad=0.0):
     path.mkdir(parents=True, exist_ok=True)
     ne = len(energy_grid)
     (path / "phase.bin").write_text(phase_bin_text(nsp=nsp, energy_grid=energy_grid,
                                                    reference_energy=np.zeros((ne, nsp), complex),
                                                    potentials=phase_potentials))
     (path / "fms.inp").write_text(fms_inp_text(lmaxph=lmaxph, rfms2=rfms2, rdirec=rdirec, sig2g=sig2g,
-                                               do_fms=do_fms))
+                                               do_fms=do_fms, idwopt=idwopt, tk=tk, thetad=thetad))
     (path / "global.inp").write_text(global_inp_text(ispin, **(global_kw or {})))
     (path / "geom.dat").write_text(geom_dat_text(positions, potentials))
     if nspu is not None:

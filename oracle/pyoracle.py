@@ -24,7 +24,7 @@ _lib = None
 
 def build(force: bool = False) -> Path:
     """Compile the oracle with its Makefile (g++, OpenMP, -ffp-contract=off)."""
-    newest = max((HERE / f).stat().st_mtime for f in ("fms_oracle.cpp", "mkgtr_oracle.cpp", "Makefile"))
+    newest = max((HERE / f).stat().st_mtime for f in ("fms_oracle.cpp", "mkgtr_oracle.cpp", "debye_oracle.cpp", "Makefile"))
     if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < newest:
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB_PATH
@@ -70,6 +70,9 @@ def _declare(L):
         "oracle_fms_spectrum_iterative": [_i, _i, _d, _d, _i, _p, _p, _i, _i, _i, _i, _i, _p, _d, _p, _d, _i, _p, _p,
                                           _p, _p, _i],
         "oracle_mkgtr_trace": [_i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p],
+        "oracle_debye_correlation": [_i, _d, _d, _d, _i, _i, _d, _p, _p],
+        "oracle_debye_waller": [_i, _d, _d, _d, _i, _p, _p, _p],
+        "oracle_debye_sigma2_table": [_i, _i, _p, _p, _i, _p, _d, _d, _d, C.c_float, _p, _p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -83,6 +86,8 @@ def _declare(L):
     L.oracle_wigner_3j.restype = _d
     L.oracle_wigner_rotation.argtypes = [_d, _i, _i, _i, _i]
     L.oracle_wigner_rotation.restype = _d
+    L.oracle_atomic_weight.argtypes = [_i]
+    L.oracle_atomic_weight.restype = _d
 
 
 def ptr(a: np.ndarray | None):
@@ -232,3 +237,41 @@ def mkgtr_trace(gg, bmats, lind, rkk, *, nsp, lmax):
     check(lib().oracle_mkgtr_trace(E, dim, int(nsp), int(lmax), nspec, ptr(li), ptr(b.view(np.float64)), ptr(g),
                                    ptr(r), int(rk.shape[2]), ptr(out)))
     return out.view(np.complex128).reshape((nspec, E), order="F")
+
+
+def atomic_weight(z: int) -> float:
+    """FEFF atwtd (crates/refeff-core/src/atomic/tables.rs:10-19): -1.0 outside Z = 1..139."""
+    return float(lib().oracle_atomic_weight(int(z)))
+
+
+def debye_correlation(r, thetad, tk, z1, z2, rsavg, *, classical=False):
+    """corrfn / corrfn2 (crates/refeff-core/src/debye/models.rs:88-132): returns (value, romberg iterations)."""
+    out = np.zeros(1)
+    it = np.zeros(1, np.int32)
+    check(lib().oracle_debye_correlation(int(classical), float(r), float(thetad), float(tk), int(z1), int(z2),
+                                         float(rsavg), ptr(out), ptr(it)))
+    return float(out[0]), int(it[0])
+
+
+def debye_waller(tk, thetad, rsavg, positions, atomic_numbers, *, classical=False):
+    """sigms / sigcl (crates/refeff-core/src/debye/models.rs:134-271) over a path (rows x 3, Angstrom)."""
+    pos = np.ascontiguousarray(np.asarray(positions, np.float64).reshape(-1, 3))
+    z = np.ascontiguousarray(np.asarray(atomic_numbers, np.int32))
+    out = np.zeros(1)
+    check(lib().oracle_debye_waller(int(classical), float(tk), float(thetad), float(rsavg), pos.shape[0], ptr(pos),
+                                    ptr(z), ptr(out)))
+    return float(out[0])
+
+
+def debye_sigma2_table(idwopt, positions, potentials, atomic_numbers, *, tk, thetad, rsavg, sig2g=0.0):
+    """The FMS pair sigma^2 table (crates/refeff-engine/src/fms.rs:4345-4433) for idwopt < 0, 0 or 3: returns
+    (table f32 (N, N) indexed [atom2, atom1], Debye term f64 (N, N))."""
+    pos = np.ascontiguousarray(np.asarray(positions, np.float32).reshape(-1, 3))
+    pots = np.ascontiguousarray(np.asarray(potentials, np.int32))
+    z = np.ascontiguousarray(np.asarray(atomic_numbers, np.int32))
+    N = pos.shape[0]
+    out = np.zeros(N * N, np.float32)
+    pair = np.zeros(N * N)
+    check(lib().oracle_debye_sigma2_table(int(idwopt), N, ptr(pos), ptr(pots), len(z), ptr(z), float(tk),
+                                          float(thetad), float(rsavg), C.c_float(sig2g), ptr(out), ptr(pair)))
+    return out.reshape((N, N), order="F"), pair.reshape((N, N), order="F")

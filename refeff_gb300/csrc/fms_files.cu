@@ -235,6 +235,8 @@ struct PhaseBin {
   std::vector<refeff_complex128> em;    // ne
   std::vector<refeff_complex128> eref;  // ne x nsp, energy fastest
   std::vector<int> lmax;                // per potential
+  std::vector<int> iz;                  // atomic number per potential (potential header)
+  double rnrmav = 0.0;                  // average Norman radius, Bohr (scalar block, parse.rs:50)
   // phase shifts per potential: (energy, l_slot, spin) with l_slot = l + lmax(pot)
   std::vector<std::vector<refeff_complex128>> ph;
 };
@@ -267,7 +269,9 @@ int read_phase_bin(const std::string& path, PhaseBin& pb, std::string& err) {
     err = cur.error;
     return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   }
+  pb.rnrmav = dum[0];
   pb.lmax.resize(size_t(pb.npot));
+  pb.iz.resize(size_t(pb.npot));
   pb.ph.resize(size_t(pb.npot));
   for (int p = 0; p < pb.npot; ++p) {
     if (cur.pos >= lines.size()) { err = "phase.bin ended before potential " + std::to_string(p); return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
@@ -275,6 +279,7 @@ int read_phase_bin(const std::string& path, PhaseBin& pb, std::string& err) {
     long long lm = 0, iz = 0;
     if (ph.size() < 2 || !parse_int(ph[0], lm) || !parse_int(ph[1], iz) || lm < 0) { err = "bad potential header"; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
     pb.lmax[size_t(p)] = int(lm);
+    pb.iz[size_t(p)] = int(iz);
     const int lc = 2 * int(lm) + 1;
     auto& tab = pb.ph[size_t(p)];
     tab.assign(size_t(pb.ne) * lc * pb.nsp, {0.0, 0.0});
@@ -524,8 +529,8 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
     }
     L = std::max(L, fi.lmaxph[size_t(p)]);
   }
-  if (fi.idwopt >= 0) {
-    set_error(ctx, "only idwopt < 0 (uniform sig2g) Debye-Waller damping is supported");
+  if (fi.idwopt >= 0 && fi.idwopt != 0 && fi.idwopt != 3) {
+    set_error(ctx, "only idwopt < 0 (uniform sig2g), 0 (correlated Debye) and 3 (classical Debye) are supported");
     return REFEFF_FMS_ERR_UNSUPPORTED;
   }
   if (fi.save_gg_slice) {
@@ -573,7 +578,17 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   in.global_lmax = L;
   in.raw_potential_lmax = fi.lmaxph.data();
   in.direct_cutoff = rdirec;
+  // pair sigma^2 (fms_mean_square_displacements_with_metadata, fms.rs:4345-4433):
+  // the Debye models take phase.bin's rnrmav and per-potential atomic numbers
+  std::vector<float> msd;
   in.mean_square_displacements = nullptr;
+  if (fi.idwopt == 0 || fi.idwopt == 3) {
+    msd.resize(size_t(natoms) * size_t(natoms));
+    rc = refeff_fms_debye_sigma2_table(ctx, fi.idwopt, natoms, opos.data(), opots.data(), pb.npot, pb.iz.data(),
+                                       fi.tk, fi.thetad, pb.rnrmav, float(fi.sig2g), msd.data(), nullptr);
+    if (rc) return rc;
+    in.mean_square_displacements = msd.data();
+  }
   in.sig2g = float(fi.sig2g);
   in.convergence_tolerance = float(fi.toler1);
   in.zero_tolerance = float(fi.toler2);
@@ -643,6 +658,8 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   char buf[128];
   std::snprintf(buf, sizeof buf, "Using %5d energy points.\n", E);
   log += buf;
+  if (fi.idwopt == 0) log += "Applying Debye-Waller factors using a Correlated Debye model.\n";
+  if (fi.idwopt == 3) log += "Applying Debye-Waller factors using the Classical Debye model.\n";
   log += "xprep done\n";
   if (fi.do_fms != 0 && natoms > 1) {
     std::snprintf(buf, sizeof buf, "FMS for a cluster of %4d atoms\n", natoms);

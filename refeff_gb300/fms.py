@@ -29,7 +29,7 @@ STATUS_NAMES = {
     5: "InvalidAngularLimit", 6: "NonFiniteInput", 7: "NonFiniteCoordinate", 8: "ZeroRho", 9: "SingularMatrix",
     10: "NotConverged", 11: "DuplicateAbsorber", 12: "MissingCentralAtom", 13: "Unsupported", 14: "Cuda",
     15: "OutOfMemory", 16: "InvalidTolerance", 17: "InvalidClusterRadius", 18: "ScratchLimit",
-    19: "IterativeSolverBreakdown",
+    19: "IterativeSolverBreakdown", 20: "DebyeError",
 }
 
 
@@ -119,6 +119,8 @@ def load(build_if_missing: bool = True):
         "refeff_fms_write_fms_bin": ([C.c_char_p, C.c_double, _i, _i, _i, _i, _i, _i, _p], _i),
         "refeff_fms_write_gtr_dat": ([C.c_char_p, _i, _p, _p], _i),
         "refeff_fms_real_space_spectrum_multi": ([_p, _i, _p, _p, _i, _p, _p, _p], _i),
+        "refeff_fms_debye_sigma2_table": ([_p, _i, _i, _p, _p, _i, _p, C.c_double, C.c_double, C.c_double,
+                                           C.c_float, _p, _p], _i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -397,6 +399,27 @@ def complex_lu_solve_device_noalloc(n: int, m: int, batch: int, d_A: int, d_B: i
             _p(d_pivot) if d_pivot else None, _p(stream) if stream else None)
     if rc:
         raise FmsError(rc, "allocation-free dense solve")
+
+
+def debye_sigma2_table(ctx: Context, idwopt, positions, potentials, atomic_numbers, *, temperature,
+                       debye_temperature, average_norman_radius, sig2g=0.0, with_debye_term=False):
+    """Pair sigma^2 table of the FMS stage on the GPU (refeff_fms_debye_sigma2_table; the reference's
+    fms_mean_square_displacements_with_metadata, crates/refeff-engine/src/fms.rs:4345-4433, for idwopt < 0, 0 and
+    3).  Returns the f32 (N, N) table indexed [atom2, atom1] (and the FP64 Debye term when asked)."""
+    lib = load()
+    pos = np.ascontiguousarray(np.asarray(positions, np.float32).reshape(-1, 3))
+    pots = np.ascontiguousarray(np.asarray(potentials, np.int32))
+    z = np.ascontiguousarray(np.asarray(atomic_numbers, np.int32))
+    N = pos.shape[0]
+    out = np.zeros(N * N, np.float32)
+    term = np.zeros(N * N) if with_debye_term else None
+    rc = lib.refeff_fms_debye_sigma2_table(ctx.handle, int(idwopt), N, _ptr(pos), _ptr(pots), len(z), _ptr(z),
+                                           float(temperature), float(debye_temperature),
+                                           float(average_norman_radius), C.c_float(sig2g), _ptr(out), _ptr(term))
+    if rc:
+        raise FmsError(rc, ctx.last_error())
+    table = out.reshape((N, N), order="F")
+    return (table, term.reshape((N, N), order="F")) if with_debye_term else table
 
 
 def transition_matrix(*, lmax, initial_kappa, polarization, polarization_tensor=None, multipole=1,

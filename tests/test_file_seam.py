@@ -135,7 +135,7 @@ def _wave_number(em, er):
     return np.complex64(complex(w.real / BOHR, w.imag / BOHR))
 
 
-def _oracle_gg(work, positions, pots, lmaxph, rdirec):
+def _oracle_gg(work, positions, pots, lmaxph, rdirec, sigsqr=None, sig2g=0.0):
     pb = fms.read_phase_bin(work / "phase.bin")
     ne, nsp = pb["reference_energy"].shape
     L, npot, lm = max(lmaxph), len(lmaxph), max(pb["potential_lmax"])
@@ -145,7 +145,8 @@ def _oracle_gg(work, positions, pots, lmaxph, rdirec):
     for p in range(npot):
         for sl in range(-lmaxph[p], lmaxph[p] + 1):
             xp[:, :, sl + L, p] = pb["phase_shifts"][:, sl + lm, :, p].astype(np.complex64)
-    scat = pyoracle.fms_spectrum(np.asarray(positions, np.float32), pots, lmaxph, k, xp, nsp=nsp, rdirec=rdirec)
+    scat = pyoracle.fms_spectrum(np.asarray(positions, np.float32), pots, lmaxph, k, xp, nsp=nsp, rdirec=rdirec,
+                                 sigsqr=sigsqr, sig2g=sig2g)
     m = nsp * (lmaxph[0] + 1) ** 2
     return scat[:, :m, :m, 0]
 
@@ -205,10 +206,12 @@ def test_run_dir_larger_cluster_and_output_spin_capacity(tmp_path):
 def test_run_dir_rejects_unsupported_and_inconsistent_inputs(tmp_path):
     ctx = fms.Context(0)
     ff.reference_engine_fixture(tmp_path)
-    (tmp_path / "fms.inp").write_text(ff.fms_inp_text(lmaxph=[1, 1], rfms2=3.0, rdirec=5.0, idwopt=0))
-    with pytest.raises(fms.FmsError) as e:
-        fms.run_fms_in_dir(ctx, tmp_path)
-    assert e.value.code == 13
+    for idwopt in (1, 2, 4, 5):  # spring, sig2.dat and DMDW models are outside this library
+        (tmp_path / "fms.inp").write_text(ff.fms_inp_text(lmaxph=[1, 1], rfms2=3.0, rdirec=5.0, idwopt=idwopt,
+                                                          tk=300.0, thetad=315.0))
+        with pytest.raises(fms.FmsError) as e:
+            fms.run_fms_in_dir(ctx, tmp_path)
+        assert e.value.code == 13
     (tmp_path / "fms.inp").write_text(ff.fms_inp_text(lmaxph=[1], rfms2=3.0, rdirec=5.0))
     with pytest.raises(fms.FmsError) as e:
         fms.run_fms_in_dir(ctx, tmp_path)
@@ -218,3 +221,36 @@ def test_run_dir_rejects_unsupported_and_inconsistent_inputs(tmp_path):
         fms.run_fms_in_dir(ctx, tmp_path)
     assert e.value.code == 5
     assert not (tmp_path / "gg.dat").exists()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("idwopt", [0, 3])
+def test_run_dir_debye_damping(tmp_path, idwopt):
+    """idwopt 0 / 3: the pair sigma^2 table comes from the correlated / classical Debye model with phase.bin's
+    rnrmav and atomic numbers (fms.rs:4345-4433); gg equals the oracle fed the oracle's own table, and the log
+    names the model (fms.rs:6048-6058)."""
+    from refeff_gb300 import workloads as wl
+    ctx = fms.Context(0)
+    rng = np.random.default_rng(31)
+    cl = wl.small_cluster(3.2, lmax=2, n_energies=1, seed=5)[0]
+    pos = np.asarray(cl.positions, float)
+    pots = [int(p) for p in cl.potentials]
+    ne = 4
+    grid = 0.6 + 0.5 * np.arange(ne) + 0.04j
+    phase_pots = _phase_potentials(rng, ne, 1, [2] * (max(pots) + 1))
+    phase_pots = [(lm, z, lab, ph) for (lm, _, lab, ph), z in zip(phase_pots, [29, 8, 26, 47][:len(phase_pots)])]
+    ff.write_workdir(tmp_path, positions=pos, potentials=pots, lmaxph=[2] * (max(pots) + 1), energy_grid=grid,
+                     phase_potentials=phase_pots, rfms2=100.0, rdirec=100.0, sig2g=0.002, idwopt=idwopt, tk=300.0,
+                     thetad=315.0)
+    fms.run_fms_in_dir(ctx, tmp_path, fms.FORM_FP64_LU)
+    got = np.array(ff.parse_gg_dat((tmp_path / "gg.dat").read_text()))
+    cpos, cpots = fms.fms_yprep_cluster(pos, pots, cluster_radius=100.0)
+    zs = [p[1] for p in phase_pots]
+    table, _ = pyoracle.debye_sigma2_table(idwopt, cpos, cpots, zs, tk=300.0, thetad=315.0, rsavg=1.2, sig2g=0.002)
+    assert table.max() > 0.002
+    want = _oracle_gg(tmp_path, cpos, cpots, [2] * (max(pots) + 1), 100.0, sigsqr=table)
+    plain = _oracle_gg(tmp_path, cpos, cpots, [2] * (max(pots) + 1), 100.0, sig2g=0.002)
+    assert np.abs(want - plain).max() > 1e-6 * np.abs(want).max()   # the damping changes gg
+    assert np.abs(got - want).max() <= 1e-9 * np.abs(want).max()
+    model = "a Correlated Debye model" if idwopt == 0 else "the Classical Debye model"
+    assert f"Applying Debye-Waller factors using {model}." in (tmp_path / "log3.dat").read_text()
