@@ -76,11 +76,21 @@ typedef enum {
   REFEFF_FMS_FORM_FP64_LU = 0,
   /* Complex FP32 LU, then FP64 iterative refinement of the full solution
    * against the FP64 system until the residual meets the plan tolerance. */
-  REFEFF_FMS_FORM_FP32_REFINED = 1
+  REFEFF_FMS_FORM_FP32_REFINED = 1,
+  /* BiCGSTAB on the complex FP32 system, all m absorber columns of a batch
+   * together, right-preconditioned by the plan's learned diagonal
+   * (refeff_fms_plan_set_preconditioner; none when unset), inside the same FP64
+   * iterative refinement as FP32_REFINED.  Energies whose solve misses the
+   * tolerance within the iteration cap are re-solved with the FP64 LU.  LU-form
+   * plans (minv = 0) only.  No reference counterpart: the reference's
+   * BiCGSTAB (minv = 1, iterative.rs:181-254) is unpreconditioned and
+   * Complex32. */
+  REFEFF_FMS_FORM_BICGSTAB = 2
 } refeff_fms_form;
 
 typedef struct refeff_fms_context refeff_fms_context;
 typedef struct refeff_fms_plan refeff_fms_plan;
+typedef struct refeff_fms_precond_model refeff_fms_precond_model;
 
 /* ---- context ---------------------------------------------------------- */
 
@@ -341,6 +351,53 @@ int refeff_fms_write_fms_bin(const char* path, double cluster_radius, int ne, in
 /* gtr.dat writer (gtr_dat_string, crates/refeff-io/src/gtr_dat.rs:60-71): per
  * energy Re E, Im E, Re gtr, Im gtr as F13.6.  Host only. */
 int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* energy, const refeff_complex128* trace);
+
+/* ---- learned preconditioner for the BiCGSTAB form ---------------------- */
+/* No reference counterpart.  A small MLP (features -> 2 tanh layers of
+ * `hidden` units -> outputs) predicts, per (energy, atom), the channel
+ * diagonal of the atom's block of (I - G0 T)^-1 as a deviation from 1; the
+ * BiCGSTAB form applies it as a right preconditioner.  Features per (energy,
+ * atom): Re/Im k, the atom's t_l (l = 0..lmax), and for three neighbour shells
+ * (< 2.9, < 3.7, < 4.6 Angstrom) the neighbour count / 12, the mean distance / 5
+ * and the neighbours' mean t_l: 2 + 2(L+1) + 3 (2 + 2(L+1)) values.  Outputs:
+ * 2 (L+1)^2 (Re, Im per channel l^2 + l + m).  Training (forward, backward,
+ * Adam) and inference run on the GPU. */
+int refeff_fms_precond_model_create(refeff_fms_context* ctx, int lmax, int hidden, unsigned long long seed,
+                                    refeff_fms_precond_model** out);
+void refeff_fms_precond_model_destroy(refeff_fms_precond_model* model);
+int refeff_fms_precond_model_query(const refeff_fms_precond_model* model, int* n_features, int* hidden, int* n_outputs,
+                                   long long* n_params);
+/* Parameters as one float vector: W1[H][F], b1[H], W2[H][H], b2[H], W3[O][H], b3[O]. */
+int refeff_fms_precond_get_params(const refeff_fms_precond_model* model, float* out);
+int refeff_fms_precond_set_params(refeff_fms_precond_model* model, const float* in);
+/* Mean squared error over n samples (X: n x F, T: n x O, row-major) and its
+ * gradient with respect to the parameters (n_params floats). */
+int refeff_fms_precond_loss_grad(refeff_fms_precond_model* model, int n_samples, const float* X, const float* T,
+                                 double* loss, float* grad);
+/* Adam (beta 0.9 / 0.999, eps 1e-8) on shuffled mini-batches; epoch_loss
+ * (optional, `epochs` doubles) receives the full-set loss after each epoch. */
+int refeff_fms_precond_train(refeff_fms_precond_model* model, int n_samples, const float* X, const float* T,
+                             int epochs, int batch_size, float learning_rate, unsigned long long seed,
+                             double* epoch_loss);
+int refeff_fms_precond_predict(refeff_fms_precond_model* model, int n_samples, const float* X, float* Y);
+/* Attach a model (built for the plan's global lmax) or detach it (NULL). The
+ * plan does not own the model. */
+int refeff_fms_plan_set_preconditioner(refeff_fms_plan* plan, refeff_fms_precond_model* model);
+/* BiCGSTAB controls: iteration cap per solve, relative residual tolerance of
+ * each solve, and how often (iterations) the host checks for completion. */
+int refeff_fms_plan_set_bicgstab(refeff_fms_plan* plan, int max_iterations, double tolerance, int poll_interval);
+/* BiCGSTAB iterations per energy of the last BICGSTAB-form call (all solves). */
+int refeff_fms_plan_bicgstab_stats(const refeff_fms_plan* plan, int n_energies, int32_t* iterations);
+/* Features of every (energy, atom), atoms in device order (absorber last):
+ * E * n_atoms rows of n_features floats. */
+int refeff_fms_plan_precond_features(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                     float* features_out);
+/* Training targets from the FP64 LU: the diagonal of atom `atom`'s block of
+ * (I - G0 T)^-1 per energy (atom: prepared-cluster index, 0 = absorber;
+ * its state count must not exceed the absorber block width).  diag_out:
+ * E x (states of the atom); status_out: per energy (optional). */
+int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
+                                     refeff_complex128* diag_out, int32_t* status_out);
 
 /* ---- dense solve (refeff-linalg boundary) ----------------------------- */
 

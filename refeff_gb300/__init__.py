@@ -5,11 +5,13 @@ this package is the Python mirror of the reference interface used by tests and
 benchmarks.  There is no CPU fallback.
 """
 from .fms import (  # noqa: F401
+    FORM_BICGSTAB,
     FORM_FP32_REFINED,
     FORM_FP64_LU,
     Context,
     FmsError,
     FmsRealSpacePlan,
+    PrecondModel,
     complex_lu_solve_batched,
     debye_sigma2_table,
     fms_real_space_plan,
@@ -31,7 +33,7 @@ from .fms import (  # noqa: F401
 )
 
 __all__ = [
-    "FORM_FP32_REFINED", "FORM_FP64_LU", "Context", "FmsError", "FmsRealSpacePlan", "complex_lu_solve_batched",
+    "FORM_BICGSTAB", "FORM_FP32_REFINED", "FORM_FP64_LU", "Context", "FmsError", "FmsRealSpacePlan", "PrecondModel", "complex_lu_solve_batched",
     "debye_sigma2_table",
     "fms_real_space_plan", "fms_real_space_spectrum", "fms_real_space_spectrum_device", "fms_real_space_spectrum_multi",
     "fms_yprep_cluster",

@@ -1,0 +1,35 @@
+// Batched right-preconditioned BiCGSTAB on the FP32 system matrices of a batch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fms_plan.cuh"
+
+namespace rfx {
+
+// Vectors kept per (matrix, column): x, r (also s), r-hat, p, v, p-hat, s-hat, t.
+constexpr int kBicgVectors = 8;
+// Doubles kept per (matrix, column): rho, alpha, omega, |b|^2, and accumulators.
+constexpr int kBicgScalars = 16;
+
+struct BicgWork {
+  float2* vec = nullptr;     // kBicgVectors * batch * lda * m
+  double* sc = nullptr;      // batch * m * kBicgScalars
+  int* state = nullptr;      // batch * m: 0 running, 1 converged, 2 breakdown
+  int* done = nullptr;       // batch: every column finished
+  int* iters = nullptr;      // batch: iterations of the slowest column
+  int* active = nullptr;     // 1 int: matrices still running (host poll)
+};
+
+// Solves A X = B for every matrix of the batch whose skip flag is clear:
+// A = the first n columns of M32, B = its last m columns, X written over B.
+// Right preconditioner: diagonal D (batch * lda complex, NULL for none), i.e.
+// BiCGSTAB on A D y = b, x = D y.  Stops a column when |r|_2 <= tol |b|_2;
+// after max_iter iterations, or on a breakdown, the matrix's flag in
+// `failed` is set to 2 (the caller's fallback marker) and its X is left as the
+// last iterate.  The host polls the number of running matrices every
+// `poll` iterations (one small device-to-host copy), so the call is not
+// capturable into a CUDA graph.
+cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BicgWork& w,
+                           double tol, int max_iter, int poll, const int* skip, int* failed, cudaStream_t s);
+
+}  // namespace rfx

@@ -23,6 +23,8 @@
 
 #include "../../include/refeff_fms.h"
 #include "batched_lu.cuh"
+#include "bicgstab.cuh"
+#include "precond_mlp.cuh"
 #include "cplx.cuh"
 #include "fms_plan.cuh"
 #include "host_internal.h"
@@ -49,6 +51,9 @@ struct refeff_fms_context {
   int use_tensor_cores = 1;  // FP32 trailing updates on tcgen05 (REFEFF_FMS_OPT_TENSOR_CORES)
   int dense_refinement = 10; // corrections of the dense FP32 solve (REFEFF_FMS_OPT_DENSE_REFINEMENT)
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
+  // the caller's handle plus one per live plan and model: the context is torn
+  // down when the last of them is destroyed, in whatever order that happens
+  std::atomic<int> refs{1};
 };
 
 void rfx::set_last_error(refeff_fms_context* ctx, const std::string& msg) {
@@ -158,8 +163,10 @@ extern "C" int refeff_fms_context_create(int device, refeff_fms_context** out) {
   return REFEFF_FMS_OK;
 }
 
-extern "C" void refeff_fms_context_destroy(refeff_fms_context* ctx) {
-  if (!ctx) return;
+void rfx::context_retain(refeff_fms_context* ctx) { ctx->refs.fetch_add(1, std::memory_order_relaxed); }
+
+void rfx::context_release(refeff_fms_context* ctx) {
+  if (!ctx || ctx->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) {
     cudaStreamSynchronize(ctx->stream);
@@ -171,6 +178,8 @@ extern "C" void refeff_fms_context_destroy(refeff_fms_context* ctx) {
   }
   delete ctx;
 }
+
+extern "C" void refeff_fms_context_destroy(refeff_fms_context* ctx) { context_release(ctx); }
 
 extern "C" const char* refeff_fms_last_error(const refeff_fms_context* ctx) {
   return ctx ? ctx->last_error.c_str() : "null context";
@@ -326,6 +335,13 @@ struct Workspace {
   DevBuf<int2> perm_in;              // row moves of the inner panels (two-level FP32 LU)
   DevBuf<int> nperm_in;
   DevBuf<int> pos_scratch;           // panel row-position bookkeeping for large n
+  // BiCGSTAB form: solver vectors and scalars, the preconditioner diagonal,
+  // per-atom features and network outputs
+  DevBuf<float2> bicg_vec, precond_D;
+  DevBuf<double> bicg_sc;
+  DevBuf<int> bicg_state, bicg_done, bicg_iters, bicg_active, bicg_total;
+  DevBuf<float> feat_X, feat_Y;
+  MlpScratch mlp;
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
   std::map<int, cudaGraphExec_t> graphs;  // key: form
@@ -363,6 +379,17 @@ struct refeff_fms_plan {
   DevBuf<int> d_status_all;
   DevBuf<int> d_partner;  // spin partner per state, device order (-1 none)
   double toler1 = 0.0, toler2 = 0.0;  // iterative forms: convergence and G0 drop tolerances (f32 values)
+  // BiCGSTAB form
+  std::vector<float> pos_dev;         // positions, device atom order (host copy)
+  std::vector<int> pot_dev;           // potentials, device atom order (host copy)
+  std::vector<int> off_dev;           // first state of each atom, device order (host copy, N + 1)
+  refeff_fms_precond_model* model = nullptr;  // learned preconditioner (not owned), NULL: none
+  DevBuf<float> d_shell_info, d_shell_pots;
+  int bicg_max_iter = 400;
+  double bicg_tol = 1.0e-6;
+  int bicg_poll = 8;
+  DevBuf<int> d_bicg_iters_all;
+  std::vector<int> last_bicg_iters;
   Workspace ws;
   bool profiling = false;
   double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0};
@@ -476,6 +503,9 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   cudaStream_t s = ctx->stream;
   const int ds = 2 * (L + 1) * (2 * L + 1) * (2 * L + 3) / 3;
   RF_CUDA(ctx, p.d_pos.upload(pos.data(), pos.size(), s));
+  p.pos_dev = pos;
+  p.pot_dev = dpot;
+  p.off_dev = doff;
   RF_CUDA(ctx, p.d_atom_pot.upload(dpot.data(), dpot.size(), s));
   RF_CUDA(ctx, p.d_atom_off.upload(doff.data(), doff.size(), s));
   RF_CUDA(ctx, p.d_atom_lmax.upload(dlmax.data(), dlmax.size(), s));
@@ -517,15 +547,18 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   launch_plan_geometry(P, s);
   RF_CUDA(ctx, cudaGetLastError());
   RF_CUDA(ctx, cudaStreamSynchronize(s));
+  context_retain(ctx);
   *out = plan.release();
   return REFEFF_FMS_OK;
 }
 
 extern "C" void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan) {
   if (!plan) return;
-  cudaSetDevice(plan->ctx->device);
-  cudaStreamSynchronize(plan->ctx->stream);
+  refeff_fms_context* ctx = plan->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   delete plan;
+  context_release(ctx);
 }
 
 extern "C" int refeff_fms_plan_set_profiling(refeff_fms_plan* plan, int enable) {
@@ -717,6 +750,86 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
   return cudaGetLastError();
 }
 
+__global__ void add_iterations_kernel(int batch, const int* iters, int* total) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) total[b] += iters[b];
+}
+
+BicgWork bicg_work(Workspace& ws) {
+  BicgWork w;
+  w.vec = ws.bicg_vec.p;
+  w.sc = ws.bicg_sc.p;
+  w.state = ws.bicg_state.p;
+  w.done = ws.bicg_done.p;
+  w.iters = ws.bicg_iters.p;
+  w.active = ws.bicg_active.p;
+  return w;
+}
+
+// BiCGSTAB form: the same refinement as refine_fp32 with the FP32 LU solves
+// replaced by preconditioned BiCGSTAB solves on the unfactored FP32 matrix
+// (M32 holds A and, in its last m columns, the right-hand side).  A system
+// whose BiCGSTAB solve misses its tolerance within the iteration cap is
+// marked converged = 2 and handed to the FP64 LU by the caller.
+cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, int iters, double tol, int max_iter,
+                            double inner_tol, int poll, cudaStream_t s, Spans* spans = nullptr) {
+  const BatchLayout& lay = ws.lay;
+  const BicgWork w = bicg_work(ws);
+  auto span = [&](int phase, auto&& fn) -> cudaError_t {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (spans) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, s);
+    }
+    cudaError_t e = fn();
+    if (spans) {
+      cudaEventRecord(b, s);
+      spans->push_back({phase, {a, b}});
+    }
+    return e;
+  };
+  const size_t nb8 = size_t(batch) * sizeof(unsigned long long);
+  cudaMemsetAsync(ws.converged.p, 0, size_t(batch) * sizeof(int), s);
+  cudaMemsetAsync(ws.iters.p, 0, size_t(batch) * sizeof(int), s);
+  cudaMemsetAsync(ws.bicg_total.p, 0, size_t(batch) * sizeof(int), s);
+  auto solve = [&]() -> cudaError_t {
+    cudaError_t e = bicgstab_solve(lay, batch, ws.M32.p, D, w, inner_tol, max_iter, poll, ws.converged.p,
+                                   ws.converged.p, s);
+    count_launch();
+    add_iterations_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.bicg_iters.p, ws.bicg_total.p);
+    return e != cudaSuccess ? e : cudaGetLastError();
+  };
+  cudaError_t e = span(1, [&] {
+    cudaError_t e1 = solve();
+    launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, true, nullptr, nullptr, nullptr, s);
+    return e1;
+  });
+  if (e != cudaSuccess) return e;
+  for (int it = 0; it < iters; ++it) {
+    span(3, [&] {
+      cudaMemsetAsync(ws.rnorm.p, 0, nb8, s);
+      cudaMemsetAsync(ws.bnorm.p, 0, nb8, s);
+      launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.Xsplit.p, ws.R.p, ws.rnorm.p,
+                      ws.bnorm.p, ws.converged.p, s);
+      return cudaGetLastError();
+    });
+    e = span(1, [&] {
+      cudaMemsetAsync(ws.dnorm.p, 0, nb8, s);
+      cudaMemsetAsync(ws.xnorm.p, 0, nb8, s);
+      launch_residual_to_rhs32(lay, batch, ws.R.p, ws.rnorm.p, ws.M32.p, ws.converged.p, s);
+      cudaError_t e1 = solve();
+      launch_accumulate_correction(lay, batch, ws.M32.p, ws.rnorm.p, ws.X64.p, false, ws.converged.p, ws.dnorm.p,
+                                   ws.xnorm.p, s);
+      launch_ir_check(batch, ws.rnorm.p, ws.bnorm.p, ws.dnorm.p, ws.xnorm.p, tol, ws.converged.p, ws.iters.p,
+                      ws.relres.p, ws.dprev.p, s);
+      return e1;
+    });
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
 __global__ void status_not_converged_kernel(int batch, const int* converged, int* status) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < batch && converged[b] != 1 && status[b] == kDevOk) status[b] = kDevNotConverged;
@@ -769,6 +882,30 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     if (e != cudaSuccess) return e;
     tick(4, [&] {
       launch_absorber_solve<double>(lay, batch, ws.M64.p, ws.gg_stage.p, ws.status.p, s);
+      return cudaGetLastError();
+    });
+  } else if (form == REFEFF_FMS_FORM_BICGSTAB) {
+    tick(0, [&] {
+      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, ws.M32.p, ws.status.p, s);
+      if (p.model) {
+        // learned diagonal: features -> network -> D per state
+        const MlpShape& sh = *model_shape(p.model);
+        launch_features(batch, p.N, p.L, p.nsp, p.npot, ws.k_stage.p, ws.x_stage.p, p.d_atom_pot.p,
+                        p.d_shell_info.p, p.d_shell_pots.p, ws.feat_X.p, s);
+        cudaError_t e1 = mlp_forward(sh, model_params(p.model), batch * p.N, ws.feat_X.p, ws.mlp, ws.feat_Y.p, s);
+        if (e1 != cudaSuccess) return e1;
+        launch_scatter_diag(batch, p.N, p.L, p.nsp, lay.lda, p.d_atom_off.p, p.d_atom_lmax.p, ws.feat_Y.p,
+                            ws.precond_D.p, s);
+      }
+      return cudaGetLastError();
+    });
+    e = refine_bicgstab(ws, batch, p.model ? ws.precond_D.p : nullptr, p.refine_iters, p.refine_tol, p.bicg_max_iter,
+                        p.bicg_tol, p.bicg_poll, s, prof ? &spans : nullptr);
+    if (e != cudaSuccess) return e;
+    tick(4, [&] {
+      count_launch();
+      status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
+      launch_extract_absorber(lay, batch, ws.X64.p, ws.gg_stage.p, s);
       return cudaGetLastError();
     });
   } else {
@@ -824,12 +961,19 @@ int pick_batch(refeff_fms_plan& p, int E, bool fp32) {
   return std::min(E, b);
 }
 
+// FP64_LU and FP32_REFINED serve every plan; BICGSTAB the LU-form plans (minv = 0).
+bool form_valid(const refeff_fms_plan& p, refeff_fms_form form) {
+  return form == REFEFF_FMS_FORM_FP64_LU || form == REFEFF_FMS_FORM_FP32_REFINED ||
+         (form == REFEFF_FMS_FORM_BICGSTAB && p.minv == 0);
+}
+
 // Solve E energies whose inputs are already on the device (d_k: E*nsp, d_x:
 // E*xph); writes d_gg (E*m*m) and d_status (E).  Uses graph replay per batch.
 int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
                           double2* d_gg, int* d_status, cudaStream_t s) {
   refeff_fms_context* ctx = p.ctx;
-  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
+  const bool fp32 = form != REFEFF_FMS_FORM_FP64_LU;  // the BiCGSTAB form uses the refined form's buffers
+  const bool bicg = form == REFEFF_FMS_FORM_BICGSTAB;
   const int B = pick_batch(p, E, fp32);
   int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, fp32);
   if (rc) return rc;
@@ -848,13 +992,30 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     RF_CUDA(ctx, p.d_relres_all.alloc(size_t(E)));
     RF_CUDA(ctx, p.d_iters_all.alloc(size_t(E)));
   }
+  if (bicg) {
+    const size_t cols = size_t(ws.batch) * p.m;
+    RF_CUDA(ctx, ws.bicg_vec.alloc(size_t(kBicgVectors) * cols * ws.lay.lda));
+    RF_CUDA(ctx, ws.bicg_sc.alloc(cols * kBicgScalars));
+    RF_CUDA(ctx, ws.bicg_state.alloc(cols));
+    RF_CUDA(ctx, ws.bicg_done.alloc(size_t(ws.batch)));
+    RF_CUDA(ctx, ws.bicg_iters.alloc(size_t(ws.batch)));
+    RF_CUDA(ctx, ws.bicg_total.alloc(size_t(ws.batch)));
+    RF_CUDA(ctx, ws.bicg_active.alloc(1));
+    RF_CUDA(ctx, p.d_bicg_iters_all.alloc(size_t(E)));
+    if (p.model) {
+      const MlpShape& sh = *model_shape(p.model);
+      RF_CUDA(ctx, ws.precond_D.alloc(size_t(ws.batch) * ws.lay.lda));
+      RF_CUDA(ctx, ws.feat_X.alloc(size_t(ws.batch) * p.N * sh.F));
+      RF_CUDA(ctx, ws.feat_Y.alloc(size_t(ws.batch) * p.N * sh.O));
+    }
+  }
   for (int e0 = 0; e0 < E; e0 += B) {
     const int nb = std::min(B, E - e0);
     RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, d_k + size_t(e0) * p.nsp, size_t(nb) * p.nsp * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
     RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
-    if (nb == B && !p.profiling) {
+    if (nb == B && !p.profiling && !bicg) {  // the BiCGSTAB form polls the host: not capturable
       const int key = int(form);
       auto it = ws.graphs.find(key);
       if (it == ws.graphs.end()) {
@@ -891,6 +1052,9 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_iters_all.p + e0, ws.iters.p, size_t(nb) * sizeof(int),
                                    cudaMemcpyDeviceToDevice, s));
     }
+    if (bicg)
+      RF_CUDA(ctx, cudaMemcpyAsync(p.d_bicg_iters_all.p + e0, ws.bicg_total.p, size_t(nb) * sizeof(int),
+                                   cudaMemcpyDeviceToDevice, s));
   }
   return REFEFF_FMS_OK;
 }
@@ -901,7 +1065,7 @@ int solve_device_energies_finish(refeff_fms_plan& p, int E, const double2* d_k, 
                                  refeff_fms_form form, double2* d_gg, int* d_status, cudaStream_t s) {
   refeff_fms_context* ctx = p.ctx;
   Workspace& ws = p.ws;
-  const bool refined = form == REFEFF_FMS_FORM_FP32_REFINED && p.minv == 0;
+  const bool refined = form != REFEFF_FMS_FORM_FP64_LU && p.minv == 0;
   const int B = ws.batch;
   const size_t xph = p.xph_per_energy();
   if (!refined) return REFEFF_FMS_OK;
@@ -960,8 +1124,7 @@ extern "C" int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int 
                                                      int32_t* d_status, void* stream) {
   if (!plan || n_energies < 0 || (n_energies > 0 && (!d_wave_numbers || !d_phase_shifts || !d_gg_out || !d_status)))
     return REFEFF_FMS_ERR_INVALID_ARGUMENT;
-  if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
-    return fail(plan->ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
+  if (!form_valid(*plan, form)) return fail(plan->ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form for this plan");
   if (n_energies == 0) return REFEFF_FMS_OK;
   RF_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : plan->ctx->stream;
@@ -982,8 +1145,7 @@ int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, r
   const int E = points->n_energies;
   if (E < 0 || (E > 0 && (!points->wave_numbers || !points->phase_shifts)))
     return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "invalid energy points");
-  if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
-    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
+  if (!form_valid(p, form)) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form for this plan");
   const size_t C = size_t(p.C), tab = C * C * size_t(p.npot);
   std::memset(scattering_out, 0, size_t(E) * tab * sizeof(refeff_complex128));
   if (E == 0) return REFEFF_FMS_OK;
@@ -1009,9 +1171,13 @@ int spectrum_end(refeff_fms_plan& p, const refeff_fms_energy_points* points, ref
   std::vector<int> st(static_cast<size_t>(E));
   RF_CUDA(ctx, cudaMemcpyAsync(gg.data(), p.d_gg_all.p, gg.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), p.d_status_all.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
-  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED && p.minv == 0;  // refinement statistics exist
+  const bool fp32 = form != REFEFF_FMS_FORM_FP64_LU && p.minv == 0;  // refinement statistics exist
   p.last_relres.assign(fp32 ? size_t(E) : 0, 0.0);
   p.last_iters.assign(fp32 ? size_t(E) : 0, 0);
+  p.last_bicg_iters.assign(form == REFEFF_FMS_FORM_BICGSTAB ? size_t(E) : 0, 0);
+  if (form == REFEFF_FMS_FORM_BICGSTAB)
+    RF_CUDA(ctx, cudaMemcpyAsync(p.last_bicg_iters.data(), p.d_bicg_iters_all.p, size_t(E) * sizeof(int),
+                                 cudaMemcpyDeviceToHost, s));
   if (fp32) {
     RF_CUDA(ctx, cudaMemcpyAsync(p.last_relres.data(), p.d_relres_all.p, size_t(E) * sizeof(double),
                                  cudaMemcpyDeviceToHost, s));
@@ -1124,6 +1290,141 @@ extern "C" int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int
   if (fp64_fallback)
     for (int e : plan->last_fallback)
       if (e < n_energies) fp64_fallback[e] = 1;
+  return REFEFF_FMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// BiCGSTAB form and its learned preconditioner
+// ---------------------------------------------------------------------------
+namespace {
+
+int ensure_shell_tables(refeff_fms_plan& p, cudaStream_t s) {
+  if (p.d_shell_info.p) return REFEFF_FMS_OK;
+  const ShellTables t = shell_tables(p.N, p.npot, p.pos_dev.data(), p.pot_dev.data());
+  RF_CUDA(p.ctx, p.d_shell_info.upload(t.info.data(), t.info.size(), s));
+  RF_CUDA(p.ctx, p.d_shell_pots.upload(t.pots.data(), t.pots.size(), s));
+  RF_CUDA(p.ctx, cudaStreamSynchronize(s));
+  return REFEFF_FMS_OK;
+}
+
+// RHS columns of M64 <- unit vectors of states [s0, s0 + cnt), zero beyond.
+__global__ void unit_rhs_kernel(BatchLayout lay, double2* M, int s0, int cnt) {
+  const int b = blockIdx.y;
+  double2* Mb = M + size_t(b) * lay.stride + size_t(lay.lda) * lay.n;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < lay.lda * lay.m; idx += gridDim.x * blockDim.x) {
+    const int r = idx % lay.lda, c = idx / lay.lda;
+    Mb[idx] = make_double2(c < cnt && r == s0 + c ? 1.0 : 0.0, 0.0);
+  }
+}
+
+__global__ void inverse_diagonal_kernel(BatchLayout lay, const double2* M, int s0, int cnt, double2* out) {
+  const int b = blockIdx.x, c = threadIdx.x;
+  if (c >= cnt) return;
+  out[size_t(b) * cnt + c] = M[size_t(b) * lay.stride + size_t(s0 + c) + size_t(lay.lda) * (lay.n + c)];
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_plan_set_preconditioner(refeff_fms_plan* plan, refeff_fms_precond_model* model) {
+  if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (model && model_lmax(model) != plan->L)
+    return fail(plan->ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "preconditioner model built for another lmax");
+  RF_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+  if (model) {
+    const int rc = ensure_shell_tables(*plan, plan->ctx->stream);
+    if (rc) return rc;
+  }
+  plan->model = model;
+  plan->ws.precond_D.release();  // re-sized on the next BiCGSTAB call
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_set_bicgstab(refeff_fms_plan* plan, int max_iterations, double tolerance,
+                                            int poll_interval) {
+  if (!plan || max_iterations < 1 || !(tolerance > 0.0) || poll_interval < 1) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->bicg_max_iter = max_iterations;
+  plan->bicg_tol = tolerance;
+  plan->bicg_poll = poll_interval;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_bicgstab_stats(const refeff_fms_plan* plan, int n_energies, int32_t* iterations) {
+  if (!plan || n_energies < 0 || (n_energies > 0 && !iterations)) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  for (int e = 0; e < n_energies; ++e)
+    iterations[e] = e < int(plan->last_bicg_iters.size()) ? plan->last_bicg_iters[size_t(e)] : 0;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_precond_features(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                                float* features_out) {
+  if (!plan || !points || points->n_energies < 0 || !features_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  refeff_fms_plan& p = *plan;
+  const int E = points->n_energies;
+  if (E == 0) return REFEFF_FMS_OK;
+  RF_CUDA(p.ctx, cudaSetDevice(p.ctx->device));
+  cudaStream_t s = p.ctx->stream;
+  int rc = ensure_shell_tables(p, s);
+  if (rc) return rc;
+  const int F = feature_count(p.L);
+  DevBuf<double2> dk, dx;
+  DevBuf<float> dX;
+  RF_CUDA(p.ctx, dk.upload(reinterpret_cast<const double2*>(points->wave_numbers), size_t(E) * p.nsp, s));
+  RF_CUDA(p.ctx, dx.upload(reinterpret_cast<const double2*>(points->phase_shifts), size_t(E) * p.xph_per_energy(), s));
+  RF_CUDA(p.ctx, dX.alloc(size_t(E) * p.N * F));
+  launch_features(E, p.N, p.L, p.nsp, p.npot, dk.p, dx.p, p.d_atom_pot.p, p.d_shell_info.p, p.d_shell_pots.p, dX.p, s);
+  RF_CUDA(p.ctx, cudaGetLastError());
+  RF_CUDA(p.ctx, cudaMemcpyAsync(features_out, dX.p, size_t(E) * p.N * F * sizeof(float), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(p.ctx, cudaStreamSynchronize(s));
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
+                                                refeff_complex128* diag_out, int32_t* status_out) {
+  if (!plan || !points || points->n_energies < 0 || !diag_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  refeff_fms_plan& p = *plan;
+  refeff_fms_context* ctx = p.ctx;
+  if (atom < 0 || atom >= p.N) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "atom index outside the cluster");
+  const int d = atom == 0 ? p.N - 1 : atom - 1;  // device order: absorber last
+  const int s0 = p.off_dev[size_t(d)], cnt = p.off_dev[size_t(d) + 1] - s0;
+  if (cnt > p.m) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "atom has more states than the absorber block");
+  const int E = points->n_energies;
+  if (E == 0) return REFEFF_FMS_OK;
+  RF_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const int B = pick_batch(p, E, false);
+  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, false);
+  if (rc) return rc;
+  Workspace& ws = p.ws;
+  const BatchLayout& lay = ws.lay;
+  const size_t xph = p.xph_per_energy();
+  RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
+  RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
+  DevBuf<double2> dout;
+  RF_CUDA(ctx, dout.alloc(size_t(ws.batch) * cnt));
+  std::vector<int> st(static_cast<size_t>(ws.batch));
+  for (int e0 = 0; e0 < E; e0 += B) {
+    const int nb = std::min(B, E - e0);
+    RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, reinterpret_cast<const double2*>(points->wave_numbers) + size_t(e0) * p.nsp,
+                                 size_t(nb) * p.nsp * sizeof(double2), cudaMemcpyHostToDevice, s));
+    RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, reinterpret_cast<const double2*>(points->phase_shifts) + size_t(e0) * xph,
+                                 size_t(nb) * xph * sizeof(double2), cudaMemcpyHostToDevice, s));
+    RF_CUDA(ctx, cudaMemsetAsync(ws.status.p, 0, size_t(nb) * sizeof(int), s));
+    RF_CUDA(ctx, cudaMemsetAsync(ws.info.p, 0, size_t(nb) * sizeof(int), s));
+    launch_build_system(p.P, nb, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, nullptr, ws.status.p, s);
+    count_launch();
+    unit_rhs_kernel<<<dim3(64, unsigned(nb)), 256, 0, s>>>(lay, ws.M64.p, s0, cnt);
+    RF_CUDA(ctx, lu_eliminate<double>(ws.pc64, lay, nb, ws.M64.p, lu_work(ws, ws.pc64), s));
+    lu_backward_rhs<double>(ws.pc64, lay, nb, ws.M64.p, nullptr, s);
+    count_launch();
+    inverse_diagonal_kernel<<<unsigned(nb), 64, 0, s>>>(lay, ws.M64.p, s0, cnt, dout.p);
+    RF_CUDA(ctx, cudaGetLastError());
+    RF_CUDA(ctx, cudaMemcpyAsync(diag_out + size_t(e0) * cnt, dout.p, size_t(nb) * cnt * sizeof(double2),
+                                 cudaMemcpyDeviceToHost, s));
+    RF_CUDA(ctx, cudaMemcpyAsync(st.data(), ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToHost, s));
+    RF_CUDA(ctx, cudaStreamSynchronize(s));
+    for (int i = 0; i < nb; ++i)
+      if (status_out) status_out[e0 + i] = map_status(st[size_t(i)]);
+  }
   return REFEFF_FMS_OK;
 }
 

@@ -8,6 +8,9 @@
 namespace rfx {
 // Records the message returned by refeff_fms_last_error for this context.
 void set_last_error(refeff_fms_context* ctx, const std::string& msg);
+// Plans and models hold a reference on their context (released on destroy).
+void context_retain(refeff_fms_context* ctx);
+void context_release(refeff_fms_context* ctx);
 // The context's device ordinal and its (non-blocking) stream.
 int context_device(const refeff_fms_context* ctx);
 cudaStream_t context_stream(const refeff_fms_context* ctx);

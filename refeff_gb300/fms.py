@@ -23,6 +23,7 @@ from . import build as _build
 
 FORM_FP64_LU = 0
 FORM_FP32_REFINED = 1
+FORM_BICGSTAB = 2
 
 STATUS_NAMES = {
     0: "OK", 1: "InvalidArgument", 2: "EmptyCluster", 3: "PotentialOutOfRange", 4: "MissingRepresentativePotential",
@@ -121,6 +122,19 @@ def load(build_if_missing: bool = True):
         "refeff_fms_real_space_spectrum_multi": ([_p, _i, _p, _p, _i, _p, _p, _p], _i),
         "refeff_fms_debye_sigma2_table": ([_p, _i, _i, _p, _p, _i, _p, C.c_double, C.c_double, C.c_double,
                                            C.c_float, _p, _p], _i),
+        "refeff_fms_precond_model_create": ([_p, _i, _i, C.c_ulonglong, _p], _i),
+        "refeff_fms_precond_model_destroy": ([_p], None),
+        "refeff_fms_precond_model_query": ([_p, _p, _p, _p, _p], _i),
+        "refeff_fms_precond_get_params": ([_p, _p], _i),
+        "refeff_fms_precond_set_params": ([_p, _p], _i),
+        "refeff_fms_precond_loss_grad": ([_p, _i, _p, _p, _p, _p], _i),
+        "refeff_fms_precond_train": ([_p, _i, _p, _p, _i, _i, C.c_float, C.c_ulonglong, _p], _i),
+        "refeff_fms_precond_predict": ([_p, _i, _p, _p], _i),
+        "refeff_fms_plan_set_preconditioner": ([_p, _p], _i),
+        "refeff_fms_plan_set_bicgstab": ([_p, _i, C.c_double, _i], _i),
+        "refeff_fms_plan_bicgstab_stats": ([_p, _i, _p], _i),
+        "refeff_fms_plan_precond_features": ([_p, _p, _p], _i),
+        "refeff_fms_plan_inverse_diagonal": ([_p, _p, _i, _p, _p], _i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -227,6 +241,53 @@ class FmsRealSpacePlan:
                                                                        _ptr(its), _ptr(fb)))
         return rel, its, fb
 
+    def _points(self, wave_numbers, phase_shifts):
+        nsp, L, npot = self.inputs["nsp"], self.inputs["L"], self.inputs["npot"]
+        k = np.ascontiguousarray(np.asarray(wave_numbers, dtype=np.complex128).reshape(-1, nsp))
+        E = k.shape[0]
+        ph = np.asarray(phase_shifts, dtype=np.complex128).reshape(E, nsp, 2 * L + 1, npot)
+        xp = np.ascontiguousarray(np.stack([ph[e].reshape(-1, order="F") for e in range(E)])) if E else \
+            np.zeros((0,), np.complex128)
+        return k, xp, _EnergyPoints(E, _ptr(k), _ptr(xp))
+
+    def set_preconditioner(self, model):
+        """Attach a learned preconditioner (PrecondModel) for the BiCGSTAB form, or detach it (None)."""
+        self._model = model  # the plan does not own the model: keep it alive here
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_preconditioner(self.handle,
+                                                                         model.handle if model else None))
+
+    def set_bicgstab(self, max_iterations=400, tolerance=1e-6, poll_interval=8):
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_bicgstab(self.handle, int(max_iterations),
+                                                                   float(tolerance), int(poll_interval)))
+
+    def bicgstab_stats(self, n_energies: int):
+        """BiCGSTAB iterations per energy of the last BICGSTAB-form call (initial solve + corrections)."""
+        its = np.zeros(n_energies, np.int32)
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_bicgstab_stats(self.handle, int(n_energies), _ptr(its)))
+        return its
+
+    def precond_features(self, wave_numbers, phase_shifts, model_features: int):
+        """Features of every (energy, atom), atoms in device order (absorber last): (E, N, F) float32."""
+        k, xp, pts = self._points(wave_numbers, phase_shifts)
+        N = len(self.inputs["potentials"])
+        out = np.zeros((k.shape[0], N, model_features), np.float32)
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_precond_features(self.handle, C.byref(pts), _ptr(out)))
+        return out
+
+    def inverse_diagonal(self, wave_numbers, phase_shifts, atom: int):
+        """Diagonal of atom `atom`'s block of (I - G0 T)^-1 per energy from the FP64 LU: (E, states) complex."""
+        k, xp, pts = self._points(wave_numbers, phase_shifts)
+        E = k.shape[0]
+        nsp, L = self.inputs["nsp"], self.inputs["L"]
+        lm = min(int(self.inputs["lmaxph"][self.inputs["potentials"][atom]]), L)
+        lm = L if lm < 0 else lm
+        cnt = nsp * (lm + 1) ** 2
+        out = np.zeros((E, cnt), np.complex128)
+        st = np.zeros(E, np.int32)
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_inverse_diagonal(self.handle, C.byref(pts), int(atom), _ptr(out),
+                                                                       _ptr(st)))
+        return out, st
+
     PHASES = ("build", "eliminate", "sweeps", "residual", "extract")
 
     def phase_times(self) -> dict:
@@ -237,6 +298,66 @@ class FmsRealSpacePlan:
     def close(self):
         if getattr(self, "handle", None):
             self.ctx._lib.refeff_fms_real_space_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PrecondModel:
+    """The learned diagonal preconditioner (refeff_fms_precond_model): an MLP trained and run on the GPU."""
+
+    def __init__(self, ctx: Context, lmax: int, hidden: int = 64, seed: int = 0):
+        self.ctx = ctx
+        h = _p()
+        ctx.check(ctx._lib.refeff_fms_precond_model_create(ctx.handle, int(lmax), int(hidden), C.c_ulonglong(seed),
+                                                           C.byref(h)))
+        self.handle = h
+        self.lmax = int(lmax)
+        f, hd, o, npar = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        ctx.check(ctx._lib.refeff_fms_precond_model_query(h, C.byref(f), C.byref(hd), C.byref(o), C.byref(npar)))
+        self.n_features, self.hidden, self.n_outputs, self.n_params = f.value, hd.value, o.value, npar.value
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, np.float32)
+        self.ctx.check(self.ctx._lib.refeff_fms_precond_get_params(self.handle, _ptr(out)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.n_params
+        self.ctx.check(self.ctx._lib.refeff_fms_precond_set_params(self.handle, _ptr(p)))
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        loss = C.c_double()
+        g = np.zeros(self.n_params, np.float32)
+        self.ctx.check(self.ctx._lib.refeff_fms_precond_loss_grad(self.handle, X.shape[0], _ptr(X), _ptr(T),
+                                                                  C.byref(loss), _ptr(g)))
+        return loss.value, g
+
+    def train(self, X, T, *, epochs=200, batch_size=256, learning_rate=2e-3, seed=0):
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        hist = np.zeros(max(epochs, 1))
+        self.ctx.check(self.ctx._lib.refeff_fms_precond_train(self.handle, X.shape[0], _ptr(X), _ptr(T), int(epochs),
+                                                              int(batch_size), C.c_float(learning_rate),
+                                                              C.c_ulonglong(seed), _ptr(hist)))
+        return hist[:epochs]
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        Y = np.zeros((X.shape[0], self.n_outputs), np.float32)
+        self.ctx.check(self.ctx._lib.refeff_fms_precond_predict(self.handle, X.shape[0], _ptr(X), _ptr(Y)))
+        return Y
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.ctx._lib.refeff_fms_precond_model_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -1,0 +1,179 @@
+"""BiCGSTAB form and its learned diagonal preconditioner.
+
+CPU: the network's CPU restatement (oracle/mlp_oracle.py) against finite differences.
+GPU: the training kernels' loss and gradient against that restatement; the feature kernel against its
+restatement; the FP64-LU training targets against a dense inverse; the BiCGSTAB form against the FP64 LU
+(<= 1e-6, the chosen-form gate); and what the trained network gains: fewer BiCGSTAB iterations than the
+unpreconditioned solve on held-out clusters and energies.  Block Jacobi with per-atom blocks is the identity
+here (the same-atom blocks of G0 vanish, so every diagonal block of I - G0 T is I), so the unpreconditioned
+solve is also the block-Jacobi baseline.
+"""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+from oracle import pyoracle as po
+from refeff_gb300 import fms, learned, workloads as wl
+
+
+def _random_problem(rng, F=7, H=5, O=4, S=9):
+    n = H * F + H + H * H + H + O * H + O
+    return rng.normal(size=n) * 0.4, rng.normal(size=(S, F)), rng.normal(size=(S, O)) * 0.3
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    F, H, O = 7, 5, 4
+    p, X, T = _random_problem(rng, F, H, O)
+    _, g = mo.loss_grad(p, F, H, O, X, T)
+    eps = 1e-6
+    for i in rng.choice(p.size, size=40, replace=False):
+        dp = np.zeros_like(p)
+        dp[i] = eps
+        num = (mo.loss_grad(p + dp, F, H, O, X, T)[0] - mo.loss_grad(p - dp, F, H, O, X, T)[0]) / (2 * eps)
+        assert abs(num - g[i]) <= 1e-7 + 1e-6 * abs(num), i
+
+
+def test_feature_and_output_counts():
+    assert mo.feature_count(3) == 40 and mo.output_count(3) == 32
+    assert mo.feature_count(4) == 48 and mo.output_count(4) == 50
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def ctx():
+    return fms.Context(0)
+
+
+@pytest.mark.gpu
+def test_gpu_loss_and_gradient_match_oracle(ctx):
+    rng = np.random.default_rng(1)
+    model = fms.PrecondModel(ctx, 2, hidden=24, seed=3)
+    F, H, O = model.n_features, model.hidden, model.n_outputs
+    p = (rng.normal(size=model.n_params) * 0.3).astype(np.float32)
+    model.set_params(p)
+    X = rng.normal(size=(300, F)).astype(np.float32)
+    T = (rng.normal(size=(300, O)) * 0.2).astype(np.float32)
+    loss, g = model.loss_grad(X, T)
+    ref_loss, ref_g = mo.loss_grad(p.astype(np.float64), F, H, O, X, T)
+    assert abs(loss - ref_loss) <= 1e-5 * ref_loss
+    assert np.linalg.norm(g - ref_g) <= 1e-4 * np.linalg.norm(ref_g)
+    Y = model.predict(X)
+    assert np.abs(Y - mo.forward(p, F, H, O, X)[2]).max() <= 1e-4
+
+
+@pytest.mark.gpu
+def test_gpu_training_reduces_loss(ctx):
+    rng = np.random.default_rng(2)
+    model = fms.PrecondModel(ctx, 1, hidden=32, seed=5)
+    X = rng.normal(size=(2048, model.n_features)).astype(np.float32)
+    T = np.tanh(X[:, :model.n_outputs] * 0.7 + 0.2 * X[:, 1:2]).astype(np.float32)
+    hist = model.train(X, T, epochs=60, batch_size=128, learning_rate=3e-3, seed=1)
+    assert hist[-1] < 0.2 * hist[0]
+    assert np.all(np.isfinite(hist))
+
+
+@pytest.mark.gpu
+def test_gpu_features_match_oracle(ctx):
+    cl, grid = wl.small_cluster(4.0, lmax=3, n_energies=5, seed=2)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    F = mo.feature_count(3)
+    got = plan.precond_features(grid.wave_numbers, grid.phase_shifts, F)
+    N = cl.n_atoms
+    order = [learned.device_index(a, N) for a in range(N)]
+    pos_dev = np.zeros((N, 3))
+    pot_dev = np.zeros(N, int)
+    for a in range(N):
+        pos_dev[order[a]] = cl.positions[a]
+        pot_dev[order[a]] = cl.potentials[a]
+    want = mo.features(grid.wave_numbers, grid.phase_shifts, pos_dev, pot_dev, 3, len(cl.lmaxph))
+    assert np.abs(got - want).max() <= 2e-5 * max(1.0, np.abs(want).max())
+
+
+@pytest.mark.gpu
+def test_gpu_inverse_diagonal_matches_dense_inverse(ctx):
+    """Training targets from the FP64 LU = the diagonal of a dense inverse of the oracle's system matrix."""
+    import sys
+    sys.path.insert(0, str(__import__("pathlib").Path(__file__).parent))
+    from test_oracle_properties import _intermediates
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=3, seed=9)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    b = 9
+    for atom in (0, 1, cl.n_atoms - 1):
+        diag, st = plan.inverse_diagonal(grid.wave_numbers, grid.phase_shifts, atom)
+        assert (st == 0).all() and diag.shape == (3, b)
+        for e in range(3):
+            _, _, A = _intermediates(cl, grid.wave_numbers[e], grid.phase_shifts[e])
+            inv = np.linalg.inv(A)
+            ref = np.diag(inv)[atom * b:(atom + 1) * b]
+            assert np.abs(diag[e] - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_gpu_bicgstab_form_matches_fp64_lu(ctx):
+    cl, grid = wl.config0()
+    sel = np.arange(50, 100, 7)      # the energies above the edge, where BiCGSTAB converges
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    k, ph = grid.wave_numbers[sel], grid.phase_shifts[sel]
+    g64, _ = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_FP64_LU)
+    gb, st = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_BICGSTAB)
+    assert (st == 0).all()
+    its = plan.bicgstab_stats(len(sel))
+    assert (its > 0).all()
+    m = plan.shape.absorber_block
+    for e in range(len(sel)):
+        ref = g64[e, :m, :m, 0]
+        assert np.linalg.norm(gb[e, :m, :m, 0] - ref) <= 1e-6 * np.linalg.norm(ref), e
+
+
+@pytest.mark.gpu
+def test_gpu_bicgstab_iteration_cap_falls_back_to_lu(ctx):
+    """A cap of 3 iterations misses the tolerance: those energies are re-solved by the FP64 LU and flagged."""
+    cl, grid = wl.config0()
+    sel = np.array([60, 80])
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    plan.set_bicgstab(max_iterations=3, tolerance=1e-6, poll_interval=1)
+    k, ph = grid.wave_numbers[sel], grid.phase_shifts[sel]
+    g64, _ = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_FP64_LU)
+    gb, st = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_BICGSTAB)
+    assert (st == 0).all()
+    _, _, fb = plan.refinement_stats(len(sel))
+    assert fb.all()
+    m = plan.shape.absorber_block
+    assert np.linalg.norm(gb[:, :m, :m, 0] - g64[:, :m, :m, 0]) <= 1e-10 * np.linalg.norm(g64[:, :m, :m, 0])
+
+
+@pytest.mark.gpu
+def test_gpu_learned_preconditioner_reduces_iterations(ctx):
+    """Train on FP64-LU targets from seeded rocksalt clusters (radius 4.5-5.5 A, one material), then solve a
+    held-out geometry of the same material: the learned diagonal needs fewer BiCGSTAB iterations than none, at
+    the same accuracy."""
+    train = learned.rocksalt_training_cases(4, radius_range=(4.5, 5.5), n_energies=120, seed=21)
+    X, T = learned.training_set(ctx, train, energies_per_case=40, atoms_per_case=12, seed=3,
+                                energy_window=(-10.0, 100.0))
+    model, hist = learned.train_preconditioner(ctx, 3, X, T, hidden=96, epochs=800, batch_size=128,
+                                               learning_rate=1e-3, seed=4)
+    assert hist[-1] < 0.5 * hist[0]
+    held = wl.rocksalt_cluster(np.random.default_rng(99), radius=5.2)
+    grid = wl.energy_grid(held, 120, -20.0, 100.0, seed=3)  # the training material
+    sel = np.where((grid.energies_ev > -8.0) & (grid.energies_ev < 30.0))[0][::4]
+    k, ph = grid.wave_numbers[sel], grid.phase_shifts[sel]
+    plan = fms.fms_real_space_plan(ctx, held.positions, held.potentials, held.lmaxph)
+    plan.set_bicgstab(max_iterations=2000, tolerance=1e-6, poll_interval=16)
+    g64, _ = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_FP64_LU)
+    g0, st0 = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_BICGSTAB)
+    it0 = plan.bicgstab_stats(len(sel))
+    plan.set_preconditioner(model)
+    g1, st1 = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_BICGSTAB)
+    it1 = plan.bicgstab_stats(len(sel))
+    assert (st0 == 0).all() and (st1 == 0).all()
+    m = plan.shape.absorber_block
+    for g in (g0, g1):
+        for e in range(len(sel)):
+            ref = g64[e, :m, :m, 0]
+            assert np.linalg.norm(g[e, :m, :m, 0] - ref) <= 1e-6 * np.linalg.norm(ref)
+    print("BiCGSTAB iterations, none vs learned:", it0.sum(), it1.sum())
+    assert it1.sum() < 0.9 * it0.sum()
