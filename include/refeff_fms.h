@@ -185,7 +185,9 @@ int refeff_fms_plan_query(const refeff_fms_plan* plan, int* n_states, int* chann
 /* Tuning: energies solved per device batch (0 = automatic from free memory)
  * and the refinement limits of REFEFF_FMS_FORM_FP32_REFINED: at most
  * max_iterations corrections; an energy has converged when its last
- * correction satisfies max|d| <= tolerance * max|x| (default 10, 1e-8).
+ * correction d_k, or the error it leaves, estimated as |d_k|^2 / |d_k-1| (the
+ * initial solve counting as d_0 = x), is within tolerance * max|x| (max norms;
+ * default 10, 1e-10).
  * Energies that reach the limit, or whose corrections stop halving, are
  * solved again with the FP64 LU. */
 int refeff_fms_plan_set_batch(refeff_fms_plan* plan, int max_batch);

@@ -576,10 +576,13 @@ __global__ void accumulate_correction_kernel(BatchLayout lay, const float2* __re
 }
 
 // Stopping rule of the refinement, per system not yet finished (done == 0):
-// record relres = |r| / |b| of this step's residual and count the step; stop
-// with done = 1 when the correction is small, |d| <= tol |x| (the solution is
-// then accurate to about cond * eps32 * tol), or with done = 2 when the
-// corrections stop shrinking (|d| > 0.5 |d_prev|): such systems go to the FP64 LU.
+// record relres = |r| / |b| of this step's residual and count the step.  The
+// corrections shrink geometrically, |d_k+1| ~ rho |d_k| with rho = |d_k| /
+// |d_k-1| (the initial solve counts as d_0 = x), so the error left after
+// applying d_k is about |d_k|^2 / |d_k-1|.  Stop with done = 1 when that
+// estimate, or the correction itself, is within tol |x|; stop with done = 2
+// when the corrections stop shrinking (|d| > 0.5 |d_prev|): such systems go
+// to the FP64 LU.
 __global__ void ir_check_kernel(int batch, const unsigned long long* rnorm, const unsigned long long* bnorm,
                                 const unsigned long long* dnorm, const unsigned long long* xnorm, double tol,
                                 int* done, int* iters, double* relres, double* dprev) {
@@ -589,8 +592,9 @@ __global__ void ir_check_kernel(int batch, const unsigned long long* rnorm, cons
   const double r = v(rnorm, b), bn = v(bnorm, b), d = v(dnorm, b), x = v(xnorm, b);
   relres[b] = bn > 0.0 ? r / bn : r;
   const int it = iters[b]++;
-  if (d <= tol * x) done[b] = 1;
-  else if (it > 0 && d > 0.5 * dprev[b]) done[b] = 2;
+  const double prev = it > 0 ? dprev[b] : x;
+  if (d <= tol * x || d * d <= tol * x * prev) done[b] = 1;
+  else if (it > 0 && d > 0.5 * prev) done[b] = 2;
   dprev[b] = d;
 }
 

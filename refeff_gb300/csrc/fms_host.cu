@@ -344,7 +344,7 @@ struct Workspace {
   MlpScratch mlp;
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
-  std::map<int, cudaGraphExec_t> graphs;  // key: form
+  std::map<int, cudaGraphExec_t> graphs;  // key: form * 65536 + energies in the batch
   std::map<int, unsigned long long> graph_launches;  // kernel launches per replay
   void drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -361,7 +361,7 @@ struct refeff_fms_plan {
   std::vector<long> rep_offsets;  // reference state order
   int max_batch = 0;
   int refine_iters = 10;
-  double refine_tol = 1.0e-8;  // stop when max|correction| <= tol * max|x|
+  double refine_tol = 1.0e-10;  // stop when the correction, or its estimated remaining error, <= tol * max|x|
   // per-energy refinement outcome of the last spectrum call (FP32_REFINED)
   DevBuf<double> d_relres_all;
   DevBuf<int> d_iters_all;
@@ -1016,7 +1016,8 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
     if (nb == B && !p.profiling && !bicg) {  // the BiCGSTAB form polls the host: not capturable
-      const int key = int(form);
+      // a graph bakes in its batch size: key by (form, energies in the batch)
+      const int key = int(form) * 65536 + nb;
       auto it = ws.graphs.find(key);
       if (it == ws.graphs.end()) {
         // first run un-captured (sets kernel attributes), then capture

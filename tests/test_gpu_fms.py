@@ -242,6 +242,24 @@ def test_fms_batching_is_invariant(ctx):
     assert rel_err(split, full) < 1e-13
 
 
+@pytest.mark.parametrize("form", [fms.FORM_FP64_LU, fms.FORM_FP32_REFINED])
+def test_fms_calls_of_different_sizes_on_one_plan(ctx, form):
+    """A plan called with few energies, then many, then few again returns what fresh plans return: a CUDA
+    graph captured for one batch size is never replayed for another."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=9, seed=15)
+    k, ph = grid.wave_numbers, grid.phase_shifts
+    fresh = {}
+    for E in (2, 9):
+        p0 = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+        fresh[E], _ = fms.fms_real_space_spectrum(p0, k[:E], ph[:E], form)
+        p0.close()
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    for E in (2, 2, 9, 9, 2):
+        got, st = fms.fms_real_space_spectrum(plan, k[:E], ph[:E], form)
+        assert (st == 0).all()
+        assert rel_err(got, fresh[E]) < 1e-12, E
+
+
 def test_device_pointer_entry_point(ctx):
     torch = pytest.importorskip("torch")
     cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=5, seed=15)
