@@ -70,7 +70,7 @@ __device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e)
 // result is renormalised (|lo| <= ulp(hi)/2) so that every step adds an error
 // of about 2^-48 |acc| only.
 __device__ __forceinline__ void df_mac(df& acc, float ah, float al, float xh, float xl) {
-  const float p = ah * xh;
+  const float p = __fmul_rn(ah, xh);  // rounded product: must not be fused into the sums below
   float e = fmaf(ah, xh, -p);
   e = fmaf(ah, xl, e);
   e = fmaf(al, xh, e);

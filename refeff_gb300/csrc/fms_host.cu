@@ -375,6 +375,8 @@ struct refeff_fms_plan {
   DevBuf<int> d_atom_pot, d_atom_off, d_atom_lmax;
   DevBuf<double> d_sigsqr, d_dist, d_phi, d_dsmall, d_xnlm, d_xnlm_w, d_t3p, d_t3m;
   DevBuf<double2> d_eph;
+  DevBuf<float2> d_dsmall_df;
+  DevBuf<float4> d_eph_df;
   DevBuf<double2> d_k_all, d_x_all, d_gg_all;
   DevBuf<int> d_status_all;
   DevBuf<int> d_partner;  // spin partner per state, device order (-1 none)
@@ -538,13 +540,17 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   RF_CUDA(ctx, p.d_phi.alloc(size_t(N) * N));
   RF_CUDA(ctx, p.d_eph.alloc(size_t(N) * N * (4 * L + 1)));
   RF_CUDA(ctx, p.d_dsmall.alloc(size_t(N) * N * ds));
+  RF_CUDA(ctx, p.d_eph_df.alloc(size_t(N) * N * (4 * L + 1)));
+  RF_CUDA(ctx, p.d_dsmall_df.alloc(size_t(N) * N * ds));
   PlanDev& P = p.P;
   P.N = N; P.L = L; P.nsp = nsp; P.ispin = p.ispin; P.npot = p.npot; P.n = p.n; P.m = p.m; P.ds = ds;
   P.pos = p.d_pos.p; P.atom_pot = p.d_atom_pot.p; P.atom_off = p.d_atom_off.p; P.atom_lmax = p.d_atom_lmax.p;
   P.sigsqr = p.d_sigsqr.p; P.pair_dist = p.d_dist.p; P.pair_phi = p.d_phi.p; P.pair_dsmall = p.d_dsmall.p;
   P.xnlm = p.d_xnlm.p; P.xnlm_w = p.d_xnlm_w.p; P.t3p = p.d_t3p.p; P.t3m = p.d_t3m.p; P.pair_eph = p.d_eph.p;
+  P.pair_dsmall_df = p.d_dsmall_df.p; P.pair_eph_df = p.d_eph_df.p;
   P.rdirec2 = double(in->direct_cutoff) * double(in->direct_cutoff);
   launch_plan_geometry(P, s);
+  launch_plan_df_tables(P, s);
   RF_CUDA(ctx, cudaGetLastError());
   RF_CUDA(ctx, cudaStreamSynchronize(s));
   context_retain(ctx);

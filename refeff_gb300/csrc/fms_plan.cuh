@@ -33,6 +33,10 @@ struct PlanDev {
   double* pair_phi = nullptr;        // [N*N] azimuth of R_i - R_j           (written by launch_plan_geometry)
   double2* pair_eph = nullptr;       // [N*N*(4L+1)] e^{i mm (phi - pi)}, mm in [-2L, 2L] (launch_plan_geometry)
   double* pair_dsmall = nullptr;     // [N*N][ds] Wigner small-d tables      (written by launch_plan_geometry)
+  // the same two tables as double-float pairs (hi, lo) for the refined form's
+  // build, written by launch_plan_df_tables
+  float2* pair_dsmall_df = nullptr;  // [N*N][ds]
+  float4* pair_eph_df = nullptr;     // [N*N*(4L+1)] (re hi, im hi, re lo, im lo)
   const double* xnlm = nullptr;      // [(L+1)*(L+1)] xnlm(mu, l) at mu + (L+1)*l
   const double* xnlm_w = nullptr;    // [(L+1)*(L+1)] (2l+1) / xnlm(mu, l), same index
   const double* t3p = nullptr;       // spin-orbit coefficients [l + (L+1)*((m+L) + (2L+1)*(s-1))]
@@ -64,6 +68,8 @@ void count_launch();
 
 // ---- geometry (once per plan) ----
 void launch_plan_geometry(const PlanDev& P, cudaStream_t s);
+// pair_dsmall_df / pair_eph_df from pair_dsmall / pair_eph (after launch_plan_geometry)
+void launch_plan_df_tables(const PlanDev& P, cudaStream_t s);
 
 // ---- system build (per energy batch) ----
 // k: [E][nsp] double2; xphase: [E][nsp*(2L+1)*npot] double2 (column-major (nsp, 2L+1, npot)).

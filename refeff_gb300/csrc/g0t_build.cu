@@ -147,6 +147,58 @@ void launch_plan_geometry(const PlanDev& P, cudaStream_t s) {
   }
 }
 
+__global__ void plan_df_tables_kernel(size_t nd, const double* __restrict__ d, float2* __restrict__ ddf, size_t ne,
+                                      const double2* __restrict__ e, float4* __restrict__ edf) {
+  for (size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nd + ne; i += size_t(gridDim.x) * blockDim.x) {
+    if (i < nd) {
+      const float h = float(d[i]);
+      ddf[i] = make_float2(h, float(d[i] - double(h)));
+    } else {
+      edf[i - nd] = split_hi_lo(e[i - nd]);
+    }
+  }
+}
+
+void launch_plan_df_tables(const PlanDev& P, cudaStream_t s) {
+  const size_t nd = size_t(P.N) * P.N * P.ds, ne = size_t(P.N) * P.N * (4 * P.L + 1);
+  count_launch();
+  plan_df_tables_kernel<<<unsigned(std::min<size_t>((nd + ne + 255) / 256, 8192)), 256, 0, s>>>(
+      nd, P.pair_dsmall, P.pair_dsmall_df, ne, P.pair_eph, P.pair_eph_df);
+}
+
+// ---- double-float (FP32 pair) helpers for the refined form's build ----
+// A complex double-float is a float4 (re hi, im hi, re lo, im lo), the layout
+// of split_hi_lo, so a result is stored as the hi/lo system entry directly.
+__device__ __forceinline__ void df_prod(float ah, float al, float bh, float bl, float& ph, float& pl) {
+  const float p = __fmul_rn(ah, bh);  // rounded product: must not be fused into the sum below
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  ph = p + e;
+  pl = e - (ph - p);
+}
+__device__ __forceinline__ float4 dfc_mul(float4 a, float4 b) {
+  df re{0.f, 0.f}, im{0.f, 0.f};
+  df_mac(re, a.x, a.z, b.x, b.z);
+  df_mac(re, -a.y, -a.w, b.y, b.w);
+  df_mac(im, a.x, a.z, b.y, b.w);
+  df_mac(im, a.y, a.w, b.x, b.z);
+  return make_float4(re.hi, im.hi, re.lo, im.lo);
+}
+__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
+  float sh, e;
+  df_two_sum(h, bh, sh, e);
+  e += l + bl;
+  h = sh + e;
+  l = e - (h - sh);
+}
+__device__ __forceinline__ float4 dfc_neg(float4 a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+__device__ __forceinline__ float4 dfc_sub(float4 a, float4 b) {
+  df_add(a.x, a.z, -b.x, -b.z);
+  df_add(a.y, a.w, -b.y, -b.w);
+  return a;
+}
+
 // ---------------------------------------------------------------------------
 // Build kernel: CTA = (column atom j, chunk of kBuildRowAtoms row atoms, energy).
 // ---------------------------------------------------------------------------
@@ -294,8 +346,13 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     colinfo[q] = make_int4(l, m, s, partner);
     double2 t0 = make_double2(0.0, 0.0), t1 = t0;
     if (kMode != 2 && !state_t_matrix(P, xe, potj, l, m, s, t0, t1)) atomicMax(status + e, int(kDevNonfinite));
-    tcol0[q] = t0;
-    tcol1[q] = t1;
+    if constexpr (kMode == 1) {
+      reinterpret_cast<float4*>(tcol0)[q] = split_hi_lo(t0);
+      reinterpret_cast<float4*>(tcol1)[q] = split_hi_lo(t1);
+    } else {
+      tcol0[q] = t0;
+      tcol1[q] = t1;
+    }
   }
   // ---- rows of the chunk ----
   // Rows are visited grouped by (l, spin), then atom and m, so that the lanes
@@ -324,12 +381,16 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
   // ---- per pair: small-d tables (resident, from the plan) ----
   for (int t = tid; t < RA * P.ds; t += nthr) {
     const int p = t / P.ds, q = t % P.ds;
-    dsm[t] = P.pair_dsmall[(size_t(j) + size_t(N) * (i0 + p)) * P.ds + q];
+    const size_t src = (size_t(j) + size_t(N) * (i0 + p)) * P.ds + q;
+    if constexpr (kMode == 1) reinterpret_cast<float2*>(dsm)[t] = P.pair_dsmall_df[src];
+    else dsm[t] = P.pair_dsmall[src];
   }
   // ---- per pair: azimuth phases e^{i m (phi - pi)}, m in [-2L, 2L] (resident, from the plan) ----
   for (int t = tid; t < RA * (4 * L + 1); t += nthr) {
     const int p = t / (4 * L + 1), q = t % (4 * L + 1);
-    eph[t] = P.pair_eph[(size_t(j) + size_t(N) * (i0 + p)) * (4 * L + 1) + q];
+    const size_t src = (size_t(j) + size_t(N) * (i0 + p)) * (4 * L + 1) + q;
+    if constexpr (kMode == 1) reinterpret_cast<float4*>(eph)[t] = P.pair_eph_df[src];
+    else eph[t] = P.pair_eph[src];
   }
   // ---- per (pair, spin): rho, prefactor, Hankel polynomial table ----
   const int rows = L + 2;
@@ -401,7 +462,8 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
       }
       g = cmul(pref[ps], g);  // the pair prefactor e^{i rho}/rho e^{-msd k^2}, folded in once per table entry
     }
-    gtab[t] = g;
+    if constexpr (kMode == 1) reinterpret_cast<float4*>(gtab)[t] = split_hi_lo(g);
+    else gtab[t] = g;
   }
   __syncthreads();
 
@@ -426,6 +488,30 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     const double2 ph = eph[p * (4 * L + 1) + (m2 - m1 + 2 * L)];
     return cmul(ph, make_double2(sx, sy));
   };
+  // the same element in double-float on the FP32 pipes (refined form): GB300
+  // runs FP32 about 64 times faster than FP64, and the system is stored as hi/lo
+  // float pairs anyway
+  const float2* dsm2 = reinterpret_cast<const float2*>(dsm);
+  const float4* gtab4 = reinterpret_cast<const float4*>(gtab);
+  const float4* eph4 = reinterpret_cast<const float4*>(eph);
+  auto g0df = [&](int p, int l1, int m1, int s1, int l2, int m2, int s2) -> float4 {
+    if (s1 != s2 || !flag[p]) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2* tf = dsm2 + size_t(p) * P.ds + lblock_offset(l2);
+    const float2* tb = dsm2 + size_t(p) * P.ds + dpd + lblock_offset(l1);
+    const float4* gg = gtab4 + size_t(p * nsp + (s1 - 1)) * gsz;
+    const int w1 = 2 * l1 + 1, w2 = 2 * l2 + 1, mn = min(l1, l2);
+    df sx{0.f, 0.f}, sy{0.f, 0.f};
+    for (int mu = -mn; mu <= mn; ++mu) {
+      const int amu = mu < 0 ? -mu : mu;
+      const float2 b = tb[(mu + l1) * w1 + (m1 + l1)], f = tf[(m2 + l2) * w2 + (mu + l2)];
+      float dh, dl;
+      df_prod(b.x, b.y, f.x, f.y, dh, dl);
+      const float4 gv = gg[l1 + L1 * (l2 + L1 * amu)];
+      df_mac(sx, dh, dl, gv.x, gv.z);
+      df_mac(sy, dh, dl, gv.y, gv.w);
+    }
+    return dfc_mul(eph4[p * (4 * L + 1) + (m2 - m1 + 2 * L)], make_float4(sx.hi, sy.hi, sx.lo, sy.lo));
+  };
   const int total = nrow * ncol;
   for (int idx = tid; idx < total; idx += nthr) {
     const int v = idx % nrow, cc = idx / nrow;
@@ -433,6 +519,29 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     const int4 ci = colinfo[cc];
     const int rp = ri.x >> 2, rs = ri.x & 3;
     const int r = r0 + ri.w, c = cj0 + cc;
+    if constexpr (kMode == 1) {
+      float4 a = make_float4(0.f, 0.f, 0.f, 0.f), gcol = a;
+      if (i0 + rp != j) {
+        const float4* t0 = reinterpret_cast<const float4*>(tcol0);
+        const float4* t1 = reinterpret_cast<const float4*>(tcol1);
+        gcol = g0df(rp, ri.y, ri.z, rs, ci.x, ci.y, ci.z);
+        a = dfc_neg(dfc_mul(gcol, t0[cc]));
+        if (ci.w >= 0) {
+          const int4 pi = colinfo[ci.w];
+          a = dfc_sub(a, dfc_mul(g0df(rp, ri.y, ri.z, rs, pi.x, pi.y, pi.z), t1[cc]));
+        }
+      }
+      if (r == c) df_add(a.x, a.z, 1.f, 0.f);
+      const size_t ai = base + size_t(r) + size_t(lay.lda) * c;
+      reinterpret_cast<float4*>(M64)[ai] = a;
+      M32[ai] = make_float2(a.x, a.y);
+      if (absorber_col) {
+        const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + cc);
+        reinterpret_cast<float4*>(M64)[bi] = gcol;
+        M32[bi] = make_float2(gcol.x, gcol.y);
+      }
+      continue;
+    }
     double2 a = make_double2(0.0, 0.0), gcol = make_double2(0.0, 0.0);
     if (i0 + rp != j) {
       gcol = g0(rp, ri.y, ri.z, rs, ci.x, ci.y, ci.z);
