@@ -375,7 +375,7 @@ struct refeff_fms_plan {
   DevBuf<int> d_atom_pot, d_atom_off, d_atom_lmax;
   DevBuf<double> d_sigsqr, d_dist, d_phi, d_dsmall, d_xnlm, d_xnlm_w, d_t3p, d_t3m;
   DevBuf<double2> d_eph;
-  DevBuf<float2> d_dsmall_df;
+  DevBuf<float2> d_dsmall_df, d_xnlm_df, d_xnlm_w_df;
   DevBuf<float4> d_eph_df;
   DevBuf<double2> d_k_all, d_x_all, d_gg_all;
   DevBuf<int> d_status_all;
@@ -518,6 +518,19 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
     for (int l = 0; l <= L; ++l)
       for (int mu = 0; mu <= l; ++mu) w[size_t(mu + (L + 1) * l)] = double(2 * l + 1) / xnlm[size_t(mu + (L + 1) * l)];
     RF_CUDA(ctx, p.d_xnlm_w.upload(w.data(), w.size(), s));
+    // double-float copies (hi = fl32(v), lo = fl32(v - hi)) for the refined form's build
+    auto split = [](const std::vector<double>& v) {
+      std::vector<float2> o(v.size());
+      for (size_t i = 0; i < v.size(); ++i) {
+        const float h = float(v[i]);
+        o[i] = make_float2(h, float(v[i] - double(h)));
+      }
+      return o;
+    };
+    const std::vector<float2> xd = split(xnlm), wd = split(w);
+    RF_CUDA(ctx, p.d_xnlm_df.upload(xd.data(), xd.size(), s));
+    RF_CUDA(ctx, p.d_xnlm_w_df.upload(wd.data(), wd.size(), s));
+    RF_CUDA(ctx, cudaStreamSynchronize(s));  // the host vectors go out of scope
   }
   RF_CUDA(ctx, p.d_t3p.upload(t3p.data(), t3p.size(), s));
   RF_CUDA(ctx, p.d_t3m.upload(t3m.data(), t3m.size(), s));
@@ -548,6 +561,7 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   P.sigsqr = p.d_sigsqr.p; P.pair_dist = p.d_dist.p; P.pair_phi = p.d_phi.p; P.pair_dsmall = p.d_dsmall.p;
   P.xnlm = p.d_xnlm.p; P.xnlm_w = p.d_xnlm_w.p; P.t3p = p.d_t3p.p; P.t3m = p.d_t3m.p; P.pair_eph = p.d_eph.p;
   P.pair_dsmall_df = p.d_dsmall_df.p; P.pair_eph_df = p.d_eph_df.p;
+  P.xnlm_df = p.d_xnlm_df.p; P.xnlm_w_df = p.d_xnlm_w_df.p;
   P.rdirec2 = double(in->direct_cutoff) * double(in->direct_cutoff);
   launch_plan_geometry(P, s);
   launch_plan_df_tables(P, s);

@@ -39,6 +39,8 @@ struct PlanDev {
   float4* pair_eph_df = nullptr;     // [N*N*(4L+1)] (re hi, im hi, re lo, im lo)
   const double* xnlm = nullptr;      // [(L+1)*(L+1)] xnlm(mu, l) at mu + (L+1)*l
   const double* xnlm_w = nullptr;    // [(L+1)*(L+1)] (2l+1) / xnlm(mu, l), same index
+  const float2* xnlm_df = nullptr;   // the two tables above as double-float pairs (hi, lo)
+  const float2* xnlm_w_df = nullptr;
   const double* t3p = nullptr;       // spin-orbit coefficients [l + (L+1)*((m+L) + (2L+1)*(s-1))]
   const double* t3m = nullptr;
   double rdirec2 = 0.0;              // direct-cutoff radius squared (Angstrom^2)

@@ -436,6 +436,11 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
                 csub(c[(il - 2) + rows * (im - 1)], cmul(f, cadd(c[(il - 1) + rows * (im - 1)], c[(il - 1) + rows * (im - 2)])));
           }
         }
+        if constexpr (kMode == 1) {
+          // the refined form works on double-float copies (same 16 bytes per entry)
+          for (int q = 0; q < rows * L1; ++q) reinterpret_cast<float4*>(c)[q] = split_hi_lo(c[q]);
+          reinterpret_cast<float4*>(pref)[t] = split_hi_lo(pref[t]);
+        }
       }
     }
     if (s == 0) flag[p] = ok;
@@ -447,6 +452,34 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     const int ps = t / gsz, rem = t % gsz;
     const int p = ps / nsp;
     const int l1 = rem % L1, l2 = (rem / L1) % L1, mu = rem / (L1 * L1);
+    if constexpr (kMode == 1) {
+      // g in double-float: gamtl = c(l1, nu) (2 l1 + 1) / xnlm, gam = c(l2, mu + nu) (-1)^mu xnlm, summed,
+      // times the pair prefactor
+      float4 gdf = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (flag[p] && mu <= l1 && mu <= l2) {
+        const float4* c = reinterpret_cast<const float4*>(clm) + size_t(ps) * rows * L1;
+        const float2 w1 = P.xnlm_w_df[mu + L1 * l1];
+        float2 n2 = P.xnlm_df[mu + L1 * l2];
+        if (mu & 1) n2 = make_float2(-n2.x, -n2.y);
+        df gr{0.f, 0.f}, gi{0.f, 0.f};
+        const int numax = min(l1, l2 - mu);
+        for (int nu = 0; nu <= numax; ++nu) {
+          const float4 c1 = c[l1 + rows * nu], c2 = c[l2 + rows * (mu + nu)];
+          float arh, arl, aih, ail, brh, brl, bih, bil;
+          df_prod(c1.x, c1.z, w1.x, w1.y, arh, arl);
+          df_prod(c1.y, c1.w, w1.x, w1.y, aih, ail);
+          df_prod(c2.x, c2.z, n2.x, n2.y, brh, brl);
+          df_prod(c2.y, c2.w, n2.x, n2.y, bih, bil);
+          df_mac(gr, arh, arl, brh, brl);
+          df_mac(gr, -aih, -ail, bih, bil);
+          df_mac(gi, arh, arl, bih, bil);
+          df_mac(gi, aih, ail, brh, brl);
+        }
+        gdf = dfc_mul(reinterpret_cast<const float4*>(pref)[ps], make_float4(gr.hi, gi.hi, gr.lo, gi.lo));
+      }
+      reinterpret_cast<float4*>(gtab)[t] = gdf;
+      continue;
+    }
     double2 g = make_double2(0.0, 0.0);
     if (flag[p] && mu <= l1 && mu <= l2) {
       const double2* c = clm + size_t(ps) * rows * L1;
@@ -462,8 +495,7 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
       }
       g = cmul(pref[ps], g);  // the pair prefactor e^{i rho}/rho e^{-msd k^2}, folded in once per table entry
     }
-    if constexpr (kMode == 1) reinterpret_cast<float4*>(gtab)[t] = split_hi_lo(g);
-    else gtab[t] = g;
+    gtab[t] = g;
   }
   __syncthreads();
 
