@@ -203,28 +203,11 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
   cluster.sync();
 }
 
-// One warp per column in [c_begin, c_end): apply the panel's row moves, then
-// solve the panel rows with the unit lower L11.
-template <typename T, int NB, bool kSolve = true>
-__global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, int c_begin, int c_end,
-                                                        cplx<T>* __restrict__ M, LuWork w, const int* skip) {
+template <typename T, int NB, bool kSolve>
+__device__ __forceinline__ void rhs_lower_column(const BatchLayout& lay, int k, int kb, cplx<T>* colp, const LuWork& w,
+                                                 int b, const cplx<T> (*L11)[NB + 1], int lane) {
   using C = cplx<T>;
-  const int b = blockIdx.y;
-  if (skip && skip[b]) return;
-  __shared__ C L11[NB][NB + 1];
-  const int n = lay.n;
-  const int kb = min(NB, n - k);
   const int panel = k / NB;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  C* Mb = M + size_t(b) * lay.stride;
-  for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
-    const int r = idx % kb, c = idx / kb;
-    L11[r][c] = Mb[size_t(k + r) + size_t(lay.lda) * (k + c)];
-  }
-  __syncthreads();
-  const int col = c_begin + blockIdx.x * (blockDim.x / 32) + wid;
-  if (col >= c_end) return;
-  C* colp = Mb + size_t(lay.lda) * col;
   const size_t pidx = size_t(b) * w.npanels + panel;
   const int np = w.nperm[pidx];
   const int2* pm = w.perm + pidx * (2 * NB);
@@ -242,7 +225,7 @@ __global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, 
   for (int t = 0; t < kMoves; ++t)
     if (dst[t] >= 0) colp[dst[t]] = v[t];
   __syncwarp();
-  if (!kSolve) return;
+  if constexpr (!kSolve) return;
   constexpr int kRows = (NB + 31) / 32;
   C x[kRows];
 #pragma unroll
@@ -272,6 +255,36 @@ __global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, 
   }
 }
 
+// Columns [c_begin, c_end), kRhsColsPerWarp per warp (one after another, so
+// that each CTA reads L11 once for 8 * kRhsColsPerWarp columns): apply the
+// panel's row moves, then solve the panel rows with the unit lower L11.
+constexpr int kRhsColsPerWarp = 4;
+
+template <typename T, int NB, bool kSolve = true>
+__global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, int c_begin, int c_end,
+                                                        cplx<T>* __restrict__ M, LuWork w, const int* skip) {
+  using C = cplx<T>;
+  const int b = blockIdx.y;
+  if (skip && skip[b]) return;
+  __shared__ C L11[kSolve ? NB : 1][NB + 1];
+  const int n = lay.n;
+  const int kb = min(NB, n - k);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  C* Mb = M + size_t(b) * lay.stride;
+  if constexpr (kSolve) {
+    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+      const int r = idx % kb, c = idx / kb;
+      L11[r][c] = Mb[size_t(k + r) + size_t(lay.lda) * (k + c)];
+    }
+    __syncthreads();
+  }
+  const int first = c_begin + blockIdx.x * (blockDim.x / 32) * kRhsColsPerWarp + wid;
+  for (int cw = 0; cw < kRhsColsPerWarp; ++cw) {
+    const int col = first + cw * (blockDim.x / 32);
+    if (col >= c_end) return;
+    rhs_lower_column<T, NB, kSolve>(lay, k, kb, Mb + size_t(lay.lda) * col, w, b, L11, lane);
+  }
+}
 // One warp per RHS column: X[k:k+kb] = U11^-1 Y[k:k+kb] (bottom-up).
 template <typename T, int NB>
 __global__ void __launch_bounds__(256) rhs_upper_kernel(BatchLayout lay, int k, cplx<T>* __restrict__ M,
@@ -723,7 +736,8 @@ static void launch_rhs_lower(const BatchLayout& lay, int batch, int k, int c_beg
                              const LuWork& w, const int* skip, cudaStream_t s) {
   const int ncols = c_end - c_begin;
   if (ncols <= 0) return;
-  dim3 grid(unsigned((ncols + 7) / 8), unsigned(batch));
+  const int per_cta = 8 * kRhsColsPerWarp;
+  dim3 grid(unsigned((ncols + per_cta - 1) / per_cta), unsigned(batch));
   count_launch();
   rhs_lower_kernel<T, NB, kSolve><<<grid, 256, 0, s>>>(lay, k, c_begin, c_end, M, w, skip);
 }

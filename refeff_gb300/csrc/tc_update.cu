@@ -121,21 +121,36 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k, int kb, const float2* __restrict__ M,
                                                          uint8_t* __restrict__ img, int nbm) {
+  // The tile is read down the columns (coalesced in the column-major matrix),
+  // turned around in shared memory, and written as 16-byte chunks of the
+  // swizzled K-major rows, so that every warp stores 512 contiguous bytes.
+  constexpr int TS = BM + 1;  // padded row of the transposed tile
+  __shared__ float2 T[KC * TS];
   const int bm = blockIdx.x >> 1, chunk = blockIdx.x & 1, b = blockIdx.y;
   const int n = lay.n;
   const int r0 = k + kb + bm * BM;
   const float2* Mb = M + size_t(b) * lay.stride;
-  uint8_t* base = img + ((size_t(b) * nbm + bm) * 2 + chunk) * size_t(A_PLANES) * A_PLANE;
   for (int e = threadIdx.x; e < BM * KC; e += blockDim.x) {
     const int r = e % BM, kk = e / BM;
     const int kcol = chunk * KC + kk;
-    float2 v = make_float2(0.f, 0.f);
-    if (r0 + r < n && kcol < kb) v = Mb[size_t(r0 + r) + size_t(lay.lda) * (k + kcol)];
-    uint32_t s[4];
-    split4(v, s);
-    const int off = sw128_offset(r, kk);
+    T[kk * TS + r] = (r0 + r < n && kcol < kb) ? Mb[size_t(r0 + r) + size_t(lay.lda) * (k + kcol)] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  uint8_t* base = img + ((size_t(b) * nbm + bm) * 2 + chunk) * size_t(A_PLANES) * A_PLANE;
+  for (int e = threadIdx.x; e < BM * (KC / 4); e += blockDim.x) {
+    const int k4 = e % (KC / 4), r = e / (KC / 4);
+    uint32_t q[4][4];
 #pragma unroll
-    for (int p = 0; p < 4; ++p) *reinterpret_cast<uint32_t*>(base + size_t(p) * A_PLANE + off) = s[p];
+    for (int i = 0; i < 4; ++i) {
+      uint32_t sv[4];
+      split4(T[(4 * k4 + i) * TS + r], sv);
+#pragma unroll
+      for (int p = 0; p < 4; ++p) q[p][i] = sv[p];
+    }
+    const int off = sw128_offset(r, 4 * k4);
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+      *reinterpret_cast<uint4*>(base + size_t(p) * A_PLANE + off) = make_uint4(q[p][0], q[p][1], q[p][2], q[p][3]);
   }
 }
 
