@@ -198,8 +198,9 @@ int refeff_fms_plan_set_refinement(refeff_fms_plan* plan, int max_iterations, do
  *   0 system build (G0, T, I - G0 T)   1 LU elimination
  *   2 triangular sweeps                3 FP64 residuals
  *   4 absorber extraction / small solves
+ *   5 the tensor-core trailing-update kernels alone (part of 1)
  * Profiling runs batches without graph replay; enabling it resets the sums. */
-#define REFEFF_FMS_PHASES 5
+#define REFEFF_FMS_PHASES 6
 int refeff_fms_plan_set_profiling(refeff_fms_plan* plan, int enable);
 int refeff_fms_plan_phase_times(const refeff_fms_plan* plan, double* ms_out, int n_phases);
 

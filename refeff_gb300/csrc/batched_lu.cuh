@@ -3,6 +3,9 @@
 // blocked triangular sweeps that reuse the stored factors.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <utility>
+#include <vector>
 #include "cplx.cuh"
 #include "fms_plan.cuh"
 
@@ -27,6 +30,12 @@ inline int panel_count(int n, int nb) { return (n + nb - 1) / nb; }
 constexpr int kTcBM = 128, kTcBN = 48;
 // bytes of the operand tile images for a batch of systems of order n with m right-hand sides
 size_t tc_image_bytes(int n, int m, int batch);
+// CUDA events around every tensor-core update kernel while `on` (plan profiling).
+struct KernelSpans {
+  bool on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spans;
+};
+KernelSpans& tc_update_spans();
 // C -= L21 U12 for elimination step k with tcgen05 MMAs (split TF32, FP32 accumulation).
 void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int col_end, float2* M, uint8_t* images,
                         int* err_flag, const int* skip, cudaStream_t s);

@@ -394,7 +394,7 @@ struct refeff_fms_plan {
   std::vector<int> last_bicg_iters;
   Workspace ws;
   bool profiling = false;
-  double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0};
+  double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0, 0};
   size_t xph_per_energy() const { return size_t(nsp) * size_t(2 * L + 1) * size_t(npot); }
 };
 
@@ -864,6 +864,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
   cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s);
   const bool prof = p.profiling;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
+  tc_update_spans().on = prof;
   auto tick = [&](int phase, auto&& fn) -> cudaError_t {
     cudaEvent_t a = nullptr, b = nullptr;
     if (prof) {
@@ -946,6 +947,10 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
   }
   if (prof) {
     cudaStreamSynchronize(s);
+    KernelSpans& tc = tc_update_spans();
+    for (auto& sp : tc.spans) spans.push_back({5, sp});
+    tc.spans.clear();
+    tc.on = false;
     for (auto& sp : spans) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, sp.second.first, sp.second.second);

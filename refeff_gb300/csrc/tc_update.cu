@@ -312,6 +312,11 @@ __global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+KernelSpans& tc_update_spans() {
+  static KernelSpans spans;
+  return spans;
+}
+
 size_t tc_image_bytes(int n, int m, int batch) {
   const int nbm = (n + BM - 1) / BM, nbn = (n + m + BN - 1) / BN;
   return size_t(batch) * 2 * (size_t(nbm) * A_PLANES * A_PLANE + size_t(nbn) * B_PLANES * B_PLANE);
@@ -334,9 +339,20 @@ void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int co
     cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     attr = true;
   }
+  KernelSpans& prof = tc_update_spans();
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (prof.on) {
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+  }
   count_launch();
   tc_update_kernel<<<dim3(unsigned(nbm), unsigned(nbn), unsigned(batch)), 128, SMEM_BYTES, s>>>(
       lay, k, kb, col_end, M, aimg, bimg, nbm_all, nbn_all, err_flag, skip);
+  if (prof.on) {
+    cudaEventRecord(e1, s);
+    prof.spans.push_back({e0, e1});
+  }
 }
 
 }  // namespace rfx

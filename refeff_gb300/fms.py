@@ -288,7 +288,7 @@ class FmsRealSpacePlan:
                                                                        _ptr(st)))
         return out, st
 
-    PHASES = ("build", "eliminate", "sweeps", "residual", "extract")
+    PHASES = ("build", "eliminate", "sweeps", "residual", "extract", "tc_update")
 
     def phase_times(self) -> dict:
         out = np.zeros(len(self.PHASES))
