@@ -139,7 +139,8 @@ typedef struct {
   const int* potentials;            /* n_atoms */
   int spin_channels;                /* nsp: 1 or 2 */
   int spin_selector;                /* global.inp ispin */
-  int lfms;                         /* 0: absorber potential only; else all potentials */
+  int lfms;                         /* 0: absorber potential only; else all potentials (LU forms, at most
+                                       64 representative states in total) */
   int minv;                         /* FEFF minv: 0 LU, 1 ggbi, 2 ggrm (recursion), 3 gggm, other ggtf (TFQMR) */
   int max_potential;                /* nph */
   int global_lmax;                  /* max over lmaxph */
@@ -238,10 +239,13 @@ int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energ
                                    refeff_fms_report* report);
 
 /* Same solve for inputs already resident in device memory (same layouts as
- * above, device pointers); writes only the absorber block per energy:
- * d_gg_out = n_energies x (m x m) complex128.  `stream` is a cudaStream_t
- * (NULL = the context stream).  Asynchronous: synchronise the stream before
- * reading results. */
+ * above, device pointers); writes the solved blocks per energy: for lfms = 0
+ * the absorber block, d_gg_out = n_energies x (m x m) complex128 (m from
+ * refeff_fms_plan_query); for lfms != 0 the block of every potential
+ * 0..max_potential in turn, each ipart(pot) x ipart(pot) column-major, packed
+ * one after another per energy.  `stream` is a cudaStream_t (NULL = the
+ * context stream).  Asynchronous: synchronise the stream before reading
+ * results. */
 int refeff_fms_real_space_spectrum_device(refeff_fms_plan* plan, int n_energies, const void* d_wave_numbers,
                                           const void* d_phase_shifts, refeff_fms_form form, void* d_gg_out,
                                           int32_t* d_status, void* stream);

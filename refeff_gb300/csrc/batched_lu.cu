@@ -1027,6 +1027,27 @@ void launch_ir_check(int batch, const unsigned long long* rnorm_bits, const unsi
                                                                 tol, done, iters, relres, dprev);
 }
 
+__global__ void extract_blocks_kernel(BatchLayout lay, const double2* __restrict__ X64, const SolvedBlock* blocks,
+                                      int nblocks, int per_matrix, double2* __restrict__ out,
+                                      const int* __restrict__ status) {
+  const int b = blockIdx.x;
+  const bool bad = status && status[b] != kDevOk;
+  for (int q = 0; q < nblocks; ++q) {
+    const SolvedBlock bl = blocks[q];
+    for (int idx = threadIdx.x; idx < bl.size * bl.size; idx += blockDim.x) {
+      const int r = idx % bl.size, c = idx / bl.size;
+      out[size_t(b) * per_matrix + bl.pack + idx] =
+          bad ? make_double2(0.0, 0.0) : X64[size_t(b) * lay.lda * lay.m + size_t(bl.row + r) + size_t(lay.lda) * (bl.col + c)];
+    }
+  }
+}
+
+void launch_extract_blocks(const BatchLayout& lay, int batch, const double2* X64, const SolvedBlock* blocks, int nblocks,
+                           int per_matrix, double2* out, const int* status, cudaStream_t s) {
+  count_launch();
+  extract_blocks_kernel<<<unsigned(batch), 256, 0, s>>>(lay, X64, blocks, nblocks, per_matrix, out, status);
+}
+
 void launch_extract_absorber(const BatchLayout& lay, int batch, const double2* X64, double2* gg, cudaStream_t s) {
   count_launch();
   extract_absorber_kernel<<<unsigned(batch), 256, 0, s>>>(lay, X64, gg);

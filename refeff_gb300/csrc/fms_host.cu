@@ -357,6 +357,13 @@ struct refeff_fms_plan {
   refeff_fms_context* ctx = nullptr;
   int N = 0, L = 0, nsp = 1, ispin = 0, npot = 0, lfms = 0, minv = 0;
   int n = 0, m = 0, C = 0, abs_pot = 0, abs_lmax = 0;
+  // m: right-hand sides (the representative blocks of every potential in the solved range);
+  // m_abs: the absorber block; gg_per: packed size of one energy's solved blocks
+  int m_abs = 0, gg_per = 0;
+  std::vector<SolvedBlock> blocks;   // per potential of the range, in potential order
+  std::vector<int> block_pot;        // the potential of each block
+  DevBuf<SolvedBlock> d_blocks;
+  DevBuf<int> d_bcol;
   std::vector<int> pot_lmax;
   std::vector<long> rep_offsets;  // reference state order
   int max_batch = 0;
@@ -456,15 +463,15 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   p.n = ref_off[size_t(N)];
   p.abs_pot = atom_pot[0];
   p.abs_lmax = std::min(L, p.pot_lmax[size_t(p.abs_pot)]);
-  p.m = nsp * (p.abs_lmax + 1) * (p.abs_lmax + 1);
+  p.m_abs = nsp * (p.abs_lmax + 1) * (p.abs_lmax + 1);
   p.C = nsp * (L + 1) * (L + 1);
   // driver.rs:36-60: active potential range must have representatives
   const int pstart = p.lfms == 0 ? p.abs_pot : 0, pend = p.lfms == 0 ? p.abs_pot : in->max_potential;
   for (int q = pstart; q <= pend; ++q)
     if (p.rep_offsets[size_t(q)] < 0)
       return fail(ctx, REFEFF_FMS_ERR_MISSING_REPRESENTATIVE, "no atom for potential " + std::to_string(q));
-  if (p.lfms != 0)
-    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "lfms != 0 (all-potential FMS) is not supported by this library");
+  if (p.lfms != 0 && p.minv != 0)
+    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "lfms != 0 with the iterative forms (minv != 0) is not supported");
   if (N < 2) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "a single-atom cluster has no scattering");
 
   // device atom order: reference atom 0 (absorber) last
@@ -478,6 +485,27 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
     dlmax[size_t(d)] = std::min(L, p.pot_lmax[size_t(atom_pot[size_t(a)])]);
   }
   for (int d = 0; d < N; ++d) doff[size_t(d) + 1] = doff[size_t(d)] + nsp * (dlmax[size_t(d)] + 1) * (dlmax[size_t(d)] + 1);
+  // solved blocks (fms_lu_scattering, solvers.rs:366-484): for each potential of the range, the
+  // representative's states (its first atom in cluster order) are right-hand sides, and its block
+  // of the solution is the scattering table entry of that potential
+  std::vector<int> bcol(static_cast<size_t>(N), -1);
+  {
+    int col = 0, pack = 0;
+    for (int q = pstart; q <= pend; ++q) {
+      int a = 0;
+      while (atom_pot[size_t(a)] != q) ++a;
+      const int d = dev(a);
+      const int size = doff[size_t(d) + 1] - doff[size_t(d)];
+      bcol[size_t(d)] = col;
+      p.blocks.push_back({doff[size_t(d)], col, size, pack});
+      p.block_pot.push_back(q);
+      col += size;
+      pack += size * size;
+    }
+    p.m = col;
+    p.gg_per = pack;
+  }
+  if (p.m > 64) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "more than 64 right-hand sides in the potential range");
   // sigma^2 table, device order [a2 + N a1] (engine/fms.rs:4394-4426)
   std::vector<double> sig(static_cast<size_t>(N) * N, 0.0);
   for (int a1 = 0; a1 < N; ++a1)
@@ -511,6 +539,8 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   RF_CUDA(ctx, p.d_atom_pot.upload(dpot.data(), dpot.size(), s));
   RF_CUDA(ctx, p.d_atom_off.upload(doff.data(), doff.size(), s));
   RF_CUDA(ctx, p.d_atom_lmax.upload(dlmax.data(), dlmax.size(), s));
+  RF_CUDA(ctx, p.d_bcol.upload(bcol.data(), bcol.size(), s));
+  RF_CUDA(ctx, p.d_blocks.upload(p.blocks.data(), p.blocks.size(), s));
   RF_CUDA(ctx, p.d_sigsqr.upload(sig.data(), sig.size(), s));
   RF_CUDA(ctx, p.d_xnlm.upload(xnlm.data(), xnlm.size(), s));
   {
@@ -560,6 +590,7 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   P.pos = p.d_pos.p; P.atom_pot = p.d_atom_pot.p; P.atom_off = p.d_atom_off.p; P.atom_lmax = p.d_atom_lmax.p;
   P.sigsqr = p.d_sigsqr.p; P.pair_dist = p.d_dist.p; P.pair_phi = p.d_phi.p; P.pair_dsmall = p.d_dsmall.p;
   P.xnlm = p.d_xnlm.p; P.xnlm_w = p.d_xnlm_w.p; P.t3p = p.d_t3p.p; P.t3m = p.d_t3m.p; P.pair_eph = p.d_eph.p;
+  P.bcol = p.d_bcol.p;
   P.pair_dsmall_df = p.d_dsmall_df.p; P.pair_eph_df = p.d_eph_df.p;
   P.xnlm_df = p.d_xnlm_df.p; P.xnlm_w_df = p.d_xnlm_w_df.p;
   P.rdirec2 = double(in->direct_cutoff) * double(in->direct_cutoff);
@@ -599,7 +630,7 @@ extern "C" int refeff_fms_plan_query(const refeff_fms_plan* plan, int* n_states,
   if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   if (n_states) *n_states = plan->n;
   if (channel_count) *channel_count = plan->C;
-  if (absorber_block) *absorber_block = plan->m;
+  if (absorber_block) *absorber_block = plan->m_abs;
   if (n_potentials) *n_potentials = plan->npot;
   return REFEFF_FMS_OK;
 }
@@ -902,7 +933,15 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     e = tick(1, [&] { return lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s); });
     if (e != cudaSuccess) return e;
     tick(4, [&] {
-      launch_absorber_solve<double>(lay, batch, ws.M64.p, ws.gg_stage.p, ws.status.p, s);
+      if (p.blocks.size() == 1) {
+        // the absorber alone: its block is the trailing m x m triangle solve
+        launch_absorber_solve<double>(lay, batch, ws.M64.p, ws.gg_stage.p, ws.status.p, s);
+      } else {
+        lu_backward_rhs<double>(ws.pc64, lay, batch, ws.M64.p, nullptr, s);
+        launch_copy_rhs64(lay, batch, ws.M64.p, ws.X64.p, s);
+        launch_extract_blocks(lay, batch, ws.X64.p, p.d_blocks.p, int(p.blocks.size()), p.gg_per, ws.gg_stage.p,
+                              ws.status.p, s);
+      }
       return cudaGetLastError();
     });
   } else if (form == REFEFF_FMS_FORM_BICGSTAB) {
@@ -926,7 +965,8 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     tick(4, [&] {
       count_launch();
       status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
-      launch_extract_absorber(lay, batch, ws.X64.p, ws.gg_stage.p, s);
+      launch_extract_blocks(lay, batch, ws.X64.p, p.d_blocks.p, int(p.blocks.size()), p.gg_per, ws.gg_stage.p,
+                            nullptr, s);
       return cudaGetLastError();
     });
   } else {
@@ -941,7 +981,8 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     tick(4, [&] {
       count_launch();
       status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
-      launch_extract_absorber(lay, batch, ws.X64.p, ws.gg_stage.p, s);
+      launch_extract_blocks(lay, batch, ws.X64.p, p.d_blocks.p, int(p.blocks.size()), p.gg_per, ws.gg_stage.p,
+                            nullptr, s);
       return cudaGetLastError();
     });
   }
@@ -1006,7 +1047,8 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
   const size_t xph = p.xph_per_energy();
   RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
-  RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.m * p.m));
+  RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.gg_per));
+  if (!fp32 && p.blocks.size() > 1) RF_CUDA(ctx, ws.X64.alloc(size_t(ws.batch) * ws.lay.lda * p.m));
   const bool refined = fp32 && p.minv == 0;  // refinement statistics and the FP64 fallback
   if (p.minv != 0) {
     RF_CUDA(ctx, ws.t_tab.alloc(size_t(ws.batch) * p.n * 2));
@@ -1069,7 +1111,7 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
       cudaError_t e = run_fms_batch(p, nb, form, s);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch");
     }
-    RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.m * p.m, ws.gg_stage.p, size_t(nb) * p.m * p.m * sizeof(double2),
+    RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.gg_per, ws.gg_stage.p, size_t(nb) * p.gg_per * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
     RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, s));
     if (refined) {
@@ -1128,8 +1170,8 @@ int solve_device_energies_finish(refeff_fms_plan& p, int E, const double2* d_k, 
     if (e != cudaSuccess) return cuda_fail(ctx, e, "fp64 fallback batch");
     for (int i = 0; i < nb; ++i) {
       const int en = redo[r0 + size_t(i)];
-      RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(en) * p.m * p.m, ws.gg_stage.p + size_t(i) * p.m * p.m,
-                                   size_t(p.m) * p.m * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+      RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(en) * p.gg_per, ws.gg_stage.p + size_t(i) * p.gg_per,
+                                   size_t(p.gg_per) * sizeof(double2), cudaMemcpyDeviceToDevice, s));
       RF_CUDA(ctx, cudaMemcpyAsync(d_status + en, ws.status.p + i, sizeof(int), cudaMemcpyDeviceToDevice, s));
     }
   }
@@ -1179,7 +1221,7 @@ int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, r
   const size_t xph = p.xph_per_energy();
   RF_CUDA(ctx, p.d_k_all.upload(reinterpret_cast<const double2*>(points->wave_numbers), size_t(E) * p.nsp, s));
   RF_CUDA(ctx, p.d_x_all.upload(reinterpret_cast<const double2*>(points->phase_shifts), size_t(E) * xph, s));
-  RF_CUDA(ctx, p.d_gg_all.alloc(size_t(E) * p.m * p.m));
+  RF_CUDA(ctx, p.d_gg_all.alloc(size_t(E) * p.gg_per));
   RF_CUDA(ctx, p.d_status_all.alloc(size_t(E)));
   return solve_device_energies_enqueue(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
 }
@@ -1193,7 +1235,7 @@ int spectrum_end(refeff_fms_plan& p, const refeff_fms_energy_points* points, ref
   const size_t C = size_t(p.C), tab = C * C * size_t(p.npot);
   int rc = solve_device_energies_finish(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
   if (rc) return rc;
-  std::vector<double2> gg(size_t(E) * p.m * p.m);
+  std::vector<double2> gg(size_t(E) * p.gg_per);
   std::vector<int> st(static_cast<size_t>(E));
   RF_CUDA(ctx, cudaMemcpyAsync(gg.data(), p.d_gg_all.p, gg.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), p.d_status_all.p, st.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1217,11 +1259,14 @@ int spectrum_end(refeff_fms_plan& p, const refeff_fms_energy_points* points, ref
     if (status_out) status_out[e] = code;
     if (code != REFEFF_FMS_OK && failed++ == 0) first_bad = e;
     refeff_complex128* outp = scattering_out + size_t(e) * tab;
-    for (int c = 0; c < p.m; ++c)
-      for (int r = 0; r < p.m; ++r) {
-        const double2 v = gg[size_t(e) * p.m * p.m + size_t(r) + size_t(p.m) * c];
-        outp[size_t(r) + C * (size_t(c) + C * size_t(p.abs_pot))] = {v.x, v.y};
-      }
+    for (size_t q = 0; q < p.blocks.size(); ++q) {
+      const SolvedBlock& bl = p.blocks[q];
+      for (int c = 0; c < bl.size; ++c)
+        for (int r = 0; r < bl.size; ++r) {
+          const double2 v = gg[size_t(e) * p.gg_per + size_t(bl.pack) + size_t(r) + size_t(bl.size) * c];
+          outp[size_t(r) + C * (size_t(c) + C * size_t(p.block_pot[q]))] = {v.x, v.y};
+        }
+    }
   }
   *failed_out = failed;
   if (failed)

@@ -44,6 +44,9 @@ struct PlanDev {
   const double* t3p = nullptr;       // spin-orbit coefficients [l + (L+1)*((m+L) + (2L+1)*(s-1))]
   const double* t3m = nullptr;
   double rdirec2 = 0.0;              // direct-cutoff radius squared (Angstrom^2)
+  // right-hand-side column of each device atom's states in B = G0[:, representatives]
+  // (the representative of each potential in the solved range), -1 for other atoms
+  const int* bcol = nullptr;         // [N]
 };
 
 // Per-batch matrix layout: [A | B] with A n x n and B n x m (column-major,

@@ -501,7 +501,8 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
 
   // ---- elements: rows fastest (coalesced column-major stores) ----
   const int dpd = P.ds / 2;
-  const bool absorber_col = (j == N - 1);
+  const int bcol_j = P.bcol ? P.bcol[j] : (j == N - 1 ? 0 : -1);
+  const bool absorber_col = bcol_j >= 0;  // the columns of a representative also form B
   const size_t base = size_t(e) * lay.stride;
   auto g0 = [&](int p, int l1, int m1, int s1, int l2, int m2, int s2) -> double2 {
     if (s1 != s2 || !flag[p]) return make_double2(0.0, 0.0);
@@ -568,7 +569,7 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
       reinterpret_cast<float4*>(M64)[ai] = a;
       M32[ai] = make_float2(a.x, a.y);
       if (absorber_col) {
-        const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + cc);
+        const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + bcol_j + cc);
         reinterpret_cast<float4*>(M64)[bi] = gcol;
         M32[bi] = make_float2(gcol.x, gcol.y);
       }
@@ -600,7 +601,7 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
       M64[ai] = a;
     }
     if (absorber_col) {
-      const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + cc);
+      const size_t bi = base + size_t(r) + size_t(lay.lda) * (size_t(lay.n) + bcol_j + cc);
       if (kMode == 1) {
         const float4 sb = split_hi_lo(gcol);
         reinterpret_cast<float4*>(M64)[bi] = sb;

@@ -121,6 +121,31 @@ def test_fms_small_cluster_fp64(ctx):
         assert rel_err(gpu[e], ref[e]) < TOL_FP64, e
 
 
+@pytest.mark.parametrize("form,tol", [(fms.FORM_FP64_LU, TOL_FP64), (fms.FORM_FP32_REFINED, 1e-6),
+                                      (fms.FORM_BICGSTAB, 1e-6)])
+def test_fms_all_potentials_lfms(ctx, form, tol):
+    """lfms != 0: every potential's representative block is solved (fms_lu_scattering over the whole potential
+    range, solvers.rs:434-471): a two-potential cluster with lmaxph [3, 2] (right-hand sides 16 + 9) and the
+    three-potential rocksalt cluster (16 + 16 + 16), against the FP64 oracle."""
+    cases = []
+    cl, grid = wl.small_cluster(3.0, lmax=3, n_energies=4, seed=17)
+    cl.lmaxph = np.array([3, 2], np.int32)
+    cases.append((cl, grid))
+    rs = wl.rocksalt_cluster(np.random.default_rng(5), radius=4.6)
+    cases.append((rs, wl.energy_grid(rs, 4, 10.0, 60.0, seed=5)))
+    for cl, grid in cases:
+        plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph, lfms=1)
+        gpu, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts, form)
+        assert (status == 0).all()
+        ref = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts,
+                              lfms=1, mode=po.F64, threads=po.threads_available())
+        npot = len(cl.lmaxph)
+        for e in range(gpu.shape[0]):
+            for q in range(npot):
+                assert np.abs(ref[e, :, :, q]).max() > 0, q
+                assert rel_err(gpu[e, :, :, q], ref[e, :, :, q]) < tol, (e, q)
+
+
 def test_fms_small_cluster_fp32_refined(ctx):
     cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=6)
     plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP32_REFINED)
