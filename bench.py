@@ -268,6 +268,16 @@ def ours(args, world, rank, local):
     gg32 = d_gg[1].cpu().numpy()
     gg64 = d_gg[0].cpu().numpy()
     rel = np.linalg.norm(gg32 - gg64, axis=1) / np.maximum(np.linalg.norm(gg64, axis=1), 1e-300)
+    # the MKGTR trace that FF2X turns into mu(E), for both forms: K edge (initial kappa -1), isotropic
+    # polarisation, dipole transition, seeded radial matrix elements rkk
+    L0 = int(round(np.sqrt(m))) - 1
+    bm, li, _ = fms.transition_matrix(lmax=L0, initial_kappa=-1, polarization=0, multipole=0, spin=0)
+    rkk = np.random.default_rng(7).normal(size=(E, 8, 1)) * (1.0 + 0.2j)
+    g32 = gg32.reshape(E, m, m).transpose(0, 2, 1)  # stored column-major per energy
+    g64 = gg64.reshape(E, m, m).transpose(0, 2, 1)
+    tr32 = fms.mkgtr_trace(ctx, g32, [bm], [li], rkk, active_spin_channels=1, lmax=L0)[0]
+    tr64 = fms.mkgtr_trace(ctx, g64, [bm], [li], rkk, active_spin_channels=1, lmax=L0)[0]
+    rel_gtr = float(np.max(np.abs(tr32 - tr64)) / max(np.max(np.abs(tr64)), 1e-300))
 
     value = world * E * args.steps / (ms_chosen / 1e3)
     plain_value = world * E * plain_steps / (ms_plain / 1e3)
@@ -379,6 +389,7 @@ def ours(args, world, rank, local):
                            "steps": plain_steps},
             "chosen_over_plain": value / plain_value,
             "max_rel_gg_err_vs_fp64": float(rel.max()),
+            "max_rel_gtr_err_vs_fp64": rel_gtr,
             "status_nonzero": int((st_chosen != 0).sum() + (st_plain != 0).sum()),
             "roofline": roofline,
             "cpu_baseline": cpu,
