@@ -155,6 +155,18 @@ typedef struct {
 int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* input,
                                       refeff_fms_plan** out);
 
+/* The same plan with the full scattering matrix requested
+ * (FmsRealSpacePlanInput::full_scattering_matrix_requested, set from fms.inp
+ * save_gg_slice at crates/refeff-engine/src/fms.rs:3610): every column of G0
+ * is a right-hand side, X = (I - G0 T)^-1 G0 (FmsLuResult::full_scattering,
+ * crates/refeff-core/src/fms/solvers.rs:473-479).  Like the reference, the
+ * request forces the LU form (fms_scattering_method_selection,
+ * driver.rs:72-96): minv is taken as 0 and only REFEFF_FMS_FORM_FP64_LU is
+ * accepted.  Every atom must carry b = nsp (L+1)^2 states (fixed-width atom
+ * blocks, fms.rs:4164-4172), else UNSUPPORTED. */
+int refeff_fms_real_space_plan_create_full(refeff_fms_context* ctx, const refeff_fms_plan_input* input,
+                                           refeff_fms_plan** out);
+
 /* The pair mean-square displacement table that feeds
  * refeff_fms_plan_input.mean_square_displacements, computed on the GPU.
  * Replaces fms_mean_square_displacements_with_metadata
@@ -238,6 +250,19 @@ int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refeff_fms_energ
                                    refeff_fms_form form, refeff_complex128* scattering_out, int32_t* status_out,
                                    refeff_fms_report* report);
 
+/* Spectrum of a full plan (refeff_fms_real_space_plan_create_full) with the
+ * FP64 LU: the scattering table as refeff_fms_real_space_spectrum, plus the
+ * two save_gg_slice outputs of build_saved_fms_scattering_outputs
+ * (crates/refeff-engine/src/fms.rs:4154-4216), reference state order:
+ *   slice_out: n_energies x (b x n) column-major, rows [0, b) (the absorber's
+ *              states) of X over every column;
+ *   diag_out:  n_energies x n_atoms x (b x b) column-major, the diagonal block
+ *              of every atom.
+ * Energies that failed hold zeros (status_out says which). */
+int refeff_fms_real_space_spectrum_full(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                        refeff_complex128* scattering_out, refeff_complex128* slice_out,
+                                        refeff_complex128* diag_out, int32_t* status_out, refeff_fms_report* report);
+
 /* Same solve for inputs already resident in device memory (same layouts as
  * above, device pointers); writes the solved blocks per energy: for lfms = 0
  * the absorber block, d_gg_out = n_energies x (m x m) complex128 (m from
@@ -283,8 +308,11 @@ int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_complex128* 
  * 3549-3695): reads fms.inp, global.inp, phase.bin, geom.dat and the optional
  * .dimensions.dat, solves every energy on the GPU, and writes gg.bin and
  * gg.dat (byte-compatible sectioned text, io/gg_dat.rs:174-233) and log3.dat
- * (fms.rs:5995-6058).  Supported: idwopt < 0 (uniform sig2g), save_gg_slice
- * off; anything else returns REFEFF_FMS_ERR_UNSUPPORTED. */
+ * (fms.rs:5995-6058).  With save_gg_slice on, the full scattering matrix is
+ * solved with the FP64 LU whatever `form` asks (the reference forces the LU
+ * form) and gg_slice.bin and gg_diag.bin are written too (fms.rs:1113-1125).
+ * Supported: idwopt < 0 (uniform sig2g), 0 and 3 (Debye models); other idwopt
+ * values return REFEFF_FMS_ERR_UNSUPPORTED. */
 int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir, refeff_fms_form form, refeff_fms_report* report);
 
 /* gg.dat / gg.bin writer (gg_dat_bytes, crates/refeff-io/src/gg_dat.rs:174-202):
@@ -292,6 +320,15 @@ int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir, refeff_fms
  * 1..n, every value as Fortran E20.10 (crates/refeff-io/src/format.rs:174-209).
  * Host only; needs no GPU. */
 int refeff_fms_write_gg_dat(const char* path, int n_sections, int dim, const refeff_complex128* values);
+
+/* gg_slice.bin / gg_diag.bin writers (rhorrp_gg_slice_bin_bytes,
+ * rhorrp_gg_diag_bin_bytes, crates/refeff-io/src/rhorrp_gg_bin.rs:138-160,
+ * 228-252): Fortran sequential records, little-endian, values narrowed to
+ * complex f32.  slice: ne blocks of rows x cols; diag: ne x n_atoms blocks of
+ * dim x dim; column-major.  NONFINITE_INPUT when a narrowed value is not
+ * finite.  Host only. */
+int refeff_fms_write_gg_slice_bin(const char* path, int ne, int rows, int cols, const refeff_complex128* values);
+int refeff_fms_write_gg_diag_bin(const char* path, int ne, int n_atoms, int dim, const refeff_complex128* values);
 
 /* phase.bin reader (crates/refeff-io/src/phase_bin/parse.rs:18-130, PAD
  * decoding crates/refeff-io/src/pad.rs:102-127).  Host only.

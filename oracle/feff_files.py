@@ -14,6 +14,8 @@ FEFF work directories and check the product's gg.bin / gg.dat byte for byte.
   geom.dat text       crates/refeff-io/src/structure_output.rs:204-223
   fms.bin text        crates/refeff-io/src/fms_bin.rs:77-98
   gtr.dat text        crates/refeff-io/src/gtr_dat.rs:60-71
+  gg_slice.bin        crates/refeff-io/src/rhorrp_gg_bin.rs:99-160
+  gg_diag.bin         crates/refeff-io/src/rhorrp_gg_bin.rs:178-252
 """
 from __future__ import annotations
 
@@ -163,6 +165,57 @@ def parse_gg_dat(text: str):
             if len(cur) == dim:
                 sections.append(np.array(cur))
     return sections
+
+
+def _record(payload: bytes) -> bytes:
+    """One Fortran sequential unformatted record: u32 length, payload, u32 length (little-endian)."""
+    n = len(payload).to_bytes(4, "little")
+    return n + payload + n
+
+
+def gg_slice_bin_bytes(values) -> bytes:
+    """gg_slice.bin from (energy, row, column) complex values (rhorrp_gg_slice_bin_bytes, rhorrp_gg_bin.rs:138-160):
+    header (ldim, istate, ne) as i32, then complex64 in energy / column / row order."""
+    v = np.asarray(values, dtype=np.complex64)
+    ne, rows, cols = v.shape
+    header = np.array([rows, cols, ne], dtype="<i4").tobytes()
+    return _record(header) + _record(v.transpose(0, 2, 1).astype("<c8").tobytes())
+
+
+def gg_diag_bin_bytes(values) -> bytes:
+    """gg_diag.bin from (energy, atom, row, column) values (rhorrp_gg_diag_bin_bytes, rhorrp_gg_bin.rs:228-252):
+    header (ldim, ldim, inclus, ne) as i32, then complex64 in energy / atom / column / row order."""
+    v = np.asarray(values, dtype=np.complex64)
+    ne, na, dim, _ = v.shape
+    header = np.array([dim, dim, na, ne], dtype="<i4").tobytes()
+    return _record(header) + _record(v.transpose(0, 1, 3, 2).astype("<c8").tobytes())
+
+
+def _records(data: bytes):
+    out, pos = [], 0
+    while pos < len(data):
+        n = int.from_bytes(data[pos:pos + 4], "little")
+        out.append(data[pos + 4:pos + 4 + n])
+        if data[pos + 4 + n:pos + 8 + n] != data[pos:pos + 4]:
+            raise ValueError("record markers differ")
+        pos += 8 + n
+    return out
+
+
+def parse_gg_slice_bin(data: bytes):
+    """(energy, row, column) complex64 array from gg_slice.bin bytes (parse_rhorrp_gg_slice_bin, :99-136)."""
+    header, payload = _records(data)
+    rows, cols, ne = np.frombuffer(header, dtype="<i4")
+    return np.frombuffer(payload, dtype="<c8").reshape(ne, cols, rows).transpose(0, 2, 1)
+
+
+def parse_gg_diag_bin(data: bytes):
+    """(energy, atom, row, column) complex64 array from gg_diag.bin bytes (parse_rhorrp_gg_diag_bin, :178-226)."""
+    header, payload = _records(data)
+    dim, dim2, na, ne = np.frombuffer(header, dtype="<i4")
+    if dim != dim2:
+        raise ValueError("gg_diag ldim values differ")
+    return np.frombuffer(payload, dtype="<c8").reshape(ne, na, dim, dim).transpose(0, 1, 3, 2)
 
 
 def phase_bin_text(*, nsp, energy_grid, reference_energy, potentials, pad_width=8, transition_count=8,

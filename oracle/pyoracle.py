@@ -188,6 +188,40 @@ def fms_spectrum_iterative(positions, pots, lmaxph, wave_numbers, xphase, *, min
     return res if raise_on_error else (res, status)
 
 
+def full_scattering(positions, pots, lmaxph, wave_numbers, xphase, *, nsp=1, ispin=0, global_lmax=None,
+                    rdirec=1.0e6, sigsqr=None, sig2g=0.0, mode=F64):
+    """Oracle save_gg_slice outputs for every energy: the full matrix X = (I - G0 T)^-1 G0 (FmsLuResult's
+    full_scattering, crates/refeff-core/src/fms/solvers.rs:473-479, solved with the oracle LU) reduced like
+    build_saved_fms_scattering_outputs (crates/refeff-engine/src/fms.rs:4154-4216): slice (E, b, n) = rows [0, b)
+    of X over every column, diag (E, N, b, b) = the diagonal block of each atom; b = nsp (L+1)^2, and every atom
+    must carry b states (fixed-width atom blocks)."""
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    pots = np.ascontiguousarray(pots, dtype=np.int32)
+    lmaxph = np.ascontiguousarray(lmaxph, dtype=np.int32)
+    npot, N = len(lmaxph), len(pots)
+    L = int(lmaxph.max()) if global_lmax is None else int(global_lmax)
+    b = nsp * (L + 1) ** 2
+    sig = None if sigsqr is None else np.asfortranarray(sigsqr, dtype=np.float32)
+    args = [mode, N, ptr(positions), ptr(pots), nsp, ispin, 0, npot - 1, L, ptr(lmaxph), float(rdirec), ptr(sig),
+            float(sig2g)]
+    slices, diags = [], []
+    for e in range(np.asarray(wave_numbers).shape[0]):
+        kb = cbuf(np.asarray(wave_numbers[e]).reshape(nsp))
+        xb = cbuf(np.asarray(xphase[e]).reshape(nsp, 2 * L + 1, npot))
+        n = np.zeros(1, np.int32)
+        check(lib().oracle_fms_energy_intermediates(*args, ptr(kb), ptr(xb), 0.0, ptr(n), None, None, None, None))
+        ns = int(n[0])
+        if ns != N * b:
+            raise ValueError(f"save_gg_slice requires fixed-width atom blocks: {ns} states for {N} atoms of {b}")
+        g0, t, a = np.zeros(2 * ns * ns), np.zeros(2 * nsp * ns), np.zeros(2 * ns * ns)
+        check(lib().oracle_fms_energy_intermediates(*args, ptr(kb), ptr(xb), 0.0, ptr(n), ptr(g0), ptr(t), ptr(a),
+                                                    None))
+        _, X, _ = lu_factor_solve(from_cbuf(a, (ns, ns)), from_cbuf(g0, (ns, ns)), mode=mode)
+        slices.append(X[:b, :].copy())
+        diags.append(np.stack([X[i * b:(i + 1) * b, i * b:(i + 1) * b] for i in range(N)]))
+    return np.array(slices), np.array(diags)
+
+
 def lu_factor_solve(A, B, mode=F64):
     A = np.asarray(A, dtype=np.complex128)
     B = np.asarray(B, dtype=np.complex128)

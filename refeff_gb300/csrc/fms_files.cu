@@ -104,6 +104,43 @@ std::string gg_dat_text(int n_sections, int dim, const refeff_complex128* values
   return out;
 }
 
+// gg_slice.bin / gg_diag.bin (crates/refeff-io/src/rhorrp_gg_bin.rs:138-160,
+// 228-252): Fortran sequential unformatted records, each a 4-byte
+// little-endian length, the payload and the length again; a header record of
+// 32-bit dimensions, then one record of default-kind complex values (two
+// little-endian f32 each) in FEFF's column-major order.  The values are the
+// reference's Complex32 data: each part narrowed to f32, and a part that is
+// not finite after narrowing is an error (validate_complex_values, :562-572).
+void put_u32_le(std::string& out, uint32_t v) {
+  for (int i = 0; i < 4; ++i) out.push_back(char((v >> (8 * i)) & 0xffu));
+}
+
+void put_record(std::string& out, const std::string& payload) {
+  put_u32_le(out, uint32_t(payload.size()));
+  out += payload;
+  put_u32_le(out, uint32_t(payload.size()));
+}
+
+// header dims, then count complex values (already in file order); false on a non-finite value
+bool rhorrp_bin(const std::vector<int>& dims, size_t count, const refeff_complex128* values, std::string& out) {
+  std::string header, payload;
+  for (int d : dims) put_u32_le(header, uint32_t(d));
+  payload.reserve(count * 8);
+  for (size_t i = 0; i < count; ++i) {
+    const float part[2] = {float(values[i].re), float(values[i].im)};
+    for (float f : part) {
+      if (!std::isfinite(f)) return false;
+      uint32_t bits;
+      std::memcpy(&bits, &f, sizeof bits);
+      put_u32_le(payload, bits);
+    }
+  }
+  out.clear();
+  put_record(out, header);
+  put_record(out, payload);
+  return true;
+}
+
 bool write_file_atomic(const std::string& path, const std::string& bytes) {
   const std::string tmp = path + ".tmp";
   {
@@ -331,6 +368,23 @@ extern "C" int refeff_fms_write_gg_dat(const char* path, int n_sections, int dim
   return write_file_atomic(path, gg_dat_text(n_sections, dim, values)) ? REFEFF_FMS_OK : REFEFF_FMS_ERR_INVALID_ARGUMENT;
 }
 
+extern "C" int refeff_fms_write_gg_slice_bin(const char* path, int ne, int rows, int cols,
+                                             const refeff_complex128* values) {
+  if (!path || ne <= 0 || rows <= 0 || cols <= 0 || !values) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  std::string out;
+  if (!rhorrp_bin({rows, cols, ne}, size_t(ne) * rows * cols, values, out)) return REFEFF_FMS_ERR_NONFINITE_INPUT;
+  return write_file_atomic(path, out) ? REFEFF_FMS_OK : REFEFF_FMS_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int refeff_fms_write_gg_diag_bin(const char* path, int ne, int n_atoms, int dim,
+                                            const refeff_complex128* values) {
+  if (!path || ne <= 0 || n_atoms <= 0 || dim <= 0 || !values) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  std::string out;
+  if (!rhorrp_bin({dim, dim, n_atoms, ne}, size_t(ne) * n_atoms * dim * dim, values, out))
+    return REFEFF_FMS_ERR_NONFINITE_INPUT;
+  return write_file_atomic(path, out) ? REFEFF_FMS_OK : REFEFF_FMS_ERR_INVALID_ARGUMENT;
+}
+
 extern "C" int refeff_fms_phase_bin_dims(const char* path, int* nsp, int* ne, int* npot, int* lmax_max) {
   if (!path) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   PhaseBin pb;
@@ -533,10 +587,6 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
     set_error(ctx, "only idwopt < 0 (uniform sig2g), 0 (correlated Debye) and 3 (classical Debye) are supported");
     return REFEFF_FMS_ERR_UNSUPPORTED;
   }
-  if (fi.save_gg_slice) {
-    set_error(ctx, "save_gg_slice is not supported");
-    return REFEFF_FMS_ERR_UNSUPPORTED;
-  }
   // effective radii (fms.rs:4260-4284)
   const float rfms2 = fi.rfms2 >= 0.0 ? float(fi.rfms2) : 0.0f;
   const float rdirec = fi.rdirec >= 0.0 ? float(fi.rdirec) : 0.0f;
@@ -592,8 +642,11 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   in.sig2g = float(fi.sig2g);
   in.convergence_tolerance = float(fi.toler1);
   in.zero_tolerance = float(fi.toler2);
+  // save_gg_slice asks for the full scattering matrix, which forces the LU form
+  // (full_scattering_matrix_requested, fms.rs:3610; driver.rs:72-96)
   refeff_fms_plan* plan = nullptr;
-  rc = refeff_fms_real_space_plan_create(ctx, &in, &plan);
+  rc = fi.save_gg_slice ? refeff_fms_real_space_plan_create_full(ctx, &in, &plan)
+                        : refeff_fms_real_space_plan_create(ctx, &in, &plan);
   if (rc) return rc;
   int n = 0, C = 0, m = 0, npot = 0;
   refeff_fms_plan_query(plan, &n, &C, &m, &npot);
@@ -620,7 +673,14 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   std::vector<refeff_complex128> scat(size_t(E) * C * C * npot);
   std::vector<int32_t> status(static_cast<size_t>(E));
   refeff_fms_energy_points pts{E, k.data(), xph.data()};
-  rc = refeff_fms_real_space_spectrum(plan, &pts, form, scat.data(), status.data(), report);
+  std::vector<refeff_complex128> slice, diag;
+  if (fi.save_gg_slice) {
+    slice.resize(size_t(E) * C * n);
+    diag.resize(size_t(E) * natoms * C * C);
+    rc = refeff_fms_real_space_spectrum_full(plan, &pts, scat.data(), slice.data(), diag.data(), status.data(), report);
+  } else {
+    rc = refeff_fms_real_space_spectrum(plan, &pts, form, scat.data(), status.data(), report);
+  }
   if (rc) {
     refeff_fms_real_space_plan_destroy(plan);
     return rc;
@@ -652,6 +712,26 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   if (!write_file_atomic(dir + "gg.bin", gg) || !write_file_atomic(dir + "gg.dat", gg)) {
     set_error(ctx, "cannot write gg.bin / gg.dat");
     return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  // gg_slice.bin and gg_diag.bin (generate_gg_outputs_from_source_handoffs, fms.rs:1102-1127)
+  if (fi.save_gg_slice) {
+    std::string bytes;
+    if (!rhorrp_bin({C, n, E}, slice.size(), slice.data(), bytes)) {
+      set_error(ctx, "gg_slice value is not finite");
+      return REFEFF_FMS_ERR_NONFINITE_INPUT;
+    }
+    if (!write_file_atomic(dir + "gg_slice.bin", bytes)) {
+      set_error(ctx, "cannot write gg_slice.bin");
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+    if (!rhorrp_bin({C, C, natoms, E}, diag.size(), diag.data(), bytes)) {
+      set_error(ctx, "gg_diag value is not finite");
+      return REFEFF_FMS_ERR_NONFINITE_INPUT;
+    }
+    if (!write_file_atomic(dir + "gg_diag.bin", bytes)) {
+      set_error(ctx, "cannot write gg_diag.bin");
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
   }
   // log3.dat (fms.rs:5995-6058)
   std::string log = "FMS calculation of full Green's function ...\nFEFF-serial using 1 thread.\n";

@@ -344,6 +344,7 @@ struct Workspace {
   MlpScratch mlp;
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
+  DevBuf<double2> full_stage;  // save_gg_slice outputs of a batch (full plans)
   std::map<int, cudaGraphExec_t> graphs;  // key: form * 65536 + energies in the batch
   std::map<int, unsigned long long> graph_launches;  // kernel launches per replay
   void drop_graphs() {
@@ -362,6 +363,11 @@ struct refeff_fms_plan {
   int m_abs = 0, gg_per = 0;
   std::vector<SolvedBlock> blocks;   // per potential of the range, in potential order
   std::vector<int> block_pot;        // the potential of each block
+  // full scattering (save_gg_slice): B = G0 entirely (m = n), and per energy the
+  // b x n slice of the absorber's rows plus every atom's b x b diagonal block
+  bool full = false;
+  int full_per = 0;
+  DevBuf<double2> d_full_all;
   DevBuf<SolvedBlock> d_blocks;
   DevBuf<int> d_bcol;
   std::vector<int> pot_lmax;
@@ -405,8 +411,9 @@ struct refeff_fms_plan {
   size_t xph_per_energy() const { return size_t(nsp) * size_t(2 * L + 1) * size_t(npot); }
 };
 
-extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* in,
-                                                 refeff_fms_plan** out) {
+namespace {
+
+int plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* in, bool full, refeff_fms_plan** out) {
   if (!ctx || !in || !out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   ctx->last_error.clear();
@@ -433,7 +440,9 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   p.ispin = in->spin_selector;
   p.npot = in->max_potential + 1;
   p.lfms = in->lfms;
-  p.minv = in->minv;
+  // a full scattering matrix forces the LU form (fms_scattering_method_selection, driver.rs:72-96)
+  p.minv = full ? 0 : in->minv;
+  p.full = full;
   p.toler1 = double(in->convergence_tolerance);
   p.toler2 = double(in->zero_tolerance);
   const int N = p.N, L = p.L, nsp = p.nsp;
@@ -470,6 +479,11 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   for (int q = pstart; q <= pend; ++q)
     if (p.rep_offsets[size_t(q)] < 0)
       return fail(ctx, REFEFF_FMS_ERR_MISSING_REPRESENTATIVE, "no atom for potential " + std::to_string(q));
+  if (full && p.n != N * p.C)
+    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED,
+                "save_gg_slice requires fixed-width atom blocks: got " + std::to_string(p.n) + " state(s), expected " +
+                    std::to_string(N * p.C) + " from " + std::to_string(N) + " atom(s) and block dimension " +
+                    std::to_string(p.C));
   if (p.lfms != 0 && p.minv != 0)
     return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "lfms != 0 with the iterative forms (minv != 0) is not supported");
   if (N < 2) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "a single-atom cluster has no scattering");
@@ -487,8 +501,11 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   for (int d = 0; d < N; ++d) doff[size_t(d) + 1] = doff[size_t(d)] + nsp * (dlmax[size_t(d)] + 1) * (dlmax[size_t(d)] + 1);
   // solved blocks (fms_lu_scattering, solvers.rs:366-484): for each potential of the range, the
   // representative's states (its first atom in cluster order) are right-hand sides, and its block
-  // of the solution is the scattering table entry of that potential
+  // of the solution is the scattering table entry of that potential.  A full plan solves for
+  // every column of G0 (solvers.rs:473-479), so B = G0 and each block sits at its own columns.
   std::vector<int> bcol(static_cast<size_t>(N), -1);
+  if (full)
+    for (int d = 0; d < N; ++d) bcol[size_t(d)] = doff[size_t(d)];
   {
     int col = 0, pack = 0;
     for (int q = pstart; q <= pend; ++q) {
@@ -496,16 +513,18 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
       while (atom_pot[size_t(a)] != q) ++a;
       const int d = dev(a);
       const int size = doff[size_t(d) + 1] - doff[size_t(d)];
-      bcol[size_t(d)] = col;
-      p.blocks.push_back({doff[size_t(d)], col, size, pack});
+      if (!full) bcol[size_t(d)] = col;
+      p.blocks.push_back({doff[size_t(d)], full ? doff[size_t(d)] : col, size, pack});
       p.block_pot.push_back(q);
       col += size;
       pack += size * size;
     }
-    p.m = col;
+    p.m = full ? p.n : col;
     p.gg_per = pack;
+    p.full_per = full ? p.C * p.n + N * p.C * p.C : 0;
   }
-  if (p.m > 64) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "more than 64 right-hand sides in the potential range");
+  if (!full && p.m > 64)
+    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "more than 64 right-hand sides in the potential range");
   // sigma^2 table, device order [a2 + N a1] (engine/fms.rs:4394-4426)
   std::vector<double> sig(static_cast<size_t>(N) * N, 0.0);
   for (int a1 = 0; a1 < N; ++a1)
@@ -601,6 +620,18 @@ extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const 
   context_retain(ctx);
   *out = plan.release();
   return REFEFF_FMS_OK;
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_real_space_plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* in,
+                                                 refeff_fms_plan** out) {
+  return plan_create(ctx, in, false, out);
+}
+
+extern "C" int refeff_fms_real_space_plan_create_full(refeff_fms_context* ctx, const refeff_fms_plan_input* in,
+                                                      refeff_fms_plan** out) {
+  return plan_create(ctx, in, true, out);
 }
 
 extern "C" void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan) {
@@ -881,6 +912,37 @@ cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, int iters
   return cudaGetLastError();
 }
 
+// save_gg_slice outputs of one batch (build_saved_fms_scattering_outputs,
+// engine/fms.rs:4154-4216) from X = (I - G0 T)^-1 G0, in reference state order:
+// reference atom a is device atom a - 1 and the absorber (a = 0) device atom
+// N - 1; every atom carries b states.  Per energy: rows [0, b) of X over every
+// column (b x n, column-major), then the b x b diagonal block of each atom
+// (column-major); zeros for energies that failed.
+__global__ void extract_full_kernel(BatchLayout lay, int N, int b, const double2* __restrict__ X64, int per,
+                                    double2* __restrict__ out, const int* status) {
+  const int e = blockIdx.y;
+  const bool bad = status[e] != kDevOk;
+  const int n = lay.n;
+  const size_t xb = size_t(e) * lay.lda * lay.m;
+  auto dstate = [N, b](int st) {
+    const int a = st / b;
+    return (a == 0 ? N - 1 : a - 1) * b + (st - a * b);
+  };
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < per; idx += gridDim.x * blockDim.x) {
+    int r, c;
+    if (idx < b * n) {
+      r = idx % b;
+      c = idx / b;
+    } else {
+      const int j = idx - b * n, a = j / (b * b), q = j - a * b * b;
+      r = a * b + q % b;
+      c = a * b + q / b;
+    }
+    out[size_t(e) * per + idx] =
+        bad ? make_double2(0.0, 0.0) : X64[xb + size_t(dstate(r)) + size_t(lay.lda) * size_t(dstate(c))];
+  }
+}
+
 __global__ void status_not_converged_kernel(int batch, const int* converged, int* status) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < batch && converged[b] != 1 && status[b] == kDevOk) status[b] = kDevNotConverged;
@@ -933,7 +995,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     e = tick(1, [&] { return lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s); });
     if (e != cudaSuccess) return e;
     tick(4, [&] {
-      if (p.blocks.size() == 1) {
+      if (p.blocks.size() == 1 && !p.full) {
         // the absorber alone: its block is the trailing m x m triangle solve
         launch_absorber_solve<double>(lay, batch, ws.M64.p, ws.gg_stage.p, ws.status.p, s);
       } else {
@@ -941,6 +1003,11 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
         launch_copy_rhs64(lay, batch, ws.M64.p, ws.X64.p, s);
         launch_extract_blocks(lay, batch, ws.X64.p, p.d_blocks.p, int(p.blocks.size()), p.gg_per, ws.gg_stage.p,
                               ws.status.p, s);
+        if (p.full) {
+          dim3 grid(unsigned(std::min(256, (p.full_per + 255) / 256)), unsigned(batch));
+          count_launch();
+          extract_full_kernel<<<grid, 256, 0, s>>>(lay, p.N, p.C, ws.X64.p, p.full_per, ws.full_stage.p, ws.status.p);
+        }
       }
       return cudaGetLastError();
     });
@@ -1020,7 +1087,8 @@ int pick_batch(refeff_fms_plan& p, int E, bool fp32) {
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   const BatchLayout lay = make_layout(p.n, p.m);
-  const size_t per = bytes_per_system(lay, fp32);
+  size_t per = bytes_per_system(lay, fp32);
+  if (p.full) per += (size_t(lay.lda) * p.m + size_t(p.full_per)) * sizeof(double2);
   const size_t budget = size_t(double(free_b) * 0.5);
   int b = int(std::max<size_t>(1, budget / std::max<size_t>(per, 1)));
   b = std::min(b, 256);
@@ -1029,6 +1097,7 @@ int pick_batch(refeff_fms_plan& p, int E, bool fp32) {
 
 // FP64_LU and FP32_REFINED serve every plan; BICGSTAB the LU-form plans (minv = 0).
 bool form_valid(const refeff_fms_plan& p, refeff_fms_form form) {
+  if (p.full) return form == REFEFF_FMS_FORM_FP64_LU;  // the full matrix is solved by the LU form only
   return form == REFEFF_FMS_FORM_FP64_LU || form == REFEFF_FMS_FORM_FP32_REFINED ||
          (form == REFEFF_FMS_FORM_BICGSTAB && p.minv == 0);
 }
@@ -1048,7 +1117,11 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
   RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
   RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.gg_per));
-  if (!fp32 && p.blocks.size() > 1) RF_CUDA(ctx, ws.X64.alloc(size_t(ws.batch) * ws.lay.lda * p.m));
+  if (!fp32 && (p.blocks.size() > 1 || p.full)) RF_CUDA(ctx, ws.X64.alloc(size_t(ws.batch) * ws.lay.lda * p.m));
+  if (p.full) {
+    RF_CUDA(ctx, ws.full_stage.alloc(size_t(ws.batch) * p.full_per));
+    RF_CUDA(ctx, p.d_full_all.alloc(size_t(E) * p.full_per));
+  }
   const bool refined = fp32 && p.minv == 0;  // refinement statistics and the FP64 fallback
   if (p.minv != 0) {
     RF_CUDA(ctx, ws.t_tab.alloc(size_t(ws.batch) * p.n * 2));
@@ -1114,6 +1187,9 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.gg_per, ws.gg_stage.p, size_t(nb) * p.gg_per * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, s));
     RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    if (p.full)
+      RF_CUDA(ctx, cudaMemcpyAsync(p.d_full_all.p + size_t(e0) * p.full_per, ws.full_stage.p,
+                                   size_t(nb) * p.full_per * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     if (refined) {
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_relres_all.p + e0, ws.relres.p, size_t(nb) * sizeof(double),
                                    cudaMemcpyDeviceToDevice, s));
@@ -1306,6 +1382,36 @@ extern "C" int refeff_fms_real_space_spectrum(refeff_fms_plan* plan, const refef
   int failed = 0;
   rc = spectrum_end(*plan, points, form, scattering_out, status_out, &failed, ctx->stream);
   fill_report(report, {plan}, form, failed, t0);
+  return rc;
+}
+
+extern "C" int refeff_fms_real_space_spectrum_full(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
+                                                   refeff_complex128* scattering_out, refeff_complex128* slice_out,
+                                                   refeff_complex128* diag_out, int32_t* status_out,
+                                                   refeff_fms_report* report) {
+  if (!plan || !points || !scattering_out || !slice_out || !diag_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  refeff_fms_context* ctx = plan->ctx;
+  ctx->last_error.clear();
+  if (!plan->full)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "the plan was not created for the full scattering matrix");
+  const auto t0 = std::chrono::steady_clock::now();
+  const refeff_fms_form form = REFEFF_FMS_FORM_FP64_LU;
+  int rc = spectrum_begin(*plan, points, form, scattering_out, ctx->stream);
+  if (rc) return rc;
+  int failed = 0;
+  rc = spectrum_end(*plan, points, form, scattering_out, status_out, &failed, ctx->stream);
+  fill_report(report, {plan}, form, failed, t0);
+  if (rc && !failed) return rc;
+  const int E = points->n_energies;
+  if (E > 0) {
+    // per energy the device holds [slice b x n | diag N x b x b]: split into the two outputs
+    const size_t b = size_t(plan->C), sl = b * size_t(plan->n), dg = size_t(plan->full_per) - sl;
+    const size_t pitch = size_t(plan->full_per) * sizeof(double2);
+    RF_CUDA(ctx, cudaMemcpy2D(slice_out, sl * sizeof(double2), plan->d_full_all.p, pitch, sl * sizeof(double2),
+                              size_t(E), cudaMemcpyDeviceToHost));
+    RF_CUDA(ctx, cudaMemcpy2D(diag_out, dg * sizeof(double2), plan->d_full_all.p + sl, pitch, dg * sizeof(double2),
+                              size_t(E), cudaMemcpyDeviceToHost));
+  }
   return rc;
 }
 

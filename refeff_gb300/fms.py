@@ -97,6 +97,10 @@ def load(build_if_missing: bool = True):
         "refeff_fms_last_error": ([_p], C.c_char_p),
         "refeff_fms_yprep_cluster": ([_i, _i, _i, _p, _p, C.c_float, _i, _p, _p, _p], _i),
         "refeff_fms_real_space_plan_create": ([_p, _p, _p], _i),
+        "refeff_fms_real_space_plan_create_full": ([_p, _p, _p], _i),
+        "refeff_fms_real_space_spectrum_full": ([_p, _p, _p, _p, _p, _p, _p], _i),
+        "refeff_fms_write_gg_slice_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
+        "refeff_fms_write_gg_diag_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
         "refeff_fms_real_space_plan_destroy": ([_p], None),
         "refeff_fms_plan_query": ([_p, _p, _p, _p, _p], _i),
         "refeff_fms_plan_set_batch": ([_p, _i], _i),
@@ -369,7 +373,13 @@ class PrecondModel:
 
 def fms_real_space_plan(ctx: Context, positions, potentials, raw_potential_lmax, *, spin_channels=1, spin_selector=0,
                         lfms=0, minv=0, global_lmax=None, direct_cutoff=1.0e6, mean_square_displacements=None,
-                        sig2g=0.0, convergence_tolerance=1.0e-3, zero_tolerance=0.0) -> FmsRealSpacePlan:
+                        sig2g=0.0, convergence_tolerance=1.0e-3, zero_tolerance=0.0,
+                        full_scattering=False) -> FmsRealSpacePlan:
+    """Energy-independent plan (fms_real_space_plan, crates/refeff-core/src/fms/driver.rs:105-140).
+
+    full_scattering: request the full matrix (I - G0 T)^-1 G0 (fms.inp save_gg_slice), which forces the LU form;
+    solve such a plan with fms_full_scattering_spectrum.
+    """
     pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
     pots = np.ascontiguousarray(potentials, dtype=np.int32)
     lmax = np.ascontiguousarray(raw_potential_lmax, dtype=np.int32)
@@ -379,9 +389,45 @@ def fms_real_space_plan(ctx: Context, positions, potentials, raw_potential_lmax,
                      len(lmax) - 1, L, _ptr(lmax), float(direct_cutoff), _ptr(msd), float(sig2g),
                      float(convergence_tolerance), float(zero_tolerance))
     h = _p()
-    ctx.check(ctx._lib.refeff_fms_real_space_plan_create(ctx.handle, C.byref(inp), C.byref(h)))
+    create = ctx._lib.refeff_fms_real_space_plan_create_full if full_scattering else \
+        ctx._lib.refeff_fms_real_space_plan_create
+    ctx.check(create(ctx.handle, C.byref(inp), C.byref(h)))
     return FmsRealSpacePlan(ctx, h, dict(positions=pos, potentials=pots, lmaxph=lmax, nsp=int(spin_channels),
                                           L=L, npot=len(lmax)))
+
+
+def _energy_inputs(plan: FmsRealSpacePlan, wave_numbers, phase_shifts):
+    nsp, L, npot = plan.inputs["nsp"], plan.inputs["L"], plan.inputs["npot"]
+    k = np.ascontiguousarray(np.asarray(wave_numbers, dtype=np.complex128).reshape(-1, nsp))
+    E = k.shape[0]
+    ph = np.asarray(phase_shifts, dtype=np.complex128).reshape(E, nsp, 2 * L + 1, npot)
+    xp = np.ascontiguousarray(np.stack([ph[e].reshape(-1, order="F") for e in range(E)])) if E else \
+        np.zeros((0,), np.complex128)
+    return k, xp, E
+
+
+def fms_full_scattering_spectrum(plan: FmsRealSpacePlan, wave_numbers, phase_shifts):
+    """Spectrum of a full-scattering plan with the FP64 LU: (tables (E, C, C, npot), slice (E, b, n),
+    diag (E, N, b, b), status (E,)), b = nsp (L+1)^2; slice and diag are the save_gg_slice outputs of
+    build_saved_fms_scattering_outputs (crates/refeff-engine/src/fms.rs:4154-4216), reference state order."""
+    npot = plan.inputs["npot"]
+    k, xp, E = _energy_inputs(plan, wave_numbers, phase_shifts)
+    Cc, n, N = plan.shape.channel_count, plan.shape.n_states, len(plan.inputs["potentials"])
+    out = np.zeros(E * Cc * Cc * npot, dtype=np.complex128)
+    sl = np.zeros(E * Cc * n, dtype=np.complex128)
+    dg = np.zeros(E * N * Cc * Cc, dtype=np.complex128)
+    status = np.zeros(E, dtype=np.int32)
+    pts = _EnergyPoints(E, _ptr(k), _ptr(xp))
+    rc = plan.ctx._lib.refeff_fms_real_space_spectrum_full(plan.handle, C.byref(pts), _ptr(out), _ptr(sl), _ptr(dg),
+                                                           _ptr(status), None)
+    if rc:
+        raise FmsError(rc, plan.ctx.last_error())
+    tabs = out.reshape(E, Cc * Cc * npot)
+    scat = np.stack([tabs[e].reshape((Cc, Cc, npot), order="F") for e in range(E)]) if E else \
+        np.zeros((0, Cc, Cc, npot), np.complex128)
+    slice_ = sl.reshape(E, n, Cc).transpose(0, 2, 1)
+    diag = dg.reshape(E, N, Cc, Cc).transpose(0, 1, 3, 2)
+    return scat, slice_, diag, status
 
 
 def fms_real_space_spectrum(plan: FmsRealSpacePlan, wave_numbers, phase_shifts, form=FORM_FP64_LU,
@@ -479,6 +525,28 @@ def write_gg_dat(path, sections) -> None:
     flat = np.ascontiguousarray(np.stack([sec[i].reshape(-1, order="F") for i in range(n)])) if n else \
         np.zeros(0, np.complex128)
     rc = lib.refeff_fms_write_gg_dat(str(path).encode(), n, dim, _ptr(flat))
+    if rc:
+        raise FmsError(rc, f"cannot write {path}")
+
+
+def write_gg_slice_bin(path, values) -> None:
+    """FEFF gg_slice.bin from (ne, rows, cols) complex values (crates/refeff-io/src/rhorrp_gg_bin.rs:138-160)."""
+    lib = load()
+    v = np.asarray(values, dtype=np.complex128)
+    ne, rows, cols = v.shape
+    flat = np.ascontiguousarray(v.transpose(0, 2, 1))
+    rc = lib.refeff_fms_write_gg_slice_bin(str(path).encode(), ne, rows, cols, _ptr(flat))
+    if rc:
+        raise FmsError(rc, f"cannot write {path}")
+
+
+def write_gg_diag_bin(path, values) -> None:
+    """FEFF gg_diag.bin from (ne, atoms, dim, dim) complex values (crates/refeff-io/src/rhorrp_gg_bin.rs:228-252)."""
+    lib = load()
+    v = np.asarray(values, dtype=np.complex128)
+    ne, na, dim, _ = v.shape
+    flat = np.ascontiguousarray(v.transpose(0, 1, 3, 2))
+    rc = lib.refeff_fms_write_gg_diag_bin(str(path).encode(), ne, na, dim, _ptr(flat))
     if rc:
         raise FmsError(rc, f"cannot write {path}")
 

@@ -18,10 +18,15 @@ from pathlib import Path
 
 FMS_TESTS = "crates/refeff-core/src/fms/tests"
 LINALG_TESTS = "crates/refeff-linalg/src/tests.rs"
+GG_BIN = "crates/refeff-io/src/rhorrp_gg_bin.rs"
 
 
 def c(re_, im_, src):
     return {"value": [re_, im_], "src": src}
+
+
+def h(hex_, src):
+    return {"hex": hex_, "src": src}
 
 
 def r(x, src):
@@ -247,6 +252,38 @@ KATS = {
         "representative_offsets": r([9, 0, 18], f"{FMS_TESTS}/driver.rs:33-36"),
         "state_count": r(22, f"{FMS_TESTS}/driver.rs:37"),
     },
+    # FEFF gg_slice.bin (ne 2, ldim 2, istate 3) and gg_diag.bin (ne 2, inclus 2, ldim 2): the reference
+    # byte streams of the codec's own tests and the values they decode to; entry keys are the
+    # (energy, row, column) and (energy, atom, row, column) indices.
+    "gg_slice_bin": {
+        "bytes": h(
+                "0c0000000200000003000000020000000c000000600000009a9931419a99a9c19a9941419a99b1c1333333413333abc1"
+                "333343413333b3c1cdcc3441cdccacc1cdcc4441cdccb4c1cdcca841cdcc24c2cdccb041cdcc28c29a99a9419a9925c2"
+                "9a99b1419a9929c26666aa41666626c26666b24166662ac260000000",
+            f"{GG_BIN}:785-795"),
+        "shape": r([2, 2, 3], f"{GG_BIN}:814-816"),
+        "entries": {
+            "0,0,0": c(11.1, -21.2, f"{GG_BIN}:817"),
+            "0,1,2": c(12.3, -22.6, f"{GG_BIN}:818"),
+            "1,0,0": c(21.1, -41.2, f"{GG_BIN}:819"),
+            "1,1,2": c(22.3, -42.6, f"{GG_BIN}:820"),
+        },
+    },
+    "gg_diag_bin": {
+        "bytes": h(
+                "100000000200000002000000020000000200000010000000800000003333de42333353c33333e042333354c36666de42"
+                "666653c36666e042666654c33333f24233335dc33333f44233335ec36666f24266665dc36666f44266665ec39a195343"
+                "9a99cdc39a1954439a19cec33333534333b3cdc3333354433333cec39a195d439a99d2c39a195e439a19d3c333335d43"
+                "33b3d2c333335e433333d3c380000000",
+            f"{GG_BIN}:797-809"),
+        "shape": r([2, 2, 2, 2], f"{GG_BIN}:828-831"),
+        "entries": {
+            "0,0,0,0": c(111.1, -211.2, f"{GG_BIN}:832"),
+            "0,1,1,1": c(122.2, -222.4, f"{GG_BIN}:833"),
+            "1,0,0,1": c(211.2, -411.4, f"{GG_BIN}:834"),
+            "1,1,1,1": c(222.2, -422.4, f"{GG_BIN}:835"),
+        },
+    },
 }
 
 
@@ -270,9 +307,27 @@ def _flatten(v):
         yield v
 
 
+def _hex_in(obj):
+    if isinstance(obj, dict):
+        if "hex" in obj and "src" in obj:
+            yield obj["hex"], obj["src"]
+        for v in obj.values():
+            if isinstance(v, dict):
+                yield from _hex_in(v)
+
+
 def audit(reference: Path) -> int:
-    """Check that each transcribed number appears in the cited lines (underscores removed)."""
+    """Check that each transcribed number appears in the cited lines (underscores removed), and that each
+    transcribed byte stream equals the 0x.. bytes of its cited lines."""
     bad = 0
+    for hex_, src in _hex_in(KATS):
+        path, _, span = src.rpartition(":")
+        lo, _, hi = span.partition("-")
+        lines = (reference / path).resolve().read_text().splitlines()
+        got = "".join(re.findall(r"0x([0-9a-f]{2})", " ".join(lines[int(lo) - 1:int(hi or lo)])))
+        if got != hex_:
+            print(f"bytes differ at {src}")
+            bad += 1
     for value, src in _numbers_in(KATS):
         path, _, span = src.rpartition(":")
         lo, _, hi = span.partition("-")

@@ -70,6 +70,50 @@ def test_write_gg_dat_byte_exact(tmp_path):
         assert path.read_text() == ff.gg_dat_text(list(sec))
 
 
+def _kat(name):
+    import json
+    from pathlib import Path
+    kat = json.loads((Path(__file__).parent / "golden" / "reference_kat.json").read_text())[name]
+    idx = {tuple(int(i) for i in key.split(",")): complex(*v["value"]) for key, v in kat["entries"].items()}
+    return bytes.fromhex(kat["bytes"]["hex"]), tuple(kat["shape"]["value"]), idx
+
+
+@pytest.mark.parametrize("name", ["gg_slice_bin", "gg_diag_bin"])
+def test_oracle_rhorrp_codecs_match_reference_bytes(name):
+    """FEFF gg_slice.bin / gg_diag.bin byte streams of the reference codec tests (rhorrp_gg_bin.rs:785-835):
+    the oracle parses them to the asserted shape and values and writes them back byte for byte."""
+    data, shape, entries = _kat(name)
+    parse, write = ((ff.parse_gg_slice_bin, ff.gg_slice_bin_bytes) if name == "gg_slice_bin" else
+                    (ff.parse_gg_diag_bin, ff.gg_diag_bin_bytes))
+    v = parse(data)
+    assert v.shape == shape
+    for key, want in entries.items():
+        assert v[key] == np.complex64(want), key
+    assert write(v) == data
+
+
+def test_write_rhorrp_bins_byte_exact(tmp_path):
+    """The product's gg_slice.bin / gg_diag.bin writers reproduce the reference byte streams from the decoded
+    values, and agree with the oracle on larger random blocks (values narrowed to complex f32)."""
+    sl_bytes, _, _ = _kat("gg_slice_bin")
+    dg_bytes, _, _ = _kat("gg_diag_bin")
+    fms.write_gg_slice_bin(tmp_path / "s.bin", ff.parse_gg_slice_bin(sl_bytes))
+    fms.write_gg_diag_bin(tmp_path / "d.bin", ff.parse_gg_diag_bin(dg_bytes))
+    assert (tmp_path / "s.bin").read_bytes() == sl_bytes
+    assert (tmp_path / "d.bin").read_bytes() == dg_bytes
+    rng = np.random.default_rng(4)
+    sl = rng.normal(size=(3, 16, 48)) + 1j * rng.normal(size=(3, 16, 48)) * 10.0 ** rng.integers(-30, 30, (3, 16, 48))
+    dg = rng.normal(size=(2, 5, 9, 9)) - 1j * rng.normal(size=(2, 5, 9, 9))
+    fms.write_gg_slice_bin(tmp_path / "s2.bin", sl)
+    fms.write_gg_diag_bin(tmp_path / "d2.bin", dg)
+    assert (tmp_path / "s2.bin").read_bytes() == ff.gg_slice_bin_bytes(sl)
+    assert (tmp_path / "d2.bin").read_bytes() == ff.gg_diag_bin_bytes(dg)
+    sl[1, 2, 3] = 1e39  # overflows f32: not finite after narrowing
+    with pytest.raises(fms.FmsError) as e:
+        fms.write_gg_slice_bin(tmp_path / "s3.bin", sl)
+    assert e.value.code == 6
+
+
 def test_write_gg_dat_empty_and_parse_round_trip(tmp_path):
     fms.write_gg_dat(tmp_path / "empty.dat", np.zeros((0, 4, 4), complex))
     assert (tmp_path / "empty.dat").read_text() == ""
@@ -200,6 +244,46 @@ def test_run_dir_larger_cluster_and_output_spin_capacity(tmp_path):
     cpos, cpots = fms.fms_yprep_cluster(pos[order], [pots[i] for i in order], cluster_radius=100.0)
     want = _oracle_gg(tmp_path, cpos, cpots, [2] + [3] * max(pots), 100.0)
     assert np.abs(got[:, :9, :9] - want).max() <= 1e-9 * np.abs(want).max()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("minv", [0, 2])
+def test_run_dir_save_gg_slice(tmp_path, minv):
+    """save_gg_slice on: gg.bin / gg.dat as before, plus gg_slice.bin and gg_diag.bin of the full scattering
+    matrix (fms.rs:1113-1125, 3659-3683), equal to the oracle's after narrowing to complex f32; minv != 0 is
+    forced back to the LU form."""
+    from refeff_gb300 import workloads as wl
+    ctx = fms.Context(0)
+    rng = np.random.default_rng(41)
+    cl = wl.small_cluster(3.0, lmax=2, n_energies=1, seed=6)[0]
+    pos = np.asarray(cl.positions, float)
+    pots = [int(p) for p in cl.potentials]
+    ne = 3
+    grid = 0.7 + 0.45 * np.arange(ne) + 0.05j
+    phase_pots = _phase_potentials(rng, ne, 1, [2] * (max(pots) + 1))
+    lmaxph = [2] * (max(pots) + 1)
+    ff.write_workdir(tmp_path, positions=pos, potentials=pots, lmaxph=lmaxph, energy_grid=grid,
+                     phase_potentials=phase_pots, rfms2=100.0, rdirec=100.0)
+    (tmp_path / "fms.inp").write_text(ff.fms_inp_text(lmaxph=lmaxph, rfms2=100.0, rdirec=100.0, minv=minv,
+                                                      save_gg_slice=True))
+    fms.run_fms_in_dir(ctx, tmp_path, fms.FORM_FP32_REFINED)
+    sl = ff.parse_gg_slice_bin((tmp_path / "gg_slice.bin").read_bytes())
+    dg = ff.parse_gg_diag_bin((tmp_path / "gg_diag.bin").read_bytes())
+    assert ff.gg_slice_bin_bytes(sl) == (tmp_path / "gg_slice.bin").read_bytes()
+    cpos, cpots = fms.fms_yprep_cluster(pos, pots, cluster_radius=100.0)
+    pb = fms.read_phase_bin(tmp_path / "phase.bin")
+    k = np.array([[_wave_number(pb["energy_grid"][e], pb["reference_energy"][e, 0])] for e in range(ne)])
+    xp = np.zeros((ne, 1, 5, len(lmaxph)), complex)
+    for p in range(len(lmaxph)):
+        xp[:, :, :, p] = pb["phase_shifts"][:, :, :, p].transpose(0, 2, 1).astype(np.complex64)
+    want_sl, want_dg = pyoracle.full_scattering(cpos, cpots, lmaxph, k, xp)
+    n = len(cpots) * 9
+    assert sl.shape == (ne, 9, n) and dg.shape == (ne, len(cpots), 9, 9)
+    # complex f32 values of FP64 solves: one rounding of each part
+    assert np.abs(sl - want_sl).max() <= 2e-7 * np.abs(want_sl).max()
+    assert np.abs(dg - want_dg).max() <= 2e-7 * np.abs(want_dg).max()
+    gg = np.array(ff.parse_gg_dat((tmp_path / "gg.dat").read_text()))
+    assert np.abs(gg - want_dg[:, 0]).max() <= 1e-9 * np.abs(want_dg[:, 0]).max()
 
 
 @pytest.mark.gpu

@@ -146,6 +146,53 @@ def test_fms_all_potentials_lfms(ctx, form, tol):
                 assert rel_err(gpu[e, :, :, q], ref[e, :, :, q]) < tol, (e, q)
 
 
+def test_full_scattering_save_gg_slice(ctx):
+    """save_gg_slice: the full matrix X = (I - G0 T)^-1 G0 (solvers.rs:473-479) reduced to the absorber's rows over
+    every column and each atom's diagonal block (engine/fms.rs:4154-4216), FP64 LU against the oracle's own LU
+    of the same system, for lfms 0 (n = 117) and lfms 1 (n = 304, all potentials); the full plan's scattering
+    table equals an ordinary plan's, and the absorber's diagonal block is its absorber block."""
+    cases = [(*wl.small_cluster(3.0, lmax=2, n_energies=3, seed=3), {}),
+             (*wl.small_cluster(3.7, lmax=3, n_energies=2, seed=4), {"lfms": 1})]
+    for cl, grid, kw in cases:
+        plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph, full_scattering=True, **kw)
+        tab, sl, dg, st = fms.fms_full_scattering_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+        assert (st == 0).all()
+        ref_sl, ref_dg = po.full_scattering(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers,
+                                            grid.phase_shifts)
+        b, n, N = plan.shape.channel_count, plan.shape.n_states, cl.n_atoms
+        assert sl.shape == ref_sl.shape == (len(st), b, n) and dg.shape == ref_dg.shape == (len(st), N, b, b)
+        for e in range(len(st)):
+            assert rel_err(sl[e], ref_sl[e]) < TOL_FP64, e
+            assert rel_err(dg[e], ref_dg[e]) < TOL_FP64, e
+        assert np.array_equal(sl[:, :, :b], dg[:, 0])
+        plain = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph, **kw)
+        tab2, _ = fms.fms_real_space_spectrum(plain, grid.wave_numbers, grid.phase_shifts)
+        assert rel_err(tab, tab2) < 1e-12
+        for e in range(len(st)):
+            assert rel_err(dg[e, 0], tab[e, :, :, 0]) < 1e-12
+
+
+def test_full_scattering_plan_rules(ctx):
+    """Atoms of different widths are refused (fixed-width atom blocks, engine/fms.rs:4164-4172); the request
+    forces the LU form (driver.rs:72-96): minv is dropped and only the FP64 LU form is accepted; an ordinary plan
+    has no full-scattering output."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=2, seed=8)
+    with pytest.raises(fms.FmsError) as e:
+        fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, [2, 1], full_scattering=True)
+    assert e.value.code == 13 and "fixed-width" in str(e.value)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph, full_scattering=True, minv=1)
+    with pytest.raises(fms.FmsError) as e:
+        fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts, fms.FORM_FP32_REFINED)
+    assert e.value.code == 1
+    tab, _, _, st = fms.fms_full_scattering_spectrum(plan, grid.wave_numbers, grid.phase_shifts)
+    lu = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    tab2, _ = fms.fms_real_space_spectrum(lu, grid.wave_numbers, grid.phase_shifts)
+    assert (st == 0).all() and rel_err(tab, tab2) < 1e-12
+    with pytest.raises(fms.FmsError) as e:
+        fms.fms_full_scattering_spectrum(lu, grid.wave_numbers, grid.phase_shifts)
+    assert e.value.code == 1
+
+
 def test_fms_small_cluster_fp32_refined(ctx):
     cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=6)
     plan, gpu, ref, status = run_pair(ctx, cl, grid, fms.FORM_FP32_REFINED)

@@ -37,6 +37,24 @@ def _intermediates(cl, k, ph, nsp=1, mode=po.F64):
     return po.from_cbuf(g0, (ns, ns)), po.from_cbuf(t, (nsp, ns)), po.from_cbuf(a, (ns, ns))
 
 
+def test_oracle_full_scattering_consistent():
+    """The oracle's save_gg_slice reduction: the absorber's diagonal block equals its scattering table block and
+    the first b columns of the slice, and every slice row block satisfies (I - G0 T) X = G0 on its rows."""
+    cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=2, seed=12)
+    sl, dg = po.full_scattering(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts)
+    scat = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts, mode=po.F64)
+    b = 9
+    assert sl.shape == (2, b, cl.n_atoms * b) and dg.shape == (2, cl.n_atoms, b, b)
+    for e in range(2):
+        assert np.abs(dg[e, 0] - scat[e, :, :, 0]).max() <= 1e-12 * np.abs(scat[e]).max()
+        assert np.array_equal(sl[e, :, :b], dg[e, 0])
+        g0, _, a = _intermediates(cl, grid.wave_numbers[e], grid.phase_shifts[e])
+        X = np.linalg.solve(a, g0)
+        assert np.abs(X[:b] - sl[e]).max() <= 1e-11 * np.abs(X).max()
+        for i in range(cl.n_atoms):
+            assert np.abs(X[i * b:(i + 1) * b, i * b:(i + 1) * b] - dg[e, i]).max() <= 1e-11 * np.abs(X).max()
+
+
 def test_oracle_scattering_equals_direct_solve():
     cl, grid = wl.small_cluster(3.0, lmax=2, n_energies=2)
     scat = po.fms_spectrum(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts, mode=po.F64)
