@@ -139,8 +139,8 @@ typedef struct {
   const int* potentials;            /* n_atoms */
   int spin_channels;                /* nsp: 1 or 2 */
   int spin_selector;                /* global.inp ispin */
-  int lfms;                         /* 0: absorber potential only; else all potentials (LU forms, at most
-                                       64 representative states in total) */
+  int lfms;                         /* 0: absorber potential only; else all potentials (at most 64
+                                       representative states in total) */
   int minv;                         /* FEFF minv: 0 LU, 1 ggbi, 2 ggrm (recursion), 3 gggm, other ggtf (TFQMR) */
   int max_potential;                /* nph */
   int global_lmax;                  /* max over lmaxph */

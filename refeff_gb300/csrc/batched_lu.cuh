@@ -114,11 +114,6 @@ void launch_accumulate_correction(const BatchLayout& lay, int batch, const float
 void launch_ir_check(int batch, const unsigned long long* rnorm_bits, const unsigned long long* bnorm_bits,
                      const unsigned long long* dnorm_bits, const unsigned long long* xnorm_bits, double tol,
                      int* done, int* iters, double* relres, double* dprev, cudaStream_t s);
-// One solved block per potential of the range: rows [row, row + size) of the
-// solution columns [col, col + size), packed at `pack` in each matrix's output.
-struct SolvedBlock {
-  int row, col, size, pack;
-};
 // out[b][pack + r + size * c] = X64 block entries (zero where status[b] != 0);
 // per_matrix = the packed size of one matrix's blocks.
 void launch_extract_blocks(const BatchLayout& lay, int batch, const double2* X64, const SolvedBlock* blocks, int nblocks,

@@ -484,8 +484,6 @@ int plan_create(refeff_fms_context* ctx, const refeff_fms_plan_input* in, bool f
                 "save_gg_slice requires fixed-width atom blocks: got " + std::to_string(p.n) + " state(s), expected " +
                     std::to_string(N * p.C) + " from " + std::to_string(N) + " atom(s) and block dimension " +
                     std::to_string(p.C));
-  if (p.lfms != 0 && p.minv != 0)
-    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "lfms != 0 with the iterative forms (minv != 0) is not supported");
   if (N < 2) return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "a single-atom cluster has no scattering");
 
   // device atom order: reference atom 0 (absorber) last
@@ -983,8 +981,8 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     });
     e = tick(1, [&] {
       return launch_iterative(form == REFEFF_FMS_FORM_FP64_LU, p.minv, lay, batch, ws.M64.p, ws.M32.p, ws.t_tab.p,
-                              p.d_partner.p, p.toler1, p.toler2, ws.grow.p, ws.iter_scratch.p, ws.gg_stage.p,
-                              ws.status.p, s);
+                              p.d_partner.p, p.toler1, p.toler2, ws.grow.p, ws.iter_scratch.p, p.d_blocks.p,
+                              int(p.blocks.size()), p.gg_per, ws.gg_stage.p, ws.status.p, s);
     });
     if (e != cudaSuccess) return e;
   } else if (form == REFEFF_FMS_FORM_FP64_LU) {

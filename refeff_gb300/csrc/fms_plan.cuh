@@ -13,6 +13,12 @@
 namespace rfx {
 
 constexpr int kMaxL = 6;          // largest global lmax the kernels accept
+
+// One solved block per potential of the range: rows [row, row + size) of the
+// solution columns [col, col + size), packed at `pack` in each energy's output.
+struct SolvedBlock {
+  int row, col, size, pack;
+};
 constexpr int kBuildRowAtoms = 16;  // row atoms per build CTA
 
 struct PlanDev {

@@ -36,15 +36,24 @@ template <typename C> __device__ __forceinline__ bool czero(C a) { return a.x ==
 // system assembly
 // ---------------------------------------------------------------------------
 
-// Absorber rows of G0 (device order: the absorber's states are the last m),
-// kept for gg = G0 x before W overwrites G0.
+// The block whose columns hold global column c (the blocks' columns partition [0, m)).
+__device__ __forceinline__ const SolvedBlock& block_of(const SolvedBlock* blocks, int nblocks, int c) {
+  int q = 0;
+  while (q + 1 < nblocks && c >= blocks[q + 1].col) ++q;
+  return blocks[q];
+}
+
+// The solved blocks' rows of G0 (row r of grow is state bl.row + r - bl.col of
+// its block bl), kept for gg = G0 x before W overwrites G0.
 template <typename R>
-__global__ void absorber_rows_kernel(BatchLayout lay, const double2* __restrict__ G0, cplx<R>* __restrict__ grow) {
-  const int e = blockIdx.y, n = lay.n, m = lay.m, off = n - m;
+__global__ void block_rows_kernel(BatchLayout lay, const double2* __restrict__ G0, const SolvedBlock* blocks,
+                                  int nblocks, cplx<R>* __restrict__ grow) {
+  const int e = blockIdx.y, n = lay.n, m = lay.m;
   const double2* g = G0 + size_t(e) * lay.stride;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < m * n; idx += gridDim.x * blockDim.x) {
     const int r = idx % m, s = idx / m;
-    grow[size_t(e) * m * n + idx] = ccast<cplx<R>>(g[size_t(off + r) + size_t(lay.lda) * s]);
+    const SolvedBlock& bl = block_of(blocks, nblocks, r);
+    grow[size_t(e) * m * n + idx] = ccast<cplx<R>>(g[size_t(bl.row + r - bl.col) + size_t(lay.lda) * s]);
   }
 }
 
@@ -451,7 +460,11 @@ __global__ void __launch_bounds__(kThreads) iterative_solve_kernel(IterArgs a) {
   Cta<R> K{n, red, vs};
   const C* W = reinterpret_cast<const C*>(a.W) + size_t(e) * a.stride;
   C* V = reinterpret_cast<C*>(a.scratch) + (size_t(e) * m + col) * kIterVectors * size_t(n);
-  const int src = n - m + col;
+  // the source state of this column: column col - bl.col of its potential's block
+  // (iterative.rs:98-150: solve A' x = e_src for every representative state)
+  const SolvedBlock& bl = block_of(a.blocks, a.nblocks, col);
+  const int lc = col - bl.col;
+  const int src = bl.row + lc;
   const R tol = R(a.tol1);
   int rc;
   if (kMethod == 1) rc = ggbi<R>(K, W, a.lda, src, tol, V, n);
@@ -462,14 +475,15 @@ __global__ void __launch_bounds__(kThreads) iterative_solve_kernel(IterArgs a) {
     if (threadIdx.x == 0) atomicMax(a.status + e, rc == kBreak ? int(kDevBreakdown) : int(kDevNotConverged));
     return;
   }
-  // gg[row, col] = sum_s G0[abs + row, s] x[s]
+  // block entry (row, lc) = sum_s G0[bl.row + row, s] x[s]
   const C* grow = reinterpret_cast<const C*>(a.grow) + size_t(e) * m * n;
   const C* x = V;
-  for (int row = 0; row < m; ++row) {
+  for (int row = 0; row < bl.size; ++row) {
     C s = mk<R>(R(0), R(0));
-    for (int i = threadIdx.x; i < n; i += kThreads) cfma(s, grow[size_t(row) + size_t(m) * i], x[i]);
+    for (int i = threadIdx.x; i < n; i += kThreads) cfma(s, grow[size_t(bl.col + row) + size_t(m) * i], x[i]);
     s = K.reduce(s);
-    if (threadIdx.x == 0) a.gg[size_t(e) * m * m + size_t(row) + size_t(m) * col] = ccast<double2>(s);
+    if (threadIdx.x == 0)
+      a.gg[size_t(e) * a.gg_per + size_t(bl.pack) + size_t(row) + size_t(bl.size) * lc] = ccast<double2>(s);
   }
 }
 
@@ -492,11 +506,13 @@ cudaError_t launch_solve(const IterArgs& a, int batch, cudaStream_t s) {
 template <typename R>
 cudaError_t launch_iterative_t(int minv, const BatchLayout& lay, int batch, const double2* G0, void* W,
                                const double2* t, const int* partner, double tol1, double tol2, void* grow,
-                               void* scratch, double2* gg, int* status, cudaStream_t s) {
+                               void* scratch, const SolvedBlock* blocks, int nblocks, int gg_per, double2* gg,
+                               int* status, cudaStream_t s) {
   {
     const unsigned gx = unsigned(std::min(256, (lay.m * lay.n + 255) / 256));
     count_launch();
-    absorber_rows_kernel<R><<<dim3(gx, unsigned(batch)), 256, 0, s>>>(lay, G0, reinterpret_cast<cplx<R>*>(grow));
+    block_rows_kernel<R><<<dim3(gx, unsigned(batch)), 256, 0, s>>>(lay, G0, blocks, nblocks,
+                                                                  reinterpret_cast<cplx<R>*>(grow));
   }
   {
     const bool gms = minv == 3;
@@ -513,6 +529,9 @@ cudaError_t launch_iterative_t(int minv, const BatchLayout& lay, int batch, cons
   a.W = W;
   a.grow = grow;
   a.scratch = scratch;
+  a.blocks = blocks;
+  a.nblocks = nblocks;
+  a.gg_per = gg_per;
   a.gg = gg;
   a.status = status;
   a.skip = nullptr;
@@ -529,10 +548,13 @@ cudaError_t launch_iterative_t(int minv, const BatchLayout& lay, int batch, cons
 
 cudaError_t launch_iterative(bool fp64, int minv, const BatchLayout& lay, int batch, double2* G0, float2* W32,
                              const double2* t, const int* partner, double tol1, double tol2, void* grow, void* scratch,
-                             double2* gg, int* status, cudaStream_t s) {
+                             const SolvedBlock* blocks, int nblocks, int gg_per, double2* gg, int* status,
+                             cudaStream_t s) {
   if (fp64)
-    return launch_iterative_t<double>(minv, lay, batch, G0, G0, t, partner, tol1, tol2, grow, scratch, gg, status, s);
-  return launch_iterative_t<float>(minv, lay, batch, G0, W32, t, partner, tol1, tol2, grow, scratch, gg, status, s);
+    return launch_iterative_t<double>(minv, lay, batch, G0, G0, t, partner, tol1, tol2, grow, scratch, blocks, nblocks,
+                                      gg_per, gg, status, s);
+  return launch_iterative_t<float>(minv, lay, batch, G0, W32, t, partner, tol1, tol2, grow, scratch, blocks, nblocks,
+                                   gg_per, gg, status, s);
 }
 
 }  // namespace rfx

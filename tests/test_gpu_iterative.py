@@ -54,6 +54,30 @@ def test_iterative_fp64_matches_oracle(ctx, minv, toler2):
     assert _rel(scat, want, m) <= bound
 
 
+@pytest.mark.parametrize("minv", [1, 2, 3, 4])
+def test_iterative_all_potentials_lfms(ctx, minv):
+    """lfms != 0: every potential's representative states are sources (iterative.rs:98-171), here lmaxph [2, 1]
+    (blocks of 9 and 4 states), both forms against the oracle's all-potential iterative run."""
+    cl, grid = _case(seed=13)
+    lmaxph = np.array([2, 1], np.int32)
+    toler1, bound = TOL64[minv]
+    for form, mode, t1, bnd in [(fms.FORM_FP64_LU, po.F64, toler1, bound),
+                                (fms.FORM_FP32_REFINED, po.F32, 1.0e-3, 1e-5 if minv == 1 else 1e-2)]:
+        plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, lmaxph, minv=minv, lfms=1,
+                                       convergence_tolerance=t1, zero_tolerance=0.0)
+        scat, st = fms.fms_real_space_spectrum(plan, grid.wave_numbers, grid.phase_shifts, form,
+                                               raise_on_error=False)
+        want, ost = po.fms_spectrum_iterative(cl.positions, cl.potentials, lmaxph, grid.wave_numbers,
+                                              grid.phase_shifts, minv=minv, toler1=t1, toler2=0.0, lfms=1,
+                                              mode=mode, raise_on_error=False)
+        both = [e for e in range(len(st)) if st[e] == 0 and ost[e] == 0]
+        assert len(both) >= len(st) // 2 and all(v in (0, 19) for v in st)
+        for q, ip in enumerate((9, 4)):
+            g, w = scat[both][:, :ip, :ip, q], want[both][:, :ip, :ip, q]
+            assert np.abs(w).max() > 0
+            assert np.abs(g - w).max() <= bnd * np.abs(w).max(), (form, q)
+
+
 @pytest.mark.parametrize("minv", [2, 3, 4])
 def test_iterative_fp64_at_reference_tolerance(ctx, minv):
     cl, grid = _case(seed=9)
