@@ -120,6 +120,38 @@ def barrier(world: int):
         dist.barrier()
 
 
+def mu_error(ctx, fms, wl, cl, grid, plan, g32, g64, bm, li, L0):
+    """mu(E) of the chosen form against the plain FP64 LU through FF2X's XANES step (refeff_ff2x_xanes_mu):
+    the bench's 200 horizontal energies plus an 8-point vertical contour at the Fermi row (solved here with
+    both forms), MKGTR traces with the seeded rkk, and a seeded smooth atomic cross section (edge step) and
+    background standing in for xsect.dat.  Returns the largest absolute mu error (mu is normalised to the
+    background 50 eV above the edge) and the largest relative one."""
+    ev, k_all, ph_all, fermi = wl.xanes_contour(cl, grid)
+    E = grid.wave_numbers.shape[0]
+    assert np.array_equal(ph_all[:E], grid.phase_shifts) and np.array_equal(k_all[:E], grid.wave_numbers)
+    c32, _ = fms.fms_real_space_spectrum(plan, k_all[E:], ph_all[E:], fms.FORM_FP32_REFINED)
+    c64, _ = fms.fms_real_space_spectrum(plan, k_all[E:], ph_all[E:], fms.FORM_FP64_LU)
+    m = g32.shape[1]
+    a32 = np.concatenate([g32, c32[:, :m, :m, 0]])
+    a64 = np.concatenate([g64, c64[:, :m, :m, 0]])
+    rkk = np.random.default_rng(7).normal(size=(len(ev), 8, 1)) * (1.0 + 0.2j)
+    t32 = fms.mkgtr_trace(ctx, a32, [bm], [li], rkk, active_spin_channels=1, lmax=L0)[0]
+    t64 = fms.mkgtr_trace(ctx, a64, [bm], [li], rkk, active_spin_channels=1, lmax=L0)[0]
+    hartree = 27.211396
+    e_h = ev / hartree
+    x = (ev.real - ev[fermi].real) / hartree
+    xsec = 1j * (2.0 + 0.5 * np.tanh(40.0 * x))
+    bg = 1.0 + 0.3 * np.exp(-3.0 * np.abs(x))
+    omega = e_h[:E].real + 8979.0 / hartree  # photon energies over a Cu K edge
+    kw = dict(energy=e_h, ne1=E, fermi_index=fermi, omega=omega, cross_section=xsec, background=bg,
+              fermi_photon_energy=omega[fermi])
+    mu32 = fms.ff2x_xanes_mu(trace=t32, **kw)[0]
+    mu64 = fms.ff2x_xanes_mu(trace=t64, **kw)[0]
+    d = float(np.max(np.abs(mu32 - mu64)))
+    return {"max_abs": d, "max_rel": d / float(np.max(np.abs(mu64))), "energies": int(len(ev)),
+            "contour_points": int(len(ev) - E)}
+
+
 def cpu_baseline_run(cl, grid, threads: int, n_sample: int):
     """The oracle restatement of the reference's Complex32 FMS path (f32-faithful), OpenMP over energies."""
     from oracle import pyoracle as po
@@ -278,6 +310,7 @@ def ours(args, world, rank, local):
     tr32 = fms.mkgtr_trace(ctx, g32, [bm], [li], rkk, active_spin_channels=1, lmax=L0)[0]
     tr64 = fms.mkgtr_trace(ctx, g64, [bm], [li], rkk, active_spin_channels=1, lmax=L0)[0]
     rel_gtr = float(np.max(np.abs(tr32 - tr64)) / max(np.max(np.abs(tr64)), 1e-300))
+    mu_err = mu_error(ctx, fms, wl, cl, grid, plan, g32, g64, bm, li, L0)
 
     value = world * E * args.steps / (ms_chosen / 1e3)
     plain_value = world * E * plain_steps / (ms_plain / 1e3)
@@ -390,6 +423,7 @@ def ours(args, world, rank, local):
             "chosen_over_plain": value / plain_value,
             "max_rel_gg_err_vs_fp64": float(rel.max()),
             "max_rel_gtr_err_vs_fp64": rel_gtr,
+            "mu_err_vs_fp64": mu_err,
             "status_nonzero": int((st_chosen != 0).sum() + (st_plain != 0).sum()),
             "roofline": roofline,
             "cpu_baseline": cpu,

@@ -394,6 +394,29 @@ int refeff_fms_write_fms_bin(const char* path, double cluster_radius, int ne, in
 
 /* gtr.dat writer (gtr_dat_string, crates/refeff-io/src/gtr_dat.rs:60-71): per
  * energy Re E, Im E, Re gtr, Im gtr as F13.6.  Host only. */
+/* FF2X XANES mu(E) from the MKGTR trace, host only: the stage after MKGTR
+ * (ff2x_xanes_corrected_components, crates/refeff-engine/src/ff2x.rs:3186-3262;
+ * ff2x_xscorr at zero electronic temperature, 4437-4641; the xmu.dat
+ * normalisation and rows, 3309-3399).  chia = s02 * trace; per main row
+ *   total  = Im(xsec + chia * background + xscorr(chia))
+ *   atomic = Im(xsec + xscorr(0))       (0 when include_atomic == 0)
+ *   mu0 = atomic / norm, chi = (total - atomic) / norm, mu = mu0 + chi,
+ * norm = background interpolated (order 1) at fermi_photon_energy + 50 eV
+ * (at fermi_photon_energy for ispec 2), or 1 when absolu == 1.
+ *   ne, ne1: xsect.dat rows (ne1 horizontal rows, then the vertical contour
+ *            whose last row lies at the Fermi level)
+ *   fermi_index: 0-based Fermi row on the horizontal grid; ispec: +-1 or +-2
+ *   energy (ne, complex Hartree), omega (ne1 photon energies, Hartree),
+ *   cross_section (ne complex), background (ne), trace (ne complex gtr(E)),
+ *   real_correction: vrcorr in Hartree (contour shift and rescale)
+ *   mu, mu0, chi: ne1 each, optional.
+ * The vicorr Lorentzian convolution, the sig_gk Debye factor and the thermal
+ * xscorr are not applied. */
+int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
+                         const refeff_complex128* energy, const double* omega, const refeff_complex128* cross_section,
+                         const double* background, const refeff_complex128* trace, double s02, double real_correction,
+                         double fermi_photon_energy, double* mu, double* mu0, double* chi);
+
 int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* energy, const refeff_complex128* trace);
 
 /* ---- learned preconditioner for the BiCGSTAB form ---------------------- */

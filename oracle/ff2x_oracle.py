@@ -1,0 +1,155 @@
+"""TEST INFRASTRUCTURE ONLY: CPU restatement of the FF2X XANES step that turns the MKGTR trace into mu(E).
+
+Used by tests and by bench.py's mu(E) error figure as the checker of the product's
+refeff_ff2x_xanes_mu; never shipped or called by the product.
+
+  lorenz, astep                  crates/refeff-engine/src/ff2x.rs:5052-5076
+                                 (crates/refeff-core/src/xscorr.rs:39-73 for the core ports and their known answers)
+  xscorr, zero temperature       crates/refeff-engine/src/ff2x.rs:4437-4641
+  corrected components           crates/refeff-engine/src/ff2x.rs:3186-3262
+  xmu.dat normalisation / rows   crates/refeff-engine/src/ff2x.rs:3309-3399
+  locat / terp window / polint   crates/refeff-core/src/interpolation.rs:119-135, 338-446
+
+Known answers pinned in tests/test_ff2x.py: the three lorenz and three astep values of
+crates/refeff-core/src/xscorr.rs:121-157 and the constant-cross-section xscorr case of
+crates/refeff-engine/src/ff2x/tests.rs:1127-1149 (fixture 5167-5195).  The contour integral with a
+non-constant integrand has no reference known answer here: for it this restatement and the product's
+C++ agree with each other (parity of that term unpinned).
+"""
+from __future__ import annotations
+
+import cmath
+import math
+
+EPS4 = 1.0e-4
+HARTREE_EV = 27.211396
+
+
+def lorenz(xloss: float, width: float, dele: float) -> complex:
+    """(xloss / pi) / (xloss^2 - (w - i dele)^2 ... ) in the expanded form of ff2x.rs:5058-5065."""
+    den = complex(xloss * xloss - width * width + dele * dele, -2.0 * width * dele)
+    if den == 0:
+        raise ZeroDivisionError("lorenz denominator is zero")
+    return complex(xloss / math.pi, 0.0) / den
+
+
+def astep(xloss: float, dele: float) -> float:
+    return min(1.0, max(0.0, 0.5 + math.atan(dele / xloss) / math.pi))
+
+
+def _locat(x, xs):
+    lo, hi = 0, len(xs) + 1
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        if x < xs[mid - 1]:
+            hi = mid
+        else:
+            lo = mid
+    return lo
+
+
+def _polint(xs, ys, x):
+    n = len(xs)
+    c, d = list(ys), list(ys)
+    ns = min(range(n), key=lambda i: (abs(x - xs[i]), i))
+    y = ys[ns]
+    for m in range(1, n):
+        for i in range(n - m):
+            ho, hp = xs[i] - x, xs[i + m] - x
+            w = (c[i + 1] - d[i]) / (ho - hp)
+            d[i], c[i] = w * hp, w * ho
+        if 2 * ns < n - m:
+            y += c[ns]
+        else:
+            y += d[ns - 1]
+            ns -= 1
+    return y
+
+
+def terp(xs, ys, order, x):
+    n = len(xs)
+    first = max(_locat(x, xs) - order // 2, 1)
+    first = min(first, n - order)
+    return _polint(xs[first - 1:first + order], ys[first - 1:first + order], x)
+
+
+def xscorr(ispec, energy, ne1, fermi, xsec, bg, chia, vrcorr=0.0):
+    """cchi[0:ne1] of the zero-temperature xscorr (ff2x.rs:4437-4641)."""
+    ne = len(energy)
+    energy = [complex(e) for e in energy]
+    xmu = [complex(xsec[r]) + complex(chia[r]) * float(bg[r]) for r in range(ne)]
+    xloss = energy[0].imag
+    ef = energy[-1].real
+    omega = [energy[r].real for r in range(ne1)]
+    scale = 1.0 + 0.0j
+    shifted = abs(vrcorr) > EPS4
+    if shifted:
+        ef -= vrcorr
+        at = terp(omega, xmu[:ne1], 1, ef)
+        for r in range(ne1, ne):
+            energy[r] -= vrcorr
+        scale = at / xmu[fermi]
+        for r in range(ne1, ne):
+            xmu[r] *= scale
+    ze = [energy[r] for r in range(ne1, ne) if energy[r].imag < xloss]
+    zv = [xmu[r] for r in range(ne1, ne) if energy[r].imag < xloss]
+    if shifted:
+        ze.append(complex(ef, xloss))
+        zv.append(scale * xmu[fermi])
+    else:
+        ze.append(energy[fermi])
+        zv.append(xmu[fermi])
+    rows = range(ne1) if ispec != 2 else range(ne1 - 1, -1, -1)
+    for r in rows:
+        past = energy[r].real - ef > EPS4 if ispec != 2 else ef - energy[r].real > EPS4
+        if past:
+            ze.append(energy[r])
+            zv.append(xmu[r])
+    out = []
+    for r in range(ne1):
+        w = omega[r]
+        if w >= ef:
+            x0 = xmu[fermi] * scale if ispec == 2 else xmu[r]
+        else:
+            x0 = xmu[r] if ispec == 2 else xmu[fermi] * scale
+        e1, e2 = complex(w, xloss), complex(w, -xloss)
+        dele = w - ef
+        conv = x0 * astep(xloss, dele)
+        if ispec == 2:
+            conv = x0 - conv
+        corr = lorenz(xloss, ze[0].imag, 0.0 if abs(dele) < EPS4 else dele) * (zv[0] - x0) * complex(0.0, ze[0].imag)
+        for q in range(len(ze) - 1):
+            z1, z2 = ze[q], ze[q + 1]
+            f1, f2 = zv[q] - x0, zv[q + 1] - x0
+            seg = 0j
+            if abs(z1 - e1) > EPS4 and abs(z2 - e1) > EPS4:
+                seg = cmath.log((z2 - e1) / (z1 - e1)) * (f1 * (z2 - e1) + f2 * (e1 - z1))
+            seg -= cmath.log((z2 - e2) / (z1 - e2)) * (f1 * (z2 - e2) + f2 * (e2 - z1))
+            corr += seg / (z2 - z1) / complex(0.0, 2.0 * math.pi)
+        if ispec == 2:
+            corr = -corr
+        out.append(conv + corr - xmu[r])
+    return out
+
+
+def xanes_mu(*, energy, ne1, fermi, omega, cross_section, background, trace, s02=1.0, ispec=1, absolu=0,
+             include_atomic=True, vrcorr=0.0, fermi_photon_energy=0.0):
+    """(mu, mu0, chi) over the ne1 main rows (ff2x.rs:3186-3262 and 3309-3399, sig_gk = 0, no vicorr)."""
+    ispec = abs(ispec)
+    ne = len(energy)
+    xsec = [complex(v) if include_atomic else 0j for v in cross_section]
+    chia = [complex(t) * s02 for t in trace]
+    tot = xscorr(ispec, energy, ne1, fermi, xsec, background, chia, vrcorr)
+    atm = xscorr(ispec, energy, ne1, fermi, xsec, background, [0j] * ne, vrcorr)
+    norm = 1.0
+    if absolu != 1:
+        at = fermi_photon_energy if ispec == 2 else fermi_photon_energy + 50.0 / HARTREE_EV
+        norm = terp(list(omega[:ne1]), [float(b) for b in background[:ne1]], 1, at)
+    mu, mu0, chi = [], [], []
+    for r in range(ne1):
+        total = (xsec[r] + chia[r] * float(background[r]) + tot[r]).imag
+        atomic = (xsec[r] + atm[r]).imag if include_atomic else 0.0
+        mu0.append(atomic / norm)
+        chi.append((total - atomic) / norm)
+        mu.append(mu0[-1] + chi[-1])
+    return mu, mu0, chi

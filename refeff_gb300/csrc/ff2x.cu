@@ -1,0 +1,245 @@
+// FF2X XANES mu(E) from the MKGTR trace (host code): the zero-temperature
+// xscorr contour correction of the broadened cross section and the xmu.dat
+// normalisation, the stage after MKGTR that turns gtr(E) into mu(E).
+//
+// Reference (crates/refeff-engine/src/ff2x.rs unless noted):
+//   chia = s02 * gtr                       ff2x_xanes_fms_trace_for_spectrum  2569-2603
+//   total / atomic / fine structure        ff2x_xanes_corrected_components    3186-3262
+//   xscorr at zero electronic temperature  ff2x_xscorr                        4437-4641
+//   lorenz, astep                          ff2x_xscorr_lorenz / _astep        5052-5076
+//   normalisation and mu0, chi, mu         ff2x_xanes_xmu_dat_from_components 3309-3399
+//   locat, terp / terpc window, polint     crates/refeff-core/src/interpolation.rs:119-135, 215-236, 338-446
+// The Lorentzian convolution by vicorr (3265-3306), the Debye factor sig_gk
+// and the thermal xscorr (4643-) are not part of this entry point.
+#include <cmath>
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/refeff_fms.h"
+
+namespace {
+
+using cd = std::complex<double>;
+constexpr double kEps4 = 1.0e-4;          // FF2X_EPS4 (ff2x.rs:41)
+constexpr double kHartreeEv = 27.211396;  // HARTREE_EV (crates/refeff-core/src/constants.rs:18)
+constexpr double kPi = 3.14159265358979323846;
+
+// FEFF locat: how many grid points are <= x (bisection on an increasing grid).
+size_t locat(double x, const double* xs, size_t n) {
+  size_t lo = 0, hi = n + 1;
+  while (hi - lo > 1) {
+    const size_t mid = (lo + hi) / 2;
+    if (x < xs[mid - 1]) hi = mid;
+    else lo = mid;
+  }
+  return lo;
+}
+
+// Neville's recurrence on the points (xs, ys), started from the point nearest
+// x and walking the tableau the way FEFF's polint does.
+template <typename T>
+bool polint(const double* xs, const T* ys, size_t n, double x, T& out) {
+  std::vector<T> c(ys, ys + n), d(ys, ys + n);
+  size_t ns = 0;
+  double best = std::fabs(x - xs[0]);
+  for (size_t i = 1; i < n; ++i)
+    if (std::fabs(x - xs[i]) < best) {
+      best = std::fabs(x - xs[i]);
+      ns = i;
+    }
+  T y = ys[ns];
+  for (size_t m = 1; m < n; ++m) {
+    for (size_t i = 0; i + m < n; ++i) {
+      const double ho = xs[i] - x, hp = xs[i + m] - x, den = ho - hp;
+      if (den == 0.0) return false;
+      const T w = (c[i + 1] - d[i]) / den;
+      d[i] = w * hp;
+      c[i] = w * ho;
+    }
+    T dy;
+    if (2 * ns < n - m) {
+      dy = c[ns];
+    } else {
+      dy = d[ns - 1];
+      --ns;
+    }
+    y = y + dy;
+  }
+  out = y;
+  return true;
+}
+
+// FEFF terp / terpc: an order-`order` polynomial through the order + 1 grid
+// points around x (window from locat, clamped to the table).
+template <typename T>
+bool terp(const double* xs, const T* ys, size_t n, size_t order, double x, T& out) {
+  if (n < order + 1) return false;
+  const size_t located = locat(x, xs, n);
+  size_t first = located > order / 2 ? located - order / 2 : 0;  // 1-based
+  if (first < 1) first = 1;
+  if (first > n - order) first = n - order;
+  return polint(xs + first - 1, ys + first - 1, order + 1, x, out);
+}
+
+double astep(double xloss, double dele) {
+  const double v = 0.5 + std::atan(dele / xloss) / kPi;
+  return v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
+}
+
+cd lorenz(double xloss, double width, double dele) {
+  const cd den(xloss * xloss - width * width + dele * dele, -2.0 * width * dele);
+  return cd(xloss / kPi, 0.0) / den;
+}
+
+bool finite(cd z) { return std::isfinite(z.real()) && std::isfinite(z.imag()); }
+
+// Zero-temperature xscorr: cchi[row] (row < ne1) = the broadened xmu minus xmu,
+// xmu = xsec + chia * xsnorm.  The broadening is the arctangent step times the
+// Fermi-level value plus a contour integral of xmu along the vertical contour
+// and the horizontal grid beyond the Fermi level (below it for ispec 2).
+int xscorr(int ispec, const cd* energy_in, size_t ne, size_t ne1, size_t fermi, const cd* xsec, const double* bg,
+           const cd* chia, double vrcorr, std::vector<cd>& cchi, std::string& err) {
+  if (ne1 < 2 || ne1 >= ne || fermi >= ne1) {
+    err = "xscorr needs at least two horizontal points, a contour after them, and the Fermi row on the horizontal grid";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  std::vector<cd> energy(energy_in, energy_in + ne), xmu(ne);
+  for (size_t r = 0; r < ne; ++r) {
+    if (!finite(energy[r]) || !finite(xsec[r]) || !std::isfinite(bg[r]) || !finite(chia[r])) {
+      err = "xscorr input row " + std::to_string(r) + " is not finite";
+      return REFEFF_FMS_ERR_NONFINITE_INPUT;
+    }
+    xmu[r] = xsec[r] + chia[r] * bg[r];
+  }
+  const double xloss = energy[0].imag();
+  if (!(xloss > 0.0)) {
+    err = "xscorr needs a positive broadening (Im of the first energy)";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  double ef = energy[ne - 1].real();
+  std::vector<double> omega(ne1);
+  for (size_t r = 0; r < ne1; ++r) omega[r] = energy[r].real();
+  cd scale(1.0, 0.0);
+  const bool shifted = std::fabs(vrcorr) > kEps4;
+  if (shifted) {
+    // move the contour by vrcorr and rescale it to the horizontal xmu at the shifted Fermi level
+    if (std::abs(xmu[fermi]) == 0.0) {
+      err = "xscorr cannot rescale the contour from a zero Fermi-level xmu";
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+    ef -= vrcorr;
+    cd at_ef;
+    if (!terp(omega.data(), xmu.data(), ne1, 1, ef, at_ef)) {
+      err = "xscorr interpolation at the shifted Fermi level failed";
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+    for (size_t r = ne1; r < ne; ++r) energy[r] -= cd(vrcorr, 0.0);
+    scale = at_ef / xmu[fermi];
+    for (size_t r = ne1; r < ne; ++r) xmu[r] *= scale;
+  }
+  // contour: the vertical points below the broadening, the Fermi point, then the
+  // horizontal points past the Fermi level (ascending; descending for ispec 2)
+  std::vector<cd> ze, zv;
+  for (size_t r = ne1; r < ne; ++r)
+    if (energy[r].imag() < xloss) {
+      ze.push_back(energy[r]);
+      zv.push_back(xmu[r]);
+    }
+  if (shifted) {
+    ze.push_back(cd(ef, xloss));
+    zv.push_back(scale * xmu[fermi]);
+  } else {
+    ze.push_back(energy[fermi]);
+    zv.push_back(xmu[fermi]);
+  }
+  if (ispec != 2) {
+    for (size_t r = 0; r < ne1; ++r)
+      if (energy[r].real() - ef > kEps4) {
+        ze.push_back(energy[r]);
+        zv.push_back(xmu[r]);
+      }
+  } else {
+    for (size_t r = ne1; r-- > 0;)
+      if (ef - energy[r].real() > kEps4) {
+        ze.push_back(energy[r]);
+        zv.push_back(xmu[r]);
+      }
+  }
+  if (ze.size() < 2) {
+    err = "xscorr contour has fewer than two points";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  cchi.assign(ne1, cd(0.0, 0.0));
+  const cd two_pi_i(0.0, 2.0 * kPi);
+  for (size_t r = 0; r < ne1; ++r) {
+    const double w = omega[r];
+    const cd ref = (w >= ef) == (ispec == 2) ? xmu[fermi] * scale : xmu[r];
+    const cd e1(w, xloss), e2(w, -xloss);
+    const double dele = w - ef;
+    cd conv = ref * astep(xloss, dele);
+    if (ispec == 2) conv = ref - conv;
+    const double dl = std::fabs(dele) < kEps4 ? 0.0 : dele;
+    cd corr = lorenz(xloss, ze[0].imag(), dl) * (zv[0] - ref) * cd(0.0, ze[0].imag());
+    for (size_t q = 0; q + 1 < ze.size(); ++q) {
+      const cd z1 = ze[q], z2 = ze[q + 1], f1 = zv[q] - ref, f2 = zv[q + 1] - ref, dz = z2 - z1;
+      if (std::abs(dz) == 0.0) {
+        err = "xscorr contour repeats a point";
+        return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+      }
+      cd seg(0.0, 0.0);
+      if (std::abs(z1 - e1) > kEps4 && std::abs(z2 - e1) > kEps4)
+        seg = std::log((z2 - e1) / (z1 - e1)) * (f1 * (z2 - e1) + f2 * (e1 - z1));
+      seg -= std::log((z2 - e2) / (z1 - e2)) * (f1 * (z2 - e2) + f2 * (e2 - z1));
+      corr += seg / dz / two_pi_i;
+    }
+    if (ispec == 2) corr = -corr;
+    cchi[r] = conv + corr - xmu[r];
+  }
+  return REFEFF_FMS_OK;
+}
+
+}  // namespace
+
+extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
+                                    const refeff_complex128* energy, const double* omega,
+                                    const refeff_complex128* cross_section, const double* background,
+                                    const refeff_complex128* trace, double s02, double real_correction,
+                                    double fermi_photon_energy, double* mu, double* mu0, double* chi) {
+  const int is = ispec < 0 ? -ispec : ispec;  // ff2x_xmu_effective_ispec (ff2x.rs:1496-1502)
+  if (ne <= 0 || ne1 <= 0 || ne1 >= ne || fermi_index < 0 || fermi_index >= ne1 || is < 1 || is > 2 || !energy ||
+      !omega || !cross_section || !background || !trace || !std::isfinite(s02))
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  const size_t n = size_t(ne), n1 = size_t(ne1);
+  std::vector<cd> e(n), xsec(n), chia(n), zero(n, cd(0.0, 0.0));
+  for (size_t r = 0; r < n; ++r) {
+    e[r] = cd(energy[r].re, energy[r].im);
+    xsec[r] = include_atomic ? cd(cross_section[r].re, cross_section[r].im) : cd(0.0, 0.0);
+    chia[r] = cd(trace[r].re, trace[r].im) * s02;
+  }
+  std::vector<cd> total_corr, atomic_corr;
+  std::string err;
+  int rc = xscorr(is, e.data(), n, n1, size_t(fermi_index), xsec.data(), background, chia.data(), real_correction,
+                  total_corr, err);
+  if (rc) return rc;
+  rc = xscorr(is, e.data(), n, n1, size_t(fermi_index), xsec.data(), background, zero.data(), real_correction,
+              atomic_corr, err);
+  if (rc) return rc;
+  double norm = 1.0;
+  if (absolu != 1) {
+    const double at = is == 2 ? fermi_photon_energy : fermi_photon_energy + 50.0 / kHartreeEv;
+    if (!terp(omega, background, n1, 1, at, norm) || !std::isfinite(norm) || norm == 0.0)
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  for (size_t r = 0; r < n1; ++r)
+    if (!finite(total_corr[r]) || !finite(atomic_corr[r])) return REFEFF_FMS_ERR_NONFINITE_INPUT;
+  for (size_t r = 0; r < n1; ++r) {
+    const double total = (xsec[r] + chia[r] * background[r] + total_corr[r]).imag();
+    const double atomic = include_atomic ? (xsec[r] + atomic_corr[r]).imag() : 0.0;
+    const double m0 = atomic / norm, c = (total - atomic) / norm;
+    if (mu0) mu0[r] = m0;
+    if (chi) chi[r] = c;
+    if (mu) mu[r] = m0 + c;
+  }
+  return REFEFF_FMS_OK;
+}

@@ -100,6 +100,8 @@ def load(build_if_missing: bool = True):
         "refeff_fms_real_space_plan_create_full": ([_p, _p, _p], _i),
         "refeff_fms_real_space_spectrum_full": ([_p, _p, _p, _p, _p, _p, _p], _i),
         "refeff_fms_write_gg_slice_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
+        "refeff_ff2x_xanes_mu": ([_i, _i, _i, _i, _i, _i, _p, _p, _p, _p, _p, C.c_double, C.c_double, C.c_double,
+                                  _p, _p, _p], _i),
         "refeff_fms_write_gg_diag_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
         "refeff_fms_real_space_plan_destroy": ([_p], None),
         "refeff_fms_plan_query": ([_p, _p, _p, _p, _p], _i),
@@ -527,6 +529,29 @@ def write_gg_dat(path, sections) -> None:
     rc = lib.refeff_fms_write_gg_dat(str(path).encode(), n, dim, _ptr(flat))
     if rc:
         raise FmsError(rc, f"cannot write {path}")
+
+
+def ff2x_xanes_mu(*, energy, ne1, fermi_index, omega, cross_section, background, trace, s02=1.0, ispec=1,
+                  absolu=0, include_atomic=True, real_correction=0.0, fermi_photon_energy=0.0):
+    """FF2X XANES mu(E) from the MKGTR trace (crates/refeff-engine/src/ff2x.rs:3186-3262, 3309-3399, 4437-4641):
+    returns (mu, mu0, chi) over the ne1 main rows.  energy, cross_section, trace: ne complex; background: ne
+    reals; omega: ne1 photon energies; all energies in Hartree.  Host only."""
+    lib = load()
+    e = np.ascontiguousarray(energy, dtype=np.complex128)
+    ne = e.shape[0]
+    om = np.ascontiguousarray(omega, dtype=np.float64)
+    xs = np.ascontiguousarray(cross_section, dtype=np.complex128)
+    bg = np.ascontiguousarray(background, dtype=np.float64)
+    tr = np.ascontiguousarray(trace, dtype=np.complex128)
+    if om.shape[0] < ne1 or xs.shape[0] != ne or bg.shape[0] != ne or tr.shape[0] != ne:
+        raise FmsError(1, "ff2x_xanes_mu: array lengths do not match ne / ne1")
+    mu, mu0, chi = (np.zeros(int(ne1)) for _ in range(3))
+    rc = lib.refeff_ff2x_xanes_mu(ne, int(ne1), int(fermi_index), int(ispec), int(absolu), int(bool(include_atomic)),
+                                  _ptr(e), _ptr(om), _ptr(xs), _ptr(bg), _ptr(tr), float(s02), float(real_correction),
+                                  float(fermi_photon_energy), _ptr(mu), _ptr(mu0), _ptr(chi))
+    if rc:
+        raise FmsError(rc, "ff2x_xanes_mu")
+    return mu, mu0, chi
 
 
 def write_gg_slice_bin(path, values) -> None:

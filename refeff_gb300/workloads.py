@@ -181,6 +181,25 @@ def energy_grid(cluster: Cluster, n_energies: int, e_lo: float, e_hi: float, see
     return EnergyGrid(ev, k, ph, dict(seed=seed, e_lo=e_lo, e_hi=e_hi))
 
 
+def xanes_contour(cluster: Cluster, grid: EnergyGrid, n_contour: int = 8, inner_potential_ev: float = 15.0,
+                  broadening_ev: float = 0.1, nsp: int = 1):
+    """The vertical contour FF2X's xscorr integrates along, appended to a horizontal grid made by energy_grid:
+    the Fermi row is the grid energy nearest 0 eV, and the contour runs at that real energy from below the
+    broadening down to the real axis (FEFF xsect.dat order: horizontal rows, then the contour, its last row at
+    the Fermi level).  The phase shifts of all rows come from one draw of the same seeded model, so the
+    horizontal rows equal grid's.  Returns (energies in eV, complex (E + n_contour,), wave numbers, phase
+    shifts, Fermi row)."""
+    fermi = int(np.argmin(np.abs(grid.energies_ev)))
+    ef = float(grid.energies_ev[fermi])
+    ims = np.r_[np.linspace(0.15, 0.9, n_contour - 1) * broadening_ev, 0.0]
+    k_c = np.concatenate([wave_numbers_from_energies(np.array([ef]), inner_potential_ev, float(y), nsp) for y in ims])
+    k_all = np.concatenate([grid.wave_numbers, k_c])
+    rng = np.random.default_rng(grid.meta["seed"])
+    ph = smooth_phase_shifts(rng, k_all, cluster.global_lmax, len(cluster.lmaxph), nsp)
+    ev = np.r_[grid.energies_ev + 1j * broadening_ev, ef + 1j * ims]
+    return ev, k_all, ph, fermi
+
+
 # ---- the named configurations ----
 
 def config0():

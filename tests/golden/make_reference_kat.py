@@ -19,6 +19,7 @@ from pathlib import Path
 FMS_TESTS = "crates/refeff-core/src/fms/tests"
 LINALG_TESTS = "crates/refeff-linalg/src/tests.rs"
 GG_BIN = "crates/refeff-io/src/rhorrp_gg_bin.rs"
+XSCORR = "crates/refeff-core/src/xscorr.rs"
 
 
 def c(re_, im_, src):
@@ -252,6 +253,20 @@ KATS = {
         "representative_offsets": r([9, 0, 18], f"{FMS_TESTS}/driver.rs:33-36"),
         "state_count": r(22, f"{FMS_TESTS}/driver.rs:37"),
     },
+    # FF2X xscorr helpers: lorenz(xloss, width, dele) and astep(xloss, dele), the core ports' known answers
+    # (the engine's ff2x_xscorr_lorenz / _astep evaluate the same expressions, ff2x.rs:5052-5076).
+    "xscorr_lorenz": [
+        {"args": r([0.08, 0.02, -0.11], f"{XSCORR}:125-127"), "want": c(1.3283935648445944, -0.3229244025036583,
+                                                                            f"{XSCORR}:128")},
+        {"args": r([0.08, 0.13, 0.0], f"{XSCORR}:130"), "want": c(-2.4252181804479287, 0.0, f"{XSCORR}:130")},
+        {"args": r([0.15, 0.05, 0.19], f"{XSCORR}:132-134"), "want": c(0.763516919522092, 0.2585886180199599,
+                                                                           f"{XSCORR}:135")},
+    ],
+    "xscorr_astep": [
+        {"args": r([0.08, -0.11], f"{XSCORR}:151"), "want": r(0.2001520743616867, f"{XSCORR}:152")},
+        {"args": r([0.08, 0.0], f"{XSCORR}:154"), "want": r(0.5, f"{XSCORR}:154")},
+        {"args": r([0.08, 0.22], f"{XSCORR}:155"), "want": r(0.8889827415450001, f"{XSCORR}:155")},
+    ],
     # FEFF gg_slice.bin (ne 2, ldim 2, istate 3) and gg_diag.bin (ne 2, inclus 2, ldim 2): the reference
     # byte streams of the codec's own tests and the values they decode to; entry keys are the
     # (energy, row, column) and (energy, atom, row, column) indices.

@@ -1,0 +1,119 @@
+"""FF2X XANES mu(E) from the MKGTR trace (host code, no GPU).
+
+The oracle restatement (oracle/ff2x_oracle.py) is pinned to the reference's lorenz / astep known answers
+(crates/refeff-core/src/xscorr.rs:121-157) and to its constant-cross-section xscorr case
+(crates/refeff-engine/src/ff2x/tests.rs:1127-1149, fixture 5167-5195); the product's refeff_ff2x_xanes_mu is
+checked against the oracle on those cases and on seeded XANES-like inputs, for both ispec and with a vrcorr
+shift.  mu is linear in the trace: the last test checks that too.
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import ff2x_oracle as fo
+from refeff_gb300 import fms
+
+KAT = json.loads((Path(__file__).parent / "golden" / "reference_kat.json").read_text())
+
+
+def test_oracle_lorenz_astep_known_answers():
+    for case in KAT["xscorr_lorenz"]:
+        got = fo.lorenz(*case["args"]["value"])
+        want = complex(*case["want"]["value"])
+        assert abs(got - want) <= 1e-12 * max(abs(want), 1.0)
+    for case in KAT["xscorr_astep"]:
+        assert abs(fo.astep(*case["args"]["value"]) - case["want"]["value"]) <= 1e-14
+
+
+def _constant_fixture():
+    """ff2x/tests.rs:5167-5195: three horizontal rows at Im 0.1, a contour (1.0, 0.02), (1.0, 0.05), (1.0, 0)."""
+    energy = [0.9 + 0.1j, 1.0 + 0.1j, 1.1 + 0.1j, 1.0 + 0.02j, 1.0 + 0.05j, 1.0 + 0.0j]
+    return dict(energy=energy, ne1=3, fermi=1, xsec=[10j] * 6, bg=[1.0] * 6)
+
+
+def test_oracle_constant_cross_section_xscorr():
+    """ff2x/tests.rs:1127-1149: with a constant atomic cross section 10i and no trace, xscorr is the step:
+    Im(xsec + cchi) = 10 astep(E - E_F) and cchi = i 10 (astep - 1)."""
+    f = _constant_fixture()
+    cchi = fo.xscorr(1, f["energy"], f["ne1"], f["fermi"], f["xsec"], f["bg"], [0j] * 6)
+    for row, e in enumerate([0.9, 1.0, 1.1]):
+        step = 0.5 + math.atan((e - 1.0) / 0.1) / math.pi
+        assert abs((10j + cchi[row]).imag - 10.0 * step) <= 1e-12
+        assert abs(cchi[row] - complex(0.0, 10.0 * (step - 1.0))) <= 1e-12
+
+
+def test_product_constant_cross_section_case():
+    f = _constant_fixture()
+    mu, mu0, chi = fms.ff2x_xanes_mu(energy=f["energy"], ne1=3, fermi_index=1, omega=[0.9, 1.0, 1.1],
+                                     cross_section=f["xsec"], background=f["bg"], trace=np.zeros(6), absolu=1)
+    for row, e in enumerate([0.9, 1.0, 1.1]):
+        step = 0.5 + math.atan((e - 1.0) / 0.1) / math.pi
+        assert abs(mu0[row] - 10.0 * step) <= 1e-12 and abs(chi[row]) <= 1e-12 and mu[row] == mu0[row] + chi[row]
+
+
+def xanes_inputs(rng, ne1=60, n_contour=8, ispec=1):
+    """Seeded XANES-like rows in Hartree: a horizontal grid at Im = xloss across the Fermi level, then a
+    vertical contour at Re = E_F ending at Im 0; a smooth atomic cross section with an edge step, a smooth
+    background and a trace with oscillations."""
+    xloss = 0.1 / fo.HARTREE_EV
+    ef = 0.3
+    main = np.linspace(ef - 15.0 / fo.HARTREE_EV, ef + 60.0 / fo.HARTREE_EV, ne1)
+    fermi = int(np.argmin(np.abs(main - ef)))
+    main[fermi] = ef
+    contour = ef + 1j * np.r_[np.linspace(0.2, 0.9, n_contour - 1) * xloss, 0.0]
+    energy = np.r_[main + 1j * xloss, contour]
+    ne = energy.shape[0]
+    x = energy.real - ef
+    xsec = 1j * (2.0 + 0.5 * np.tanh(40.0 * x)) + 0.05 * rng.normal(size=ne)
+    bg = 1.0 + 0.3 * np.exp(-3.0 * np.abs(x)) + 0.01 * rng.normal(size=ne)
+    trace = (0.2 * np.exp(1j * (9.0 * x + rng.uniform(0, 6)))) * (1 + 0.1 * rng.normal(size=ne))
+    omega = main + 8.979  # photon energies (Hartree), a Cu K edge offset
+    return dict(energy=energy, ne1=ne1, fermi=fermi, omega=omega, xsec=xsec, bg=bg, trace=trace,
+                fermi_photon=omega[fermi])
+
+
+@pytest.mark.parametrize("ispec,vrcorr,include_atomic,absolu",
+                         [(1, 0.0, True, 0), (2, 0.0, True, 0), (1, 0.5 / 27.211396, True, 0),
+                          (1, 0.0, False, 1), (-2, -0.4 / 27.211396, True, 0)])
+def test_product_matches_oracle(ispec, vrcorr, include_atomic, absolu):
+    rng = np.random.default_rng(7 + ispec)
+    d = xanes_inputs(rng)
+    got = fms.ff2x_xanes_mu(energy=d["energy"], ne1=d["ne1"], fermi_index=d["fermi"], omega=d["omega"],
+                            cross_section=d["xsec"], background=d["bg"], trace=d["trace"], s02=0.9, ispec=ispec,
+                            absolu=absolu, include_atomic=include_atomic, real_correction=vrcorr,
+                            fermi_photon_energy=d["fermi_photon"])
+    want = fo.xanes_mu(energy=list(d["energy"]), ne1=d["ne1"], fermi=d["fermi"], omega=list(d["omega"]),
+                       cross_section=list(d["xsec"]), background=list(d["bg"]), trace=list(d["trace"]), s02=0.9,
+                       ispec=ispec, absolu=absolu, include_atomic=include_atomic, vrcorr=vrcorr,
+                       fermi_photon_energy=d["fermi_photon"])
+    for g, w in zip(got, want):
+        w = np.asarray(w)
+        assert np.abs(g - w).max() <= 1e-12 * max(np.abs(w).max(), 1.0)
+
+
+def test_mu_is_affine_in_the_trace():
+    """mu(trace) - mu(0) is linear: doubling the trace doubles chi, and mu0 does not depend on the trace."""
+    d = xanes_inputs(np.random.default_rng(3))
+    kw = dict(energy=d["energy"], ne1=d["ne1"], fermi_index=d["fermi"], omega=d["omega"], cross_section=d["xsec"],
+              background=d["bg"], fermi_photon_energy=d["fermi_photon"])
+    _, m0a, ca = fms.ff2x_xanes_mu(trace=d["trace"], **kw)
+    _, m0b, cb = fms.ff2x_xanes_mu(trace=2.0 * d["trace"], **kw)
+    assert np.abs(m0a - m0b).max() == 0.0
+    assert np.abs(cb - 2.0 * ca).max() <= 1e-12 * np.abs(ca).max()
+
+
+def test_invalid_rows_are_rejected():
+    d = xanes_inputs(np.random.default_rng(5))
+    kw = dict(energy=d["energy"], fermi_index=d["fermi"], omega=d["omega"], cross_section=d["xsec"],
+              background=d["bg"], trace=d["trace"])
+    with pytest.raises(fms.FmsError):
+        fms.ff2x_xanes_mu(ne1=len(d["energy"]), **kw)          # no contour rows
+    bad = dict(kw)
+    bad["trace"] = d["trace"].copy()
+    bad["trace"][4] = np.nan
+    with pytest.raises(fms.FmsError) as e:
+        fms.ff2x_xanes_mu(ne1=d["ne1"], **bad)
+    assert e.value.code == 6
