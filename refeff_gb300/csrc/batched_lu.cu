@@ -285,6 +285,117 @@ __global__ void __launch_bounds__(256) rhs_lower_kernel(BatchLayout lay, int k, 
     rhs_lower_column<T, NB, kSolve>(lay, k, kb, Mb + size_t(lay.lda) * col, w, b, L11, lane);
   }
 }
+// The outer block row of the two-level FP32 elimination as a product:
+// U12 = L11^-1 (P A12).  First each matrix's unit lower L11 (rows and columns
+// [k, k + kb)) is inverted, one warp per column of the inverse; then each CTA
+// takes kLtN columns of the block row, applies the block's composed row moves
+// (rows in [k, n)) and multiplies the kb panel rows by L11^-1 from shared
+// memory, each thread keeping 8 rows of one column in registers.  The
+// column-by-column substitution it replaces walked a 64-step dependent chain
+// of shuffles per column; here the same flops run with full instruction-level
+// parallelism.  Partial pivoting keeps |L11| <= 1, so the explicit inverse is
+// as good a triangular solve as substitution for the FP32 factors, which the
+// FP64 refinement corrects in any case.
+constexpr int kLtN = 32;  // block-row columns per CTA of rhs_lower_tile_kernel
+
+__global__ void __launch_bounds__(256) unit_lower_inverse_kernel(BatchLayout lay, int k,
+                                                                 const float2* __restrict__ M,
+                                                                 float2* __restrict__ linv) {
+  constexpr int NB = 64, kRows = NB / 32;
+  const int b = blockIdx.x;
+  __shared__ float2 L11[NB][NB + 1];
+  const int kb = min(NB, lay.n - k);
+  const float2* Mb = M + size_t(b) * lay.stride;
+  for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+    const int r = idx % kb, c = idx / kb;
+    L11[r][c] = Mb[size_t(k + r) + size_t(lay.lda) * (k + c)];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2* out = linv + size_t(b) * NB * NB;
+  for (int j = wid; j < NB; j += 8) {
+    float2 x[kRows];
+#pragma unroll
+    for (int t = 0; t < kRows; ++t) x[t] = make_float2(lane + 32 * t == j ? 1.f : 0.f, 0.f);
+    for (int p = j; p < kb; ++p) {
+      const int ot = p >> 5, ol = p & 31;
+      float2 xp = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int t = 0; t < kRows; ++t) {
+        const float re = __shfl_sync(0xffffffffu, x[t].x, ol);
+        const float im = __shfl_sync(0xffffffffu, x[t].y, ol);
+        if (t == ot) xp = make_float2(re, im);
+      }
+#pragma unroll
+      for (int t = 0; t < kRows; ++t) {
+        const int i = lane + 32 * t;
+        if (i > p && i < kb) cfms(x[t], L11[i][p], xp);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < kRows; ++t) {
+      const int i = lane + 32 * t;
+      out[i + NB * j] = (i < kb && j < kb) ? x[t] : make_float2(0.f, 0.f);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) rhs_lower_tile_kernel(BatchLayout lay, int k, int c_begin, int c_end,
+                                                             float2* __restrict__ M, LuWork w,
+                                                             const float2* __restrict__ linv) {
+  constexpr int NB = 64;
+  const int b = blockIdx.y, cb = c_begin + blockIdx.x * kLtN;
+  const int ncols = min(kLtN, c_end - cb);
+  const int kb = min(NB, lay.n - k);
+  extern __shared__ float2 lt_sm[];
+  float2* Li = lt_sm;               // [NB][NB]: Li[i + NB * j] = (L11^-1)(i, j)
+  float2* Bt = lt_sm + NB * NB;     // [2 NB][kLtN]: the moves' staging, then the panel rows [NB][kLtN]
+  float2* Mb = M + size_t(b) * lay.stride;
+  const size_t lda = size_t(lay.lda);
+  const int tid = threadIdx.x;
+  // the block's composed row moves on these columns
+  const size_t pidx = size_t(b) * w.npanels + k / NB;
+  const int np = w.nperm[pidx];
+  const int2* pm = w.perm + pidx * (2 * NB);
+  for (int idx = tid; idx < np * ncols; idx += 256) {
+    const int i = idx % np, c = idx / np;
+    Bt[i * kLtN + c] = Mb[size_t(pm[i].y) + lda * size_t(cb + c)];
+  }
+  const float4* src = reinterpret_cast<const float4*>(linv + size_t(b) * NB * NB);
+  for (int idx = tid; idx < NB * NB / 2; idx += 256) reinterpret_cast<float4*>(Li)[idx] = src[idx];
+  __syncthreads();
+  for (int idx = tid; idx < np * ncols; idx += 256) {
+    const int i = idx % np, c = idx / np;
+    Mb[size_t(pm[i].x) + lda * size_t(cb + c)] = Bt[i * kLtN + c];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < NB * kLtN; idx += 256) {
+    const int i = idx % NB, c = idx / NB;
+    Bt[i * kLtN + c] = (i < kb && c < ncols) ? Mb[size_t(k + i) + lda * size_t(cb + c)] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  // rows r0 .. r0 + 7 of column `col`; L11^-1 is lower triangular, so j <= r0 + 7
+  const int col = tid & 31, r0 = (tid >> 5) * 8;
+  float2 acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = make_float2(0.f, 0.f);
+  const int jend = min(kb, r0 + 8);
+  for (int j = 0; j < jend; ++j) {
+    const float2 bv = Bt[j * kLtN + col];
+    const float4* lr = reinterpret_cast<const float4*>(Li + r0 + NB * j);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 l2 = lr[q];
+      cfma(acc[2 * q], make_float2(l2.x, l2.y), bv);
+      cfma(acc[2 * q + 1], make_float2(l2.z, l2.w), bv);
+    }
+  }
+  if (col < ncols)
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (r0 + q < kb) Mb[size_t(k + r0 + q) + lda * size_t(cb + col)] = acc[q];
+}
+
 // One warp per RHS column: X[k:k+kb] = U11^-1 Y[k:k+kb] (bottom-up).
 template <typename T, int NB>
 __global__ void __launch_bounds__(256) rhs_upper_kernel(BatchLayout lay, int k, cplx<T>* __restrict__ M,
@@ -502,14 +613,14 @@ __global__ void __launch_bounds__(256) residual_df_kernel(BatchLayout lay, const
 #pragma unroll
       for (int q = 0; q < kCols; ++q) {
         const float4 x = Xs[kk * XW + cg + kRdGroups * q];
-        df_mac(acc[0][q][0], a0.x, a0.z, x.x, x.z);    // re += a.re x.re
-        df_mac(acc[0][q][0], -a0.y, -a0.w, x.y, x.w);  // re -= a.im x.im
-        df_mac(acc[0][q][1], a0.x, a0.z, x.y, x.w);    // im += a.re x.im
-        df_mac(acc[0][q][1], a0.y, a0.w, x.x, x.z);    // im += a.im x.re
-        df_mac(acc[1][q][0], a1.x, a1.z, x.x, x.z);
-        df_mac(acc[1][q][0], -a1.y, -a1.w, x.y, x.w);
-        df_mac(acc[1][q][1], a1.x, a1.z, x.y, x.w);
-        df_mac(acc[1][q][1], a1.y, a1.w, x.x, x.z);
+        dot2_mac(acc[0][q][0], a0.x, a0.z, x.x, x.z);    // re += a.re x.re
+        dot2_mac(acc[0][q][0], -a0.y, -a0.w, x.y, x.w);  // re -= a.im x.im
+        dot2_mac(acc[0][q][1], a0.x, a0.z, x.y, x.w);    // im += a.re x.im
+        dot2_mac(acc[0][q][1], a0.y, a0.w, x.x, x.z);    // im += a.im x.re
+        dot2_mac(acc[1][q][0], a1.x, a1.z, x.x, x.z);
+        dot2_mac(acc[1][q][0], -a1.y, -a1.w, x.y, x.w);
+        dot2_mac(acc[1][q][1], a1.x, a1.z, x.y, x.w);
+        dot2_mac(acc[1][q][1], a1.y, a1.w, x.x, x.z);
       }
     }
   }
@@ -895,7 +1006,24 @@ static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayo
     }
     count_launch();
     compose_moves_kernel<<<batch, 128, 0, s>>>(k, iw, P, w, wi);
-    launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
+    if (w.linv) {
+      count_launch();
+      unit_lower_inverse_kernel<<<batch, 256, 0, s>>>(lay, k, M, w.linv);
+      const int ncols = col_end - (k + kb);
+      if (ncols > 0) {
+        constexpr int smem = (64 * 64 + 2 * 64 * kLtN) * int(sizeof(float2));
+        static bool attr = false;  // raised once, before any stream capture
+        if (!attr) {
+          cudaFuncSetAttribute(rhs_lower_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+          attr = true;
+        }
+        count_launch();
+        rhs_lower_tile_kernel<<<dim3(unsigned((ncols + kLtN - 1) / kLtN), unsigned(batch)), 256, smem, s>>>(
+            lay, k, k + kb, col_end, M, w, w.linv);
+      }
+    } else {
+      launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
+    }
     if (w.tc_images) tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
     else gemm_any<float>(64, lay, batch, k + kb, n, k + kb, col_end, k, kb, M, nullptr, s);
     cudaError_t err = cudaGetLastError();

@@ -53,6 +53,9 @@ struct LuWork {
   // blocks keep their composed moves in perm / nperm.
   int2* perm_in = nullptr;
   int* nperm_in = nullptr;
+  // [batch][64 x 64] inverse of the outer block's unit lower L11 (two-level FP32
+  // elimination); null = the block row is solved column by column
+  float2* linv = nullptr;
   // row-position bookkeeping of the panel kernel when it does not fit in
   // shared memory: [batch][2n] ints (row2pos, pos2row)
   int* pos_scratch = nullptr;

@@ -80,6 +80,22 @@ __device__ __forceinline__ void df_mac(df& acc, float ah, float al, float xh, fl
   acc.hi = s + t;
   acc.lo = t - (acc.hi - s);
 }
+// Compensated dot product step (Ogita, Rump and Oishi, "Accurate sum and dot
+// product", SIAM J. Sci. Comput. 26 (2005), Dot2): s carries the rounded sum
+// of the products ah*xh, c the sum of their exact rounding errors (two_prod
+// and two_sum) plus the cross terms ah*xl + al*xh, in plain FP32.  s + c is as
+// accurate as the sum computed in twice the working precision; 12 FP32
+// operations per product against 15 for a renormalised double-float step.
+__device__ __forceinline__ void dot2_mac(df& acc, float ah, float al, float xh, float xl) {
+  const float p = __fmul_rn(ah, xh);  // rounded product: must not be fused into the sums below
+  float e = fmaf(ah, xh, -p);
+  e = fmaf(ah, xl, e);
+  e = fmaf(al, xh, e);
+  float s, q;
+  df_two_sum(acc.hi, p, s, q);
+  acc.hi = s;
+  acc.lo += q + e;
+}
 __device__ __forceinline__ void df_renorm(df& a) {
   const float s = a.hi + a.lo;
   a.lo = a.lo - (s - a.hi);

@@ -333,6 +333,7 @@ struct Workspace {
   DevBuf<int> tc_err;                // set by a tensor-core wait that timed out
   DevBuf<int2> perm;
   DevBuf<int2> perm_in;              // row moves of the inner panels (two-level FP32 LU)
+  DevBuf<float2> linv;               // inverse of each outer block's unit lower L11 (two-level FP32 LU)
   DevBuf<int> nperm_in;
   DevBuf<int> pos_scratch;           // panel row-position bookkeeping for large n
   // BiCGSTAB form: solver vectors and scalars, the preconditioner diagonal,
@@ -732,6 +733,7 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
   if (ws.fp32 && ws.pc32.inner_nb) {
     RF_CUDA(ctx, ws.perm_in.alloc(size_t(B) * panel_count(n, ws.pc32.inner_nb) * 2 * ws.pc32.inner_nb));
     RF_CUDA(ctx, ws.nperm_in.alloc(size_t(B) * panel_count(n, ws.pc32.inner_nb)));
+    RF_CUDA(ctx, ws.linv.alloc(size_t(B) * 64 * 64));
   }
   RF_CUDA(ctx, ws.ipiv.alloc(size_t(B) * n));
   RF_CUDA(ctx, ws.perm.alloc(size_t(B) * npanels * 2 * nb_max));
@@ -760,6 +762,7 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
   if (&pc == &ws.pc32) {
     w.perm_in = ws.perm_in.p;
     w.nperm_in = ws.nperm_in.p;
+    w.linv = ws.linv.p;
   }
   if (&pc == &ws.pc32 && ws.use_tc) {
     w.tc_images = ws.tc_images.p;
