@@ -18,7 +18,7 @@ namespace rfx {
 namespace {
 
 constexpr int kSwThreads = 512;
-constexpr int kSwUnroll = 8;
+constexpr int kSwUnroll = 16;
 
 template <int NB, int CG>
 struct SweepSmem {
