@@ -310,6 +310,287 @@ __global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, 
 }
 
 // ---------------------------------------------------------------------------
+// the update, persistent and warp-specialised
+// ---------------------------------------------------------------------------
+// One CTA per SM walks the tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
+// (t -> matrix b, row tile bm, column tile bn, bn fastest).  Roles:
+//   warp 0   producer: bulk-copies each K-chunk (100 KB of planes) into a
+//            two-stage ring, waiting for the stage to be released;
+//   warp 1   MMA: 24 tcgen05.mma per chunk into one of two TMEM accumulators
+//            (128 columns each), releasing the stage with tcgen05.commit and
+//            signalling the tile's accumulator the same way;
+//   warps 2-5 and 6-9   two epilogue groups, each taking every other tile of
+//            the CTA: C of the tile is loaded into registers before waiting
+//            for the accumulator, then tcgen05.ld, subtract, store, release.
+// The copies of tile i + 1, its MMAs and the epilogue of tile i overlap, and
+// two epilogues are in flight per SM.  Every wait is bounded; a timeout sets
+// the error flag and a shared abort flag that ends every role's loop, then
+// the producer waits (bounded) for its copies still in flight and the MMA
+// thread for its MMAs before the tensor memory is freed.
+constexpr int kPStages = 2;
+constexpr int kPThreads = 320;
+constexpr uint32_t kPTmemCols = 256;
+constexpr int kPSmem = kPStages * SMEM_OPS + 1024 + 256;
+
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                                   int* err_flag) {
+  const uint64_t t0 = global_ns();
+  for (long long it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((it & 255) == 255) {
+      if (*abort_flag) return false;
+      if (global_ns() - t0 > 1000000000ull) break;
+    }
+  }
+  *abort_flag = 1;
+  atomicExch(err_flag, 1);
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
+    BatchLayout lay, int k, int kb, int col_end, float2* __restrict__ M, const uint8_t* __restrict__ aimg,
+    const uint8_t* __restrict__ bimg, int nbm_all, int nbn_all, int nbm, int nbn, int batch, int* __restrict__ err_flag,
+    const int* skip) {
+  extern __shared__ uint8_t smraw[];
+  const uint32_t raw = smem_u32(smraw);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t* const gbase = smraw + (sbase - raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + kPStages * SMEM_OPS);
+  // bars: full[2], empty[2], acc_full[2], acc_empty[2], drain
+  auto bar = [&](int i) { return smem_u32(&bars[i]); };
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kPStages * SMEM_OPS + 128);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(gbase + kPStages * SMEM_OPS + 132);
+  int* consumed = reinterpret_cast<int*>(gbase + kPStages * SMEM_OPS + 136);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n = lay.n;
+  const int per_matrix = nbm * nbn;
+  const long long total = (long long)per_matrix * batch;
+  const int nchunks = kb > KC ? 2 : 1;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kPTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 32) {
+    for (int i = 0; i < kPStages; ++i) {
+      mbar_init(bar(i), 1);             // full: the producer's expect_tx
+      mbar_init(bar(2 + i), 1);         // empty: one commit
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(bar(4 + a), 1);         // accumulator full: one commit
+      mbar_init(bar(6 + a), 128);       // accumulator empty: the 128 threads of one epilogue group
+    }
+    mbar_init(bar(8), 1);               // drain
+    *abort_flag = 0;
+    *consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  auto tile_of = [&](long long t, int& b, int& bm, int& bn) {
+    b = int(t / per_matrix);
+    const int rem = int(t - (long long)b * per_matrix);
+    bm = rem / nbn;
+    bn = rem - bm * nbn;
+  };
+
+  if (warp == 0) {
+    // ---- producer ----
+    if (lane == 0) {
+      long long c = 0;  // chunks issued
+      for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+        int b, bm, bn;
+        tile_of(t, b, bm, bn);
+        if (skip && skip[b]) continue;
+        const uint8_t* ab = aimg + (size_t(b) * nbm_all + bm) * 2 * size_t(A_PLANES) * A_PLANE;
+        const uint8_t* bb = bimg + (size_t(b) * nbn_all + bn) * 2 * size_t(B_PLANES) * B_PLANE;
+        bool ok = true;
+        for (int ch = 0; ch < nchunks; ++ch, ++c) {
+          const int st = int(c % kPStages);
+          const uint32_t ph = uint32_t((c / kPStages) & 1);
+          if (!mbar_wait_or_abort(bar(2 + st), ph ^ 1u, abort_flag, err_flag)) { ok = false; break; }
+          const uint32_t sA = sbase + uint32_t(st) * SMEM_OPS, sB = sA + A_PLANES * A_PLANE;
+          mbar_expect_tx(bar(st), uint32_t(SMEM_OPS));
+          const uint8_t* ach = ab + size_t(ch) * A_PLANES * A_PLANE;
+          const uint8_t* bch = bb + size_t(ch) * B_PLANES * B_PLANE;
+          for (int p = 0; p < A_PLANES; ++p) bulk_copy(sA + p * A_PLANE, ach + size_t(p) * A_PLANE, A_PLANE, bar(st));
+          for (int p = 0; p < B_PLANES; ++p) bulk_copy(sB + p * B_PLANE, bch + size_t(p) * B_PLANE, B_PLANE, bar(st));
+        }
+        if (!ok) break;
+      }
+      if (*abort_flag) {
+        // copies issued but not yet seen complete by the MMA thread: wait for them (bounded)
+        for (long long q = *(volatile int*)consumed; q < c; ++q) {
+          const uint64_t t0 = global_ns();
+          for (long long it = 0; it < kWaitLimit; ++it) {
+            uint32_t done;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                : "=r"(done)
+                : "r"(bar(int(q % kPStages))), "r"(uint32_t((q / kPStages) & 1))
+                : "memory");
+            if (done || ((it & 1023) == 1023 && global_ns() - t0 > 1000000000ull)) break;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer ----
+    if (lane == 0) {
+      long long c = 0, i = 0;  // chunks consumed, tiles of this CTA
+      bool issued = false;
+      for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+        int b, bm, bn;
+        tile_of(t, b, bm, bn);
+        if (skip && skip[b]) continue;
+        const int a = int(i & 1);
+        if (!mbar_wait_or_abort(bar(6 + a), uint32_t(((i >> 1) & 1) ^ 1), abort_flag, err_flag)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t tmem_r = tmem + uint32_t(a * 128), tmem_i = tmem_r + 64;
+        bool ok = true;
+        for (int ch = 0; ch < nchunks; ++ch, ++c) {
+          const int st = int(c % kPStages);
+          if (!mbar_wait_or_abort(bar(st), uint32_t((c / kPStages) & 1), abort_flag, err_flag)) { ok = false; break; }
+          *(volatile int*)consumed = int(c + 1);
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sA = sbase + uint32_t(st) * SMEM_OPS, sB = sA + A_PLANES * A_PLANE;
+          for (int ks = 0; ks < KC / 8; ++ks) {
+            const uint32_t koff = uint32_t(ks * 32);
+            auto ad = [&](int p) { return umma_desc_sw128(sA + p * A_PLANE + koff); };
+            auto bd = [&](int p) { return umma_desc_sw128(sB + p * B_PLANE + koff); };
+            const uint32_t acc0 = (ch == 0 && ks == 0) ? 0u : 1u;
+            // Cr += Ar Br + Ai (-Bi)
+            mma_tf32(tmem_r, ad(0), bd(0), acc0);
+            mma_tf32(tmem_r, ad(0), bd(1), 1u);
+            mma_tf32(tmem_r, ad(1), bd(0), 1u);
+            mma_tf32(tmem_r, ad(2), bd(4), 1u);
+            mma_tf32(tmem_r, ad(2), bd(5), 1u);
+            mma_tf32(tmem_r, ad(3), bd(4), 1u);
+            // Ci += Ar Bi + Ai Br
+            mma_tf32(tmem_i, ad(0), bd(2), acc0);
+            mma_tf32(tmem_i, ad(0), bd(3), 1u);
+            mma_tf32(tmem_i, ad(1), bd(2), 1u);
+            mma_tf32(tmem_i, ad(2), bd(0), 1u);
+            mma_tf32(tmem_i, ad(2), bd(1), 1u);
+            mma_tf32(tmem_i, ad(3), bd(0), 1u);
+          }
+          issued = true;
+          umma_commit(bar(2 + st));  // the stage is free once these MMAs have read it
+        }
+        if (!ok) break;
+        umma_commit(bar(4 + a));  // the accumulator is complete
+        ++i;
+      }
+      if (issued) {
+        // every MMA of this CTA has completed before the tensor memory is freed
+        umma_commit(bar(8));
+        const uint64_t t0 = global_ns();
+        for (long long it = 0; it < kWaitLimit; ++it) {
+          uint32_t done;
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+              : "=r"(done)
+              : "r"(bar(8))
+              : "memory");
+          if (done || ((it & 1023) == 1023 && global_ns() - t0 > 1000000000ull)) break;
+        }
+      }
+    }
+  } else {
+    // ---- epilogue groups ----
+    const int g = (warp - 2) >> 2;     // group 0: warps 2-5, group 1: warps 6-9
+    const int quarter = warp & 3;      // tensor-memory lanes [32 quarter, 32 quarter + 32)
+    const uint32_t lane_off = uint32_t(quarter * 32) << 16;
+    long long i = 0;                   // tiles of this CTA
+    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+      // every branch below is uniform across the warp (tcgen05.ld is .sync.aligned)
+      if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
+      int b, bm, bn;
+      tile_of(t, b, bm, bn);
+      if (skip && skip[b]) continue;
+      const long long mine = i++;
+      if ((mine & 1) != g) continue;
+      const int r0 = k + kb + bm * BM, c0 = k + kb + bn * BN;
+      const int row = r0 + quarter * 32 + lane;
+      const bool row_ok = row < n;
+      const size_t ld = size_t(lay.lda);
+      float2* crow = M + size_t(b) * lay.stride + size_t(row) + ld * size_t(c0);
+      // C of 16 columns at a time, the next part loaded while this one is stored
+      float2 cn[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        cn[j] = (row_ok && c0 + j < col_end) ? crow[ld * size_t(j)] : make_float2(0.f, 0.f);
+      const bool ready = mbar_wait_or_abort(bar(4 + g), uint32_t((mine >> 1) & 1), abort_flag, err_flag);
+      if (!__all_sync(0xffffffffu, ready)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tmem_r = tmem + uint32_t(g * 128) + lane_off, tmem_i = tmem_r + 64;
+#pragma unroll
+      for (int part = 0; part < BN / 16; ++part) {
+        float2 cc[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) cc[j] = cn[j];
+        if (part + 1 < BN / 16) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = c0 + (part + 1) * 16 + j;
+            cn[j] = (row_ok && col < col_end) ? crow[ld * size_t((part + 1) * 16 + j)] : make_float2(0.f, 0.f);
+          }
+        }
+        uint32_t cr[16], ci[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(cr[0]), "=r"(cr[1]), "=r"(cr[2]), "=r"(cr[3]), "=r"(cr[4]), "=r"(cr[5]), "=r"(cr[6]), "=r"(cr[7]),
+              "=r"(cr[8]), "=r"(cr[9]), "=r"(cr[10]), "=r"(cr[11]), "=r"(cr[12]), "=r"(cr[13]), "=r"(cr[14]),
+              "=r"(cr[15])
+            : "r"(tmem_r + uint32_t(part * 16)));
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(ci[0]), "=r"(ci[1]), "=r"(ci[2]), "=r"(ci[3]), "=r"(ci[4]), "=r"(ci[5]), "=r"(ci[6]), "=r"(ci[7]),
+              "=r"(ci[8]), "=r"(ci[9]), "=r"(ci[10]), "=r"(ci[11]), "=r"(ci[12]), "=r"(ci[13]), "=r"(ci[14]),
+              "=r"(ci[15])
+            : "r"(tmem_i + uint32_t(part * 16)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row_ok) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int col = c0 + part * 16 + j;
+            if (col < col_end) {
+              float2 v = cc[j];
+              v.x -= __uint_as_float(cr[j]);
+              v.y -= __uint_as_float(ci[j]);
+              crow[ld * size_t(part * 16 + j)] = v;
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(bar(6 + g));  // the accumulator may be overwritten
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPTmemCols));
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 KernelSpans& tc_update_spans() {
@@ -334,11 +615,16 @@ void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int co
   tc_split_a_kernel<<<dim3(unsigned(2 * nbm), unsigned(batch)), 256, 0, s>>>(lay, k, kb, M, aimg, nbm_all);
   count_launch();
   tc_split_b_kernel<<<dim3(unsigned(2 * nbn), unsigned(batch)), 256, 0, s>>>(lay, k, kb, col_end, M, bimg, nbn_all);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(tc_update_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    attr = true;
+  static int sms = 0;  // attributes and the SM count, once (before any stream capture)
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaFuncSetAttribute(tc_update_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem);
+    if (sms <= 0) sms = 1;
   }
+  const long long tiles = (long long)nbm * nbn * batch;
+  const unsigned grid = unsigned(tiles < sms ? tiles : sms);
   KernelSpans& prof = tc_update_spans();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (prof.on) {
@@ -347,8 +633,8 @@ void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int co
     cudaEventRecord(e0, s);
   }
   count_launch();
-  tc_update_kernel<<<dim3(unsigned(nbm), unsigned(nbn), unsigned(batch)), 128, SMEM_BYTES, s>>>(
-      lay, k, kb, col_end, M, aimg, bimg, nbm_all, nbn_all, err_flag, skip);
+  tc_update_persistent_kernel<<<grid, kPThreads, kPSmem, s>>>(lay, k, kb, col_end, M, aimg, bimg, nbm_all, nbn_all,
+                                                              nbm, nbn, batch, err_flag, skip);
   if (prof.on) {
     cudaEventRecord(e1, s);
     prof.spans.push_back({e0, e1});
