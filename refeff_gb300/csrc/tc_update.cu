@@ -319,17 +319,19 @@ __global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, 
 //   warp 1   MMA: 24 tcgen05.mma per chunk into one of two TMEM accumulators
 //            (128 columns each), releasing the stage with tcgen05.commit and
 //            signalling the tile's accumulator the same way;
-//   warps 2-5 and 6-9   two epilogue groups, each taking every other tile of
-//            the CTA: C of the tile is loaded into registers before waiting
-//            for the accumulator, then tcgen05.ld, subtract, store, release.
-// The copies of tile i + 1, its MMAs and the epilogue of tile i overlap, and
-// two epilogues are in flight per SM.  Every wait is bounded; a timeout sets
+//   warps 2-17   four epilogue groups of four warps, group g taking the tiles
+//            i = g mod 4 of the CTA: C of the tile is loaded into registers
+//            16 columns ahead, then tcgen05.ld, subtract, store, release.
+// The copies of tile i + 1, its MMAs and the epilogues of the previous tiles
+// overlap; four epilogues are in flight per SM, which keeps enough C loads
+// outstanding to approach the bandwidth of moving C.  Every wait is bounded; a timeout sets
 // the error flag and a shared abort flag that ends every role's loop, then
 // the producer waits (bounded) for its copies still in flight and the MMA
 // thread for its MMAs before the tensor memory is freed.
 constexpr int kPStages = 2;
-constexpr int kPThreads = 320;
-constexpr uint32_t kPTmemCols = 256;
+constexpr int kPGroups = 4;                     // epilogue groups of 4 warps, one accumulator each
+constexpr int kPThreads = 64 + kPGroups * 128;  // producer warp, MMA warp, epilogue groups
+constexpr uint32_t kPTmemCols = 512;  // kPGroups * 128 columns, rounded up to a power of two
 constexpr int kPSmem = kPStages * SMEM_OPS + 1024 + 256;
 
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag,
@@ -370,7 +372,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
   const uint32_t sbase = (raw + 1023u) & ~1023u;
   uint8_t* const gbase = smraw + (sbase - raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + kPStages * SMEM_OPS);
-  // bars: full[2], empty[2], acc_full[2], acc_empty[2], drain
+  // bars: full[2], empty[2], acc_full[4], acc_empty[4], drain
   auto bar = [&](int i) { return smem_u32(&bars[i]); };
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kPStages * SMEM_OPS + 128);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(gbase + kPStages * SMEM_OPS + 132);
@@ -378,7 +380,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n = lay.n;
   const int per_matrix = nbm * nbn;
-  const long long total = (long long)per_matrix * batch;
+  const int total = per_matrix * batch;  // the host keeps this below 2^31
   const int nchunks = kb > KC ? 2 : 1;
 
   if (warp == 0) {
@@ -391,11 +393,11 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
       mbar_init(bar(i), 1);             // full: the producer's expect_tx
       mbar_init(bar(2 + i), 1);         // empty: one commit
     }
-    for (int a = 0; a < 2; ++a) {
-      mbar_init(bar(4 + a), 1);         // accumulator full: one commit
-      mbar_init(bar(6 + a), 128);       // accumulator empty: the 128 threads of one epilogue group
+    for (int a = 0; a < kPGroups; ++a) {
+      mbar_init(bar(4 + a), 1);             // accumulator full: one commit
+      mbar_init(bar(4 + kPGroups + a), 128);  // accumulator empty: the 128 threads of one epilogue group
     }
-    mbar_init(bar(8), 1);               // drain
+    mbar_init(bar(4 + 2 * kPGroups), 1);  // drain
     *abort_flag = 0;
     *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -405,9 +407,9 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  auto tile_of = [&](long long t, int& b, int& bm, int& bn) {
-    b = int(t / per_matrix);
-    const int rem = int(t - (long long)b * per_matrix);
+  auto tile_of = [&](int t, int& b, int& bm, int& bn) {
+    b = t / per_matrix;
+    const int rem = t - b * per_matrix;
     bm = rem / nbn;
     bn = rem - bm * nbn;
   };
@@ -416,7 +418,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
     // ---- producer ----
     if (lane == 0) {
       long long c = 0;  // chunks issued
-      for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+      for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
         int b, bm, bn;
         tile_of(t, b, bm, bn);
         if (skip && skip[b]) continue;
@@ -457,12 +459,13 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
     if (lane == 0) {
       long long c = 0, i = 0;  // chunks consumed, tiles of this CTA
       bool issued = false;
-      for (long long t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
+      for (int t = blockIdx.x; t < total && !*abort_flag; t += gridDim.x) {
         int b, bm, bn;
         tile_of(t, b, bm, bn);
         if (skip && skip[b]) continue;
-        const int a = int(i & 1);
-        if (!mbar_wait_or_abort(bar(6 + a), uint32_t(((i >> 1) & 1) ^ 1), abort_flag, err_flag)) break;
+        const int a = int(i % kPGroups);
+        if (!mbar_wait_or_abort(bar(4 + kPGroups + a), uint32_t(((i / kPGroups) & 1) ^ 1), abort_flag, err_flag))
+          break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t tmem_r = tmem + uint32_t(a * 128), tmem_i = tmem_r + 64;
         bool ok = true;
@@ -501,14 +504,14 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
       }
       if (issued) {
         // every MMA of this CTA has completed before the tensor memory is freed
-        umma_commit(bar(8));
+        umma_commit(bar(4 + 2 * kPGroups));
         const uint64_t t0 = global_ns();
         for (long long it = 0; it < kWaitLimit; ++it) {
           uint32_t done;
           asm volatile(
               "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
               : "=r"(done)
-              : "r"(bar(8))
+              : "r"(bar(4 + 2 * kPGroups))
               : "memory");
           if (done || ((it & 1023) == 1023 && global_ns() - t0 > 1000000000ull)) break;
         }
@@ -516,33 +519,33 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
     }
   } else {
     // ---- epilogue groups ----
-    const int g = (warp - 2) >> 2;     // group 0: warps 2-5, group 1: warps 6-9
+    const int g = (warp - 2) >> 2;     // group g: warps 2 + 4g .. 5 + 4g
     const int quarter = warp & 3;      // tensor-memory lanes [32 quarter, 32 quarter + 32)
     const uint32_t lane_off = uint32_t(quarter * 32) << 16;
     long long i = 0;                   // tiles of this CTA
-    for (long long t = blockIdx.x; t < total; t += gridDim.x) {
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
       // every branch below is uniform across the warp (tcgen05.ld is .sync.aligned)
       if (__shfl_sync(0xffffffffu, *abort_flag, 0)) break;
       int b, bm, bn;
       tile_of(t, b, bm, bn);
       if (skip && skip[b]) continue;
       const long long mine = i++;
-      if ((mine & 1) != g) continue;
+      if (mine % kPGroups != g) continue;
       const int r0 = k + kb + bm * BM, c0 = k + kb + bn * BN;
       const int row = r0 + quarter * 32 + lane;
       const bool row_ok = row < n;
-      const size_t ld = size_t(lay.lda);
-      float2* crow = M + size_t(b) * lay.stride + size_t(row) + ld * size_t(c0);
+      const int ld = lay.lda;  // column offsets within a tile stay far below 2^31 elements
+      float2* crow = M + size_t(b) * lay.stride + size_t(row) + size_t(lay.lda) * size_t(c0);
       // C of 16 columns at a time, the next part loaded while this one is stored
       float2 cn[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j)
-        cn[j] = (row_ok && c0 + j < col_end) ? crow[ld * size_t(j)] : make_float2(0.f, 0.f);
-      const bool ready = mbar_wait_or_abort(bar(4 + g), uint32_t((mine >> 1) & 1), abort_flag, err_flag);
+        cn[j] = (row_ok && c0 + j < col_end) ? crow[j * ld] : make_float2(0.f, 0.f);
+      const bool ready = mbar_wait_or_abort(bar(4 + g), uint32_t((mine / kPGroups) & 1), abort_flag, err_flag);
       if (!__all_sync(0xffffffffu, ready)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tmem_r = tmem + uint32_t(g * 128) + lane_off, tmem_i = tmem_r + 64;
-#pragma unroll
+#pragma unroll 1
       for (int part = 0; part < BN / 16; ++part) {
         float2 cc[16];
 #pragma unroll
@@ -551,38 +554,37 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int col = c0 + (part + 1) * 16 + j;
-            cn[j] = (row_ok && col < col_end) ? crow[ld * size_t((part + 1) * 16 + j)] : make_float2(0.f, 0.f);
+            cn[j] = (row_ok && col < col_end) ? crow[((part + 1) * 16 + j) * ld] : make_float2(0.f, 0.f);
           }
         }
-        uint32_t cr[16], ci[16];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(cr[0]), "=r"(cr[1]), "=r"(cr[2]), "=r"(cr[3]), "=r"(cr[4]), "=r"(cr[5]), "=r"(cr[6]), "=r"(cr[7]),
-              "=r"(cr[8]), "=r"(cr[9]), "=r"(cr[10]), "=r"(cr[11]), "=r"(cr[12]), "=r"(cr[13]), "=r"(cr[14]),
-              "=r"(cr[15])
-            : "r"(tmem_r + uint32_t(part * 16)));
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(ci[0]), "=r"(ci[1]), "=r"(ci[2]), "=r"(ci[3]), "=r"(ci[4]), "=r"(ci[5]), "=r"(ci[6]), "=r"(ci[7]),
-              "=r"(ci[8]), "=r"(ci[9]), "=r"(ci[10]), "=r"(ci[11]), "=r"(ci[12]), "=r"(ci[13]), "=r"(ci[14]),
-              "=r"(ci[15])
-            : "r"(tmem_i + uint32_t(part * 16)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (row_ok) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int col = c0 + part * 16 + j;
-            if (col < col_end) {
-              float2 v = cc[j];
-              v.x -= __uint_as_float(cr[j]);
-              v.y -= __uint_as_float(ci[j]);
-              crow[ld * size_t(part * 16 + j)] = v;
+        for (int h = 0; h < 2; ++h) {
+          uint32_t cr[8], ci[8];
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(cr[0]), "=r"(cr[1]), "=r"(cr[2]), "=r"(cr[3]), "=r"(cr[4]), "=r"(cr[5]), "=r"(cr[6]),
+                         "=r"(cr[7])
+                       : "r"(tmem_r + uint32_t(part * 16 + h * 8)));
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                       : "=r"(ci[0]), "=r"(ci[1]), "=r"(ci[2]), "=r"(ci[3]), "=r"(ci[4]), "=r"(ci[5]), "=r"(ci[6]),
+                         "=r"(ci[7])
+                       : "r"(tmem_i + uint32_t(part * 16 + h * 8)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const int col = c0 + part * 16 + h * 8 + j;
+              if (col < col_end) {
+                float2 v = cc[h * 8 + j];
+                v.x -= __uint_as_float(cr[j]);
+                v.y -= __uint_as_float(ci[j]);
+                crow[(part * 16 + h * 8 + j) * ld] = v;
+              }
             }
           }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(bar(6 + g));  // the accumulator may be overwritten
+      mbar_arrive(bar(4 + kPGroups + g));  // the accumulator may be overwritten
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -624,6 +626,10 @@ void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int co
     if (sms <= 0) sms = 1;
   }
   const long long tiles = (long long)nbm * nbn * batch;
+  if (tiles > 0x7fffffffLL) {  // the kernel numbers tiles with 32-bit integers
+    if (err_flag) cudaMemsetAsync(err_flag, 0xff, sizeof(int), s);
+    return;
+  }
   const unsigned grid = unsigned(tiles < sms ? tiles : sms);
   KernelSpans& prof = tc_update_spans();
   cudaEvent_t e0 = nullptr, e1 = nullptr;
