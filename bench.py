@@ -218,7 +218,7 @@ def tc_update_c_bytes(n: int, m: int, E: int, nb: int = 64):
 
 
 def tc_update_traffic(E: int):
-    """DRAM bytes of all tc_update_kernel launches of one E-energy sweep, from the committed ncu capture
+    """DRAM bytes of all tc_update_persistent_kernel launches of one E-energy sweep, from the committed ncu capture
     (16-energy case, every launch) scaled by energies; None when the summary is absent."""
     p = ROOT / "profiles" / "tc_update_config1.md"
     if not p.exists():
@@ -347,7 +347,7 @@ def ours(args, world, rank, local):
     tc_gbs = c_bytes / (tc_ms / 1e3) / 1e9 if tc_ms > 0 else 0.0
     tc_tf = tc_flops / (tc_ms / 1e3) / 1e12 if tc_ms > 0 else 0.0
     traffic = tc_update_traffic(E)
-    roofline = {"bound": "hbm", "kernel": "tc_update_kernel", "achieved": tc_gbs, "peak": hbm,
+    roofline = {"bound": "hbm", "kernel": "tc_update_persistent_kernel", "achieved": tc_gbs, "peak": hbm,
                 "unit": "GB/s", "frac": tc_gbs / hbm, "peak_source": peak_kind,
                 "traffic": traffic / tc_launches if traffic else None,
                 "algorithmic_bytes_per_launch": c_bytes / max(tc_launches, 1),
