@@ -10,12 +10,11 @@
 // The operands are first written by tc_split_* into tile images that are
 // already in the UMMA shared-memory layout (K-major, 128-byte rows, 128-byte
 // swizzle), so the update kernel moves them with plain cp.async.bulk copies
-// completed on an mbarrier.  One CTA (4 warps) computes a 128 x 48 complex
-// tile: thread 0 issues copies and MMAs, all warps run the epilogue
-// (C prefetched into registers at entry, tcgen05.ld from TMEM, subtract and
-// store, coalesced along the rows).
+// completed on mbarriers.  The update runs as one persistent, warp-specialised
+// CTA per SM over 128 x 48 complex tiles (tc_update_persistent_kernel below).
 // Every wait on an mbarrier is bounded; on timeout the kernel records an error
-// flag, skips the epilogue, frees its tensor memory and returns.
+// flag, ends every role, waits for its copies and MMAs in flight, frees its
+// tensor memory and returns.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "cplx.cuh"
@@ -33,8 +32,6 @@ constexpr int B_PLANE = BN * 128; // bytes per B plane per chunk (6 KB)
 constexpr int A_PLANES = 4;       // re_hi, re_lo, im_hi, im_lo
 constexpr int B_PLANES = 6;       // re_hi, re_lo, im_hi, im_lo, -im_hi, -im_lo
 constexpr int SMEM_OPS = A_PLANES * A_PLANE + B_PLANES * B_PLANE;  // 100 KB
-constexpr int SMEM_BYTES = SMEM_OPS + 1024 + 64;                      // + alignment slack + barriers
-constexpr uint32_t TMEM_COLS = 128;  // Cr at column 0, Ci at column 64
 constexpr long long kWaitLimit = 1LL << 26;
 
 __device__ __forceinline__ uint32_t tf32_bits(float x) {
@@ -90,22 +87,6 @@ __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
-}
-
-// Bounded wait: gives up after kWaitLimit polls or one second, whichever comes first.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  const uint64_t t0 = global_ns();
-  for (long long it = 0; it < kWaitLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if ((it & 1023) == 1023 && global_ns() - t0 > 1000000000ull) return false;
-  }
-  return false;
 }
 
 __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
@@ -174,139 +155,6 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
     *reinterpret_cast<uint32_t*>(base + size_t(4) * B_PLANE + off) = s[2] ^ 0x80000000u;  // -im_hi
     *reinterpret_cast<uint32_t*>(base + size_t(5) * B_PLANE + off) = s[3] ^ 0x80000000u;  // -im_lo
   }
-}
-
-// ---------------------------------------------------------------------------
-// the update
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) tc_update_kernel(BatchLayout lay, int k, int kb, int col_end,
-                                                        float2* __restrict__ M, const uint8_t* __restrict__ aimg,
-                                                        const uint8_t* __restrict__ bimg, int nbm, int nbn,
-                                                        int* __restrict__ err_flag, const int* skip) {
-  const int bm = blockIdx.x, bn = blockIdx.y, b = blockIdx.z;
-  if (skip && skip[b]) return;
-  const int n = lay.n;
-  const int r0 = k + kb + bm * BM, c0 = k + kb + bn * BN;
-  if (r0 >= n || c0 >= col_end) return;
-  extern __shared__ uint8_t smraw[];
-  const uint32_t raw = smem_u32(smraw);
-  const uint32_t sbase = (raw + 1023u) & ~1023u;
-  uint8_t* const gbase = smraw + (sbase - raw);
-  const uint32_t sA = sbase;
-  const uint32_t sB = sbase + A_PLANES * A_PLANE;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + SMEM_OPS);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + SMEM_OPS + 16);
-  int* shared_err = reinterpret_cast<int*>(gbase + SMEM_OPS + 20);
-  const uint32_t bar_load = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-
-  // Every thread owns one row of the tile: its 48 C values are loaded now, so
-  // that their memory latency overlaps the operand copies and the MMAs.
-  const int row = r0 + warp * 32 + lane;
-  float2* Mb = M + size_t(b) * lay.stride;
-  float2 cv[BN];
-#pragma unroll
-  for (int j = 0; j < BN; ++j) {
-    const int col = c0 + j;
-    cv[j] = (row < n && col < col_end) ? Mb[size_t(row) + size_t(lay.lda) * col] : make_float2(0.f, 0.f);
-  }
-
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  if (tid == 0) {
-    mbar_init(bar_load, 1);
-    mbar_init(bar_mma, 1);
-    *shared_err = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
-  const uint32_t tmem_r = tmem, tmem_i = tmem + 64;
-
-  const int nchunks = kb > KC ? 2 : 1;
-  if (tid == 0) {
-    int bad = 0;
-    const uint8_t* ab = aimg + (size_t(b) * nbm + bm) * 2 * size_t(A_PLANES) * A_PLANE;
-    const uint8_t* bb = bimg + (size_t(b) * nbn + bn) * 2 * size_t(B_PLANES) * B_PLANE;
-    for (int ch = 0; ch < nchunks && !bad; ++ch) {
-      mbar_expect_tx(bar_load, uint32_t(SMEM_OPS));
-      const uint8_t* ach = ab + size_t(ch) * A_PLANES * A_PLANE;
-      const uint8_t* bch = bb + size_t(ch) * B_PLANES * B_PLANE;
-      for (int p = 0; p < A_PLANES; ++p) bulk_copy(sA + p * A_PLANE, ach + size_t(p) * A_PLANE, A_PLANE, bar_load);
-      for (int p = 0; p < B_PLANES; ++p) bulk_copy(sB + p * B_PLANE, bch + size_t(p) * B_PLANE, B_PLANE, bar_load);
-      if (!mbar_wait(bar_load, uint32_t(ch & 1))) { bad = 1; break; }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      for (int ks = 0; ks < KC / 8; ++ks) {
-        const uint32_t koff = uint32_t(ks * 32);  // 8 tf32 = 32 bytes along the swizzled row
-        auto ad = [&](int p) { return umma_desc_sw128(sA + p * A_PLANE + koff); };
-        auto bd = [&](int p) { return umma_desc_sw128(sB + p * B_PLANE + koff); };
-        const uint32_t acc0 = (ch == 0 && ks == 0) ? 0u : 1u;
-        // Cr += Ar Br + Ai (-Bi)
-        mma_tf32(tmem_r, ad(0), bd(0), acc0);
-        mma_tf32(tmem_r, ad(0), bd(1), 1u);
-        mma_tf32(tmem_r, ad(1), bd(0), 1u);
-        mma_tf32(tmem_r, ad(2), bd(4), 1u);
-        mma_tf32(tmem_r, ad(2), bd(5), 1u);
-        mma_tf32(tmem_r, ad(3), bd(4), 1u);
-        // Ci += Ar Bi + Ai Br
-        mma_tf32(tmem_i, ad(0), bd(2), acc0);
-        mma_tf32(tmem_i, ad(0), bd(3), 1u);
-        mma_tf32(tmem_i, ad(1), bd(2), 1u);
-        mma_tf32(tmem_i, ad(2), bd(0), 1u);
-        mma_tf32(tmem_i, ad(2), bd(1), 1u);
-        mma_tf32(tmem_i, ad(3), bd(0), 1u);
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_mma)
-                   : "memory");
-      if (!mbar_wait(bar_mma, uint32_t(ch & 1))) { bad = 1; break; }
-    }
-    if (bad) {
-      *shared_err = 1;
-      atomicExch(err_flag, 1);
-    }
-  }
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (*shared_err == 0) {
-    const uint32_t lane_off = uint32_t(warp * 32) << 16;
-#pragma unroll
-    for (int part = 0; part < BN / 16; ++part) {
-      uint32_t cr[16], ci[16];
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(cr[0]), "=r"(cr[1]), "=r"(cr[2]), "=r"(cr[3]), "=r"(cr[4]), "=r"(cr[5]), "=r"(cr[6]), "=r"(cr[7]),
-            "=r"(cr[8]), "=r"(cr[9]), "=r"(cr[10]), "=r"(cr[11]), "=r"(cr[12]), "=r"(cr[13]), "=r"(cr[14]),
-            "=r"(cr[15])
-          : "r"(tmem_r + lane_off + uint32_t(part * 16)));
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-          : "=r"(ci[0]), "=r"(ci[1]), "=r"(ci[2]), "=r"(ci[3]), "=r"(ci[4]), "=r"(ci[5]), "=r"(ci[6]), "=r"(ci[7]),
-            "=r"(ci[8]), "=r"(ci[9]), "=r"(ci[10]), "=r"(ci[11]), "=r"(ci[12]), "=r"(ci[13]), "=r"(ci[14]),
-            "=r"(ci[15])
-          : "r"(tmem_i + lane_off + uint32_t(part * 16)));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < n) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int col = c0 + part * 16 + j;
-          if (col < col_end) {
-            float2 v = cv[part * 16 + j];
-            v.x -= __uint_as_float(cr[j]);
-            v.y -= __uint_as_float(ci[j]);
-            Mb[size_t(row) + size_t(lay.lda) * col] = v;
-          }
-        }
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-  __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
 // ---------------------------------------------------------------------------
