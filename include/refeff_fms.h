@@ -466,6 +466,35 @@ int refeff_fms_plan_precond_features(refeff_fms_plan* plan, const refeff_fms_ene
 int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
                                      refeff_complex128* diag_out, int32_t* status_out);
 
+/* ---- reciprocal-space FMS (KKR integration of given structure factors) -- */
+
+/* One energy of FEFF kkrintegral (crates/refeff-core/src/fms/reciprocal.rs:67-223):
+ * for every k-point X_k = (I - G(k) T)^-1 G(k) (FmsReciprocalPlan::solve_k_point,
+ * solved on the GPU as one batch over the k-points), then the Brillouin-zone
+ * average sum_k w_k X_k / sum_k w_k (FmsReciprocalAccumulator).
+ *   structure_factors: n_kpoints x (order x order) complex, column-major (the
+ *     KSPACE structure factors G(k); this library does not compute them)
+ *   weights: n_kpoints positive finite weights
+ *   t_matrix: order x order lattice T (zeros skipped, as the reference plan does)
+ *   form: REFEFF_FMS_FORM_FP64_LU, or REFEFF_FMS_FORM_FP32_REFINED for order <= 64
+ *   green_out: order x order; status_out (optional): per k-point status
+ * Errors: INVALID_ARGUMENT (empty matrix, no k-point, a weight that is not
+ * positive and finite), NONFINITE_INPUT, SINGULAR_MATRIX (first failing
+ * k-point in last_error). */
+int refeff_fms_reciprocal_integrate(refeff_fms_context* ctx, int order, int n_kpoints,
+                                    const refeff_complex128* structure_factors, const double* weights,
+                                    const refeff_complex128* t_matrix, refeff_fms_form form,
+                                    refeff_complex128* green_out, int32_t* status_out);
+
+/* FEFF kkrintegral core-hole method 1 (fms_reciprocal_apply_core_hole,
+ * reciprocal.rs:236-302): G' = G - G[:, a] (I + C G_aa)^-1 C G[a, :] with
+ * a = [absorber_offset, absorber_offset + block) and C = t_difference
+ * (block x block, FEFF strength * (T_ground - T_core_hole)).  Host only, FP64.
+ * Errors: INVALID_ARGUMENT (block outside the matrix), NONFINITE_INPUT,
+ * SINGULAR_MATRIX (the Dyson matrix). */
+int refeff_fms_reciprocal_core_hole(int order, const refeff_complex128* green, int absorber_offset, int block,
+                                    const refeff_complex128* t_difference, refeff_complex128* out);
+
 /* ---- dense solve (refeff-linalg boundary) ----------------------------- */
 
 /* Batched dense complex solve A X = B, replacing complex32_faer_lu_factor +

@@ -26,6 +26,8 @@ from .fms import (  # noqa: F401
     mkgtr_trace,
     mkgtr_trace_device,
     read_phase_bin,
+    reciprocal_core_hole,
+    reciprocal_integrate,
     run_fms_in_dir,
     run_mkgtr_in_dir,
     transition_matrix,
@@ -41,7 +43,8 @@ __all__ = [
     "debye_sigma2_table", "ff2x_xanes_mu", "fms_full_scattering_spectrum",
     "fms_real_space_plan", "fms_real_space_spectrum", "fms_real_space_spectrum_device", "fms_real_space_spectrum_multi",
     "fms_yprep_cluster",
-    "gg_section", "load", "mkgtr_trace", "mkgtr_trace_device", "read_phase_bin", "run_fms_in_dir", "run_mkgtr_in_dir",
+    "gg_section", "load", "mkgtr_trace", "mkgtr_trace_device", "read_phase_bin", "reciprocal_core_hole",
+    "reciprocal_integrate", "run_fms_in_dir", "run_mkgtr_in_dir",
     "transition_matrix", "write_fms_bin", "write_gg_dat", "write_gg_diag_bin", "write_gg_slice_bin",
     "write_gtr_dat",
 ]

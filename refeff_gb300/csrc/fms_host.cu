@@ -14,6 +14,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -1622,6 +1623,259 @@ extern "C" int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_c
 // ---------------------------------------------------------------------------
 // dense batched solve
 // ---------------------------------------------------------------------------
+namespace {
+
+// [A | B] already in M64 (every system of the batch): solve and leave X in
+// ws.X64 (n x m per system, leading dimension lay.lda), statuses in ws.status
+// and first zero pivots in ws.info.  Asynchronous on stream s.
+int dense_solve_device(refeff_fms_context* ctx, Workspace& ws, int batch, bool fp32, cudaStream_t s) {
+  const BatchLayout& lay = ws.lay;
+  RF_CUDA(ctx, cudaMemsetAsync(ws.status.p, 0, size_t(batch) * sizeof(int), s));
+  RF_CUDA(ctx, cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s));
+  if (!fp32) {
+    cudaError_t e = lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<double>");
+    lu_backward_rhs<double>(ws.pc64, lay, batch, ws.M64.p, nullptr, s);
+    RF_CUDA(ctx, ws.X64.alloc(size_t(ws.batch) * lay.lda * lay.m));
+    launch_copy_rhs64(lay, batch, ws.M64.p, ws.X64.p, s);
+  } else {
+    launch_split_system(lay, batch, ws.M64.p, ws.M32.p, s);
+    cudaError_t e = lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<float>");
+    // M32's RHS columns hold Y32; refinement uses the hi/lo split system in M64
+    e = refine_fp32(ws, batch, ctx->dense_refinement, 1.0e-10, s);  // 0 corrections: the FP32 LU solution
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "refine");
+    count_launch();
+    status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
+  }
+  RF_CUDA(ctx, cudaGetLastError());
+  return REFEFF_FMS_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// KKR system of each k-point in place (fms reciprocal solve_k_point,
+// crates/refeff-core/src/fms/reciprocal.rs:103-134): with G(k) in the right-hand
+// side columns of [A | B], A = I - G(k) T, T given by its non-zero entries per
+// column (tcol_ptr / tcol_row / tcol_val, rows ascending as the reference
+// subtracts them).
+__global__ void kkr_system_kernel(BatchLayout lay, double2* __restrict__ M, const int* __restrict__ tcol_ptr,
+                                  const int* __restrict__ tcol_row, const double2* __restrict__ tcol_val) {
+  const int b = blockIdx.z, c = blockIdx.y, n = lay.n;
+  double2* Mb = M + size_t(b) * lay.stride;
+  const double2* G = Mb + size_t(lay.lda) * n;  // G(k) = B
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    double2 a = make_double2(r == c ? 1.0 : 0.0, 0.0);
+    for (int q = tcol_ptr[c]; q < tcol_ptr[c + 1]; ++q) a = csub(a, cmul(G[size_t(r) + size_t(lay.lda) * tcol_row[q]], tcol_val[q]));
+    Mb[size_t(r) + size_t(lay.lda) * c] = a;
+  }
+}
+
+// acc[r + n c] += sum over the batch (in k-point order) of w_b X_b[r, c] (FmsReciprocalAccumulator::push, reciprocal.rs:172-200).
+__global__ void kkr_accumulate_kernel(BatchLayout lay, int batch, const double2* __restrict__ X, const double* __restrict__ w,
+                                      double2* __restrict__ acc) {
+  const int n = lay.n;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n * n; idx += gridDim.x * blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    double2 s = acc[idx];
+    for (int b = 0; b < batch; ++b) {
+      const double2 x = X[size_t(b) * lay.lda * lay.m + size_t(r) + size_t(lay.lda) * c];
+      s.x = fma(w[b], x.x, s.x);
+      s.y = fma(w[b], x.y, s.y);
+    }
+    acc[idx] = s;
+  }
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_reciprocal_integrate(refeff_fms_context* ctx, int order, int n_kpoints,
+                                               const refeff_complex128* structure_factors, const double* weights,
+                                               const refeff_complex128* t_matrix, refeff_fms_form form,
+                                               refeff_complex128* green_out, int32_t* status_out) {
+  if (!ctx || !structure_factors || !weights || !t_matrix || !green_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  ctx->last_error.clear();
+  if (order <= 0) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "reciprocal FMS needs a nonempty square matrix");
+  if (n_kpoints <= 0) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "reciprocal FMS requires at least one k-point");
+  if (form != REFEFF_FMS_FORM_FP64_LU && form != REFEFF_FMS_FORM_FP32_REFINED)
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "unknown form");
+  const bool fp32 = form == REFEFF_FMS_FORM_FP32_REFINED;
+  if (fp32 && order > 64)
+    return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "the refined form solves at most 64 right-hand sides; use the FP64 LU");
+  const size_t nn = size_t(order) * order;
+  double total = 0.0;
+  for (int q = 0; q < n_kpoints; ++q) {
+    if (!std::isfinite(weights[q]) || !(weights[q] > 0.0))
+      return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "reciprocal FMS k-point weight must be positive and finite");
+    total += weights[q];
+  }
+  if (!std::isfinite(total) || !(total > 0.0))
+    return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "reciprocal FMS total k-point weight must be positive and finite");
+  for (size_t i = 0; i < nn * size_t(n_kpoints); ++i)
+    if (!std::isfinite(structure_factors[i].re) || !std::isfinite(structure_factors[i].im))
+      return fail(ctx, REFEFF_FMS_ERR_NONFINITE_INPUT, "non-finite structure factor");
+  // the lattice T by columns, non-zero entries only (FmsReciprocalPlan::new, reciprocal.rs:80-97)
+  std::vector<int> ptr(static_cast<size_t>(order) + 1, 0), rows;
+  std::vector<double2> vals;
+  for (int c = 0; c < order; ++c) {
+    for (int r = 0; r < order; ++r) {
+      const refeff_complex128 v = t_matrix[size_t(r) + size_t(order) * c];
+      if (!std::isfinite(v.re) || !std::isfinite(v.im)) return fail(ctx, REFEFF_FMS_ERR_NONFINITE_INPUT, "non-finite T");
+      if (v.re != 0.0 || v.im != 0.0) {
+        rows.push_back(r);
+        vals.push_back(make_double2(v.re, v.im));
+      }
+    }
+    ptr[size_t(c) + 1] = int(rows.size());
+  }
+  if (rows.empty()) {  // the reference's empty column lists: A = I
+    rows.push_back(0);
+    vals.push_back(make_double2(0.0, 0.0));
+  }
+  RF_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  Workspace ws;
+  const BatchLayout lay0 = make_layout(order, order);
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const size_t per = bytes_per_system(lay0, fp32) + size_t(lay0.lda) * order * sizeof(double2);
+  const int B = int(std::max<size_t>(1, std::min<size_t>(size_t(n_kpoints), std::min<size_t>(256, free_b / 2 / per))));
+  int rc = ensure_workspace(ctx, ws, order, order, B, fp32);
+  if (rc) return rc;
+  const BatchLayout& lay = ws.lay;
+  DevBuf<int> d_ptr, d_rows;
+  DevBuf<double2> d_vals, d_acc;
+  DevBuf<double> d_w;
+  RF_CUDA(ctx, d_ptr.upload(ptr.data(), ptr.size(), s));
+  RF_CUDA(ctx, d_rows.upload(rows.data(), rows.size(), s));
+  RF_CUDA(ctx, d_vals.upload(vals.data(), vals.size(), s));
+  RF_CUDA(ctx, d_w.upload(weights, size_t(n_kpoints), s));
+  RF_CUDA(ctx, d_acc.alloc(nn));
+  RF_CUDA(ctx, cudaMemsetAsync(d_acc.p, 0, nn * sizeof(double2), s));
+  std::vector<int> st(static_cast<size_t>(n_kpoints));
+  for (int k0 = 0; k0 < n_kpoints; k0 += B) {
+    const int nb = std::min(B, n_kpoints - k0);
+    RF_CUDA(ctx, cudaMemsetAsync(ws.M64.p, 0, size_t(nb) * lay.stride * sizeof(double2), s));
+    for (int b = 0; b < nb; ++b)
+      RF_CUDA(ctx, cudaMemcpy2DAsync(ws.M64.p + size_t(b) * lay.stride + size_t(lay.lda) * order,
+                                     size_t(lay.lda) * sizeof(double2), structure_factors + size_t(k0 + b) * nn,
+                                     size_t(order) * sizeof(double2), size_t(order) * sizeof(double2), size_t(order),
+                                     cudaMemcpyHostToDevice, s));
+    count_launch();
+    kkr_system_kernel<<<dim3(unsigned((order + 127) / 128), unsigned(order), unsigned(nb)), 128, 0, s>>>(
+        lay, ws.M64.p, d_ptr.p, d_rows.p, d_vals.p);
+    rc = dense_solve_device(ctx, ws, nb, fp32, s);
+    if (rc) return rc;
+    count_launch();
+    kkr_accumulate_kernel<<<unsigned(std::min<size_t>(1024, (nn + 255) / 256)), 256, 0, s>>>(lay, nb, ws.X64.p,
+                                                                                            d_w.p + k0, d_acc.p);
+    RF_CUDA(ctx, cudaMemcpyAsync(st.data() + k0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
+  std::vector<double2> acc(nn);
+  RF_CUDA(ctx, cudaMemcpyAsync(acc.data(), d_acc.p, nn * sizeof(double2), cudaMemcpyDeviceToHost, s));
+  int tc_timeout = 0;
+  if (ws.use_tc) RF_CUDA(ctx, cudaMemcpyAsync(&tc_timeout, ws.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RF_CUDA(ctx, cudaStreamSynchronize(s));
+  if (tc_timeout) return fail(ctx, REFEFF_FMS_ERR_CUDA, "tensor-core update timed out");
+  int first_bad = -1;
+  for (int q = 0; q < n_kpoints; ++q) {
+    const int code = map_status(st[size_t(q)]);
+    if (status_out) status_out[q] = code;
+    if (code != REFEFF_FMS_OK && first_bad < 0) first_bad = q;
+  }
+  if (first_bad >= 0)
+    return fail(ctx, map_status(st[size_t(first_bad)]),
+                "reciprocal KKR solve failed at k-point " + std::to_string(first_bad + 1));
+  // FmsReciprocalAccumulator::finish (reciprocal.rs:203-222)
+  for (size_t i = 0; i < nn; ++i) {
+    green_out[i] = {acc[i].x / total, acc[i].y / total};
+    if (!std::isfinite(green_out[i].re) || !std::isfinite(green_out[i].im))
+      return fail(ctx, REFEFF_FMS_ERR_NONFINITE_INPUT, "non-finite integrated Green matrix");
+  }
+  return REFEFF_FMS_OK;
+}
+
+namespace {
+
+// In-place partial-pivot LU solve of the small dense system A X = B (n x n,
+// n x m, column-major, FP64); false when a pivot is zero.
+bool small_lu_solve(int n, int m, std::vector<std::complex<double>>& A, std::vector<std::complex<double>>& B) {
+  using cd = std::complex<double>;
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double best = std::abs(A[size_t(k) + size_t(n) * k].real()) + std::abs(A[size_t(k) + size_t(n) * k].imag());
+    for (int r = k + 1; r < n; ++r) {
+      const cd v = A[size_t(r) + size_t(n) * k];
+      const double a = std::abs(v.real()) + std::abs(v.imag());
+      if (a > best) { best = a; p = r; }
+    }
+    if (!(best > 0.0)) return false;
+    if (p != k) {
+      for (int c = 0; c < n; ++c) std::swap(A[size_t(k) + size_t(n) * c], A[size_t(p) + size_t(n) * c]);
+      for (int c = 0; c < m; ++c) std::swap(B[size_t(k) + size_t(n) * c], B[size_t(p) + size_t(n) * c]);
+    }
+    const cd piv = A[size_t(k) + size_t(n) * k];
+    for (int r = k + 1; r < n; ++r) {
+      const cd l = A[size_t(r) + size_t(n) * k] / piv;
+      A[size_t(r) + size_t(n) * k] = l;
+      for (int c = k + 1; c < n; ++c) A[size_t(r) + size_t(n) * c] -= l * A[size_t(k) + size_t(n) * c];
+      for (int c = 0; c < m; ++c) B[size_t(r) + size_t(n) * c] -= l * B[size_t(k) + size_t(n) * c];
+    }
+  }
+  for (int c = 0; c < m; ++c)
+    for (int r = n - 1; r >= 0; --r) {
+      cd v = B[size_t(r) + size_t(n) * c];
+      for (int q = r + 1; q < n; ++q) v -= A[size_t(r) + size_t(n) * q] * B[size_t(q) + size_t(n) * c];
+      B[size_t(r) + size_t(n) * c] = v / A[size_t(r) + size_t(n) * r];
+    }
+  return true;
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_reciprocal_core_hole(int order, const refeff_complex128* green, int absorber_offset, int block,
+                                               const refeff_complex128* t_difference, refeff_complex128* out) {
+  using cd = std::complex<double>;
+  if (order <= 0 || !green || !t_difference || !out || absorber_offset < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (block <= 0 || absorber_offset + block > order) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  const size_t n = size_t(order), b = size_t(block), a = size_t(absorber_offset);
+  auto G = [&](size_t r, size_t c) { return cd(green[r + n * c].re, green[r + n * c].im); };
+  for (size_t i = 0; i < n * n; ++i)
+    if (!std::isfinite(green[i].re) || !std::isfinite(green[i].im)) return REFEFF_FMS_ERR_NONFINITE_INPUT;
+  std::vector<cd> C(b * b), dyson(b * b), eff(b * b);
+  for (size_t i = 0; i < b * b; ++i) {
+    C[i] = cd(t_difference[i].re, t_difference[i].im);
+    if (!std::isfinite(C[i].real()) || !std::isfinite(C[i].imag())) return REFEFF_FMS_ERR_NONFINITE_INPUT;
+  }
+  // dyson = I + C G_aa; effective T = dyson^-1 C (fms_reciprocal_apply_core_hole, reciprocal.rs:268-275)
+  for (size_t c = 0; c < b; ++c)
+    for (size_t r = 0; r < b; ++r) {
+      cd v = r == c ? cd(1.0, 0.0) : cd(0.0, 0.0);
+      for (size_t q = 0; q < b; ++q) v += C[r + b * q] * G(a + q, a + c);
+      dyson[r + b * c] = v;
+    }
+  eff = C;
+  if (!small_lu_solve(block, block, dyson, eff)) return REFEFF_FMS_ERR_SINGULAR_MATRIX;
+  // G - G[:, a] eff G[a, :] (reciprocal.rs:277-301)
+  std::vector<cd> left(n * b);
+  for (size_t c = 0; c < b; ++c)
+    for (size_t r = 0; r < n; ++r) {
+      cd v(0.0, 0.0);
+      for (size_t q = 0; q < b; ++q) v += G(r, a + q) * eff[q + b * c];
+      left[r + n * c] = v;
+    }
+  for (size_t c = 0; c < n; ++c)
+    for (size_t r = 0; r < n; ++r) {
+      cd v = G(r, c);
+      for (size_t q = 0; q < b; ++q) v -= left[r + n * q] * G(a + q, c);
+      if (!std::isfinite(v.real()) || !std::isfinite(v.imag())) return REFEFF_FMS_ERR_NONFINITE_INPUT;
+      out[r + n * c] = {v.real(), v.imag()};
+    }
+  return REFEFF_FMS_OK;
+}
+
 extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, int m, int batch,
                                                const refeff_complex128* A, const refeff_complex128* B,
                                                refeff_complex128* X, refeff_fms_form form, int32_t* status_out,
@@ -1646,25 +1900,8 @@ extern "C" int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, i
                                    size_t(lay.lda) * sizeof(double2), B + size_t(b) * n * m, size_t(n) * sizeof(double2),
                                    size_t(n) * sizeof(double2), size_t(m), cudaMemcpyHostToDevice, s));
   }
-  RF_CUDA(ctx, cudaMemsetAsync(ws.status.p, 0, size_t(batch) * sizeof(int), s));
-  RF_CUDA(ctx, cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s));
-  if (!fp32) {
-    cudaError_t e = lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<double>");
-    lu_backward_rhs<double>(ws.pc64, lay, batch, ws.M64.p, nullptr, s);
-    RF_CUDA(ctx, ws.X64.alloc(size_t(batch) * lay.lda * m));
-    launch_copy_rhs64(lay, batch, ws.M64.p, ws.X64.p, s);
-  } else {
-    launch_split_system(lay, batch, ws.M64.p, ws.M32.p, s);
-    cudaError_t e = lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "lu_eliminate<float>");
-    // M32's RHS columns hold Y32; refinement uses the hi/lo split system in M64
-    e = refine_fp32(ws, batch, ctx->dense_refinement, 1.0e-10, s);  // 0 corrections: the FP32 LU solution
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "refine");
-    count_launch();
-    status_not_converged_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.converged.p, ws.status.p);
-  }
-  RF_CUDA(ctx, cudaGetLastError());
+  rc = dense_solve_device(ctx, ws, batch, fp32, s);
+  if (rc) return rc;
   for (int b = 0; b < batch; ++b)
     RF_CUDA(ctx, cudaMemcpy2DAsync(X + size_t(b) * n * m, size_t(n) * sizeof(double2), ws.X64.p + size_t(b) * lay.lda * m,
                                    size_t(lay.lda) * sizeof(double2), size_t(n) * sizeof(double2), size_t(m),

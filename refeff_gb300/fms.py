@@ -100,6 +100,8 @@ def load(build_if_missing: bool = True):
         "refeff_fms_real_space_plan_create_full": ([_p, _p, _p], _i),
         "refeff_fms_real_space_spectrum_full": ([_p, _p, _p, _p, _p, _p, _p], _i),
         "refeff_fms_write_gg_slice_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
+        "refeff_fms_reciprocal_integrate": ([_p, _i, _i, _p, _p, _p, _i, _p, _p], _i),
+        "refeff_fms_reciprocal_core_hole": ([_i, _p, _i, _i, _p, _p], _i),
         "refeff_ff2x_xanes_mu": ([_i, _i, _i, _i, _i, _i, _p, _p, _p, _p, _p, C.c_double, C.c_double, C.c_double,
                                   _p, _p, _p], _i),
         "refeff_fms_write_gg_diag_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
@@ -552,6 +554,38 @@ def ff2x_xanes_mu(*, energy, ne1, fermi_index, omega, cross_section, background,
     if rc:
         raise FmsError(rc, "ff2x_xanes_mu")
     return mu, mu0, chi
+
+
+def reciprocal_integrate(ctx: Context, structure_factors, weights, t_matrix, form=FORM_FP64_LU,
+                         raise_on_error=True):
+    """Reciprocal-space FMS of one energy (crates/refeff-core/src/fms/reciprocal.rs:67-223): the weighted
+    k-point average of (I - G(k) T)^-1 G(k) on the GPU.  structure_factors: (K, n, n) complex; weights: (K,);
+    t_matrix: (n, n).  Returns (green (n, n), per-k-point status)."""
+    G = np.asarray(structure_factors, dtype=np.complex128)
+    K, n, _ = G.shape
+    g = np.ascontiguousarray(G.transpose(0, 2, 1))  # column-major per k-point
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    t = np.asfortranarray(t_matrix, dtype=np.complex128)
+    out = np.zeros((n, n), dtype=np.complex128, order="F")
+    st = np.zeros(K, np.int32)
+    rc = ctx._lib.refeff_fms_reciprocal_integrate(ctx.handle, n, K, _ptr(g), _ptr(w), _ptr(t), int(form), _ptr(out),
+                                                  _ptr(st))
+    if rc and raise_on_error:
+        raise FmsError(rc, ctx.last_error())
+    return np.array(out), st
+
+
+def reciprocal_core_hole(green, absorber_offset, t_difference):
+    """FEFF kkrintegral core-hole Dyson update (reciprocal.rs:236-302), host FP64."""
+    lib = load()
+    G = np.asfortranarray(green, dtype=np.complex128)
+    C = np.asfortranarray(t_difference, dtype=np.complex128)
+    n, b = G.shape[0], C.shape[0]
+    out = np.zeros((n, n), dtype=np.complex128, order="F")
+    rc = lib.refeff_fms_reciprocal_core_hole(n, _ptr(G), int(absorber_offset), b, _ptr(C), _ptr(out))
+    if rc:
+        raise FmsError(rc, "reciprocal core hole")
+    return np.array(out)
 
 
 def write_gg_slice_bin(path, values) -> None:

@@ -20,6 +20,7 @@ FMS_TESTS = "crates/refeff-core/src/fms/tests"
 LINALG_TESTS = "crates/refeff-linalg/src/tests.rs"
 GG_BIN = "crates/refeff-io/src/rhorrp_gg_bin.rs"
 XSCORR = "crates/refeff-core/src/xscorr.rs"
+RECIP = "crates/refeff-core/src/fms/tests/reciprocal.rs"
 
 
 def c(re_, im_, src):
@@ -267,6 +268,24 @@ KATS = {
         {"args": r([0.08, 0.0], f"{XSCORR}:154"), "want": r(0.5, f"{XSCORR}:154")},
         {"args": r([0.08, 0.22], f"{XSCORR}:155"), "want": r(0.8889827415450001, f"{XSCORR}:155")},
     ],
+    # Reciprocal-space FMS (kkrintegral): the inputs of the reference's identity tests; the expected values are
+    # the closed forms those tests assert (one-site resolvent average, scalar and 2x2 Dyson updates).
+    "reciprocal_one_site": {
+        "t": c(0.2, -0.1, f"{RECIP}:18"),
+        "structure_factors": [c(0.3, 0.05, f"{RECIP}:20"), c(-0.1, 0.2, f"{RECIP}:20")],
+        "weights": r([1.0, 3.0], f"{RECIP}:21"),
+        "tolerance": r(2.0e-6, f"{RECIP}:11"),
+    },
+    "reciprocal_core_hole_scalar": {
+        "green": c(0.4, 0.1, f"{RECIP}:40"),
+        "t_difference": c(-0.15, 0.08, f"{RECIP}:41"),
+    },
+    "reciprocal_core_hole_2x2": {
+        "green": [[c(0.4, 0.1, f"{RECIP}:58"), c(-0.2, 0.05, f"{RECIP}:58")],
+                  [c(0.3, -0.08, f"{RECIP}:59"), c(0.15, 0.2, f"{RECIP}:59")]],
+        "t_difference": [[c(-0.15, 0.08, f"{RECIP}:62"), c(0.06, 0.02, f"{RECIP}:62")],
+                         [c(-0.04, 0.03, f"{RECIP}:63"), c(0.11, -0.05, f"{RECIP}:63")]],
+    },
     # FEFF gg_slice.bin (ne 2, ldim 2, istate 3) and gg_diag.bin (ne 2, inclus 2, ldim 2): the reference
     # byte streams of the codec's own tests and the values they decode to; entry keys are the
     # (energy, row, column) and (energy, atom, row, column) indices.
