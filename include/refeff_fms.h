@@ -409,13 +409,23 @@ int refeff_fms_write_fms_bin(const char* path, double cluster_radius, int ne, in
  *   energy (ne, complex Hartree), omega (ne1 photon energies, Hartree),
  *   cross_section (ne complex), background (ne), trace (ne complex gtr(E)),
  *   real_correction: vrcorr in Hartree (contour shift and rescale)
+ *   imaginary_correction: the broadening in Hartree (vicorr, or half the core-hole width with
+ *     i_gamma_ch = 1; ff2x.rs:5416-5425); above 1e-4 (total, atomic) are Lorentz-broadened over
+ *     omega before normalisation (ff2x.rs:3265-3306, FMS-only spectra)
  *   mu, mu0, chi: ne1 each, optional.
- * The vicorr Lorentzian convolution, the sig_gk Debye factor and the thermal
- * xscorr are not applied. */
+ * The sig_gk Debye factor and the thermal xscorr are not applied. */
 int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
                          const refeff_complex128* energy, const double* omega, const refeff_complex128* cross_section,
                          const double* background, const refeff_complex128* trace, double s02, double real_correction,
-                         double fermi_photon_energy, double* mu, double* mu0, double* chi);
+                         double imaginary_correction, double fermi_photon_energy, double* mu, double* mu0,
+                         double* chi);
+
+/* FEFF conv (crates/refeff-core/src/convolution/lorentzian.rs:32-100): the
+ * piecewise-linear spectrum (n >= 2 points over increasing omega) broadened by
+ * a Lorentzian of half width `width`, divided by single-precision pi as FEFF
+ * does.  Host only. */
+int refeff_ff2x_lorentz_convolve(int n, const double* omega, const refeff_complex128* spectrum, double width,
+                                 refeff_complex128* out);
 
 int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* energy, const refeff_complex128* trace);
 

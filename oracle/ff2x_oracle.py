@@ -9,6 +9,8 @@ refeff_ff2x_xanes_mu; never shipped or called by the product.
   corrected components           crates/refeff-engine/src/ff2x.rs:3186-3262
   xmu.dat normalisation / rows   crates/refeff-engine/src/ff2x.rs:3309-3399
   locat / terp window / polint   crates/refeff-core/src/interpolation.rs:119-135, 338-446
+  vicorr broadening: conv1, conv crates/refeff-engine/src/ff2x.rs:3265-3306,
+                                 crates/refeff-core/src/convolution/lorentzian.rs:4-100
 
 Known answers pinned in tests/test_ff2x.py: the three lorenz and three astep values of
 crates/refeff-core/src/xscorr.rs:121-157 and the constant-cross-section xscorr case of
@@ -132,9 +134,44 @@ def xscorr(ispec, energy, ne1, fermi, xsec, bg, chia, vrcorr=0.0):
     return out
 
 
+PI_F32 = float(__import__("numpy").float32(math.pi))  # FEFF divides by the single-precision pi (convolution.rs:17)
+
+
+def conv1(x1, x2, y1, y2, x0, width):
+    """Lorentzian integral at x0 of the segment (x1, y1)-(x2, y2), per part (lorentzian.rs:4-30)."""
+    t = complex((x2 - x1) / 2.0, 0.0) / complex((x1 + x2) / 2.0 - x0, -width)
+
+    def part(slope, mid):
+        if abs(t) >= 0.1:
+            v = slope * 2.0 + (mid - slope / t) * cmath.log((1.0 + t) / (1.0 - t))
+        else:
+            v = mid * (2.0 * (t + t * t * t / 3.0)) - slope * (2.0 * t * t / 3.0)
+        return complex(v).imag
+    y1, y2 = complex(y1), complex(y2)
+    return complex(part((y2.real - y1.real) / 2.0, (y2.real + y1.real) / 2.0),
+                   part((y2.imag - y1.imag) / 2.0, (y2.imag + y1.imag) / 2.0))
+
+
+def conv(omega, spectrum, width):
+    """FEFF conv (lorentzian.rs:32-100): the spectrum extended past its last point, broadened at every omega."""
+    n = len(omega)
+    fs = omega[-1] - omega[-2]
+    ew = max(fs, 50.0 * width)
+    xlast = omega[-1] + ew
+    ylast = complex(spectrum[-1]) + (complex(spectrum[-1]) - complex(spectrum[-2])) * (ew / fs)
+    out = []
+    for x0 in omega:
+        s = 0j
+        for i in range(n - 1):
+            s += conv1(omega[i], omega[i + 1], spectrum[i], spectrum[i + 1], x0, width)
+        s += conv1(omega[-1], xlast, spectrum[-1], ylast, x0, width)
+        out.append(s / PI_F32)
+    return out
+
+
 def xanes_mu(*, energy, ne1, fermi, omega, cross_section, background, trace, s02=1.0, ispec=1, absolu=0,
-             include_atomic=True, vrcorr=0.0, fermi_photon_energy=0.0):
-    """(mu, mu0, chi) over the ne1 main rows (ff2x.rs:3186-3262 and 3309-3399, sig_gk = 0, no vicorr)."""
+             include_atomic=True, vrcorr=0.0, vicorr=0.0, fermi_photon_energy=0.0):
+    """(mu, mu0, chi) over the ne1 main rows (ff2x.rs:3186-3306 and 3309-3399, sig_gk = 0)."""
     ispec = abs(ispec)
     ne = len(energy)
     xsec = [complex(v) if include_atomic else 0j for v in cross_section]
@@ -145,11 +182,14 @@ def xanes_mu(*, energy, ne1, fermi, omega, cross_section, background, trace, s02
     if absolu != 1:
         at = fermi_photon_energy if ispec == 2 else fermi_photon_energy + 50.0 / HARTREE_EV
         norm = terp(list(omega[:ne1]), [float(b) for b in background[:ne1]], 1, at)
+    total = [(xsec[r] + chia[r] * float(background[r]) + tot[r]).imag for r in range(ne1)]
+    atomic = [(xsec[r] + atm[r]).imag if include_atomic else 0.0 for r in range(ne1)]
+    if vicorr > EPS4:
+        c = conv(list(omega[:ne1]), [complex(a, b) for a, b in zip(total, atomic)], vicorr)
+        total, atomic = [v.real for v in c], [v.imag for v in c]
     mu, mu0, chi = [], [], []
     for r in range(ne1):
-        total = (xsec[r] + chia[r] * float(background[r]) + tot[r]).imag
-        atomic = (xsec[r] + atm[r]).imag if include_atomic else 0.0
-        mu0.append(atomic / norm)
-        chi.append((total - atomic) / norm)
+        mu0.append(atomic[r] / norm)
+        chi.append((total[r] - atomic[r]) / norm)
         mu.append(mu0[-1] + chi[-1])
     return mu, mu0, chi

@@ -9,8 +9,11 @@
 //   lorenz, astep                          ff2x_xscorr_lorenz / _astep        5052-5076
 //   normalisation and mu0, chi, mu         ff2x_xanes_xmu_dat_from_components 3309-3399
 //   locat, terp / terpc window, polint     crates/refeff-core/src/interpolation.rs:119-135, 215-236, 338-446
-// The Lorentzian convolution by vicorr (3265-3306), the Debye factor sig_gk
-// and the thermal xscorr (4643-) are not part of this entry point.
+//   vicorr Lorentzian broadening          ff2x_xanes_apply_vicorr_convolution 3265-3306
+//   conv1 / conv                           crates/refeff-core/src/convolution/lorentzian.rs:4-100
+// The Debye factor sig_gk and the thermal xscorr (4643-) are not part of this
+// entry point.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <string>
@@ -93,6 +96,49 @@ cd lorenz(double xloss, double width, double dele) {
 }
 
 bool finite(cd z) { return std::isfinite(z.real()) && std::isfinite(z.imag()); }
+
+// FEFF divides the broadened spectrum by the single-precision pi
+// (crates/refeff-core/src/convolution.rs:17).
+constexpr double kPiF32 = double(float(3.14159265358979323846));
+
+// FEFF conv1: the Lorentzian (half width `width`) integral at x0 of the
+// straight segment from (x1, y1) to (x2, y2), per real and imaginary part, with
+// a series for short segments (|t| < 0.1).
+cd conv1(double x1, double x2, cd y1, cd y2, double x0, double width) {
+  const cd t = cd((x2 - x1) / 2.0, 0.0) / cd((x1 + x2) / 2.0 - x0, -width);
+  auto part = [&](double slope, double mid) {
+    const cd s(slope, 0.0), m(mid, 0.0);
+    const cd v = std::abs(t) >= 0.1 ? s * 2.0 + (m - s / t) * std::log((cd(1.0, 0.0) + t) / (cd(1.0, 0.0) - t))
+                                    : m * (2.0 * (t + t * t * t / 3.0)) - s * (2.0 * t * t / 3.0);
+    return v.imag();
+  };
+  return cd(part((y2.real() - y1.real()) / 2.0, (y2.real() + y1.real()) / 2.0),
+            part((y2.imag() - y1.imag()) / 2.0, (y2.imag() + y1.imag()) / 2.0));
+}
+
+// FEFF conv: the piecewise-linear spectrum over omega, extended past the last
+// point by max(last spacing, 50 width) along its last slope, broadened at
+// every omega.  False on bad input (fewer than two points, width <= 0, a
+// repeated last energy, non-finite values).
+bool lorentz_conv(const double* omega, const cd* y, size_t n, double width, std::vector<cd>& out) {
+  if (n < 2 || !(width > 0.0) || !std::isfinite(width)) return false;
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(omega[i]) || !finite(y[i])) return false;
+  const size_t last = n - 1, prev = n - 2;
+  const double fs = omega[last] - omega[prev];
+  if (fs == 0.0) return false;
+  const double ew = std::max(fs, 50.0 * width);
+  const double xlast = omega[last] + ew;
+  const cd ylast = y[last] + (y[last] - y[prev]) * (ew / fs);
+  out.assign(n, cd(0.0, 0.0));
+  for (size_t r = 0; r < n; ++r) {
+    cd sum(0.0, 0.0);
+    for (size_t i = 0; i + 1 < n; ++i) sum += conv1(omega[i], omega[i + 1], y[i], y[i + 1], omega[r], width);
+    sum += conv1(omega[last], xlast, y[last], ylast, omega[r], width);
+    out[r] = sum / kPiF32;
+  }
+  return true;
+}
 
 // Zero-temperature xscorr: cchi[row] (row < ne1) = the broadened xmu minus xmu,
 // xmu = xsec + chia * xsnorm.  The broadening is the arctangent step times the
@@ -201,11 +247,22 @@ int xscorr(int ispec, const cd* energy_in, size_t ne, size_t ne1, size_t fermi, 
 
 }  // namespace
 
+extern "C" int refeff_ff2x_lorentz_convolve(int n, const double* omega, const refeff_complex128* spectrum, double width,
+                                            refeff_complex128* out) {
+  if (n < 0 || (n > 0 && (!omega || !spectrum || !out))) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  std::vector<cd> y(static_cast<size_t>(n)), r;
+  for (int i = 0; i < n; ++i) y[size_t(i)] = cd(spectrum[i].re, spectrum[i].im);
+  if (!lorentz_conv(omega, y.data(), size_t(n), width, r)) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < n; ++i) out[i] = {r[size_t(i)].real(), r[size_t(i)].imag()};
+  return REFEFF_FMS_OK;
+}
+
 extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
                                     const refeff_complex128* energy, const double* omega,
                                     const refeff_complex128* cross_section, const double* background,
                                     const refeff_complex128* trace, double s02, double real_correction,
-                                    double fermi_photon_energy, double* mu, double* mu0, double* chi) {
+                                    double imaginary_correction, double fermi_photon_energy, double* mu, double* mu0,
+                                    double* chi) {
   const int is = ispec < 0 ? -ispec : ispec;  // ff2x_xmu_effective_ispec (ff2x.rs:1496-1502)
   if (ne <= 0 || ne1 <= 0 || ne1 >= ne || fermi_index < 0 || fermi_index >= ne1 || is < 1 || is > 2 || !energy ||
       !omega || !cross_section || !background || !trace || !std::isfinite(s02))
@@ -233,10 +290,23 @@ extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec,
   }
   for (size_t r = 0; r < n1; ++r)
     if (!finite(total_corr[r]) || !finite(atomic_corr[r])) return REFEFF_FMS_ERR_NONFINITE_INPUT;
+  std::vector<double> total(n1), atomic(n1);
   for (size_t r = 0; r < n1; ++r) {
-    const double total = (xsec[r] + chia[r] * background[r] + total_corr[r]).imag();
-    const double atomic = include_atomic ? (xsec[r] + atomic_corr[r]).imag() : 0.0;
-    const double m0 = atomic / norm, c = (total - atomic) / norm;
+    total[r] = (xsec[r] + chia[r] * background[r] + total_corr[r]).imag();
+    atomic[r] = include_atomic ? (xsec[r] + atomic_corr[r]).imag() : 0.0;
+  }
+  // vicorr broadening of (total, atomic) over the photon energies (FMS-only spectra, ff2x.rs:3265-3306)
+  if (imaginary_correction > kEps4) {
+    std::vector<cd> spec(n1), conv;
+    for (size_t r = 0; r < n1; ++r) spec[r] = cd(total[r], atomic[r]);
+    if (!lorentz_conv(omega, spec.data(), n1, imaginary_correction, conv)) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    for (size_t r = 0; r < n1; ++r) {
+      total[r] = conv[r].real();
+      atomic[r] = conv[r].imag();
+    }
+  }
+  for (size_t r = 0; r < n1; ++r) {
+    const double m0 = atomic[r] / norm, c = (total[r] - atomic[r]) / norm;
     if (mu0) mu0[r] = m0;
     if (chi) chi[r] = c;
     if (mu) mu[r] = m0 + c;

@@ -103,7 +103,8 @@ def load(build_if_missing: bool = True):
         "refeff_fms_reciprocal_integrate": ([_p, _i, _i, _p, _p, _p, _i, _p, _p], _i),
         "refeff_fms_reciprocal_core_hole": ([_i, _p, _i, _i, _p, _p], _i),
         "refeff_ff2x_xanes_mu": ([_i, _i, _i, _i, _i, _i, _p, _p, _p, _p, _p, C.c_double, C.c_double, C.c_double,
-                                  _p, _p, _p], _i),
+                                  C.c_double, _p, _p, _p], _i),
+        "refeff_ff2x_lorentz_convolve": ([_i, _p, _p, C.c_double, _p], _i),
         "refeff_fms_write_gg_diag_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
         "refeff_fms_real_space_plan_destroy": ([_p], None),
         "refeff_fms_plan_query": ([_p, _p, _p, _p, _p], _i),
@@ -534,7 +535,8 @@ def write_gg_dat(path, sections) -> None:
 
 
 def ff2x_xanes_mu(*, energy, ne1, fermi_index, omega, cross_section, background, trace, s02=1.0, ispec=1,
-                  absolu=0, include_atomic=True, real_correction=0.0, fermi_photon_energy=0.0):
+                  absolu=0, include_atomic=True, real_correction=0.0, imaginary_correction=0.0,
+                  fermi_photon_energy=0.0):
     """FF2X XANES mu(E) from the MKGTR trace (crates/refeff-engine/src/ff2x.rs:3186-3262, 3309-3399, 4437-4641):
     returns (mu, mu0, chi) over the ne1 main rows.  energy, cross_section, trace: ne complex; background: ne
     reals; omega: ne1 photon energies; all energies in Hartree.  Host only."""
@@ -550,7 +552,8 @@ def ff2x_xanes_mu(*, energy, ne1, fermi_index, omega, cross_section, background,
     mu, mu0, chi = (np.zeros(int(ne1)) for _ in range(3))
     rc = lib.refeff_ff2x_xanes_mu(ne, int(ne1), int(fermi_index), int(ispec), int(absolu), int(bool(include_atomic)),
                                   _ptr(e), _ptr(om), _ptr(xs), _ptr(bg), _ptr(tr), float(s02), float(real_correction),
-                                  float(fermi_photon_energy), _ptr(mu), _ptr(mu0), _ptr(chi))
+                                  float(imaginary_correction), float(fermi_photon_energy), _ptr(mu), _ptr(mu0),
+                                  _ptr(chi))
     if rc:
         raise FmsError(rc, "ff2x_xanes_mu")
     return mu, mu0, chi
@@ -586,6 +589,18 @@ def reciprocal_core_hole(green, absorber_offset, t_difference):
     if rc:
         raise FmsError(rc, "reciprocal core hole")
     return np.array(out)
+
+
+def ff2x_lorentz_convolve(omega, spectrum, width):
+    """FEFF conv (crates/refeff-core/src/convolution/lorentzian.rs:32-100), host only."""
+    lib = load()
+    om = np.ascontiguousarray(omega, dtype=np.float64)
+    y = np.ascontiguousarray(spectrum, dtype=np.complex128)
+    out = np.zeros_like(y)
+    rc = lib.refeff_ff2x_lorentz_convolve(int(om.shape[0]), _ptr(om), _ptr(y), float(width), _ptr(out))
+    if rc:
+        raise FmsError(rc, "ff2x_lorentz_convolve")
+    return out
 
 
 def write_gg_slice_bin(path, values) -> None:

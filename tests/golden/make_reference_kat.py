@@ -21,6 +21,7 @@ LINALG_TESTS = "crates/refeff-linalg/src/tests.rs"
 GG_BIN = "crates/refeff-io/src/rhorrp_gg_bin.rs"
 XSCORR = "crates/refeff-core/src/xscorr.rs"
 RECIP = "crates/refeff-core/src/fms/tests/reciprocal.rs"
+CONV = "crates/refeff-core/src/convolution/tests.rs"
 
 
 def c(re_, im_, src):
@@ -268,6 +269,20 @@ KATS = {
         {"args": r([0.08, 0.0], f"{XSCORR}:154"), "want": r(0.5, f"{XSCORR}:154")},
         {"args": r([0.08, 0.22], f"{XSCORR}:155"), "want": r(0.8889827415450001, f"{XSCORR}:155")},
     ],
+    # FEFF conv1 / conv on the convolution fixture (omega, spectrum), width 0.2, tolerance 1e-12.
+    "lorentz_conv": {
+        "omega": r([-2.0, -0.5, 0.25, 1.5, 3.0], f"{CONV}:13"),
+        "spectrum": [c(0.0, -0.2, f"{CONV}:15"), c(1.0, 0.3, f"{CONV}:16"), c(0.25, 0.8, f"{CONV}:17"),
+                     c(2.0, -0.1, f"{CONV}:18"), c(1.5, 0.5, f"{CONV}:19")],
+        "conv1_args": r([1, 2, 0.75, 0.2], f"{CONV}:69"),
+        "conv1": c(0.11548114784993968, 0.1374686458618049, f"{CONV}:73"),
+        "conv": [c(0.11859251775642239, -0.02108887292319812, f"{CONV}:83"),
+                 c(0.7780612100410474, 0.3262922950470956, f"{CONV}:84"),
+                 c(0.565152671501454, 0.5900533350655084, f"{CONV}:85"),
+                 c(1.6561626472085706, 0.10570908207293085, f"{CONV}:86"),
+                 c(1.4178395137621587, 0.5320419613503408, f"{CONV}:87")],
+        "tolerance": r(1.0e-12, f"{CONV}:5"),
+    },
     # Reciprocal-space FMS (kkrintegral): the inputs of the reference's identity tests; the expected values are
     # the closed forms those tests assert (one-site resolvent average, scalar and 2x2 Dyson updates).
     "reciprocal_one_site": {

@@ -28,6 +28,20 @@ def test_oracle_lorenz_astep_known_answers():
         assert abs(fo.astep(*case["args"]["value"]) - case["want"]["value"]) <= 1e-14
 
 
+def test_lorentz_convolution_known_answers():
+    """FEFF conv1 / conv on the reference fixture (crates/refeff-core/src/convolution/tests.rs:11-94), oracle and
+    product, at the reference's 1e-12."""
+    k = KAT["lorentz_conv"]
+    omega = k["omega"]["value"]
+    spec = [complex(*v["value"]) for v in k["spectrum"]]
+    tol = k["tolerance"]["value"]
+    i1, i2, x0, width = k["conv1_args"]["value"]
+    assert abs(fo.conv1(omega[i1], omega[i2], spec[i1], spec[i2], x0, width) - complex(*k["conv1"]["value"])) < tol
+    want = [complex(*v["value"]) for v in k["conv"]]
+    for got in (fo.conv(omega, spec, 0.2), fms.ff2x_lorentz_convolve(omega, spec, 0.2)):
+        assert max(abs(g - w) for g, w in zip(got, want)) < tol
+
+
 def _constant_fixture():
     """ff2x/tests.rs:5167-5195: three horizontal rows at Im 0.1, a contour (1.0, 0.02), (1.0, 0.05), (1.0, 0)."""
     energy = [0.9 + 0.1j, 1.0 + 0.1j, 1.1 + 0.1j, 1.0 + 0.02j, 1.0 + 0.05j, 1.0 + 0.0j]
@@ -75,23 +89,39 @@ def xanes_inputs(rng, ne1=60, n_contour=8, ispec=1):
                 fermi_photon=omega[fermi])
 
 
-@pytest.mark.parametrize("ispec,vrcorr,include_atomic,absolu",
-                         [(1, 0.0, True, 0), (2, 0.0, True, 0), (1, 0.5 / 27.211396, True, 0),
-                          (1, 0.0, False, 1), (-2, -0.4 / 27.211396, True, 0)])
-def test_product_matches_oracle(ispec, vrcorr, include_atomic, absolu):
+@pytest.mark.parametrize("ispec,vrcorr,include_atomic,absolu,vicorr",
+                         [(1, 0.0, True, 0, 0.0), (2, 0.0, True, 0, 0.0), (1, 0.5 / 27.211396, True, 0, 0.0),
+                          (1, 0.0, False, 1, 0.0), (-2, -0.4 / 27.211396, True, 0, 0.0),
+                          (1, 0.0, True, 0, 1.5 / 27.211396), (2, 0.3 / 27.211396, True, 0, 0.8 / 27.211396),
+                          (1, 0.0, False, 0, 0.8 / 27.211396)])
+def test_product_matches_oracle(ispec, vrcorr, include_atomic, absolu, vicorr):
     rng = np.random.default_rng(7 + ispec)
     d = xanes_inputs(rng)
     got = fms.ff2x_xanes_mu(energy=d["energy"], ne1=d["ne1"], fermi_index=d["fermi"], omega=d["omega"],
                             cross_section=d["xsec"], background=d["bg"], trace=d["trace"], s02=0.9, ispec=ispec,
                             absolu=absolu, include_atomic=include_atomic, real_correction=vrcorr,
-                            fermi_photon_energy=d["fermi_photon"])
+                            imaginary_correction=vicorr, fermi_photon_energy=d["fermi_photon"])
     want = fo.xanes_mu(energy=list(d["energy"]), ne1=d["ne1"], fermi=d["fermi"], omega=list(d["omega"]),
                        cross_section=list(d["xsec"]), background=list(d["bg"]), trace=list(d["trace"]), s02=0.9,
-                       ispec=ispec, absolu=absolu, include_atomic=include_atomic, vrcorr=vrcorr,
+                       ispec=ispec, absolu=absolu, include_atomic=include_atomic, vrcorr=vrcorr, vicorr=vicorr,
                        fermi_photon_energy=d["fermi_photon"])
     for g, w in zip(got, want):
         w = np.asarray(w)
         assert np.abs(g - w).max() <= 1e-12 * max(np.abs(w).max(), 1.0)
+
+
+def test_vrcorr_without_atomic_background_is_rejected():
+    """With the atomic background off, the atomic xscorr sees a zero Fermi-level xmu, which a vrcorr shift
+    cannot rescale: the reference bails there (ff2x.rs:4526-4529), and so do both restatements."""
+    d = xanes_inputs(np.random.default_rng(9))
+    with pytest.raises(fms.FmsError):
+        fms.ff2x_xanes_mu(energy=d["energy"], ne1=d["ne1"], fermi_index=d["fermi"], omega=d["omega"],
+                          cross_section=d["xsec"], background=d["bg"], trace=d["trace"], include_atomic=False,
+                          real_correction=0.3 / 27.211396, fermi_photon_energy=d["fermi_photon"])
+    with pytest.raises(ZeroDivisionError):
+        fo.xanes_mu(energy=list(d["energy"]), ne1=d["ne1"], fermi=d["fermi"], omega=list(d["omega"]),
+                    cross_section=list(d["xsec"]), background=list(d["bg"]), trace=list(d["trace"]),
+                    include_atomic=False, vrcorr=0.3 / 27.211396, fermi_photon_energy=d["fermi_photon"])
 
 
 def test_mu_is_affine_in_the_trace():
