@@ -791,8 +791,10 @@ PanelConfig choose_panel(int n) {
   PanelConfig pc;
   pc.cluster = 0;
   if (sizeof(T) == 4 && n >= 512) {
-    // two-level: 64-column blocks of 32- or 16-column cluster panels
-    for (int iw : {32, 16})
+    // two-level: 64-column blocks of 16- or 32-column cluster panels.  16 columns
+    // halve the shared memory of a panel, so twice as many panels (energies) are
+    // factored at once; the panel's column chain, not its arithmetic, bounds it.
+    for (int iw : {16, 32})
       if (fit_panel(8, iw, n, pc.inner_cluster, pc.inner_rpc, pc.inner_smem, pc.inner_pos_global)) {
         pc.nb = 64;
         pc.inner_nb = iw;
