@@ -768,9 +768,10 @@ void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* 
 // panels of at most 100 KB within a portable cluster (two CTAs per SM:
 // measured 3% faster elimination at n = 2256 than one CTA of up to 200 KB;
 // 16-CTA clusters were slower) and falling back to 200 KB and 16 CTAs.
-static bool fit_panel(int elem, int nb, int n, int& cluster, int& rpc, int& smem, int& pos_global) {
+static bool fit_panel(int elem, int nb, int n, int& cluster, int& rpc, int& smem, int& pos_global,
+                      bool global_first = false) {
   for (int pass = 0; pass < 2; ++pass)
-    for (int g = 0; g < (pass == 0 ? 1 : 2); ++g)  // bookkeeping in global memory only as the last resort
+    for (int g = global_first ? 1 : 0; g < (pass == 0 && !global_first ? 1 : 2); ++g)  // bookkeeping in global memory only as the last resort
       for (int cl = 1; cl <= (pass == 0 ? 8 : 16); cl *= 2) {
         const size_t budget = size_t(pass == 0 ? 100 : 200) * 1024;
         const int r = (n + cl - 1) / cl;
@@ -792,10 +793,13 @@ PanelConfig choose_panel(int n) {
   pc.cluster = 0;
   if (sizeof(T) == 4 && n >= 512) {
     // two-level: 64-column blocks of 16- or 32-column cluster panels.  16 columns
-    // halve the shared memory of a panel, so twice as many panels (energies) are
-    // factored at once; the panel's column chain, not its arithmetic, bounds it.
+    // halve the shared memory of a panel, and with the row bookkeeping in global
+    // scratch a 4-CTA panel takes 72 KB per CTA, three CTAs per SM: about three
+    // times as many panels (energies) are factored at once as with 32 columns
+    // and the bookkeeping in shared memory.  The panel's column chain, not its
+    // arithmetic, bounds it (measured at n = 2256: elimination 103.8 -> 90.8 ms).
     for (int iw : {16, 32})
-      if (fit_panel(8, iw, n, pc.inner_cluster, pc.inner_rpc, pc.inner_smem, pc.inner_pos_global)) {
+      if (fit_panel(8, iw, n, pc.inner_cluster, pc.inner_rpc, pc.inner_smem, pc.inner_pos_global, iw == 16)) {
         pc.nb = 64;
         pc.inner_nb = iw;
         pc.cluster = pc.inner_cluster;
