@@ -347,6 +347,8 @@ struct Workspace {
   // staging so that a captured graph can be replayed on every batch
   DevBuf<double2> k_stage, x_stage, gg_stage;
   DevBuf<double2> full_stage;  // save_gg_slice outputs of a batch (full plans)
+  DevBuf<double2> hank;        // pair prefactors and Hankel tables of a batch (pair_hankel_kernel)
+  DevBuf<int> hflag;
   std::map<int, cudaGraphExec_t> graphs;  // key: form * 65536 + energies in the batch
   std::map<int, unsigned long long> graph_launches;  // kernel launches per replay
   void drop_graphs() {
@@ -955,6 +957,10 @@ __global__ void status_not_converged_kernel(int batch, const int* converged, int
 cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, cudaStream_t s) {
   Workspace& ws = p.ws;
   const BatchLayout& lay = ws.lay;
+  BuildScratch bscratch;
+  bscratch.hank = ws.hank.p;
+  bscratch.hflag = ws.hflag.p;
+  const BuildScratch* bs = ws.hank.p && ws.hflag.p ? &bscratch : nullptr;
   cudaMemsetAsync(ws.status.p, 0, size_t(batch) * sizeof(int), s);
   cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s);
   const bool prof = p.profiling;
@@ -979,7 +985,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     // FEFF iterative forms: G0 and the per-state T table, then one CTA per
     // (energy, absorber column) runs the minv solver on W = I - T G0
     tick(0, [&] {
-      launch_build_g0(p.P, batch, ws.k_stage.p, lay, ws.M64.p, ws.status.p, s);
+      launch_build_g0(p.P, batch, ws.k_stage.p, lay, ws.M64.p, ws.status.p, s, bs);
       launch_t_table(p.P, batch, ws.x_stage.p, ws.t_tab.p, ws.status.p, s);
       return cudaGetLastError();
     });
@@ -991,7 +997,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     if (e != cudaSuccess) return e;
   } else if (form == REFEFF_FMS_FORM_FP64_LU) {
     tick(0, [&] {
-      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, nullptr, ws.status.p, s);
+      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, nullptr, ws.status.p, s, bs);
       return cudaGetLastError();
     });
     e = tick(1, [&] { return lu_eliminate<double>(ws.pc64, lay, batch, ws.M64.p, lu_work(ws, ws.pc64), s); });
@@ -1015,7 +1021,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     });
   } else if (form == REFEFF_FMS_FORM_BICGSTAB) {
     tick(0, [&] {
-      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, ws.M32.p, ws.status.p, s);
+      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, ws.M32.p, ws.status.p, s, bs);
       if (p.model) {
         // learned diagonal: features -> network -> D per state
         const MlpShape& sh = *model_shape(p.model);
@@ -1040,7 +1046,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
     });
   } else {
     tick(0, [&] {
-      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, ws.M32.p, ws.status.p, s);
+      launch_build_system(p.P, batch, ws.k_stage.p, ws.x_stage.p, lay, ws.M64.p, ws.M32.p, ws.status.p, s, bs);
       return cudaGetLastError();
     });
     e = tick(1, [&] { return lu_eliminate<float>(ws.pc32, lay, batch, ws.M32.p, lu_work(ws, ws.pc32), s); });
@@ -1091,6 +1097,7 @@ int pick_batch(refeff_fms_plan& p, int E, bool fp32) {
   const BatchLayout lay = make_layout(p.n, p.m);
   size_t per = bytes_per_system(lay, fp32);
   if (p.full) per += (size_t(lay.lda) * p.m + size_t(p.full_per)) * sizeof(double2);
+  per += build_scratch_entries(p.P, 1) * sizeof(double2) + size_t(p.N) * p.N * sizeof(int);
   const size_t budget = size_t(double(free_b) * 0.5);
   int b = int(std::max<size_t>(1, budget / std::max<size_t>(per, 1)));
   b = std::min(b, 256);
@@ -1120,6 +1127,8 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
   RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.gg_per));
   if (!fp32 && (p.blocks.size() > 1 || p.full)) RF_CUDA(ctx, ws.X64.alloc(size_t(ws.batch) * ws.lay.lda * p.m));
+  RF_CUDA(ctx, ws.hank.alloc(build_scratch_entries(p.P, ws.batch)));
+  RF_CUDA(ctx, ws.hflag.alloc(size_t(ws.batch) * p.N * p.N));
   if (p.full) {
     RF_CUDA(ctx, ws.full_stage.alloc(size_t(ws.batch) * p.full_per));
     RF_CUDA(ctx, p.d_full_all.alloc(size_t(E) * p.full_per));

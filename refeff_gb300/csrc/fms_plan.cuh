@@ -85,11 +85,18 @@ void launch_plan_df_tables(const PlanDev& P, cudaStream_t s);
 // ---- system build (per energy batch) ----
 // k: [E][nsp] double2; xphase: [E][nsp*(2L+1)*npot] double2 (column-major (nsp, 2L+1, npot)).
 // Writes A (= I - G0 T) and B (= G0[:, absorber]) into M64 (and a float copy into M32 if non-null).
+// With `scratch` (build_scratch_entries(P, E) entries of hank, E N^2 of hflag), the pair prefactors and
+// Hankel tables are computed for the whole batch by one kernel first; without it, inside the build CTAs.
+struct BuildScratch {
+  double2* hank = nullptr;
+  int* hflag = nullptr;
+};
+size_t build_scratch_entries(const PlanDev& P, int E);
 void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
-                         double2* M64, float2* M32, int* status, cudaStream_t s);
+                         double2* M64, float2* M32, int* status, cudaStream_t s, const BuildScratch* scratch = nullptr);
 // Plain free propagator G0 (FP64, device state order) into G0[e * lay.stride + r + lay.lda * c].
 void launch_build_g0(const PlanDev& P, int E, const double2* k, const BatchLayout& lay, double2* G0, int* status,
-                     cudaStream_t s);
+                     cudaStream_t s, const BuildScratch* scratch = nullptr);
 // T table per state: t[(e * n + state) * 2 + band], band 0 = T(0, .), 1 = T(1, .).
 void launch_t_table(const PlanDev& P, int E, const double2* xphase, double2* t, int* status, cudaStream_t s);
 

@@ -299,13 +299,91 @@ void launch_t_table(const PlanDev& P, int E, const double2* xphase, double2* t, 
   t_table_kernel<<<dim3(unsigned(P.N), unsigned(E)), 64, 0, s>>>(P, xphase, t, status);
 }
 
+// Per ordered pair (i, j) and wave number k: whether the pair scatters (i != j,
+// within rdirec), the pair prefactor e^{i rho}/rho e^{-msd k^2} and the Hankel
+// polynomial table xclmz(rho), clm(il, im) at c[il + (L+2) im] (pairs.rs:9-51,
+// polynomial.rs:8-83), in FP64; the refined form (kMode 1) stores them as
+// double-float pairs in the same 16 bytes.
+template <int kMode>
+__device__ __forceinline__ void pair_tables(const PlanDev& P, double2 k, int i, int j, double2* c, double2* pref,
+                                            int& ok, int* status_e) {
+  const int L = P.L, L1 = L + 1, rows = L + 2, N = P.N;
+  const size_t pij = size_t(j) + size_t(N) * i;
+  const double dist = P.pair_dist[pij];
+  ok = (i != j) && (dist * dist <= P.rdirec2);
+  if (!cfinite(k)) { atomicMax(status_e, int(kDevNonfinite)); ok = 0; }
+  if (!ok) return;
+  const double2 rho = make_double2(k.x * dist, k.y * dist);
+  if (rho.x == 0.0 && rho.y == 0.0) { atomicMax(status_e, int(kDevZeroRho)); ok = 0; return; }
+  const double msd = P.sigsqr[size_t(j) + size_t(N) * i];
+  // e^{i rho} / rho * e^{-msd k^2}
+  const double2 ph = cdiv(cexp(make_double2(-rho.y, rho.x)), rho);
+  const double2 k2 = cmul(k, k);
+  const double2 damp = cexp(make_double2(-msd * k2.x, -msd * k2.y));
+  *pref = cmul(ph, damp);
+  // xclmz recursion
+  const double2 z = cdiv(make_double2(0.0, -1.0), rho);
+  const double2 one = make_double2(1.0, 0.0);
+  for (int q = 0; q < rows * L1; ++q) c[q] = make_double2(0.0, 0.0);
+  c[0] = one;
+  if (L >= 1) c[1] = csub(one, z);
+  for (int il = 2; il <= L; ++il) {
+    const double2 f = cscale(z, double(2 * il - 1));
+    c[il] = csub(c[il - 2], cmul(f, c[il - 1]));
+  }
+  double2 cmm = one;
+  for (int im = 2; im <= L1; ++im) {
+    const int mmm = im - 1;
+    cmm = cmul(cneg(cmm), cscale(z, double(2 * mmm - 1)));
+    c[(im - 1) + rows * (im - 1)] = cmm;
+    const double2 oz = csub(one, cscale(z, double(im)));
+    c[im + rows * (im - 1)] = cmul(cscale(cmm, double(2 * im - 1)), oz);
+    for (int il = im + 1; il <= L; ++il) {
+      const double2 f = cscale(z, double(2 * il - 1));
+      c[il + rows * (im - 1)] =
+          csub(c[(il - 2) + rows * (im - 1)], cmul(f, cadd(c[(il - 1) + rows * (im - 1)], c[(il - 1) + rows * (im - 2)])));
+    }
+  }
+  if constexpr (kMode == 1) {
+    // the refined form works on double-float copies (same 16 bytes per entry)
+    for (int q = 0; q < rows * L1; ++q) reinterpret_cast<float4*>(c)[q] = split_hi_lo(c[q]);
+    *reinterpret_cast<float4*>(pref) = split_hi_lo(*pref);
+  }
+}
+
+// The pair tables of every (energy, ordered pair, spin) of a batch, one thread
+// each: hank[((e N + j) N + i) nsp + s] holds (L+2)(L+1) Hankel entries and the
+// prefactor, hflag[(e N + j) N + i] whether the pair scatters.  In the build
+// CTAs this FP64 work ran on one thread per pair while the others waited at a
+// barrier; here it fills the GPU and the build starts from finished tables.
+template <int kMode>
+__global__ void __launch_bounds__(256) pair_hankel_kernel(PlanDev P, int E, const double2* __restrict__ kE,
+                                                          double2* __restrict__ hank, int* __restrict__ hflag,
+                                                          int* __restrict__ status) {
+  const int N = P.N, nsp = P.nsp, per = (P.L + 2) * (P.L + 1) + 1;
+  const long long total = (long long)E * N * N * nsp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int s = int(t % nsp);
+    long long q = t / nsp;
+    const int i = int(q % N);
+    q /= N;
+    const int j = int(q % N);
+    const int e = int(q / N);
+    double2* c = hank + size_t(t) * per;
+    int ok = 0;
+    pair_tables<kMode>(P, kE[size_t(e) * nsp + s], i, j, c, c + (per - 1), ok, status + e);
+    if (s == 0) hflag[(size_t(e) * N + j) * N + i] = ok;
+  }
+}
+
 // kMode 0: FP64 system [A | B]; 1: the same as hi/lo float pairs plus the FP32
 // copy; 2: the plain free propagator G0 (FP64, n x n, for the iterative forms).
 template <int kMode>
 __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const double2* __restrict__ kE,
                                                            const double2* __restrict__ xph, BatchLayout lay,
                                                            double2* __restrict__ M64, float2* __restrict__ M32,
-                                                           int* __restrict__ status) {
+                                                           int* __restrict__ status, const double2* __restrict__ hank,
+                                                           const int* __restrict__ hflag) {
   extern __shared__ double sm[];
   const int L = P.L, L1 = L + 1, nsp = P.nsp, N = P.N;
   const int j = blockIdx.x;
@@ -394,56 +472,24 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
   }
   // ---- per (pair, spin): rho, prefactor, Hankel polynomial table ----
   const int rows = L + 2;
-  for (int t = tid; t < RA * nsp; t += nthr) {
-    const int p = t / nsp, s = t % nsp;
-    const int i = i0 + p;
-    const size_t pij = size_t(j) + size_t(N) * i;
-    const double dist = P.pair_dist[pij];
-    int ok = (i != j) && (dist * dist <= P.rdirec2);
-    const double2 k = ke[s];
-    if (!cfinite(k)) { atomicMax(status + e, int(kDevNonfinite)); ok = 0; }
-    double2* c = clm + size_t(t) * rows * L1;
-    if (ok) {
-      const double2 rho = make_double2(k.x * dist, k.y * dist);
-      if (rho.x == 0.0 && rho.y == 0.0) { atomicMax(status + e, int(kDevZeroRho)); ok = 0; }
-      else {
-        const double msd = P.sigsqr[size_t(j) + size_t(N) * i];
-        // e^{i rho} / rho * e^{-msd k^2}
-        const double2 ph = cdiv(cexp(make_double2(-rho.y, rho.x)), rho);
-        const double2 k2 = cmul(k, k);
-        const double2 damp = cexp(make_double2(-msd * k2.x, -msd * k2.y));
-        pref[t] = cmul(ph, damp);
-        // xclmz recursion, clm(il, im) at c[il + rows*im]
-        const double2 z = cdiv(make_double2(0.0, -1.0), rho);
-        const double2 one = make_double2(1.0, 0.0);
-        for (int q = 0; q < rows * L1; ++q) c[q] = make_double2(0.0, 0.0);
-        c[0] = one;
-        if (L >= 1) c[1] = csub(one, z);
-        for (int il = 2; il <= L; ++il) {
-          const double2 f = cscale(z, double(2 * il - 1));
-          c[il] = csub(c[il - 2], cmul(f, c[il - 1]));
-        }
-        double2 cmm = one;
-        for (int im = 2; im <= L1; ++im) {
-          const int mmm = im - 1;
-          cmm = cmul(cneg(cmm), cscale(z, double(2 * mmm - 1)));
-          c[(im - 1) + rows * (im - 1)] = cmm;
-          const double2 oz = csub(one, cscale(z, double(im)));
-          c[im + rows * (im - 1)] = cmul(cscale(cmm, double(2 * im - 1)), oz);
-          for (int il = im + 1; il <= L; ++il) {
-            const double2 f = cscale(z, double(2 * il - 1));
-            c[il + rows * (im - 1)] =
-                csub(c[(il - 2) + rows * (im - 1)], cmul(f, cadd(c[(il - 1) + rows * (im - 1)], c[(il - 1) + rows * (im - 2)])));
-          }
-        }
-        if constexpr (kMode == 1) {
-          // the refined form works on double-float copies (same 16 bytes per entry)
-          for (int q = 0; q < rows * L1; ++q) reinterpret_cast<float4*>(c)[q] = split_hi_lo(c[q]);
-          reinterpret_cast<float4*>(pref)[t] = split_hi_lo(pref[t]);
-        }
-      }
+  if (hank) {
+    // computed for the whole batch by pair_hankel_kernel: copy this CTA's 16 pairs
+    const int per = rows * L1 + 1;
+    const size_t t0 = (size_t(e) * N + j) * N + i0;
+    for (int idx = tid; idx < RA * nsp * per; idx += nthr) {
+      const int tl = idx / per, q = idx - tl * per;
+      const double2 v = hank[(t0 * nsp + tl) * per + q];
+      if (q < rows * L1) clm[size_t(tl) * rows * L1 + q] = v;
+      else pref[tl] = v;
     }
-    if (s == 0) flag[p] = ok;
+    for (int p = tid; p < RA; p += nthr) flag[p] = hflag[t0 + p];
+  } else {
+    for (int t = tid; t < RA * nsp; t += nthr) {
+      const int p = t / nsp, sp = t % nsp;
+      int ok = 0;
+      pair_tables<kMode>(P, ke[sp], i0 + p, j, clm + size_t(t) * rows * L1, pref + t, ok, status + e);
+      if (sp == 0) flag[p] = ok;
+    }
   }
   __syncthreads();
   // ---- z-axis propagator g(l1, l2, mu) per (pair, spin) (xgllm) ----
@@ -615,7 +661,7 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
 
 template <int kMode>
 static void launch_build_mode(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
-                              double2* M64, float2* M32, int* status, cudaStream_t s) {
+                              double2* M64, float2* M32, int* status, const BuildScratch* scratch, cudaStream_t s) {
   const BuildSmem b = build_smem_layout(P.L, P.nsp, P.ds);
   dim3 grid(unsigned(P.N), unsigned((P.N + kBuildRowAtoms - 1) / kBuildRowAtoms), unsigned(E));
   static int smem_set = 0;  // raised once to the largest request (before any stream capture)
@@ -623,19 +669,34 @@ static void launch_build_mode(const PlanDev& P, int E, const double2* k, const d
     cudaFuncSetAttribute(build_system_kernel<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
     smem_set = b.total_bytes;
   }
+  double2* hank = scratch ? scratch->hank : nullptr;
+  int* hflag = scratch ? scratch->hflag : nullptr;
+  if (hank && hflag) {
+    const long long work = (long long)E * P.N * P.N * P.nsp;
+    count_launch();
+    pair_hankel_kernel<kMode><<<unsigned(std::min<long long>(4096, (work + 255) / 256)), 256, 0, s>>>(P, E, k, hank,
+                                                                                                     hflag, status);
+  } else {
+    hank = nullptr;
+    hflag = nullptr;
+  }
   count_launch();
-  build_system_kernel<kMode><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, M32, status);
+  build_system_kernel<kMode><<<grid, 256, b.total_bytes, s>>>(P, k, xphase, lay, M64, M32, status, hank, hflag);
+}
+
+size_t build_scratch_entries(const PlanDev& P, int E) {
+  return size_t(E) * P.N * P.N * P.nsp * size_t((P.L + 2) * (P.L + 1) + 1);
 }
 
 void launch_build_system(const PlanDev& P, int E, const double2* k, const double2* xphase, const BatchLayout& lay,
-                         double2* M64, float2* M32, int* status, cudaStream_t s) {
-  if (M32) launch_build_mode<1>(P, E, k, xphase, lay, M64, M32, status, s);
-  else launch_build_mode<0>(P, E, k, xphase, lay, M64, nullptr, status, s);
+                         double2* M64, float2* M32, int* status, cudaStream_t s, const BuildScratch* scratch) {
+  if (M32) launch_build_mode<1>(P, E, k, xphase, lay, M64, M32, status, scratch, s);
+  else launch_build_mode<0>(P, E, k, xphase, lay, M64, nullptr, status, scratch, s);
 }
 
 void launch_build_g0(const PlanDev& P, int E, const double2* k, const BatchLayout& lay, double2* G0, int* status,
-                     cudaStream_t s) {
-  launch_build_mode<2>(P, E, k, nullptr, lay, G0, nullptr, status, s);
+                     cudaStream_t s, const BuildScratch* scratch) {
+  launch_build_mode<2>(P, E, k, nullptr, lay, G0, nullptr, status, scratch, s);
 }
 
 }  // namespace rfx
