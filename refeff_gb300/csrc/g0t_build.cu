@@ -318,9 +318,13 @@ __device__ __forceinline__ void pair_tables(const PlanDev& P, double2 k, int i, 
   const double msd = P.sigsqr[size_t(j) + size_t(N) * i];
   // e^{i rho} / rho * e^{-msd k^2}
   const double2 ph = cdiv(cexp(make_double2(-rho.y, rho.x)), rho);
-  const double2 k2 = cmul(k, k);
-  const double2 damp = cexp(make_double2(-msd * k2.x, -msd * k2.y));
-  *pref = cmul(ph, damp);
+  if (msd != 0.0) {
+    const double2 k2 = cmul(k, k);
+    const double2 damp = cexp(make_double2(-msd * k2.x, -msd * k2.y));
+    *pref = cmul(ph, damp);
+  } else {
+    *pref = ph;  // e^{0} = 1 exactly: the same value without the FP64 exponential
+  }
   // xclmz recursion
   const double2 z = cdiv(make_double2(0.0, -1.0), rho);
   const double2 one = make_double2(1.0, 0.0);
