@@ -111,9 +111,17 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     0 runs them on the CUDA cores.
  *   REFEFF_FMS_OPT_DENSE_REFINEMENT: corrections allowed in
  *     refeff_complex_lu_solve_batched with REFEFF_FMS_FORM_FP32_REFINED
- *     (default 10; 0 returns the plain FP32 LU solution, flagged NOT_CONVERGED). */
+ *     (default 10; 0 returns the plain FP32 LU solution, flagged NOT_CONVERGED).
+ *   REFEFF_FMS_OPT_TC_WAIT_POLLS: poll budget of each wait between the
+ *     roles of the tensor-core update (copy, MMA, epilogue); 0 restores the
+ *     default 2^26 (each wait also gives up after one second).  A wait that
+ *     gives up marks the call's tensor-core result void and every energy of
+ *     the call is solved again with the FP64 LU (status 0, same results as
+ *     REFEFF_FMS_FORM_FP64_LU; refeff_fms_last_error names the timeout).
+ *     Applies from the next solve call of every plan of the context. */
 #define REFEFF_FMS_OPT_TENSOR_CORES 1
 #define REFEFF_FMS_OPT_DENSE_REFINEMENT 2
+#define REFEFF_FMS_OPT_TC_WAIT_POLLS 3
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
 
 /* ---- cluster preparation (host) -------------------------------------- */
@@ -534,7 +542,10 @@ int refeff_complex_lu_solve_batched(refeff_fms_context* ctx, int n, int m, int b
  * d_A: batch x (n x n), d_B / d_X: batch x (n x m), column-major device
  * buffers (d_X must not overlap d_A or d_B); d_status / d_pivot (optional,
  * device, batch entries) receive the per-system status code and 1-based
- * first zero pivot.  Runs asynchronously on `stream` (NULL = legacy default
+ * first zero pivot.  Per-system failures (a singular or non-finite system)
+ * are reported through d_status only: the return code covers the arguments,
+ * the scratch limit and the launches, so a caller that passes no d_status
+ * gets no signal for a failed system.  Runs asynchronously on `stream` (NULL = legacy default
  * stream) on the calling thread's current device; results are ready when
  * the stream reaches them.  The scratch needed is about
  * batch * roundup(n, 32) * (n + m) * 16 bytes plus small pivot tables (one

@@ -823,19 +823,11 @@ template <typename T, int NB>
 static cudaError_t launch_panel(const PanelConfig& pc, const BatchLayout& lay, int batch, int k, cplx<T>* M,
                                 const LuWork& w, cudaStream_t s) {
   auto kern = panel_kernel<T, NB>;
-  // Attributes are raised once to the largest request (before any stream capture).
-  static int smem_set = 0;
-  static bool nonportable_set = false;
-  cudaError_t err;
-  if (pc.smem > smem_set) {
-    err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, pc.smem);
+  cudaError_t err = ensure_smem_limit(reinterpret_cast<const void*>(kern), size_t(pc.smem));
+  if (err != cudaSuccess) return err;
+  if (pc.cluster > 8) {
+    err = ensure_nonportable_clusters(reinterpret_cast<const void*>(kern));
     if (err != cudaSuccess) return err;
-    smem_set = pc.smem;
-  }
-  if (pc.cluster > 8 && !nonportable_set) {
-    err = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (err != cudaSuccess) return err;
-    nonportable_set = true;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(unsigned(pc.cluster), unsigned(batch), 1);
@@ -914,11 +906,7 @@ static void launch_gemm(const BatchLayout& lay, int batch, int r_begin, int r_en
   if (rows <= 0 || cols <= 0 || kb <= 0) return;
   const size_t smem = size_t(KMAX) * (BM + BN) * sizeof(cplx<T>);
   auto kern = gemm_update_kernel<T, TM, TN, KMAX>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    attr_set = true;
-  }
+  ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
   dim3 grid(unsigned((rows + BM - 1) / BM), unsigned((cols + BN - 1) / BN), unsigned(batch));
   count_launch();
   kern<<<grid, 256, smem, s>>>(lay, r_begin, r_end, c_begin, c_end, ka, kb, M, skip);
@@ -1018,11 +1006,7 @@ static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayo
       const int ncols = col_end - (k + kb);
       if (ncols > 0) {
         constexpr int smem = (64 * 64 + 2 * 64 * kLtN) * int(sizeof(float2));
-        static bool attr = false;  // raised once, before any stream capture
-        if (!attr) {
-          cudaFuncSetAttribute(rhs_lower_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-          attr = true;
-        }
+        ensure_smem_limit(reinterpret_cast<const void*>(rhs_lower_tile_kernel), size_t(smem));
         count_launch();
         rhs_lower_tile_kernel<<<dim3(unsigned((ncols + kLtN - 1) / kLtN), unsigned(batch)), 256, smem, s>>>(
             lay, k, k + kb, col_end, M, w, w.linv);
@@ -1030,7 +1014,7 @@ static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayo
     } else {
       launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
     }
-    if (w.tc_images) tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
+    if (w.tc_images) tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, w.tc_wait_polls, w.tc_spans, s);
     else gemm_any<float>(64, lay, batch, k + kb, n, k + kb, col_end, k, kb, M, nullptr, s);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
@@ -1055,7 +1039,7 @@ cudaError_t lu_eliminate(const PanelConfig& pc, const BatchLayout& lay, int batc
     rhs_lower_any<T>(pc.nb, lay, batch, k, k + kb, col_end, M, wl, nullptr, s);
     if constexpr (sizeof(T) == 4) {
       if (w.tc_images) {
-        tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, s);
+        tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, w.tc_wait_polls, w.tc_spans, s);
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         continue;
@@ -1114,11 +1098,7 @@ static void launch_residual_df(const BatchLayout& lay, int batch, const float4* 
                                unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
                                cudaStream_t s) {
   constexpr size_t smem = size_t(kRdK) * (kRdRows + kCols * kRdGroups) * sizeof(float4);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(residual_df_kernel<kCols>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    attr_set = true;
-  }
+  ensure_smem_limit(reinterpret_cast<const void*>(residual_df_kernel<kCols>), smem);
   dim3 grid(unsigned((lay.n + kRdRows - 1) / kRdRows), unsigned(batch));
   count_launch();
   residual_df_kernel<kCols><<<grid, 256, smem, s>>>(lay, Ms, Xs, R, rnorm_bits, bnorm_bits, skip);

@@ -30,19 +30,28 @@ inline int panel_count(int n, int nb) { return (n + nb - 1) / nb; }
 constexpr int kTcBM = 128, kTcBN = 48;
 // bytes of the operand tile images for a batch of systems of order n with m right-hand sides
 size_t tc_image_bytes(int n, int m, int batch);
-// CUDA events around every tensor-core update kernel while `on` (plan profiling).
+// CUDA events around every tensor-core update kernel of one plan while `on`
+// (plan profiling); each plan's workspace owns its own list.
 struct KernelSpans {
   bool on = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> spans;
 };
-KernelSpans& tc_update_spans();
+// Default poll budget of each mbarrier wait in the tensor-core update (the
+// waits also give up after one second of %globaltimer).
+constexpr long long kTcWaitPolls = 1LL << 26;
 // C -= L21 U12 for elimination step k with tcgen05 MMAs (split TF32, FP32 accumulation).
+// wait_polls bounds the waits of the producer, MMA and epilogue roles on each
+// other; the final waits for copies and MMAs still in flight keep the default
+// budget, so nothing is outstanding when a CTA exits.  spans (nullable)
+// records CUDA events around the kernel while spans->on.
 void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int col_end, float2* M, uint8_t* images,
-                        int* err_flag, const int* skip, cudaStream_t s);
+                        int* err_flag, const int* skip, long long wait_polls, KernelSpans* spans, cudaStream_t s);
 
 struct LuWork {
   uint8_t* tc_images = nullptr;  // operand images for the tensor-core update (FP32 only); null = CUDA cores
   int* tc_err = nullptr;         // set when a tensor-core wait timed out
+  long long tc_wait_polls = kTcWaitPolls;  // poll budget of the role waits in the tensor-core update
+  KernelSpans* tc_spans = nullptr;         // events around the tensor-core update launches (profiling)
   int* ipiv = nullptr;    // [batch][n]  LAPACK-style: row k+j was swapped with row ipiv
   int2* perm = nullptr;   // [batch][npanels][2*nb] (dst, src) row moves per panel
   int* nperm = nullptr;   // [batch][npanels]

@@ -19,6 +19,8 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -39,6 +41,49 @@ std::atomic<unsigned long long> g_launches{0};
 
 void rfx::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+namespace {
+std::mutex g_attr_mu;
+std::map<std::pair<int, const void*>, size_t> g_smem_limit;
+std::set<std::pair<int, const void*>> g_nonportable;
+std::map<int, int> g_sm_count;
+}  // namespace
+
+cudaError_t rfx::ensure_smem_limit(const void* kernel, size_t bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_attr_mu);
+  size_t& granted = g_smem_limit[{dev, kernel}];
+  if (bytes <= granted) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess) granted = bytes;
+  return e;
+}
+
+cudaError_t rfx::ensure_nonportable_clusters(const void* kernel) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_attr_mu);
+  if (g_nonportable.count({dev, kernel})) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess) g_nonportable.insert({dev, kernel});
+  return e;
+}
+
+int rfx::current_sm_count() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lock(g_attr_mu);
+  auto it = g_sm_count.find(dev);
+  if (it != g_sm_count.end()) return it->second;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 1;
+  g_sm_count[dev] = sms;
+  return sms;
+}
+
 extern "C" unsigned long long refeff_fms_kernel_launches(void) { return g_launches.load(); }
 
 // ---------------------------------------------------------------------------
@@ -51,6 +96,7 @@ struct refeff_fms_context {
   int sm_count = 0;
   int use_tensor_cores = 1;  // FP32 trailing updates on tcgen05 (REFEFF_FMS_OPT_TENSOR_CORES)
   int dense_refinement = 10; // corrections of the dense FP32 solve (REFEFF_FMS_OPT_DENSE_REFINEMENT)
+  long long tc_wait_polls = kTcWaitPolls;  // REFEFF_FMS_OPT_TC_WAIT_POLLS
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
   // the caller's handle plus one per live plan and model: the context is torn
   // down when the last of them is destroyed, in whatever order that happens
@@ -71,6 +117,10 @@ extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option
     case REFEFF_FMS_OPT_DENSE_REFINEMENT:
       if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
       ctx->dense_refinement = int(value);
+      return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_TC_WAIT_POLLS:
+      if (value < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+      ctx->tc_wait_polls = value == 0 ? kTcWaitPolls : value;
       return REFEFF_FMS_OK;
     default: return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   }
@@ -332,6 +382,8 @@ struct Workspace {
   bool use_tc = false;               // FP32 trailing update on the tensor cores
   DevBuf<uint8_t> tc_images;         // operand images of the tensor-core update
   DevBuf<int> tc_err;                // set by a tensor-core wait that timed out
+  long long tc_wait_polls = kTcWaitPolls;  // poll budget of the tensor-core update's role waits (baked into graphs)
+  KernelSpans tc_spans;              // events around this workspace's tensor-core updates (profiling)
   DevBuf<int2> perm;
   DevBuf<int2> perm_in;              // row moves of the inner panels (two-level FP32 LU)
   DevBuf<float2> linv;               // inverse of each outer block's unit lower L11 (two-level FP32 LU)
@@ -704,6 +756,10 @@ size_t bytes_per_system(const BatchLayout& lay, bool fp32) {
 
 int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32) {
   const BatchLayout lay = make_layout(n, m);
+  if (ws.tc_wait_polls != ctx->tc_wait_polls) {  // a kernel argument: captured graphs hold the old budget
+    ws.drop_graphs();
+    ws.tc_wait_polls = ctx->tc_wait_polls;
+  }
   if (ws.batch >= batch && ws.lay.n == n && ws.lay.m == m && (ws.fp32 || !fp32)) return REFEFF_FMS_OK;
   ws.drop_graphs();
   ws.batch = std::max(batch, ws.lay.n == n && ws.lay.m == m ? ws.batch : 0);
@@ -770,6 +826,8 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
   if (&pc == &ws.pc32 && ws.use_tc) {
     w.tc_images = ws.tc_images.p;
     w.tc_err = ws.tc_err.p;
+    w.tc_wait_polls = ws.tc_wait_polls;
+    w.tc_spans = &ws.tc_spans;
   }
   return w;
 }
@@ -965,7 +1023,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
   cudaMemsetAsync(ws.info.p, 0, size_t(batch) * sizeof(int), s);
   const bool prof = p.profiling;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> spans;
-  tc_update_spans().on = prof;
+  ws.tc_spans.on = prof;
   auto tick = [&](int phase, auto&& fn) -> cudaError_t {
     cudaEvent_t a = nullptr, b = nullptr;
     if (prof) {
@@ -1063,7 +1121,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
   }
   if (prof) {
     cudaStreamSynchronize(s);
-    KernelSpans& tc = tc_update_spans();
+    KernelSpans& tc = ws.tc_spans;
     for (auto& sp : tc.spans) spans.push_back({5, sp});
     tc.spans.clear();
     tc.on = false;

@@ -77,6 +77,18 @@ enum DevStatus : int {
 // launches replayed inside CUDA graphs) is reported by refeff_fms_kernel_launches.
 void count_launch();
 
+// Kernel attributes set with cudaFuncSetAttribute apply to the calling
+// thread's current device only, so every request is remembered per
+// (device, kernel) under a lock.  The first request for a pair must come
+// outside any stream capture: the library runs each batch shape un-captured
+// once before it captures it.
+// Raises the kernel's dynamic shared-memory limit to at least `bytes`.
+cudaError_t ensure_smem_limit(const void* kernel, size_t bytes);
+// Allows cluster sizes above the portable 8 CTAs for the kernel.
+cudaError_t ensure_nonportable_clusters(const void* kernel);
+// SM count of the current device (looked up once per device).
+int current_sm_count();
+
 // ---- geometry (once per plan) ----
 void launch_plan_geometry(const PlanDev& P, cudaStream_t s);
 // pair_dsmall_df / pair_eph_df from pair_dsmall / pair_eph (after launch_plan_geometry)

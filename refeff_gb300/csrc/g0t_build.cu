@@ -668,11 +668,7 @@ static void launch_build_mode(const PlanDev& P, int E, const double2* k, const d
                               double2* M64, float2* M32, int* status, const BuildScratch* scratch, cudaStream_t s) {
   const BuildSmem b = build_smem_layout(P.L, P.nsp, P.ds);
   dim3 grid(unsigned(P.N), unsigned((P.N + kBuildRowAtoms - 1) / kBuildRowAtoms), unsigned(E));
-  static int smem_set = 0;  // raised once to the largest request (before any stream capture)
-  if (b.total_bytes > smem_set) {
-    cudaFuncSetAttribute(build_system_kernel<kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize, b.total_bytes);
-    smem_set = b.total_bytes;
-  }
+  ensure_smem_limit(reinterpret_cast<const void*>(build_system_kernel<kMode>), size_t(b.total_bytes));
   double2* hank = scratch ? scratch->hank : nullptr;
   int* hflag = scratch ? scratch->hflag : nullptr;
   if (hank && hflag) {

@@ -491,12 +491,9 @@ template <typename R, int kMethod>
 cudaError_t launch_solve(const IterArgs& a, int batch, cudaStream_t s) {
   const size_t smem = (size_t(a.n) + kWarps + 1) * sizeof(cplx<R>);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  static size_t smem_set = 0;  // raised once to the largest request (before any stream capture)
-  if (smem > 48 * 1024 && smem > smem_set) {
-    cudaError_t e = cudaFuncSetAttribute(iterative_solve_kernel<R, kMethod>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (smem > 48 * 1024) {
+    cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(iterative_solve_kernel<R, kMethod>), smem);
     if (e != cudaSuccess) return e;
-    smem_set = smem;
   }
   count_launch();
   iterative_solve_kernel<R, kMethod><<<dim3(unsigned(a.m), unsigned(batch)), kThreads, smem, s>>>(a);

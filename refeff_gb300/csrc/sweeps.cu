@@ -203,13 +203,8 @@ bool launch_sweep_cg(bool forward, const BatchLayout& lay, int batch, float2* M,
   const size_t smem = SweepSmem<NB, CG>::bytes(lay.n);
   // each column group streams the whole triangle: decline narrow groups for many columns
   if (smem > kSwSmemBudget || CG < (lay.m < 4 ? lay.m : 4)) return false;
-  static size_t set_f = 0, set_b = 0;  // raised once to the largest request (before any stream capture)
-  size_t& set = forward ? set_f : set_b;
-  if (smem > set) {
-    if (forward) cudaFuncSetAttribute(fwd_sweep_kernel<NB, CG>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    else cudaFuncSetAttribute(bwd_sweep_kernel<NB, CG>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    set = smem;
-  }
+  if (forward) ensure_smem_limit(reinterpret_cast<const void*>(fwd_sweep_kernel<NB, CG>), smem);
+  else ensure_smem_limit(reinterpret_cast<const void*>(bwd_sweep_kernel<NB, CG>), smem);
   dim3 grid(unsigned((lay.m + CG - 1) / CG), unsigned(batch));
   count_launch();
   if (forward) fwd_sweep_kernel<NB, CG><<<grid, kSwThreads, smem, s>>>(lay, M, *w, skip);

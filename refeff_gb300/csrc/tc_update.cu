@@ -32,7 +32,7 @@ constexpr int B_PLANE = BN * 128; // bytes per B plane per chunk (6 KB)
 constexpr int A_PLANES = 4;       // re_hi, re_lo, im_hi, im_lo
 constexpr int B_PLANES = 6;       // re_hi, re_lo, im_hi, im_lo, -im_hi, -im_lo
 constexpr int SMEM_OPS = A_PLANES * A_PLANE + B_PLANES * B_PLANE;  // 100 KB
-constexpr long long kWaitLimit = 1LL << 26;
+constexpr long long kWaitLimit = kTcWaitPolls;  // drains of copies and MMAs in flight
 
 __device__ __forceinline__ uint32_t tf32_bits(float x) {
   uint32_t r;
@@ -183,9 +183,9 @@ constexpr uint32_t kPTmemCols = 512;  // kPGroups * 128 columns, rounded up to a
 constexpr int kPSmem = kPStages * SMEM_OPS + 1024 + 256;
 
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                                   int* err_flag) {
+                                                   int* err_flag, long long polls) {
   const uint64_t t0 = global_ns();
-  for (long long it = 0; it < kWaitLimit; ++it) {
+  for (long long it = 0; it < polls; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
@@ -214,7 +214,7 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
 __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
     BatchLayout lay, int k, int kb, int col_end, float2* __restrict__ M, const uint8_t* __restrict__ aimg,
     const uint8_t* __restrict__ bimg, int nbm_all, int nbn_all, int nbm, int nbn, int batch, int* __restrict__ err_flag,
-    const int* skip) {
+    const int* skip, long long polls) {
   extern __shared__ uint8_t smraw[];
   const uint32_t raw = smem_u32(smraw);
   const uint32_t sbase = (raw + 1023u) & ~1023u;
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
         for (int ch = 0; ch < nchunks; ++ch, ++c) {
           const int st = int(c % kPStages);
           const uint32_t ph = uint32_t((c / kPStages) & 1);
-          if (!mbar_wait_or_abort(bar(2 + st), ph ^ 1u, abort_flag, err_flag)) { ok = false; break; }
+          if (!mbar_wait_or_abort(bar(2 + st), ph ^ 1u, abort_flag, err_flag, polls)) { ok = false; break; }
           const uint32_t sA = sbase + uint32_t(st) * SMEM_OPS, sB = sA + A_PLANES * A_PLANE;
           mbar_expect_tx(bar(st), uint32_t(SMEM_OPS));
           const uint8_t* ach = ab + size_t(ch) * A_PLANES * A_PLANE;
@@ -312,14 +312,14 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
         tile_of(t, b, bm, bn);
         if (skip && skip[b]) continue;
         const int a = int(i % kPGroups);
-        if (!mbar_wait_or_abort(bar(4 + kPGroups + a), uint32_t(((i / kPGroups) & 1) ^ 1), abort_flag, err_flag))
+        if (!mbar_wait_or_abort(bar(4 + kPGroups + a), uint32_t(((i / kPGroups) & 1) ^ 1), abort_flag, err_flag, polls))
           break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t tmem_r = tmem + uint32_t(a * 128), tmem_i = tmem_r + 64;
         bool ok = true;
         for (int ch = 0; ch < nchunks; ++ch, ++c) {
           const int st = int(c % kPStages);
-          if (!mbar_wait_or_abort(bar(st), uint32_t((c / kPStages) & 1), abort_flag, err_flag)) { ok = false; break; }
+          if (!mbar_wait_or_abort(bar(st), uint32_t((c / kPStages) & 1), abort_flag, err_flag, polls)) { ok = false; break; }
           *(volatile int*)consumed = int(c + 1);
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sA = sbase + uint32_t(st) * SMEM_OPS, sB = sA + A_PLANES * A_PLANE;
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
 #pragma unroll
       for (int j = 0; j < 16; ++j)
         cn[j] = (row_ok && c0 + j < col_end) ? crow[j * ld] : make_float2(0.f, 0.f);
-      const bool ready = mbar_wait_or_abort(bar(4 + g), uint32_t((mine / kPGroups) & 1), abort_flag, err_flag);
+      const bool ready = mbar_wait_or_abort(bar(4 + g), uint32_t((mine / kPGroups) & 1), abort_flag, err_flag, polls);
       if (!__all_sync(0xffffffffu, ready)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tmem_r = tmem + uint32_t(g * 128) + lane_off, tmem_i = tmem_r + 64;
@@ -443,18 +443,13 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-KernelSpans& tc_update_spans() {
-  static KernelSpans spans;
-  return spans;
-}
-
 size_t tc_image_bytes(int n, int m, int batch) {
   const int nbm = (n + BM - 1) / BM, nbn = (n + m + BN - 1) / BN;
   return size_t(batch) * 2 * (size_t(nbm) * A_PLANES * A_PLANE + size_t(nbn) * B_PLANES * B_PLANE);
 }
 
 void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int col_end, float2* M, uint8_t* images,
-                        int* err_flag, const int* skip, cudaStream_t s) {
+                        int* err_flag, const int* skip, long long wait_polls, KernelSpans* spans, cudaStream_t s) {
   const int rows = lay.n - (k + kb), cols = col_end - (k + kb);
   if (rows <= 0 || cols <= 0 || kb <= 0) return;
   const int nbm_all = (lay.n + BM - 1) / BM, nbn_all = (lay.n + lay.m + BN - 1) / BN;
@@ -465,33 +460,28 @@ void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int co
   tc_split_a_kernel<<<dim3(unsigned(2 * nbm), unsigned(batch)), 256, 0, s>>>(lay, k, kb, M, aimg, nbm_all);
   count_launch();
   tc_split_b_kernel<<<dim3(unsigned(2 * nbn), unsigned(batch)), 256, 0, s>>>(lay, k, kb, col_end, M, bimg, nbn_all);
-  static int sms = 0;  // attributes and the SM count, once (before any stream capture)
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(tc_update_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmem);
-    if (sms <= 0) sms = 1;
-  }
+  const int sms = current_sm_count();
+  ensure_smem_limit(reinterpret_cast<const void*>(tc_update_persistent_kernel), size_t(kPSmem));
   const long long tiles = (long long)nbm * nbn * batch;
   if (tiles > 0x7fffffffLL) {  // the kernel numbers tiles with 32-bit integers
     if (err_flag) cudaMemsetAsync(err_flag, 0xff, sizeof(int), s);
     return;
   }
   const unsigned grid = unsigned(tiles < sms ? tiles : sms);
-  KernelSpans& prof = tc_update_spans();
+  const bool prof = spans && spans->on;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  if (prof.on) {
+  if (prof) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
   }
   count_launch();
   tc_update_persistent_kernel<<<grid, kPThreads, kPSmem, s>>>(lay, k, kb, col_end, M, aimg, bimg, nbm_all, nbn_all,
-                                                              nbm, nbn, batch, err_flag, skip);
-  if (prof.on) {
+                                                              nbm, nbn, batch, err_flag, skip,
+                                                              wait_polls > 0 ? wait_polls : kTcWaitPolls);
+  if (prof) {
     cudaEventRecord(e1, s);
-    prof.spans.push_back({e0, e1});
+    spans->spans.push_back({e0, e1});
   }
 }
 

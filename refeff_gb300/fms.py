@@ -189,6 +189,7 @@ class Context:
 
     OPT_TENSOR_CORES = 1
     OPT_DENSE_REFINEMENT = 2
+    OPT_TC_WAIT_POLLS = 3
 
     def set_option(self, option: int, value: int):
         """Context option (applies to plans / dense solves started afterwards)."""

@@ -65,6 +65,21 @@ def test_noalloc_matches_allocating_solve_twice(torch_cuda, n, m, batch):
     ctx.close()
 
 
+def test_noalloc_on_a_second_device(torch_cuda):
+    """The scratch address and the kernels' shared-memory limits are set up per device: a call with device 1
+    current must match the allocating solve on device 1 (skipped with one GPU)."""
+    if torch_cuda.cuda.device_count() < 2:
+        pytest.skip("one GPU")
+    with torch_cuda.cuda.device(1):
+        ctx = fms.Context(1)
+        A, B = _systems(21, 700, 16, 2)
+        X_ref, st_ref, _ = fms.complex_lu_solve_batched(ctx, A, B, fms.FORM_FP64_LU)
+        X, st, _ = _noalloc_solve(torch_cuda, A, B)
+        assert list(st) == [0, 0] and list(st_ref) == [0, 0]
+        assert np.abs(X - X_ref).max() <= TOL * np.abs(X_ref).max()
+        ctx.close()
+
+
 def test_noalloc_singular_system_status_matches(torch_cuda):
     ctx = fms.Context(0)
     A, B = _systems(9, 64, 2, 2)
