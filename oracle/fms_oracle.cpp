@@ -624,7 +624,7 @@ inline void t_matrix_table(const Plan<R>& P, const cx<R>* xphase, std::vector<cx
 // crates/refeff-core/src/fms/pairs.rs:242-323, 413-460, 519-553: the G0
 // matrix (column-major n x n), with rho/xclm per spin (pairs.rs:9-98).
 template <typename R>
-inline int free_propagator_matrix(const Plan<R>& P, const cx<R>* k, std::vector<cx<R>>& g0) {
+inline int free_propagator_matrix(const Plan<R>& P, const cx<R>* k, std::vector<cx<R>>& g0, int threads = 1) {
   const size_t n = P.n(), N = P.atoms.size();
   const int L = P.L, L1 = L + 1, D = 2 * L + 1;
   g0.assign(n * n, cx<R>());
@@ -659,7 +659,13 @@ inline int free_propagator_matrix(const Plan<R>& P, const cx<R>* k, std::vector<
     return xclm[((size_t(s) * N * N + a2 + N * a1) * L1 + size_t(l)) * L1 + size_t(m)];
   };
   R cutoff2 = P.rdirec * P.rdirec;
-  for (size_t col = 0; col < n; ++col) {
+  // Columns are independent; with threads > 1 they are shared out, and the
+  // first error code in column order is returned.
+  std::vector<int> col_err(n, OK);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(threads > 0 ? threads : 1)
+  for (long colv = 0; colv < long(n); ++colv) {
+    const size_t col = size_t(colv);
+    col_err[col] = [&]() -> int {
     const Ket& b = P.kets[col];
     for (size_t row = 0; row < n; ++row) {
       const Ket& a = P.kets[row];
@@ -699,7 +705,11 @@ inline int free_propagator_matrix(const Plan<R>& P, const cx<R>* k, std::vector<
       (void)D;
       g0[row + n * col] = free_propagator_prefactor(r, k[s], msd) * sum;
     }
+    return OK;
+    }();
   }
+  for (size_t col = 0; col < n; ++col)
+    if (col_err[col] != OK) return col_err[col];
   return OK;
 }
 
@@ -1487,6 +1497,58 @@ int oracle_fms_energy_intermediates(int mode, int n_atoms, const float* position
       for (size_t i = 0; i < n * n; ++i) st(a_out + 2 * i, A[i]);
     if (ait_out)
       for (size_t i = 0; i < n * n; ++i) st(ait_out + 2 * i, Ait[i]);
+    return OK;
+  };
+  return mode == 0 ? run(float(0)) : run(double(0));
+}
+
+// The dense system of one energy as the LU form solves it
+// (crates/refeff-core/src/fms/internals/linear.rs:102-135 and
+// solvers.rs:434-446): A = I - G0 T (n x n, column-major) and the absorber's
+// right-hand sides B = G0[:, off .. off + ipart) (n x ipart), for an
+// independent host solve.  With a_out null only n, off and ipart are set.
+// G0 columns are built on `threads` OpenMP threads.
+int oracle_fms_lu_system(int mode, int n_atoms, const float* positions, const int* pots, int nsp, int ispin,
+                         int global_lmax, const int* lmaxph, int npot, double rdirec, const float* sigsqr, double sig2g,
+                         const double* wave_numbers, const double* xphase, int threads, long* n_states,
+                         long* absorber_offset, long* absorber_width, double* a_out, double* b_out) {
+  std::vector<Atom> atoms(static_cast<size_t>(n_atoms));
+  for (int i = 0; i < n_atoms; ++i) { std::memcpy(atoms[size_t(i)].pos, positions + 3 * i, 12); atoms[size_t(i)].pot = pots[i]; }
+  auto run = [&](auto tag) -> int {
+    using R = decltype(tag);
+    Plan<R> P;
+    int rc = make_plan<R>(P, atoms.data(), n_atoms, nsp, ispin, 0, npot - 1, global_lmax, lmaxph, R(float(rdirec)),
+                          sigsqr, float(sig2g));
+    if (rc) return rc;
+    const size_t n = P.n();
+    const int lm = std::min(P.pot_lmax[0], P.L);
+    const size_t ipart = size_t(P.nsp) * size_t((lm + 1) * (lm + 1));
+    const size_t off = size_t(P.rep_offsets[0]);
+    *n_states = long(n);
+    *absorber_offset = long(off);
+    *absorber_width = long(ipart);
+    if (!a_out) return OK;
+    const size_t xph_sz = size_t(P.nsp) * size_t(2 * P.L + 1) * size_t(P.npot);
+    std::vector<cx<R>> k(static_cast<size_t>(P.nsp)), xp(xph_sz), g0, t;
+    for (int s = 0; s < P.nsp; ++s) k[size_t(s)] = ld<R>(wave_numbers + 2 * size_t(s));
+    for (size_t i = 0; i < xph_sz; ++i) xp[i] = ld<R>(xphase + 2 * i);
+    rc = free_propagator_matrix(P, k.data(), g0, threads);
+    if (rc) return rc;
+    t_matrix_table(P, xp.data(), t);
+    // A = I - G0 T written straight into the caller's buffer (lu_system_matrix's arithmetic, column by column)
+#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1)
+    for (long cv = 0; cv < long(n); ++cv) {
+      const size_t c = size_t(cv);
+      const long partner = P.nsp == 2 ? spin_partner_index(P.kets[c], long(c), long(n)) : -1;
+      for (size_t r = 0; r < n; ++r) {
+        cx<R> v = (-g0[r + n * c]) * t[size_t(P.nsp) * c];
+        if (partner >= 0) v -= g0[r + n * size_t(partner)] * t[1 + 2 * c];
+        if (r == c) v += cx<R>(R(1), R(0));
+        st(a_out + 2 * (r + n * c), v);
+      }
+    }
+    for (size_t c = 0; c < ipart; ++c)
+      for (size_t r = 0; r < n; ++r) st(b_out + 2 * (r + n * c), g0[r + n * (off + c)]);
     return OK;
   };
   return mode == 0 ? run(float(0)) : run(double(0));

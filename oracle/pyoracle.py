@@ -73,6 +73,7 @@ def _declare(L):
         "oracle_debye_correlation": [_i, _d, _d, _d, _i, _i, _d, _p, _p],
         "oracle_debye_waller": [_i, _d, _d, _d, _i, _p, _p, _p],
         "oracle_debye_sigma2_table": [_i, _i, _p, _p, _i, _p, _d, _d, _d, C.c_float, _p, _p],
+        "oracle_fms_lu_system": [_i, _i, _p, _p, _i, _i, _i, _p, _i, _d, _p, _d, _p, _p, _i, _p, _p, _p, _p, _p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -188,6 +189,34 @@ def fms_spectrum_iterative(positions, pots, lmaxph, wave_numbers, xphase, *, min
     return res if raise_on_error else (res, status)
 
 
+def iterative_order_spread(positions, pots, lmaxph, wave_numbers, xphase, *, minv, toler1, toler2, mode=F64,
+                           permutations=6, seed=0):
+    """How far the oracle's own iterative gg moves when the cluster's atoms are listed in another order (the
+    representatives of each potential kept in front, the rest shuffled): the same mathematics summed in another
+    order.  The FEFF iterative solvers stop on a residual estimate below toler1, so rounding differences move
+    their result by up to about toler1 (times the recurrences' amplification); this spread is the scale of any
+    faithful reimplementation's disagreement with the oracle.  Returns max |gg' - gg| / max |gg| over the
+    absorber block and the energies both runs solved."""
+    positions = np.asarray(positions, np.float32)
+    pots = np.asarray(pots, np.int32)
+    npot = len(lmaxph)
+    L = int(np.max(lmaxph))
+    m = (L + 1) ** 2
+    base, st0 = fms_spectrum_iterative(positions, pots, lmaxph, wave_numbers, xphase, minv=minv, toler1=toler1,
+                                       toler2=toler2, mode=mode, raise_on_error=False)
+    rng = np.random.default_rng(seed)
+    spread = 0.0
+    for _ in range(permutations):
+        perm = np.concatenate([np.arange(npot), npot + rng.permutation(len(pots) - npot)])
+        g, st = fms_spectrum_iterative(positions[perm], pots[perm], lmaxph, wave_numbers, xphase, minv=minv,
+                                       toler1=toler1, toler2=toler2, mode=mode, raise_on_error=False)
+        ok = [e for e in range(len(st)) if st[e] == 0 and st0[e] == 0]
+        if ok:
+            ref = np.abs(base[ok, :m, :m, 0]).max()
+            spread = max(spread, float(np.abs(g[ok, :m, :m, 0] - base[ok, :m, :m, 0]).max() / ref))
+    return spread
+
+
 def full_scattering(positions, pots, lmaxph, wave_numbers, xphase, *, nsp=1, ispin=0, global_lmax=None,
                     rdirec=1.0e6, sigsqr=None, sig2g=0.0, mode=F64):
     """Oracle save_gg_slice outputs for every energy: the full matrix X = (I - G0 T)^-1 G0 (FmsLuResult's
@@ -220,6 +249,31 @@ def full_scattering(positions, pots, lmaxph, wave_numbers, xphase, *, nsp=1, isp
         slices.append(X[:b, :].copy())
         diags.append(np.stack([X[i * b:(i + 1) * b, i * b:(i + 1) * b] for i in range(N)]))
     return np.array(slices), np.array(diags)
+
+
+def lu_system(positions, pots, lmaxph, wave_number, xphase, *, nsp=1, ispin=0, global_lmax=None, rdirec=1.0e6,
+              sigsqr=None, sig2g=0.0, mode=F64, threads=1):
+    """The dense system of one energy as the LU form solves it (crates/refeff-core/src/fms/internals/linear.rs:102-135,
+    solvers.rs:434-446): returns (A, B, off) with A = I - G0 T (n x n complex128, Fortran order), B = the absorber's
+    right-hand sides G0[:, off:off+w] (n x w), so that gg = solve(A, B)[off:off+w, :].  G0 is built on `threads`
+    OpenMP threads.  wave_number: (nsp,) complex; xphase: (nsp, 2L+1, npot) complex."""
+    positions = np.ascontiguousarray(positions, dtype=np.float32)
+    pots = np.ascontiguousarray(pots, dtype=np.int32)
+    lmaxph = np.ascontiguousarray(lmaxph, dtype=np.int32)
+    npot = len(lmaxph)
+    L = int(lmaxph.max()) if global_lmax is None else int(global_lmax)
+    kb = cbuf(np.asarray(wave_number).reshape(nsp))
+    xb = cbuf(np.asarray(xphase).reshape(nsp, 2 * L + 1, npot))
+    sig = None if sigsqr is None else np.asfortranarray(sigsqr, dtype=np.float32)
+    n, off, w = (np.zeros(1, np.int64) for _ in range(3))
+    args = [mode, len(pots), ptr(positions), ptr(pots), nsp, ispin, L, ptr(lmaxph), npot, float(rdirec), ptr(sig),
+            float(sig2g), ptr(kb), ptr(xb), int(threads), ptr(n), ptr(off), ptr(w)]
+    check(lib().oracle_fms_lu_system(*args, None, None))
+    ns, wd = int(n[0]), int(w[0])
+    A = np.zeros((ns, ns), dtype=np.complex128, order="F")
+    B = np.zeros((ns, wd), dtype=np.complex128, order="F")
+    check(lib().oracle_fms_lu_system(*args, ptr(A), ptr(B)))
+    return A, B, int(off[0])
 
 
 def lu_factor_solve(A, B, mode=F64):

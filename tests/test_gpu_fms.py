@@ -216,9 +216,10 @@ def test_fms_config0_subset_both_forms(ctx):
 
 
 def test_fms_config1_sample_against_oracle(ctx):
-    """fcc Cu <= 7.5 A (141 atoms, n = 2256, two-level cluster panels): 4 energies against the FP64 oracle."""
+    """fcc Cu <= 7.5 A (141 atoms, n = 2256, two-level cluster panels): 16 of the 200 energies against the FP64
+    oracle, weighted to the low end of the grid where k is smallest and the systems are worst conditioned."""
     cl, grid = wl.config1()
-    sel = np.array([0, 36, 120, 199])
+    sel = np.array([0, 1, 2, 3, 4, 6, 9, 14, 22, 36, 60, 90, 120, 150, 175, 199])
     plan, gpu64, ref, st64 = run_pair(ctx, cl, grid, fms.FORM_FP64_LU, energies=sel)
     assert plan.shape.n_states == 2256
     gpu32, st32 = fms.fms_real_space_spectrum(plan, grid.wave_numbers[sel], grid.phase_shifts[sel],

@@ -4,9 +4,11 @@ restatement (itself pinned to the reference's solver known answers, crates/refef
 These solvers stop once a residual estimate falls below toler1, and their recurrences amplify rounding: the
 oracle run on the same cluster with the atoms listed in another order (same mathematics, other summation
 order) already moves gg by up to ~1e-3 of max|gg| for gggm / ggtf at toler1 = 1e-3, ~4e-6 for ggrm, and
-~1e-16 for the single-step ggbi.  The GPU keeps the absorber last, so its tolerances are set from that
-spread (10x): ggbi 1e-9 (FP64) / 1e-5 (FP32); the others 1e-6 at toler1 = 1e-7, where all of them are
-converged, and 1e-2 at the reference default toler1 = 1e-3.
+~1e-16 for the single-step ggbi (tests/test_oracle_properties.py shows that this spread follows toler1).
+The GPU keeps the absorber last, so its tolerances are set from that spread: ggbi 1e-9 (FP64) / 1e-5 (FP32);
+the others 1e-6 at toler1 = 1e-7, where all of them are converged, and at the reference default
+toler1 = 1e-3 30x the spread measured on the same case and arithmetic (pyoracle.iterative_order_spread),
+capped at 1e-2.
 """
 import numpy as np
 import pytest
@@ -39,6 +41,13 @@ TOL64 = {1: (1.0e-3, 1.0e-9), 2: (1.0e-7, 1.0e-6), 3: (1.0e-7, 1.0e-6), 4: (1.0e
 
 def _rel(g, w, m):
     return np.abs(g[:, :m, :m, 0] - w[:, :m, :m, 0]).max() / np.abs(w[:, :m, :m, 0]).max()
+
+
+def _spread_gate(cl, grid, minv, toler1, toler2, mode):
+    """30x the oracle's own atom-order spread on this case, at most 1e-2 and at least 1e-9."""
+    spread = po.iterative_order_spread(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts,
+                                       minv=minv, toler1=toler1, toler2=toler2, mode=mode)
+    return min(1e-2, max(30.0 * spread, 1e-9))
 
 
 @pytest.mark.parametrize("minv", [1, 2, 3, 4])
@@ -85,7 +94,7 @@ def test_iterative_fp64_at_reference_tolerance(ctx, minv):
     want = po.fms_spectrum_iterative(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers, grid.phase_shifts,
                                      minv=minv, toler1=1.0e-3, toler2=1.0e-3, mode=po.F64)
     assert list(st) == [0] * len(st)
-    assert _rel(scat, want, m) <= 1e-2
+    assert _rel(scat, want, m) <= _spread_gate(cl, grid, minv, 1.0e-3, 1.0e-3, po.F64)
 
 
 @pytest.mark.parametrize("minv", [1, 2, 3, 4])
@@ -100,7 +109,7 @@ def test_iterative_fp32_matches_reference_precision_oracle(ctx, minv):
     both = [e for e in range(len(st)) if st[e] == 0 and ost[e] == 0]
     assert len(both) >= len(st) // 2
     assert all(st[e] in (0, 19) for e in range(len(st)))
-    bound = 1e-5 if minv == 1 else 1e-2
+    bound = 1e-5 if minv == 1 else _spread_gate(cl, grid, minv, 1.0e-3, 1.0e-3, po.F32)
     assert _rel(scat[both], want[both], m) <= bound
 
 
