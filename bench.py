@@ -6,9 +6,19 @@ systems, absorber block 16), seeded synthetic phase shifts.  The chosen form
 (complex FP32 LU + FP64 iterative refinement) is the headline `value`; the
 plain FP64 LU form is measured beside it on the same inputs.
 
+Beside the headline, one run also measures the chosen form against the plain
+FP64 LU on the batched, learned-preconditioner and large configurations (the
+`configs` key): 32 seeded fcc clusters in one call, the rocksalt cluster
+(n = 4112) and the random close packed cluster (n = 15000), each on a stated
+energy sample, with the largest relative gg error of the chosen form against
+the FP64 LU and the clocks seen while they ran.
+
 Contract: python bench.py --gpus N --steps K --warmup W [--impl reference]
 Prints one JSON line on rank 0.  Under torchrun each rank solves its own
 sweep (energy points are independent; weak scaling, no data-path collective).
+
+Profiling mode (a small repeatable case for ncu, no JSON line):
+    python bench.py --profile-case 1 --energies 16 --form fp32 --sweeps 2
 """
 from __future__ import annotations
 
@@ -217,16 +227,14 @@ def tc_update_c_bytes(n: int, m: int, E: int, nb: int = 64):
     return b * E
 
 
-def tc_update_traffic(E: int):
-    """DRAM bytes of all tc_update_persistent_kernel launches of one E-energy sweep, from the committed ncu capture
-    (16-energy case, every launch) scaled by energies; None when the summary is absent."""
-    p = ROOT / "profiles" / "tc_update_config1.md"
+def ncu_traffic(kernel: str):
+    """The ncu DRAM-traffic record of a kernel (profiles/ncu_traffic.json: dram__bytes_read.sum +
+    dram__bytes_write.sum of a small capture, per energy and per launch position, with the command that made
+    it); None when absent."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
     if not p.exists():
         return None
-    for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_sweep_per_energy:"):
-            return float(line.split(":")[1]) * E
-    return None
+    return json.loads(p.read_text()).get(kernel)
 
 
 def algorithmic(n: int, m: int, E: int):
@@ -236,6 +244,162 @@ def algorithmic(n: int, m: int, E: int):
         "build_bytes_fp32": E * n * n * 8.0,                     # c64 mirror for the FP32 LU
         "residual_bytes": E * n * n * 16.0,                      # one pass over A (c128) per residual
     }
+
+
+def cpu_lapack_run(cl, grid, threads: int, n_sample: int):
+    """A faer-class CPU figure for the same path: per energy the oracle builds the Complex32 system
+    A = I - G0 T and B = G0[:, absorber] (its f32-faithful arithmetic, G0 columns on all threads), then LAPACK's
+    blocked cgetrf / cgetrs (scipy's bundled OpenBLAS, all threads) factor and solve it, standing in for the
+    reference's faer PartialPivLu<Complex32> (crates/refeff-linalg/src/lu.rs:385-397)."""
+    import scipy.linalg as sla
+    from oracle import pyoracle as po
+    sel = np.arange(n_sample) * (grid.wave_numbers.shape[0] // n_sample)
+    t0 = time.perf_counter()
+    for e in sel:
+        A, B, off = po.lu_system(cl.positions, cl.potentials, cl.lmaxph, grid.wave_numbers[e], grid.phase_shifts[e],
+                                 mode=po.F32, threads=threads)
+        A32, B32 = np.asfortranarray(A, dtype=np.complex64), np.asfortranarray(B, dtype=np.complex64)
+        lu = sla.lu_factor(A32, overwrite_a=True, check_finite=False)
+        X = sla.lu_solve(lu, B32, check_finite=False)
+        _ = X[off:off + B.shape[1]]
+    dt = time.perf_counter() - t0
+    return n_sample / dt, dt
+
+
+def _rel_blocks(a, b, m):
+    """Largest relative Frobenius difference of the absorber blocks a[e, :m, :m, 0] against b (per energy)."""
+    return float(max(np.linalg.norm(a[e, :m, :m, 0] - b[e, :m, :m, 0]) / max(np.linalg.norm(b[e, :m, :m, 0]), 1e-300)
+                     for e in range(a.shape[0])))
+
+
+def _wall(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def _sample(E: int, count: int) -> np.ndarray:
+    return np.unique(np.linspace(0, E - 1, min(count, E)).round().astype(int))
+
+
+def config_batched(ctx, fms, wl, local):
+    """32 seeded displaced fcc clusters (n 171-1392), 150 energies each, every cluster in one host-buffer call;
+    both forms on all 4800 points (a full-size warm call first, then the median of three timed calls for the
+    chosen form and one for the FP64 LU)."""
+    cases = wl.config2()
+    plans = [fms.fms_real_space_plan(ctx, c.positions, c.potentials, c.lmaxph) for c, _ in cases]
+    ks = [g.wave_numbers for _, g in cases]
+    phs = [g.phase_shifts for _, g in cases]
+    pts = int(sum(len(k) for k in ks))
+    out = {"workload": "32 seeded displaced fcc clusters (a 3.5-4.1 A, sigma 0.05 A, R 4-7 A, lmax 2-3, "
+                       "2 potentials), 150 energies each, one host-buffer call per form",
+           "energy_points": pts, "n_min": min(p.shape.n_states for p in plans),
+           "n_max": max(p.shape.n_states for p in plans), "energy_sample": "all 150 energies of every cluster"}
+    sampler = ClockSampler(local)
+    fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED)
+    each = []
+    with sampler:
+        for _ in range(3):
+            (t32, s32), dt = _wall(lambda: fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED))
+            each.append(dt)
+    fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP64_LU)
+    (t64, s64), dt64 = _wall(lambda: fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP64_LU))
+    chosen = pts / float(np.median(each))
+    plain = pts / dt64
+    out.update({"chosen": {"value": chosen, "seconds_each": each}, "plain_fp64": {"value": plain, "seconds": dt64},
+                "chosen_over_plain": chosen / plain,
+                "max_rel_gg_err_vs_fp64": max(_rel_blocks(a, b, p.shape.absorber_block)
+                                              for a, b, p in zip(t32, t64, plans)),
+                "status_nonzero": int(sum(int((x != 0).sum()) for x in list(s32) + list(s64))),
+                "clocks": sampler.summary()})
+    for p in plans:
+        p.close()
+    return out
+
+
+def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, batch_plain, bicgstab_energies=0):
+    """One large cluster: the chosen form on an evenly spaced sample of n_chosen energies (in batches of
+    batch_chosen, one warm batch first) and the plain FP64 LU on an evenly spaced sub-sample of n_plain of
+    them (in batches of batch_plain, one warm batch first); the gg error is taken on the common energies."""
+    cl, grid = (wl.config3 if which == 3 else wl.config4)()
+    E = grid.wave_numbers.shape[0]
+    sel = _sample(E, n_chosen)
+    sub = sel[_sample(len(sel), n_plain)]
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    m = plan.shape.absorber_block
+    k, ph = grid.wave_numbers, grid.phase_shifts
+    sampler = ClockSampler(local)
+    plan.set_batch(batch_chosen)
+    fms.fms_real_space_spectrum(plan, k[sel[:batch_chosen]], ph[sel[:batch_chosen]], fms.FORM_FP32_REFINED)
+    with sampler:
+        (g32, s32), t32 = _wall(lambda: fms.fms_real_space_spectrum(plan, k[sel], ph[sel], fms.FORM_FP32_REFINED,
+                                                                    raise_on_error=False))
+    _, _, fb = plan.refinement_stats(len(sel))
+    plan.set_batch(batch_plain)
+    fms.fms_real_space_spectrum(plan, k[sub[:batch_plain]], ph[sub[:batch_plain]], fms.FORM_FP64_LU)
+    (g64, s64), t64 = _wall(lambda: fms.fms_real_space_spectrum(plan, k[sub], ph[sub], fms.FORM_FP64_LU,
+                                                                raise_on_error=False))
+    pos = {int(e): i for i, e in enumerate(sel)}
+    idx = np.array([pos[int(e)] for e in sub])
+    chosen, plain = len(sel) / t32, len(sub) / t64
+    out = {"n": plan.shape.n_states, "m": m,
+           "energy_sample": f"chosen on {len(sel)} of {E} energies evenly spaced (batches of {batch_chosen}), "
+                            f"FP64 LU on {len(sub)} of them (batches of {batch_plain}); "
+                            "points/s = sampled energies / wall time of the host-buffer call",
+           "chosen": {"value": chosen, "seconds": t32, "energies": int(len(sel)), "fp64_fallbacks": int(fb.sum())},
+           "plain_fp64": {"value": plain, "seconds": t64, "energies": int(len(sub))},
+           "chosen_over_plain": chosen / plain,
+           "max_rel_gg_err_vs_fp64": _rel_blocks(g32[idx], g64, m),
+           "status_nonzero": int((s32 != 0).sum() + (s64 != 0).sum()),
+           "clocks": sampler.summary()}
+    if bicgstab_energies:
+        bsel = sub[_sample(len(sub), bicgstab_energies)]
+        plan.set_batch(len(bsel))
+        fms.fms_real_space_spectrum(plan, k[bsel[:1]], ph[bsel[:1]], fms.FORM_BICGSTAB, raise_on_error=False)
+        (gb, sb), tb = _wall(lambda: fms.fms_real_space_spectrum(plan, k[bsel], ph[bsel], fms.FORM_BICGSTAB,
+                                                                 raise_on_error=False))
+        bidx = np.array([list(sub).index(int(e)) for e in bsel])
+        _, _, bfb = plan.refinement_stats(len(bsel))
+        out["bicgstab"] = {"value": len(bsel) / tb, "energies": int(len(bsel)),
+                           "over_plain": (len(bsel) / tb) / plain, "max_rel_gg_err_vs_fp64": _rel_blocks(gb, g64[bidx], m),
+                           "fp64_fallbacks": int(bfb.sum()), "status_nonzero": int((sb != 0).sum()),
+                           "note": "unpreconditioned batched BiCGSTAB inside the FP64 refinement"}
+    plan.close()
+    return out
+
+
+def configs_block(ctx, fms, wl, local):
+    return {
+        "2": config_batched(ctx, fms, wl, local),
+        "3": dict(workload="rocksalt AB a = 4.44 A, sigma 0.04 A, R 9 A (257 atoms), 3 potentials, lmax 3, "
+                           "300 energies -20..+100 eV",
+                  **config_single(ctx, fms, wl, local, 3, n_chosen=300, batch_chosen=150, n_plain=24, batch_plain=8,
+                                  bicgstab_energies=12)),
+        "4": dict(workload="random close packed binary cluster, 600 atoms, lmax 4, 400 energies -20..+300 eV",
+                  **config_single(ctx, fms, wl, local, 4, n_chosen=40, batch_chosen=20, n_plain=2, batch_plain=1)),
+    }
+
+
+def profile_case(args):
+    """A small repeatable FMS workload for ncu: one configuration, a given number of energies, one form, a given
+    number of sweeps (the first sweep of a batch size runs un-captured and captures the CUDA graph)."""
+    from refeff_gb300 import fms, workloads as wl
+    cl, grid = {0: wl.config0, 1: wl.config1, 3: wl.config3, 4: wl.config4}[args.profile_case]()
+    E = args.energies
+    form = {"fp32": fms.FORM_FP32_REFINED, "fp64": fms.FORM_FP64_LU, "bicgstab": fms.FORM_BICGSTAB}[args.form]
+    ctx = fms.Context(0)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    plan.set_batch(E)
+    status = None
+    for _ in range(args.sweeps):
+        _, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers[:E], grid.phase_shifts[:E], form,
+                                                raise_on_error=False)
+    print("ok", int((status != 0).sum()), "failed energies", flush=True)
+    plan.close()
+    ctx.close()
 
 
 def ours(args, world, rank, local):
@@ -346,7 +510,8 @@ def ours(args, world, rank, local):
     c_bytes = tc_update_c_bytes(n, m, E)
     tc_gbs = c_bytes / (tc_ms / 1e3) / 1e9 if tc_ms > 0 else 0.0
     tc_tf = tc_flops / (tc_ms / 1e3) / 1e12 if tc_ms > 0 else 0.0
-    traffic = tc_update_traffic(E)
+    tr = ncu_traffic("tc_update_persistent_kernel")
+    traffic = tr["dram_bytes_per_energy_per_sweep"] * E if tr else None
     roofline = {"bound": "hbm", "kernel": "tc_update_persistent_kernel", "achieved": tc_gbs, "peak": hbm,
                 "unit": "GB/s", "frac": tc_gbs / hbm, "peak_source": peak_kind,
                 "traffic": traffic / tc_launches if traffic else None,
@@ -355,8 +520,9 @@ def ours(args, world, rank, local):
                 "tensor_view": {"achieved": tc_tf, "unit": "TFLOP/s", "peak": bf16, "frac": tc_tf / bf16,
                                 "note": "useful complex-FP32 flops; split TF32 issues 3 tensor products per useful "
                                         "one at a TF32 rate half the bf16 peak (useful ceiling ~1/6 of it)"},
-                "traffic_note": "ncu DRAM bytes of all 35 launches of the 16-energy case, per launch, scaled by "
-                                "energies (profiles/tc_update_config1.md)",
+                "traffic_note": (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of {tr['captured']}, per energy, "
+                                 f"scaled to {E} energies and averaged over the sweep's launches (ncu_traffic.json)"
+                                 if tr else "no ncu record"),
                 "phase_ms": ph, "phase_achieved": phase_ach,
                 "refinement": {"corrections_max": int(iters.max()), "corrections_mean": float(iters.mean()),
                                "relres_max": float(relres.max()), "fp64_fallbacks": int(fallback.sum())}}
@@ -373,31 +539,11 @@ def ours(args, world, rank, local):
     h2d = int(k_h.nbytes + x_h.nbytes)
     d2h = int(E * m * m * 16 + E * 4)
 
-    # the many-cluster workload (32 seeded displaced fcc clusters, 150 energies each) through the one-call
-    # host API: every plan's energies in flight on the context's stream pool; one warm call, one timed call
-    multi = None
-    if not args.no_multi:
-        cases = wl.config2()
-        mplans = [fms.fms_real_space_plan(ctx, c.positions, c.potentials, c.lmaxph) for c, _ in cases]
-        mk = [g.wave_numbers for _, g in cases]
-        mph = [g.phase_shifts for _, g in cases]
-        fms.fms_real_space_spectrum_multi(mplans, mk, mph, fms.FORM_FP32_REFINED)
-        each = []
-        for _ in range(3):
-            barrier(world)
-            t0 = time.perf_counter()
-            _, msts = fms.fms_real_space_spectrum_multi(mplans, mk, mph, fms.FORM_FP32_REFINED)
-            each.append(max_over_ranks(time.perf_counter() - t0, world))
-        m_s = float(np.median(each))
-        pts = sum(len(x) for x in mk)
-        sizes = [p.shape.n_states for p in mplans]
-        multi = {"workload": "32 seeded displaced fcc clusters (a 3.5-4.1 A, R 4-7 A, lmax 2-3), 150 energies each, "
-                             "one host-buffer call (median of 3)", "value": world * pts / m_s, "unit": UNIT, "seconds": m_s,
-                 "seconds_each": each,
-                 "energy_points": pts, "n_min": min(sizes), "n_max": max(sizes),
-                 "status_nonzero": int(sum(int((x != 0).sum()) for x in msts))}
-        for p in mplans:
-            p.close()
+    plan.close()
+    # the batched, learned-preconditioner and large configurations: chosen vs plain FP64 LU with gg error
+    configs = None
+    if not args.no_configs:
+        configs = configs_block(ctx, fms, wl, local)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -407,6 +553,14 @@ def ours(args, world, rank, local):
         v, dt = cpu_baseline_run(cl, grid, threads, n_sample)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n_sample} of the 200 energies, f32-faithful oracle (reference arithmetic), {dt:.1f} s"}
+        try:
+            lv, ldt = cpu_lapack_run(cl, grid, threads, 8)
+            cpu["lapack"] = {"value": lv, "unit": UNIT, "cores": threads,
+                             "sample": f"8 of the 200 energies, {ldt:.1f} s: oracle Complex32 system build "
+                                       "(G0 columns on all threads) + LAPACK cgetrf/cgetrs (scipy, all threads)",
+                             "note": "a faer-class CPU LU standing in for the reference's PartialPivLu<Complex32>"}
+        except ImportError as exc:
+            cpu["lapack"] = {"unavailable": str(exc)}
 
     if rank == 0:
         clocks = sampler.summary()
@@ -429,11 +583,10 @@ def ours(args, world, rank, local):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
-            "many_clusters": multi,
+            "configs": configs,
             "clocks": clocks,
         }
         print(json.dumps(out), flush=True)
-    plan.close()
     ctx.close()
 
 
@@ -445,8 +598,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-multi", action="store_true", help="skip the many-cluster figure")
+    ap.add_argument("--no-configs", action="store_true", help="skip the batched / learned / large configurations")
+    ap.add_argument("--profile-case", type=int, choices=[0, 1, 3, 4], default=None,
+                    help="profiling mode: run one small case (no JSON line)")
+    ap.add_argument("--energies", type=int, default=16, help="profiling mode: energies of the case")
+    ap.add_argument("--form", default="fp32", choices=["fp32", "fp64", "bicgstab"], help="profiling mode: form")
+    ap.add_argument("--sweeps", type=int, default=2, help="profiling mode: sweeps")
     args = ap.parse_args()
+    if args.profile_case is not None:
+        profile_case(args)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         reference_arm(args, world, rank)
