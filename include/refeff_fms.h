@@ -320,8 +320,33 @@ int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_complex128* 
  * solved with the FP64 LU whatever `form` asks (the reference forces the LU
  * form) and gg_slice.bin and gg_diag.bin are written too (fms.rs:1113-1125).
  * Supported: idwopt < 0 (uniform sig2g), 0 and 3 (Debye models); other idwopt
- * values return REFEFF_FMS_ERR_UNSUPPORTED. */
+ * values return REFEFF_FMS_ERR_UNSUPPORTED.  A work directory without
+ * geom.dat but with feff.inp gets its cluster from feff.inp, through the same
+ * geom.dat text FEFF's rdinp would have written (refeff_fms_write_geom_dat). */
 int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir, refeff_fms_form form, refeff_fms_report* report);
+
+/* The cluster of a feff.inp as FEFF's rdinp hands it to the FMS stage: the
+ * ATOMS rows (x y z ipot, fields after '*' ignored) read with FEFF's line rules
+ * (full-line comments ; * % #, inline comments ! # % outside delimiters,
+ * BWORDS fields, block cards, INCLUDE / LOAD, END; crates/refeff-io/src/input.rs:64-372,
+ * model.rs:626-676), scaled by RMULTIPLIER (model.rs:198-207), moved so the
+ * absorber (the first atom of potential 0, else the first atom) sits at the
+ * origin as row 0, coincident atoms dropped, and ordered by FEFF's strict
+ * selection sort on the fused distance z*z + (x*x + y*y)
+ * (crates/refeff-io/src/rdinp/geometry.rs:18-88).  model_atoms_out gets the
+ * one-based first row of each potential (iatph, geometry.rs:90-119).
+ * xyz_out: row_capacity x 3 doubles; ipot_out: row_capacity; model_atoms_out:
+ * model_capacity.  With both capacities 0 only the counts are returned.
+ * LATTICE / CIF clusters, OVERLAP shells and the NRIXS frame rotation return
+ * REFEFF_FMS_ERR_UNSUPPORTED; the reason is in refeff_fms_feff_inp_last_error. */
+int refeff_fms_geometry_from_feff_inp(const char* feff_inp_path, int row_capacity, double* xyz_out, int32_t* ipot_out,
+                                      int32_t* n_rows, int model_capacity, int32_t* model_atoms_out,
+                                      int32_t* n_model);
+/* geom.dat for that cluster, byte-compatible with rdinp's write_geom_dat
+ * (crates/refeff-io/src/rdinp/structure.rs:57-81). */
+int refeff_fms_write_geom_dat(const char* feff_inp_path, const char* geom_dat_path);
+/* Message of the last failing feff.inp call on this thread ("" if none). */
+const char* refeff_fms_feff_inp_last_error(void);
 
 /* gg.dat / gg.bin writer (gg_dat_bytes, crates/refeff-io/src/gg_dat.rs:174-202):
  * n_sections square dim x dim complex blocks (column-major), section numbers

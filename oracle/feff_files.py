@@ -16,10 +16,15 @@ FEFF work directories and check the product's gg.bin / gg.dat byte for byte.
   gtr.dat text        crates/refeff-io/src/gtr_dat.rs:60-71
   gg_slice.bin        crates/refeff-io/src/rhorrp_gg_bin.rs:99-160
   gg_diag.bin         crates/refeff-io/src/rhorrp_gg_bin.rs:178-252
+  feff.inp -> geom    crates/refeff-io/src/input.rs:146-372 (lines, comments, BWORDS),
+                      crates/refeff-io/src/model.rs:626-676 (ATOMS / POTENTIALS rows),
+                      crates/refeff-io/src/rdinp/geometry.rs:18-119 (rows, ffsort, iatph),
+                      crates/refeff-io/src/rdinp/structure.rs:57-81 (write_geom_dat)
 """
 from __future__ import annotations
 
 import math
+from fractions import Fraction
 from pathlib import Path
 
 import numpy as np
@@ -357,3 +362,146 @@ def reference_engine_fixture(path: Path):
     write_workdir(path, positions=[[0, 0, 0], [1.4, 0, 0]], potentials=[0, 1], lmaxph=[1, 1], energy_grid=grid,
                   phase_potentials=pots, rfms2=3.0, rdirec=5.0,
                   global_kw={"polarization_tensor": np.eye(3) / 3.0})
+
+
+# ---- feff.inp -> geometry rows (rdinp) ----
+
+_BLOCKS = {"ATOMS", "POTENTIALS", "OVERLAP", "LATTICE", "EGRID", "DENSITY", "CONFIG", "STRETCHES", "ANGLES", "ELNES",
+           "EXELFS", "NRIXS", "MDFF"}
+_CANON = {"ATOM": "ATOMS", "CONF": "CONFIG", "DENS": "DENSITY", "ELNE": "ELNES", "EXEL": "EXELFS", "EGRI": "EGRID",
+          "LATT": "LATTICE", "MDFF": "MDFF", "NRIX": "NRIXS", "OVER": "OVERLAP", "POTE": "POTENTIALS", "TITL": "TITLE"}
+
+
+def fma(a: float, b: float, c: float) -> float:
+    """Correctly rounded a*b + c (the exact value through rationals, rounded once)."""
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+def _strip_inline(line: str) -> str:
+    opens, closes = "[{\"'(", "]}\"')"
+    prot = None
+    for i, ch in enumerate(line):
+        if prot is not None:
+            if ch == closes[prot]:
+                prot = None
+            continue
+        if ch in opens:
+            prot = opens.index(ch)
+            continue
+        if ch in "!#%":
+            return line[:i]
+    return line
+
+
+def _bwords(line: str):
+    words, start, comma = [], None, True
+    for i, ch in enumerate(line):
+        if ch in " \t":
+            if start is not None:
+                words.append(line[start:i])
+                start, comma = None, False
+        elif ch == ",":
+            if start is not None:
+                words.append(line[start:i])
+                start = None
+            elif comma:
+                words.append("")
+            comma = True
+        elif start is None:
+            start = i
+    if start is not None:
+        words.append(line[start:].rstrip())
+    return words
+
+
+def feff_inp_lines(text: str):
+    """(is_card, keyword_or_section, fields) per logical line, stopping after END (no INCLUDE here)."""
+    out, active = [], None
+    for raw in text.splitlines():
+        t = raw.replace("\t", " ").lstrip()
+        if not t or t[0] in ";*%#":
+            continue
+        u = _strip_inline(t).strip()
+        if not u:
+            continue
+        tok = _bwords(u)
+        if not tok:
+            continue
+        first = tok[0]
+        payload = (active == "EGRID" and first.lower() in ("e_grid", "k_grid", "exp_grid", "user_grid")) or \
+                  (active == "DENSITY" and first.lower() in ("line", "plane", "volume"))
+        if not payload and first[:1].isascii() and first[:1].isalpha():
+            key = first.upper()
+            key = _CANON.get(key[:4], key)
+            out.append((True, key, tok[1:]))
+            if key == "END":
+                break
+            if key in _BLOCKS:
+                active = key
+            elif key != "TITLE":
+                active = None
+        elif active is not None:
+            out.append((False, active, tok))
+        else:
+            raise ValueError("data row found outside a block card")
+    return out
+
+
+def _f64(v: str) -> float:
+    return float(v.replace("D", "E").replace("d", "E"))
+
+
+def feff_inp_geometry(text: str):
+    """(rows, iatph): rows = [(x, y, z, ipot)] in geom.dat order, iatph one-based model atoms."""
+    lines = feff_inp_lines(text)
+    rmult = None
+    atoms, pots = [], []
+    for card, key, f in lines:
+        if card:
+            if rmult is None and (key == "RMULT" or key[:4] == "RMUL"):
+                rmult = _f64(f[0])
+            continue
+        f = f[:f.index("*")] if "*" in f else f
+        if key == "ATOMS":
+            atoms.append([_f64(f[0]), _f64(f[1]), _f64(f[2]), int(f[3])])
+        elif key == "POTENTIALS":
+            int(f[1])
+            pots.append(int(f[0]))
+    rmult = 1.0 if rmult is None else rmult
+    atoms = [[a[0] * rmult, a[1] * rmult, a[2] * rmult, a[3]] for a in atoms]
+    ia = next((i for i, a in enumerate(atoms) if a[3] == 0), 0)
+    c = atoms[ia]
+    rows = [(0.0, 0.0, 0.0, 0, 0.0)]
+    for i, a in enumerate(atoms):
+        if i == ia:
+            continue
+        x, y, z = a[0] - c[0], a[1] - c[1], a[2] - c[2]
+        d2 = fma(z, z, fma(x, x, y * y))
+        if d2 > 0.0:
+            rows.append((x, y, z, a[3], d2))
+    for i in range(len(rows) - 1):
+        mi, md = i, rows[i][4]
+        for j in range(i + 1, len(rows)):
+            if rows[j][4] < md:
+                mi, md = j, rows[j][4]
+        if mi != i:
+            rows[i], rows[mi] = rows[mi], rows[i]
+    maxp = max((max(p, 0) for p in pots), default=None)
+    if maxp is None:
+        maxp = max(max(r[3], 0) for r in rows)
+    iatph = [0] * (maxp + 1)
+    iatph[0] = 1
+    for iph in range(1, maxp + 1):
+        iatph[iph] = next((k + 1 for k, r in enumerate(rows) if r[3] == iph), 0)
+    while len(iatph) > 1 and iatph[-1] == 0:
+        iatph.pop()
+    return [r[:4] for r in rows], iatph
+
+
+def rdinp_geom_dat_text(rows, iatph) -> str:
+    """write_geom_dat (crates/refeff-io/src/rdinp/structure.rs:57-81)."""
+    out = f"nat, nph = {len(rows):5d}{len(iatph) - 1:5d}\n" + "".join(f"{m:5d}" for m in iatph) + "\n"
+    out += " iat     x       y        z       iph  \n " + "-" * 71 + "\n"
+    for i, r in enumerate(rows):
+        out += f"{i + 1:4d}{r[0]:13.5f}{r[1]:13.5f}{r[2]:13.5f}{r[3]:4d}{1:4d}\n"
+    return out

@@ -504,9 +504,7 @@ struct GeomRow {
   int iph;
 };
 
-int parse_geom(const std::string& path, int& nph, std::vector<GeomRow>& rows, std::string& err) {
-  std::string text;
-  if (!read_file(path, text)) { err = "cannot read " + path; return REFEFF_FMS_ERR_INVALID_ARGUMENT; }
+int parse_geom_text(const std::string& text, int& nph, std::vector<GeomRow>& rows, std::string& err) {
   const auto L = split_lines(text);
   size_t i = 0;
   while (i < L.size() && trim(L[i]).empty()) ++i;
@@ -563,7 +561,15 @@ extern "C" int refeff_fms_run_dir(refeff_fms_context* ctx, const char* work_dir,
   if (rc) { set_error(ctx, err); return rc; }
   int nph = 0;
   std::vector<GeomRow> geom;
-  rc = parse_geom(dir + "geom.dat", nph, geom, err);
+  std::string gtext;
+  if (!read_file(dir + "geom.dat", gtext)) {
+    // no geom.dat: FEFF's rdinp writes it from feff.inp before this stage runs;
+    // build the same text (same 5-decimal rounding) from feff.inp here
+    std::string ferr;
+    rc = rfx::geom_dat_from_feff_inp(dir + "feff.inp", gtext, ferr);
+    if (rc) { set_error(ctx, "no geom.dat, and feff.inp: " + ferr); return rc; }
+  }
+  rc = parse_geom_text(gtext, nph, geom, err);
   if (rc) { set_error(ctx, err); return rc; }
   const int max_potential = pb.npot - 1;
   if (nph != max_potential) {

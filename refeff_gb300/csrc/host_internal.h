@@ -18,4 +18,6 @@ cudaStream_t context_stream(const refeff_fms_context* ctx);
 int mkgtr_transition_matrix(int lmax, int kinit, int polarization, const refeff_complex128* ptz9, int multipole,
                             int trace_orbital, int spin, int nsp, double angks, refeff_complex128* out,
                             int32_t* lind, int32_t* kiind);
+// geom.dat text (FEFF rdinp's write_geom_dat) for the cluster of a feff.inp (feff_inp.cu).
+int geom_dat_from_feff_inp(const std::string& path, std::string& text, std::string& err);
 }  // namespace rfx

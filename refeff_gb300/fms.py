@@ -144,6 +144,9 @@ def load(build_if_missing: bool = True):
         "refeff_fms_plan_bicgstab_stats": ([_p, _i, _p], _i),
         "refeff_fms_plan_precond_features": ([_p, _p, _p], _i),
         "refeff_fms_plan_inverse_diagonal": ([_p, _p, _i, _p, _p], _i),
+        "refeff_fms_geometry_from_feff_inp": ([C.c_char_p, _i, _p, _p, _p, _i, _p, _p], _i),
+        "refeff_fms_write_geom_dat": ([C.c_char_p, C.c_char_p], _i),
+        "refeff_fms_feff_inp_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -624,6 +627,33 @@ def write_gg_diag_bin(path, values) -> None:
     rc = lib.refeff_fms_write_gg_diag_bin(str(path).encode(), ne, na, dim, _ptr(flat))
     if rc:
         raise FmsError(rc, f"cannot write {path}")
+
+
+def geometry_from_feff_inp(path):
+    """The cluster of a feff.inp as FEFF's rdinp hands it to the FMS stage (refeff_fms_geometry_from_feff_inp):
+    returns (xyz (n, 3) float64, ipot (n,) int32, model_atoms (nph + 1,) int32); row 0 is the absorber."""
+    lib = load()
+    n, nm = C.c_int32(), C.c_int32()
+    b = str(path).encode()
+    rc = lib.refeff_fms_geometry_from_feff_inp(b, 0, None, None, C.byref(n), 0, None, C.byref(nm))
+    if rc:
+        raise FmsError(rc, lib.refeff_fms_feff_inp_last_error().decode())
+    xyz = np.zeros((n.value, 3))
+    ipot = np.zeros(n.value, np.int32)
+    model = np.zeros(nm.value, np.int32)
+    rc = lib.refeff_fms_geometry_from_feff_inp(b, n.value, _ptr(xyz), _ptr(ipot), C.byref(n), nm.value, _ptr(model),
+                                               C.byref(nm))
+    if rc:
+        raise FmsError(rc, lib.refeff_fms_feff_inp_last_error().decode())
+    return xyz, ipot, model
+
+
+def write_geom_dat(feff_inp, geom_dat) -> None:
+    """geom.dat for the cluster of a feff.inp, byte-compatible with FEFF rdinp's writer."""
+    lib = load()
+    rc = lib.refeff_fms_write_geom_dat(str(feff_inp).encode(), str(geom_dat).encode())
+    if rc:
+        raise FmsError(rc, lib.refeff_fms_feff_inp_last_error().decode())
 
 
 def read_phase_bin(path) -> dict:

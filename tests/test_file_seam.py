@@ -338,3 +338,35 @@ def test_run_dir_debye_damping(tmp_path, idwopt):
     assert np.abs(got - want).max() <= 1e-9 * np.abs(want).max()
     model = "a Correlated Debye model" if idwopt == 0 else "the Classical Debye model"
     assert f"Applying Debye-Waller factors using {model}." in (tmp_path / "log3.dat").read_text()
+
+
+@pytest.mark.gpu
+def test_run_dir_cluster_from_feff_inp(tmp_path):
+    """A work directory with feff.inp and no geom.dat: the stage takes its cluster from feff.inp through the
+    geom.dat text FEFF's rdinp would write, so gg.dat equals the run on that geom.dat byte for byte."""
+    from refeff_gb300 import workloads as wl
+    ctx = fms.Context(0)
+    rng = np.random.default_rng(5)
+    cl = wl.small_cluster(3.2, lmax=2, n_energies=1, seed=4)[0]
+    pos = np.asarray(cl.positions, float) + np.array([1.25, -0.5, 2.0])   # absorber off the origin
+    pots = [int(p) for p in cl.potentials]
+    order = rng.permutation(len(pots))
+    lines = ["POTENTIALS"] + [f" {p} 29 Cu" for p in range(max(pots) + 1)] + ["ATOMS"]
+    lines += [f" {pos[i, 0]:.6f} {pos[i, 1]:.6f} {pos[i, 2]:.6f} {pots[i]}" for i in order] + ["END"]
+    ne = 3
+    grid = 0.5 + 0.4 * np.arange(ne) + 0.03j
+    phase_pots = _phase_potentials(rng, ne, 1, [2] * (max(pots) + 1))
+    runs = {}
+    for name in ("from_feff_inp", "from_geom_dat"):
+        d = tmp_path / name
+        ff.write_workdir(d, positions=pos, potentials=pots, lmaxph=[2] * (max(pots) + 1), energy_grid=grid,
+                         phase_potentials=phase_pots, rfms2=100.0, rdirec=100.0)
+        (d / "geom.dat").unlink()
+        (d / "feff.inp").write_text("\n".join(lines) + "\n")
+        if name == "from_geom_dat":
+            fms.write_geom_dat(d / "feff.inp", d / "geom.dat")
+        rep = fms.run_fms_in_dir(ctx, d, fms.FORM_FP64_LU)
+        assert rep["energies_failed"] == 0
+        runs[name] = (d / "gg.dat").read_bytes()
+    assert runs["from_feff_inp"] == runs["from_geom_dat"]
+    assert not (tmp_path / "from_feff_inp" / "geom.dat").exists()
