@@ -203,28 +203,37 @@ def reference_arm(args, world, rank):
     print(json.dumps(out), flush=True)
 
 
-def tc_update_flops(n: int, m: int, E: int, nb: int = 64):
-    """Useful flops of the tensor-core trailing updates: one per 64-column block, C (rows x cols, the RHS
-    included) -= L21 (rows x kb) U12 (kb x cols), 8 real flops per complex MAC."""
-    f, launches = 0, 0
-    for k in range(0, n, nb):
-        kb = min(nb, n - k)
-        rows, cols = n - k - kb, n + m - k - kb
+def tc_update_work(n: int, m: int, E: int, paired: bool = True):
+    """Useful flops, algorithmic bytes and launches of the tensor-core trailing updates of one E-energy sweep,
+    following the FP32 elimination's launch sequence: with paired 64-column blocks (the library's default when
+    the tensor cores and the fused forward sweep serve the system, as for the 2256-state cluster) each pair
+    [k, k + 128) launches one K = 64 update of the second block's columns and one K = 128 update of everything
+    beyond the pair; otherwise one K = 64 update per block.  Each launch reads and writes its block C once
+    (8 B per complex entry) and does 8 real flops per complex multiply-add."""
+    col_end = n + m
+    flops = nbytes = launches = 0
+
+    def add(k_depth, rows, cols):
+        nonlocal flops, nbytes, launches
         if rows > 0 and cols > 0:
-            f += 8 * rows * cols * kb
+            flops += 8 * rows * cols * k_depth
+            nbytes += 2 * rows * cols * 8
             launches += 1
-    return f * E, launches
 
-
-def tc_update_c_bytes(n: int, m: int, E: int, nb: int = 64):
-    """Algorithmic bytes of the trailing updates: each reads and writes its block C (8 B per complex entry)."""
-    b = 0
-    for k in range(0, n, nb):
-        kb = min(nb, n - k)
-        rows, cols = n - k - kb, n + m - k - kb
-        if rows > 0 and cols > 0:
-            b += 2 * rows * cols * 8
-    return b * E
+    k = 0
+    while k < n:
+        kb = min(64, n - k)
+        k2 = k + kb
+        if not paired or k2 >= n:
+            add(kb, n - k2, col_end - k2)
+            k += 64
+            continue
+        kb2 = min(64, n - k2)
+        add(kb, n - k2, kb2)
+        k3 = k2 + kb2
+        add(kb + kb2, n - k3, col_end - k3)
+        k += 128
+    return flops * E, nbytes * E, launches
 
 
 def ncu_traffic(kernel: str):
@@ -320,7 +329,8 @@ def config_batched(ctx, fms, wl, local):
     return out
 
 
-def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, batch_plain, bicgstab_energies=0):
+def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, batch_plain, bicgstab_energies=0,
+                  learned=None):
     """One large cluster: the chosen form on an evenly spaced sample of n_chosen energies (in batches of
     batch_chosen, one warm batch first) and the plain FP64 LU on an evenly spaced sub-sample of n_plain of
     them (in batches of batch_plain, one warm batch first); the gg error is taken on the common energies."""
@@ -363,12 +373,47 @@ def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, b
                                                                  raise_on_error=False))
         bidx = np.array([list(sub).index(int(e)) for e in bsel])
         _, _, bfb = plan.refinement_stats(len(bsel))
+        its0 = plan.bicgstab_stats(len(bsel))
         out["bicgstab"] = {"value": len(bsel) / tb, "energies": int(len(bsel)),
                            "over_plain": (len(bsel) / tb) / plain, "max_rel_gg_err_vs_fp64": _rel_blocks(gb, g64[bidx], m),
                            "fp64_fallbacks": int(bfb.sum()), "status_nonzero": int((sb != 0).sum()),
+                           "iterations": int(its0.sum()),
                            "note": "unpreconditioned batched BiCGSTAB inside the FP64 refinement"}
+        if learned is not None:
+            model, train_info, window = learned
+            plan.set_preconditioner(model)
+            plan.set_precond_window(*window)
+            fms.fms_real_space_spectrum(plan, k[bsel[:1]], ph[bsel[:1]], fms.FORM_BICGSTAB, raise_on_error=False)
+            (gl, sl), tl = _wall(lambda: fms.fms_real_space_spectrum(plan, k[bsel], ph[bsel], fms.FORM_BICGSTAB,
+                                                                     raise_on_error=False))
+            _, _, lfb = plan.refinement_stats(len(bsel))
+            its1 = plan.bicgstab_stats(len(bsel))
+            plan.set_preconditioner(None)
+            out["bicgstab_learned"] = {
+                "value": len(bsel) / tl, "energies": int(len(bsel)), "over_plain": (len(bsel) / tl) / plain,
+                "over_unpreconditioned": tb / tl, "max_rel_gg_err_vs_fp64": _rel_blocks(gl, g64[bidx], m),
+                "fp64_fallbacks": int(lfb.sum()), "status_nonzero": int((sl != 0).sum()),
+                "iterations": int(its1.sum()), "training": train_info,
+                "window_ev_above_eref": list(window),
+                "note": "the same BiCGSTAB with the learned diagonal right preconditioner, applied only inside "
+                        "the energy window where it was trained"}
     plan.close()
     return out
+
+
+def train_learned(ctx, fms):
+    """The learned preconditioner for the rocksalt material: FP64-LU targets from seeded rocksalt clusters
+    (radius 6-8 A) inside -8..+10 eV (7..25 eV above E_ref with the 15 eV inner potential), trained on the GPU
+    by the library's own forward / backward / Adam kernels."""
+    from refeff_gb300 import learned as lr
+    t0 = time.perf_counter()
+    train = lr.rocksalt_training_cases(6, radius_range=(6.0, 8.0), n_energies=120, seed=11, material_seed=3)
+    X, T = lr.training_set(ctx, train, energies_per_case=20, atoms_per_case=10, seed=5, energy_window=(-8.0, 10.0))
+    model, hist = lr.train_preconditioner(ctx, 3, X, T, hidden=96, epochs=400, batch_size=128, learning_rate=1e-3,
+                                          seed=6)
+    info = {"samples": int(X.shape[0]), "clusters": 6, "epochs": 400, "loss_first": float(hist[0]),
+            "loss_last": float(hist[-1]), "seconds": time.perf_counter() - t0}
+    return model, info, (7.0, 25.0)
 
 
 def configs_block(ctx, fms, wl, local):
@@ -377,7 +422,7 @@ def configs_block(ctx, fms, wl, local):
         "3": dict(workload="rocksalt AB a = 4.44 A, sigma 0.04 A, R 9 A (257 atoms), 3 potentials, lmax 3, "
                            "300 energies -20..+100 eV",
                   **config_single(ctx, fms, wl, local, 3, n_chosen=300, batch_chosen=150, n_plain=24, batch_plain=8,
-                                  bicgstab_energies=12)),
+                                  bicgstab_energies=24, learned=train_learned(ctx, fms))),
         "4": dict(workload="random close packed binary cluster, 600 atoms, lmax 4, 400 energies -20..+300 eV",
                   **config_single(ctx, fms, wl, local, 4, n_chosen=40, batch_chosen=20, n_plain=2, batch_plain=1)),
     }
@@ -488,13 +533,13 @@ def ours(args, world, rank, local):
     relres, iters, fallback = plan.refinement_stats(E)
     work = algorithmic(n, m, E)
     hbm, bf16, bf16_sus, peak_kind = peaks()
-    residual_passes = int(np.sum(iters + 1))          # one FP64 residual per check, per energy
-    sweep_passes = int(np.sum(iters + 1))             # initial back-substitution + one solve per correction
+    residual_passes = int(np.sum(iters))              # one residual per correction, per energy
+    sweep_triangles = float(np.sum(0.5 + iters))      # initial back-substitution (U), then L and U per correction
     phase_work = {
         "eliminate": ("tensor", work["lu_flops"], "TFLOP/s", bf16, 1e12),
         "build": ("hbm", work["build_bytes_fp64"] + work["build_bytes_fp32"], "GB/s", hbm, 1e9),
         "residual": ("hbm", work["residual_bytes"] / E * residual_passes, "GB/s", hbm, 1e9),
-        "sweeps": ("hbm", n * n * 8.0 * sweep_passes, "GB/s", hbm, 1e9),
+        "sweeps": ("hbm", n * n * 8.0 * sweep_triangles, "GB/s", hbm, 1e9),
     }
     phase_ach = {}
     for k_, (bound, w_, unit, peak, scale) in phase_work.items():
@@ -505,9 +550,8 @@ def ours(args, world, rank, local):
     # the dominant kernel: the tensor-core trailing update (CUDA events around each of its launches). Its
     # DRAM traffic equals the read + write of the trailing block C (ncu), so HBM bounds it: achieved = C bytes
     # per launch / average launch time; the tensor-pipe view is reported beside it.
-    tc_flops, tc_launches = tc_update_flops(n, m, E)
+    tc_flops, c_bytes, tc_launches = tc_update_work(n, m, E, paired=True)
     tc_ms = ph.get("tc_update", 0.0)
-    c_bytes = tc_update_c_bytes(n, m, E)
     tc_gbs = c_bytes / (tc_ms / 1e3) / 1e9 if tc_ms > 0 else 0.0
     tc_tf = tc_flops / (tc_ms / 1e3) / 1e12 if tc_ms > 0 else 0.0
     tr = ncu_traffic("tc_update_persistent_kernel")

@@ -118,10 +118,21 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     gives up marks the call's tensor-core result void and every energy of
  *     the call is solved again with the FP64 LU (status 0, same results as
  *     REFEFF_FMS_FORM_FP64_LU; refeff_fms_last_error names the timeout).
- *     Applies from the next solve call of every plan of the context. */
+ *     Applies from the next solve call of every plan of the context.
+ *   REFEFF_FMS_OPT_PAIRED_BLOCKS: 1 (default) lets the FP32 LU on the tensor
+ *     cores take its 64-column blocks in pairs, with one K = 128 trailing
+ *     update per pair (half the trailing-matrix traffic); 0 updates after
+ *     every block.  Same factors up to rounding.  Applies from the next solve
+ *     call of every plan of the context. */
 #define REFEFF_FMS_OPT_TENSOR_CORES 1
 #define REFEFF_FMS_OPT_DENSE_REFINEMENT 2
 #define REFEFF_FMS_OPT_TC_WAIT_POLLS 3
+#define REFEFF_FMS_OPT_PAIRED_BLOCKS 4
+/*   REFEFF_FMS_OPT_MULTI_STREAMS: streams that refeff_fms_real_space_spectrum_multi
+ *     spreads its plans over (1..64, default 4); plans are packed onto them by
+ *     estimated cost (energies x n^3), largest first, each to the least-loaded
+ *     stream. */
+#define REFEFF_FMS_OPT_MULTI_STREAMS 5
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
 
 /* ---- cluster preparation (host) -------------------------------------- */
@@ -294,6 +305,36 @@ int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int n_plans, r
                                          refeff_complex128* const* scattering_out, int32_t* const* status_out,
                                          refeff_fms_report* report);
 
+/* No reference counterpart: the autotuner of the batched form.  For the
+ * clusters of one refeff_fms_real_space_spectrum_multi workload it times, on
+ * up to sample_energies evenly spaced energies of every cluster (0 = all),
+ * per size bucket (state counts rounded up to a multiple of 256) the FP32
+ * elimination's inner panel width and block pairing (FP32_REFINED only), then
+ * the number of streams the clusters are packed onto, and applies the fastest
+ * (refeff_fms_plan_set_tuning on each plan, REFEFF_FMS_OPT_MULTI_STREAMS on
+ * the context).  With cache_path, the choice is stored in that JSON file under
+ * a key of the device name, the form and the clusters' sizes, and a later call
+ * with the same key applies the stored choice without measuring
+ * (out->from_cache = 1).  The results of the many-cluster call do not depend on
+ * the choice beyond rounding. */
+typedef struct {
+  int streams;             /* streams chosen for the many-cluster call */
+  int buckets;             /* size buckets tuned */
+  double seconds_default;  /* sample time with the default choices */
+  double seconds_tuned;    /* sample time with the chosen ones */
+  int from_cache;          /* 1: applied from cache_path without measuring */
+} refeff_fms_tuning;
+int refeff_fms_autotune_multi(refeff_fms_context* ctx, int n_plans, refeff_fms_plan* const* plans,
+                              const refeff_fms_energy_points* points, refeff_fms_form form, int sample_energies,
+                              const char* cache_path, refeff_fms_tuning* out);
+/* Per-plan choices of the FP32 elimination: inner_width 0 (by size: two-level
+ * from n = 512 with 16-column inner panels first), 16 or 32 (two-level with
+ * that inner panel width first, from n = 128) or 1 (single-level panels);
+ * paired_blocks -1 (the context's REFEFF_FMS_OPT_PAIRED_BLOCKS), 0 or 1.
+ * Applies from the plan's next solve. */
+int refeff_fms_plan_set_tuning(refeff_fms_plan* plan, int inner_width, int paired_blocks);
+int refeff_fms_plan_get_tuning(const refeff_fms_plan* plan, int* inner_width, int* paired_blocks);
+
 /* Per-energy outcome of the last refeff_fms_real_space_spectrum call with
  * REFEFF_FMS_FORM_FP32_REFINED: relative residual max|b - A x| / max|b| of
  * the last residual evaluated (the one that produced the final correction),
@@ -460,6 +501,13 @@ int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu
 int refeff_ff2x_lorentz_convolve(int n, const double* omega, const refeff_complex128* spectrum, double width,
                                  refeff_complex128* out);
 
+/* FF2X's Debye factor sig_gk on the fine structure of the xmu.dat rows
+ * (crates/refeff-engine/src/ff2x.rs:3388-3397): with sig_gk > 1e-4, chi[r] *=
+ * exp(-(sig_gk * wave_number[r])^2) (wave numbers in 1/Angstrom), then mu[r] =
+ * mu0[r] + chi[r] when mu and mu0 are given.  Host only. */
+int refeff_ff2x_debye_factor(int n, const double* wave_number, double sig_gk, const double* mu0, double* chi,
+                             double* mu);
+
 int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* energy, const refeff_complex128* trace);
 
 /* ---- learned preconditioner for the BiCGSTAB form ---------------------- */
@@ -493,6 +541,10 @@ int refeff_fms_precond_predict(refeff_fms_precond_model* model, int n_samples, c
 /* Attach a model (built for the plan's global lmax) or detach it (NULL). The
  * plan does not own the model. */
 int refeff_fms_plan_set_preconditioner(refeff_fms_plan* plan, refeff_fms_precond_model* model);
+/* Energy gate of the attached model: it preconditions only the energies with
+ * E - E_ref = Re((k a0)^2) / 2 Hartree (first spin's wave number) in
+ * [e_lo_ev, e_hi_ev]; the others run unpreconditioned.  Default: all energies. */
+int refeff_fms_plan_set_precond_window(refeff_fms_plan* plan, double e_lo_ev, double e_hi_ev);
 /* BiCGSTAB controls: iteration cap per solve, relative residual tolerance of
  * each solve, and how often (iterations) the host checks for completion. */
 int refeff_fms_plan_set_bicgstab(refeff_fms_plan* plan, int max_iterations, double tolerance, int poll_interval);

@@ -23,6 +23,8 @@ from __future__ import annotations
 import cmath
 import math
 
+import numpy as np
+
 EPS4 = 1.0e-4
 HARTREE_EV = 27.211396
 
@@ -193,3 +195,11 @@ def xanes_mu(*, energy, ne1, fermi, omega, cross_section, background, trace, s02
         chi.append((total[r] - atomic[r]) / norm)
         mu.append(mu0[-1] + chi[-1])
     return mu, mu0, chi
+
+
+def debye_factor(wave_number, sig_gk, mu0, chi):
+    """ff2x.rs:3388-3397: chi *= exp(-(sig_gk k)^2) when sig_gk > 1e-4 (k in 1/Angstrom); mu = mu0 + chi."""
+    chi = np.array(chi, float)
+    if sig_gk > 1e-4:
+        chi = chi * np.exp(-(sig_gk * np.asarray(wave_number, float)) ** 2)
+    return np.asarray(mu0, float) + chi, chi

@@ -340,9 +340,14 @@ __global__ void __launch_bounds__(256) unit_lower_inverse_kernel(BatchLayout lay
   }
 }
 
+// With kprev >= 0 (paired blocks) the block is the second of a pair whose
+// first block starts at kprev and whose update of these columns was deferred:
+// between the row moves and the L11^-1 product the panel rows get
+// A12 -= L21prev (rows [k, k + kb), columns [kprev, kprev + 64)) U12prev
+// (rows [kprev, kprev + 64) of these columns).
 __global__ void __launch_bounds__(256) rhs_lower_tile_kernel(BatchLayout lay, int k, int c_begin, int c_end,
                                                              float2* __restrict__ M, LuWork w,
-                                                             const float2* __restrict__ linv) {
+                                                             const float2* __restrict__ linv, int kprev) {
   constexpr int NB = 64;
   const int b = blockIdx.y, cb = c_begin + blockIdx.x * kLtN;
   const int ncols = min(kLtN, c_end - cb);
@@ -362,7 +367,8 @@ __global__ void __launch_bounds__(256) rhs_lower_tile_kernel(BatchLayout lay, in
     Bt[i * kLtN + c] = Mb[size_t(pm[i].y) + lda * size_t(cb + c)];
   }
   const float4* src = reinterpret_cast<const float4*>(linv + size_t(b) * NB * NB);
-  for (int idx = tid; idx < NB * NB / 2; idx += 256) reinterpret_cast<float4*>(Li)[idx] = src[idx];
+  if (kprev < 0)
+    for (int idx = tid; idx < NB * NB / 2; idx += 256) reinterpret_cast<float4*>(Li)[idx] = src[idx];
   __syncthreads();
   for (int idx = tid; idx < np * ncols; idx += 256) {
     const int i = idx % np, c = idx / np;
@@ -373,9 +379,40 @@ __global__ void __launch_bounds__(256) rhs_lower_tile_kernel(BatchLayout lay, in
     const int i = idx % NB, c = idx / NB;
     Bt[i * kLtN + c] = (i < kb && c < ncols) ? Mb[size_t(k + i) + lda * size_t(cb + c)] : make_float2(0.f, 0.f);
   }
-  __syncthreads();
-  // rows r0 .. r0 + 7 of column `col`; L11^-1 is lower triangular, so j <= r0 + 7
+  // rows r0 .. r0 + 7 of column `col`
   const int col = tid & 31, r0 = (tid >> 5) * 8;
+  if (kprev >= 0) {
+    // the deferred update by the pair's first block: Li <- L21prev, Bt rows [NB, 2 NB) <- U12prev
+    float2* Up = Bt + NB * kLtN;
+    for (int idx = tid; idx < NB * NB; idx += 256) {
+      const int i = idx % NB, j = idx / NB;
+      Li[i + NB * j] = i < kb ? Mb[size_t(k + i) + lda * size_t(kprev + j)] : make_float2(0.f, 0.f);
+    }
+    for (int idx = tid; idx < NB * kLtN; idx += 256) {
+      const int j = idx % NB, c = idx / NB;
+      Up[j * kLtN + c] = c < ncols ? Mb[size_t(kprev + j) + lda * size_t(cb + c)] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 d[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) d[q] = Bt[(r0 + q) * kLtN + col];
+    for (int j = 0; j < NB; ++j) {
+      const float2 uv = Up[j * kLtN + col];
+      const float4* lr = reinterpret_cast<const float4*>(Li + r0 + NB * j);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 l2 = lr[q];
+        cfms(d[2 * q], make_float2(l2.x, l2.y), uv);
+        cfms(d[2 * q + 1], make_float2(l2.z, l2.w), uv);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) Bt[(r0 + q) * kLtN + col] = d[q];
+    for (int idx = tid; idx < NB * NB / 2; idx += 256) reinterpret_cast<float4*>(Li)[idx] = src[idx];
+  }
+  __syncthreads();
+  // L11^-1 is lower triangular, so j <= r0 + 7
   float2 acc[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) acc[q] = make_float2(0.f, 0.f);
@@ -788,17 +825,19 @@ static bool fit_panel(int elem, int nb, int n, int& cluster, int& rpc, int& smem
 }
 
 template <typename T>
-PanelConfig choose_panel(int n) {
+PanelConfig choose_panel(int n, int inner_pref) {
   PanelConfig pc;
   pc.cluster = 0;
-  if (sizeof(T) == 4 && n >= 512) {
+  const bool forced = inner_pref == 16 || inner_pref == 32;
+  if (sizeof(T) == 4 && ((inner_pref == 0 && n >= 512) || (forced && n >= 128))) {
     // two-level: 64-column blocks of 16- or 32-column cluster panels.  16 columns
     // halve the shared memory of a panel, and with the row bookkeeping in global
     // scratch a 4-CTA panel takes 72 KB per CTA, three CTAs per SM: about three
     // times as many panels (energies) are factored at once as with 32 columns
     // and the bookkeeping in shared memory.  The panel's column chain, not its
     // arithmetic, bounds it (measured at n = 2256: elimination 103.8 -> 90.8 ms).
-    for (int iw : {16, 32})
+    const int order[2] = {inner_pref == 32 ? 32 : 16, inner_pref == 32 ? 16 : 32};
+    for (int iw : order)
       if (fit_panel(8, iw, n, pc.inner_cluster, pc.inner_rpc, pc.inner_smem, pc.inner_pos_global, iw == 16)) {
         pc.nb = 64;
         pc.inner_nb = iw;
@@ -968,6 +1007,15 @@ static cudaError_t panel_any(const PanelConfig& pc, int nb, const BatchLayout& l
 // so that the block's L is in one row order.  The panels' moves are composed,
 // and the trailing matrix (right-hand sides included) gets one K = 64 update:
 // on the tensor cores when operand images are available, else on CUDA cores.
+//
+// Paired blocks (pc.pair128, tensor cores): the blocks are taken two at a
+// time, a = [k, k + 64) and b = [k + 64, k + 128).  Block a's update reaches
+// only b's columns (K = 64 over 64 columns); b is factored with its moves also
+// applied to a's L; b's block row gets a's deferred update inside the
+// L11^-1 product (rhs_lower_tile_kernel, kprev = k); and one K = 128 update
+// covers everything beyond the pair.  Each trailing entry is read and written
+// once per pair instead of once per block, which halves the traffic of the
+// dominant kernel for the same flops.
 static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayout& lay, int batch, float2* M,
                                           const LuWork& w, cudaStream_t s) {
   const int n = lay.n, col_end = lay.n + lay.m, iw = pc.inner_nb;
@@ -984,14 +1032,15 @@ static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayo
   wi.nb = iw;
   wi.npanels = panel_count(n, iw);
   if (!pin.pos_global) wi.pos_scratch = nullptr;
-  for (int k = 0; k < n; k += 64) {
-    const int kb = min(64, n - k);
+  const bool pair = pc.pair128 && w.pair128 && w.tc_images && w.linv;
+  // the inner panels of block [k, k + kb); their row moves also reach the L columns [l_begin, k)
+  auto factor_block = [&](int k, int kb, int l_begin) -> cudaError_t {
     int P = 0;
     for (int ki = k; ki < k + kb; ki += iw, ++P) {
       const int kbi = min(iw, k + kb - ki);
       cudaError_t err = panel_any<float>(pin, iw, lay, batch, ki, M, wi, s);
       if (err != cudaSuccess) return err;
-      if (ki > k) rhs_lower_any<float, false>(iw, lay, batch, ki, k, ki, M, wi, nullptr, s);  // moves on earlier L
+      if (ki > l_begin) rhs_lower_any<float, false>(iw, lay, batch, ki, l_begin, ki, M, wi, nullptr, s);  // moves on earlier L
       if (ki + kbi < k + kb) {
         // the block's remaining columns: this panel's moves and L11, then its rank-IW update
         rhs_lower_any<float>(iw, lay, batch, ki, ki + kbi, k + kb, M, wi, nullptr, s);
@@ -1000,23 +1049,47 @@ static cudaError_t lu_eliminate_two_level(const PanelConfig& pc, const BatchLayo
     }
     count_launch();
     compose_moves_kernel<<<batch, 128, 0, s>>>(k, iw, P, w, wi);
-    if (w.linv) {
-      count_launch();
-      unit_lower_inverse_kernel<<<batch, 256, 0, s>>>(lay, k, M, w.linv);
-      const int ncols = col_end - (k + kb);
-      if (ncols > 0) {
-        constexpr int smem = (64 * 64 + 2 * 64 * kLtN) * int(sizeof(float2));
-        ensure_smem_limit(reinterpret_cast<const void*>(rhs_lower_tile_kernel), size_t(smem));
-        count_launch();
-        rhs_lower_tile_kernel<<<dim3(unsigned((ncols + kLtN - 1) / kLtN), unsigned(batch)), 256, smem, s>>>(
-            lay, k, k + kb, col_end, M, w, w.linv);
-      }
-    } else {
+    return cudaSuccess;
+  };
+  // the block row of block [k, k + kb) for every column beyond it: moves, then U12 = L11^-1 (P A12)
+  auto block_row = [&](int k, int kb, int kprev) {
+    if (!w.linv) {
       launch_rhs_lower<float, 64>(lay, batch, k, k + kb, col_end, M, w, nullptr, s);
+      return;
     }
-    if (w.tc_images) tc_trailing_update(lay, batch, k, kb, col_end, M, w.tc_images, w.tc_err, nullptr, w.tc_wait_polls, w.tc_spans, s);
-    else gemm_any<float>(64, lay, batch, k + kb, n, k + kb, col_end, k, kb, M, nullptr, s);
-    cudaError_t err = cudaGetLastError();
+    count_launch();
+    unit_lower_inverse_kernel<<<batch, 256, 0, s>>>(lay, k, M, w.linv);
+    const int ncols = col_end - (k + kb);
+    if (ncols > 0) {
+      constexpr int smem = (64 * 64 + 2 * 64 * kLtN) * int(sizeof(float2));
+      ensure_smem_limit(reinterpret_cast<const void*>(rhs_lower_tile_kernel), size_t(smem));
+      count_launch();
+      rhs_lower_tile_kernel<<<dim3(unsigned((ncols + kLtN - 1) / kLtN), unsigned(batch)), 256, smem, s>>>(
+          lay, k, k + kb, col_end, M, w, w.linv, kprev);
+    }
+  };
+  auto update = [&](int k, int kb, int c_end) {
+    if (w.tc_images) tc_trailing_update(lay, batch, k, kb, c_end, M, w.tc_images, w.tc_err, nullptr, w.tc_wait_polls,
+                                        w.tc_spans, s);
+    else gemm_any<float>(64, lay, batch, k + kb, n, k + kb, c_end, k, kb, M, nullptr, s);
+  };
+  for (int k = 0; k < n; k += pair ? 128 : 64) {
+    const int kb = min(64, n - k);
+    cudaError_t err = factor_block(k, kb, k);
+    if (err != cudaSuccess) return err;
+    block_row(k, kb, -1);
+    const int k2 = k + kb;
+    if (!pair || k2 >= n) {
+      update(k, kb, col_end);
+    } else {
+      const int kb2 = min(64, n - k2);
+      update(k, kb, k2 + kb2);              // block a into block b's columns only
+      err = factor_block(k2, kb2, k);       // b's moves also on a's L
+      if (err != cudaSuccess) return err;
+      block_row(k2, kb2, k);                // with a's deferred update of b's block row
+      update(k, kb + kb2, col_end);         // K = kb + kb2 over everything beyond the pair
+    }
+    err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
   return cudaSuccess;
@@ -1173,8 +1246,8 @@ void launch_copy_rhs64(const BatchLayout& lay, int batch, const double2* M64, do
   copy_rhs64_kernel<<<grid, 256, 0, s>>>(lay, M64, X64);
 }
 
-template PanelConfig choose_panel<double>(int);
-template PanelConfig choose_panel<float>(int);
+template PanelConfig choose_panel<double>(int, int);
+template PanelConfig choose_panel<float>(int, int);
 template cudaError_t lu_eliminate<double>(const PanelConfig&, const BatchLayout&, int, double2*, const LuWork&,
                                           cudaStream_t);
 template cudaError_t lu_eliminate<float>(const PanelConfig&, const BatchLayout&, int, float2*, const LuWork&,

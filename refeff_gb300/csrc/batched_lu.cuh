@@ -20,14 +20,22 @@ struct PanelConfig {
   int pos_global = 0;  // row-position bookkeeping in global scratch (large n) instead of shared memory
   // two-level elimination (FP32, nb = 64): the cluster panels are inner_nb wide
   int inner_nb = 0, inner_cluster = 0, inner_rpc = 0, inner_smem = 0, inner_pos_global = 0;
+  // two-level elimination with tensor cores: 64-column blocks taken in pairs,
+  // one K = 128 trailing update per pair (set by the workspace when the fused
+  // forward sweep, which replays the paired row moves, serves the system)
+  int pair128 = 0;
 };
 
-template <typename T> PanelConfig choose_panel(int n);
+// inner_pref (FP32): 0 picks by n (two-level from n = 512, 16-column inner
+// panels first); 16 or 32 asks for two-level with that inner width first
+// (from n = 128); 1 asks for single-level panels.
+template <typename T> PanelConfig choose_panel(int n, int inner_pref = 0);
 
 inline int panel_count(int n, int nb) { return (n + nb - 1) / nb; }
 
 // Tensor-core trailing update (tc_update.cu) for the FP32 elimination.
-constexpr int kTcBM = 128, kTcBN = 48;
+constexpr int kTcBM = 128, kTcBN = 64;
+constexpr int kTcKMax = 128;  // deepest update: two 64-column blocks at once
 // bytes of the operand tile images for a batch of systems of order n with m right-hand sides
 size_t tc_image_bytes(int n, int m, int batch);
 // CUDA events around every tensor-core update kernel of one plan while `on`
@@ -70,6 +78,10 @@ struct LuWork {
   int* pos_scratch = nullptr;
   int npanels = 0;
   int nb = 0;
+  // the elimination paired its 64-column blocks (PanelConfig::pair128): the
+  // second block's row moves were also applied to the first block's L, so a
+  // forward sweep applies both blocks' moves before solving the pair
+  int pair128 = 0;
 };
 
 // Elimination of the whole augmented system: after it, columns [0, n) hold
@@ -108,6 +120,9 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
 bool fused_forward_sweep(int nb, const BatchLayout& lay, int batch, float2* M, const LuWork& w, const int* skip,
                          cudaStream_t s);
 bool fused_backward_sweep(int nb, const BatchLayout& lay, int batch, float2* M, const int* skip, cudaStream_t s);
+// Whether the fused sweeps above serve systems of this layout (their right-hand
+// sides fit in shared memory).
+bool fused_sweep_available(int nb, const BatchLayout& lay);
 
 void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
                      double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,

@@ -11,8 +11,9 @@
 //   locat, terp / terpc window, polint     crates/refeff-core/src/interpolation.rs:119-135, 215-236, 338-446
 //   vicorr Lorentzian broadening          ff2x_xanes_apply_vicorr_convolution 3265-3306
 //   conv1 / conv                           crates/refeff-core/src/convolution/lorentzian.rs:4-100
-// The Debye factor sig_gk and the thermal xscorr (4643-) are not part of this
-// entry point.
+//   sig_gk Debye factor on chi            ff2x_xanes_xmu_dat_from_components 3388-3397
+//                                          (refeff_ff2x_debye_factor, after the mu(E) step)
+// The thermal xscorr (4643-) is not restated.
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -310,6 +311,22 @@ extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec,
     if (mu0) mu0[r] = m0;
     if (chi) chi[r] = c;
     if (mu) mu[r] = m0 + c;
+  }
+  return REFEFF_FMS_OK;
+}
+
+// ff2x.rs:3388-3397: with sig_gk > 1e-4 the fine structure of every output row
+// is damped by exp(-(sig_gk k)^2), k the row's wave number in 1/Angstrom, and
+// mu = mu0 + chi is formed again (the xmu.dat normalisation branch).
+extern "C" int refeff_ff2x_debye_factor(int n, const double* wave_number, double sig_gk, const double* mu0, double* chi,
+                                        double* mu) {
+  if (n < 0 || (n > 0 && (!wave_number || !chi)) || !std::isfinite(sig_gk)) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  for (int r = 0; r < n; ++r) {
+    if (sig_gk > kEps4) {
+      const double x = sig_gk * wave_number[r];
+      chi[r] *= std::exp(-(x * x));
+    }
+    if (mu && mu0) mu[r] = mu0[r] + chi[r];
   }
   return REFEFF_FMS_OK;
 }

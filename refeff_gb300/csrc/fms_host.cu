@@ -97,6 +97,8 @@ struct refeff_fms_context {
   int use_tensor_cores = 1;  // FP32 trailing updates on tcgen05 (REFEFF_FMS_OPT_TENSOR_CORES)
   int dense_refinement = 10; // corrections of the dense FP32 solve (REFEFF_FMS_OPT_DENSE_REFINEMENT)
   long long tc_wait_polls = kTcWaitPolls;  // REFEFF_FMS_OPT_TC_WAIT_POLLS
+  int paired_blocks = 1;     // REFEFF_FMS_OPT_PAIRED_BLOCKS
+  int multi_streams = 4;     // REFEFF_FMS_OPT_MULTI_STREAMS
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
   // the caller's handle plus one per live plan and model: the context is torn
   // down when the last of them is destroyed, in whatever order that happens
@@ -117,6 +119,11 @@ extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option
     case REFEFF_FMS_OPT_DENSE_REFINEMENT:
       if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
       ctx->dense_refinement = int(value);
+      return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_PAIRED_BLOCKS: ctx->paired_blocks = value != 0; return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_MULTI_STREAMS:
+      if (value < 1 || value > 64) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+      ctx->multi_streams = int(value);
       return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_TC_WAIT_POLLS:
       if (value < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
@@ -364,11 +371,21 @@ double so_coefficient(bool plus, int l, int m, int spin) {
 
 }  // namespace
 
+// Per-plan choices of the FP32 elimination (set by the caller or the
+// autotuner): the inner panel width preference of choose_panel and whether
+// 64-column blocks are paired (-1: the context's REFEFF_FMS_OPT_PAIRED_BLOCKS).
+struct TunePrefs {
+  int inner = 0;
+  int paired = -1;
+};
+
 struct Workspace {
   int batch = 0;
   bool fp32 = false;
   BatchLayout lay;
   PanelConfig pc64, pc32;
+  int inner_pref = 0;    // choose_panel<float> preference the workspace was built with
+  int paired_pref = 1;   // pairing asked for (context or plan)
   DevBuf<double2> M64;
   DevBuf<float2> M32;
   DevBuf<double2> X64, R;
@@ -455,12 +472,14 @@ struct refeff_fms_plan {
   std::vector<int> pot_dev;           // potentials, device atom order (host copy)
   std::vector<int> off_dev;           // first state of each atom, device order (host copy, N + 1)
   refeff_fms_precond_model* model = nullptr;  // learned preconditioner (not owned), NULL: none
+  double precond_e_lo = -1e300, precond_e_hi = 1e300;  // energies (E - E_ref, eV) where the model is applied
   DevBuf<float> d_shell_info, d_shell_pots;
   int bicg_max_iter = 400;
   double bicg_tol = 1.0e-6;
   int bicg_poll = 8;
   DevBuf<int> d_bicg_iters_all;
   std::vector<int> last_bicg_iters;
+  TunePrefs tune;  // per-plan FP32 elimination choices (refeff_fms_plan_set_tuning, the autotuner)
   Workspace ws;
   bool profiling = false;
   double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0, 0};
@@ -720,6 +739,22 @@ extern "C" int refeff_fms_plan_query(const refeff_fms_plan* plan, int* n_states,
   return REFEFF_FMS_OK;
 }
 
+extern "C" int refeff_fms_plan_set_tuning(refeff_fms_plan* plan, int inner_width, int paired_blocks) {
+  if (!plan || !(inner_width == 0 || inner_width == 1 || inner_width == 16 || inner_width == 32) || paired_blocks < -1 ||
+      paired_blocks > 1)
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->tune.inner = inner_width;
+  plan->tune.paired = paired_blocks;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_get_tuning(const refeff_fms_plan* plan, int* inner_width, int* paired_blocks) {
+  if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (inner_width) *inner_width = plan->tune.inner;
+  if (paired_blocks) *paired_blocks = plan->tune.paired;
+  return REFEFF_FMS_OK;
+}
+
 extern "C" int refeff_fms_plan_set_batch(refeff_fms_plan* plan, int max_batch) {
   if (!plan || max_batch < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   plan->max_batch = max_batch;
@@ -754,20 +789,38 @@ size_t bytes_per_system(const BatchLayout& lay, bool fp32) {
   return b;
 }
 
-int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32) {
+// Paired 64-column blocks (one K = 128 tensor-core update per pair) when the
+// tensor cores run the FP32 LU and the fused forward sweep replays its moves.
+int want_pair128(const Workspace& ws) {
+  return ws.paired_pref && ws.fp32 && ws.use_tc && ws.pc32.inner_nb && fused_sweep_available(ws.pc32.nb, ws.lay)
+             ? 1 : 0;
+}
+
+int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32,
+                     const TunePrefs* tune = nullptr) {
   const BatchLayout lay = make_layout(n, m);
   if (ws.tc_wait_polls != ctx->tc_wait_polls) {  // a kernel argument: captured graphs hold the old budget
     ws.drop_graphs();
     ws.tc_wait_polls = ctx->tc_wait_polls;
   }
-  if (ws.batch >= batch && ws.lay.n == n && ws.lay.m == m && (ws.fp32 || !fp32)) return REFEFF_FMS_OK;
+  const int inner = tune ? tune->inner : 0;
+  ws.paired_pref = tune && tune->paired >= 0 ? tune->paired : ctx->paired_blocks;
+  if (ws.batch >= batch && ws.lay.n == n && ws.lay.m == m && (ws.fp32 || !fp32) && ws.inner_pref == inner) {
+    const int pair = want_pair128(ws);
+    if (pair != ws.pc32.pair128) {  // the elimination's launch sequence changes: recapture
+      ws.drop_graphs();
+      ws.pc32.pair128 = pair;
+    }
+    return REFEFF_FMS_OK;
+  }
   ws.drop_graphs();
+  ws.inner_pref = inner;
   ws.batch = std::max(batch, ws.lay.n == n && ws.lay.m == m ? ws.batch : 0);
   ws.fp32 = fp32 || (ws.lay.n == n && ws.lay.m == m && ws.fp32);
   ws.lay = lay;
   const int B = ws.batch;
   ws.pc64 = choose_panel<double>(n);
-  ws.pc32 = choose_panel<float>(n);
+  ws.pc32 = choose_panel<float>(n, inner);
   if (ws.pc64.cluster <= 0 || (ws.fp32 && ws.pc32.cluster <= 0))
     return fail(ctx, REFEFF_FMS_ERR_UNSUPPORTED, "system too large for the cluster panel factorization");
   const int nb_min = std::min(ws.pc64.nb, ws.pc32.nb);
@@ -805,6 +858,7 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
     RF_CUDA(ctx, ws.tc_err.alloc(1));
     RF_CUDA(ctx, cudaMemset(ws.tc_err.p, 0, sizeof(int)));
   }
+  ws.pc32.pair128 = want_pair128(ws);
   return REFEFF_FMS_OK;
 }
 
@@ -822,6 +876,7 @@ LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
     w.perm_in = ws.perm_in.p;
     w.nperm_in = ws.nperm_in.p;
     w.linv = ws.linv.p;
+    w.pair128 = pc.pair128;
   }
   if (&pc == &ws.pc32 && ws.use_tc) {
     w.tc_images = ws.tc_images.p;
@@ -1088,7 +1143,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, c
         cudaError_t e1 = mlp_forward(sh, model_params(p.model), batch * p.N, ws.feat_X.p, ws.mlp, ws.feat_Y.p, s);
         if (e1 != cudaSuccess) return e1;
         launch_scatter_diag(batch, p.N, p.L, p.nsp, lay.lda, p.d_atom_off.p, p.d_atom_lmax.p, ws.feat_Y.p,
-                            ws.precond_D.p, s);
+                            ws.k_stage.p, p.precond_e_lo, p.precond_e_hi, ws.precond_D.p, s);
       }
       return cudaGetLastError();
     });
@@ -1177,7 +1232,7 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
   const bool fp32 = form != REFEFF_FMS_FORM_FP64_LU;  // the BiCGSTAB form uses the refined form's buffers
   const bool bicg = form == REFEFF_FMS_FORM_BICGSTAB;
   const int B = pick_batch(p, E, fp32);
-  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, fp32);
+  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, fp32, &p.tune);
   if (rc) return rc;
   Workspace& ws = p.ws;
   const size_t xph = p.xph_per_energy();
@@ -1499,28 +1554,51 @@ extern "C" int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int
       if (plans[i] == plans[j]) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "a plan appears twice");
   const auto t0 = std::chrono::steady_clock::now();
   RF_CUDA(ctx, cudaSetDevice(ctx->device));
-  constexpr int kStreams = 4;
-  while (int(ctx->pool.size()) < kStreams) {
+  const int n_streams = std::max(1, std::min(ctx->multi_streams, n_plans));
+  while (int(ctx->pool.size()) < n_streams) {
     cudaStream_t q = nullptr;
     RF_CUDA(ctx, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
     ctx->pool.push_back(q);
   }
-  // every plan's work in flight first (round-robin over the streams), then completion
+  // Packing: plans in decreasing estimated cost (energies x n^3, the LU's
+  // work), each onto the stream with the least cost so far (longest
+  // processing time first), so that the streams finish together; every plan's
+  // work is put in flight before any is completed.
+  std::vector<int> order(static_cast<size_t>(n_plans));
+  std::vector<double> cost(static_cast<size_t>(n_plans));
+  for (int i = 0; i < n_plans; ++i) {
+    order[size_t(i)] = i;
+    const double n = double(plans[i]->n);
+    cost[size_t(i)] = double(std::max(points[i].n_energies, 0)) * n * n * n;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[size_t(a)] > cost[size_t(b)]; });
+  std::vector<double> load(static_cast<size_t>(n_streams), 0.0);
+  std::vector<int> stream_of(static_cast<size_t>(n_plans), 0);
+  for (int i : order) {
+    const int q = int(std::min_element(load.begin(), load.end()) - load.begin());
+    stream_of[size_t(i)] = q;
+    load[size_t(q)] += cost[size_t(i)];
+  }
   int rc = REFEFF_FMS_OK;
   int begun = 0;
-  for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun)
-    rc = spectrum_begin(*plans[begun], &points[begun], form, scattering_out[begun], ctx->pool[size_t(begun % kStreams)]);
+  for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun) {
+    const int i = order[size_t(begun)];
+    rc = spectrum_begin(*plans[i], &points[i], form, scattering_out[i], ctx->pool[size_t(stream_of[size_t(i)])]);
+  }
   int failed = 0, first_rc = rc;
-  for (int i = 0; i < begun; ++i) {
+  std::vector<refeff_fms_plan*> done_plans;
+  for (int j = 0; j < begun; ++j) {
+    const int i = order[size_t(j)];
+    cudaStream_t q = ctx->pool[size_t(stream_of[size_t(i)])];
     int f = 0;
     const int r = rc == REFEFF_FMS_OK ? spectrum_end(*plans[i], &points[i], form, scattering_out[i],
-                                                     status_out ? status_out[i] : nullptr, &f,
-                                                     ctx->pool[size_t(i % kStreams)])
-                                      : (cudaStreamSynchronize(ctx->pool[size_t(i % kStreams)]), REFEFF_FMS_OK);
+                                                     status_out ? status_out[i] : nullptr, &f, q)
+                                      : (cudaStreamSynchronize(q), REFEFF_FMS_OK);
     failed += f;
     if (first_rc == REFEFF_FMS_OK) first_rc = r;
+    done_plans.push_back(plans[i]);
   }
-  fill_report(report, std::vector<refeff_fms_plan*>(plans, plans + begun), form, failed, t0);
+  fill_report(report, done_plans, form, failed, t0);
   return first_rc;
 }
 
@@ -1570,6 +1648,13 @@ __global__ void inverse_diagonal_kernel(BatchLayout lay, const double2* M, int s
 }
 
 }  // namespace
+
+extern "C" int refeff_fms_plan_set_precond_window(refeff_fms_plan* plan, double e_lo_ev, double e_hi_ev) {
+  if (!plan || std::isnan(e_lo_ev) || std::isnan(e_hi_ev) || e_lo_ev > e_hi_ev) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->precond_e_lo = e_lo_ev;
+  plan->precond_e_hi = e_hi_ev;
+  return REFEFF_FMS_OK;
+}
 
 extern "C" int refeff_fms_plan_set_preconditioner(refeff_fms_plan* plan, refeff_fms_precond_model* model) {
   if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
@@ -1638,7 +1723,7 @@ extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const ref
   RF_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t s = ctx->stream;
   const int B = pick_batch(p, E, false);
-  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, false);
+  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, false, &p.tune);
   if (rc) return rc;
   Workspace& ws = p.ws;
   const BatchLayout& lay = ws.lay;

@@ -187,9 +187,11 @@ __global__ void features_kernel(int batch, int N, int L, int nsp, int npot, int 
   }
 }
 
+// Energies whose E - E_ref = Re((k a0)^2) / 2 Hartree (wave number of spin 0)
+// lies outside [e_lo, e_hi] eV get D = 1: no preconditioning there.
 __global__ void scatter_diag_kernel(int batch, int N, int L, int nsp, int lda, const int* __restrict__ atom_off,
                                     const int* __restrict__ atom_lmax, const float* __restrict__ Y,
-                                    float2* __restrict__ D) {
+                                    const double2* __restrict__ k, double e_lo, double e_hi, float2* __restrict__ D) {
   const int per = nsp * (L + 1) * (L + 1), O = 2 * (L + 1) * (L + 1);
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)batch * N * per) return;
@@ -200,7 +202,14 @@ __global__ void scatter_diag_kernel(int batch, int N, int L, int nsp, int lda, c
   if (q >= nsp * (lm + 1) * (lm + 1)) return;
   const int c = q / nsp;
   const float* y = Y + (size_t(b) * N + d) * O;
-  D[size_t(b) * lda + atom_off[d] + q] = make_float2(1.f + y[2 * c], y[2 * c + 1]);
+  bool on = true;
+  if (k) {
+    constexpr double kBohr = 0.529177249, kHartreeEv = 27.211396;
+    const double2 kk = k[size_t(b) * nsp];
+    const double e_ev = 0.5 * (kk.x * kk.x - kk.y * kk.y) * kBohr * kBohr * kHartreeEv;
+    on = e_ev >= e_lo && e_ev <= e_hi;
+  }
+  D[size_t(b) * lda + atom_off[d] + q] = on ? make_float2(1.f + y[2 * c], y[2 * c + 1]) : make_float2(1.f, 0.f);
 }
 
 }  // namespace
@@ -254,10 +263,11 @@ void launch_features(int batch, int N, int L, int nsp, int npot, const double2* 
 }
 
 void launch_scatter_diag(int batch, int N, int L, int nsp, int lda, const int* atom_off, const int* atom_lmax,
-                         const float* Y, float2* D, cudaStream_t s) {
+                         const float* Y, const double2* k, double e_lo, double e_hi, float2* D, cudaStream_t s) {
   const long long total = (long long)batch * N * nsp * (L + 1) * (L + 1);
   count_launch();
-  scatter_diag_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(batch, N, L, nsp, lda, atom_off, atom_lmax, Y, D);
+  scatter_diag_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(batch, N, L, nsp, lda, atom_off, atom_lmax, Y, k,
+                                                                    e_lo, e_hi, D);
 }
 
 cudaError_t MlpScratch::ensure(const MlpShape& sh, int S) {

@@ -59,8 +59,9 @@ const MlpShape* model_shape(const refeff_fms_precond_model* m);
 const float* model_params(const refeff_fms_precond_model* m);
 int model_lmax(const refeff_fms_precond_model* m);
 
-// D[b][state] = 1 + (Y[b*N + atom][2c] + i Y[..][2c+1]), c = channel of the state (spin-independent).
+// D[b][state] = 1 + (Y[b*N + atom][2c] + i Y[..][2c+1]), c = channel of the state (spin-independent);
+// with k (batch * nsp wave numbers), energies with E - E_ref outside [e_lo, e_hi] eV get D = 1.
 void launch_scatter_diag(int batch, int N, int L, int nsp, int lda, const int* atom_off, const int* atom_lmax,
-                         const float* Y, float2* D, cudaStream_t s);
+                         const float* Y, const double2* k, double e_lo, double e_hi, float2* D, cudaStream_t s);
 
 }  // namespace rfx

@@ -74,17 +74,25 @@ __global__ void __launch_bounds__(kSwThreads) fwd_sweep_kernel(BatchLayout lay, 
   __syncthreads();
   for (int k = 0; k < n; k += NB) {
     const int kb = min(NB, n - k);
-    // row moves of this panel, applied as one gather
-    const size_t pidx = size_t(b) * w.npanels + k / NB;
-    const int np = w.nperm[pidx];
-    const int2* pm = w.perm + pidx * (2 * NB);
-    for (int idx = tid; idx < np * CG; idx += kSwThreads) tmp[idx] = Y[pm[idx / CG].y * CG + idx % CG];
+    // row moves of this panel, applied as one gather; with paired blocks both
+    // blocks' moves are applied before the first block of the pair is solved
+    // (the second block's moves only touch rows below the first block)
+    const bool pair = w.pair128 && NB == 64;
+    const int p0 = k / NB;
+    const int nmoves = !pair ? 1 : (p0 % 2 == 1 ? 0 : (k + NB < n ? 2 : 1));
     for (int idx = tid; idx < kb * kb; idx += kSwThreads) {
       const int r = idx % kb, c = idx / kb;
       T[r * (NB + 1) + c] = Mb[size_t(k + r) + lda * size_t(k + c)];
     }
-    __syncthreads();
-    for (int idx = tid; idx < np * CG; idx += kSwThreads) Y[pm[idx / CG].x * CG + idx % CG] = tmp[idx];
+    for (int q = 0; q < nmoves; ++q) {
+      const size_t pidx = size_t(b) * w.npanels + p0 + q;
+      const int np = w.nperm[pidx];
+      const int2* pm = w.perm + pidx * (2 * NB);
+      for (int idx = tid; idx < np * CG; idx += kSwThreads) tmp[idx] = Y[pm[idx / CG].y * CG + idx % CG];
+      __syncthreads();
+      for (int idx = tid; idx < np * CG; idx += kSwThreads) Y[pm[idx / CG].x * CG + idx % CG] = tmp[idx];
+      __syncthreads();
+    }
     __syncthreads();
     // unit-lower solve of the block rows, one warp per column
     if (wid < ncols) {
@@ -227,6 +235,19 @@ bool fused_forward_sweep(int nb, const BatchLayout& lay, int batch, float2* M, c
                          cudaStream_t s) {
   if (nb == 64) return launch_sweep_nb<64>(true, lay, batch, M, &w, skip, s);
   if (nb == 32) return launch_sweep_nb<32>(true, lay, batch, M, &w, skip, s);
+  return false;
+}
+
+bool fused_sweep_available(int nb, const BatchLayout& lay) {
+  const int need = lay.m < 4 ? lay.m : 4;  // the narrowest column group launch_sweep_cg accepts
+  if (nb == 64) return SweepSmem<64, 8>::bytes(lay.n) <= kSwSmemBudget ||
+                       (need <= 4 && SweepSmem<64, 4>::bytes(lay.n) <= kSwSmemBudget) ||
+                       (need <= 2 && SweepSmem<64, 2>::bytes(lay.n) <= kSwSmemBudget) ||
+                       (need <= 1 && SweepSmem<64, 1>::bytes(lay.n) <= kSwSmemBudget);
+  if (nb == 32) return SweepSmem<32, 8>::bytes(lay.n) <= kSwSmemBudget ||
+                       (need <= 4 && SweepSmem<32, 4>::bytes(lay.n) <= kSwSmemBudget) ||
+                       (need <= 2 && SweepSmem<32, 2>::bytes(lay.n) <= kSwSmemBudget) ||
+                       (need <= 1 && SweepSmem<32, 1>::bytes(lay.n) <= kSwSmemBudget);
   return false;
 }
 

@@ -1,6 +1,7 @@
 // Tensor-core (tcgen05, sm_103a) trailing update of the FP32 LU:
-//     C[r, c] -= sum_k A[r, k] B[k, c]      (complex, K = panel width <= 64)
-// with A = L21 (rows below the panel) and B = U12 (panel rows, trailing columns).
+//     C[r, c] -= sum_k A[r, k] B[k, c]      (complex, K <= 128)
+// with A = L21 (rows below the block) and B = U12 (block rows, trailing
+// columns); K is one 64-column block, or two when the elimination pairs them.
 //
 // Each complex product is formed from real TF32 MMAs with FP32 accumulation in
 // tensor memory, using a two-term split x = hi + lo (hi = tf32(x), lo =
@@ -11,7 +12,7 @@
 // already in the UMMA shared-memory layout (K-major, 128-byte rows, 128-byte
 // swizzle), so the update kernel moves them with plain cp.async.bulk copies
 // completed on mbarriers.  The update runs as one persistent, warp-specialised
-// CTA per SM over 128 x 48 complex tiles (tc_update_persistent_kernel below).
+// CTA per SM over 128 x 64 complex tiles (tc_update_persistent_kernel below).
 // Every wait on an mbarrier is bounded; on timeout the kernel records an error
 // flag, ends every role, waits for its copies and MMAs in flight, frees its
 // tensor memory and returns.
@@ -25,14 +26,20 @@ namespace rfx {
 namespace {
 
 constexpr int BM = kTcBM;         // 128 rows per tile (MMA M)
-constexpr int BN = kTcBN;         // 48 columns per tile (MMA N)
-constexpr int KC = 32;            // K elements per chunk: 32 x 4 B = one 128-byte swizzle row
-constexpr int A_PLANE = BM * 128; // bytes per A plane per chunk (16 KB)
-constexpr int B_PLANE = BN * 128; // bytes per B plane per chunk (6 KB)
+constexpr int BN = kTcBN;         // 64 columns per tile (MMA N)
+// Operand rows of kRowBytes bytes with the matching swizzle (128 or 64): with
+// 128-byte rows a K chunk holds KC = 32 TF32 values per row.  64-byte rows
+// (half the chunk, twice the ring depth) measured slower: the update is bound
+// by the tensor pipe, not by the depth of the operand ring.
+constexpr int kRowBytes = 128;
+constexpr int KC = kRowBytes / 4;          // K elements per chunk
+constexpr int A_PLANE = BM * kRowBytes;    // bytes per A plane per chunk (16 KB)
+constexpr int B_PLANE = BN * kRowBytes;    // bytes per B plane per chunk (8 KB)
 constexpr int A_PLANES = 4;       // re_hi, re_lo, im_hi, im_lo
 constexpr int B_PLANES = 6;       // re_hi, re_lo, im_hi, im_lo, -im_hi, -im_lo
-constexpr int SMEM_OPS = A_PLANES * A_PLANE + B_PLANES * B_PLANE;  // 100 KB
+constexpr int SMEM_OPS = A_PLANES * A_PLANE + B_PLANES * B_PLANE;  // 112 KB
 constexpr long long kWaitLimit = kTcWaitPolls;  // drains of copies and MMAs in flight
+constexpr int kChunks = kTcKMax / KC;  // K chunks per tile image (K up to 128)
 
 __device__ __forceinline__ uint32_t tf32_bits(float x) {
   uint32_t r;
@@ -40,10 +47,13 @@ __device__ __forceinline__ uint32_t tf32_bits(float x) {
   return r;
 }
 
-// Byte offset of element (row, k) (k < 32, 4 bytes) in a K-major tile with
-// 128-byte rows and the 128-byte swizzle (16-byte chunk index XOR row % 8).
-__device__ __forceinline__ int sw128_offset(int row, int k) {
-  return row * 128 + ((((k >> 2) ^ (row & 7))) << 4) + ((k & 3) << 2);
+// Byte offset of element (row, k) (k < KC, 4 bytes) in a K-major tile of
+// kRowBytes-byte rows with the matching swizzle: the 16-byte chunk index is
+// XORed with address bits [7, 10) shifted down (row % 8 for 128-byte rows,
+// (row / 2) % 4 for 64-byte rows), the canonical UMMA layouts.
+__device__ __forceinline__ int sw_offset(int row, int k) {
+  if constexpr (kRowBytes == 128) return row * 128 + ((((k >> 2) ^ (row & 7))) << 4) + ((k & 3) << 2);
+  return row * 64 + ((((k >> 2) ^ ((row >> 1) & 3))) << 4) + ((k & 3) << 2);
 }
 
 __device__ __forceinline__ void split4(float2 v, uint32_t out[4]) {
@@ -58,11 +68,12 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
-  // start address >> 4 (14 bits), LBO = 1 (unused for swizzled K-major), SBO = 1024 B (8-row groups),
-  // descriptor version 1, base offset 0, layout type 2 = 128-byte swizzle.
-  return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) |
-         (uint64_t(2) << 61);
+__device__ __forceinline__ uint64_t umma_desc_sw(uint32_t saddr) {
+  // start address >> 4 (14 bits), LBO = 1 (unused for swizzled K-major), SBO = 8 rows (the 8-row groups),
+  // descriptor version 1, base offset 0, layout type 2 = 128-byte swizzle / 4 = 64-byte swizzle.
+  constexpr uint64_t kLayout = kRowBytes == 128 ? 2 : 4;
+  return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t(1) << 16) | (uint64_t((8 * kRowBytes) >> 4) << 32) |
+         (uint64_t(1) << 46) | (kLayout << 61);
 }
 
 // kind::tf32, D = F32, A = B = TF32, both K-major, N = BN, M = BM.
@@ -98,7 +109,7 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// operand images: A[b][bm][chunk][plane] (16 KB), B[b][bn][chunk][plane] (6 KB)
+// operand images: A[b][bm][chunk][plane] (16 KB), B[b][bn][chunk][plane] (8 KB), chunks of KC = 32
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k, int kb, const float2* __restrict__ M,
                                                          uint8_t* __restrict__ img, int nbm) {
@@ -107,7 +118,8 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k,
   // swizzled K-major rows, so that every warp stores 512 contiguous bytes.
   constexpr int TS = BM + 1;  // padded row of the transposed tile
   __shared__ float2 T[KC * TS];
-  const int bm = blockIdx.x >> 1, chunk = blockIdx.x & 1, b = blockIdx.y;
+  const int nch = (kb + KC - 1) / KC;  // the grid holds nch chunks per row tile
+  const int bm = blockIdx.x / nch, chunk = blockIdx.x % nch, b = blockIdx.y;
   const int n = lay.n;
   const int r0 = k + kb + bm * BM;
   const float2* Mb = M + size_t(b) * lay.stride;
@@ -117,7 +129,7 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k,
     T[kk * TS + r] = (r0 + r < n && kcol < kb) ? Mb[size_t(r0 + r) + size_t(lay.lda) * (k + kcol)] : make_float2(0.f, 0.f);
   }
   __syncthreads();
-  uint8_t* base = img + ((size_t(b) * nbm + bm) * 2 + chunk) * size_t(A_PLANES) * A_PLANE;
+  uint8_t* base = img + ((size_t(b) * nbm + bm) * kChunks + chunk) * size_t(A_PLANES) * A_PLANE;
   for (int e = threadIdx.x; e < BM * (KC / 4); e += blockDim.x) {
     const int k4 = e % (KC / 4), r = e / (KC / 4);
     uint32_t q[4][4];
@@ -128,7 +140,7 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k,
 #pragma unroll
       for (int p = 0; p < 4; ++p) q[p][i] = sv[p];
     }
-    const int off = sw128_offset(r, 4 * k4);
+    const int off = sw_offset(r, 4 * k4);
 #pragma unroll
     for (int p = 0; p < 4; ++p)
       *reinterpret_cast<uint4*>(base + size_t(p) * A_PLANE + off) = make_uint4(q[p][0], q[p][1], q[p][2], q[p][3]);
@@ -138,10 +150,11 @@ __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k,
 __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k, int kb, int col_end,
                                                          const float2* __restrict__ M, uint8_t* __restrict__ img,
                                                          int nbn) {
-  const int bn = blockIdx.x >> 1, chunk = blockIdx.x & 1, b = blockIdx.y;
+  const int nch = (kb + KC - 1) / KC;  // the grid holds nch chunks per column tile
+  const int bn = blockIdx.x / nch, chunk = blockIdx.x % nch, b = blockIdx.y;
   const int c0 = k + kb + bn * BN;
   const float2* Mb = M + size_t(b) * lay.stride;
-  uint8_t* base = img + ((size_t(b) * nbn + bn) * 2 + chunk) * size_t(B_PLANES) * B_PLANE;
+  uint8_t* base = img + ((size_t(b) * nbn + bn) * kChunks + chunk) * size_t(B_PLANES) * B_PLANE;
   for (int e = threadIdx.x; e < BN * KC; e += blockDim.x) {
     const int kk = e % KC, c = e / KC;
     const int krow = chunk * KC + kk;
@@ -149,7 +162,7 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
     if (c0 + c < col_end && krow < kb) v = Mb[size_t(k + krow) + size_t(lay.lda) * (c0 + c)];
     uint32_t s[4];
     split4(v, s);
-    const int off = sw128_offset(c, kk);
+    const int off = sw_offset(c, kk);
 #pragma unroll
     for (int p = 0; p < 4; ++p) *reinterpret_cast<uint32_t*>(base + size_t(p) * B_PLANE + off) = s[p];
     *reinterpret_cast<uint32_t*>(base + size_t(4) * B_PLANE + off) = s[2] ^ 0x80000000u;  // -im_hi
@@ -162,9 +175,9 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
 // ---------------------------------------------------------------------------
 // One CTA per SM walks the tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
 // (t -> matrix b, row tile bm, column tile bn, bn fastest).  Roles:
-//   warp 0   producer: bulk-copies each K-chunk (100 KB of planes) into a
+//   warp 0   producer: bulk-copies each K-chunk (112 KB of planes) into a
 //            two-stage ring, waiting for the stage to be released;
-//   warp 1   MMA: 24 tcgen05.mma per chunk into one of two TMEM accumulators
+//   warp 1   MMA: 48 tcgen05.mma per chunk into one of four TMEM accumulators
 //            (128 columns each), releasing the stage with tcgen05.commit and
 //            signalling the tile's accumulator the same way;
 //   warps 2-17   four epilogue groups of four warps, group g taking the tiles
@@ -176,11 +189,16 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
 // the error flag and a shared abort flag that ends every role's loop, then
 // the producer waits (bounded) for its copies still in flight and the MMA
 // thread for its MMAs before the tensor memory is freed.
-constexpr int kPStages = 2;
+constexpr int kPStages = 2;                    // operand ring depth (2 x 112 KB)
 constexpr int kPGroups = 4;                     // epilogue groups of 4 warps, one accumulator each
 constexpr int kPThreads = 64 + kPGroups * 128;  // producer warp, MMA warp, epilogue groups
 constexpr uint32_t kPTmemCols = 512;  // kPGroups * 128 columns, rounded up to a power of two
-constexpr int kPSmem = kPStages * SMEM_OPS + 1024 + 256;
+// barriers: full[kPStages], empty[kPStages], acc_full[kPGroups], acc_empty[kPGroups], drain
+constexpr int kBarFull = 0, kBarEmpty = kPStages, kBarAccFull = 2 * kPStages, kBarAccEmpty = 2 * kPStages + kPGroups,
+              kBarDrain = 2 * kPStages + 2 * kPGroups;
+static_assert((kBarDrain + 1) * 8 <= 256, "barrier area");
+constexpr int kPSmem = kPStages * SMEM_OPS + 1024 + 512;
+static_assert(kPSmem <= 227 * 1024, "dynamic shared memory per CTA");
 
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                                    int* err_flag, long long polls) {
@@ -220,16 +238,16 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
   const uint32_t sbase = (raw + 1023u) & ~1023u;
   uint8_t* const gbase = smraw + (sbase - raw);
   uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + kPStages * SMEM_OPS);
-  // bars: full[2], empty[2], acc_full[4], acc_empty[4], drain
+  // bars at kBarFull / kBarEmpty / kBarAccFull / kBarAccEmpty / kBarDrain; then the TMEM slot and flags
   auto bar = [&](int i) { return smem_u32(&bars[i]); };
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kPStages * SMEM_OPS + 128);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(gbase + kPStages * SMEM_OPS + 132);
-  int* consumed = reinterpret_cast<int*>(gbase + kPStages * SMEM_OPS + 136);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kPStages * SMEM_OPS + 256);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(gbase + kPStages * SMEM_OPS + 260);
+  int* consumed = reinterpret_cast<int*>(gbase + kPStages * SMEM_OPS + 264);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n = lay.n;
   const int per_matrix = nbm * nbn;
   const int total = per_matrix * batch;  // the host keeps this below 2^31
-  const int nchunks = kb > KC ? 2 : 1;
+  const int nchunks = (kb + KC - 1) / KC;  // 1 .. kChunks
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -238,14 +256,14 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
   }
   if (tid == 32) {
     for (int i = 0; i < kPStages; ++i) {
-      mbar_init(bar(i), 1);             // full: the producer's expect_tx
-      mbar_init(bar(2 + i), 1);         // empty: one commit
+      mbar_init(bar(kBarFull + i), 1);   // full: the producer's expect_tx
+      mbar_init(bar(kBarEmpty + i), 1);  // empty: one commit
     }
     for (int a = 0; a < kPGroups; ++a) {
-      mbar_init(bar(4 + a), 1);             // accumulator full: one commit
-      mbar_init(bar(4 + kPGroups + a), 128);  // accumulator empty: the 128 threads of one epilogue group
+      mbar_init(bar(kBarAccFull + a), 1);     // accumulator full: one commit
+      mbar_init(bar(kBarAccEmpty + a), 128);  // accumulator empty: the 128 threads of one epilogue group
     }
-    mbar_init(bar(4 + 2 * kPGroups), 1);  // drain
+    mbar_init(bar(kBarDrain), 1);  // drain
     *abort_flag = 0;
     *consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -270,19 +288,19 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
         int b, bm, bn;
         tile_of(t, b, bm, bn);
         if (skip && skip[b]) continue;
-        const uint8_t* ab = aimg + (size_t(b) * nbm_all + bm) * 2 * size_t(A_PLANES) * A_PLANE;
-        const uint8_t* bb = bimg + (size_t(b) * nbn_all + bn) * 2 * size_t(B_PLANES) * B_PLANE;
+        const uint8_t* ab = aimg + (size_t(b) * nbm_all + bm) * kChunks * size_t(A_PLANES) * A_PLANE;
+        const uint8_t* bb = bimg + (size_t(b) * nbn_all + bn) * kChunks * size_t(B_PLANES) * B_PLANE;
         bool ok = true;
         for (int ch = 0; ch < nchunks; ++ch, ++c) {
           const int st = int(c % kPStages);
           const uint32_t ph = uint32_t((c / kPStages) & 1);
-          if (!mbar_wait_or_abort(bar(2 + st), ph ^ 1u, abort_flag, err_flag, polls)) { ok = false; break; }
+          if (!mbar_wait_or_abort(bar(kBarEmpty + st), ph ^ 1u, abort_flag, err_flag, polls)) { ok = false; break; }
           const uint32_t sA = sbase + uint32_t(st) * SMEM_OPS, sB = sA + A_PLANES * A_PLANE;
-          mbar_expect_tx(bar(st), uint32_t(SMEM_OPS));
+          mbar_expect_tx(bar(kBarFull + st), uint32_t(SMEM_OPS));
           const uint8_t* ach = ab + size_t(ch) * A_PLANES * A_PLANE;
           const uint8_t* bch = bb + size_t(ch) * B_PLANES * B_PLANE;
-          for (int p = 0; p < A_PLANES; ++p) bulk_copy(sA + p * A_PLANE, ach + size_t(p) * A_PLANE, A_PLANE, bar(st));
-          for (int p = 0; p < B_PLANES; ++p) bulk_copy(sB + p * B_PLANE, bch + size_t(p) * B_PLANE, B_PLANE, bar(st));
+          for (int p = 0; p < A_PLANES; ++p) bulk_copy(sA + p * A_PLANE, ach + size_t(p) * A_PLANE, A_PLANE, bar(kBarFull + st));
+          for (int p = 0; p < B_PLANES; ++p) bulk_copy(sB + p * B_PLANE, bch + size_t(p) * B_PLANE, B_PLANE, bar(kBarFull + st));
         }
         if (!ok) break;
       }
@@ -295,7 +313,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
             asm volatile(
                 "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
                 : "=r"(done)
-                : "r"(bar(int(q % kPStages))), "r"(uint32_t((q / kPStages) & 1))
+                : "r"(bar(kBarFull + int(q % kPStages))), "r"(uint32_t((q / kPStages) & 1))
                 : "memory");
             if (done || ((it & 1023) == 1023 && global_ns() - t0 > 1000000000ull)) break;
           }
@@ -312,21 +330,21 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
         tile_of(t, b, bm, bn);
         if (skip && skip[b]) continue;
         const int a = int(i % kPGroups);
-        if (!mbar_wait_or_abort(bar(4 + kPGroups + a), uint32_t(((i / kPGroups) & 1) ^ 1), abort_flag, err_flag, polls))
+        if (!mbar_wait_or_abort(bar(kBarAccEmpty + a), uint32_t(((i / kPGroups) & 1) ^ 1), abort_flag, err_flag, polls))
           break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t tmem_r = tmem + uint32_t(a * 128), tmem_i = tmem_r + 64;
         bool ok = true;
         for (int ch = 0; ch < nchunks; ++ch, ++c) {
           const int st = int(c % kPStages);
-          if (!mbar_wait_or_abort(bar(st), uint32_t((c / kPStages) & 1), abort_flag, err_flag, polls)) { ok = false; break; }
+          if (!mbar_wait_or_abort(bar(kBarFull + st), uint32_t((c / kPStages) & 1), abort_flag, err_flag, polls)) { ok = false; break; }
           *(volatile int*)consumed = int(c + 1);
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t sA = sbase + uint32_t(st) * SMEM_OPS, sB = sA + A_PLANES * A_PLANE;
           for (int ks = 0; ks < KC / 8; ++ks) {
             const uint32_t koff = uint32_t(ks * 32);
-            auto ad = [&](int p) { return umma_desc_sw128(sA + p * A_PLANE + koff); };
-            auto bd = [&](int p) { return umma_desc_sw128(sB + p * B_PLANE + koff); };
+            auto ad = [&](int p) { return umma_desc_sw(sA + p * A_PLANE + koff); };
+            auto bd = [&](int p) { return umma_desc_sw(sB + p * B_PLANE + koff); };
             const uint32_t acc0 = (ch == 0 && ks == 0) ? 0u : 1u;
             // Cr += Ar Br + Ai (-Bi)
             mma_tf32(tmem_r, ad(0), bd(0), acc0);
@@ -344,22 +362,22 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
             mma_tf32(tmem_i, ad(3), bd(0), 1u);
           }
           issued = true;
-          umma_commit(bar(2 + st));  // the stage is free once these MMAs have read it
+          umma_commit(bar(kBarEmpty + st));  // the stage is free once these MMAs have read it
         }
         if (!ok) break;
-        umma_commit(bar(4 + a));  // the accumulator is complete
+        umma_commit(bar(kBarAccFull + a));  // the accumulator is complete
         ++i;
       }
       if (issued) {
         // every MMA of this CTA has completed before the tensor memory is freed
-        umma_commit(bar(4 + 2 * kPGroups));
+        umma_commit(bar(kBarDrain));
         const uint64_t t0 = global_ns();
         for (long long it = 0; it < kWaitLimit; ++it) {
           uint32_t done;
           asm volatile(
               "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
               : "=r"(done)
-              : "r"(bar(4 + 2 * kPGroups))
+              : "r"(bar(kBarDrain))
               : "memory");
           if (done || ((it & 1023) == 1023 && global_ns() - t0 > 1000000000ull)) break;
         }
@@ -389,7 +407,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
 #pragma unroll
       for (int j = 0; j < 16; ++j)
         cn[j] = (row_ok && c0 + j < col_end) ? crow[j * ld] : make_float2(0.f, 0.f);
-      const bool ready = mbar_wait_or_abort(bar(4 + g), uint32_t((mine / kPGroups) & 1), abort_flag, err_flag, polls);
+      const bool ready = mbar_wait_or_abort(bar(kBarAccFull + g), uint32_t((mine / kPGroups) & 1), abort_flag, err_flag, polls);
       if (!__all_sync(0xffffffffu, ready)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tmem_r = tmem + uint32_t(g * 128) + lane_off, tmem_i = tmem_r + 64;
@@ -432,7 +450,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(bar(4 + kPGroups + g));  // the accumulator may be overwritten
+      mbar_arrive(bar(kBarAccEmpty + g));  // the accumulator may be overwritten
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -445,7 +463,7 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
 // ---------------------------------------------------------------------------
 size_t tc_image_bytes(int n, int m, int batch) {
   const int nbm = (n + BM - 1) / BM, nbn = (n + m + BN - 1) / BN;
-  return size_t(batch) * 2 * (size_t(nbm) * A_PLANES * A_PLANE + size_t(nbn) * B_PLANES * B_PLANE);
+  return size_t(batch) * kChunks * (size_t(nbm) * A_PLANES * A_PLANE + size_t(nbn) * B_PLANES * B_PLANE);
 }
 
 void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int col_end, float2* M, uint8_t* images,
@@ -454,12 +472,13 @@ void tc_trailing_update(const BatchLayout& lay, int batch, int k, int kb, int co
   if (rows <= 0 || cols <= 0 || kb <= 0) return;
   const int nbm_all = (lay.n + BM - 1) / BM, nbn_all = (lay.n + lay.m + BN - 1) / BN;
   uint8_t* aimg = images;
-  uint8_t* bimg = images + size_t(batch) * 2 * size_t(nbm_all) * A_PLANES * A_PLANE;
+  uint8_t* bimg = images + size_t(batch) * kChunks * size_t(nbm_all) * A_PLANES * A_PLANE;
   const int nbm = (rows + BM - 1) / BM, nbn = (cols + BN - 1) / BN;
   count_launch();
-  tc_split_a_kernel<<<dim3(unsigned(2 * nbm), unsigned(batch)), 256, 0, s>>>(lay, k, kb, M, aimg, nbm_all);
+  const int nch = (kb + KC - 1) / KC;
+  tc_split_a_kernel<<<dim3(unsigned(nch * nbm), unsigned(batch)), 256, 0, s>>>(lay, k, kb, M, aimg, nbm_all);
   count_launch();
-  tc_split_b_kernel<<<dim3(unsigned(2 * nbn), unsigned(batch)), 256, 0, s>>>(lay, k, kb, col_end, M, bimg, nbn_all);
+  tc_split_b_kernel<<<dim3(unsigned(nch * nbn), unsigned(batch)), 256, 0, s>>>(lay, k, kb, col_end, M, bimg, nbn_all);
   const int sms = current_sm_count();
   ensure_smem_limit(reinterpret_cast<const void*>(tc_update_persistent_kernel), size_t(kPSmem));
   const long long tiles = (long long)nbm * nbn * batch;

@@ -61,6 +61,11 @@ class _EnergyPoints(C.Structure):
     _fields_ = [("n_energies", C.c_int), ("wave_numbers", _p), ("phase_shifts", _p)]
 
 
+class _Tuning(C.Structure):
+    _fields_ = [("streams", C.c_int), ("buckets", C.c_int), ("seconds_default", C.c_double),
+                ("seconds_tuned", C.c_double), ("from_cache", C.c_int)]
+
+
 class _Report(C.Structure):
     _fields_ = [("seconds", C.c_double), ("refinement_iterations", C.c_int), ("residual_max", C.c_double),
                 ("energies_failed", C.c_int), ("fp64_fallbacks", C.c_int)]
@@ -105,6 +110,7 @@ def load(build_if_missing: bool = True):
         "refeff_ff2x_xanes_mu": ([_i, _i, _i, _i, _i, _i, _p, _p, _p, _p, _p, C.c_double, C.c_double, C.c_double,
                                   C.c_double, _p, _p, _p], _i),
         "refeff_ff2x_lorentz_convolve": ([_i, _p, _p, C.c_double, _p], _i),
+        "refeff_ff2x_debye_factor": ([_i, _p, C.c_double, _p, _p, _p], _i),
         "refeff_fms_write_gg_diag_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
         "refeff_fms_real_space_plan_destroy": ([_p], None),
         "refeff_fms_plan_query": ([_p, _p, _p, _p, _p], _i),
@@ -145,6 +151,10 @@ def load(build_if_missing: bool = True):
         "refeff_fms_plan_precond_features": ([_p, _p, _p], _i),
         "refeff_fms_plan_inverse_diagonal": ([_p, _p, _i, _p, _p], _i),
         "refeff_fms_geometry_from_feff_inp": ([C.c_char_p, _i, _p, _p, _p, _i, _p, _p], _i),
+        "refeff_fms_autotune_multi": ([_p, _i, _p, _p, _i, _i, C.c_char_p, _p], _i),
+        "refeff_fms_plan_set_tuning": ([_p, _i, _i], _i),
+        "refeff_fms_plan_set_precond_window": ([_p, C.c_double, C.c_double], _i),
+        "refeff_fms_plan_get_tuning": ([_p, _p, _p], _i),
         "refeff_fms_write_geom_dat": ([C.c_char_p, C.c_char_p], _i),
         "refeff_fms_feff_inp_last_error": ([], C.c_char_p),
     }
@@ -193,6 +203,8 @@ class Context:
     OPT_TENSOR_CORES = 1
     OPT_DENSE_REFINEMENT = 2
     OPT_TC_WAIT_POLLS = 3
+    OPT_PAIRED_BLOCKS = 4
+    OPT_MULTI_STREAMS = 5
 
     def set_option(self, option: int, value: int):
         """Context option (applies to plans / dense solves started afterwards)."""
@@ -239,6 +251,15 @@ class FmsRealSpacePlan:
     def set_batch(self, max_batch: int):
         self.ctx.check(self.ctx._lib.refeff_fms_plan_set_batch(self.handle, int(max_batch)))
 
+    def set_tuning(self, inner_width: int = 0, paired_blocks: int = -1):
+        """FP32 elimination choices of this plan (refeff_fms_plan_set_tuning)."""
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_tuning(self.handle, int(inner_width), int(paired_blocks)))
+
+    def tuning(self):
+        i, p = C.c_int(), C.c_int()
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_get_tuning(self.handle, C.byref(i), C.byref(p)))
+        return i.value, p.value
+
     def set_refinement(self, max_iterations: int, tolerance: float):
         self.ctx.check(self.ctx._lib.refeff_fms_plan_set_refinement(self.handle, int(max_iterations), float(tolerance)))
 
@@ -268,6 +289,10 @@ class FmsRealSpacePlan:
         self._model = model  # the plan does not own the model: keep it alive here
         self.ctx.check(self.ctx._lib.refeff_fms_plan_set_preconditioner(self.handle,
                                                                          model.handle if model else None))
+
+    def set_precond_window(self, e_lo_ev: float = -1e300, e_hi_ev: float = 1e300):
+        """Apply the learned preconditioner only for E - E_ref in [e_lo_ev, e_hi_ev] eV."""
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_precond_window(self.handle, float(e_lo_ev), float(e_hi_ev)))
 
     def set_bicgstab(self, max_iterations=400, tolerance=1e-6, poll_interval=8):
         self.ctx.check(self.ctx._lib.refeff_fms_plan_set_bicgstab(self.handle, int(max_iterations),
@@ -595,6 +620,18 @@ def reciprocal_core_hole(green, absorber_offset, t_difference):
     return np.array(out)
 
 
+def ff2x_debye_factor(wave_number, sig_gk, mu0, chi):
+    """FF2X's sig_gk Debye factor on chi (refeff_ff2x_debye_factor): returns (mu, chi)."""
+    k = np.ascontiguousarray(wave_number, np.float64)
+    c = np.array(chi, np.float64)
+    m0 = np.ascontiguousarray(mu0, np.float64)
+    mu = np.zeros_like(c)
+    rc = load().refeff_ff2x_debye_factor(len(k), _ptr(k), float(sig_gk), _ptr(m0), _ptr(c), _ptr(mu))
+    if rc:
+        raise FmsError(rc, "ff2x debye factor")
+    return mu, c
+
+
 def ff2x_lorentz_convolve(omega, spectrum, width):
     """FEFF conv (crates/refeff-core/src/convolution/lorentzian.rs:32-100), host only."""
     lib = load()
@@ -835,3 +872,26 @@ def fms_real_space_spectrum_multi(plans, wave_numbers, phase_shifts, form=FORM_F
         tables.append(np.stack([t[e].reshape((Cc, Cc, npot), order="F") for e in range(E)]) if E else
                       np.zeros((0, Cc, Cc, npot), np.complex128))
     return tables, sts
+
+
+def autotune_multi(plans, wave_numbers, phase_shifts, form=FORM_FP32_REFINED, sample_energies=16, cache_path=None):
+    """Tune the many-cluster call for these plans (refeff_fms_autotune_multi): per size bucket the inner panel
+    width and block pairing, then the stream count; cached under cache_path.  Returns a dict of the choice."""
+    ctx = plans[0].ctx
+    keep, pts = [], (_EnergyPoints * len(plans))()
+    for i, plan in enumerate(plans):
+        nsp, L, npot = plan.inputs["nsp"], plan.inputs["L"], plan.inputs["npot"]
+        k = np.ascontiguousarray(np.asarray(wave_numbers[i], dtype=np.complex128).reshape(-1, nsp))
+        E = k.shape[0]
+        ph = np.asarray(phase_shifts[i], dtype=np.complex128).reshape(E, nsp, 2 * L + 1, npot)
+        x = np.ascontiguousarray(np.stack([ph[e].reshape(-1, order="F") for e in range(E)])) if E else \
+            np.zeros((0, nsp * (2 * L + 1) * npot), np.complex128)
+        keep += [k, x]
+        pts[i].n_energies, pts[i].wave_numbers, pts[i].phase_shifts = E, _ptr(k), _ptr(x)
+    handles = (_p * len(plans))(*[p.handle for p in plans])
+    out = _Tuning()
+    path = None if cache_path is None else str(cache_path).encode()
+    ctx.check(ctx._lib.refeff_fms_autotune_multi(ctx.handle, len(plans), handles, pts, int(form), int(sample_energies),
+                                                 path, C.byref(out)))
+    return {"streams": out.streams, "buckets": out.buckets, "seconds_default": out.seconds_default,
+            "seconds_tuned": out.seconds_tuned, "from_cache": bool(out.from_cache)}

@@ -147,3 +147,20 @@ def test_invalid_rows_are_rejected():
     with pytest.raises(fms.FmsError) as e:
         fms.ff2x_xanes_mu(ne1=d["ne1"], **bad)
     assert e.value.code == 6
+
+
+@pytest.mark.parametrize("sig_gk", [0.0, 5e-5, 0.02, 0.08])
+def test_debye_factor_matches_oracle(sig_gk):
+    """FF2X's sig_gk Debye factor (ff2x.rs:3388-3397): chi damped by exp(-(sig_gk k)^2) above the 1e-4
+    threshold, mu = mu0 + chi, through the C ABI against the oracle."""
+    rng = np.random.default_rng(4)
+    k = np.linspace(0.0, 12.0, 57)
+    mu0 = 1.0 + 0.1 * rng.normal(size=57)
+    chi = 0.05 * rng.normal(size=57)
+    mu, c = fms.ff2x_debye_factor(k, sig_gk, mu0, chi)
+    mu_o, c_o = fo.debye_factor(k, sig_gk, mu0, chi)
+    assert np.allclose(c, c_o, rtol=1e-15, atol=0) and np.allclose(mu, mu_o, rtol=1e-15, atol=1e-17)
+    if sig_gk <= 1e-4:
+        assert np.array_equal(c, chi)
+    else:
+        assert abs(c[-1]) < abs(chi[-1])

@@ -98,6 +98,39 @@ def test_tensor_core_update_matches_cuda_cores(n, m):
         assert rel_err(out[1][b], out[0][b]) < 1e-5
 
 
+@pytest.mark.parametrize("n,m", [(300, 4), (700, 16), (1100, 25)])
+def test_paired_blocks_match_single_blocks_with_pivoting(n, m):
+    """FP32 LU on the tensor cores with paired 64-column blocks (one K = 128 update per pair, the second block's
+    moves applied to the first block's L, its block row corrected by the first block's deferred update) against
+    one update per block, on unscaled random systems that pivot in almost every column; without refinement both
+    must be FP32-accurate solutions, and with it both must reach the FP64 answer."""
+    rng = np.random.default_rng(3 * n + m)
+    A = rng.normal(size=(2, n, n)) + 1j * rng.normal(size=(2, n, n))
+    B = rng.normal(size=(2, n, m)) + 1j * rng.normal(size=(2, n, m))
+    ref = [np.linalg.solve(A[b], B[b]) for b in range(2)]
+    raw, refined = {}, {}
+    for paired in (0, 1):
+        c = fms.Context(0)
+        c.set_option(c.OPT_PAIRED_BLOCKS, paired)
+        c.set_option(c.OPT_DENSE_REFINEMENT, 0)
+        raw[paired], st, _ = fms.complex_lu_solve_batched(c, A, B, fms.FORM_FP32_REFINED)
+        assert (st == 10).all()
+        c.set_option(c.OPT_DENSE_REFINEMENT, 10)
+        refined[paired], st, _ = fms.complex_lu_solve_batched(c, A, B, fms.FORM_FP32_REFINED)
+        assert (st == 0).all()
+        c.close()
+    for b in range(2):
+        # complex64 LAPACK reaches ~1e-6 on these systems (condition numbers 4e2 - 4e3); the split-TF32 products
+        # keep 22 of FP32's 24 bits and the block rows use the explicit L11^-1, so the GPU's unrefined FP32
+        # solutions land near 1e-4 (measured 1.7e-4 at n = 700); a wrong row order or a missed deferred update
+        # gives O(1) errors
+        assert rel_err(raw[0][b], ref[b]) < 2e-3
+        assert rel_err(raw[1][b], ref[b]) < 2e-3
+        assert rel_err(raw[1][b], raw[0][b]) < 2e-3
+        assert rel_err(refined[1][b], ref[b]) < 1e-10
+        assert rel_err(refined[0][b], ref[b]) < 1e-10
+
+
 def test_dense_lu_singular_reports_pivot(ctx):
     n = 40
     rng = np.random.default_rng(5)

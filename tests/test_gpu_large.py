@@ -116,3 +116,36 @@ def test_config2_many_clusters_in_one_call(ctx):
             m = plans[i].shape.absorber_block
             for e in range(len(sel)):
                 assert rel_err(tables[i][e, :m, :m, 0], ref[e, :m, :m, 0]) < tol, (i, e)
+
+
+def test_autotuned_many_cluster_call_matches_default(ctx, tmp_path):
+    """The batched form's autotuner (per size bucket: inner panel width and block pairing; then the stream count)
+    on 10 of config 2's clusters with a 4-energy sample: the tuned many-cluster call gives the default call's
+    results (both within the chosen-form gate of the FP64 LU), the choice is written to the JSON cache, and a
+    second call with the same workload applies it from the cache without measuring."""
+    import json
+    cases = wl.config2()[::3]
+    sel = np.array([0, 40, 80, 120, 149])
+    plans = [fms.fms_real_space_plan(ctx, c.positions, c.potentials, c.lmaxph) for c, _ in cases]
+    ks = [g.wave_numbers[sel] for _, g in cases]
+    phs = [g.phase_shifts[sel] for _, g in cases]
+    ref64, _ = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP64_LU)
+    before, _ = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED)
+    cache = tmp_path / "autotune.json"
+    got = fms.autotune_multi(plans, ks, phs, fms.FORM_FP32_REFINED, sample_energies=4, cache_path=cache)
+    assert not got["from_cache"] and got["streams"] in (2, 4, 8, 16) and got["buckets"] >= 2
+    assert got["seconds_tuned"] <= got["seconds_default"] * 1.5
+    entries = json.loads(cache.read_text())["entries"]
+    assert len(entries) == 1 and next(iter(entries.values()))["streams"] == got["streams"]
+    after, sts = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED)
+    assert all((s == 0).all() for s in sts)
+    for p, a, b, r in zip(plans, after, before, ref64):
+        m = p.shape.absorber_block
+        assert rel_err(a[:, :m, :m, 0], r[:, :m, :m, 0]) < TOL_CHOSEN
+        assert rel_err(b[:, :m, :m, 0], r[:, :m, :m, 0]) < TOL_CHOSEN
+    for p in plans:
+        p.set_tuning(0, -1)
+    again = fms.autotune_multi(plans, ks, phs, fms.FORM_FP32_REFINED, sample_energies=4, cache_path=cache)
+    assert again["from_cache"] and again["streams"] == got["streams"]
+    for p in plans:
+        p.close()
