@@ -475,6 +475,7 @@ def profile_case(args):
     E = args.energies
     form = {"fp32": fms.FORM_FP32_REFINED, "fp64": fms.FORM_FP64_LU, "bicgstab": fms.FORM_BICGSTAB}[args.form]
     ctx = fms.Context(0)
+    ctx.set_option(ctx.OPT_DUAL_STREAMS, 0)  # one batch per sweep: ncu's launch counts follow the sweep
     plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
     plan.set_batch(E)
     status = None

@@ -133,6 +133,13 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     estimated cost (energies x n^3), largest first, each to the least-loaded
  *     stream. */
 #define REFEFF_FMS_OPT_MULTI_STREAMS 5
+/*   REFEFF_FMS_OPT_DUAL_STREAMS: 1 (default) lets a single plan's spectrum of at
+ *     least 8 energies run as batches alternating between two workspaces on two
+ *     streams (the caller's and one of the plan's), so that the latency-bound
+ *     phases of one batch overlap the arithmetic of the other, when device
+ *     memory has room for the second workspace; 0 runs one batch after another
+ *     on the caller's stream.  Same results. */
+#define REFEFF_FMS_OPT_DUAL_STREAMS 6
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
 
 /* ---- cluster preparation (host) -------------------------------------- */

@@ -99,6 +99,7 @@ struct refeff_fms_context {
   long long tc_wait_polls = kTcWaitPolls;  // REFEFF_FMS_OPT_TC_WAIT_POLLS
   int paired_blocks = 1;     // REFEFF_FMS_OPT_PAIRED_BLOCKS
   int multi_streams = 4;     // REFEFF_FMS_OPT_MULTI_STREAMS
+  int dual_streams = 1;      // REFEFF_FMS_OPT_DUAL_STREAMS
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
   // the caller's handle plus one per live plan and model: the context is torn
   // down when the last of them is destroyed, in whatever order that happens
@@ -121,6 +122,7 @@ extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option
       ctx->dense_refinement = int(value);
       return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_PAIRED_BLOCKS: ctx->paired_blocks = value != 0; return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_DUAL_STREAMS: ctx->dual_streams = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_MULTI_STREAMS:
       if (value < 1 || value > 64) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
       ctx->multi_streams = int(value);
@@ -481,6 +483,18 @@ struct refeff_fms_plan {
   std::vector<int> last_bicg_iters;
   TunePrefs tune;  // per-plan FP32 elimination choices (refeff_fms_plan_set_tuning, the autotuner)
   Workspace ws;
+  // the second workspace and stream of two-stream batching, and its fork / join events (created on first use)
+  Workspace ws2;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  ~refeff_fms_plan() {
+    if (s2) {
+      cudaStreamSynchronize(s2);
+      cudaStreamDestroy(s2);
+    }
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+  }
   bool profiling = false;
   double phase_ms[REFEFF_FMS_PHASES] = {0, 0, 0, 0, 0, 0};
   size_t xph_per_energy() const { return size_t(nsp) * size_t(2 * L + 1) * size_t(npot); }
@@ -1067,8 +1081,7 @@ __global__ void status_not_converged_kernel(int batch, const int* converged, int
 
 // One batch of energies from the staging buffers (k_stage, x_stage) into gg_stage/status.
 // With profiling on, CUDA events bracket each phase (see refeff_fms_plan_phase_times).
-cudaError_t run_fms_batch(refeff_fms_plan& p, int batch, refeff_fms_form form, cudaStream_t s) {
-  Workspace& ws = p.ws;
+cudaError_t run_fms_batch(refeff_fms_plan& p, Workspace& ws, int batch, refeff_fms_form form, cudaStream_t s) {
   const BatchLayout& lay = ws.lay;
   BuildScratch bscratch;
   bscratch.hank = ws.hank.p;
@@ -1226,35 +1239,41 @@ bool form_valid(const refeff_fms_plan& p, refeff_fms_form form) {
 
 // Solve E energies whose inputs are already on the device (d_k: E*nsp, d_x:
 // E*xph); writes d_gg (E*m*m) and d_status (E).  Uses graph replay per batch.
+// With two streams (allow_dual, the context's REFEFF_FMS_OPT_DUAL_STREAMS,
+// graph replay possible, E >= 8, room for a second workspace) the energies are
+// split into batches alternating between two workspaces on two streams (the
+// caller's stream and one of the plan's, forked and joined with events), so
+// that one batch's latency-bound phases (panels, sweeps) overlap the other's
+// arithmetic-bound ones (build, residual, tensor-core updates).
 int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
-                          double2* d_gg, int* d_status, cudaStream_t s) {
+                          double2* d_gg, int* d_status, cudaStream_t s, bool allow_dual = true) {
   refeff_fms_context* ctx = p.ctx;
   const bool fp32 = form != REFEFF_FMS_FORM_FP64_LU;  // the BiCGSTAB form uses the refined form's buffers
   const bool bicg = form == REFEFF_FMS_FORM_BICGSTAB;
-  const int B = pick_batch(p, E, fp32);
-  int rc = ensure_workspace(ctx, p.ws, p.n, p.m, B, fp32, &p.tune);
-  if (rc) return rc;
-  Workspace& ws = p.ws;
+  bool dual = allow_dual && ctx->dual_streams && !p.profiling && !bicg && E >= 8;
+  const int B = pick_batch(p, dual ? (E + 1) / 2 : E, fp32);
+  const bool refined = fp32 && p.minv == 0;  // refinement statistics and the FP64 fallback
   const size_t xph = p.xph_per_energy();
+  if (p.full) RF_CUDA(ctx, p.d_full_all.alloc(size_t(E) * p.full_per));
+  if (refined) {
+    RF_CUDA(ctx, p.d_relres_all.alloc(size_t(E)));
+    RF_CUDA(ctx, p.d_iters_all.alloc(size_t(E)));
+  }
+  if (bicg) RF_CUDA(ctx, p.d_bicg_iters_all.alloc(size_t(E)));
+  auto prepare = [&](Workspace& ws) -> int {
+  int rc = ensure_workspace(ctx, ws, p.n, p.m, B, fp32, &p.tune);
+  if (rc) return rc;
   RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
   RF_CUDA(ctx, ws.gg_stage.alloc(size_t(ws.batch) * p.gg_per));
   if (!fp32 && (p.blocks.size() > 1 || p.full)) RF_CUDA(ctx, ws.X64.alloc(size_t(ws.batch) * ws.lay.lda * p.m));
   RF_CUDA(ctx, ws.hank.alloc(build_scratch_entries(p.P, ws.batch)));
   RF_CUDA(ctx, ws.hflag.alloc(size_t(ws.batch) * p.N * p.N));
-  if (p.full) {
-    RF_CUDA(ctx, ws.full_stage.alloc(size_t(ws.batch) * p.full_per));
-    RF_CUDA(ctx, p.d_full_all.alloc(size_t(E) * p.full_per));
-  }
-  const bool refined = fp32 && p.minv == 0;  // refinement statistics and the FP64 fallback
+  if (p.full) RF_CUDA(ctx, ws.full_stage.alloc(size_t(ws.batch) * p.full_per));
   if (p.minv != 0) {
     RF_CUDA(ctx, ws.t_tab.alloc(size_t(ws.batch) * p.n * 2));
     RF_CUDA(ctx, ws.grow.alloc(size_t(ws.batch) * p.m * p.n));
     RF_CUDA(ctx, ws.iter_scratch.alloc(size_t(ws.batch) * p.m * kIterVectors * p.n));
-  }
-  if (refined) {
-    RF_CUDA(ctx, p.d_relres_all.alloc(size_t(E)));
-    RF_CUDA(ctx, p.d_iters_all.alloc(size_t(E)));
   }
   if (bicg) {
     const size_t cols = size_t(ws.batch) * p.m;
@@ -1265,7 +1284,6 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     RF_CUDA(ctx, ws.bicg_iters.alloc(size_t(ws.batch)));
     RF_CUDA(ctx, ws.bicg_total.alloc(size_t(ws.batch)));
     RF_CUDA(ctx, ws.bicg_active.alloc(1));
-    RF_CUDA(ctx, p.d_bicg_iters_all.alloc(size_t(E)));
     if (p.model) {
       const MlpShape& sh = *model_shape(p.model);
       RF_CUDA(ctx, ws.precond_D.alloc(size_t(ws.batch) * ws.lay.lda));
@@ -1273,26 +1291,54 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
       RF_CUDA(ctx, ws.feat_Y.alloc(size_t(ws.batch) * p.N * sh.O));
     }
   }
-  for (int e0 = 0; e0 < E; e0 += B) {
+  return REFEFF_FMS_OK;
+  };
+  int rc = prepare(p.ws);
+  if (rc) return rc;
+  if (dual && !(p.ws2.batch >= B && p.ws2.lay.n == p.n && p.ws2.lay.m == p.m && (p.ws2.fp32 || !fp32))) {
+    // a second workspace only where it fits beside the first with room to spare
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t need = bytes_per_system(make_layout(p.n, p.m), fp32) * size_t(B) +
+                        (p.ws.use_tc ? tc_image_bytes(p.n, p.m, B) : 0) +
+                        build_scratch_entries(p.P, B) * sizeof(double2);
+    if (double(need) > 0.8 * double(free_b)) dual = false;
+  }
+  if (dual) {
+    rc = prepare(p.ws2);
+    if (rc) return rc;
+    if (!p.s2) {
+      RF_CUDA(ctx, cudaStreamCreateWithFlags(&p.s2, cudaStreamNonBlocking));
+      RF_CUDA(ctx, cudaEventCreateWithFlags(&p.fork_ev, cudaEventDisableTiming));
+      RF_CUDA(ctx, cudaEventCreateWithFlags(&p.join_ev, cudaEventDisableTiming));
+    }
+    RF_CUDA(ctx, cudaEventRecord(p.fork_ev, s));  // the second stream starts after the caller's earlier work
+    RF_CUDA(ctx, cudaStreamWaitEvent(p.s2, p.fork_ev, 0));
+  }
+  int batch_index = 0;
+  for (int e0 = 0; e0 < E; e0 += B, ++batch_index) {
     const int nb = std::min(B, E - e0);
+    const bool second = dual && (batch_index & 1);
+    Workspace& ws = second ? p.ws2 : p.ws;
+    const cudaStream_t q = second ? p.s2 : s;
     RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, d_k + size_t(e0) * p.nsp, size_t(nb) * p.nsp * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, s));
+                                 cudaMemcpyDeviceToDevice, q));
     RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, s));
+                                 cudaMemcpyDeviceToDevice, q));
     if (nb == B && !p.profiling && !bicg) {  // the BiCGSTAB form polls the host: not capturable
       // a graph bakes in its batch size: key by (form, energies in the batch)
       const int key = int(form) * 65536 + nb;
       auto it = ws.graphs.find(key);
       if (it == ws.graphs.end()) {
         // first run un-captured (sets kernel attributes), then capture
-        cudaError_t e = run_fms_batch(p, nb, form, s);
+        cudaError_t e = run_fms_batch(p, ws, nb, form, q);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch");
         cudaGraph_t g = nullptr;
-        RF_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        RF_CUDA(ctx, cudaStreamBeginCapture(q, cudaStreamCaptureModeThreadLocal));
         const unsigned long long before = g_launches.load();
-        e = run_fms_batch(p, nb, form, s);
+        e = run_fms_batch(p, ws, nb, form, q);
         ws.graph_launches[key] = g_launches.load() - before;
-        cudaError_t e2 = cudaStreamEndCapture(s, &g);
+        cudaError_t e2 = cudaStreamEndCapture(q, &g);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch capture");
         if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "end capture");
         cudaGraphExec_t ge = nullptr;
@@ -1301,28 +1347,32 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
         if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
         ws.graphs[key] = ge;
       } else {
-        RF_CUDA(ctx, cudaGraphLaunch(it->second, s));
+        RF_CUDA(ctx, cudaGraphLaunch(it->second, q));
         g_launches.fetch_add(ws.graph_launches[key], std::memory_order_relaxed);
       }
     } else {
-      cudaError_t e = run_fms_batch(p, nb, form, s);
+      cudaError_t e = run_fms_batch(p, ws, nb, form, q);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch");
     }
     RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.gg_per, ws.gg_stage.p, size_t(nb) * p.gg_per * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, s));
-    RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, s));
+                                 cudaMemcpyDeviceToDevice, q));
+    RF_CUDA(ctx, cudaMemcpyAsync(d_status + e0, ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToDevice, q));
     if (p.full)
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_full_all.p + size_t(e0) * p.full_per, ws.full_stage.p,
-                                   size_t(nb) * p.full_per * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+                                   size_t(nb) * p.full_per * sizeof(double2), cudaMemcpyDeviceToDevice, q));
     if (refined) {
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_relres_all.p + e0, ws.relres.p, size_t(nb) * sizeof(double),
-                                   cudaMemcpyDeviceToDevice, s));
+                                   cudaMemcpyDeviceToDevice, q));
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_iters_all.p + e0, ws.iters.p, size_t(nb) * sizeof(int),
-                                   cudaMemcpyDeviceToDevice, s));
+                                   cudaMemcpyDeviceToDevice, q));
     }
     if (bicg)
       RF_CUDA(ctx, cudaMemcpyAsync(p.d_bicg_iters_all.p + e0, ws.bicg_total.p, size_t(nb) * sizeof(int),
-                                   cudaMemcpyDeviceToDevice, s));
+                                   cudaMemcpyDeviceToDevice, q));
+  }
+  if (dual) {
+    RF_CUDA(ctx, cudaEventRecord(p.join_ev, p.s2));  // the caller's stream resumes after both
+    RF_CUDA(ctx, cudaStreamWaitEvent(s, p.join_ev, 0));
   }
   return REFEFF_FMS_OK;
 }
@@ -1341,15 +1391,18 @@ int solve_device_energies_finish(refeff_fms_plan& p, int E, const double2* d_k, 
   // plain FP64 LU (same inputs), so every returned block meets the FP64 bar.
   std::vector<int> st(static_cast<size_t>(E));
   RF_CUDA(ctx, cudaMemcpyAsync(st.data(), d_status, size_t(E) * sizeof(int), cudaMemcpyDeviceToHost, s));
-  int tc_timeout = 0;
+  int tc_timeout = 0, tc_timeout2 = 0;
   if (ws.use_tc) RF_CUDA(ctx, cudaMemcpyAsync(&tc_timeout, ws.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (p.ws2.use_tc && p.ws2.tc_err.p)
+    RF_CUDA(ctx, cudaMemcpyAsync(&tc_timeout2, p.ws2.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   RF_CUDA(ctx, cudaStreamSynchronize(s));
-  if (tc_timeout) {
+  if (tc_timeout || tc_timeout2) {
     // A tensor-core wait gave up: the update of that batch is incomplete, so
     // every FP32 result is redone on the FP64 LU below.
     for (auto& v : st)
       if (v == kDevOk) v = kDevNotConverged;
     RF_CUDA(ctx, cudaMemsetAsync(ws.tc_err.p, 0, sizeof(int), s));
+    if (tc_timeout2) RF_CUDA(ctx, cudaMemsetAsync(p.ws2.tc_err.p, 0, sizeof(int), s));
     ctx->last_error = "tensor-core update timed out; energies re-solved with the FP64 LU";
   }
   std::vector<int> redo;
@@ -1366,7 +1419,7 @@ int solve_device_energies_finish(refeff_fms_plan& p, int E, const double2* d_k, 
       RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p + size_t(i) * xph, d_x + size_t(e) * xph, xph * sizeof(double2),
                                    cudaMemcpyDeviceToDevice, s));
     }
-    cudaError_t e = run_fms_batch(p, nb, REFEFF_FMS_FORM_FP64_LU, s);
+    cudaError_t e = run_fms_batch(p, p.ws, nb, REFEFF_FMS_FORM_FP64_LU, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "fp64 fallback batch");
     for (int i = 0; i < nb; ++i) {
       const int en = redo[r0 + size_t(i)];
@@ -1407,7 +1460,7 @@ namespace {
 // device work in flight at once: begin validates, uploads and enqueues on
 // stream s; end waits, runs the FP64 fallback, downloads and scatters.
 int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
-                   refeff_complex128* scattering_out, cudaStream_t s) {
+                   refeff_complex128* scattering_out, cudaStream_t s, bool allow_dual = true) {
   refeff_fms_context* ctx = p.ctx;
   if (!points || !scattering_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   const int E = points->n_energies;
@@ -1423,7 +1476,8 @@ int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, r
   RF_CUDA(ctx, p.d_x_all.upload(reinterpret_cast<const double2*>(points->phase_shifts), size_t(E) * xph, s));
   RF_CUDA(ctx, p.d_gg_all.alloc(size_t(E) * p.gg_per));
   RF_CUDA(ctx, p.d_status_all.alloc(size_t(E)));
-  return solve_device_energies_enqueue(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s);
+  return solve_device_energies_enqueue(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s,
+                                       allow_dual);
 }
 
 int spectrum_end(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
@@ -1583,7 +1637,9 @@ extern "C" int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int
   int begun = 0;
   for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun) {
     const int i = order[size_t(begun)];
-    rc = spectrum_begin(*plans[i], &points[i], form, scattering_out[i], ctx->pool[size_t(stream_of[size_t(i)])]);
+    // the many-cluster call already overlaps clusters on its stream pool: one stream per plan
+    rc = spectrum_begin(*plans[i], &points[i], form, scattering_out[i], ctx->pool[size_t(stream_of[size_t(i)])],
+                        false);
   }
   int failed = 0, first_rc = rc;
   std::vector<refeff_fms_plan*> done_plans;

@@ -205,6 +205,7 @@ class Context:
     OPT_TC_WAIT_POLLS = 3
     OPT_PAIRED_BLOCKS = 4
     OPT_MULTI_STREAMS = 5
+    OPT_DUAL_STREAMS = 6
 
     def set_option(self, option: int, value: int):
         """Context option (applies to plans / dense solves started afterwards)."""
