@@ -407,35 +407,48 @@ def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, b
     if bicgstab_energies:
         bsel = sub[_sample(len(sub), bicgstab_energies)]
         plan.set_batch(len(bsel))
+        # energies below 25 eV above E_ref miss the 400-iteration cap unpreconditioned: the refined LU takes them
+        bwin = 25.0
+        plan.set_bicgstab_window(bwin, 1e300)
         fms.fms_real_space_spectrum(plan, k[bsel[:1]], ph[bsel[:1]], fms.FORM_BICGSTAB, raise_on_error=False)
         (gb, sb), tb = _wall(lambda: fms.fms_real_space_spectrum(plan, k[bsel], ph[bsel], fms.FORM_BICGSTAB,
                                                                  raise_on_error=False))
         bidx = np.array([list(sub).index(int(e)) for e in bsel])
         _, _, bfb = plan.refinement_stats(len(bsel))
         its0 = plan.bicgstab_stats(len(bsel))
+        lu0 = plan.bicgstab_lu_energies(len(bsel))
         out["bicgstab"] = {"value": len(bsel) / tb, "energies": int(len(bsel)),
                            "over_plain": (len(bsel) / tb) / plain, "max_rel_gg_err_vs_fp64": _rel_blocks(gb, g64[bidx], m),
                            "fp64_fallbacks": int(bfb.sum()), "status_nonzero": int((sb != 0).sum()),
-                           "iterations": int(its0.sum()),
-                           "note": "unpreconditioned batched BiCGSTAB inside the FP64 refinement"}
+                           "iterations": int(its0.sum()), "window_ev_above_eref": [bwin, None],
+                           "refined_lu_outside_window": int((lu0 == 2).sum()),
+                           "refined_lu_missed_cap": int((lu0 == 1).sum()),
+                           "note": "unpreconditioned batched BiCGSTAB inside the FP64 refinement on the energies of its "
+                                   "window; the rest, and energies that miss the 400-iteration cap, by the refined LU"}
         if learned is not None:
             model, train_info, window = learned
             plan.set_preconditioner(model)
             plan.set_precond_window(*window)
+            plan.set_bicgstab_window(window[0], 1e300)  # iterate from the model's window up
             fms.fms_real_space_spectrum(plan, k[bsel[:1]], ph[bsel[:1]], fms.FORM_BICGSTAB, raise_on_error=False)
             (gl, sl), tl = _wall(lambda: fms.fms_real_space_spectrum(plan, k[bsel], ph[bsel], fms.FORM_BICGSTAB,
                                                                      raise_on_error=False))
             _, _, lfb = plan.refinement_stats(len(bsel))
             its1 = plan.bicgstab_stats(len(bsel))
+            lu1 = plan.bicgstab_lu_energies(len(bsel))
             plan.set_preconditioner(None)
+            plan.set_bicgstab_window()
             out["bicgstab_learned"] = {
                 "value": len(bsel) / tl, "energies": int(len(bsel)), "over_plain": (len(bsel) / tl) / plain,
                 "over_unpreconditioned": tb / tl, "max_rel_gg_err_vs_fp64": _rel_blocks(gl, g64[bidx], m),
                 "fp64_fallbacks": int(lfb.sum()), "status_nonzero": int((sl != 0).sum()),
                 "iterations": int(its1.sum()), "training": train_info,
-                "window_ev_above_eref": list(window),
+                "window_ev_above_eref": list(window), "bicgstab_window_ev_above_eref": [window[0], None],
+                "refined_lu_outside_window": int((lu1 == 2).sum()),
+                "refined_lu_missed_cap": int((lu1 == 1).sum()),
                 "note": "the same BiCGSTAB with the learned diagonal right preconditioner, applied only inside "
-                        "the energy window where it was trained"}
+                        "the energy window where it was trained; energies from that window up iterate, those "
+                        "below it and those that miss the cap go to the refined LU"}
     plan.close()
     return out
 

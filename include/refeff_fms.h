@@ -529,6 +529,17 @@ int refeff_fms_write_gtr_dat(const char* path, int ne, const refeff_complex128* 
  * Adam) and inference run on the GPU. */
 int refeff_fms_precond_model_create(refeff_fms_context* ctx, int lmax, int hidden, unsigned long long seed,
                                     refeff_fms_precond_model** out);
+/* Model kinds: the channel diagonal above (REFEFF_FMS_PRECOND_DIAGONAL, what
+ * refeff_fms_precond_model_create makes) or the whole per-atom block
+ * (REFEFF_FMS_PRECOND_BLOCK): 2 C^2 outputs, C = (L+1)^2, the block of
+ * (I - G0 T)^-1 minus the identity, row-major, Re/Im interleaved; rows and
+ * columns beyond an atom's own (lmax_atom+1)^2 channels are ignored.  The
+ * BiCGSTAB form then applies the predicted block per atom (block Jacobi on the
+ * inverse).  Block models need lmax <= 4 and plans with one spin channel
+ * (refeff_fms_plan_set_preconditioner: UNSUPPORTED otherwise). */
+enum { REFEFF_FMS_PRECOND_DIAGONAL = 0, REFEFF_FMS_PRECOND_BLOCK = 1 };
+int refeff_fms_precond_model_create_kind(refeff_fms_context* ctx, int lmax, int hidden, int kind,
+                                         unsigned long long seed, refeff_fms_precond_model** out);
 void refeff_fms_precond_model_destroy(refeff_fms_precond_model* model);
 int refeff_fms_precond_model_query(const refeff_fms_precond_model* model, int* n_features, int* hidden, int* n_outputs,
                                    long long* n_params);
@@ -555,8 +566,18 @@ int refeff_fms_plan_set_precond_window(refeff_fms_plan* plan, double e_lo_ev, do
 /* BiCGSTAB controls: iteration cap per solve, relative residual tolerance of
  * each solve, and how often (iterations) the host checks for completion. */
 int refeff_fms_plan_set_bicgstab(refeff_fms_plan* plan, int max_iterations, double tolerance, int poll_interval);
-/* BiCGSTAB iterations per energy of the last BICGSTAB-form call (all solves). */
+/* BiCGSTAB iterations per energy of the last BICGSTAB-form call (all solves;
+ * 0 for energies outside the window below). */
 int refeff_fms_plan_bicgstab_stats(const refeff_fms_plan* plan, int n_energies, int32_t* iterations);
+/* Energy window of the BICGSTAB form (E - E_ref in eV, as the preconditioner
+ * window): energies outside it are not iterated but solved by the refined LU
+ * (REFEFF_FMS_FORM_FP32_REFINED), as are energies whose BiCGSTAB misses the
+ * tolerance within the iteration cap; an energy the refined LU misses goes on
+ * to the FP64 LU.  Default: all energies iterate. */
+int refeff_fms_plan_set_bicgstab_window(refeff_fms_plan* plan, double e_lo_ev, double e_hi_ev);
+/* Per energy of the last BICGSTAB-form call: 0 solved by BiCGSTAB, 1 missed
+ * the tolerance and solved by the refined LU, 2 outside the window (refined LU). */
+int refeff_fms_plan_bicgstab_lu_energies(const refeff_fms_plan* plan, int n_energies, int32_t* flags);
 /* Features of every (energy, atom), atoms in device order (absorber last):
  * E * n_atoms rows of n_features floats. */
 int refeff_fms_plan_precond_features(refeff_fms_plan* plan, const refeff_fms_energy_points* points,
@@ -567,6 +588,11 @@ int refeff_fms_plan_precond_features(refeff_fms_plan* plan, const refeff_fms_ene
  * E x (states of the atom); status_out: per energy (optional). */
 int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
                                      refeff_complex128* diag_out, int32_t* status_out);
+/* Block-model targets: the whole block of atom `atom` in (I - G0 T)^-1,
+ * block_out: E x cnt x cnt row-major (cnt = the atom's states),
+ * block_out[(e cnt + r) cnt + c] = (A^-1)[s0 + r, s0 + c]. */
+int refeff_fms_plan_inverse_block(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
+                                  refeff_complex128* block_out, int32_t* status_out);
 
 /* ---- reciprocal-space FMS (KKR integration of given structure factors) -- */
 

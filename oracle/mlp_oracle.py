@@ -19,8 +19,29 @@ def feature_count(L: int) -> int:
     return 2 + 2 * (L + 1) + 3 * (2 + 2 * (L + 1))
 
 
-def output_count(L: int) -> int:
-    return 2 * (L + 1) ** 2
+def output_count(L: int, kind: int = 0) -> int:
+    """Diagonal model (kind 0): Re/Im per channel; block model (kind 1): Re/Im of the C x C block, C = (L+1)^2."""
+    c = (L + 1) ** 2
+    return 2 * c * c if kind == 1 else 2 * c
+
+
+def block_preconditioner(Y, atom_lmax, L, on):
+    """The per-atom blocks the BiCGSTAB form applies for a block model's outputs Y (S x N x 2C^2, row-major,
+    Re/Im interleaved): identity plus the prediction on the atom's own (lmax_atom+1)^2 channels when `on`
+    (the energy lies in the model's window), the identity alone otherwise; zero beyond those channels."""
+    c = (L + 1) ** 2
+    Y = np.asarray(Y, np.float64)
+    S, N = Y.shape[0], Y.shape[1]
+    B = np.zeros((S, N, c, c), np.complex128)
+    for s in range(S):
+        for d in range(N):
+            cnt = (int(atom_lmax[d]) + 1) ** 2
+            blk = np.eye(cnt, dtype=np.complex128)
+            if on[s]:
+                y = Y[s, d, 0::2] + 1j * Y[s, d, 1::2]
+                blk = blk + y.reshape(c, c)[:cnt, :cnt]
+            B[s, d, :cnt, :cnt] = blk
+    return B
 
 
 def unpack(p, F, H, O):

@@ -6,8 +6,9 @@
 // Here the m absorber columns of every energy in a batch advance together:
 // one product kernel reads each FP32 system matrix once per product for all m
 // columns, and the per-column scalars (rho, alpha, omega) live in FP64 with
-// FP64 dot-product accumulation.  Right preconditioning by a diagonal D
-// (the learned form) solves A D y = b and returns x = D y.
+// FP64 dot-product accumulation.  Right preconditioning by a diagonal D or a
+// block diagonal (one channel block per atom; the learned form) solves
+// A P y = b and returns x = P y.
 //
 // Iteration (van der Vorst), per column:
 //   beta = (rho_new / rho)(alpha / omega);  p = r + beta (p - omega v);  p^ = D p
@@ -234,6 +235,27 @@ __global__ void bicg_alpha_kernel(View w, const int* skip) {
   sc[kRho + 1] = rho_new.y;
 }
 
+// dst = Bblk src for every running column: the block-diagonal preconditioner,
+// one C x C block per atom (Bblk[(b N + atom) C^2 + q C + q']), one thread
+// per row.
+__global__ void bicg_block_apply_kernel(View w, int src, int dst, const float2* __restrict__ Bblk,
+                                        const int* __restrict__ state_atom, const int* __restrict__ atom_off, int N,
+                                        int C, const int* skip) {
+  const int b = blockIdx.y, c = blockIdx.z;
+  if (column_idle(w, b, c, skip)) return;
+  const float2* in = w.v(src, b, c);
+  float2* out = w.v(dst, b, c);
+  for (int k = 0; k < kVecRowsPerThread; ++k) {
+    const int i = blockIdx.x * kVecRows + k * kVecThreads + threadIdx.x;
+    if (i >= w.n) break;
+    const int a = state_atom[i], s0 = atom_off[a], cnt = atom_off[a + 1] - s0, q = i - s0;
+    const float2* row = Bblk + ((size_t(b) * N + a) * C + q) * C;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int q2 = 0; q2 < cnt; ++q2) cfma(acc, row[q2], in[s0 + q2]);
+    out[i] = acc;
+  }
+}
+
 // s = r - alpha v (in r);  s^ = D s
 __global__ void bicg_s_kernel(View w, const float2* __restrict__ D, const int* skip) {
   const int b = blockIdx.y, c = blockIdx.z;
@@ -350,8 +372,9 @@ __global__ void bicg_finish_kernel(View w, float2* __restrict__ M32, size_t stri
 
 }  // namespace
 
-cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BicgWork& w,
-                           double tol, int max_iter, int poll, const int* skip, int* failed, cudaStream_t s) {
+cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BlockPrecond* blk,
+                           const BicgWork& w, double tol, int max_iter, int poll, const int* skip, int* failed,
+                           cudaStream_t s) {
   View v{lay.n, lay.m, lay.lda, batch, w.vec, w.sc, w.state, w.done};
   const dim3 vgrid(unsigned((lay.n + kVecRows - 1) / kVecRows), unsigned(batch), unsigned(lay.m));
   const dim3 mgrid(unsigned((lay.n + kMvRows - 1) / kMvRows), unsigned(batch), unsigned((lay.m + kMvCols - 1) / kMvCols));
@@ -378,7 +401,12 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
   int running = batch;
   for (int it = 1; it <= max_iter && running > 0; ++it) {
     count_launch();
-    bicg_p_kernel<<<vgrid, kVecThreads, 0, s>>>(v, D, skip);
+    bicg_p_kernel<<<vgrid, kVecThreads, 0, s>>>(v, blk ? nullptr : D, skip);
+    if (blk) {
+      count_launch();
+      bicg_block_apply_kernel<<<vgrid, kVecThreads, 0, s>>>(v, kP, kPh, blk->B, blk->state_atom, blk->atom_off,
+                                                            blk->N, blk->C, skip);
+    }
     count_launch();
     bicg_matvec_kernel<<<mgrid, kMvThreads, 0, s>>>(v, M32, lay.stride, kPh, kV, skip);
     count_launch();
@@ -386,7 +414,12 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
     count_launch();
     bicg_alpha_kernel<<<sblocks, sthreads, 0, s>>>(v, skip);
     count_launch();
-    bicg_s_kernel<<<vgrid, kVecThreads, 0, s>>>(v, D, skip);
+    bicg_s_kernel<<<vgrid, kVecThreads, 0, s>>>(v, blk ? nullptr : D, skip);
+    if (blk) {
+      count_launch();
+      bicg_block_apply_kernel<<<vgrid, kVecThreads, 0, s>>>(v, kR, kSh, blk->B, blk->state_atom, blk->atom_off,
+                                                            blk->N, blk->C, skip);
+    }
     count_launch();
     bicg_matvec_kernel<<<mgrid, kMvThreads, 0, s>>>(v, M32, lay.stride, kSh, kT, skip);
     count_launch();

@@ -22,14 +22,25 @@ struct BicgWork {
 
 // Solves A X = B for every matrix of the batch whose skip flag is clear:
 // A = the first n columns of M32, B = its last m columns, X written over B.
-// Right preconditioner: diagonal D (batch * lda complex, NULL for none), i.e.
-// BiCGSTAB on A D y = b, x = D y.  Stops a column when |r|_2 <= tol |b|_2;
+// Right preconditioner: diagonal D (batch * lda complex, NULL for none) or the
+// block diagonal blk, i.e. BiCGSTAB on A P y = b, x = P y.  Stops a column when |r|_2 <= tol |b|_2;
 // after max_iter iterations, or on a breakdown, the matrix's flag in
 // `failed` is set to 2 (the caller's fallback marker) and its X is left as the
 // last iterate.  The host polls the number of running matrices every
 // `poll` iterations (one small device-to-host copy), so the call is not
 // capturable into a CUDA graph.
-cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BicgWork& w,
-                           double tol, int max_iter, int poll, const int* skip, int* failed, cudaStream_t s);
+// Block-diagonal right preconditioner: per matrix and atom a C x C block
+// B[(b N + atom) C^2 + q C + q'] acting on the atom's states [atom_off[a],
+// atom_off[a + 1]); state_atom[i] is the atom of state i (device order).
+struct BlockPrecond {
+  const float2* B = nullptr;
+  const int* state_atom = nullptr;
+  const int* atom_off = nullptr;
+  int N = 0, C = 0;
+};
+// blk (nullable) replaces D when given.
+cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BlockPrecond* blk,
+                           const BicgWork& w, double tol, int max_iter, int poll, const int* skip, int* failed,
+                           cudaStream_t s);
 
 }  // namespace rfx

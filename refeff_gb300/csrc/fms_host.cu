@@ -411,6 +411,7 @@ struct Workspace {
   // BiCGSTAB form: solver vectors and scalars, the preconditioner diagonal,
   // per-atom features and network outputs
   DevBuf<float2> bicg_vec, precond_D;
+  DevBuf<float2> precond_B;  // block-diagonal learned preconditioner: batch x N x C^2
   DevBuf<double> bicg_sc;
   DevBuf<int> bicg_state, bicg_done, bicg_iters, bicg_active, bicg_total;
   DevBuf<float> feat_X, feat_Y;
@@ -475,12 +476,17 @@ struct refeff_fms_plan {
   std::vector<int> off_dev;           // first state of each atom, device order (host copy, N + 1)
   refeff_fms_precond_model* model = nullptr;  // learned preconditioner (not owned), NULL: none
   double precond_e_lo = -1e300, precond_e_hi = 1e300;  // energies (E - E_ref, eV) where the model is applied
+  double bicg_e_lo = -1e300, bicg_e_hi = 1e300;  // energies the BiCGSTAB form iterates on; the rest go to the LU
   DevBuf<float> d_shell_info, d_shell_pots;
+  DevBuf<int> d_state_atom;  // device atom of each state (device order), for the block preconditioner
   int bicg_max_iter = 400;
   double bicg_tol = 1.0e-6;
   int bicg_poll = 8;
   DevBuf<int> d_bicg_iters_all;
   std::vector<int> last_bicg_iters;
+  // BiCGSTAB-form energies handed to the refined LU: 1 missed the tolerance, 2 outside the window
+  std::vector<int> bicg_lu;
+  std::vector<int> bicg_order;  // energies of the last BiCGSTAB-form call that iterated (window routing)
   TunePrefs tune;  // per-plan FP32 elimination choices (refeff_fms_plan_set_tuning, the autotuner)
   Workspace ws;
   // the second workspace and stream of two-stream batching, and its fork / join events (created on first use)
@@ -984,8 +990,8 @@ BicgWork bicg_work(Workspace& ws) {
 // (M32 holds A and, in its last m columns, the right-hand side).  A system
 // whose BiCGSTAB solve misses its tolerance within the iteration cap is
 // marked converged = 2 and handed to the FP64 LU by the caller.
-cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, int iters, double tol, int max_iter,
-                            double inner_tol, int poll, cudaStream_t s, Spans* spans = nullptr) {
+cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, const BlockPrecond* blk, int iters, double tol,
+                            int max_iter, double inner_tol, int poll, cudaStream_t s, Spans* spans = nullptr) {
   const BatchLayout& lay = ws.lay;
   const BicgWork w = bicg_work(ws);
   auto span = [&](int phase, auto&& fn) -> cudaError_t {
@@ -1007,7 +1013,7 @@ cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, int iters
   cudaMemsetAsync(ws.iters.p, 0, size_t(batch) * sizeof(int), s);
   cudaMemsetAsync(ws.bicg_total.p, 0, size_t(batch) * sizeof(int), s);
   auto solve = [&]() -> cudaError_t {
-    cudaError_t e = bicgstab_solve(lay, batch, ws.M32.p, D, w, inner_tol, max_iter, poll, ws.converged.p,
+    cudaError_t e = bicgstab_solve(lay, batch, ws.M32.p, D, blk, w, inner_tol, max_iter, poll, ws.converged.p,
                                    ws.converged.p, s);
     count_launch();
     add_iterations_kernel<<<(batch + 127) / 128, 128, 0, s>>>(batch, ws.bicg_iters.p, ws.bicg_total.p);
@@ -1155,13 +1161,25 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, Workspace& ws, int batch, refeff_f
                         p.d_shell_info.p, p.d_shell_pots.p, ws.feat_X.p, s);
         cudaError_t e1 = mlp_forward(sh, model_params(p.model), batch * p.N, ws.feat_X.p, ws.mlp, ws.feat_Y.p, s);
         if (e1 != cudaSuccess) return e1;
-        launch_scatter_diag(batch, p.N, p.L, p.nsp, lay.lda, p.d_atom_off.p, p.d_atom_lmax.p, ws.feat_Y.p,
-                            ws.k_stage.p, p.precond_e_lo, p.precond_e_hi, ws.precond_D.p, s);
+        if (model_kind(p.model) == kPrecondBlock)
+          launch_scatter_block(batch, p.N, p.L, p.d_atom_lmax.p, ws.feat_Y.p, ws.k_stage.p, p.precond_e_lo,
+                               p.precond_e_hi, ws.precond_B.p, s);
+        else
+          launch_scatter_diag(batch, p.N, p.L, p.nsp, lay.lda, p.d_atom_off.p, p.d_atom_lmax.p, ws.feat_Y.p,
+                              ws.k_stage.p, p.precond_e_lo, p.precond_e_hi, ws.precond_D.p, s);
       }
       return cudaGetLastError();
     });
-    e = refine_bicgstab(ws, batch, p.model ? ws.precond_D.p : nullptr, p.refine_iters, p.refine_tol, p.bicg_max_iter,
-                        p.bicg_tol, p.bicg_poll, s, prof ? &spans : nullptr);
+    const bool block = p.model && model_kind(p.model) == kPrecondBlock;
+    BlockPrecond blk;
+    blk.B = ws.precond_B.p;
+    blk.state_atom = p.d_state_atom.p;
+    blk.atom_off = p.d_atom_off.p;
+    blk.N = p.N;
+    blk.C = (p.L + 1) * (p.L + 1);
+    e = refine_bicgstab(ws, batch, p.model && !block ? ws.precond_D.p : nullptr, block ? &blk : nullptr,
+                        p.refine_iters, p.refine_tol, p.bicg_max_iter, p.bicg_tol, p.bicg_poll, s,
+                        prof ? &spans : nullptr);
     if (e != cudaSuccess) return e;
     tick(4, [&] {
       count_launch();
@@ -1237,6 +1255,30 @@ bool form_valid(const refeff_fms_plan& p, refeff_fms_form form) {
          (form == REFEFF_FMS_FORM_BICGSTAB && p.minv == 0);
 }
 
+// E - E_ref in eV of a wave number in 1/Angstrom: Re((k a0)^2) / 2 Hartree, the
+// definition the learned preconditioner's window uses on the device.
+double energy_above_eref_ev(double2 k) {
+  constexpr double kBohr = 0.529177249, kHartreeEv = 27.211396;
+  return 0.5 * (k.x * k.x - k.y * k.y) * kBohr * kBohr * kHartreeEv;
+}
+
+// Results of batch slot i of a workspace -> energy e of the call's outputs
+// (gg block, status, full-scattering slice, refinement statistics).
+cudaError_t copy_energy_results(refeff_fms_plan& p, Workspace& ws, int i, int e, double2* d_gg, int* d_status,
+                                cudaStream_t q) {
+  cudaError_t r = cudaMemcpyAsync(d_gg + size_t(e) * p.gg_per, ws.gg_stage.p + size_t(i) * p.gg_per,
+                                  size_t(p.gg_per) * sizeof(double2), cudaMemcpyDeviceToDevice, q);
+  if (!r) r = cudaMemcpyAsync(d_status + e, ws.status.p + i, sizeof(int), cudaMemcpyDeviceToDevice, q);
+  if (!r && p.full)
+    r = cudaMemcpyAsync(p.d_full_all.p + size_t(e) * p.full_per, ws.full_stage.p + size_t(i) * p.full_per,
+                        size_t(p.full_per) * sizeof(double2), cudaMemcpyDeviceToDevice, q);
+  if (!r && p.minv == 0 && p.d_relres_all.p && ws.relres.p) {
+    r = cudaMemcpyAsync(p.d_relres_all.p + e, ws.relres.p + i, sizeof(double), cudaMemcpyDeviceToDevice, q);
+    if (!r) r = cudaMemcpyAsync(p.d_iters_all.p + e, ws.iters.p + i, sizeof(int), cudaMemcpyDeviceToDevice, q);
+  }
+  return r;
+}
+
 // Solve E energies whose inputs are already on the device (d_k: E*nsp, d_x:
 // E*xph); writes d_gg (E*m*m) and d_status (E).  Uses graph replay per batch.
 // With two streams (allow_dual, the context's REFEFF_FMS_OPT_DUAL_STREAMS,
@@ -1287,6 +1329,8 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     if (p.model) {
       const MlpShape& sh = *model_shape(p.model);
       RF_CUDA(ctx, ws.precond_D.alloc(size_t(ws.batch) * ws.lay.lda));
+      if (model_kind(p.model) == kPrecondBlock)
+        RF_CUDA(ctx, ws.precond_B.alloc(size_t(ws.batch) * p.N * size_t((p.L + 1) * (p.L + 1)) * (p.L + 1) * (p.L + 1)));
       RF_CUDA(ctx, ws.feat_X.alloc(size_t(ws.batch) * p.N * sh.F));
       RF_CUDA(ctx, ws.feat_Y.alloc(size_t(ws.batch) * p.N * sh.O));
     }
@@ -1315,16 +1359,47 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     RF_CUDA(ctx, cudaEventRecord(p.fork_ev, s));  // the second stream starts after the caller's earlier work
     RF_CUDA(ctx, cudaStreamWaitEvent(p.s2, p.fork_ev, 0));
   }
+  // BiCGSTAB energy window: energies outside it skip the iteration and are
+  // solved by the refined LU in the finish step
+  bool routed = false;
+  if (bicg) {
+    p.bicg_lu.assign(size_t(E), 0);
+    p.bicg_order.clear();
+    RF_CUDA(ctx, cudaMemsetAsync(p.d_bicg_iters_all.p, 0, size_t(E) * sizeof(int), s));
+    if (p.bicg_e_lo > -1e299 || p.bicg_e_hi < 1e299) {
+      std::vector<double2> hk(size_t(E) * p.nsp);
+      RF_CUDA(ctx, cudaMemcpyAsync(hk.data(), d_k, hk.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
+      RF_CUDA(ctx, cudaStreamSynchronize(s));
+      for (int e = 0; e < E; ++e) {
+        const double ev = energy_above_eref_ev(hk[size_t(e) * p.nsp]);
+        if (ev >= p.bicg_e_lo && ev <= p.bicg_e_hi) p.bicg_order.push_back(e);
+        else p.bicg_lu[size_t(e)] = 2;
+      }
+      routed = int(p.bicg_order.size()) != E;
+    }
+  }
+  const int Eit = routed ? int(p.bicg_order.size()) : E;  // energies this loop solves
+  auto energy_of = [&](int i) { return routed ? p.bicg_order[size_t(i)] : i; };
   int batch_index = 0;
-  for (int e0 = 0; e0 < E; e0 += B, ++batch_index) {
-    const int nb = std::min(B, E - e0);
+  for (int e0 = 0; e0 < Eit; e0 += B, ++batch_index) {
+    const int nb = std::min(B, Eit - e0);
     const bool second = dual && (batch_index & 1);
     Workspace& ws = second ? p.ws2 : p.ws;
     const cudaStream_t q = second ? p.s2 : s;
-    RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, d_k + size_t(e0) * p.nsp, size_t(nb) * p.nsp * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, q));
-    RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, q));
+    if (routed) {
+      for (int i = 0; i < nb; ++i) {
+        const int e = energy_of(e0 + i);
+        RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p + size_t(i) * p.nsp, d_k + size_t(e) * p.nsp,
+                                     p.nsp * sizeof(double2), cudaMemcpyDeviceToDevice, q));
+        RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p + size_t(i) * xph, d_x + size_t(e) * xph, xph * sizeof(double2),
+                                     cudaMemcpyDeviceToDevice, q));
+      }
+    } else {
+      RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p, d_k + size_t(e0) * p.nsp, size_t(nb) * p.nsp * sizeof(double2),
+                                   cudaMemcpyDeviceToDevice, q));
+      RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
+                                   cudaMemcpyDeviceToDevice, q));
+    }
     if (nb == B && !p.profiling && !bicg) {  // the BiCGSTAB form polls the host: not capturable
       // a graph bakes in its batch size: key by (form, energies in the batch)
       const int key = int(form) * 65536 + nb;
@@ -1353,6 +1428,14 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
     } else {
       cudaError_t e = run_fms_batch(p, ws, nb, form, q);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "fms batch");
+    }
+    if (routed) {  // scatter the batch's results back to its energies
+      for (int i = 0; i < nb; ++i) {
+        RF_CUDA(ctx, copy_energy_results(p, ws, i, energy_of(e0 + i), d_gg, d_status, q));
+        RF_CUDA(ctx, cudaMemcpyAsync(p.d_bicg_iters_all.p + energy_of(e0 + i), ws.bicg_total.p + i, sizeof(int),
+                                     cudaMemcpyDeviceToDevice, q));
+      }
+      continue;
     }
     RF_CUDA(ctx, cudaMemcpyAsync(d_gg + size_t(e0) * p.gg_per, ws.gg_stage.p, size_t(nb) * p.gg_per * sizeof(double2),
                                  cudaMemcpyDeviceToDevice, q));
@@ -1404,6 +1487,45 @@ int solve_device_energies_finish(refeff_fms_plan& p, int E, const double2* d_k, 
     RF_CUDA(ctx, cudaMemsetAsync(ws.tc_err.p, 0, sizeof(int), s));
     if (tc_timeout2) RF_CUDA(ctx, cudaMemsetAsync(p.ws2.tc_err.p, 0, sizeof(int), s));
     ctx->last_error = "tensor-core update timed out; energies re-solved with the FP64 LU";
+  }
+  if (form == REFEFF_FMS_FORM_BICGSTAB) {
+    // The BiCGSTAB form's energies that missed the tolerance within the
+    // iteration cap, and those outside its window, are solved by the refined
+    // LU (FP32 factorisation + FP64 refinement); what that misses goes on to
+    // the FP64 LU below.
+    std::vector<int> lu;
+    for (int e = 0; e < E; ++e) {
+      if (p.bicg_lu[size_t(e)] == 2) {
+        lu.push_back(e);
+      } else if (st[size_t(e)] == kDevNotConverged) {
+        p.bicg_lu[size_t(e)] = 1;
+        lu.push_back(e);
+      }
+    }
+    for (size_t r0 = 0; r0 < lu.size(); r0 += size_t(B)) {
+      const int nb = int(std::min(lu.size() - r0, size_t(B)));
+      for (int i = 0; i < nb; ++i) {
+        const int e = lu[r0 + size_t(i)];
+        RF_CUDA(ctx, cudaMemcpyAsync(ws.k_stage.p + size_t(i) * p.nsp, d_k + size_t(e) * p.nsp,
+                                     p.nsp * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+        RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p + size_t(i) * xph, d_x + size_t(e) * xph, xph * sizeof(double2),
+                                     cudaMemcpyDeviceToDevice, s));
+      }
+      cudaError_t e = run_fms_batch(p, ws, nb, REFEFF_FMS_FORM_FP32_REFINED, s);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "refined LU batch of the BiCGSTAB form");
+      for (int i = 0; i < nb; ++i) RF_CUDA(ctx, copy_energy_results(p, ws, i, lu[r0 + size_t(i)], d_gg, d_status, s));
+    }
+    if (!lu.empty()) {
+      RF_CUDA(ctx, cudaMemcpyAsync(st.data(), d_status, size_t(E) * sizeof(int), cudaMemcpyDeviceToHost, s));
+      int lu_timeout = 0;
+      if (ws.use_tc) RF_CUDA(ctx, cudaMemcpyAsync(&lu_timeout, ws.tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      RF_CUDA(ctx, cudaStreamSynchronize(s));
+      if (lu_timeout) {
+        for (int e : lu) st[size_t(e)] = kDevNotConverged;
+        RF_CUDA(ctx, cudaMemsetAsync(ws.tc_err.p, 0, sizeof(int), s));
+        ctx->last_error = "tensor-core update timed out; energies re-solved with the FP64 LU";
+      }
+    }
   }
   std::vector<int> redo;
   for (int e = 0; e < E; ++e)
@@ -1703,6 +1825,15 @@ __global__ void inverse_diagonal_kernel(BatchLayout lay, const double2* M, int s
   out[size_t(b) * cnt + c] = M[size_t(b) * lay.stride + size_t(s0 + c) + size_t(lay.lda) * (lay.n + c)];
 }
 
+// out[(b cnt + r) cnt + c] = (A^-1)[s0 + r, s0 + c]: the solved unit columns, row-major per energy
+__global__ void inverse_block_kernel(BatchLayout lay, const double2* M, int s0, int cnt, double2* out) {
+  const int b = blockIdx.x;
+  for (int idx = threadIdx.x; idx < cnt * cnt; idx += blockDim.x) {
+    const int r = idx / cnt, c = idx % cnt;
+    out[size_t(b) * cnt * cnt + idx] = M[size_t(b) * lay.stride + size_t(s0 + r) + size_t(lay.lda) * (lay.n + c)];
+  }
+}
+
 }  // namespace
 
 extern "C" int refeff_fms_plan_set_precond_window(refeff_fms_plan* plan, double e_lo_ev, double e_hi_ev) {
@@ -1712,14 +1843,37 @@ extern "C" int refeff_fms_plan_set_precond_window(refeff_fms_plan* plan, double 
   return REFEFF_FMS_OK;
 }
 
+extern "C" int refeff_fms_plan_set_bicgstab_window(refeff_fms_plan* plan, double e_lo_ev, double e_hi_ev) {
+  if (!plan || std::isnan(e_lo_ev) || std::isnan(e_hi_ev) || e_lo_ev > e_hi_ev) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  plan->bicg_e_lo = e_lo_ev;
+  plan->bicg_e_hi = e_hi_ev;
+  return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_plan_bicgstab_lu_energies(const refeff_fms_plan* plan, int n_energies, int32_t* flags) {
+  if (!plan || n_energies < 0 || (n_energies > 0 && !flags)) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  for (int e = 0; e < n_energies; ++e) flags[e] = e < int(plan->bicg_lu.size()) ? plan->bicg_lu[size_t(e)] : 0;
+  return REFEFF_FMS_OK;
+}
+
 extern "C" int refeff_fms_plan_set_preconditioner(refeff_fms_plan* plan, refeff_fms_precond_model* model) {
   if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   if (model && model_lmax(model) != plan->L)
     return fail(plan->ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "preconditioner model built for another lmax");
+  if (model && model_kind(model) == kPrecondBlock && plan->nsp != 1)
+    return fail(plan->ctx, REFEFF_FMS_ERR_UNSUPPORTED, "block-diagonal preconditioner needs one spin channel");
   RF_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
   if (model) {
     const int rc = ensure_shell_tables(*plan, plan->ctx->stream);
     if (rc) return rc;
+  }
+  if (model && model_kind(model) == kPrecondBlock && !plan->d_state_atom.p) {
+    // state -> device atom, for the per-atom block apply
+    std::vector<int> sa(static_cast<size_t>(plan->n));
+    for (int d = 0; d < plan->N; ++d)
+      for (int st = plan->off_dev[size_t(d)]; st < plan->off_dev[size_t(d) + 1]; ++st) sa[size_t(st)] = d;
+    RF_CUDA(plan->ctx, plan->d_state_atom.upload(sa.data(), sa.size(), plan->ctx->stream));
+    RF_CUDA(plan->ctx, cudaStreamSynchronize(plan->ctx->stream));
   }
   plan->model = model;
   plan->ws.precond_D.release();  // re-sized on the next BiCGSTAB call
@@ -1765,9 +1919,13 @@ extern "C" int refeff_fms_plan_precond_features(refeff_fms_plan* plan, const ref
   return REFEFF_FMS_OK;
 }
 
-extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
-                                                refeff_complex128* diag_out, int32_t* status_out) {
-  if (!plan || !points || points->n_energies < 0 || !diag_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+namespace {
+
+// Columns s0..s0+cnt of A^-1 for the states of one atom, solved in FP64 per energy batch; the diagonal or the
+// whole cnt x cnt block of the atom is copied out.
+int inverse_columns(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom, bool whole_block,
+                    refeff_complex128* out_host, int32_t* status_out) {
+  if (!plan || !points || points->n_energies < 0 || !out_host) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   refeff_fms_plan& p = *plan;
   refeff_fms_context* ctx = p.ctx;
   if (atom < 0 || atom >= p.N) return fail(ctx, REFEFF_FMS_ERR_INVALID_ARGUMENT, "atom index outside the cluster");
@@ -1786,8 +1944,9 @@ extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const ref
   const size_t xph = p.xph_per_energy();
   RF_CUDA(ctx, ws.k_stage.alloc(size_t(ws.batch) * p.nsp));
   RF_CUDA(ctx, ws.x_stage.alloc(size_t(ws.batch) * xph));
+  const size_t per = whole_block ? size_t(cnt) * cnt : size_t(cnt);
   DevBuf<double2> dout;
-  RF_CUDA(ctx, dout.alloc(size_t(ws.batch) * cnt));
+  RF_CUDA(ctx, dout.alloc(size_t(ws.batch) * per));
   std::vector<int> st(static_cast<size_t>(ws.batch));
   for (int e0 = 0; e0 < E; e0 += B) {
     const int nb = std::min(B, E - e0);
@@ -1803,9 +1962,12 @@ extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const ref
     RF_CUDA(ctx, lu_eliminate<double>(ws.pc64, lay, nb, ws.M64.p, lu_work(ws, ws.pc64), s));
     lu_backward_rhs<double>(ws.pc64, lay, nb, ws.M64.p, nullptr, s);
     count_launch();
-    inverse_diagonal_kernel<<<unsigned(nb), 64, 0, s>>>(lay, ws.M64.p, s0, cnt, dout.p);
+    if (whole_block)
+      inverse_block_kernel<<<unsigned(nb), 256, 0, s>>>(lay, ws.M64.p, s0, cnt, dout.p);
+    else
+      inverse_diagonal_kernel<<<unsigned(nb), 64, 0, s>>>(lay, ws.M64.p, s0, cnt, dout.p);
     RF_CUDA(ctx, cudaGetLastError());
-    RF_CUDA(ctx, cudaMemcpyAsync(diag_out + size_t(e0) * cnt, dout.p, size_t(nb) * cnt * sizeof(double2),
+    RF_CUDA(ctx, cudaMemcpyAsync(out_host + size_t(e0) * per, dout.p, size_t(nb) * per * sizeof(double2),
                                  cudaMemcpyDeviceToHost, s));
     RF_CUDA(ctx, cudaMemcpyAsync(st.data(), ws.status.p, size_t(nb) * sizeof(int), cudaMemcpyDeviceToHost, s));
     RF_CUDA(ctx, cudaStreamSynchronize(s));
@@ -1813,6 +1975,18 @@ extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const ref
       if (status_out) status_out[e0 + i] = map_status(st[size_t(i)]);
   }
   return REFEFF_FMS_OK;
+}
+
+}  // namespace
+
+extern "C" int refeff_fms_plan_inverse_diagonal(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
+                                                refeff_complex128* diag_out, int32_t* status_out) {
+  return inverse_columns(plan, points, atom, false, diag_out, status_out);
+}
+
+extern "C" int refeff_fms_plan_inverse_block(refeff_fms_plan* plan, const refeff_fms_energy_points* points, int atom,
+                                             refeff_complex128* block_out, int32_t* status_out) {
+  return inverse_columns(plan, points, atom, true, block_out, status_out);
 }
 
 extern "C" int refeff_fms_gg_section(const refeff_fms_plan* plan, const refeff_complex128* scattering, int nspu,

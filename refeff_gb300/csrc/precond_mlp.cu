@@ -218,7 +218,10 @@ __global__ void scatter_diag_kernel(int batch, int N, int L, int nsp, int lda, c
 // host-side pieces used by the plan
 // ---------------------------------------------------------------------------
 int feature_count(int L) { return 2 + 2 * (L + 1) + kShells * (2 + 2 * (L + 1)); }
-int output_count(int L) { return 2 * (L + 1) * (L + 1); }
+int output_count(int L, int kind) {
+  const int C = (L + 1) * (L + 1);
+  return kind == kPrecondBlock ? 2 * C * C : 2 * C;
+}
 
 ShellTables shell_tables(int N, int npot, const float* pos, const int* pot) {
   static const double edges[kShells + 1] = {0.0, 2.9, 3.7, 4.6};
@@ -260,6 +263,42 @@ void launch_features(int batch, int N, int L, int nsp, int npot, const double2* 
   count_launch();
   features_kernel<<<(total + 127) / 128, 128, 0, s>>>(batch, N, L, nsp, npot, feature_count(L), k, xph, atom_pot,
                                                       shell_info, shell_pots, X);
+}
+
+// Dblk[(b N + atom) C^2 + q C + q'] = delta(q, q') + (Y[b*N + atom][2 (q C + q')] + i Y[..][2 (q C + q') + 1])
+// for q, q' below the atom's channel count, zero beyond it; identity outside the energy window.
+__global__ void scatter_block_kernel(int batch, int N, int L, const int* __restrict__ atom_lmax,
+                                     const float* __restrict__ Y, const double2* __restrict__ k, double e_lo,
+                                     double e_hi, float2* __restrict__ B) {
+  const int C = (L + 1) * (L + 1), CC = C * C;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)batch * N * CC) return;
+  const int e = int(idx % CC), d = int((idx / CC) % N), b = int(idx / CC / N);
+  const int q = e / C, q2 = e % C;
+  const int cnt = (atom_lmax[d] + 1) * (atom_lmax[d] + 1);
+  bool on = true;
+  if (k) {
+    constexpr double kBohr = 0.529177249, kHartreeEv = 27.211396;
+    const double2 kk = k[b];
+    const double e_ev = 0.5 * (kk.x * kk.x - kk.y * kk.y) * kBohr * kBohr * kHartreeEv;
+    on = e_ev >= e_lo && e_ev <= e_hi;
+  }
+  float2 v = make_float2(q == q2 ? 1.f : 0.f, 0.f);
+  if (q >= cnt || q2 >= cnt) v = make_float2(0.f, 0.f);
+  else if (on) {
+    const float* y = Y + (size_t(b) * N + d) * 2 * CC + 2 * e;
+    v.x += y[0];
+    v.y += y[1];
+  }
+  B[idx] = v;
+}
+
+void launch_scatter_block(int batch, int N, int L, const int* atom_lmax, const float* Y, const double2* k, double e_lo,
+                          double e_hi, float2* B, cudaStream_t s) {
+  const int C = (L + 1) * (L + 1);
+  const long long total = (long long)batch * N * C * C;
+  count_launch();
+  scatter_block_kernel<<<unsigned((total + 255) / 256), 256, 0, s>>>(batch, N, L, atom_lmax, Y, k, e_lo, e_hi, B);
 }
 
 void launch_scatter_diag(int batch, int N, int L, int nsp, int lda, const int* atom_off, const int* atom_lmax,
@@ -362,6 +401,7 @@ using namespace rfx;
 struct refeff_fms_precond_model {
   refeff_fms_context* ctx = nullptr;
   int L = 0;
+  int kind = kPrecondDiagonal;
   MlpShape shape;
   float* params = nullptr;
   float* grad = nullptr;
@@ -382,6 +422,7 @@ namespace rfx {
 const MlpShape* model_shape(const refeff_fms_precond_model* m) { return m ? &m->shape : nullptr; }
 const float* model_params(const refeff_fms_precond_model* m) { return m ? m->params : nullptr; }
 int model_lmax(const refeff_fms_precond_model* m) { return m ? m->L : -1; }
+int model_kind(const refeff_fms_precond_model* m) { return m ? m->kind : kPrecondDiagonal; }
 }  // namespace rfx
 
 namespace rfx {
@@ -409,16 +450,19 @@ int set_device(refeff_fms_precond_model* m) {
 }  // namespace
 }  // namespace rfx
 
-extern "C" int refeff_fms_precond_model_create(refeff_fms_context* ctx, int lmax, int hidden, unsigned long long seed,
-                                               refeff_fms_precond_model** out) {
-  if (!ctx || !out || lmax < 0 || lmax > 6 || hidden < 1 || hidden > 1024) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+extern "C" int refeff_fms_precond_model_create_kind(refeff_fms_context* ctx, int lmax, int hidden, int kind,
+                                                    unsigned long long seed, refeff_fms_precond_model** out) {
+  if (!ctx || !out || lmax < 0 || lmax > 6 || hidden < 1 || hidden > 1024 ||
+      (kind != kPrecondDiagonal && kind != kPrecondBlock) || (kind == kPrecondBlock && lmax > 4))
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   auto m = new refeff_fms_precond_model;
   m->ctx = ctx;
   m->L = lmax;
+  m->kind = kind;
   m->shape.F = feature_count(lmax);
   m->shape.H = hidden;
-  m->shape.O = output_count(lmax);
+  m->shape.O = output_count(lmax, kind);
   const size_t np = m->shape.n_params();
   if (set_device(m) || cudaMalloc(&m->params, np * sizeof(float)) || cudaMalloc(&m->grad, np * sizeof(float)) ||
       cudaMalloc(&m->m1, np * sizeof(float)) || cudaMalloc(&m->m2, np * sizeof(float))) {
@@ -446,6 +490,11 @@ extern "C" int refeff_fms_precond_model_create(refeff_fms_context* ctx, int lmax
   context_retain(ctx);
   *out = m;
   return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_fms_precond_model_create(refeff_fms_context* ctx, int lmax, int hidden, unsigned long long seed,
+                                               refeff_fms_precond_model** out) {
+  return refeff_fms_precond_model_create_kind(ctx, lmax, hidden, kPrecondDiagonal, seed, out);
 }
 
 extern "C" void refeff_fms_precond_model_destroy(refeff_fms_precond_model* m) {

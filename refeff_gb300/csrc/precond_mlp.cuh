@@ -48,7 +48,9 @@ struct ShellTables {
 };
 ShellTables shell_tables(int N, int npot, const float* pos_dev_order, const int* pot_dev_order);
 int feature_count(int L);
-int output_count(int L);
+// Model kinds: the channel diagonal of each atom's block of A^-1, or the whole block.
+constexpr int kPrecondDiagonal = 0, kPrecondBlock = 1;
+int output_count(int L, int kind = kPrecondDiagonal);
 
 // Features of every (energy, device atom): S = batch * N rows of feature_count(L).
 // k: batch * nsp wave numbers; xph: batch * xph_per_energy phase shifts.
@@ -58,10 +60,15 @@ void launch_features(int batch, int N, int L, int nsp, int npot, const double2* 
 const MlpShape* model_shape(const refeff_fms_precond_model* m);
 const float* model_params(const refeff_fms_precond_model* m);
 int model_lmax(const refeff_fms_precond_model* m);
+int model_kind(const refeff_fms_precond_model* m);
 
 // D[b][state] = 1 + (Y[b*N + atom][2c] + i Y[..][2c+1]), c = channel of the state (spin-independent);
 // with k (batch * nsp wave numbers), energies with E - E_ref outside [e_lo, e_hi] eV get D = 1.
 void launch_scatter_diag(int batch, int N, int L, int nsp, int lda, const int* atom_off, const int* atom_lmax,
                          const float* Y, const double2* k, double e_lo, double e_hi, float2* D, cudaStream_t s);
+// Block kind (one spin channel): Bblk[(b N + atom) C^2 + q C + q'] = I + the network's block, C = (L+1)^2,
+// identity outside [e_lo, e_hi] eV (k: batch wave numbers), zero rows / columns beyond the atom's channels.
+void launch_scatter_block(int batch, int N, int L, const int* atom_lmax, const float* Y, const double2* k, double e_lo,
+                          double e_hi, float2* B, cudaStream_t s);
 
 }  // namespace rfx

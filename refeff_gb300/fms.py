@@ -138,6 +138,7 @@ def load(build_if_missing: bool = True):
         "refeff_fms_debye_sigma2_table": ([_p, _i, _i, _p, _p, _i, _p, C.c_double, C.c_double, C.c_double,
                                            C.c_float, _p, _p], _i),
         "refeff_fms_precond_model_create": ([_p, _i, _i, C.c_ulonglong, _p], _i),
+        "refeff_fms_precond_model_create_kind": ([_p, _i, _i, _i, C.c_ulonglong, _p], _i),
         "refeff_fms_precond_model_destroy": ([_p], None),
         "refeff_fms_precond_model_query": ([_p, _p, _p, _p, _p], _i),
         "refeff_fms_precond_get_params": ([_p, _p], _i),
@@ -150,10 +151,13 @@ def load(build_if_missing: bool = True):
         "refeff_fms_plan_bicgstab_stats": ([_p, _i, _p], _i),
         "refeff_fms_plan_precond_features": ([_p, _p, _p], _i),
         "refeff_fms_plan_inverse_diagonal": ([_p, _p, _i, _p, _p], _i),
+        "refeff_fms_plan_inverse_block": ([_p, _p, _i, _p, _p], _i),
         "refeff_fms_geometry_from_feff_inp": ([C.c_char_p, _i, _p, _p, _p, _i, _p, _p], _i),
         "refeff_fms_autotune_multi": ([_p, _i, _p, _p, _i, _i, C.c_char_p, _p], _i),
         "refeff_fms_plan_set_tuning": ([_p, _i, _i], _i),
         "refeff_fms_plan_set_precond_window": ([_p, C.c_double, C.c_double], _i),
+        "refeff_fms_plan_set_bicgstab_window": ([_p, C.c_double, C.c_double], _i),
+        "refeff_fms_plan_bicgstab_lu_energies": ([_p, _i, _p], _i),
         "refeff_fms_plan_get_tuning": ([_p, _p, _p], _i),
         "refeff_fms_write_geom_dat": ([C.c_char_p, C.c_char_p], _i),
         "refeff_fms_feff_inp_last_error": ([], C.c_char_p),
@@ -299,6 +303,17 @@ class FmsRealSpacePlan:
         self.ctx.check(self.ctx._lib.refeff_fms_plan_set_bicgstab(self.handle, int(max_iterations),
                                                                    float(tolerance), int(poll_interval)))
 
+    def set_bicgstab_window(self, e_lo_ev: float = -1e300, e_hi_ev: float = 1e300):
+        """Iterate the BiCGSTAB form only for E - E_ref in [e_lo_ev, e_hi_ev] eV; other energies go to the refined LU."""
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_set_bicgstab_window(self.handle, float(e_lo_ev), float(e_hi_ev)))
+
+    def bicgstab_lu_energies(self, n_energies: int):
+        """Per energy of the last BiCGSTAB-form call: 0 BiCGSTAB, 1 missed the tolerance -> refined LU, 2 outside
+        the window -> refined LU."""
+        fl = np.zeros(n_energies, np.int32)
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_bicgstab_lu_energies(self.handle, int(n_energies), _ptr(fl)))
+        return fl
+
     def bicgstab_stats(self, n_energies: int):
         """BiCGSTAB iterations per energy of the last BICGSTAB-form call (initial solve + corrections)."""
         its = np.zeros(n_energies, np.int32)
@@ -327,6 +342,21 @@ class FmsRealSpacePlan:
                                                                        _ptr(st)))
         return out, st
 
+    def inverse_block(self, wave_numbers, phase_shifts, atom: int):
+        """Atom `atom`'s whole block of (I - G0 T)^-1 per energy from the FP64 LU: (E, states, states) complex,
+        [e, r, c] = (A^-1)[s0 + r, s0 + c]."""
+        k, xp, pts = self._points(wave_numbers, phase_shifts)
+        E = k.shape[0]
+        nsp, L = self.inputs["nsp"], self.inputs["L"]
+        lm = min(int(self.inputs["lmaxph"][self.inputs["potentials"][atom]]), L)
+        lm = L if lm < 0 else lm
+        cnt = nsp * (lm + 1) ** 2
+        out = np.zeros((E, cnt, cnt), np.complex128)
+        st = np.zeros(E, np.int32)
+        self.ctx.check(self.ctx._lib.refeff_fms_plan_inverse_block(self.handle, C.byref(pts), int(atom), _ptr(out),
+                                                                    _ptr(st)))
+        return out, st
+
     PHASES = ("build", "eliminate", "sweeps", "residual", "extract", "tc_update")
 
     def phase_times(self) -> dict:
@@ -346,16 +376,23 @@ class FmsRealSpacePlan:
             pass
 
 
-class PrecondModel:
-    """The learned diagonal preconditioner (refeff_fms_precond_model): an MLP trained and run on the GPU."""
+PRECOND_DIAGONAL = 0
+PRECOND_BLOCK = 1
 
-    def __init__(self, ctx: Context, lmax: int, hidden: int = 64, seed: int = 0):
+
+class PrecondModel:
+    """The learned preconditioner (refeff_fms_precond_model): an MLP trained and run on the GPU that predicts,
+    per (energy, atom), the channel diagonal (kind PRECOND_DIAGONAL) or the whole block (PRECOND_BLOCK) of the
+    atom's block of (I - G0 T)^-1 as a deviation from the identity."""
+
+    def __init__(self, ctx: Context, lmax: int, hidden: int = 64, seed: int = 0, kind: int = PRECOND_DIAGONAL):
         self.ctx = ctx
         h = _p()
-        ctx.check(ctx._lib.refeff_fms_precond_model_create(ctx.handle, int(lmax), int(hidden), C.c_ulonglong(seed),
-                                                           C.byref(h)))
+        ctx.check(ctx._lib.refeff_fms_precond_model_create_kind(ctx.handle, int(lmax), int(hidden), int(kind),
+                                                                C.c_ulonglong(seed), C.byref(h)))
         self.handle = h
         self.lmax = int(lmax)
+        self.kind = int(kind)
         f, hd, o, npar = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
         ctx.check(ctx._lib.refeff_fms_precond_model_query(h, C.byref(f), C.byref(hd), C.byref(o), C.byref(npar)))
         self.n_features, self.hidden, self.n_outputs, self.n_params = f.value, hd.value, o.value, npar.value

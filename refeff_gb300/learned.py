@@ -19,16 +19,20 @@ def device_index(atom: int, n_atoms: int) -> int:
 
 
 def training_set(ctx: fms.Context, cases, *, energies_per_case: int, atoms_per_case: int, seed: int = 0,
-                 energy_window=None):
-    """(X, T): features and targets (diag(block of A^-1) - 1, Re/Im per channel) of sampled atoms and energies.
+                 energy_window=None, kind: int = fms.PRECOND_DIAGONAL):
+    """(X, T): features and targets of sampled atoms and energies.
 
-    cases: list of (Cluster, EnergyGrid); energy_window: optional (lo, hi) in eV on the grid's energies."""
+    Targets: diag(block of A^-1) - 1, Re/Im per channel (kind PRECOND_DIAGONAL), or the whole block of A^-1
+    minus the identity, row-major C x C (C = (L+1)^2), Re/Im interleaved, zero beyond the atom's own channels
+    (PRECOND_BLOCK, one spin channel).  cases: list of (Cluster, EnergyGrid); energy_window: optional (lo, hi)
+    in eV on the grid's energies."""
     rng = np.random.default_rng(seed)
     Xs, Ts = [], []
     for cl, grid in cases:
         plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
         L = plan.inputs["L"]
-        F, O = 2 + 2 * (L + 1) + 3 * (2 + 2 * (L + 1)), 2 * (L + 1) ** 2
+        Cc = (L + 1) ** 2
+        F, O = 2 + 2 * (L + 1) + 3 * (2 + 2 * (L + 1)), (2 * Cc * Cc if kind == fms.PRECOND_BLOCK else 2 * Cc)
         idx = np.arange(grid.wave_numbers.shape[0])
         if energy_window is not None:
             idx = idx[(grid.energies_ev >= energy_window[0]) & (grid.energies_ev <= energy_window[1])]
@@ -38,6 +42,18 @@ def training_set(ctx: fms.Context, cases, *, energies_per_case: int, atoms_per_c
         N = cl.n_atoms
         atoms = rng.choice(N, size=min(atoms_per_case, N), replace=False)
         for a in atoms:
+            if kind == fms.PRECOND_BLOCK:
+                blk, st = plan.inverse_block(k, ph, int(a))
+                ok = st == 0
+                cnt = blk.shape[1]
+                full = np.zeros((len(sel), Cc, Cc), np.complex128)
+                full[:, :cnt, :cnt] = blk - np.eye(cnt)
+                t = np.zeros((len(sel), O), np.float32)
+                t[:, 0::2] = full.reshape(len(sel), -1).real
+                t[:, 1::2] = full.reshape(len(sel), -1).imag
+                Xs.append(feats[ok, device_index(int(a), N)])
+                Ts.append(t[ok])
+                continue
             diag, st = plan.inverse_diagonal(k, ph, int(a))
             ok = st == 0
             nch = diag.shape[1] // plan.inputs["nsp"]
@@ -67,8 +83,9 @@ def rocksalt_training_cases(n_cases: int, radius_range=(6.0, 8.0), n_energies: i
 
 
 def train_preconditioner(ctx: fms.Context, lmax: int, X, T, *, hidden: int = 64, epochs: int = 300,
-                         batch_size: int = 256, learning_rate: float = 2e-3, seed: int = 0):
-    """A PrecondModel trained on (X, T); returns (model, per-epoch full-set loss)."""
-    model = fms.PrecondModel(ctx, lmax, hidden, seed)
+                         batch_size: int = 256, learning_rate: float = 2e-3, seed: int = 0,
+                         kind: int = fms.PRECOND_DIAGONAL):
+    """A PrecondModel of the given kind trained on (X, T); returns (model, per-epoch full-set loss)."""
+    model = fms.PrecondModel(ctx, lmax, hidden, seed, kind)
     hist = model.train(X, T, epochs=epochs, batch_size=batch_size, learning_rate=learning_rate, seed=seed)
     return model, hist
