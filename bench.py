@@ -491,9 +491,13 @@ def profile_case(args):
     ctx.set_option(ctx.OPT_DUAL_STREAMS, 0)  # one batch per sweep: ncu's launch counts follow the sweep
     plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
     plan.set_batch(E)
+    if args.bicgstab_window is not None:
+        plan.set_bicgstab_window(args.bicgstab_window, 1e300)
+    # the first E energies of the grid, or E evenly spaced over it
+    sel = _sample(grid.wave_numbers.shape[0], E) if args.spread else np.arange(E)
     status = None
     for _ in range(args.sweeps):
-        _, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers[:E], grid.phase_shifts[:E], form,
+        _, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers[sel], grid.phase_shifts[sel], form,
                                                 raise_on_error=False)
     print("ok", int((status != 0).sum()), "failed energies", flush=True)
     plan.close()
@@ -702,6 +706,9 @@ def main():
                     help="profiling mode: run one small case (no JSON line)")
     ap.add_argument("--energies", type=int, default=16, help="profiling mode: energies of the case")
     ap.add_argument("--form", default="fp32", choices=["fp32", "fp64", "bicgstab"], help="profiling mode: form")
+    ap.add_argument("--spread", action="store_true", help="profiling mode: energies evenly spaced over the grid")
+    ap.add_argument("--bicgstab-window", type=float, default=None,
+                    help="profiling mode: iterate BiCGSTAB only from this energy above E_ref (eV)")
     ap.add_argument("--sweeps", type=int, default=2, help="profiling mode: sweeps")
     args = ap.parse_args()
     if args.profile_case is not None:

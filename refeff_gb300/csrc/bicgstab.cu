@@ -40,10 +40,26 @@ struct View {
   double* sc;
   int* state;
   int* done;
+  float2* part;    // partial products of slices 1..nsplit-1 of the last split product
+  int nsplit = 1;  // column slices of that product (1: not split)
+  const int* act = nullptr;  // running matrices, compacted (-1 past the count); NULL: blockIdx.y is the matrix
+  __device__ __forceinline__ int matrix() const { return act ? act[blockIdx.y] : int(blockIdx.y); }
   __device__ float2* v(int k, int b, int c) const {
     return vec + (size_t(k) * batch + b) * size_t(lda) * m + size_t(lda) * c;
   }
+  __device__ float2* pv(int slice, int b, int c) const {  // slice >= 1
+    return part + ((size_t(slice - 1) * batch + b) * m + c) * size_t(lda);
+  }
   __device__ double* s(int b, int c) const { return sc + (size_t(b) * m + c) * kBicgScalars; }
+  // y[i] += the other slices' partial products, written back (slice 0 wrote y)
+  __device__ __forceinline__ float2 gather(float2* y, int b, int c, int i) const {
+    float2 a = y[i];
+    if (nsplit > 1) {
+      for (int sl = 1; sl < nsplit; ++sl) a = cadd(a, pv(sl, b, c)[i]);
+      y[i] = a;
+    }
+    return a;
+  }
 };
 
 __device__ __forceinline__ double2 cdot_acc(double2 acc, float2 a, float2 b) {  // acc += conj(a) b
@@ -107,7 +123,8 @@ __global__ void bicg_init_kernel(View w, const float2* __restrict__ M32, size_t 
 
 // p = r + beta (p - omega v);  p^ = D p
 __global__ void bicg_p_kernel(View w, const float2* __restrict__ D, const int* skip) {
-  const int b = blockIdx.y, c = blockIdx.z;
+  const int b = w.matrix(), c = blockIdx.z;
+  if (b < 0) return;
   if (column_idle(w, b, c, skip)) return;
   const double* sc = w.s(b, c);
   const double2 rho_new = make_double2(sc[kAcc1], sc[kAcc1 + 1]);
@@ -130,61 +147,96 @@ __global__ void bicg_p_kernel(View w, const float2* __restrict__ D, const int* s
 }
 
 // Y = A X for the FP32 system matrices: 128 rows x 16 columns per CTA, each
-// thread 4 rows x 4 columns, A staged through shared memory in 32-column
-// slabs (each A entry is read from HBM once per product).
-constexpr int kMvRows = 128, kMvCols = 16, kMvK = 32, kMvThreads = 128;
+// thread 4 rows x 4 columns, A streamed through shared memory in 32-column
+// slabs by a two-stage cp.async pipeline (each A entry is read from HBM once
+// per product; rows past n and columns past the slice are zero-filled by the
+// copies).  The columns of A are split into w.nsplit slices of kchunk
+// (blockIdx.z = column group + groups * slice), so that even one running
+// matrix spreads over the SMs: slice 0 writes Y, slice s > 0 its partial
+// product, and the next dot kernel sums them in slice order.
+constexpr int kMvRows = 128, kMvCols = 16, kMvK = 32, kMvThreads = 128, kMvStages = 2, kMvSliceCols = 512;
+constexpr size_t kMvSmem = size_t(kMvStages) * kMvK * (kMvRows + kMvCols) * sizeof(float2);
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, int bytes) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 
 __global__ void __launch_bounds__(kMvThreads) bicg_matvec_kernel(View w, const float2* __restrict__ M32, size_t stride,
-                                                                  int src, int dst, const int* skip) {
-  const int b = blockIdx.y;
-  if ((skip && skip[b]) || w.done[b]) return;
-  __shared__ __align__(16) float2 As[kMvK][kMvRows];
-  __shared__ float2 Xs[kMvK][kMvCols];
-  const int n = w.n, r0 = blockIdx.x * kMvRows, c0 = blockIdx.z * kMvCols;
+                                                                  int src, int dst, int groups, int kchunk,
+                                                                  const int* skip) {
+  const int b = w.matrix();
+  if (b < 0 || (skip && skip[b]) || w.done[b]) return;
+  extern __shared__ __align__(16) float2 mv_smem[];
+  float2* As = mv_smem;                                   // [stage][kMvK][kMvRows]
+  float2* Xs = mv_smem + size_t(kMvStages) * kMvK * kMvRows;  // [stage][kMvK][kMvCols]
+  const int slice = blockIdx.z / groups;
+  const int n = w.n, r0 = blockIdx.x * kMvRows, c0 = (blockIdx.z % groups) * kMvCols;
+  const int kbeg = slice * kchunk, kend = min(n, kbeg + kchunk);
   const float2* A = M32 + size_t(b) * stride;
   const int tid = threadIdx.x, rg = tid & 31, cq = tid >> 5;
+  // one slab: kMvK columns of A (128 rows as 16-byte row pairs) and of X
+  auto load = [&](int stage, int k0) {
+    float2* as = As + size_t(stage) * kMvK * kMvRows;
+    float2* xs = Xs + size_t(stage) * kMvK * kMvCols;
+    for (int idx = tid; idx < kMvK * (kMvRows / 2); idx += kMvThreads) {
+      const int rr = (idx % (kMvRows / 2)) * 2, kk = idx / (kMvRows / 2), row = r0 + rr;
+      const bool in = k0 + kk < kend && row < n;
+      const int bytes = in ? (row + 1 < n ? 16 : 8) : 0;
+      cp_async16(as + size_t(kk) * kMvRows + rr, in ? A + size_t(row) + size_t(w.lda) * (k0 + kk) : A, bytes);
+    }
+    for (int idx = tid; idx < kMvK * kMvCols; idx += kMvThreads) {
+      const int kk = idx % kMvK, cc = idx / kMvK;
+      const bool in = k0 + kk < kend && c0 + cc < w.m;
+      const float2* xsrc = in ? w.v(src, b, c0 + cc) + (k0 + kk) : A;
+      cp_async8(xs + size_t(kk) * kMvCols + cc, xsrc, in ? 8 : 0);
+    }
+    cp_async_commit();
+  };
   float2 acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
-  for (int k0 = 0; k0 < n; k0 += kMvK) {
-    const int kn = min(kMvK, n - k0);
-    __syncthreads();
-    // A slab: kMvK columns x 128 rows as float4 pairs (lda is a multiple of 32,
-    // r0 a multiple of 128, so every float4 is aligned)
-    for (int idx = tid; idx < kMvK * (kMvRows / 2); idx += kMvThreads) {
-      const int rr = (idx % (kMvRows / 2)) * 2, kk = idx / (kMvRows / 2);
-      float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (kk < kn && r0 + rr < w.lda)
-        a = *reinterpret_cast<const float4*>(A + size_t(r0 + rr) + size_t(w.lda) * (k0 + kk));
-      if (r0 + rr >= n) a.x = a.y = 0.f;
-      if (r0 + rr + 1 >= n) a.z = a.w = 0.f;
-      *reinterpret_cast<float4*>(&As[kk][rr]) = a;
-    }
-    for (int idx = tid; idx < kMvK * kMvCols; idx += kMvThreads) {
-      const int kk = idx % kMvK, cc = idx / kMvK;
-      Xs[kk][cc] = (kk < kn && c0 + cc < w.m) ? w.v(src, b, c0 + cc)[k0 + kk] : make_float2(0.f, 0.f);
+  int stage = 0;
+  if (kbeg < kend) load(0, kbeg);
+  for (int k0 = kbeg; k0 < kend; k0 += kMvK, stage ^= 1) {
+    if (k0 + kMvK < kend) {
+      load(stage ^ 1, k0 + kMvK);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
     }
     __syncthreads();
-#pragma unroll 4
-    for (int kk = 0; kk < kn; ++kk) {
+    const float2* as = As + size_t(stage) * kMvK * kMvRows;
+    const float2* xs = Xs + size_t(stage) * kMvK * kMvCols;
+#pragma unroll 8
+    for (int kk = 0; kk < kMvK; ++kk) {
       float2 a[4], x[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][rg + 32 * i];
+      for (int i = 0; i < 4; ++i) a[i] = as[kk * kMvRows + rg + 32 * i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) x[j] = Xs[kk][cq + 4 * j];
+      for (int j = 0; j < 4; ++j) x[j] = xs[kk * kMvCols + cq + 4 * j];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], x[j]);
     }
+    __syncthreads();  // the next iteration's copy overwrites this stage
   }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int c = c0 + cq + 4 * j;
     if (c >= w.m) continue;
-    float2* y = w.v(dst, b, c);
+    float2* y = slice == 0 ? w.v(dst, b, c) : w.pv(slice, b, c);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = r0 + rg + 32 * i;
@@ -195,14 +247,16 @@ __global__ void __launch_bounds__(kMvThreads) bicg_matvec_kernel(View w, const f
 
 // acc2 += (r~, v)
 __global__ void bicg_dot_rv_kernel(View w, const int* skip) {
-  const int b = blockIdx.y, c = blockIdx.z;
+  const int b = w.matrix(), c = blockIdx.z;
+  if (b < 0) return;
   if (column_idle(w, b, c, skip)) return;
-  const float2 *rh = w.v(kRh, b, c), *v = w.v(kV, b, c);
+  const float2* rh = w.v(kRh, b, c);
+  float2* v = w.v(kV, b, c);
   double2 acc = make_double2(0.0, 0.0);
   for (int k = 0; k < kVecRowsPerThread; ++k) {
     const int i = blockIdx.x * kVecRows + k * kVecThreads + threadIdx.x;
     if (i >= w.n) break;
-    acc = cdot_acc(acc, rh[i], v[i]);
+    acc = cdot_acc(acc, rh[i], w.gather(v, b, c, i));
   }
   double* sc = w.s(b, c);
   block_accumulate(sc + kAcc2, acc.x, sc + kAcc2 + 1, acc.y, nullptr, 0.0);
@@ -241,7 +295,8 @@ __global__ void bicg_alpha_kernel(View w, const int* skip) {
 __global__ void bicg_block_apply_kernel(View w, int src, int dst, const float2* __restrict__ Bblk,
                                         const int* __restrict__ state_atom, const int* __restrict__ atom_off, int N,
                                         int C, const int* skip) {
-  const int b = blockIdx.y, c = blockIdx.z;
+  const int b = w.matrix(), c = blockIdx.z;
+  if (b < 0) return;
   if (column_idle(w, b, c, skip)) return;
   const float2* in = w.v(src, b, c);
   float2* out = w.v(dst, b, c);
@@ -258,7 +313,8 @@ __global__ void bicg_block_apply_kernel(View w, int src, int dst, const float2* 
 
 // s = r - alpha v (in r);  s^ = D s
 __global__ void bicg_s_kernel(View w, const float2* __restrict__ D, const int* skip) {
-  const int b = blockIdx.y, c = blockIdx.z;
+  const int b = w.matrix(), c = blockIdx.z;
+  if (b < 0) return;
   if (column_idle(w, b, c, skip)) return;
   const double* sc = w.s(b, c);
   const float2 af = make_float2(float(sc[kAlpha]), float(sc[kAlpha + 1]));
@@ -276,16 +332,19 @@ __global__ void bicg_s_kernel(View w, const float2* __restrict__ D, const int* s
 
 // acc2 += (t, s), acc3 += |t|^2
 __global__ void bicg_dot_ts_kernel(View w, const int* skip) {
-  const int b = blockIdx.y, c = blockIdx.z;
+  const int b = w.matrix(), c = blockIdx.z;
+  if (b < 0) return;
   if (column_idle(w, b, c, skip)) return;
-  const float2 *t = w.v(kT, b, c), *sv = w.v(kR, b, c);
+  float2* t = w.v(kT, b, c);
+  const float2* sv = w.v(kR, b, c);
   double2 ts = make_double2(0.0, 0.0);
   double tt = 0.0;
   for (int k = 0; k < kVecRowsPerThread; ++k) {
     const int i = blockIdx.x * kVecRows + k * kVecThreads + threadIdx.x;
     if (i >= w.n) break;
-    ts = cdot_acc(ts, t[i], sv[i]);
-    tt += double(t[i].x) * t[i].x + double(t[i].y) * t[i].y;
+    const float2 ti = w.gather(t, b, c, i);
+    ts = cdot_acc(ts, ti, sv[i]);
+    tt += double(ti.x) * ti.x + double(ti.y) * ti.y;
   }
   double* sc = w.s(b, c);
   block_accumulate(sc + kAcc2, ts.x, sc + kAcc2 + 1, ts.y, sc + kAcc3, tt);
@@ -311,7 +370,8 @@ __global__ void bicg_omega_kernel(View w, const int* skip) {
 
 // x += alpha p^ + omega s^;  r = s - omega t;  acc4 += |r|^2, acc1 += (r~, r)
 __global__ void bicg_xr_kernel(View w, const int* skip) {
-  const int b = blockIdx.y, c = blockIdx.z;
+  const int b = w.matrix(), c = blockIdx.z;
+  if (b < 0) return;
   if (column_idle(w, b, c, skip)) return;
   const double* sc = w.s(b, c);
   const float2 af = make_float2(float(sc[kAlpha]), float(sc[kAlpha + 1]));
@@ -356,6 +416,59 @@ __global__ void bicg_check_kernel(View w, double tol2, int iter, int* iters, int
   else atomicAdd(active, 1);
 }
 
+// The compacted list of running matrices (one block, batch <= kCompactMax):
+// act[0..count) the running ones in order, -1 after.
+constexpr int kCompactMax = 1024;
+__device__ __forceinline__ void compact_running(bool alive, int b, int batch, int* act) {
+  __shared__ int warp_total[kCompactMax / 32];
+  const unsigned bal = __ballot_sync(0xffffffffu, alive);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_total[wid] = __popc(bal);
+  __syncthreads();
+  int base = 0, total = 0;
+  for (int i = 0; i < int(blockDim.x >> 5); ++i) {
+    if (i < wid) base += warp_total[i];
+    total += warp_total[i];
+  }
+  if (alive) act[base + __popc(bal & ((1u << lane) - 1u))] = b;
+  if (b >= total && b < batch) act[b] = -1;  // disjoint from the positions below total
+}
+
+__global__ void bicg_act_init_kernel(int batch, const int* skip, int* act) {
+  const int b = threadIdx.x;
+  compact_running(b < batch && !(skip && skip[b]), b, batch, act);
+}
+
+// bicg_check_kernel for one block over the whole batch, which also rebuilds
+// the compacted list of running matrices for the next iteration's launches.
+__global__ void bicg_check_compact_kernel(View w, double tol2, int iter, int* iters, int* active, const int* skip,
+                                          int* act) {
+  const int b = threadIdx.x;
+  bool alive = false;
+  if (b < w.batch && !(skip && skip[b]) && !w.done[b]) {
+    bool all = true;
+    for (int c = 0; c < w.m; ++c) {
+      int& st = w.state[size_t(b) * w.m + c];
+      double* sc = w.s(b, c);
+      if (st == 0) {
+        const double rr = sc[kAcc4];
+        if (!isfinite(rr)) st = 2;
+        else if (rr <= tol2 * sc[kB2]) st = 1;
+      }
+      sc[kAcc4] = 0.0;
+      all = all && st != 0;
+    }
+    iters[b] = iter;
+    if (all) {
+      w.done[b] = 1;
+    } else {
+      alive = true;
+      atomicAdd(active, 1);
+    }
+  }
+  compact_running(alive, b, w.batch, act);
+}
+
 // Solution X -> RHS columns of M32; failed[b] = 2 when a column did not converge.
 __global__ void bicg_finish_kernel(View w, float2* __restrict__ M32, size_t stride, int* failed, const int* skip) {
   const int b = blockIdx.y, c = blockIdx.z;
@@ -375,9 +488,23 @@ __global__ void bicg_finish_kernel(View w, float2* __restrict__ M32, size_t stri
 cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BlockPrecond* blk,
                            const BicgWork& w, double tol, int max_iter, int poll, const int* skip, int* failed,
                            cudaStream_t s) {
-  View v{lay.n, lay.m, lay.lda, batch, w.vec, w.sc, w.state, w.done};
+  View v{lay.n, lay.m, lay.lda, batch, w.vec, w.sc, w.state, w.done, w.part, 1};
   const dim3 vgrid(unsigned((lay.n + kVecRows - 1) / kVecRows), unsigned(batch), unsigned(lay.m));
-  const dim3 mgrid(unsigned((lay.n + kMvRows - 1) / kMvRows), unsigned(batch), unsigned((lay.m + kMvCols - 1) / kMvCols));
+  const int row_blocks = (lay.n + kMvRows - 1) / kMvRows, groups = (lay.m + kMvCols - 1) / kMvCols;
+  {
+    const cudaError_t e = cudaFuncSetAttribute(bicg_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               int(kMvSmem));
+    if (e != cudaSuccess) return e;
+  }
+  // Slices of A's columns: 512 columns each (more for n > 8192, at most
+  // kBicgMaxSplit slices), so that the last running matrices still fill the
+  // GPU with product CTAs.  The slicing depends on n alone: a matrix's
+  // arithmetic does not depend on which others share its batch.
+  int chunk = lay.n, nsplit = 1;
+  if (w.part) {
+    chunk = std::max(kMvSliceCols, ((lay.n + kBicgMaxSplit - 1) / kBicgMaxSplit + kMvK - 1) / kMvK * kMvK);
+    nsplit = (lay.n + chunk - 1) / chunk;
+  }
   const int sthreads = 128, sblocks = (batch * lay.m + sthreads - 1) / sthreads;
   const int bblocks = (batch + sthreads - 1) / sthreads;
   cudaMemsetAsync(w.sc, 0, size_t(batch) * lay.m * kBicgScalars * sizeof(double), s);
@@ -398,40 +525,58 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
     // the host vector must outlive the copy
     cudaStreamSynchronize(s);
   }
+  // The iteration's launches cover only the running matrices: the check
+  // kernel keeps a compacted list of them, and the grids are sized by the
+  // count of the last host poll (an upper bound: matrices only finish).
+  const bool compact = w.act && batch <= kCompactMax;
+  const unsigned cthreads = unsigned((batch + 31) / 32 * 32);
+  if (compact) {
+    count_launch();
+    bicg_act_init_kernel<<<1, cthreads, 0, s>>>(batch, skip, w.act);
+  }
+  View vr = v;  // the view of the iteration's launches
+  vr.act = compact ? w.act : nullptr;
   int running = batch;
   for (int it = 1; it <= max_iter && running > 0; ++it) {
+    vr.nsplit = nsplit;  // the dot kernels sum the slices
+    const unsigned rows_y = unsigned(compact ? running : batch);
+    const dim3 rgrid(vgrid.x, rows_y, vgrid.z);
+    const dim3 mgrid(unsigned(row_blocks), rows_y, unsigned(groups * vr.nsplit));
     count_launch();
-    bicg_p_kernel<<<vgrid, kVecThreads, 0, s>>>(v, blk ? nullptr : D, skip);
+    bicg_p_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, blk ? nullptr : D, skip);
     if (blk) {
       count_launch();
-      bicg_block_apply_kernel<<<vgrid, kVecThreads, 0, s>>>(v, kP, kPh, blk->B, blk->state_atom, blk->atom_off,
+      bicg_block_apply_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, kP, kPh, blk->B, blk->state_atom, blk->atom_off,
                                                             blk->N, blk->C, skip);
     }
     count_launch();
-    bicg_matvec_kernel<<<mgrid, kMvThreads, 0, s>>>(v, M32, lay.stride, kPh, kV, skip);
+    bicg_matvec_kernel<<<mgrid, kMvThreads, kMvSmem, s>>>(vr, M32, lay.stride, kPh, kV, groups, chunk, skip);
     count_launch();
-    bicg_dot_rv_kernel<<<vgrid, kVecThreads, 0, s>>>(v, skip);
+    bicg_dot_rv_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, skip);
     count_launch();
     bicg_alpha_kernel<<<sblocks, sthreads, 0, s>>>(v, skip);
     count_launch();
-    bicg_s_kernel<<<vgrid, kVecThreads, 0, s>>>(v, blk ? nullptr : D, skip);
+    bicg_s_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, blk ? nullptr : D, skip);
     if (blk) {
       count_launch();
-      bicg_block_apply_kernel<<<vgrid, kVecThreads, 0, s>>>(v, kR, kSh, blk->B, blk->state_atom, blk->atom_off,
+      bicg_block_apply_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, kR, kSh, blk->B, blk->state_atom, blk->atom_off,
                                                             blk->N, blk->C, skip);
     }
     count_launch();
-    bicg_matvec_kernel<<<mgrid, kMvThreads, 0, s>>>(v, M32, lay.stride, kSh, kT, skip);
+    bicg_matvec_kernel<<<mgrid, kMvThreads, kMvSmem, s>>>(vr, M32, lay.stride, kSh, kT, groups, chunk, skip);
     count_launch();
-    bicg_dot_ts_kernel<<<vgrid, kVecThreads, 0, s>>>(v, skip);
+    bicg_dot_ts_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, skip);
     count_launch();
     bicg_omega_kernel<<<sblocks, sthreads, 0, s>>>(v, skip);
     count_launch();
-    bicg_xr_kernel<<<vgrid, kVecThreads, 0, s>>>(v, skip);
+    bicg_xr_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, skip);
     const bool poll_now = (it % std::max(poll, 1)) == 0 || it == max_iter;
     if (poll_now) cudaMemsetAsync(w.active, 0, sizeof(int), s);
     count_launch();
-    bicg_check_kernel<<<bblocks, sthreads, 0, s>>>(v, tol * tol, it, w.iters, w.active, skip);
+    if (compact)
+      bicg_check_compact_kernel<<<1, cthreads, 0, s>>>(v, tol * tol, it, w.iters, w.active, skip, w.act);
+    else
+      bicg_check_kernel<<<bblocks, sthreads, 0, s>>>(v, tol * tol, it, w.iters, w.active, skip);
     if (poll_now) {
       cudaError_t e = cudaMemcpyAsync(&running, w.active, sizeof(int), cudaMemcpyDeviceToHost, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);

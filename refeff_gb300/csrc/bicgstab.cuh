@@ -10,6 +10,9 @@ namespace rfx {
 constexpr int kBicgVectors = 8;
 // Doubles kept per (matrix, column): rho, alpha, omega, |b|^2, and accumulators.
 constexpr int kBicgScalars = 16;
+// Most slices the matrix-vector product splits A's columns into (partial
+// products summed by the dot kernels).
+constexpr int kBicgMaxSplit = 16;
 
 struct BicgWork {
   float2* vec = nullptr;     // kBicgVectors * batch * lda * m
@@ -18,6 +21,8 @@ struct BicgWork {
   int* done = nullptr;       // batch: every column finished
   int* iters = nullptr;      // batch: iterations of the slowest column
   int* active = nullptr;     // 1 int: matrices still running (host poll)
+  float2* part = nullptr;    // (kBicgMaxSplit - 1) * batch * lda * m: partial products of the split product
+  int* act = nullptr;        // batch: compacted list of running matrices
 };
 
 // Solves A X = B for every matrix of the batch whose skip flag is clear:

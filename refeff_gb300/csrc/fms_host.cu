@@ -411,6 +411,8 @@ struct Workspace {
   // BiCGSTAB form: solver vectors and scalars, the preconditioner diagonal,
   // per-atom features and network outputs
   DevBuf<float2> bicg_vec, precond_D;
+  DevBuf<float2> bicg_part;  // partial products of the split matrix-vector product
+  DevBuf<int> bicg_act;      // compacted list of the running matrices
   DevBuf<float2> precond_B;  // block-diagonal learned preconditioner: batch x N x C^2
   DevBuf<double> bicg_sc;
   DevBuf<int> bicg_state, bicg_done, bicg_iters, bicg_active, bicg_total;
@@ -982,6 +984,8 @@ BicgWork bicg_work(Workspace& ws) {
   w.done = ws.bicg_done.p;
   w.iters = ws.bicg_iters.p;
   w.active = ws.bicg_active.p;
+  w.part = ws.bicg_part.p;
+  w.act = ws.bicg_act.p;
   return w;
 }
 
@@ -989,7 +993,7 @@ BicgWork bicg_work(Workspace& ws) {
 // replaced by preconditioned BiCGSTAB solves on the unfactored FP32 matrix
 // (M32 holds A and, in its last m columns, the right-hand side).  A system
 // whose BiCGSTAB solve misses its tolerance within the iteration cap is
-// marked converged = 2 and handed to the FP64 LU by the caller.
+// marked converged = 2 and handed to the refined LU by the caller.
 cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, const BlockPrecond* blk, int iters, double tol,
                             int max_iter, double inner_tol, int poll, cudaStream_t s, Spans* spans = nullptr) {
   const BatchLayout& lay = ws.lay;
@@ -1320,6 +1324,8 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
   if (bicg) {
     const size_t cols = size_t(ws.batch) * p.m;
     RF_CUDA(ctx, ws.bicg_vec.alloc(size_t(kBicgVectors) * cols * ws.lay.lda));
+    RF_CUDA(ctx, ws.bicg_part.alloc(size_t(kBicgMaxSplit - 1) * cols * ws.lay.lda));
+    RF_CUDA(ctx, ws.bicg_act.alloc(size_t(ws.batch)));
     RF_CUDA(ctx, ws.bicg_sc.alloc(cols * kBicgScalars));
     RF_CUDA(ctx, ws.bicg_state.alloc(cols));
     RF_CUDA(ctx, ws.bicg_done.alloc(size_t(ws.batch)));
