@@ -494,12 +494,34 @@ int refeff_fms_write_fms_bin(const char* path, double cluster_radius, int ne, in
  *     i_gamma_ch = 1; ff2x.rs:5416-5425); above 1e-4 (total, atomic) are Lorentz-broadened over
  *     omega before normalisation (ff2x.rs:3265-3306, FMS-only spectra)
  *   mu, mu0, chi: ne1 each, optional.
- * The sig_gk Debye factor and the thermal xscorr are not applied. */
+ * The sig_gk Debye factor is applied by refeff_ff2x_debye_factor; this call
+ * runs the zero-temperature xscorr (refeff_ff2x_xanes_mu_thermal takes the
+ * electronic temperature). */
 int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
                          const refeff_complex128* energy, const double* omega, const refeff_complex128* cross_section,
                          const double* background, const refeff_complex128* trace, double s02, double real_correction,
                          double imaginary_correction, double fermi_photon_energy, double* mu, double* mu0,
                          double* chi);
+/* refeff_ff2x_xanes_mu with FEFF's electronic temperature (eV; 0 = the
+ * zero-temperature xscorr, > 0 the thermal xscorr below). */
+int refeff_ff2x_xanes_mu_thermal(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
+                                 const refeff_complex128* energy, const double* omega,
+                                 const refeff_complex128* cross_section, const double* background,
+                                 const refeff_complex128* trace, double s02, double real_correction,
+                                 double imaginary_correction, double fermi_photon_energy,
+                                 double electronic_temperature_ev, double* mu, double* mu0, double* chi);
+/* FF2X xscorr (ff2x_xscorr, crates/refeff-engine/src/ff2x.rs:4437-4641, and
+ * at electronic_temperature_ev > 0 ff2x_thermal_xscorr, 4643-5050): the
+ * correction cchi (ne1 rows) of xmu = cross_section + path_chi * background
+ * over the xsect.dat rows.  The thermal form needs ne >= 2 ne1 + 11 rows (the
+ * horizontal rows, ne1 loss rows, 10 auxiliary rows, the poles and a last row
+ * at the Fermi level) and ignores fermi_index.  Host only.  Errors:
+ * INVALID_ARGUMENT (layout, temperature < 0, a Fermi window outside the grid),
+ * NONFINITE_INPUT. */
+int refeff_ff2x_xscorr(int ne, int ne1, int fermi_index, int ispec, const refeff_complex128* energy,
+                       const refeff_complex128* cross_section, const double* background,
+                       const refeff_complex128* path_chi, double real_correction, double electronic_temperature_ev,
+                       refeff_complex128* cchi_out);
 
 /* FEFF conv (crates/refeff-core/src/convolution/lorentzian.rs:32-100): the
  * piecewise-linear spectrum (n >= 2 points over increasing omega) broadened by

@@ -6,6 +6,7 @@ refeff_ff2x_xanes_mu; never shipped or called by the product.
   lorenz, astep                  crates/refeff-engine/src/ff2x.rs:5052-5076
                                  (crates/refeff-core/src/xscorr.rs:39-73 for the core ports and their known answers)
   xscorr, zero temperature       crates/refeff-engine/src/ff2x.rs:4437-4641
+  xscorr, thermal                crates/refeff-engine/src/ff2x.rs:4643-5050 (thermal_xscorr below)
   corrected components           crates/refeff-engine/src/ff2x.rs:3186-3262
   xmu.dat normalisation / rows   crates/refeff-engine/src/ff2x.rs:3309-3399
   locat / terp window / polint   crates/refeff-core/src/interpolation.rs:119-135, 338-446
@@ -14,7 +15,8 @@ refeff_ff2x_xanes_mu; never shipped or called by the product.
 
 Known answers pinned in tests/test_ff2x.py: the three lorenz and three astep values of
 crates/refeff-core/src/xscorr.rs:121-157 and the constant-cross-section xscorr case of
-crates/refeff-engine/src/ff2x/tests.rs:1127-1149 (fixture 5167-5195).  The contour integral with a
+crates/refeff-engine/src/ff2x/tests.rs:1127-1149 (fixture 5167-5195), and the thermal xscorr's
+constant-cross-section case at 0.5 eV of tests.rs:1152-1178 (fixture 5197-5238).  The contour integral with a
 non-constant integrand has no reference known answer here: for it this restatement and the product's
 C++ agree with each other (parity of that term unpinned).
 """
@@ -133,6 +135,136 @@ def xscorr(ispec, energy, ne1, fermi, xsec, bg, chia, vrcorr=0.0):
         if ispec == 2:
             corr = -corr
         out.append(conv + corr - xmu[r])
+    return out
+
+
+def _fermi(e, t, ef):
+    """Fermi function, zero above (e - ef) / t = 100 (ff2x.rs:5029-5042); e may be an array."""
+    x = (np.asarray(e, dtype=np.float64) - ef) / t
+    with np.errstate(over="ignore"):
+        return np.where(x < 100.0, 1.0 / (np.exp(np.minimum(x, 100.0)) + 1.0), 0.0)
+
+
+def _cauchy_real(e, w, xloss):
+    return (xloss / math.pi) / ((e - w) ** 2 + xloss ** 2)
+
+
+def _fermi_lorentz(w, t, ef, xloss):
+    """Fermi-weighted Lorentzian over the real axis (ff2x.rs:4802-4859): rectangles on [-1, 0] and [0, 1]
+    plus the two tails mapped by E = 1/u, 20000 points each."""
+    n, top = 20000, 1.0
+    dw = top / (n - 1.0)
+    i = np.arange(n - 1, dtype=np.float64)
+    z = 1.0 / (-top + i * dw)
+    keep = (z - ef) / t < 100.0
+    total = np.sum(np.where(keep, _fermi(z, t, ef) * _cauchy_real(z, w, xloss) * z * z, 0.0))
+    neg, pos = -top + i * dw, i * dw
+    total += np.sum(_fermi(neg, t, ef) * _cauchy_real(neg, w, xloss) + _fermi(pos, t, ef) * _cauchy_real(pos, w, xloss))
+    idx = np.arange(n, 1, -1, dtype=np.float64)
+    z = 1.0 / (top - (n - idx) * dw)
+    keep = (z - ef) / t < 100.0
+    total += np.sum(np.where(keep, _fermi(z, t, ef) * _cauchy_real(z, w, xloss) * z * z, 0.0))
+    return float(total * dw)
+
+
+def _search1(x0, x):
+    """1-based insertion index (len + 1 past the end; ff2x.rs:5015-5027)."""
+    if x0 >= x[-1]:
+        return len(x) + 1
+    if x0 <= x[0]:
+        return 1
+    return int(np.searchsorted(x, x0, side="left")) + 1
+
+
+def _interp1(x0, x, y):
+    if x[0] < x0 < x[-1]:
+        hi = _search1(x0, x) - 1
+        lo = hi - 1
+        return (y[hi] - y[lo]) * ((x0 - x[lo]) / (x[hi] - x[lo])) + y[lo]
+    if x[0] == x0:
+        return y[0]
+    if abs(x[-1] - x0) < 1e-10:
+        return y[-1]
+    raise ValueError("interpolation point outside the grid")
+
+
+def _thermal_contour(en, xmu, ef, t, xmu0, xloss, w, ispec):
+    """The Fermi-weighted Lorentzian integral of xmu - xmu0 along the horizontal grid, its Fermi window
+    resampled at 10000 points (ff2x.rs:4861-4978)."""
+    re = np.array([e.real for e in en])
+    window = 10.0
+    if ef > re[0]:
+        window = min(math.floor((ef - re[0]) / t), 10.0)
+    if not window > 0.0:
+        raise ValueError("Fermi window collapsed")
+    ns = 10000
+    de = 2.0 * window * t / ns
+    lo, hi = ef - window * t, ef + window * t
+    if lo < re[0] or hi > re[-1]:
+        raise ValueError("Fermi window outside the horizontal grid")
+    i_lo = max(max(_search1(lo, re) - 1, 0), 1)
+    i_hi = min(_search1(hi, re), len(en))
+    ze = list(en[:i_lo])
+    zv = list(xmu[:i_lo])
+    for i in range(ns):
+        x = lo + i * de
+        ze.append(complex(x, en[0].imag))
+        zv.append(_interp1(x, re, xmu))
+    ze.append(complex(hi, en[0].imag))
+    zv.append(_interp1(hi, re, xmu))
+    ze += list(en[i_hi:])
+    zv += list(xmu[i_hi:])
+    ze, zv = np.array(ze), np.array(zv)
+    z1, z2 = ze[:-1], ze[1:]
+    k1, k2 = zv[:-1] - xmu0, zv[1:] - xmu0
+    f1, f2 = _fermi(z1.real, t, ef), _fermi(z2.real, t, ef)
+    if ispec != 2:
+        f1, f2 = 1.0 - f1, 1.0 - f2
+    dz = z2 - z1
+    assert np.all(np.abs(dz) > 0.0)
+    e1, e2 = complex(w, xloss), complex(w, -xloss)
+
+    def cauchy(z):
+        return (xloss / math.pi) / ((z - w) ** 2 + xloss * xloss)
+
+    inside = (z1.real > lo) & (z1.real < hi)
+    trap = 0.5 * dz * (k1 * f1 * cauchy(z1) + k2 * f2 * cauchy(z2))
+    near = (np.abs(z1 - e1) > EPS4) & (np.abs(z2 - e1) > EPS4)
+    with np.errstate(all="ignore"):
+        seg = np.where(near, -np.log((z2 - e1) / (z1 - e1)) * (k1 * f1 * (z2 - e1) + k2 * f2 * (e1 - z1)), 0.0)
+        seg = seg + np.log((z2 - e2) / (z1 - e2)) * (k1 * f1 * (z2 - e2) + k2 * f2 * (e2 - z1))
+    exact = -seg / dz / complex(0.0, 2.0 * math.pi)
+    return complex(np.sum(np.where(inside, trap, exact)))
+
+
+def thermal_xscorr(ispec, energy, ne1, xsec, bg, chia, vrcorr=0.0, temperature_ev=0.5):
+    """cchi[0:ne1] of the thermal xscorr (ff2x.rs:4643-4800).  Rows: ne1 horizontal, ne1 at the loss width,
+    10 auxiliary, the poles, and the Fermi-level row last."""
+    ne = len(energy)
+    energy = np.array([complex(e) for e in energy])
+    xmu = np.array([complex(xsec[r]) + complex(chia[r]) * float(bg[r]) for r in range(ne)])
+    pole_start = 2 * ne1 + 10
+    assert ne >= pole_start + 1 and temperature_ev > 0.0
+    xloss = energy[ne1].imag
+    ef = energy[-1].real
+    shifted = abs(vrcorr) > EPS4
+    if shifted:
+        ef -= vrcorr
+    t = temperature_ev / HARTREE_EV
+    poles = energy[pole_start:ne - 1] - (vrcorr if shifted else 0.0)
+    out = []
+    for r in range(ne1):
+        w = energy[r].real
+        xmu0 = xmu[ne1 + r]
+        conv = xmu0 * _fermi_lorentz(w, t, ef, xloss)
+        if ispec != 2:
+            conv = xmu0 - conv
+        res = complex(np.sum((xmu[pole_start:ne - 1] - xmu0) * xloss / ((poles - w) ** 2 + xloss * xloss)))
+        res *= complex(0.0, -2.0 * t)
+        if ispec != 2:
+            res = -res
+        contour = _thermal_contour(energy[:ne1], xmu[:ne1], ef, t, xmu0, xloss, w, ispec)
+        out.append(conv + contour + res - xmu[r])
     return out
 
 

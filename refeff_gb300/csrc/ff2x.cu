@@ -246,7 +246,253 @@ int xscorr(int ispec, const cd* energy_in, size_t ne, size_t ne1, size_t fermi, 
   return REFEFF_FMS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Thermal xscorr (electronic temperature > 0; ff2x_thermal_xscorr,
+// crates/refeff-engine/src/ff2x.rs:4643-4800).  The xsect.dat rows then hold
+// the ne1 horizontal rows, ne1 loss rows (the horizontal energies at the loss
+// width), 10 auxiliary rows, the Matsubara-like poles and a last row at the
+// Fermi level.  Per horizontal row (photon energy w, loss-row value xmu0):
+//   cchi = xmu0 * [FL(w) or 1 - FL(w)] + contour(w) + residue(w) - xmu[row]
+// FL: the Fermi-weighted Lorentzian over the real axis (fermi_lorentz below),
+// residue: -2 i T sum over poles z_p of (xmu_p - xmu0) xloss / ((z_p - w)^2 +
+// xloss^2) (negated unless ispec == 2), contour: the Fermi-weighted Lorentzian
+// integral of xmu - xmu0 along the horizontal grid, refined to 10000 linear
+// samples within +-min(10, (E_F - E_0)/T) T of the Fermi level.
+
+double fermi_fn(double e, double t, double ef) {  // ff2x.rs:5029-5042
+  if (t > 0.0) {
+    const double x = (e - ef) / t;
+    return x < 100.0 ? 1.0 / (std::exp(x) + 1.0) : 0.0;
+  }
+  return e > ef ? 1.0 : 0.0;
+}
+
+double cauchy_real(double e, double w, double xloss) { return (xloss / kPi) / ((e - w) * (e - w) + xloss * xloss); }
+
+cd cauchy(cd z, double w, double xloss) {
+  const cd d = z - cd(w, 0.0);
+  return (xloss / kPi) / (d * d + cd(xloss * xloss, 0.0));
+}
+
+// 1-based insertion index of x0 in the ascending grid (len + 1 past the end).
+size_t search1(double x0, const std::vector<double>& x) {
+  if (x0 >= x.back()) return x.size() + 1;
+  if (x0 <= x.front()) return 1;
+  return size_t(std::lower_bound(x.begin(), x.end(), x0) - x.begin()) + 1;
+}
+
+bool interp1(double x0, const std::vector<double>& x, const cd* y, cd& out) {
+  const size_t n = x.size();
+  if (x.front() < x0 && x0 < x.back()) {
+    const size_t hi = search1(x0, x) - 1, lo = hi - 1;
+    if (x[hi] == x[lo]) return false;
+    out = (y[hi] - y[lo]) * ((x0 - x[lo]) / (x[hi] - x[lo])) + y[lo];
+    return true;
+  }
+  if (x.front() == x0) {
+    out = y[0];
+    return true;
+  }
+  if (std::fabs(x.back() - x0) < 1.0e-10) {
+    out = y[n - 1];
+    return true;
+  }
+  return false;
+}
+
+// Integral over the real axis of f(E) * Lorentzian(E - w): 20000-point
+// rectangles on [-1, 0] and [0, 1] plus the tails mapped by E = 1/u.
+double fermi_lorentz(double w, double t, double ef, double xloss) {
+  constexpr int kCount = 20000;
+  constexpr double kMax = 1.0, dw = kMax / (kCount - 1.0);
+  double sum = 0.0;
+  for (int i = 0; i < kCount - 1; ++i) {
+    const double z = 1.0 / (-kMax + i * dw);
+    if ((z - ef) / t < 100.0) sum += fermi_fn(z, t, ef) * cauchy_real(z, w, xloss) * (z * z);
+  }
+  for (int i = 0; i < kCount - 1; ++i) {
+    const double neg = -kMax + i * dw, pos = i * dw;
+    sum += fermi_fn(neg, t, ef) * cauchy_real(neg, w, xloss);
+    sum += fermi_fn(pos, t, ef) * cauchy_real(pos, w, xloss);
+  }
+  for (int idx = kCount; idx >= 2; --idx) {
+    const double z = 1.0 / (kMax - (kCount - idx) * dw);
+    if ((z - ef) / t < 100.0) sum += fermi_fn(z, t, ef) * cauchy_real(z, w, xloss) * (z * z);
+  }
+  return sum * dw;
+}
+
+// The contour part: the horizontal grid with its Fermi window resampled,
+// trapezoids inside the window, the exact linear-segment Lorentzian integral
+// outside it.
+int thermal_contour(const std::vector<cd>& en, const std::vector<cd>& xmu, double ef, double t, cd xmu0, double xloss,
+                    double w, int ispec, cd& out, std::string& err) {
+  const double first = en.front().real(), last = en.back().real();
+  double window = 10.0;
+  if (ef > first) window = std::min(std::floor((ef - first) / t), 10.0);
+  if (!(std::isfinite(window) && window > 0.0)) {
+    err = "thermal xscorr: the Fermi window collapsed";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  constexpr int kSamples = 10000;
+  const double de = 2.0 * window * t / kSamples, lo = ef - window * t, hi = ef + window * t;
+  if (lo < first || hi > last) {
+    err = "thermal xscorr: the Fermi window lies outside the horizontal grid";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  std::vector<double> re(en.size());
+  for (size_t i = 0; i < en.size(); ++i) re[i] = en[i].real();
+  const size_t s_lo = search1(lo, re), s_hi = search1(hi, re);
+  const size_t i_lo = std::max<size_t>(s_lo > 0 ? s_lo - 1 : 0, 1), i_hi = std::min(s_hi, en.size());
+  std::vector<cd> ze, zv;
+  ze.reserve(i_lo + kSamples + en.size());
+  zv.reserve(ze.capacity());
+  for (size_t i = 0; i < i_lo; ++i) {
+    ze.push_back(en[i]);
+    zv.push_back(xmu[i]);
+  }
+  cd v;
+  for (int i = 0; i < kSamples; ++i) {
+    const double x = lo + i * de;
+    if (!interp1(x, re, xmu.data(), v)) {
+      err = "thermal xscorr: interpolation outside the horizontal grid";
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+    ze.push_back(cd(x, en[0].imag()));
+    zv.push_back(v);
+  }
+  if (!interp1(hi, re, xmu.data(), v)) {
+    err = "thermal xscorr: interpolation outside the horizontal grid";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  ze.push_back(cd(hi, en[0].imag()));
+  zv.push_back(v);
+  for (size_t i = i_hi; i < en.size(); ++i) {
+    ze.push_back(en[i]);
+    zv.push_back(xmu[i]);
+  }
+  const cd e1(w, xloss), e2(w, -xloss), two_pi_i(0.0, 2.0 * kPi);
+  cd sum(0.0, 0.0);
+  for (size_t q = 0; q + 1 < ze.size(); ++q) {
+    const cd z1 = ze[q], z2 = ze[q + 1], k1 = zv[q] - xmu0, k2 = zv[q + 1] - xmu0, dz = z2 - z1;
+    double f1 = fermi_fn(z1.real(), t, ef), f2 = fermi_fn(z2.real(), t, ef);
+    if (ispec != 2) {
+      f1 = 1.0 - f1;
+      f2 = 1.0 - f2;
+    }
+    if (std::abs(dz) == 0.0) {
+      err = "thermal xscorr: the resampled contour repeats a point";
+      return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+    }
+    if (z1.real() > lo && z1.real() < hi) {
+      sum += 0.5 * dz * (k1 * f1 * cauchy(z1, w, xloss) + k2 * f2 * cauchy(z2, w, xloss));
+    } else {
+      cd seg(0.0, 0.0);
+      if (std::abs(z1 - e1) > kEps4 && std::abs(z2 - e1) > kEps4)
+        seg = -std::log((z2 - e1) / (z1 - e1)) * (k1 * f1 * (z2 - e1) + k2 * f2 * (e1 - z1));
+      seg += std::log((z2 - e2) / (z1 - e2)) * (k1 * f1 * (z2 - e2) + k2 * f2 * (e2 - z1));
+      sum -= seg / dz / two_pi_i;
+    }
+  }
+  out = sum;
+  return finite(out) ? REFEFF_FMS_OK : REFEFF_FMS_ERR_NONFINITE_INPUT;
+}
+
+int thermal_xscorr(int ispec, const cd* energy, size_t ne, size_t ne1, const cd* xsec, const double* bg,
+                   const cd* chia, double vrcorr, double temp_ev, std::vector<cd>& cchi, std::string& err) {
+  constexpr size_t kAux = 10;
+  if (ne1 < 2) {
+    err = "thermal xscorr needs at least two horizontal points";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  const size_t pole_start = 2 * ne1 + kAux;
+  if (ne < pole_start + 1) {
+    err = "thermal xscorr needs 2 ne1 + 11 xsect.dat rows";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  if (!(std::isfinite(temp_ev) && temp_ev > 0.0) || !std::isfinite(vrcorr)) {
+    err = "thermal xscorr needs a positive finite temperature and a finite real correction";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  std::vector<cd> xmu(ne);
+  for (size_t r = 0; r < ne; ++r) {
+    if (!finite(energy[r]) || !finite(xsec[r]) || !std::isfinite(bg[r]) || !finite(chia[r])) {
+      err = "thermal xscorr input row " + std::to_string(r) + " is not finite";
+      return REFEFF_FMS_ERR_NONFINITE_INPUT;
+    }
+    xmu[r] = xsec[r] + chia[r] * bg[r];
+  }
+  const double xloss = energy[ne1].imag();
+  if (!(xloss > 0.0)) {
+    err = "thermal xscorr needs a positive loss width (Im of the first loss row)";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  const bool shifted = std::fabs(vrcorr) > kEps4;
+  double ef = energy[ne - 1].real();
+  if (shifted) ef -= vrcorr;
+  const double t = temp_ev / kHartreeEv;
+  const std::vector<cd> hor_e(energy, energy + ne1), hor_x(xmu.begin(), xmu.begin() + ne1);
+  cchi.assign(ne1, cd(0.0, 0.0));
+  for (size_t r = 0; r < ne1; ++r) {
+    const double w = energy[r].real();
+    const cd xmu0 = xmu[ne1 + r];
+    cd conv = xmu0 * fermi_lorentz(w, t, ef, xloss);
+    if (ispec != 2) conv = xmu0 - conv;
+    cd res(0.0, 0.0);
+    for (size_t p = pole_start; p < ne - 1; ++p) {
+      cd z = energy[p];
+      if (shifted) z -= cd(vrcorr, 0.0);
+      const cd d = z - cd(w, 0.0);
+      res += (xmu[p] - xmu0) * xloss / (d * d + cd(xloss * xloss, 0.0));
+    }
+    res *= cd(0.0, -2.0 * t);
+    if (ispec != 2) res = -res;
+    cd contour;
+    const int rc = thermal_contour(hor_e, hor_x, ef, t, xmu0, xloss, w, ispec, contour, err);
+    if (rc) return rc;
+    cchi[r] = conv + contour + res - hor_x[r];
+    if (!finite(cchi[r])) {
+      err = "thermal xscorr row " + std::to_string(r) + " is not finite";
+      return REFEFF_FMS_ERR_NONFINITE_INPUT;
+    }
+  }
+  return REFEFF_FMS_OK;
+}
+
+// ff2x_xscorr (ff2x.rs:4437-4641): the thermal form above zero temperature.
+int xscorr_at(int ispec, const cd* energy, size_t ne, size_t ne1, size_t fermi, const cd* xsec, const double* bg,
+              const cd* chia, double vrcorr, double temp_ev, std::vector<cd>& cchi, std::string& err) {
+  if (!(std::isfinite(temp_ev) && temp_ev >= 0.0)) {
+    err = "xscorr electronic temperature must be finite and non-negative";
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  }
+  if (temp_ev > 0.0) return thermal_xscorr(ispec, energy, ne, ne1, xsec, bg, chia, vrcorr, temp_ev, cchi, err);
+  return xscorr(ispec, energy, ne, ne1, fermi, xsec, bg, chia, vrcorr, cchi, err);
+}
+
 }  // namespace
+
+extern "C" int refeff_ff2x_xscorr(int ne, int ne1, int fermi_index, int ispec, const refeff_complex128* energy,
+                                  const refeff_complex128* cross_section, const double* background,
+                                  const refeff_complex128* path_chi, double real_correction,
+                                  double electronic_temperature_ev, refeff_complex128* cchi_out) {
+  if (ne <= 0 || ne1 <= 0 || ne1 > ne || fermi_index < 0 || fermi_index >= ne1 || !energy || !cross_section ||
+      !background || !path_chi || !cchi_out)
+    return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  const size_t n = size_t(ne);
+  std::vector<cd> e(n), xsec(n), chia(n), out;
+  for (size_t r = 0; r < n; ++r) {
+    e[r] = cd(energy[r].re, energy[r].im);
+    xsec[r] = cd(cross_section[r].re, cross_section[r].im);
+    chia[r] = cd(path_chi[r].re, path_chi[r].im);
+  }
+  std::string err;
+  const int rc = xscorr_at(ispec, e.data(), n, size_t(ne1), size_t(fermi_index), xsec.data(), background, chia.data(),
+                           real_correction, electronic_temperature_ev, out, err);
+  if (rc) return rc;
+  for (int r = 0; r < ne1; ++r) cchi_out[r] = {out[size_t(r)].real(), out[size_t(r)].imag()};
+  return REFEFF_FMS_OK;
+}
 
 extern "C" int refeff_ff2x_lorentz_convolve(int n, const double* omega, const refeff_complex128* spectrum, double width,
                                             refeff_complex128* out) {
@@ -258,12 +504,12 @@ extern "C" int refeff_ff2x_lorentz_convolve(int n, const double* omega, const re
   return REFEFF_FMS_OK;
 }
 
-extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
-                                    const refeff_complex128* energy, const double* omega,
-                                    const refeff_complex128* cross_section, const double* background,
-                                    const refeff_complex128* trace, double s02, double real_correction,
-                                    double imaginary_correction, double fermi_photon_energy, double* mu, double* mu0,
-                                    double* chi) {
+extern "C" int refeff_ff2x_xanes_mu_thermal(int ne, int ne1, int fermi_index, int ispec, int absolu,
+                                            int include_atomic, const refeff_complex128* energy, const double* omega,
+                                            const refeff_complex128* cross_section, const double* background,
+                                            const refeff_complex128* trace, double s02, double real_correction,
+                                            double imaginary_correction, double fermi_photon_energy,
+                                            double electronic_temperature_ev, double* mu, double* mu0, double* chi) {
   const int is = ispec < 0 ? -ispec : ispec;  // ff2x_xmu_effective_ispec (ff2x.rs:1496-1502)
   if (ne <= 0 || ne1 <= 0 || ne1 >= ne || fermi_index < 0 || fermi_index >= ne1 || is < 1 || is > 2 || !energy ||
       !omega || !cross_section || !background || !trace || !std::isfinite(s02))
@@ -277,11 +523,11 @@ extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec,
   }
   std::vector<cd> total_corr, atomic_corr;
   std::string err;
-  int rc = xscorr(is, e.data(), n, n1, size_t(fermi_index), xsec.data(), background, chia.data(), real_correction,
-                  total_corr, err);
+  int rc = xscorr_at(is, e.data(), n, n1, size_t(fermi_index), xsec.data(), background, chia.data(),
+                     real_correction, electronic_temperature_ev, total_corr, err);
   if (rc) return rc;
-  rc = xscorr(is, e.data(), n, n1, size_t(fermi_index), xsec.data(), background, zero.data(), real_correction,
-              atomic_corr, err);
+  rc = xscorr_at(is, e.data(), n, n1, size_t(fermi_index), xsec.data(), background, zero.data(), real_correction,
+                 electronic_temperature_ev, atomic_corr, err);
   if (rc) return rc;
   double norm = 1.0;
   if (absolu != 1) {
@@ -313,6 +559,17 @@ extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec,
     if (mu) mu[r] = m0 + c;
   }
   return REFEFF_FMS_OK;
+}
+
+extern "C" int refeff_ff2x_xanes_mu(int ne, int ne1, int fermi_index, int ispec, int absolu, int include_atomic,
+                                    const refeff_complex128* energy, const double* omega,
+                                    const refeff_complex128* cross_section, const double* background,
+                                    const refeff_complex128* trace, double s02, double real_correction,
+                                    double imaginary_correction, double fermi_photon_energy, double* mu, double* mu0,
+                                    double* chi) {
+  return refeff_ff2x_xanes_mu_thermal(ne, ne1, fermi_index, ispec, absolu, include_atomic, energy, omega,
+                                      cross_section, background, trace, s02, real_correction, imaginary_correction,
+                                      fermi_photon_energy, 0.0, mu, mu0, chi);
 }
 
 // ff2x.rs:3388-3397: with sig_gk > 1e-4 the fine structure of every output row

@@ -109,6 +109,9 @@ def load(build_if_missing: bool = True):
         "refeff_fms_reciprocal_core_hole": ([_i, _p, _i, _i, _p, _p], _i),
         "refeff_ff2x_xanes_mu": ([_i, _i, _i, _i, _i, _i, _p, _p, _p, _p, _p, C.c_double, C.c_double, C.c_double,
                                   C.c_double, _p, _p, _p], _i),
+        "refeff_ff2x_xanes_mu_thermal": ([_i, _i, _i, _i, _i, _i, _p, _p, _p, _p, _p, C.c_double, C.c_double,
+                                          C.c_double, C.c_double, C.c_double, _p, _p, _p], _i),
+        "refeff_ff2x_xscorr": ([_i, _i, _i, _i, _p, _p, _p, _p, C.c_double, C.c_double, _p], _i),
         "refeff_ff2x_lorentz_convolve": ([_i, _p, _p, C.c_double, _p], _i),
         "refeff_ff2x_debye_factor": ([_i, _p, C.c_double, _p, _p, _p], _i),
         "refeff_fms_write_gg_diag_bin": ([C.c_char_p, _i, _i, _i, _p], _i),
@@ -603,10 +606,11 @@ def write_gg_dat(path, sections) -> None:
 
 def ff2x_xanes_mu(*, energy, ne1, fermi_index, omega, cross_section, background, trace, s02=1.0, ispec=1,
                   absolu=0, include_atomic=True, real_correction=0.0, imaginary_correction=0.0,
-                  fermi_photon_energy=0.0):
-    """FF2X XANES mu(E) from the MKGTR trace (crates/refeff-engine/src/ff2x.rs:3186-3262, 3309-3399, 4437-4641):
+                  fermi_photon_energy=0.0, electronic_temperature=0.0):
+    """FF2X XANES mu(E) from the MKGTR trace (crates/refeff-engine/src/ff2x.rs:3186-3262, 3309-3399, 4437-5050):
     returns (mu, mu0, chi) over the ne1 main rows.  energy, cross_section, trace: ne complex; background: ne
-    reals; omega: ne1 photon energies; all energies in Hartree.  Host only."""
+    reals; omega: ne1 photon energies; all energies in Hartree; electronic_temperature in eV (> 0: the thermal
+    xscorr).  Host only."""
     lib = load()
     e = np.ascontiguousarray(energy, dtype=np.complex128)
     ne = e.shape[0]
@@ -617,13 +621,35 @@ def ff2x_xanes_mu(*, energy, ne1, fermi_index, omega, cross_section, background,
     if om.shape[0] < ne1 or xs.shape[0] != ne or bg.shape[0] != ne or tr.shape[0] != ne:
         raise FmsError(1, "ff2x_xanes_mu: array lengths do not match ne / ne1")
     mu, mu0, chi = (np.zeros(int(ne1)) for _ in range(3))
-    rc = lib.refeff_ff2x_xanes_mu(ne, int(ne1), int(fermi_index), int(ispec), int(absolu), int(bool(include_atomic)),
-                                  _ptr(e), _ptr(om), _ptr(xs), _ptr(bg), _ptr(tr), float(s02), float(real_correction),
-                                  float(imaginary_correction), float(fermi_photon_energy), _ptr(mu), _ptr(mu0),
-                                  _ptr(chi))
+    rc = lib.refeff_ff2x_xanes_mu_thermal(ne, int(ne1), int(fermi_index), int(ispec), int(absolu),
+                                          int(bool(include_atomic)), _ptr(e), _ptr(om), _ptr(xs), _ptr(bg), _ptr(tr),
+                                          float(s02), float(real_correction), float(imaginary_correction),
+                                          float(fermi_photon_energy), float(electronic_temperature), _ptr(mu),
+                                          _ptr(mu0), _ptr(chi))
     if rc:
         raise FmsError(rc, "ff2x_xanes_mu")
     return mu, mu0, chi
+
+
+def ff2x_xscorr(*, energy, ne1, fermi_index, cross_section, background, path_chi, ispec=1, real_correction=0.0,
+                electronic_temperature=0.0):
+    """FF2X xscorr (crates/refeff-engine/src/ff2x.rs:4437-5050): the correction cchi (ne1 complex) of
+    xmu = cross_section + path_chi * background over the xsect.dat rows; the thermal form when
+    electronic_temperature (eV) > 0.  Host only."""
+    lib = load()
+    e = np.ascontiguousarray(energy, dtype=np.complex128)
+    ne = e.shape[0]
+    xs = np.ascontiguousarray(cross_section, dtype=np.complex128)
+    bg = np.ascontiguousarray(background, dtype=np.float64)
+    pc = np.ascontiguousarray(path_chi, dtype=np.complex128)
+    if xs.shape[0] != ne or bg.shape[0] != ne or pc.shape[0] != ne:
+        raise FmsError(1, "ff2x_xscorr: array lengths do not match the energy rows")
+    out = np.zeros(int(ne1), np.complex128)
+    rc = lib.refeff_ff2x_xscorr(ne, int(ne1), int(fermi_index), int(ispec), _ptr(e), _ptr(xs), _ptr(bg), _ptr(pc),
+                                float(real_correction), float(electronic_temperature), _ptr(out))
+    if rc:
+        raise FmsError(rc, "ff2x_xscorr")
+    return out
 
 
 def reciprocal_integrate(ctx: Context, structure_factors, weights, t_matrix, form=FORM_FP64_LU,

@@ -22,6 +22,7 @@ GG_BIN = "crates/refeff-io/src/rhorrp_gg_bin.rs"
 XSCORR = "crates/refeff-core/src/xscorr.rs"
 RECIP = "crates/refeff-core/src/fms/tests/reciprocal.rs"
 CONV = "crates/refeff-core/src/convolution/tests.rs"
+FF2X_TESTS = "crates/refeff-engine/src/ff2x/tests.rs"
 
 
 def c(re_, im_, src):
@@ -269,6 +270,25 @@ KATS = {
         {"args": r([0.08, 0.0], f"{XSCORR}:154"), "want": r(0.5, f"{XSCORR}:154")},
         {"args": r([0.08, 0.22], f"{XSCORR}:155"), "want": r(0.8889827415450001, f"{XSCORR}:155")},
     ],
+    # FF2X thermal xscorr on the constant-cross-section fixture (17 xsect.dat rows, ne1 = 3, cross section 10i,
+    # background 1, no trace), electronic temperature 0.5 eV: Im(xsec + cchi) of the three horizontal rows.
+    "thermal_xscorr": {
+        "energy": [c(0.9, 0.2, f"{FF2X_TESTS}:5199"), c(1.0, 0.2, f"{FF2X_TESTS}:5200"),
+                   c(1.1, 0.2, f"{FF2X_TESTS}:5201"), c(0.9, 0.1, f"{FF2X_TESTS}:5202"),
+                   c(1.0, 0.1, f"{FF2X_TESTS}:5203"), c(1.1, 0.1, f"{FF2X_TESTS}:5204"),
+                   c(1.0, 0.01, f"{FF2X_TESTS}:5205"), c(1.0, 0.02, f"{FF2X_TESTS}:5206"),
+                   c(1.0, 0.03, f"{FF2X_TESTS}:5207"), c(1.0, 0.04, f"{FF2X_TESTS}:5208"),
+                   c(1.0, 0.05, f"{FF2X_TESTS}:5209"), c(1.0, 0.06, f"{FF2X_TESTS}:5210"),
+                   c(1.0, 0.07, f"{FF2X_TESTS}:5211"), c(1.0, 0.08, f"{FF2X_TESTS}:5212"),
+                   c(1.0, 0.09, f"{FF2X_TESTS}:5213"), c(1.0, 0.10, f"{FF2X_TESTS}:5214"),
+                   c(1.0, 0.0, f"{FF2X_TESTS}:5215")],
+        "ne1": r(3, f"{FF2X_TESTS}:5228"),
+        "cross_section": c(0.0, 10.0, f"{FF2X_TESTS}:5235"),
+        "background": r(1.0, f"{FF2X_TESTS}:5234"),
+        "temperature_ev": r(0.5, f"{FF2X_TESTS}:1166"),
+        "corrected_im": r([2.585850230196276, 5.000003995527989, 7.414157694791554], f"{FF2X_TESTS}:1170-1173"),
+        "tolerance": r(1.0e-11, f"{FF2X_TESTS}:1176"),
+    },
     # FEFF conv1 / conv on the convolution fixture (omega, spectrum), width 0.2, tolerance 1e-12.
     "lorentz_conv": {
         "omega": r([-2.0, -0.5, 0.25, 1.5, 3.0], f"{CONV}:13"),

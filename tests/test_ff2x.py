@@ -164,3 +164,76 @@ def test_debye_factor_matches_oracle(sig_gk):
         assert np.array_equal(c, chi)
     else:
         assert abs(c[-1]) < abs(chi[-1])
+
+
+# ---------------------------------------------------------------------------
+# thermal xscorr (electronic temperature > 0)
+# ---------------------------------------------------------------------------
+
+def _thermal_fixture():
+    """ff2x/tests.rs:5197-5238 through the audited known-answer file: 17 xsect.dat rows (3 horizontal at Im 0.2,
+    3 loss rows at Im 0.1, 10 auxiliary / pole rows, the Fermi row (1.0, 0)), cross section 10i, background 1."""
+    k = KAT["thermal_xscorr"]
+    energy = [complex(*v["value"]) for v in k["energy"]]
+    ne = len(energy)
+    return dict(energy=energy, ne1=k["ne1"]["value"], xsec=[complex(*k["cross_section"]["value"])] * ne,
+                bg=[k["background"]["value"]] * ne, temp=k["temperature_ev"]["value"],
+                want=k["corrected_im"]["value"], tol=k["tolerance"]["value"])
+
+
+def test_oracle_thermal_xscorr_known_answer():
+    """tests.rs:1152-1178: at 0.5 eV the thermal xscorr of the constant cross section gives Im(xsec + cchi) =
+    2.5858..., 5.0000..., 7.4141... on the three horizontal rows, and cchi = i (those - 10)."""
+    f = _thermal_fixture()
+    ne = len(f["energy"])
+    cchi = fo.thermal_xscorr(1, f["energy"], f["ne1"], f["xsec"], f["bg"], [0j] * ne, 0.0, f["temp"])
+    for row, want in enumerate(f["want"]):
+        assert abs(cchi[row] - complex(0.0, want - 10.0)) <= f["tol"]
+        assert abs((f["xsec"][row] + cchi[row]).imag - want) <= f["tol"]
+
+
+def test_product_thermal_xscorr_known_answer():
+    f = _thermal_fixture()
+    ne = len(f["energy"])
+    cchi = fms.ff2x_xscorr(energy=f["energy"], ne1=f["ne1"], fermi_index=1, cross_section=f["xsec"],
+                           background=f["bg"], path_chi=np.zeros(ne), electronic_temperature=f["temp"])
+    for row, want in enumerate(f["want"]):
+        assert abs(cchi[row] - complex(0.0, want - 10.0)) <= f["tol"]
+    # through the XANES step: mu0 = the corrected atomic cross section, no fine structure
+    mu, mu0, chi = fms.ff2x_xanes_mu(energy=f["energy"], ne1=f["ne1"], fermi_index=1, omega=[0.9, 1.0, 1.1],
+                                     cross_section=f["xsec"], background=f["bg"], trace=np.zeros(ne), absolu=1,
+                                     electronic_temperature=f["temp"])
+    assert np.abs(mu0 - np.array(f["want"])).max() <= f["tol"] and np.abs(chi).max() <= 1e-12
+
+
+@pytest.mark.parametrize("ispec,vrcorr,temp", [(1, 0.0, 0.5), (2, 0.0, 0.3), (1, 0.01, 0.4), (1, 0.0, 1.0)])
+def test_product_thermal_xscorr_matches_oracle(ispec, vrcorr, temp):
+    """A non-constant xmu (seeded cross section and trace on a 7-point horizontal grid): the product's C++ and
+    the oracle's restatement agree (the contour, residue and Fermi-Lorentz terms all non-trivial)."""
+    rng = np.random.default_rng(int(temp * 10) + ispec)
+    ne1 = 7
+    hor = [complex(0.7 + 0.1 * i, 0.15) for i in range(ne1)]
+    loss = [complex(0.7 + 0.1 * i, 0.08) for i in range(ne1)]
+    aux = [complex(1.0, 0.01 * (i + 1)) for i in range(10)]
+    poles = [complex(1.0 + 0.003 * i, 0.02 * (i + 1)) for i in range(4)]
+    energy = hor + loss + aux + poles + [complex(1.0, 0.0)]
+    ne = len(energy)
+    xsec = list(rng.normal(size=ne) * 0.3 + 1j * (8.0 + rng.normal(size=ne)))
+    bg = list(1.0 + 0.1 * rng.random(ne))
+    chia = list(rng.normal(size=ne) * 0.2 + 1j * rng.normal(size=ne) * 0.2)
+    want = fo.thermal_xscorr(ispec, energy, ne1, xsec, bg, chia, vrcorr, temp)
+    got = fms.ff2x_xscorr(energy=energy, ne1=ne1, fermi_index=3, cross_section=xsec, background=bg, path_chi=chia,
+                          ispec=ispec, real_correction=vrcorr, electronic_temperature=temp)
+    scale = max(abs(w) for w in want)
+    assert max(abs(g - w) for g, w in zip(got, want)) <= 1e-10 * scale
+
+
+def test_thermal_xscorr_rejects_short_layouts_and_bad_temperatures():
+    f = _thermal_fixture()
+    ne = len(f["energy"])
+    with pytest.raises(fms.FmsError):  # 2 ne1 + 11 rows needed
+        fms.ff2x_xscorr(energy=f["energy"][:12] + [1.0 + 0j], ne1=3, fermi_index=1, cross_section=f["xsec"][:13],
+                        background=f["bg"][:13], path_chi=np.zeros(13), electronic_temperature=0.5)
+    with pytest.raises(fms.FmsError):
+        fms.ff2x_xscorr(energy=f["energy"], ne1=3, fermi_index=1, cross_section=f["xsec"], background=f["bg"],
+                        path_chi=np.zeros(ne), electronic_temperature=-0.1)
