@@ -147,14 +147,15 @@ __global__ void bicg_p_kernel(View w, const float2* __restrict__ D, const int* s
 }
 
 // Y = A X for the FP32 system matrices: 128 rows x 16 columns per CTA, each
-// thread 4 rows x 4 columns, A streamed through shared memory in 32-column
-// slabs by a two-stage cp.async pipeline (each A entry is read from HBM once
-// per product; rows past n and columns past the slice are zero-filled by the
-// copies).  The columns of A are split into w.nsplit slices of kchunk
-// (blockIdx.z = column group + groups * slice), so that even one running
-// matrix spreads over the SMs: slice 0 writes Y, slice s > 0 its partial
-// product, and the next dot kernel sums them in slice order.
-constexpr int kMvRows = 128, kMvCols = 16, kMvK = 32, kMvThreads = 128, kMvStages = 2, kMvSliceCols = 512;
+// thread 4 rows (rg + 32 i) x 4 adjacent columns (read as two 16-byte
+// shared loads), A streamed through shared memory in 16-column slabs by a
+// three-stage cp.async pipeline (each A entry is read from HBM once per
+// product; rows past n and columns past the slice are zero-filled by the
+// copies; 55 KB per CTA, four CTAs per SM).  The columns of A are split into
+// w.nsplit slices of kchunk (blockIdx.z = column group + groups * slice), so
+// that even one running matrix spreads over the SMs: slice 0 writes Y, slice
+// s > 0 its partial product, and the next dot kernel sums them in slice order.
+constexpr int kMvRows = 128, kMvCols = 16, kMvK = 16, kMvThreads = 128, kMvStages = 3, kMvSliceCols = 512;
 constexpr size_t kMvSmem = size_t(kMvStages) * kMvK * (kMvRows + kMvCols) * sizeof(float2);
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, int bytes) {
@@ -176,28 +177,33 @@ __global__ void __launch_bounds__(kMvThreads) bicg_matvec_kernel(View w, const f
   const int b = w.matrix();
   if (b < 0 || (skip && skip[b]) || w.done[b]) return;
   extern __shared__ __align__(16) float2 mv_smem[];
-  float2* As = mv_smem;                                   // [stage][kMvK][kMvRows]
+  float2* As = mv_smem;                                       // [stage][kMvK][kMvRows]
   float2* Xs = mv_smem + size_t(kMvStages) * kMvK * kMvRows;  // [stage][kMvK][kMvCols]
   const int slice = blockIdx.z / groups;
   const int n = w.n, r0 = blockIdx.x * kMvRows, c0 = (blockIdx.z % groups) * kMvCols;
   const int kbeg = slice * kchunk, kend = min(n, kbeg + kchunk);
+  const int slabs = (kend - kbeg + kMvK - 1) / kMvK;
   const float2* A = M32 + size_t(b) * stride;
   const int tid = threadIdx.x, rg = tid & 31, cq = tid >> 5;
-  // one slab: kMvK columns of A (128 rows as 16-byte row pairs) and of X
-  auto load = [&](int stage, int k0) {
-    float2* as = As + size_t(stage) * kMvK * kMvRows;
-    float2* xs = Xs + size_t(stage) * kMvK * kMvCols;
-    for (int idx = tid; idx < kMvK * (kMvRows / 2); idx += kMvThreads) {
-      const int rr = (idx % (kMvRows / 2)) * 2, kk = idx / (kMvRows / 2), row = r0 + rr;
-      const bool in = k0 + kk < kend && row < n;
-      const int bytes = in ? (row + 1 < n ? 16 : 8) : 0;
-      cp_async16(as + size_t(kk) * kMvRows + rr, in ? A + size_t(row) + size_t(w.lda) * (k0 + kk) : A, bytes);
-    }
-    for (int idx = tid; idx < kMvK * kMvCols; idx += kMvThreads) {
-      const int kk = idx % kMvK, cc = idx / kMvK;
-      const bool in = k0 + kk < kend && c0 + cc < w.m;
-      const float2* xsrc = in ? w.v(src, b, c0 + cc) + (k0 + kk) : A;
-      cp_async8(xs + size_t(kk) * kMvCols + cc, xsrc, in ? 8 : 0);
+  // one slab: kMvK columns of A (128 rows as 16-byte row pairs) and of X; a
+  // slab past the slice's end commits an empty group (uniform group counts)
+  auto load = [&](int slab) {
+    if (slab < slabs) {
+      const int k0 = kbeg + slab * kMvK, stage = slab % kMvStages;
+      float2* as = As + size_t(stage) * kMvK * kMvRows;
+      float2* xs = Xs + size_t(stage) * kMvK * kMvCols;
+      for (int idx = tid; idx < kMvK * (kMvRows / 2); idx += kMvThreads) {
+        const int rr = (idx % (kMvRows / 2)) * 2, kk = idx / (kMvRows / 2), row = r0 + rr;
+        const bool in = k0 + kk < kend && row < n;
+        const int bytes = in ? (row + 1 < n ? 16 : 8) : 0;
+        cp_async16(as + size_t(kk) * kMvRows + rr, in ? A + size_t(row) + size_t(w.lda) * (k0 + kk) : A, bytes);
+      }
+      for (int idx = tid; idx < kMvK * kMvCols; idx += kMvThreads) {
+        const int kk = idx % kMvK, cc = idx / kMvK;
+        const bool in = k0 + kk < kend && c0 + cc < w.m;
+        const float2* xsrc = in ? w.v(src, b, c0 + cc) + (k0 + kk) : A;
+        cp_async8(xs + size_t(kk) * kMvCols + cc, xsrc, in ? 8 : 0);
+      }
     }
     cp_async_commit();
   };
@@ -206,35 +212,35 @@ __global__ void __launch_bounds__(kMvThreads) bicg_matvec_kernel(View w, const f
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
-  int stage = 0;
-  if (kbeg < kend) load(0, kbeg);
-  for (int k0 = kbeg; k0 < kend; k0 += kMvK, stage ^= 1) {
-    if (k0 + kMvK < kend) {
-      load(stage ^ 1, k0 + kMvK);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
-    __syncthreads();
+#pragma unroll
+  for (int sl = 0; sl < kMvStages - 1; ++sl) load(sl);
+  for (int sl = 0; sl < slabs; ++sl) {
+    cp_async_wait<kMvStages - 2>();  // slab sl has landed (this thread's copies)
+    __syncthreads();                 // ... everyone's; and slab sl - 1's stage is free again
+    load(sl + kMvStages - 1);
+    const int stage = sl % kMvStages;
     const float2* as = As + size_t(stage) * kMvK * kMvRows;
-    const float2* xs = Xs + size_t(stage) * kMvK * kMvCols;
-#pragma unroll 8
+    const float4* xs = reinterpret_cast<const float4*>(Xs + size_t(stage) * kMvK * kMvCols);
+#pragma unroll
     for (int kk = 0; kk < kMvK; ++kk) {
       float2 a[4], x[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = as[kk * kMvRows + rg + 32 * i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) x[j] = xs[kk * kMvCols + cq + 4 * j];
+      const float4 x01 = xs[(kk * kMvCols + 4 * cq) / 2], x23 = xs[(kk * kMvCols + 4 * cq) / 2 + 1];
+      x[0] = make_float2(x01.x, x01.y);
+      x[1] = make_float2(x01.z, x01.w);
+      x[2] = make_float2(x23.x, x23.y);
+      x[3] = make_float2(x23.z, x23.w);
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], x[j]);
     }
-    __syncthreads();  // the next iteration's copy overwrites this stage
   }
+  cp_async_wait<0>();  // no copy outlives the CTA (the trailing groups are empty)
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const int c = c0 + cq + 4 * j;
+    const int c = c0 + 4 * cq + j;
     if (c >= w.m) continue;
     float2* y = slice == 0 ? w.v(dst, b, c) : w.pv(slice, b, c);
 #pragma unroll
@@ -496,8 +502,8 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
                                                int(kMvSmem));
     if (e != cudaSuccess) return e;
   }
-  // Slices of A's columns: 512 columns each (more for n > 8192, at most
-  // kBicgMaxSplit slices), so that the last running matrices still fill the
+  // Slices of A's columns: kMvSliceCols columns each (more for large n, at
+  // most kBicgMaxSplit slices), so that the last running matrices still fill the
   // GPU with product CTAs.  The slicing depends on n alone: a matrix's
   // arithmetic does not depend on which others share its batch.
   int chunk = lay.n, nsplit = 1;
