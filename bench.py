@@ -354,8 +354,12 @@ def config_batched(ctx, fms, wl, local):
     default = pts / float(np.median(each))
     chosen = pts / float(np.median(each_t))
     plain = pts / dt64
+    captures, replays = ctx.graph_stats()
     out.update({"chosen": {"value": chosen, "seconds_each": each_t, "autotune": tune,
-                           "note": "autotuned (sizes bucketed; inner panel width, block pairing, stream count)"},
+                           "note": "autotuned (sizes bucketed; inner panel width, block pairing, stream count); "
+                                   "a repeated call runs as one CUDA graph (captured on the first repeat, "
+                                   "replayed after that)"},
+                "one_graph": {"captures": captures, "replays": replays},
                 "chosen_default": {"value": default, "seconds_each": each},
                 "plain_fp64": {"value": plain, "seconds": dt64},
                 "chosen_over_plain": chosen / plain,

@@ -140,7 +140,16 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     memory has room for the second workspace; 0 runs one batch after another
  *     on the caller's stream.  Same results. */
 #define REFEFF_FMS_OPT_DUAL_STREAMS 6
+/*   REFEFF_FMS_OPT_MULTI_GRAPH: 1 (default) runs the device work of a
+ *     refeff_fms_real_space_spectrum_multi call that repeats the previous one
+ *     (same plans in the same order, energy counts, batch sizes and form; the
+ *     LU forms) as one CUDA graph: captured on the repeat, replayed by every
+ *     later repeat until a buffer of any plan is reallocated or freed, or an
+ *     option or plan setting changes; 0 keeps one launch sequence per plan. */
+#define REFEFF_FMS_OPT_MULTI_GRAPH 7
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
+/* How often the context captured and replayed the many-cluster graph. */
+int refeff_fms_context_graph_stats(const refeff_fms_context* ctx, long long* captures, long long* replays);
 
 /* ---- cluster preparation (host) -------------------------------------- */
 

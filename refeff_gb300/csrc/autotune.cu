@@ -237,7 +237,8 @@ extern "C" int refeff_fms_autotune_multi(refeff_fms_context* ctx, int n_plans, r
     sts[size_t(i)].resize(size_t(S));
   }
   // time of the many-cluster call over a subset of the plans: one warm call
-  // (graph capture for the batch shape), then the best of two
+  // (graph capture for the batch shape), then the best of two (the first
+  // repeat captures the call as one graph, the second replays it)
   auto timed = [&](const std::vector<int>& subset, double& seconds) -> int {
     std::vector<refeff_fms_plan*> pl;
     std::vector<refeff_fms_energy_points> pt;

@@ -37,6 +37,12 @@ using namespace rfx;
 
 namespace {
 std::atomic<unsigned long long> g_launches{0};
+// Bumped by every device (re)allocation and release of the solve's buffers
+// and by every option or plan setting a captured graph bakes in: the
+// many-cluster graph (which holds device pointers and kernel arguments of
+// several plans) is replayed only while it has not moved.
+std::atomic<unsigned long long> g_state_epoch{1};
+void bump_epoch() { g_state_epoch.fetch_add(1, std::memory_order_relaxed); }
 }
 
 void rfx::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
@@ -101,6 +107,16 @@ struct refeff_fms_context {
   int multi_streams = 4;     // REFEFF_FMS_OPT_MULTI_STREAMS
   int dual_streams = 1;      // REFEFF_FMS_OPT_DUAL_STREAMS
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
+  std::vector<cudaEvent_t> pool_join;  // one per pool stream: joins it back into a capture
+  cudaEvent_t fork_ev = nullptr;
+  // the many-cluster call's device work as one CUDA graph (REFEFF_FMS_OPT_MULTI_GRAPH): captured on
+  // the second call with the same plans, energy counts, batch sizes and form, replayed after that
+  // while g_state_epoch is unchanged
+  int multi_graph = 1;
+  std::vector<long long> mg_key, mg_seen;
+  unsigned long long mg_epoch = 0, mg_launches = 0, mg_seen_epoch = 0;
+  cudaGraphExec_t mg_exec = nullptr;
+  long long mg_captures = 0, mg_replays = 0;
   // the caller's handle plus one per live plan and model: the context is torn
   // down when the last of them is destroyed, in whatever order that happens
   std::atomic<int> refs{1};
@@ -115,7 +131,9 @@ cudaStream_t rfx::context_stream(const refeff_fms_context* ctx) { return ctx->st
 
 extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value) {
   if (!ctx) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  bump_epoch();
   switch (option) {
+    case REFEFF_FMS_OPT_MULTI_GRAPH: ctx->multi_graph = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_TENSOR_CORES: ctx->use_tensor_cores = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_DENSE_REFINEMENT:
       if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
@@ -162,7 +180,10 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      bump_epoch();
+    }
     p = nullptr;
     n = 0;
   }
@@ -172,6 +193,7 @@ struct DevBuf {
     if (count == 0) return cudaSuccess;
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
     if (e == cudaSuccess) n = count;
+    bump_epoch();
     return e;
   }
   cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
@@ -236,6 +258,9 @@ void rfx::context_release(refeff_fms_context* ctx) {
     cudaStreamSynchronize(q);
     cudaStreamDestroy(q);
   }
+  for (cudaEvent_t ev : ctx->pool_join) cudaEventDestroy(ev);
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->mg_exec) cudaGraphExecDestroy(ctx->mg_exec);
   delete ctx;
 }
 
@@ -428,6 +453,7 @@ struct Workspace {
   void drop_graphs() {
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     graphs.clear();
+    bump_epoch();
   }
   ~Workspace() { drop_graphs(); }
 };
@@ -731,6 +757,7 @@ extern "C" int refeff_fms_real_space_plan_create_full(refeff_fms_context* ctx, c
 
 extern "C" void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan) {
   if (!plan) return;
+  bump_epoch();
   refeff_fms_context* ctx = plan->ctx;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
@@ -740,6 +767,7 @@ extern "C" void refeff_fms_real_space_plan_destroy(refeff_fms_plan* plan) {
 
 extern "C" int refeff_fms_plan_set_profiling(refeff_fms_plan* plan, int enable) {
   if (!plan) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  bump_epoch();
   plan->profiling = enable != 0;
   for (double& v : plan->phase_ms) v = 0.0;
   return REFEFF_FMS_OK;
@@ -765,6 +793,7 @@ extern "C" int refeff_fms_plan_set_tuning(refeff_fms_plan* plan, int inner_width
   if (!plan || !(inner_width == 0 || inner_width == 1 || inner_width == 16 || inner_width == 32) || paired_blocks < -1 ||
       paired_blocks > 1)
     return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  bump_epoch();
   plan->tune.inner = inner_width;
   plan->tune.paired = paired_blocks;
   return REFEFF_FMS_OK;
@@ -779,6 +808,7 @@ extern "C" int refeff_fms_plan_get_tuning(const refeff_fms_plan* plan, int* inne
 
 extern "C" int refeff_fms_plan_set_batch(refeff_fms_plan* plan, int max_batch) {
   if (!plan || max_batch < 0) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  bump_epoch();
   plan->max_batch = max_batch;
   return REFEFF_FMS_OK;
 }
@@ -818,8 +848,8 @@ int want_pair128(const Workspace& ws) {
              ? 1 : 0;
 }
 
-int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32,
-                     const TunePrefs* tune = nullptr) {
+int ensure_workspace_impl(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32,
+                          const TunePrefs* tune) {
   const BatchLayout lay = make_layout(n, m);
   if (ws.tc_wait_polls != ctx->tc_wait_polls) {  // a kernel argument: captured graphs hold the old budget
     ws.drop_graphs();
@@ -882,6 +912,20 @@ int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int b
   }
   ws.pc32.pair128 = want_pair128(ws);
   return REFEFF_FMS_OK;
+}
+
+// A workspace whose (re)configuration failed part-way (an allocation) is left
+// unconfigured, so that the next call configures it again instead of running
+// on buffers sized for another shape.
+int ensure_workspace(refeff_fms_context* ctx, Workspace& ws, int n, int m, int batch, bool fp32,
+                     const TunePrefs* tune = nullptr) {
+  const int rc = ensure_workspace_impl(ctx, ws, n, m, batch, fp32, tune);
+  if (rc) {
+    ws.drop_graphs();
+    ws.batch = 0;
+    ws.lay.n = -1;
+  }
+  return rc;
 }
 
 LuWork lu_work(Workspace& ws, const PanelConfig& pc) {
@@ -1291,13 +1335,16 @@ cudaError_t copy_energy_results(refeff_fms_plan& p, Workspace& ws, int i, int e,
 // caller's stream and one of the plan's, forked and joined with events), so
 // that one batch's latency-bound phases (panels, sweeps) overlap the other's
 // arithmetic-bound ones (build, residual, tensor-core updates).
+// `batch` > 0 fixes the batch size (one stream); `direct` runs every batch
+// un-captured, for a caller that is itself capturing the stream.
 int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k, const double2* d_x, refeff_fms_form form,
-                          double2* d_gg, int* d_status, cudaStream_t s, bool allow_dual = true) {
+                          double2* d_gg, int* d_status, cudaStream_t s, bool allow_dual = true, int batch = 0,
+                          bool direct = false) {
   refeff_fms_context* ctx = p.ctx;
   const bool fp32 = form != REFEFF_FMS_FORM_FP64_LU;  // the BiCGSTAB form uses the refined form's buffers
   const bool bicg = form == REFEFF_FMS_FORM_BICGSTAB;
-  bool dual = allow_dual && ctx->dual_streams && !p.profiling && !bicg && E >= 8;
-  const int B = pick_batch(p, dual ? (E + 1) / 2 : E, fp32);
+  bool dual = allow_dual && ctx->dual_streams && !p.profiling && !bicg && E >= 8 && batch <= 0;
+  const int B = batch > 0 ? std::min(batch, E) : pick_batch(p, dual ? (E + 1) / 2 : E, fp32);
   const bool refined = fp32 && p.minv == 0;  // refinement statistics and the FP64 fallback
   const size_t xph = p.xph_per_energy();
   if (p.full) RF_CUDA(ctx, p.d_full_all.alloc(size_t(E) * p.full_per));
@@ -1406,7 +1453,7 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
       RF_CUDA(ctx, cudaMemcpyAsync(ws.x_stage.p, d_x + size_t(e0) * xph, size_t(nb) * xph * sizeof(double2),
                                    cudaMemcpyDeviceToDevice, q));
     }
-    if (nb == B && !p.profiling && !bicg) {  // the BiCGSTAB form polls the host: not capturable
+    if (nb == B && !p.profiling && !bicg && !direct) {  // the BiCGSTAB form polls the host: not capturable
       // a graph bakes in its batch size: key by (form, energies in the batch)
       const int key = int(form) * 65536 + nb;
       auto it = ws.graphs.find(key);
@@ -1587,8 +1634,10 @@ namespace {
 // Host-buffer spectrum in two halves, so that several plans can have their
 // device work in flight at once: begin validates, uploads and enqueues on
 // stream s; end waits, runs the FP64 fallback, downloads and scatters.
-int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
-                   refeff_complex128* scattering_out, cudaStream_t s, bool allow_dual = true) {
+// First half of spectrum_begin: validation, the zeroed host table, the uploads
+// of k and the phase shifts, and the device result buffers.
+int spectrum_prepare(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
+                     refeff_complex128* scattering_out, cudaStream_t s) {
   refeff_fms_context* ctx = p.ctx;
   if (!points || !scattering_out) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
   const int E = points->n_energies;
@@ -1604,8 +1653,15 @@ int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, r
   RF_CUDA(ctx, p.d_x_all.upload(reinterpret_cast<const double2*>(points->phase_shifts), size_t(E) * xph, s));
   RF_CUDA(ctx, p.d_gg_all.alloc(size_t(E) * p.gg_per));
   RF_CUDA(ctx, p.d_status_all.alloc(size_t(E)));
-  return solve_device_energies_enqueue(p, E, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p, p.d_status_all.p, s,
-                                       allow_dual);
+  return REFEFF_FMS_OK;
+}
+
+int spectrum_begin(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
+                   refeff_complex128* scattering_out, cudaStream_t s, bool allow_dual = true, int batch = 0) {
+  const int rc = spectrum_prepare(p, points, form, scattering_out, s);
+  if (rc || points->n_energies == 0) return rc;
+  return solve_device_energies_enqueue(p, points->n_energies, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p,
+                                       p.d_status_all.p, s, allow_dual, batch);
 }
 
 int spectrum_end(refeff_fms_plan& p, const refeff_fms_energy_points* points, refeff_fms_form form,
@@ -1761,19 +1817,119 @@ extern "C" int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int
     stream_of[size_t(i)] = q;
     load[size_t(q)] += cost[size_t(i)];
   }
+  // Batch sizes are fixed here so that a repeated call has the same launch structure.
+  const bool fp32 = form != REFEFF_FMS_FORM_FP64_LU;
+  std::vector<int> batch_of(static_cast<size_t>(n_plans), 0);
+  bool graphable = ctx->multi_graph && form != REFEFF_FMS_FORM_BICGSTAB;
+  std::vector<long long> key{static_cast<long long>(form), static_cast<long long>(n_streams)};
+  for (int i : order) {
+    const int E = points[i].n_energies;
+    if (E > 0) batch_of[size_t(i)] = pick_batch(*plans[i], E, fp32);
+    if (plans[i]->profiling) graphable = false;
+    key.push_back(static_cast<long long>(reinterpret_cast<intptr_t>(plans[i])));
+    key.push_back(E);
+    key.push_back(batch_of[size_t(i)]);
+  }
+  cudaStream_t s0 = ctx->stream;
   int rc = REFEFF_FMS_OK;
   int begun = 0;
-  for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun) {
-    const int i = order[size_t(begun)];
-    // the many-cluster call already overlaps clusters on its stream pool: one stream per plan
-    rc = spectrum_begin(*plans[i], &points[i], form, scattering_out[i], ctx->pool[size_t(stream_of[size_t(i)])],
-                        false);
+  const bool replay = graphable && ctx->mg_exec && ctx->mg_key == key &&
+                      ctx->mg_epoch == g_state_epoch.load(std::memory_order_relaxed);
+  // capture only a repeat of the last call with nothing moved since (so the capture allocates nothing)
+  const bool capture = graphable && !replay && ctx->mg_seen == key &&
+                       ctx->mg_seen_epoch == g_state_epoch.load(std::memory_order_relaxed);
+  bool on_s0 = false;  // the device work runs on s0 (as the graph) rather than on the pool
+  if (replay || capture) {
+    // the uploads of every plan on s0, then the device work of all plans as one graph
+    for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun) {
+      const int i = order[size_t(begun)];
+      rc = spectrum_prepare(*plans[i], &points[i], form, scattering_out[i], s0);
+    }
+    if (rc == REFEFF_FMS_OK && capture) {
+      if (!ctx->fork_ev) RF_CUDA(ctx, cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming));
+      while (int(ctx->pool_join.size()) < n_streams) {
+        cudaEvent_t ev = nullptr;
+        RF_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        ctx->pool_join.push_back(ev);
+      }
+      if (ctx->mg_exec) {
+        cudaGraphExecDestroy(ctx->mg_exec);
+        ctx->mg_exec = nullptr;
+      }
+      const unsigned long long epoch = g_state_epoch.load(std::memory_order_relaxed);
+      bool ok = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      const unsigned long long before = g_launches.load();
+      if (ok) {
+        // fork the pool into the capture, put every plan's batches on its stream, join back
+        ok = cudaEventRecord(ctx->fork_ev, s0) == cudaSuccess;
+        for (int q = 0; q < n_streams && ok; ++q) ok = cudaStreamWaitEvent(ctx->pool[size_t(q)], ctx->fork_ev, 0) == cudaSuccess;
+        for (int j = 0; j < n_plans && ok; ++j) {
+          const int i = order[size_t(j)];
+          refeff_fms_plan& p = *plans[i];
+          if (points[i].n_energies == 0) continue;
+          ok = solve_device_energies_enqueue(p, points[i].n_energies, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p,
+                                             p.d_status_all.p, ctx->pool[size_t(stream_of[size_t(i)])], false,
+                                             batch_of[size_t(i)], true) == REFEFF_FMS_OK;
+        }
+        for (int q = 0; q < n_streams; ++q) {  // join every forked stream, also after a failure
+          cudaEventRecord(ctx->pool_join[size_t(q)], ctx->pool[size_t(q)]);
+          cudaStreamWaitEvent(s0, ctx->pool_join[size_t(q)], 0);
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(s0, &g);
+        ok = ok && ec == cudaSuccess && g != nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (ok) ok = cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+        // no buffer may have moved while capturing (an allocation inside the capture fails it anyway)
+        if (ok && g_state_epoch.load(std::memory_order_relaxed) == epoch) {
+          ctx->mg_exec = ge;
+          ctx->mg_key = key;
+          ctx->mg_epoch = epoch;
+          ctx->mg_launches = g_launches.load() - before;
+          ++ctx->mg_captures;
+        } else if (ge) {
+          cudaGraphExecDestroy(ge);
+        }
+      }
+      cudaGetLastError();  // a failed capture leaves no device work and no sticky error
+      g_launches.fetch_sub(g_launches.load() - before);  // captured launches count when they run
+      ctx->last_error.clear();
+    }
+    if (rc == REFEFF_FMS_OK && ctx->mg_exec && ctx->mg_key == key) {
+      RF_CUDA(ctx, cudaGraphLaunch(ctx->mg_exec, s0));
+      g_launches.fetch_add(ctx->mg_launches, std::memory_order_relaxed);
+      if (replay) ++ctx->mg_replays;
+      on_s0 = true;
+    } else if (rc == REFEFF_FMS_OK) {
+      // the capture did not take: the same batches one launch sequence per plan, on the pool after the uploads
+      RF_CUDA(ctx, cudaEventRecord(ctx->fork_ev, s0));
+      for (int q = 0; q < n_streams; ++q) RF_CUDA(ctx, cudaStreamWaitEvent(ctx->pool[size_t(q)], ctx->fork_ev, 0));
+      for (int j = 0; j < n_plans && rc == REFEFF_FMS_OK; ++j) {
+        const int i = order[size_t(j)];
+        refeff_fms_plan& p = *plans[i];
+        if (points[i].n_energies == 0) continue;
+        rc = solve_device_energies_enqueue(p, points[i].n_energies, p.d_k_all.p, p.d_x_all.p, form, p.d_gg_all.p,
+                                           p.d_status_all.p, ctx->pool[size_t(stream_of[size_t(i)])], false,
+                                           batch_of[size_t(i)]);
+      }
+      ctx->mg_seen.clear();
+    }
+  } else {
+    ctx->mg_seen.clear();
+    for (; begun < n_plans && rc == REFEFF_FMS_OK; ++begun) {
+      const int i = order[size_t(begun)];
+      // the many-cluster call already overlaps clusters on its stream pool: one stream per plan
+      rc = spectrum_begin(*plans[i], &points[i], form, scattering_out[i], ctx->pool[size_t(stream_of[size_t(i)])],
+                          false, batch_of[size_t(i)]);
+    }
   }
   int failed = 0, first_rc = rc;
   std::vector<refeff_fms_plan*> done_plans;
   for (int j = 0; j < begun; ++j) {
     const int i = order[size_t(j)];
-    cudaStream_t q = ctx->pool[size_t(stream_of[size_t(i)])];
+    cudaStream_t q = on_s0 ? s0 : ctx->pool[size_t(stream_of[size_t(i)])];
+    if (!on_s0 && (replay || capture)) RF_CUDA(ctx, cudaStreamSynchronize(s0));  // uploads were on s0
     int f = 0;
     const int r = rc == REFEFF_FMS_OK ? spectrum_end(*plans[i], &points[i], form, scattering_out[i],
                                                      status_out ? status_out[i] : nullptr, &f, q)
@@ -1782,8 +1938,19 @@ extern "C" int refeff_fms_real_space_spectrum_multi(refeff_fms_context* ctx, int
     if (first_rc == REFEFF_FMS_OK) first_rc = r;
     done_plans.push_back(plans[i]);
   }
+  if (graphable && !on_s0 && first_rc == REFEFF_FMS_OK) {  // a repeat of this call is captured
+    ctx->mg_seen = key;
+    ctx->mg_seen_epoch = g_state_epoch.load(std::memory_order_relaxed);
+  }
   fill_report(report, done_plans, form, failed, t0);
   return first_rc;
+}
+
+extern "C" int refeff_fms_context_graph_stats(const refeff_fms_context* ctx, long long* captures, long long* replays) {
+  if (!ctx) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  if (captures) *captures = ctx->mg_captures;
+  if (replays) *replays = ctx->mg_replays;
+  return REFEFF_FMS_OK;
 }
 
 extern "C" int refeff_fms_plan_refinement_stats(const refeff_fms_plan* plan, int n_energies, double* rel_residual,

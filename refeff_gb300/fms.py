@@ -160,6 +160,7 @@ def load(build_if_missing: bool = True):
         "refeff_fms_plan_set_tuning": ([_p, _i, _i], _i),
         "refeff_fms_plan_set_precond_window": ([_p, C.c_double, C.c_double], _i),
         "refeff_fms_plan_set_bicgstab_window": ([_p, C.c_double, C.c_double], _i),
+        "refeff_fms_context_graph_stats": ([_p, _p, _p], _i),
         "refeff_fms_plan_bicgstab_lu_energies": ([_p, _i, _p], _i),
         "refeff_fms_plan_get_tuning": ([_p, _p, _p], _i),
         "refeff_fms_write_geom_dat": ([C.c_char_p, C.c_char_p], _i),
@@ -213,10 +214,17 @@ class Context:
     OPT_PAIRED_BLOCKS = 4
     OPT_MULTI_STREAMS = 5
     OPT_DUAL_STREAMS = 6
+    OPT_MULTI_GRAPH = 7
 
     def set_option(self, option: int, value: int):
         """Context option (applies to plans / dense solves started afterwards)."""
         self.check(self._lib.refeff_fms_context_set_option(self.handle, int(option), int(value)))
+
+    def graph_stats(self):
+        """(captures, replays) of the many-cluster call's single graph."""
+        c, r = C.c_longlong(), C.c_longlong()
+        self.check(self._lib.refeff_fms_context_graph_stats(self.handle, C.byref(c), C.byref(r)))
+        return c.value, r.value
 
     def last_error(self) -> str:
         return self._lib.refeff_fms_last_error(self.handle).decode()

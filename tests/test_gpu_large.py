@@ -118,6 +118,43 @@ def test_config2_many_clusters_in_one_call(ctx):
                 assert rel_err(tables[i][e, :m, :m, 0], ref[e, :m, :m, 0]) < tol, (i, e)
 
 
+def test_repeated_many_cluster_call_runs_as_one_graph():
+    """A repeated many-cluster call with the same plans, energies and form is captured once as one CUDA graph and
+    replayed: every call gives bit-identical tables (the graph holds the same kernels as the per-plan launch
+    sequences), a plan setting between calls retires the graph (no replay with stale arguments), and the option
+    switches it off."""
+    ctx = fms.Context(0)
+    cases = wl.config2()[::4]
+    sel = np.array([0, 75, 149])
+    plans = [fms.fms_real_space_plan(ctx, c.positions, c.potentials, c.lmaxph) for c, _ in cases]
+    ks = [g.wave_numbers[sel] for _, g in cases]
+    phs = [g.phase_shifts[sel] for _, g in cases]
+    runs = []
+    for _ in range(4):
+        tables, sts = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED)
+        assert all((s == 0).all() for s in sts)
+        runs.append(tables)
+    assert ctx.graph_stats() == (1, 2)  # plain, capture + launch, two replays
+    for t in runs[1:]:
+        assert all(np.array_equal(a, b) for a, b in zip(t, runs[0]))
+    plans[0].set_tuning(16, -1)  # a setting the graph bakes in: the next call may not replay
+    t5, _ = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED)
+    assert ctx.graph_stats()[1] == 2
+    plans[0].set_tuning(0, -1)
+    ref64, _ = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP64_LU)
+    for p, a, r in zip(plans, t5, ref64):
+        m = p.shape.absorber_block
+        assert rel_err(a[:, :m, :m, 0], r[:, :m, :m, 0]) < TOL_CHOSEN
+    ctx.set_option(ctx.OPT_MULTI_GRAPH, 0)
+    for _ in range(3):
+        t, _ = fms.fms_real_space_spectrum_multi(plans, ks, phs, fms.FORM_FP32_REFINED)
+        assert all(np.array_equal(a, b) for a, b in zip(t, runs[0]))
+    assert ctx.graph_stats()[1] == 2
+    for p in plans:
+        p.close()
+    ctx.close()
+
+
 def test_autotuned_many_cluster_call_matches_default(ctx, tmp_path):
     """The batched form's autotuner (per size bucket: inner panel width and block pairing; then the stream count)
     on 10 of config 2's clusters with a 4-energy sample: the tuned many-cluster call gives the default call's
