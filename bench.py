@@ -493,7 +493,7 @@ def profile_case(args):
     form = {"fp32": fms.FORM_FP32_REFINED, "fp64": fms.FORM_FP64_LU, "bicgstab": fms.FORM_BICGSTAB}[args.form]
     ctx = fms.Context(0)
     ctx.set_option(ctx.OPT_DUAL_STREAMS, 0)  # one batch per sweep: ncu's launch counts follow the sweep
-    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph, minv=args.minv)
     plan.set_batch(E)
     if args.bicgstab_window is not None:
         plan.set_bicgstab_window(args.bicgstab_window, 1e300)
@@ -501,8 +501,15 @@ def profile_case(args):
     sel = _sample(grid.wave_numbers.shape[0], E) if args.spread else np.arange(E)
     status = None
     for _ in range(args.sweeps):
-        _, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers[sel], grid.phase_shifts[sel], form,
-                                                raise_on_error=False)
+        tab, status = fms.fms_real_space_spectrum(plan, grid.wave_numbers[sel], grid.phase_shifts[sel], form,
+                                                  raise_on_error=False)
+    if args.trace:  # the MKGTR trace of the absorber blocks (K edge, seeded radial integrals)
+        L0 = int(cl.lmaxph[0])
+        m = plan.shape.absorber_block
+        bm, li, _ = fms.transition_matrix(lmax=L0, initial_kappa=-1, polarization=0, multipole=0, spin=0)
+        rkk = np.random.default_rng(7).normal(size=(len(sel), 8, 1)) * (1.0 + 0.2j)
+        for _ in range(args.sweeps):
+            fms.mkgtr_trace(ctx, tab[:, :m, :m, 0], [bm], [li], rkk, active_spin_channels=1, lmax=L0)
     print("ok", int((status != 0).sum()), "failed energies", flush=True)
     plan.close()
     ctx.close()
@@ -711,6 +718,8 @@ def main():
     ap.add_argument("--energies", type=int, default=16, help="profiling mode: energies of the case")
     ap.add_argument("--form", default="fp32", choices=["fp32", "fp64", "bicgstab"], help="profiling mode: form")
     ap.add_argument("--spread", action="store_true", help="profiling mode: energies evenly spaced over the grid")
+    ap.add_argument("--minv", type=int, default=0, help="profiling mode: FEFF solver selector of the plan")
+    ap.add_argument("--trace", action="store_true", help="profiling mode: also the MKGTR trace of the blocks")
     ap.add_argument("--bicgstab-window", type=float, default=None,
                     help="profiling mode: iterate BiCGSTAB only from this energy above E_ref (eV)")
     ap.add_argument("--sweeps", type=int, default=2, help="profiling mode: sweeps")
