@@ -608,14 +608,17 @@ __global__ void split_x_kernel(BatchLayout lay, const double2* __restrict__ X64,
 // r = b - A x in double-float: 64 rows per CTA, each thread two rows (r, r + 32)
 // and kCols right-hand sides (columns cg, cg + 8, ...), so that every a and x
 // value read from shared memory feeds several complex MACs.
-constexpr int kRdRows = 64, kRdK = 32, kRdGroups = 8;
+constexpr int kRdRows = 64, kRdK = 32;
 
-template <int kCols>
-__global__ void __launch_bounds__(256) residual_df_kernel(BatchLayout lay, const float4* __restrict__ Ms,
-                                                          const float4* __restrict__ Xsp, double2* __restrict__ R,
-                                                          unsigned long long* rnorm, unsigned long long* bnorm,
-                                                          const int* skip) {
-  constexpr int BR = kRdRows, BK = kRdK, XW = kCols * kRdGroups;
+// kGroups warps, one column group each (columns cg, cg + kGroups, ...), so
+// that kCols x kGroups covers the right-hand sides with little padding (25 as
+// 5 x 5, 9 as 3 x 3).
+template <int kCols, int kGroups>
+__global__ void __launch_bounds__(32 * kGroups) residual_df_kernel(BatchLayout lay, const float4* __restrict__ Ms,
+                                                                   const float4* __restrict__ Xsp,
+                                                                   double2* __restrict__ R, unsigned long long* rnorm,
+                                                                   unsigned long long* bnorm, const int* skip) {
+  constexpr int BR = kRdRows, BK = kRdK, XW = kCols * kGroups, kThreads = 32 * kGroups;
   const int b = blockIdx.y;
   if (skip && skip[b]) return;
   extern __shared__ float4 rd_sm[];
@@ -635,12 +638,12 @@ __global__ void __launch_bounds__(256) residual_df_kernel(BatchLayout lay, const
   for (int k0 = 0; k0 < n; k0 += BK) {
     const int kk_n = min(BK, n - k0);
     __syncthreads();
-    for (int idx = tid; idx < BK * BR; idx += 256) {
+    for (int idx = tid; idx < BK * BR; idx += kThreads) {
       const int r = idx % BR, kk = idx / BR;
       As[kk * BR + r] = (r0 + r < n && kk < kk_n) ? A[size_t(r0 + r) + size_t(lay.lda) * (k0 + kk)]
                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    for (int idx = tid; idx < BK * XW; idx += 256) {
+    for (int idx = tid; idx < BK * XW; idx += kThreads) {
       const int kk = idx % BK, c = idx / BK;
       Xs[kk * XW + c] = (kk < kk_n && c < m) ? X[size_t(k0 + kk) + size_t(lay.lda) * c] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -649,7 +652,7 @@ __global__ void __launch_bounds__(256) residual_df_kernel(BatchLayout lay, const
       const float4 a0 = As[kk * BR + rp], a1 = As[kk * BR + rp + 32];
 #pragma unroll
       for (int q = 0; q < kCols; ++q) {
-        const float4 x = Xs[kk * XW + cg + kRdGroups * q];
+        const float4 x = Xs[kk * XW + cg + kGroups * q];
         dot2_mac(acc[0][q][0], a0.x, a0.z, x.x, x.z);    // re += a.re x.re
         dot2_mac(acc[0][q][0], -a0.y, -a0.w, x.y, x.w);  // re -= a.im x.im
         dot2_mac(acc[0][q][1], a0.x, a0.z, x.y, x.w);    // im += a.re x.im
@@ -668,7 +671,7 @@ __global__ void __launch_bounds__(256) residual_df_kernel(BatchLayout lay, const
     if (row >= n) continue;
 #pragma unroll
     for (int q = 0; q < kCols; ++q) {
-      const int c = cg + kRdGroups * q;
+      const int c = cg + kGroups * q;
       if (c >= m) continue;
       const double2 bv = join_hi_lo(A[size_t(row) + size_t(lay.lda) * (n + c)]);
       const double ax = double(acc[h][q][0].hi) + double(acc[h][q][0].lo);
@@ -1166,15 +1169,15 @@ void launch_absorber_solve(const BatchLayout& lay, int batch, const cplx<T>* M, 
   absorber_solve_kernel<T><<<unsigned(batch), threads, smem, s>>>(lay, M, gg, status);
 }
 
-template <int kCols>
+template <int kCols, int kGroups>
 static void launch_residual_df(const BatchLayout& lay, int batch, const float4* Ms, const float4* Xs, double2* R,
                                unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
                                cudaStream_t s) {
-  constexpr size_t smem = size_t(kRdK) * (kRdRows + kCols * kRdGroups) * sizeof(float4);
-  ensure_smem_limit(reinterpret_cast<const void*>(residual_df_kernel<kCols>), smem);
+  constexpr size_t smem = size_t(kRdK) * (kRdRows + kCols * kGroups) * sizeof(float4);
+  ensure_smem_limit(reinterpret_cast<const void*>(residual_df_kernel<kCols, kGroups>), smem);
   dim3 grid(unsigned((lay.n + kRdRows - 1) / kRdRows), unsigned(batch));
   count_launch();
-  residual_df_kernel<kCols><<<grid, 256, smem, s>>>(lay, Ms, Xs, R, rnorm_bits, bnorm_bits, skip);
+  residual_df_kernel<kCols, kGroups><<<grid, 32 * kGroups, smem, s>>>(lay, Ms, Xs, R, rnorm_bits, bnorm_bits, skip);
 }
 
 void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
@@ -1185,9 +1188,14 @@ void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const 
     count_launch();
     split_x_kernel<<<grid, 256, 0, s>>>(lay, X64, Xsplit, skip);
   }
-  if (lay.m <= 16) launch_residual_df<2>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
-  else if (lay.m <= 32) launch_residual_df<4>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
-  else launch_residual_df<8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  // column groups sized to the right-hand sides: 9 (lmax 2) and 25 (lmax 4) without padding
+  if (lay.m <= 8) launch_residual_df<1, 8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else if (lay.m == 9) launch_residual_df<3, 3>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else if (lay.m <= 16) launch_residual_df<2, 8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else if (lay.m <= 24) launch_residual_df<3, 8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else if (lay.m == 25) launch_residual_df<5, 5>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else if (lay.m <= 32) launch_residual_df<4, 8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
+  else launch_residual_df<8, 8>(lay, batch, Ms, Xsplit, R, rnorm_bits, bnorm_bits, skip, s);
 }
 
 void launch_residual_to_rhs32(const BatchLayout& lay, int batch, const double2* R,

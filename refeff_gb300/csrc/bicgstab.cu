@@ -251,6 +251,291 @@ __global__ void __launch_bounds__(kMvThreads) bicg_matvec_kernel(View w, const f
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core product (tcgen05, split TF32): the same Y = A X, slices and
+// partial products as bicg_matvec_kernel, with the complex products on the
+// 5th-generation tensor cores.  Each of the four operand warps owns one row of
+// the CTA's 128-row tile: it loads the row's 16 A entries of a slab with
+// coalesced global loads (two slabs ahead in registers), splits them into TF32
+// hi / lo parts and stores the four real planes (re hi, re lo, im hi, im lo)
+// in the K-major 64-byte-swizzled UMMA layout; the X slab becomes six planes
+// (re hi, re lo, im hi, im lo, -im hi, -im lo).  One thread issues 12 MMAs
+// per K step of 8 into two TMEM accumulators (Yr, Yi; N = 16 or 32 columns),
+// as the LU's trailing update does:
+//     Yr += Ar Xr + Ai (-Xi)        Yi += Ar Xi + Ai Xr,
+// each real product hi*hi + hi*lo + lo*hi.  Two plane stages let the operand
+// warps fill one while the MMAs read the other.  Every wait is bounded; a
+// timeout sets *err (the solve then hands its matrices to the LU) and the
+// CTA drains its MMAs and frees its tensor memory before it returns.
+constexpr int kTcRows = 128, kTcK = 16, kTcThreads = 160, kTcStages = 2;
+constexpr long long kTcBicgPolls = 1LL << 26;  // poll budget of each wait (about 1 s is the other bound)
+constexpr int kTcAPlane = kTcRows * 64;  // 8 KB: 128 rows of 16 TF32 values
+
+template <int N> struct TcMv {
+  static constexpr int kA = 4 * kTcAPlane;  // 32 KB
+  static constexpr int kBPlane = N * 64;
+  static constexpr int kB = 6 * kBPlane;
+  static constexpr int kStage = kA + kB;
+  static constexpr int kBars = 128;        // barriers, TMEM slot, abort flag
+  static constexpr int kSmem = kTcStages * kStage + kBars + 1024;
+  static constexpr uint32_t kCols = 2 * N;  // TMEM columns: Yr, Yi (a power of two >= 32)
+  // kind::tf32, D = F32, A = B = TF32, both K-major, M = 128
+  static constexpr uint32_t kIdesc =
+      (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
+};
+
+__device__ __forceinline__ uint32_t tc_smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint32_t tc_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+// hi / lo TF32 parts of the real and imaginary parts
+__device__ __forceinline__ void tc_split(float2 v, uint32_t out[4]) {
+  const uint32_t rh = tc_tf32(v.x), ih = tc_tf32(v.y);
+  out[0] = rh;
+  out[1] = tc_tf32(v.x - __uint_as_float(rh));
+  out[2] = ih;
+  out[3] = tc_tf32(v.y - __uint_as_float(ih));
+}
+// Byte offset of (row, k), k < 16, in a K-major tile of 64-byte rows with the
+// 64-byte swizzle: the 16-byte chunk index XOR (row / 2) % 4.
+__device__ __forceinline__ int tc_sw64(int row, int k) {
+  return row * 64 + ((((k >> 2) ^ ((row >> 1) & 3))) << 4) + ((k & 3) << 2);
+}
+// start >> 4, LBO 1 (unused when swizzled), SBO = 8 rows x 64 B, version 1, 64-byte swizzle (layout 4)
+__device__ __forceinline__ uint64_t tc_desc64(uint32_t saddr) {
+  return uint64_t((saddr >> 4) & 0x3FFFu) | (uint64_t(1) << 16) | (uint64_t(512 >> 4) << 32) | (uint64_t(1) << 46) |
+         (uint64_t(4) << 61);
+}
+template <uint32_t kIdesc>
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tc_bar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void tc_bar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ uint64_t tc_now() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ bool tc_try(uint32_t bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait (poll budget, or 1 s); a timeout raises the CTA's abort flag and *err.
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
+                                        long long polls) {
+  const uint64_t t0 = tc_now();
+  for (long long it = 0; it < polls; ++it) {
+    if (tc_try(bar, parity)) return true;
+    if ((it & 255) == 255) {
+      if (*abort_flag) return false;
+      if (tc_now() - t0 > 1000000000ull) break;
+    }
+  }
+  *abort_flag = 1;
+  atomicExch(err, 1);
+  return false;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, const float2* __restrict__ M32,
+                                                                     size_t stride, int src, int dst, int kchunk,
+                                                                     const int* skip, int* err, long long polls) {
+  using L = TcMv<N>;
+  const int b = w.matrix();
+  // uniform over the CTA, before any tensor memory is taken; a raised error skips the product
+  if (b < 0 || (skip && skip[b]) || w.done[b] || *reinterpret_cast<volatile int*>(err)) return;
+  extern __shared__ uint8_t tsm[];
+  const uint32_t raw = tc_smem_u32(tsm);
+  const uint32_t sbase = (raw + 1023u) & ~1023u;
+  uint8_t* const gbase = tsm + (sbase - raw);
+  uint8_t* const meta = gbase + kTcStages * L::kStage;
+  // barriers: full[2] (128 operand threads), empty[2] (commit), acc (commit), drain (commit)
+  auto bar = [&](int i) { return tc_smem_u32(meta + 8 * i); };
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(meta + 64);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(meta + 68);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int slice = blockIdx.z;
+  const int n = w.n, r0 = blockIdx.x * kTcRows;
+  const int kbeg = slice * kchunk, kend = min(n, kbeg + kchunk);
+  const int slabs = (kend - kbeg + kTcK - 1) / kTcK;  // >= 1: slices start below n
+  const float2* A = M32 + size_t(b) * stride;
+
+  if (warp == 4) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem_u32(tmem_slot)),
+                 "r"(L::kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kTcStages; ++i) {
+      tc_bar_init(bar(i), 128);            // full: every operand thread
+      tc_bar_init(bar(kTcStages + i), 1);  // empty: one commit
+    }
+    tc_bar_init(bar(2 * kTcStages), 1);      // accumulators complete
+    tc_bar_init(bar(2 * kTcStages + 1), 1);  // drain
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < 4) {
+    // ---- operand warps: row r0 + tid of A, and the X slab ----
+    const int row = r0 + tid;
+    const bool row_ok = row < n;
+    auto load = [&](int sl, float2 (&v)[kTcK]) {
+      const int k0 = kbeg + sl * kTcK;
+#pragma unroll
+      for (int kk = 0; kk < kTcK; ++kk)
+        v[kk] = (row_ok && sl < slabs && k0 + kk < kend) ? __ldcs(A + size_t(row) + size_t(w.lda) * (k0 + kk))
+                                                          : make_float2(0.f, 0.f);
+    };
+    float2 v0[kTcK], v1[kTcK], v2[kTcK];
+    load(0, v0);
+    load(1, v1);
+    bool ok = true;
+    for (int sl = 0; sl < slabs && ok; ++sl) {
+      load(sl + 2, v2);
+      const int st = sl & 1;
+      const uint32_t ph = uint32_t((sl >> 1) & 1);
+      ok = tc_wait(bar(kTcStages + st), ph ^ 1u, abort_flag, err, polls);  // the MMAs of slab sl - 2 are done
+      if (!ok) break;
+      uint8_t* const sA = gbase + st * L::kStage;
+      uint8_t* const sB = sA + L::kA;
+#pragma unroll
+      for (int k4 = 0; k4 < kTcK / 4; ++k4) {
+        uint32_t q[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          uint32_t sv[4];
+          tc_split(v0[4 * k4 + i], sv);
+#pragma unroll
+          for (int pl = 0; pl < 4; ++pl) q[pl][i] = sv[pl];
+        }
+        const int off = tc_sw64(tid, 4 * k4);
+#pragma unroll
+        for (int pl = 0; pl < 4; ++pl)
+          *reinterpret_cast<uint4*>(sA + pl * kTcAPlane + off) = make_uint4(q[pl][0], q[pl][1], q[pl][2], q[pl][3]);
+      }
+      const int k0 = kbeg + sl * kTcK;
+#pragma unroll
+      for (int j = 0; j < N * kTcK / 128; ++j) {
+        const int e = tid + 128 * j, kk = e % kTcK, c = e / kTcK;
+        const float2 x = (c < w.m && k0 + kk < kend) ? w.v(src, b, c)[k0 + kk] : make_float2(0.f, 0.f);
+        uint32_t sv[4];
+        tc_split(x, sv);
+        const int off = tc_sw64(c, kk);
+#pragma unroll
+        for (int pl = 0; pl < 4; ++pl) *reinterpret_cast<uint32_t*>(sB + pl * L::kBPlane + off) = sv[pl];
+        *reinterpret_cast<uint32_t*>(sB + 4 * L::kBPlane + off) = sv[2] ^ 0x80000000u;  // -im hi
+        *reinterpret_cast<uint32_t*>(sB + 5 * L::kBPlane + off) = sv[3] ^ 0x80000000u;  // -im lo
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the planes are read by the tensor cores
+      tc_bar_arrive(bar(st));
+#pragma unroll
+      for (int kk = 0; kk < kTcK; ++kk) {
+        v0[kk] = v1[kk];
+        v1[kk] = v2[kk];
+      }
+    }
+    // ---- epilogue: the tile's rows of Y (or of this slice's partial product) ----
+    const bool ready = ok && tc_wait(bar(2 * kTcStages), 0u, abort_flag, err, polls);
+    if (__all_sync(0xffffffffu, ready)) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t tr = tmem + (uint32_t(warp * 32) << 16), ti = tr + uint32_t(N);
+#pragma unroll
+      for (int cb = 0; cb < N / 8; ++cb) {
+        uint32_t yr[8], yi[8];
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(yr[0]), "=r"(yr[1]), "=r"(yr[2]), "=r"(yr[3]), "=r"(yr[4]), "=r"(yr[5]), "=r"(yr[6]),
+                       "=r"(yr[7])
+                     : "r"(tr + uint32_t(cb * 8)));
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(yi[0]), "=r"(yi[1]), "=r"(yi[2]), "=r"(yi[3]), "=r"(yi[4]), "=r"(yi[5]), "=r"(yi[6]),
+                       "=r"(yi[7])
+                     : "r"(ti + uint32_t(cb * 8)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row_ok) {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int c = cb * 8 + j;
+            if (c < w.m) {
+              float2* y = slice == 0 ? w.v(dst, b, c) : w.pv(slice, b, c);
+              y[row] = make_float2(__uint_as_float(yr[j]), __uint_as_float(yi[j]));
+            }
+          }
+        }
+      }
+    }
+  } else if (lane == 0) {
+    // ---- MMA issuer ----
+    bool issued = false, ok = true;
+    for (int sl = 0; sl < slabs; ++sl) {
+      const int st = sl & 1;
+      ok = tc_wait(bar(st), uint32_t((sl >> 1) & 1), abort_flag, err, polls);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sA = sbase + uint32_t(st * L::kStage), sB = sA + uint32_t(L::kA);
+#pragma unroll
+      for (int ks = 0; ks < kTcK / 8; ++ks) {
+        const uint32_t koff = uint32_t(ks * 32);
+        auto ad = [&](int pl) { return tc_desc64(sA + uint32_t(pl * kTcAPlane) + koff); };
+        auto bd = [&](int pl) { return tc_desc64(sB + uint32_t(pl * L::kBPlane) + koff); };
+        const uint32_t a0 = (sl == 0 && ks == 0) ? 0u : 1u;
+        const uint32_t tr = tmem, ti = tmem + uint32_t(N);
+        // Yr += Ar Xr + Ai (-Xi)
+        tc_mma<L::kIdesc>(tr, ad(0), bd(0), a0);
+        tc_mma<L::kIdesc>(tr, ad(0), bd(1), 1u);
+        tc_mma<L::kIdesc>(tr, ad(1), bd(0), 1u);
+        tc_mma<L::kIdesc>(tr, ad(2), bd(4), 1u);
+        tc_mma<L::kIdesc>(tr, ad(2), bd(5), 1u);
+        tc_mma<L::kIdesc>(tr, ad(3), bd(4), 1u);
+        // Yi += Ar Xi + Ai Xr
+        tc_mma<L::kIdesc>(ti, ad(0), bd(2), a0);
+        tc_mma<L::kIdesc>(ti, ad(0), bd(3), 1u);
+        tc_mma<L::kIdesc>(ti, ad(1), bd(2), 1u);
+        tc_mma<L::kIdesc>(ti, ad(2), bd(0), 1u);
+        tc_mma<L::kIdesc>(ti, ad(2), bd(1), 1u);
+        tc_mma<L::kIdesc>(ti, ad(3), bd(0), 1u);
+      }
+      issued = true;
+      tc_commit(bar(kTcStages + st));  // the stage is free once these MMAs have read it
+    }
+    if (ok) tc_commit(bar(2 * kTcStages));  // Y complete
+    if (issued) {
+      // every MMA of this CTA has completed before the tensor memory is freed
+      tc_commit(bar(2 * kTcStages + 1));
+      const uint64_t t0 = tc_now();
+      for (long long it = 0; it < polls; ++it)
+        if (tc_try(bar(2 * kTcStages + 1), 0u) || ((it & 1023) == 1023 && tc_now() - t0 > 1000000000ull)) break;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 4) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(L::kCols));
+}
+
 // acc2 += (r~, v)
 __global__ void bicg_dot_rv_kernel(View w, const int* skip) {
   const int b = w.matrix(), c = blockIdx.z;
@@ -476,7 +761,8 @@ __global__ void bicg_check_compact_kernel(View w, double tol2, int iter, int* it
 }
 
 // Solution X -> RHS columns of M32; failed[b] = 2 when a column did not converge.
-__global__ void bicg_finish_kernel(View w, float2* __restrict__ M32, size_t stride, int* failed, const int* skip) {
+__global__ void bicg_finish_kernel(View w, float2* __restrict__ M32, size_t stride, int* failed, const int* skip,
+                                   const int* tc_err) {
   const int b = blockIdx.y, c = blockIdx.z;
   if (skip && skip[b]) return;
   const float2* x = w.v(kX, b, c);
@@ -486,10 +772,18 @@ __global__ void bicg_finish_kernel(View w, float2* __restrict__ M32, size_t stri
     if (i >= w.n) break;
     out[i] = x[i];
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0 && w.state[size_t(b) * w.m + c] != 1) failed[b] = 2;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (w.state[size_t(b) * w.m + c] != 1 || (tc_err && *tc_err))) failed[b] = 2;
 }
 
 }  // namespace
+
+int bicg_slices(int n, bool tensor, int* chunk) {
+  int c = tensor ? kBicgTcSliceCols
+                 : std::max(kMvSliceCols, ((n + kBicgMaxSplit - 1) / kBicgMaxSplit + kMvK - 1) / kMvK * kMvK);
+  c = std::min(c, std::max(n, 1));
+  if (chunk) *chunk = c;
+  return (n + c - 1) / c;
+}
 
 cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const float2* D, const BlockPrecond* blk,
                            const BicgWork& w, double tol, int max_iter, int poll, const int* skip, int* failed,
@@ -502,15 +796,24 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
                                                int(kMvSmem));
     if (e != cudaSuccess) return e;
   }
-  // Slices of A's columns: kMvSliceCols columns each (more for large n, at
-  // most kBicgMaxSplit slices), so that the last running matrices still fill the
-  // GPU with product CTAs.  The slicing depends on n alone: a matrix's
-  // arithmetic does not depend on which others share its batch.
-  int chunk = lay.n, nsplit = 1;
-  if (w.part) {
-    chunk = std::max(kMvSliceCols, ((lay.n + kBicgMaxSplit - 1) / kBicgMaxSplit + kMvK - 1) / kMvK * kMvK);
-    nsplit = (lay.n + chunk - 1) / chunk;
+  // the tensor-core product for up to 32 right-hand sides (N = 16 or 32 accumulator columns)
+  const bool tensor = w.tensor && w.tc_err && lay.m <= 32;
+  const bool n16 = lay.m <= 16;
+  if (tensor) {
+    const cudaError_t e = n16 ? cudaFuncSetAttribute(bicg_tc_matvec_kernel<16>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, TcMv<16>::kSmem)
+                              : cudaFuncSetAttribute(bicg_tc_matvec_kernel<32>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, TcMv<32>::kSmem);
+    if (e != cudaSuccess) return e;
+    cudaMemsetAsync(w.tc_err, 0, sizeof(int), s);
   }
+  const unsigned tc_row_blocks = unsigned((lay.n + kTcRows - 1) / kTcRows);
+  // Slices of A's columns (bicg_slices): the last running matrices still fill
+  // the GPU with product CTAs.  The slicing depends on n (and the product's
+  // kind) alone: a matrix's arithmetic does not depend on which others share
+  // its batch.
+  int chunk = lay.n, nsplit = 1;
+  if (w.part) nsplit = bicg_slices(lay.n, tensor, &chunk);
   const int sthreads = 128, sblocks = (batch * lay.m + sthreads - 1) / sthreads;
   const int bblocks = (batch + sthreads - 1) / sthreads;
   cudaMemsetAsync(w.sc, 0, size_t(batch) * lay.m * kBicgScalars * sizeof(double), s);
@@ -542,12 +845,27 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
   }
   View vr = v;  // the view of the iteration's launches
   vr.act = compact ? w.act : nullptr;
+  // dst = A src over the running matrices: V = A P^ or T = A S^
+  auto product = [&](unsigned rows_y, int src, int dst) {
+    count_launch();
+    if (tensor) {
+      const dim3 tgrid(tc_row_blocks, rows_y, unsigned(nsplit));
+      if (n16)
+        bicg_tc_matvec_kernel<16><<<tgrid, kTcThreads, TcMv<16>::kSmem, s>>>(vr, M32, lay.stride, src, dst, chunk,
+                                                                              skip, w.tc_err, kTcBicgPolls);
+      else
+        bicg_tc_matvec_kernel<32><<<tgrid, kTcThreads, TcMv<32>::kSmem, s>>>(vr, M32, lay.stride, src, dst, chunk,
+                                                                              skip, w.tc_err, kTcBicgPolls);
+    } else {
+      const dim3 mgrid(unsigned(row_blocks), rows_y, unsigned(groups * nsplit));
+      bicg_matvec_kernel<<<mgrid, kMvThreads, kMvSmem, s>>>(vr, M32, lay.stride, src, dst, groups, chunk, skip);
+    }
+  };
   int running = batch;
   for (int it = 1; it <= max_iter && running > 0; ++it) {
     vr.nsplit = nsplit;  // the dot kernels sum the slices
     const unsigned rows_y = unsigned(compact ? running : batch);
     const dim3 rgrid(vgrid.x, rows_y, vgrid.z);
-    const dim3 mgrid(unsigned(row_blocks), rows_y, unsigned(groups * vr.nsplit));
     count_launch();
     bicg_p_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, blk ? nullptr : D, skip);
     if (blk) {
@@ -555,8 +873,7 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
       bicg_block_apply_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, kP, kPh, blk->B, blk->state_atom, blk->atom_off,
                                                             blk->N, blk->C, skip);
     }
-    count_launch();
-    bicg_matvec_kernel<<<mgrid, kMvThreads, kMvSmem, s>>>(vr, M32, lay.stride, kPh, kV, groups, chunk, skip);
+    product(rows_y, kPh, kV);
     count_launch();
     bicg_dot_rv_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, skip);
     count_launch();
@@ -568,8 +885,7 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
       bicg_block_apply_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, kR, kSh, blk->B, blk->state_atom, blk->atom_off,
                                                             blk->N, blk->C, skip);
     }
-    count_launch();
-    bicg_matvec_kernel<<<mgrid, kMvThreads, kMvSmem, s>>>(vr, M32, lay.stride, kSh, kT, groups, chunk, skip);
+    product(rows_y, kSh, kT);
     count_launch();
     bicg_dot_ts_kernel<<<rgrid, kVecThreads, 0, s>>>(vr, skip);
     count_launch();
@@ -590,7 +906,7 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
     }
   }
   count_launch();
-  bicg_finish_kernel<<<vgrid, kVecThreads, 0, s>>>(v, M32, lay.stride, failed, skip);
+  bicg_finish_kernel<<<vgrid, kVecThreads, 0, s>>>(v, M32, lay.stride, failed, skip, tensor ? w.tc_err : nullptr);
   return cudaGetLastError();
 }
 

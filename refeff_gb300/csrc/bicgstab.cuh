@@ -10,9 +10,13 @@ namespace rfx {
 constexpr int kBicgVectors = 8;
 // Doubles kept per (matrix, column): rho, alpha, omega, |b|^2, and accumulators.
 constexpr int kBicgScalars = 16;
-// Most slices the matrix-vector product splits A's columns into (partial
-// products summed by the dot kernels).
+// Column slices of the matrix-vector product (partial products summed by the
+// dot kernels): slices of at least 512 columns, at most 16, on the CUDA cores;
+// slices of 256 columns on the tensor cores, whose FP32 accumulation is
+// exact only for short sums.  bicg_slices gives the count for n.
 constexpr int kBicgMaxSplit = 16;
+constexpr int kBicgTcSliceCols = 256;
+int bicg_slices(int n, bool tensor, int* chunk = nullptr);
 
 struct BicgWork {
   float2* vec = nullptr;     // kBicgVectors * batch * lda * m
@@ -21,8 +25,10 @@ struct BicgWork {
   int* done = nullptr;       // batch: every column finished
   int* iters = nullptr;      // batch: iterations of the slowest column
   int* active = nullptr;     // 1 int: matrices still running (host poll)
-  float2* part = nullptr;    // (kBicgMaxSplit - 1) * batch * lda * m: partial products of the split product
+  float2* part = nullptr;    // (slices - 1) * batch * lda * m: partial products of the split product
   int* act = nullptr;        // batch: compacted list of running matrices
+  int* tc_err = nullptr;     // 1 int: set when a wait of the tensor-core product gave up
+  int tensor = 0;            // products on the tensor cores (up to 32 right-hand sides)
 };
 
 // Solves A X = B for every matrix of the batch whose skip flag is clear:

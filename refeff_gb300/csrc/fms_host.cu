@@ -106,6 +106,7 @@ struct refeff_fms_context {
   int paired_blocks = 1;     // REFEFF_FMS_OPT_PAIRED_BLOCKS
   int multi_streams = 4;     // REFEFF_FMS_OPT_MULTI_STREAMS
   int dual_streams = 1;      // REFEFF_FMS_OPT_DUAL_STREAMS
+  int bicg_tensor = 1;       // REFEFF_FMS_OPT_BICG_TENSOR
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
   std::vector<cudaEvent_t> pool_join;  // one per pool stream: joins it back into a capture
   cudaEvent_t fork_ev = nullptr;
@@ -134,6 +135,7 @@ extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option
   bump_epoch();
   switch (option) {
     case REFEFF_FMS_OPT_MULTI_GRAPH: ctx->multi_graph = value != 0; return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_BICG_TENSOR: ctx->bicg_tensor = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_TENSOR_CORES: ctx->use_tensor_cores = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_DENSE_REFINEMENT:
       if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
@@ -438,6 +440,7 @@ struct Workspace {
   DevBuf<float2> bicg_vec, precond_D;
   DevBuf<float2> bicg_part;  // partial products of the split matrix-vector product
   DevBuf<int> bicg_act;      // compacted list of the running matrices
+  DevBuf<int> bicg_err;      // set when a wait of the tensor-core product gave up
   DevBuf<float2> precond_B;  // block-diagonal learned preconditioner: batch x N x C^2
   DevBuf<double> bicg_sc;
   DevBuf<int> bicg_state, bicg_done, bicg_iters, bicg_active, bicg_total;
@@ -1030,6 +1033,7 @@ BicgWork bicg_work(Workspace& ws) {
   w.active = ws.bicg_active.p;
   w.part = ws.bicg_part.p;
   w.act = ws.bicg_act.p;
+  w.tc_err = ws.bicg_err.p;
   return w;
 }
 
@@ -1039,9 +1043,11 @@ BicgWork bicg_work(Workspace& ws) {
 // whose BiCGSTAB solve misses its tolerance within the iteration cap is
 // marked converged = 2 and handed to the refined LU by the caller.
 cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, const BlockPrecond* blk, int iters, double tol,
-                            int max_iter, double inner_tol, int poll, cudaStream_t s, Spans* spans = nullptr) {
+                            int max_iter, double inner_tol, int poll, bool tensor, cudaStream_t s,
+                            Spans* spans = nullptr) {
   const BatchLayout& lay = ws.lay;
-  const BicgWork w = bicg_work(ws);
+  BicgWork w = bicg_work(ws);
+  w.tensor = tensor ? 1 : 0;
   auto span = [&](int phase, auto&& fn) -> cudaError_t {
     cudaEvent_t a = nullptr, b = nullptr;
     if (spans) {
@@ -1226,8 +1232,8 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, Workspace& ws, int batch, refeff_f
     blk.N = p.N;
     blk.C = (p.L + 1) * (p.L + 1);
     e = refine_bicgstab(ws, batch, p.model && !block ? ws.precond_D.p : nullptr, block ? &blk : nullptr,
-                        p.refine_iters, p.refine_tol, p.bicg_max_iter, p.bicg_tol, p.bicg_poll, s,
-                        prof ? &spans : nullptr);
+                        p.refine_iters, p.refine_tol, p.bicg_max_iter, p.bicg_tol, p.bicg_poll, p.ctx->bicg_tensor != 0,
+                        s, prof ? &spans : nullptr);
     if (e != cudaSuccess) return e;
     tick(4, [&] {
       count_launch();
@@ -1371,8 +1377,10 @@ int solve_device_energies_enqueue(refeff_fms_plan& p, int E, const double2* d_k,
   if (bicg) {
     const size_t cols = size_t(ws.batch) * p.m;
     RF_CUDA(ctx, ws.bicg_vec.alloc(size_t(kBicgVectors) * cols * ws.lay.lda));
-    RF_CUDA(ctx, ws.bicg_part.alloc(size_t(kBicgMaxSplit - 1) * cols * ws.lay.lda));
+    const int slices = std::max(bicg_slices(p.n, false), bicg_slices(p.n, ctx->bicg_tensor != 0));
+    RF_CUDA(ctx, ws.bicg_part.alloc(size_t(slices - 1) * cols * ws.lay.lda));
     RF_CUDA(ctx, ws.bicg_act.alloc(size_t(ws.batch)));
+    RF_CUDA(ctx, ws.bicg_err.alloc(1));
     RF_CUDA(ctx, ws.bicg_sc.alloc(cols * kBicgScalars));
     RF_CUDA(ctx, ws.bicg_state.alloc(cols));
     RF_CUDA(ctx, ws.bicg_done.alloc(size_t(ws.batch)));

@@ -215,6 +215,7 @@ class Context:
     OPT_MULTI_STREAMS = 5
     OPT_DUAL_STREAMS = 6
     OPT_MULTI_GRAPH = 7
+    OPT_BICG_TENSOR = 8
 
     def set_option(self, option: int, value: int):
         """Context option (applies to plans / dense solves started afterwards)."""

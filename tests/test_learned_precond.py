@@ -199,6 +199,35 @@ def test_gpu_bicgstab_form_matches_fp64_lu(ctx):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("lmax", [3, 4])
+def test_gpu_bicgstab_tensor_product_matches_cuda_cores(ctx, lmax):
+    """The BiCGSTAB form with its matrix-vector products on the tensor cores (split TF32; 16 accumulator columns
+    at lmax 3, 32 at lmax 4 for the 25 right-hand sides) and on the FP32 CUDA cores: both meet the 1e-6 gate
+    against the FP64 LU with every energy solved by BiCGSTAB (no product gave up), in about the same number of
+    iterations."""
+    cl, grid = wl.small_cluster(6.0, lmax=lmax, n_energies=12, seed=5)
+    sel = np.arange(6, 12)  # 17..40 eV: every energy converges within the 400-iteration cap
+    k, ph = grid.wave_numbers[sel], grid.phase_shifts[sel]
+    plan = fms.fms_real_space_plan(ctx, cl.positions, cl.potentials, cl.lmaxph)
+    g64, _ = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_FP64_LU)
+    m = plan.shape.absorber_block
+    its = {}
+    try:
+        for tensor in (1, 0):
+            ctx.set_option(ctx.OPT_BICG_TENSOR, tensor)
+            g, st = fms.fms_real_space_spectrum(plan, k, ph, fms.FORM_BICGSTAB)
+            its[tensor] = plan.bicgstab_stats(len(sel))
+            assert (st == 0).all() and (plan.bicgstab_lu_energies(len(sel)) == 0).all(), tensor
+            for e in range(len(sel)):
+                ref = g64[e, :m, :m, 0]
+                assert np.linalg.norm(g[e, :m, :m, 0] - ref) <= 1e-6 * np.linalg.norm(ref), (tensor, e)
+    finally:
+        ctx.set_option(ctx.OPT_BICG_TENSOR, 1)
+    print("iterations, tensor cores vs CUDA cores:", its[1].sum(), its[0].sum())
+    assert abs(int(its[1].sum()) - int(its[0].sum())) <= 0.25 * its[0].sum()
+
+
+@pytest.mark.gpu
 def test_gpu_bicgstab_iteration_cap_falls_back_to_lu(ctx):
     """A cap of 3 iterations misses the tolerance: those energies are re-solved by the refined LU (FP32
     factorisation + FP64 refinement) and flagged; no FP64 fallback is needed."""
