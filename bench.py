@@ -373,7 +373,7 @@ def config_batched(ctx, fms, wl, local):
 
 
 def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, batch_plain, bicgstab_energies=0,
-                  learned=None):
+                  learned=None, bicgstab_on_chosen=None):
     """One large cluster: the chosen form on an evenly spaced sample of n_chosen energies (in batches of
     batch_chosen, one warm batch first) and the plain FP64 LU on an evenly spaced sub-sample of n_plain of
     them (in batches of batch_plain, one warm batch first); the gg error is taken on the common energies."""
@@ -453,6 +453,28 @@ def config_single(ctx, fms, wl, local, which, n_chosen, batch_chosen, n_plain, b
                 "note": "the same BiCGSTAB with the learned diagonal right preconditioner, applied only inside "
                         "the energy window where it was trained; energies from that window up iterate, those "
                         "below it and those that miss the cap go to the refined LU"}
+    if bicgstab_on_chosen is not None:
+        # the BiCGSTAB form on the chosen form's energies (its window from bwin eV above E_ref, the rest by the
+        # refined LU), against the chosen form on the same energies
+        bwin = float(bicgstab_on_chosen)
+        plan.set_batch(batch_chosen)
+        plan.set_bicgstab_window(bwin, 1e300)
+        fms.fms_real_space_spectrum(plan, k[sel[-batch_chosen:]], ph[sel[-batch_chosen:]], fms.FORM_BICGSTAB,
+                                    raise_on_error=False)
+        with sampler:
+            (gb, sb), tb = _wall(lambda: fms.fms_real_space_spectrum(plan, k[sel], ph[sel], fms.FORM_BICGSTAB,
+                                                                     raise_on_error=False))
+        its = plan.bicgstab_stats(len(sel))
+        lu = plan.bicgstab_lu_energies(len(sel))
+        plan.set_bicgstab_window()
+        out["bicgstab_on_chosen_energies"] = {
+            "value": len(sel) / tb, "seconds": tb, "energies": int(len(sel)), "over_chosen": t32 / tb,
+            "over_plain": (len(sel) / tb) / plain, "max_rel_gg_err_vs_chosen": _rel_blocks(gb, g32, m),
+            "max_rel_gg_err_vs_fp64": _rel_blocks(gb[idx], g64, m), "status_nonzero": int((sb != 0).sum()),
+            "iterations": int(its.sum()), "window_ev_above_eref": [bwin, None],
+            "refined_lu_outside_window": int((lu == 2).sum()), "refined_lu_missed_cap": int((lu == 1).sum()),
+            "note": "batched BiCGSTAB (tensor-core products) inside the FP64 refinement on the energies of its "
+                    "window, the others by the refined LU, on the chosen form's energies and batches"}
     plan.close()
     return out
 
@@ -480,7 +502,8 @@ def configs_block(ctx, fms, wl, local):
                   **config_single(ctx, fms, wl, local, 3, n_chosen=300, batch_chosen=150, n_plain=24, batch_plain=8,
                                   bicgstab_energies=24, learned=train_learned(ctx, fms))),
         "4": dict(workload="random close packed binary cluster, 600 atoms, lmax 4, 400 energies -20..+300 eV",
-                  **config_single(ctx, fms, wl, local, 4, n_chosen=40, batch_chosen=20, n_plain=2, batch_plain=1)),
+                  **config_single(ctx, fms, wl, local, 4, n_chosen=40, batch_chosen=20, n_plain=2, batch_plain=1,
+                                  bicgstab_on_chosen=60.0)),
     }
 
 
