@@ -148,9 +148,10 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     option or plan setting changes; 0 keeps one launch sequence per plan. */
 #define REFEFF_FMS_OPT_MULTI_GRAPH 7
 /*   REFEFF_FMS_OPT_BICG_TENSOR: 1 (default) runs the BICGSTAB form's
- *     matrix-vector products on the tensor cores (split TF32, up to 32
- *     right-hand sides); 0 on the FP32 CUDA cores.  A product whose bounded
- *     wait gives up hands its matrices to the refined LU. */
+ *     matrix-vector products on the tensor cores (split TF32, four real
+ *     products, up to 32 right-hand sides); 2 the three-product (3M) form of
+ *     the same; 0 on the FP32 CUDA cores.  A product whose bounded wait gives
+ *     up hands its matrices to the refined LU. */
 #define REFEFF_FMS_OPT_BICG_TENSOR 8
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
 /* How often the context captured and replayed the many-cluster graph. */

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "bicgstab.cuh"
@@ -271,14 +272,19 @@ constexpr int kTcRows = 128, kTcK = 16, kTcThreads = 160, kTcStages = 2;
 constexpr long long kTcBicgPolls = 1LL << 26;  // poll budget of each wait (about 1 s is the other bound)
 constexpr int kTcAPlane = kTcRows * 64;  // 8 KB: 128 rows of 16 TF32 values
 
-template <int N> struct TcMv {
-  static constexpr int kA = 4 * kTcAPlane;  // 32 KB
+// k3M: the three-product form P1 = Ar Xr, P2 = Ai Xi, P3 = (Ar + Ai)(Xr + Xi),
+// Yr = P1 - P2, Yi = P3 - P1 - P2 (9 MMAs per K step; six A planes, three
+// accumulators); otherwise the four products above (12 MMAs, two accumulators).
+template <int N, bool k3M = false> struct TcMv {
+  static constexpr int kAPlanes = k3M ? 6 : 4;
+  static constexpr int kA = kAPlanes * kTcAPlane;
   static constexpr int kBPlane = N * 64;
   static constexpr int kB = 6 * kBPlane;
   static constexpr int kStage = kA + kB;
   static constexpr int kBars = 128;        // barriers, TMEM slot, abort flag
   static constexpr int kSmem = kTcStages * kStage + kBars + 1024;
-  static constexpr uint32_t kCols = 2 * N;  // TMEM columns: Yr, Yi (a power of two >= 32)
+  // TMEM columns (a power of two >= 32): Yr, Yi, or P1, P2, P3
+  static constexpr uint32_t kCols = k3M ? (3 * N <= 64 ? 64u : 128u) : 2u * N;
   // kind::tf32, D = F32, A = B = TF32, both K-major, M = 128
   static constexpr uint32_t kIdesc =
       (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
@@ -356,11 +362,11 @@ __device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile 
   return false;
 }
 
-template <int N>
+template <int N, bool k3M>
 __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, const float2* __restrict__ M32,
                                                                      size_t stride, int src, int dst, int kchunk,
                                                                      const int* skip, int* err, long long polls) {
-  using L = TcMv<N>;
+  using L = TcMv<N, k3M>;
   const int b = w.matrix();
   // uniform over the CTA, before any tensor memory is taken; a raised error skips the product
   if (b < 0 || (skip && skip[b]) || w.done[b] || *reinterpret_cast<volatile int*>(err)) return;
@@ -425,17 +431,24 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
       uint8_t* const sB = sA + L::kA;
 #pragma unroll
       for (int k4 = 0; k4 < kTcK / 4; ++k4) {
-        uint32_t q[4][4];
+        uint32_t q[L::kAPlanes][4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
+          const float2 a = v0[4 * k4 + i];
           uint32_t sv[4];
-          tc_split(v0[4 * k4 + i], sv);
+          tc_split(a, sv);
 #pragma unroll
           for (int pl = 0; pl < 4; ++pl) q[pl][i] = sv[pl];
+          if constexpr (k3M) {  // Ar + Ai, hi and lo
+            const float sum = a.x + a.y;
+            const uint32_t hi = tc_tf32(sum);
+            q[4][i] = hi;
+            q[5][i] = tc_tf32(sum - __uint_as_float(hi));
+          }
         }
         const int off = tc_sw64(tid, 4 * k4);
 #pragma unroll
-        for (int pl = 0; pl < 4; ++pl)
+        for (int pl = 0; pl < L::kAPlanes; ++pl)
           *reinterpret_cast<uint4*>(sA + pl * kTcAPlane + off) = make_uint4(q[pl][0], q[pl][1], q[pl][2], q[pl][3]);
       }
       const int k0 = kbeg + sl * kTcK;
@@ -448,8 +461,15 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
         const int off = tc_sw64(c, kk);
 #pragma unroll
         for (int pl = 0; pl < 4; ++pl) *reinterpret_cast<uint32_t*>(sB + pl * L::kBPlane + off) = sv[pl];
-        *reinterpret_cast<uint32_t*>(sB + 4 * L::kBPlane + off) = sv[2] ^ 0x80000000u;  // -im hi
-        *reinterpret_cast<uint32_t*>(sB + 5 * L::kBPlane + off) = sv[3] ^ 0x80000000u;  // -im lo
+        if constexpr (k3M) {  // Xr + Xi, hi and lo
+          const float sum = x.x + x.y;
+          const uint32_t hi = tc_tf32(sum);
+          *reinterpret_cast<uint32_t*>(sB + 4 * L::kBPlane + off) = hi;
+          *reinterpret_cast<uint32_t*>(sB + 5 * L::kBPlane + off) = tc_tf32(sum - __uint_as_float(hi));
+        } else {
+          *reinterpret_cast<uint32_t*>(sB + 4 * L::kBPlane + off) = sv[2] ^ 0x80000000u;  // -im hi
+          *reinterpret_cast<uint32_t*>(sB + 5 * L::kBPlane + off) = sv[3] ^ 0x80000000u;  // -im lo
+        }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the planes are read by the tensor cores
       tc_bar_arrive(bar(st));
@@ -464,17 +484,17 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
     if (__all_sync(0xffffffffu, ready)) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tr = tmem + (uint32_t(warp * 32) << 16), ti = tr + uint32_t(N);
+      auto ld8 = [](uint32_t addr, uint32_t (&o)[8]) {
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=r"(o[0]), "=r"(o[1]), "=r"(o[2]), "=r"(o[3]), "=r"(o[4]), "=r"(o[5]), "=r"(o[6]), "=r"(o[7])
+                     : "r"(addr));
+      };
 #pragma unroll
       for (int cb = 0; cb < N / 8; ++cb) {
-        uint32_t yr[8], yi[8];
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(yr[0]), "=r"(yr[1]), "=r"(yr[2]), "=r"(yr[3]), "=r"(yr[4]), "=r"(yr[5]), "=r"(yr[6]),
-                       "=r"(yr[7])
-                     : "r"(tr + uint32_t(cb * 8)));
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(yi[0]), "=r"(yi[1]), "=r"(yi[2]), "=r"(yi[3]), "=r"(yi[4]), "=r"(yi[5]), "=r"(yi[6]),
-                       "=r"(yi[7])
-                     : "r"(ti + uint32_t(cb * 8)));
+        uint32_t yr[8], yi[8], y3[8];
+        ld8(tr + uint32_t(cb * 8), yr);
+        ld8(ti + uint32_t(cb * 8), yi);
+        if constexpr (k3M) ld8(ti + uint32_t(N + cb * 8), y3);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (row_ok) {
 #pragma unroll
@@ -482,7 +502,14 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
             const int c = cb * 8 + j;
             if (c < w.m) {
               float2* y = slice == 0 ? w.v(dst, b, c) : w.pv(slice, b, c);
-              y[row] = make_float2(__uint_as_float(yr[j]), __uint_as_float(yi[j]));
+              float2 out;
+              if constexpr (k3M) {  // Yr = P1 - P2, Yi = P3 - P1 - P2
+                const float p1 = __uint_as_float(yr[j]), p2 = __uint_as_float(yi[j]), p3 = __uint_as_float(y3[j]);
+                out = make_float2(p1 - p2, p3 - p1 - p2);
+              } else {
+                out = make_float2(__uint_as_float(yr[j]), __uint_as_float(yi[j]));
+              }
+              y[row] = out;
             }
           }
         }
@@ -504,20 +531,34 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
         auto bd = [&](int pl) { return tc_desc64(sB + uint32_t(pl * L::kBPlane) + koff); };
         const uint32_t a0 = (sl == 0 && ks == 0) ? 0u : 1u;
         const uint32_t tr = tmem, ti = tmem + uint32_t(N);
-        // Yr += Ar Xr + Ai (-Xi)
-        tc_mma<L::kIdesc>(tr, ad(0), bd(0), a0);
-        tc_mma<L::kIdesc>(tr, ad(0), bd(1), 1u);
-        tc_mma<L::kIdesc>(tr, ad(1), bd(0), 1u);
-        tc_mma<L::kIdesc>(tr, ad(2), bd(4), 1u);
-        tc_mma<L::kIdesc>(tr, ad(2), bd(5), 1u);
-        tc_mma<L::kIdesc>(tr, ad(3), bd(4), 1u);
-        // Yi += Ar Xi + Ai Xr
-        tc_mma<L::kIdesc>(ti, ad(0), bd(2), a0);
-        tc_mma<L::kIdesc>(ti, ad(0), bd(3), 1u);
-        tc_mma<L::kIdesc>(ti, ad(1), bd(2), 1u);
-        tc_mma<L::kIdesc>(ti, ad(2), bd(0), 1u);
-        tc_mma<L::kIdesc>(ti, ad(2), bd(1), 1u);
-        tc_mma<L::kIdesc>(ti, ad(3), bd(0), 1u);
+        if constexpr (k3M) {
+          const uint32_t t3 = tmem + uint32_t(2 * N);
+          // P1 = Ar Xr, P2 = Ai Xi, P3 = (Ar + Ai)(Xr + Xi), each hi*hi + hi*lo + lo*hi
+          tc_mma<L::kIdesc>(tr, ad(0), bd(0), a0);
+          tc_mma<L::kIdesc>(tr, ad(0), bd(1), 1u);
+          tc_mma<L::kIdesc>(tr, ad(1), bd(0), 1u);
+          tc_mma<L::kIdesc>(ti, ad(2), bd(2), a0);
+          tc_mma<L::kIdesc>(ti, ad(2), bd(3), 1u);
+          tc_mma<L::kIdesc>(ti, ad(3), bd(2), 1u);
+          tc_mma<L::kIdesc>(t3, ad(4), bd(4), a0);
+          tc_mma<L::kIdesc>(t3, ad(4), bd(5), 1u);
+          tc_mma<L::kIdesc>(t3, ad(5), bd(4), 1u);
+        } else {
+          // Yr += Ar Xr + Ai (-Xi)
+          tc_mma<L::kIdesc>(tr, ad(0), bd(0), a0);
+          tc_mma<L::kIdesc>(tr, ad(0), bd(1), 1u);
+          tc_mma<L::kIdesc>(tr, ad(1), bd(0), 1u);
+          tc_mma<L::kIdesc>(tr, ad(2), bd(4), 1u);
+          tc_mma<L::kIdesc>(tr, ad(2), bd(5), 1u);
+          tc_mma<L::kIdesc>(tr, ad(3), bd(4), 1u);
+          // Yi += Ar Xi + Ai Xr
+          tc_mma<L::kIdesc>(ti, ad(0), bd(2), a0);
+          tc_mma<L::kIdesc>(ti, ad(0), bd(3), 1u);
+          tc_mma<L::kIdesc>(ti, ad(1), bd(2), 1u);
+          tc_mma<L::kIdesc>(ti, ad(2), bd(0), 1u);
+          tc_mma<L::kIdesc>(ti, ad(2), bd(1), 1u);
+          tc_mma<L::kIdesc>(ti, ad(3), bd(0), 1u);
+        }
       }
       issued = true;
       tc_commit(bar(kTcStages + st));  // the stage is free once these MMAs have read it
@@ -798,12 +839,27 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
   }
   // the tensor-core product for up to 32 right-hand sides (N = 16 or 32 accumulator columns)
   const bool tensor = w.tensor && w.tc_err && lay.m <= 32;
-  const bool n16 = lay.m <= 16;
+  const bool n16 = lay.m <= 16, three = w.tensor == 2;
+  // the four instantiations: N = 16 / 32 accumulator columns, four or three products
+  auto tc_launch = [&](auto kN, auto k3, const dim3& grid, const View& view, int src, int dst, int chunk) {
+    constexpr int N = decltype(kN)::value;
+    constexpr bool M3 = decltype(k3)::value;
+    bicg_tc_matvec_kernel<N, M3><<<grid, kTcThreads, TcMv<N, M3>::kSmem, s>>>(view, M32, lay.stride, src, dst, chunk,
+                                                                              skip, w.tc_err, kTcBicgPolls);
+  };
+  auto tc_attr = [&](auto kN, auto k3) {
+    constexpr int N = decltype(kN)::value;
+    constexpr bool M3 = decltype(k3)::value;
+    return cudaFuncSetAttribute(bicg_tc_matvec_kernel<N, M3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                TcMv<N, M3>::kSmem);
+  };
+  using I16 = std::integral_constant<int, 16>;
+  using I32 = std::integral_constant<int, 32>;
+  using T3 = std::true_type;
+  using T4 = std::false_type;
   if (tensor) {
-    const cudaError_t e = n16 ? cudaFuncSetAttribute(bicg_tc_matvec_kernel<16>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, TcMv<16>::kSmem)
-                              : cudaFuncSetAttribute(bicg_tc_matvec_kernel<32>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, TcMv<32>::kSmem);
+    const cudaError_t e = n16 ? (three ? tc_attr(I16{}, T3{}) : tc_attr(I16{}, T4{}))
+                              : (three ? tc_attr(I32{}, T3{}) : tc_attr(I32{}, T4{}));
     if (e != cudaSuccess) return e;
     cudaMemsetAsync(w.tc_err, 0, sizeof(int), s);
   }
@@ -850,12 +906,13 @@ cudaError_t bicgstab_solve(const BatchLayout& lay, int batch, float2* M32, const
     count_launch();
     if (tensor) {
       const dim3 tgrid(tc_row_blocks, rows_y, unsigned(nsplit));
-      if (n16)
-        bicg_tc_matvec_kernel<16><<<tgrid, kTcThreads, TcMv<16>::kSmem, s>>>(vr, M32, lay.stride, src, dst, chunk,
-                                                                              skip, w.tc_err, kTcBicgPolls);
-      else
-        bicg_tc_matvec_kernel<32><<<tgrid, kTcThreads, TcMv<32>::kSmem, s>>>(vr, M32, lay.stride, src, dst, chunk,
-                                                                              skip, w.tc_err, kTcBicgPolls);
+      if (n16) {
+        if (three) tc_launch(I16{}, T3{}, tgrid, vr, src, dst, chunk);
+        else tc_launch(I16{}, T4{}, tgrid, vr, src, dst, chunk);
+      } else {
+        if (three) tc_launch(I32{}, T3{}, tgrid, vr, src, dst, chunk);
+        else tc_launch(I32{}, T4{}, tgrid, vr, src, dst, chunk);
+      }
     } else {
       const dim3 mgrid(unsigned(row_blocks), rows_y, unsigned(groups * nsplit));
       bicg_matvec_kernel<<<mgrid, kMvThreads, kMvSmem, s>>>(vr, M32, lay.stride, src, dst, groups, chunk, skip);

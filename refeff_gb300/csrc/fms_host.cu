@@ -135,7 +135,10 @@ extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option
   bump_epoch();
   switch (option) {
     case REFEFF_FMS_OPT_MULTI_GRAPH: ctx->multi_graph = value != 0; return REFEFF_FMS_OK;
-    case REFEFF_FMS_OPT_BICG_TENSOR: ctx->bicg_tensor = value != 0; return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_BICG_TENSOR:
+      if (value < 0 || value > 2) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+      ctx->bicg_tensor = int(value);
+      return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_TENSOR_CORES: ctx->use_tensor_cores = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_DENSE_REFINEMENT:
       if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
@@ -1043,11 +1046,11 @@ BicgWork bicg_work(Workspace& ws) {
 // whose BiCGSTAB solve misses its tolerance within the iteration cap is
 // marked converged = 2 and handed to the refined LU by the caller.
 cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, const BlockPrecond* blk, int iters, double tol,
-                            int max_iter, double inner_tol, int poll, bool tensor, cudaStream_t s,
+                            int max_iter, double inner_tol, int poll, int tensor, cudaStream_t s,
                             Spans* spans = nullptr) {
   const BatchLayout& lay = ws.lay;
   BicgWork w = bicg_work(ws);
-  w.tensor = tensor ? 1 : 0;
+  w.tensor = tensor;
   auto span = [&](int phase, auto&& fn) -> cudaError_t {
     cudaEvent_t a = nullptr, b = nullptr;
     if (spans) {
@@ -1232,7 +1235,7 @@ cudaError_t run_fms_batch(refeff_fms_plan& p, Workspace& ws, int batch, refeff_f
     blk.N = p.N;
     blk.C = (p.L + 1) * (p.L + 1);
     e = refine_bicgstab(ws, batch, p.model && !block ? ws.precond_D.p : nullptr, block ? &blk : nullptr,
-                        p.refine_iters, p.refine_tol, p.bicg_max_iter, p.bicg_tol, p.bicg_poll, p.ctx->bicg_tensor != 0,
+                        p.refine_iters, p.refine_tol, p.bicg_max_iter, p.bicg_tol, p.bicg_poll, p.ctx->bicg_tensor,
                         s, prof ? &spans : nullptr);
     if (e != cudaSuccess) return e;
     tick(4, [&] {
