@@ -259,12 +259,14 @@ __global__ void __launch_bounds__(kMvThreads) bicg_matvec_kernel(View w, const f
 // the CTA's 128-row tile: it loads the row's 16 A entries of a slab with
 // coalesced global loads (two slabs ahead in registers), splits them into TF32
 // hi / lo parts and stores the four real planes (re hi, re lo, im hi, im lo)
-// in the K-major 64-byte-swizzled UMMA layout; the X slab becomes six planes
-// (re hi, re lo, im hi, im lo, -im hi, -im lo).  One thread issues 12 MMAs
-// per K step of 8 into two TMEM accumulators (Yr, Yi; N = 16 or 32 columns),
-// as the LU's trailing update does:
+// in the K-major 64-byte-swizzled UMMA layout; the X slab becomes six slots
+// (-im hi, re hi, im hi, -im lo, re lo, im lo) in an order where each adjacent
+// pair is one 2N-row B operand.  One thread issues 6 MMAs of 2N columns per K
+// step of 8 into the adjacent TMEM accumulators [Yr | Yi] (N = 16 or 32):
 //     Yr += Ar Xr + Ai (-Xi)        Yi += Ar Xi + Ai Xr,
-// each real product hi*hi + hi*lo + lo*hi.  Two plane stages let the operand
+// each real product hi*hi + hi*lo + lo*hi, one A plane against [Xr | Xi] or
+// [-Xi | Xr] at a time (half the MMA instructions of N-column products, as
+// many multiply-adds).  Two plane stages let the operand
 // warps fill one while the MMAs read the other.  Every wait is bounded; a
 // timeout sets *err (the solve then hands its matrices to the LU) and the
 // CTA drains its MMAs and frees its tensor memory before it returns.
@@ -285,9 +287,10 @@ template <int N, bool k3M = false> struct TcMv {
   static constexpr int kSmem = kTcStages * kStage + kBars + 1024;
   // TMEM columns (a power of two >= 32): Yr, Yi, or P1, P2, P3
   static constexpr uint32_t kCols = k3M ? (3 * N <= 64 ? 64u : 128u) : 2u * N;
-  // kind::tf32, D = F32, A = B = TF32, both K-major, M = 128
-  static constexpr uint32_t kIdesc =
-      (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
+  // kind::tf32, D = F32, A = B = TF32, both K-major, M = 128; N columns per MMA for the three-product
+  // form, 2N (one A plane against two adjacent B slots) for the four-product form
+  static constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t((k3M ? N : 2 * N) >> 3) << 17) |
+                                     (uint32_t(kTcRows >> 4) << 24);
 };
 
 __device__ __forceinline__ uint32_t tc_smem_u32(const void* p) {
@@ -459,16 +462,22 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
         uint32_t sv[4];
         tc_split(x, sv);
         const int off = tc_sw64(c, kk);
+        auto put = [&](int slot, uint32_t v) { *reinterpret_cast<uint32_t*>(sB + slot * L::kBPlane + off) = v; };
+        if constexpr (k3M) {  // Xr hi, Xr lo, Xi hi, Xi lo, (Xr + Xi) hi, lo
 #pragma unroll
-        for (int pl = 0; pl < 4; ++pl) *reinterpret_cast<uint32_t*>(sB + pl * L::kBPlane + off) = sv[pl];
-        if constexpr (k3M) {  // Xr + Xi, hi and lo
+          for (int pl = 0; pl < 4; ++pl) put(pl, sv[pl]);
           const float sum = x.x + x.y;
           const uint32_t hi = tc_tf32(sum);
-          *reinterpret_cast<uint32_t*>(sB + 4 * L::kBPlane + off) = hi;
-          *reinterpret_cast<uint32_t*>(sB + 5 * L::kBPlane + off) = tc_tf32(sum - __uint_as_float(hi));
+          put(4, hi);
+          put(5, tc_tf32(sum - __uint_as_float(hi)));
         } else {
-          *reinterpret_cast<uint32_t*>(sB + 4 * L::kBPlane + off) = sv[2] ^ 0x80000000u;  // -im hi
-          *reinterpret_cast<uint32_t*>(sB + 5 * L::kBPlane + off) = sv[3] ^ 0x80000000u;  // -im lo
+          // slots -Xi hi, Xr hi, Xi hi, -Xi lo, Xr lo, Xi lo: each adjacent pair is one 2N-row B operand
+          put(0, sv[2] ^ 0x80000000u);
+          put(1, sv[0]);
+          put(2, sv[2]);
+          put(3, sv[3] ^ 0x80000000u);
+          put(4, sv[1]);
+          put(5, sv[3]);
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the planes are read by the tensor cores
@@ -544,20 +553,17 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
           tc_mma<L::kIdesc>(t3, ad(4), bd(5), 1u);
           tc_mma<L::kIdesc>(t3, ad(5), bd(4), 1u);
         } else {
-          // Yr += Ar Xr + Ai (-Xi)
-          tc_mma<L::kIdesc>(tr, ad(0), bd(0), a0);
-          tc_mma<L::kIdesc>(tr, ad(0), bd(1), 1u);
-          tc_mma<L::kIdesc>(tr, ad(1), bd(0), 1u);
-          tc_mma<L::kIdesc>(tr, ad(2), bd(4), 1u);
-          tc_mma<L::kIdesc>(tr, ad(2), bd(5), 1u);
-          tc_mma<L::kIdesc>(tr, ad(3), bd(4), 1u);
-          // Yi += Ar Xi + Ai Xr
-          tc_mma<L::kIdesc>(ti, ad(0), bd(2), a0);
-          tc_mma<L::kIdesc>(ti, ad(0), bd(3), 1u);
-          tc_mma<L::kIdesc>(ti, ad(1), bd(2), 1u);
-          tc_mma<L::kIdesc>(ti, ad(2), bd(0), 1u);
-          tc_mma<L::kIdesc>(ti, ad(2), bd(1), 1u);
-          tc_mma<L::kIdesc>(ti, ad(3), bd(0), 1u);
+          // [Yr | Yi] (2N columns) += A-plane x [left | right] B slots:
+          //   Ar hi [Xr hi | Xi hi], Ar hi [Xr lo | Xi lo], Ar lo [Xr hi | Xi hi],
+          //   Ai hi [-Xi hi | Xr hi], Ai hi [-Xi lo | Xr lo], Ai lo [-Xi hi | Xr hi]
+          // i.e. Yr += Ar Xr + Ai (-Xi), Yi += Ar Xi + Ai Xr, each hi*hi + hi*lo + lo*hi, six MMAs
+          (void)ti;
+          tc_mma<L::kIdesc>(tr, ad(0), bd(1), a0);
+          tc_mma<L::kIdesc>(tr, ad(0), bd(4), 1u);
+          tc_mma<L::kIdesc>(tr, ad(1), bd(1), 1u);
+          tc_mma<L::kIdesc>(tr, ad(2), bd(0), 1u);
+          tc_mma<L::kIdesc>(tr, ad(2), bd(3), 1u);
+          tc_mma<L::kIdesc>(tr, ad(3), bd(0), 1u);
         }
       }
       issued = true;
