@@ -36,7 +36,8 @@ constexpr int KC = kRowBytes / 4;          // K elements per chunk
 constexpr int A_PLANE = BM * kRowBytes;    // bytes per A plane per chunk (16 KB)
 constexpr int B_PLANE = BN * kRowBytes;    // bytes per B plane per chunk (8 KB)
 constexpr int A_PLANES = 4;       // re_hi, re_lo, im_hi, im_lo
-constexpr int B_PLANES = 6;       // re_hi, re_lo, im_hi, im_lo, -im_hi, -im_lo
+// B slots -im_hi, re_hi, im_hi, -im_lo, re_lo, im_lo: each adjacent pair is one 2 BN-row B operand
+constexpr int B_PLANES = 6;
 constexpr int SMEM_OPS = A_PLANES * A_PLANE + B_PLANES * B_PLANE;  // 112 KB
 constexpr long long kWaitLimit = kTcWaitPolls;  // drains of copies and MMAs in flight
 constexpr int kChunks = kTcKMax / KC;  // K chunks per tile image (K up to 128)
@@ -76,8 +77,10 @@ __device__ __forceinline__ uint64_t umma_desc_sw(uint32_t saddr) {
          (uint64_t(1) << 46) | (kLayout << 61);
 }
 
-// kind::tf32, D = F32, A = B = TF32, both K-major, N = BN, M = BM.
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+// kind::tf32, D = F32, A = B = TF32, both K-major, M = BM, N = 2 BN: one A plane against two adjacent B
+// slots, into the adjacent accumulators [Cr | Ci].
+constexpr uint32_t kIdesc =
+    (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t((2 * BN) >> 3) << 17) | (uint32_t(BM >> 4) << 24);
 
 __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
   asm volatile(
@@ -163,10 +166,13 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
     uint32_t s[4];
     split4(v, s);
     const int off = sw_offset(c, kk);
-#pragma unroll
-    for (int p = 0; p < 4; ++p) *reinterpret_cast<uint32_t*>(base + size_t(p) * B_PLANE + off) = s[p];
-    *reinterpret_cast<uint32_t*>(base + size_t(4) * B_PLANE + off) = s[2] ^ 0x80000000u;  // -im_hi
-    *reinterpret_cast<uint32_t*>(base + size_t(5) * B_PLANE + off) = s[3] ^ 0x80000000u;  // -im_lo
+    auto put = [&](int slot, uint32_t x) { *reinterpret_cast<uint32_t*>(base + size_t(slot) * B_PLANE + off) = x; };
+    put(0, s[2] ^ 0x80000000u);  // -im_hi
+    put(1, s[0]);                // re_hi
+    put(2, s[2]);                // im_hi
+    put(3, s[3] ^ 0x80000000u);  // -im_lo
+    put(4, s[1]);                // re_lo
+    put(5, s[3]);                // im_lo
   }
 }
 
@@ -177,7 +183,7 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
 // (t -> matrix b, row tile bm, column tile bn, bn fastest).  Roles:
 //   warp 0   producer: bulk-copies each K-chunk (112 KB of planes) into a
 //            two-stage ring, waiting for the stage to be released;
-//   warp 1   MMA: 48 tcgen05.mma per chunk into one of four TMEM accumulators
+//   warp 1   MMA: 24 tcgen05.mma (N = 128: [Cr | Ci]) per chunk into one of four TMEM accumulators
 //            (128 columns each), releasing the stage with tcgen05.commit and
 //            signalling the tile's accumulator the same way;
 //   warps 2-17   four epilogue groups of four warps, group g taking the tiles
@@ -346,20 +352,16 @@ __global__ void __launch_bounds__(kPThreads, 1) tc_update_persistent_kernel(
             auto ad = [&](int p) { return umma_desc_sw(sA + p * A_PLANE + koff); };
             auto bd = [&](int p) { return umma_desc_sw(sB + p * B_PLANE + koff); };
             const uint32_t acc0 = (ch == 0 && ks == 0) ? 0u : 1u;
-            // Cr += Ar Br + Ai (-Bi)
-            mma_tf32(tmem_r, ad(0), bd(0), acc0);
-            mma_tf32(tmem_r, ad(0), bd(1), 1u);
-            mma_tf32(tmem_r, ad(1), bd(0), 1u);
-            mma_tf32(tmem_r, ad(2), bd(4), 1u);
-            mma_tf32(tmem_r, ad(2), bd(5), 1u);
-            mma_tf32(tmem_r, ad(3), bd(4), 1u);
-            // Ci += Ar Bi + Ai Br
-            mma_tf32(tmem_i, ad(0), bd(2), acc0);
-            mma_tf32(tmem_i, ad(0), bd(3), 1u);
-            mma_tf32(tmem_i, ad(1), bd(2), 1u);
-            mma_tf32(tmem_i, ad(2), bd(0), 1u);
-            mma_tf32(tmem_i, ad(2), bd(1), 1u);
-            mma_tf32(tmem_i, ad(3), bd(0), 1u);
+            // [Cr | Ci] += Ar hi [Br hi | Bi hi] + Ar hi [Br lo | Bi lo] + Ar lo [Br hi | Bi hi]
+            //            + Ai hi [-Bi hi | Br hi] + Ai hi [-Bi lo | Br lo] + Ai lo [-Bi hi | Br hi],
+            // i.e. Cr += Ar Br + Ai (-Bi), Ci += Ar Bi + Ai Br, each hi*hi + hi*lo + lo*hi
+            (void)tmem_i;
+            mma_tf32(tmem_r, ad(0), bd(1), acc0);
+            mma_tf32(tmem_r, ad(0), bd(4), 1u);
+            mma_tf32(tmem_r, ad(1), bd(1), 1u);
+            mma_tf32(tmem_r, ad(2), bd(0), 1u);
+            mma_tf32(tmem_r, ad(2), bd(3), 1u);
+            mma_tf32(tmem_r, ad(3), bd(0), 1u);
           }
           issued = true;
           umma_commit(bar(kBarEmpty + st));  // the stage is free once these MMAs have read it
