@@ -153,6 +153,14 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     the same; 0 on the FP32 CUDA cores.  A product whose bounded wait gives
  *     up hands its matrices to the refined LU. */
 #define REFEFF_FMS_OPT_BICG_TENSOR 8
+/*   REFEFF_FMS_OPT_RESIDUAL_TENSOR: 1 (default) computes the refinement
+ *     residual r = b - A x of the FP32 LU forms on the tensor cores (exact
+ *     products of 8-bit digits of A and x on the bf16 path, summed in
+ *     double-float; up to 16 right-hand sides, with the tensor-core update on);
+ *     0 in double-float on the FP32 CUDA cores.  Both reach about 2^-46 of
+ *     sum |a||x|.  A residual whose bounded wait gives up sends the call's
+ *     energies to the FP64 LU. */
+#define REFEFF_FMS_OPT_RESIDUAL_TENSOR 9
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);
 /* How often the context captured and replayed the many-cluster graph. */
 int refeff_fms_context_graph_stats(const refeff_fms_context* ctx, long long* captures, long long* replays);

@@ -19,7 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "build"
 LIB = BUILD / "librefeff_fms.so"
-SOURCES = ["g0t_build.cu", "batched_lu.cu", "tc_update.cu", "fms_host.cu", "fms_files.cu", "noalloc.cu", "mkgtr.cu", "iterative.cu", "sweeps.cu", "debye.cu", "bicgstab.cu", "precond_mlp.cu", "ff2x.cu", "feff_inp.cu", "autotune.cu"]
+SOURCES = ["g0t_build.cu", "batched_lu.cu", "tc_update.cu", "fms_host.cu", "fms_files.cu", "noalloc.cu", "mkgtr.cu", "iterative.cu", "sweeps.cu", "debye.cu", "bicgstab.cu", "precond_mlp.cu", "ff2x.cu", "feff_inp.cu", "autotune.cu", "tc_residual.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -1182,7 +1182,8 @@ static void launch_residual_df(const BatchLayout& lay, int batch, const float4* 
 
 void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
                      double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
-                     cudaStream_t s) {
+                     cudaStream_t s, const ResidualTc* tc) {
+  if (tc && launch_residual_tc(lay, batch, Ms, X64, *tc, R, rnorm_bits, bnorm_bits, skip, s)) return;
   {
     dim3 grid(unsigned(min(64, (lay.n * lay.m + 255) / 256)), unsigned(batch));
     count_launch();

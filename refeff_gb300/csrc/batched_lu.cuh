@@ -124,9 +124,26 @@ bool fused_backward_sweep(int nb, const BatchLayout& lay, int batch, float2* M, 
 // sides fit in shared memory).
 bool fused_sweep_available(int nb, const BatchLayout& lay);
 
+// The refinement residual on the tensor cores (tc_residual.cu): scratch for the
+// digit slots of X (the tensor-core update's operand images, unused while the
+// residual runs), the error flag a timed-out wait raises, the role-wait budget.
+struct ResidualTc {
+  uint8_t* images = nullptr;
+  size_t bytes = 0;
+  int* err = nullptr;
+  long long polls = kTcWaitPolls;
+};
+size_t residual_tc_image_bytes(int n, int batch);
+// R = B - A X (A, B as hi/lo float4, X FP64) from exact digit products on the
+// bf16 tensor path; false (nothing launched) when m > 16 or the scratch is short.
+bool launch_residual_tc(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, const ResidualTc& tc,
+                        double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
+                        cudaStream_t s);
+// R = B - A X and max |r|, max |b| per system: on the tensor cores when tc is
+// given and serves the shape, else in double-float (Dot2) on the FP32 pipes.
 void launch_residual(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, float4* Xsplit,
                      double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
-                     cudaStream_t s);
+                     cudaStream_t s, const ResidualTc* tc = nullptr);
 // In place: M (double2 entries) -> hi/lo float4 entries, M32 <- hi (for the dense solve API).
 void launch_split_system(const BatchLayout& lay, int batch, double2* M, float2* M32, cudaStream_t s);
 // RHS columns of M32 <- float(R / rnorm_b)

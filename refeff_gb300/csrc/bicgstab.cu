@@ -371,8 +371,12 @@ __global__ void __launch_bounds__(kTcThreads) bicg_tc_matvec_kernel(View w, cons
                                                                      const int* skip, int* err, long long polls) {
   using L = TcMv<N, k3M>;
   const int b = w.matrix();
-  // uniform over the CTA, before any tensor memory is taken; a raised error skips the product
-  if (b < 0 || (skip && skip[b]) || w.done[b] || *reinterpret_cast<volatile int*>(err)) return;
+  // decided once for the whole CTA (another CTA may raise the error flag meanwhile), before any tensor
+  // memory is taken; a raised error skips the product
+  __shared__ int go;
+  if (threadIdx.x == 0) go = !(b < 0 || (skip && skip[b]) || w.done[b] || *reinterpret_cast<volatile int*>(err));
+  __syncthreads();
+  if (!go) return;
   extern __shared__ uint8_t tsm[];
   const uint32_t raw = tc_smem_u32(tsm);
   const uint32_t sbase = (raw + 1023u) & ~1023u;

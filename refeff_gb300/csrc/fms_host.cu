@@ -107,6 +107,7 @@ struct refeff_fms_context {
   int multi_streams = 4;     // REFEFF_FMS_OPT_MULTI_STREAMS
   int dual_streams = 1;      // REFEFF_FMS_OPT_DUAL_STREAMS
   int bicg_tensor = 1;       // REFEFF_FMS_OPT_BICG_TENSOR
+  int residual_tensor = 1;   // REFEFF_FMS_OPT_RESIDUAL_TENSOR
   std::vector<cudaStream_t> pool;  // extra streams for the multi-cluster spectrum (created on first use)
   std::vector<cudaEvent_t> pool_join;  // one per pool stream: joins it back into a capture
   cudaEvent_t fork_ev = nullptr;
@@ -140,6 +141,7 @@ extern "C" int refeff_fms_context_set_option(refeff_fms_context* ctx, int option
       ctx->bicg_tensor = int(value);
       return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_TENSOR_CORES: ctx->use_tensor_cores = value != 0; return REFEFF_FMS_OK;
+    case REFEFF_FMS_OPT_RESIDUAL_TENSOR: ctx->residual_tensor = value != 0; return REFEFF_FMS_OK;
     case REFEFF_FMS_OPT_DENSE_REFINEMENT:
       if (value < 0 || value > 1000) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
       ctx->dense_refinement = int(value);
@@ -429,7 +431,9 @@ struct Workspace {
   DevBuf<double> relres;
   DevBuf<int> ipiv, nperm, status, info;
   bool use_tc = false;               // FP32 trailing update on the tensor cores
-  DevBuf<uint8_t> tc_images;         // operand images of the tensor-core update
+  DevBuf<uint8_t> tc_images;         // operand images of the tensor-core update (and the residual's X digits)
+  size_t tc_image_size = 0;
+  int residual_pref = 1;             // refinement residual on the tensor cores (baked into graphs)
   DevBuf<int> tc_err;                // set by a tensor-core wait that timed out
   long long tc_wait_polls = kTcWaitPolls;  // poll budget of the tensor-core update's role waits (baked into graphs)
   KernelSpans tc_spans;              // events around this workspace's tensor-core updates (profiling)
@@ -861,6 +865,10 @@ int ensure_workspace_impl(refeff_fms_context* ctx, Workspace& ws, int n, int m, 
     ws.drop_graphs();
     ws.tc_wait_polls = ctx->tc_wait_polls;
   }
+  if (ws.residual_pref != ctx->residual_tensor) {  // the residual's launch sequence changes: recapture
+    ws.drop_graphs();
+    ws.residual_pref = ctx->residual_tensor;
+  }
   const int inner = tune ? tune->inner : 0;
   ws.paired_pref = tune && tune->paired >= 0 ? tune->paired : ctx->paired_blocks;
   if (ws.batch >= batch && ws.lay.n == n && ws.lay.m == m && (ws.fp32 || !fp32) && ws.inner_pref == inner) {
@@ -912,7 +920,8 @@ int ensure_workspace_impl(refeff_fms_context* ctx, Workspace& ws, int n, int m, 
   RF_CUDA(ctx, ws.info.alloc(size_t(B)));
   ws.use_tc = ws.fp32 && ctx->use_tensor_cores != 0;
   if (ws.use_tc) {
-    RF_CUDA(ctx, ws.tc_images.alloc(tc_image_bytes(n, m, B)));
+    ws.tc_image_size = tc_image_bytes(n, m, B);
+    RF_CUDA(ctx, ws.tc_images.alloc(ws.tc_image_size));
     RF_CUDA(ctx, ws.tc_err.alloc(1));
     RF_CUDA(ctx, cudaMemset(ws.tc_err.p, 0, sizeof(int)));
   }
@@ -967,7 +976,19 @@ using Spans = std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>>;
 // |d| <= tol |x| (converged[b] = 1) or when |d| stops halving (converged[b] = 2,
 // handed to the FP64 LU by the caller).  With `spans`, events bracket the
 // sweeps (phase 2) and the residuals (phase 3).
+// The tensor-core residual's arguments when the workspace runs it (the
+// tensor-core update's images hold its scratch), else null: the Dot2 residual.
+const ResidualTc* residual_tc(const Workspace& ws, ResidualTc& out) {
+  if (!ws.use_tc || !ws.residual_pref || !ws.tc_images.p) return nullptr;
+  out.images = ws.tc_images.p;
+  out.bytes = ws.tc_image_size;
+  out.err = ws.tc_err.p;
+  out.polls = ws.tc_wait_polls;
+  return &out;
+}
+
 cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStream_t s, Spans* spans = nullptr) {
+  ResidualTc rtc;
   const BatchLayout& lay = ws.lay;
   const LuWork w32 = lu_work(ws, ws.pc32);
   auto span = [&](int phase, auto&& fn) {
@@ -1004,7 +1025,7 @@ cudaError_t refine_fp32(Workspace& ws, int batch, int iters, double tol, cudaStr
       cudaMemsetAsync(ws.rnorm.p, 0, nb8, s);
       cudaMemsetAsync(ws.bnorm.p, 0, nb8, s);
       launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.Xsplit.p, ws.R.p, ws.rnorm.p,
-                      ws.bnorm.p, ws.converged.p, s);
+                      ws.bnorm.p, ws.converged.p, s, residual_tc(ws, rtc));
     });
     span(2, [&] {
       cudaMemsetAsync(ws.dnorm.p, 0, nb8, s);
@@ -1049,6 +1070,7 @@ cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, const Blo
                             int max_iter, double inner_tol, int poll, int tensor, cudaStream_t s,
                             Spans* spans = nullptr) {
   const BatchLayout& lay = ws.lay;
+  ResidualTc rtc;
   BicgWork w = bicg_work(ws);
   w.tensor = tensor;
   auto span = [&](int phase, auto&& fn) -> cudaError_t {
@@ -1087,7 +1109,7 @@ cudaError_t refine_bicgstab(Workspace& ws, int batch, const float2* D, const Blo
       cudaMemsetAsync(ws.rnorm.p, 0, nb8, s);
       cudaMemsetAsync(ws.bnorm.p, 0, nb8, s);
       launch_residual(lay, batch, reinterpret_cast<const float4*>(ws.M64.p), ws.X64.p, ws.Xsplit.p, ws.R.p, ws.rnorm.p,
-                      ws.bnorm.p, ws.converged.p, s);
+                      ws.bnorm.p, ws.converged.p, s, residual_tc(ws, rtc));
       return cudaGetLastError();
     });
     e = span(1, [&] {

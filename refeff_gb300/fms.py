@@ -216,6 +216,7 @@ class Context:
     OPT_DUAL_STREAMS = 6
     OPT_MULTI_GRAPH = 7
     OPT_BICG_TENSOR = 8
+    OPT_RESIDUAL_TENSOR = 9
 
     def set_option(self, option: int, value: int):
         """Context option (applies to plans / dense solves started afterwards)."""
