@@ -86,16 +86,14 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
   extern __shared__ __align__(16) unsigned char smraw[];
   C* pan = reinterpret_cast<C*>(smraw);
   C* urow = pan + size_t(NB) * rpc_max;
-  ArgSlot<T>* slot = reinterpret_cast<ArgSlot<T>*>(urow + NB);
-  int* done = reinterpret_cast<int*>(slot + 2);
+  int* done = reinterpret_cast<int*>(reinterpret_cast<ArgSlot<T>*>(urow + NB) + 2);  // after two reserved slots
   // row-position bookkeeping (rank 0): shared memory, or global scratch for large n
   const bool pos_global = w.pos_scratch != nullptr;
   int* row2pos = pos_global ? w.pos_scratch + size_t(b) * 2 * n : done + rpc_max;
   int* pos2row = row2pos + n;
-  int* scratch = pos_global ? done + rpc_max : pos2row + n;  // [0] winner row, [2] move count
-  __shared__ T red_v[kPanelThreads / 32];
-  __shared__ int red_r[kPanelThreads / 32];
-  __shared__ T win_v;
+  int* scratch = pos_global ? done + rpc_max : pos2row + n;  // [2] move count
+  // per-warp arg-max slots, double-buffered by column parity
+  __shared__ ArgSlot<T> wslot[2][kPanelThreads / 32];
 
   C* Mb = M + size_t(b) * lay.stride;
   for (int idx = tid; idx < nloc * kb; idx += nthr) {
@@ -109,53 +107,47 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
   }
   __syncthreads();
 
+  // Each thread keeps the same rows (r = tid, tid + nthr, ...) for the whole
+  // panel, so their done flags are its own and the arg-max of column j + 1 is
+  // taken while column j's update writes it.  Per column: one cluster barrier
+  // (every warp has published its arg-max), one CTA barrier (the pivot row is
+  // in shared memory).  Ties go to the lowest row, so the pivots do not depend
+  // on the reduction order.
+  const int nw = nthr / 32;
+  T best = T(-1);
+  int brow = INT_MAX;
+  for (int r = tid; r < nloc; r += nthr) {
+    T v = cabs1(pan[r]);
+    if (!(v >= T(0))) v = T(0);  // a NaN entry competes as zero, so a valid row is always chosen
+    argmax_merge(best, brow, v, row_lo + r);
+  }
   for (int j = 0; j < kb; ++j) {
-    // local arg-max of column j over rows not yet used as pivots
-    T best = T(-1);
-    int brow = INT_MAX;
-    for (int r = tid; r < nloc; r += nthr) {
-      if (done[r]) continue;
-      T v = cabs1(pan[size_t(j) * rpc_max + r]);
-      if (!(v >= T(0))) v = T(0);  // a NaN entry competes as zero, so a valid row is always chosen
-      argmax_merge(best, brow, v, row_lo + r);
-    }
     for (int off = 16; off > 0; off >>= 1) {
       const T ov = __shfl_down_sync(0xffffffffu, best, off);
       const int orow = __shfl_down_sync(0xffffffffu, brow, off);
       argmax_merge(best, brow, ov, orow);
     }
-    if (lane == 0) { red_v[wid] = best; red_r[wid] = brow; }
-    __syncthreads();
-    if (tid == 0) {
-      T v = red_v[0];
-      int r = red_r[0];
-      for (int q = 1; q < nthr / 32; ++q) argmax_merge(v, r, red_v[q], red_r[q]);
-      slot[j & 1].val = v;
-      slot[j & 1].row = r;
+    if (lane == 0) {
+      wslot[j & 1][wid].val = best;
+      wslot[j & 1][wid].row = brow;
     }
     cluster.sync();
-    // cluster arg-max over DSMEM
-    if (wid == 0) {
-      T v = T(-1);
-      int r = INT_MAX;
-      if (lane < CL) {
-        const ArgSlot<T>* rs = cluster.map_shared_rank(slot, lane);
-        v = rs[j & 1].val;
-        r = rs[j & 1].row;
-      }
-      for (int off = 16; off > 0; off >>= 1) {
-        const T ov = __shfl_down_sync(0xffffffffu, v, off);
-        const int orow = __shfl_down_sync(0xffffffffu, r, off);
-        argmax_merge(v, r, ov, orow);
-      }
-      if (lane == 0) { scratch[0] = r; win_v = v; }
+    // every warp reduces the cluster's slots over DSMEM; the butterfly leaves the winner in every lane
+    T wv = T(-1);
+    int wrow = INT_MAX;
+    for (int q = lane; q < CL * nw; q += 32) {
+      const ArgSlot<T>* rs = cluster.map_shared_rank(&wslot[j & 1][0], q / nw);
+      argmax_merge(wv, wrow, rs[q % nw].val, rs[q % nw].row);
     }
-    __syncthreads();
-    const int wrow = scratch[0];
+    for (int off = 16; off > 0; off >>= 1) {
+      const T ov = __shfl_xor_sync(0xffffffffu, wv, off);
+      const int orow = __shfl_xor_sync(0xffffffffu, wrow, off);
+      argmax_merge(wv, wrow, ov, orow);
+    }
     const int owner = wrow / rpc, lr = wrow % rpc;
     const C* opan = cluster.map_shared_rank(pan, owner);
     for (int c = j + tid; c < kb; c += nthr) urow[c] = opan[size_t(c) * rpc_max + lr];
-    if (rank == owner && tid == 0) done[lr] = 1;
+    if (rank == owner && tid == lr % nthr) done[lr] = 1;
     if (rank == 0 && tid == 0) {
       const int q = row2pos[wrow];
       const int pj = pos2row[j];
@@ -164,21 +156,28 @@ __global__ void __launch_bounds__(kPanelThreads) panel_kernel(BatchLayout lay, i
       row2pos[wrow] = j;
       row2pos[pj] = q;
       w.ipiv[size_t(b) * n + k + j] = k + q;
-      if (!(win_v > T(0))) {
+      if (!(wv > T(0))) {
         atomicMax(w.status + b, int(kDevSingular));
         atomicCAS(w.info + b, 0, k + j + 1);
       }
     }
     __syncthreads();
-    // multipliers and rank-1 update of own rows
+    // multipliers, rank-1 update of own rows, and the local arg-max of column j + 1
     const C pv = urow[j];
     const bool zero_pivot = !(cabs1(pv) > T(0));
+    best = T(-1);
+    brow = INT_MAX;
     for (int r = tid; r < nloc; r += nthr) {
       if (done[r]) continue;
       C l = pan[size_t(j) * rpc_max + r];
       l = zero_pivot ? mk<T>(T(0), T(0)) : cdiv(l, pv);
       pan[size_t(j) * rpc_max + r] = l;
       for (int c = j + 1; c < kb; ++c) cfms(pan[size_t(c) * rpc_max + r], l, urow[c]);
+      if (j + 1 < kb) {
+        T v = cabs1(pan[size_t(j + 1) * rpc_max + r]);
+        if (!(v >= T(0))) v = T(0);
+        argmax_merge(best, brow, v, row_lo + r);
+      }
     }
   }
   cluster.sync();
