@@ -16,7 +16,7 @@
 //     with FP32 accumulation sums the products of one level s = i + j (digit i
 //     of A times digit j of X) without rounding as long as every partial sum
 //     stays below 2^24: at most 6 pairs x 2 real products x 32 columns x 2^14
-//     = 2^23.6 per level and segment.
+//     = 2^22.6 per level and segment.
 //
 // Levels 2 .. 8 are kept (26 digit pairs; a dropped pair weighs at most 2^-54
 // of the scales).  After each segment the seven exact level sums are combined
