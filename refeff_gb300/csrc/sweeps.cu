@@ -26,31 +26,72 @@ struct SweepSmem {
 };
 
 // Y[r] -= sum_j T(r, j) X[j] for rows [r_begin, r_end), j < kb, T column j at
-// Mb + lda (c0 + j); kSwUnroll loads in flight per thread.
+// Mb + lda (c0 + j).  Each thread walks its rows (r_begin + tid + q kSwThreads)
+// in batches of kSwUnroll columns and loads the next batch (of the same row or
+// of its next row) before it multiplies the current one, so that the loads of
+// one batch are in flight while the previous batch is computed.
 template <int CG>
 __device__ __forceinline__ void sweep_update(const float2* __restrict__ Mb, size_t lda, int c0, int kb, int r_begin,
                                              int r_end, const float2* X, float2* Y) {
-  for (int r = r_begin + int(threadIdx.x); r < r_end; r += kSwThreads) {
-    float2 acc[CG];
+  const int nfull = kb / kSwUnroll;
+  if (nfull == 0) {  // a narrow last block: one column at a time
+    for (int r = r_begin + int(threadIdx.x); r < r_end; r += kSwThreads) {
+      float2 acc[CG];
 #pragma unroll
-    for (int c = 0; c < CG; ++c) acc[c] = make_float2(0.f, 0.f);
-    int j = 0;
-    for (; j + kSwUnroll <= kb; j += kSwUnroll) {
-      float2 l[kSwUnroll];
+      for (int c = 0; c < CG; ++c) acc[c] = make_float2(0.f, 0.f);
+      for (int j = 0; j < kb; ++j) {
+        const float2 l = Mb[size_t(r) + lda * size_t(c0 + j)];
 #pragma unroll
-      for (int u = 0; u < kSwUnroll; ++u) l[u] = Mb[size_t(r) + lda * size_t(c0 + j + u)];
+        for (int c = 0; c < CG; ++c) cfma(acc[c], l, X[j * CG + c]);
+      }
 #pragma unroll
-      for (int u = 0; u < kSwUnroll; ++u)
-#pragma unroll
-        for (int c = 0; c < CG; ++c) cfma(acc[c], l[u], X[(j + u) * CG + c]);
+      for (int c = 0; c < CG; ++c) Y[r * CG + c] = csub(Y[r * CG + c], acc[c]);
     }
-    for (; j < kb; ++j) {
-      const float2 l = Mb[size_t(r) + lda * size_t(c0 + j)];
+    return;
+  }
+  int r = r_begin + int(threadIdx.x);
+  if (r >= r_end) return;
+  auto load = [&](int rr, int bb, float2 (&v)[kSwUnroll]) {
 #pragma unroll
-      for (int c = 0; c < CG; ++c) cfma(acc[c], l, X[j * CG + c]);
+    for (int u = 0; u < kSwUnroll; ++u) v[u] = Mb[size_t(rr) + lda * size_t(c0 + bb * kSwUnroll + u)];
+  };
+  float2 acc[CG];
+#pragma unroll
+  for (int c = 0; c < CG; ++c) acc[c] = make_float2(0.f, 0.f);
+  float2 cur[kSwUnroll];
+  load(r, 0, cur);
+  int bi = 0;
+  for (;;) {
+    int rn = r, bn = bi + 1;
+    if (bn == nfull) {
+      rn = r + kSwThreads;
+      bn = 0;
     }
+    const bool more = rn < r_end;
+    float2 nxt[kSwUnroll];
+    if (more) load(rn, bn, nxt);
+    const int j0 = bi * kSwUnroll;
 #pragma unroll
-    for (int c = 0; c < CG; ++c) Y[r * CG + c] = csub(Y[r * CG + c], acc[c]);
+    for (int u = 0; u < kSwUnroll; ++u)
+#pragma unroll
+      for (int c = 0; c < CG; ++c) cfma(acc[c], cur[u], X[(j0 + u) * CG + c]);
+    if (bn == 0) {  // row r done with its full batches: the remaining columns, then the row
+      for (int j = nfull * kSwUnroll; j < kb; ++j) {
+        const float2 l = Mb[size_t(r) + lda * size_t(c0 + j)];
+#pragma unroll
+        for (int c = 0; c < CG; ++c) cfma(acc[c], l, X[j * CG + c]);
+      }
+#pragma unroll
+      for (int c = 0; c < CG; ++c) {
+        Y[r * CG + c] = csub(Y[r * CG + c], acc[c]);
+        acc[c] = make_float2(0.f, 0.f);
+      }
+    }
+    if (!more) break;
+    r = rn;
+    bi = bn;
+#pragma unroll
+    for (int u = 0; u < kSwUnroll; ++u) cur[u] = nxt[u];
   }
 }
 
@@ -143,6 +184,7 @@ __global__ void __launch_bounds__(kSwThreads) bwd_sweep_kernel(BatchLayout lay, 
   extern __shared__ float2 sw_sm[];
   float2* Y = sw_sm;
   float2* T = Y + size_t(n) * CG;
+  float2* dinv = T + NB * (NB + 1);  // reciprocals of the block's diagonal (0 for a zero pivot)
   float2* Mb = M + size_t(b) * lay.stride;
   const size_t lda = size_t(lay.lda);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -155,7 +197,9 @@ __global__ void __launch_bounds__(kSwThreads) bwd_sweep_kernel(BatchLayout lay, 
     const int kb = min(NB, n - k);
     for (int idx = tid; idx < kb * kb; idx += kSwThreads) {
       const int r = idx % kb, c = idx / kb;
-      T[r * (NB + 1) + c] = Mb[size_t(k + r) + lda * size_t(k + c)];
+      const float2 v = Mb[size_t(k + r) + lda * size_t(k + c)];
+      T[r * (NB + 1) + c] = v;
+      if (r == c) dinv[r] = (v.x == 0.f && v.y == 0.f) ? make_float2(0.f, 0.f) : cdiv(make_float2(1.f, 0.f), v);
     }
     __syncthreads();
     if (wid < ncols) {
@@ -170,10 +214,7 @@ __global__ void __launch_bounds__(kSwThreads) bwd_sweep_kernel(BatchLayout lay, 
         const int ot = p >> 5, ol = p & 31;
 #pragma unroll
         for (int t = 0; t < kR; ++t)
-          if (t == ot && lane == ol) {
-            const float2 d = T[p * (NB + 1) + p];
-            x[t] = (d.x == 0.f && d.y == 0.f) ? make_float2(0.f, 0.f) : cdiv(x[t], d);
-          }
+          if (t == ot && lane == ol) x[t] = cmul(x[t], dinv[p]);
         float2 xp = make_float2(0.f, 0.f);
 #pragma unroll
         for (int t = 0; t < kR; ++t) {
