@@ -870,14 +870,19 @@ static cudaError_t launch_panel(const PanelConfig& pc, const BatchLayout& lay, i
     err = ensure_nonportable_clusters(reinterpret_cast<const void*>(kern));
     if (err != cudaSuccess) return err;
   }
+  // the trailing rows shrink as k grows: the smallest cluster whose CTAs still hold them (same
+  // shared memory, rpc_max rows each), so that late panels pay fewer or no cluster barriers
+  int cl = pc.cluster;
+  const int R = lay.n - k;
+  while (cl > 1 && (R + cl / 2 - 1) / (cl / 2) <= pc.rpc_max) cl /= 2;
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(unsigned(pc.cluster), unsigned(batch), 1);
+  cfg.gridDim = dim3(unsigned(cl), unsigned(batch), 1);
   cfg.blockDim = dim3(kPanelThreads, 1, 1);
   cfg.dynamicSmemBytes = size_t(pc.smem);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = unsigned(pc.cluster);
+  attr[0].val.clusterDim.x = unsigned(cl);
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
