@@ -156,7 +156,8 @@ unsigned long long refeff_fms_kernel_launches(void);
 /*   REFEFF_FMS_OPT_RESIDUAL_TENSOR: 1 (default) computes the refinement
  *     residual r = b - A x of the FP32 LU forms on the tensor cores (exact
  *     products of 8-bit digits of A and x on the bf16 path, summed in
- *     double-float; up to 16 right-hand sides, with the tensor-core update on);
+ *     double-float, one pass per 16 right-hand sides; with the tensor-core
+ *     update on);
  *     0 in double-float on the FP32 CUDA cores.  Both reach about 2^-46 of
  *     sum |a||x|.  A residual whose bounded wait gives up sends the call's
  *     energies to the FP64 LU. */

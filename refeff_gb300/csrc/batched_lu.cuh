@@ -135,7 +135,8 @@ struct ResidualTc {
 };
 size_t residual_tc_image_bytes(int n, int batch);
 // R = B - A X (A, B as hi/lo float4, X FP64) from exact digit products on the
-// bf16 tensor path; false (nothing launched) when m > 16 or the scratch is short.
+// bf16 tensor path, one pass per 16 right-hand sides; false (nothing launched)
+// when the scratch is short.
 bool launch_residual_tc(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, const ResidualTc& tc,
                         double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
                         cudaStream_t s);

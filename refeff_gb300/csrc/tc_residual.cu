@@ -24,7 +24,7 @@
 // to a double-float accumulator per output; the column's power of two is
 // applied at the end.
 //
-// One CTA per (128 rows, system), 10 warps:
+// One pass per 16 right-hand sides; per pass one CTA per (128 rows, system), 10 warps:
 //   warps 0-7  load their rows of A (two threads per row, 16 columns each), cut
 //              the digits into 12 bf16 planes (re / im x 6 digits; 128 rows x
 //              16 columns, K-major, 32-byte swizzle) of a three-stage ring,
@@ -55,7 +55,7 @@ constexpr int kRtDigits = 6;
 constexpr int kRtStages = 3;
 constexpr int kRtWorkerWarps = 8;
 constexpr int kRtThreads = 32 * (kRtWorkerWarps + 2);
-constexpr int kRtCols = 16;                               // right-hand sides per system (m <= 16)
+constexpr int kRtCols = 16;                               // right-hand sides per pass
 constexpr int kRtAPlane = kRtRows * kRtK * 2;             // 4 KB: 128 rows of 16 bf16
 constexpr int kRtA = 2 * kRtDigits * kRtAPlane;           // 48 KB
 constexpr int kRtSlot = 2 * kRtCols * kRtK * 2;           // 1 KB: 32 rows of 16 bf16
@@ -193,16 +193,17 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 // The column scales tau_c (powers of two, max |x| < tau_c) follow the slots.
 __global__ void __launch_bounds__(512) residual_x_image_kernel(BatchLayout lay, const double2* __restrict__ X64,
                                                                 uint8_t* __restrict__ ximg, float* __restrict__ tau,
-                                                                int nseg, const int* skip, int* err) {
+                                                                int nseg, int c0, const int* skip, int* err) {
   const int b = blockIdx.x;
   if (skip && skip[b]) return;
   __shared__ unsigned long long cmax[kRtCols];
   __shared__ double tinv[kRtCols];
-  const int n = lay.n, m = lay.m, tid = threadIdx.x;
-  const double2* X = X64 + size_t(b) * lay.lda * m;
+  // columns c0 .. c0 + mc - 1 of X in this pass
+  const int n = lay.n, mc = min(kRtCols, lay.m - c0), tid = threadIdx.x;
+  const double2* X = X64 + size_t(b) * lay.lda * lay.m + size_t(lay.lda) * c0;
   if (tid < kRtCols) cmax[tid] = 0ull;
   __syncthreads();
-  for (int idx = tid; idx < n * m; idx += blockDim.x) {
+  for (int idx = tid; idx < n * mc; idx += blockDim.x) {
     const int r = idx % n, c = idx / n;
     const double2 v = X[size_t(r) + size_t(lay.lda) * c];
     const double a = fmax(fabs(v.x), fabs(v.y));
@@ -232,7 +233,7 @@ __global__ void __launch_bounds__(512) residual_x_image_kernel(BatchLayout lay, 
 #pragma unroll
       for (int v = 0; v < 2; ++v) {
         const int k = g * kRtK + ch * 8 + u + v;
-        double2 x = (c < m && k < n) ? X[size_t(k) + size_t(lay.lda) * c] : make_double2(0.0, 0.0);
+        double2 x = (c < mc && k < n) ? X[size_t(k) + size_t(lay.lda) * c] : make_double2(0.0, 0.0);
         x.x *= tinv[c];
         x.y *= tinv[c];
         const float rh = float(x.x), ih = float(x.y);
@@ -265,7 +266,7 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* p, double 
 
 __global__ void __launch_bounds__(kRtThreads, 1)
     residual_tc_kernel(BatchLayout lay, const float4* __restrict__ Ms, const uint8_t* __restrict__ ximg,
-                       const float* __restrict__ tau, int nseg, double2* __restrict__ R, unsigned long long* rnorm,
+                       const float* __restrict__ tau, int nseg, int c0, double2* __restrict__ R, unsigned long long* rnorm,
                        unsigned long long* bnorm, const int* skip, int* err, long long polls) {
   const int b = blockIdx.y;
   // decided once for the whole CTA (another CTA may raise the error flag meanwhile), before any tensor
@@ -284,7 +285,8 @@ __global__ void __launch_bounds__(kRtThreads, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(meta + 128);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(meta + 132);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n = lay.n, m = lay.m, r0 = blockIdx.x * kRtRows;
+  // right-hand sides c0 .. c0 + mc - 1 in this pass
+  const int n = lay.n, mc = min(kRtCols, lay.m - c0), r0 = blockIdx.x * kRtRows;
   const float4* A = Ms + size_t(b) * lay.stride;
 
   if (warp == kRtWorkerWarps + 1) {
@@ -449,15 +451,15 @@ __global__ void __launch_bounds__(kRtThreads, 1)
       const int row = r0 + erow;
       double rmax = 0.0, bmax = 0.0;
       if (row < n) {
-        double2* Rb = R + size_t(b) * lay.lda * m;
+        double2* Rb = R + size_t(b) * lay.lda * lay.m + size_t(lay.lda) * c0;
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int c = 8 * hw + u;
-          if (c >= m) continue;
+          if (c >= mc) continue;
           const double t = double(tau[size_t(b) * kRtCols + c]);
           const double ax = (double(acc_r[u].hi) + double(acc_r[u].lo)) * t;
           const double ay = (double(acc_i[u].hi) + double(acc_i[u].lo)) * t;
-          const double2 bv = join_hi_lo(A[size_t(row) + size_t(lay.lda) * (n + c)]);
+          const double2 bv = join_hi_lo(A[size_t(row) + size_t(lay.lda) * (n + c0 + c)]);
           const double2 rv = make_double2(bv.x - ax, bv.y - ay);
           Rb[size_t(row) + size_t(lay.lda) * c] = rv;
           rmax = fmax(rmax, cabs1(rv));
@@ -545,18 +547,21 @@ size_t residual_tc_image_bytes(int n, int batch) {
 bool launch_residual_tc(const BatchLayout& lay, int batch, const float4* Ms, const double2* X64, const ResidualTc& tc,
                         double2* R, unsigned long long* rnorm_bits, unsigned long long* bnorm_bits, const int* skip,
                         cudaStream_t s) {
-  if (lay.m < 1 || lay.m > kRtCols || !tc.images || !tc.err || residual_tc_image_bytes(lay.n, batch) > tc.bytes)
-    return false;
+  if (lay.m < 1 || !tc.images || !tc.err || residual_tc_image_bytes(lay.n, batch) > tc.bytes) return false;
   if (ensure_smem_limit(reinterpret_cast<const void*>(residual_tc_kernel), size_t(kRtSmem)) != cudaSuccess)
     return false;
   const int nseg = (lay.n + kRtSeg - 1) / kRtSeg;
   float* tau = reinterpret_cast<float*>(tc.images + size_t(batch) * size_t(2 * nseg) * kRtImage);
-  count_launch();
-  residual_x_image_kernel<<<unsigned(batch), 512, 0, s>>>(lay, X64, tc.images, tau, nseg, skip, tc.err);
   dim3 grid(unsigned((lay.n + kRtRows - 1) / kRtRows), unsigned(batch));
-  count_launch();
-  residual_tc_kernel<<<grid, kRtThreads, kRtSmem, s>>>(lay, Ms, tc.images, tau, nseg, R, rnorm_bits, bnorm_bits, skip,
-                                                        tc.err, tc.polls);
+  // one pass per 16 right-hand sides (the passes reuse the scratch, one after the other on the stream);
+  // each pass reads A again, which costs far less than the double-float products it replaces
+  for (int c0 = 0; c0 < lay.m; c0 += kRtCols) {
+    count_launch();
+    residual_x_image_kernel<<<unsigned(batch), 512, 0, s>>>(lay, X64, tc.images, tau, nseg, c0, skip, tc.err);
+    count_launch();
+    residual_tc_kernel<<<grid, kRtThreads, kRtSmem, s>>>(lay, Ms, tc.images, tau, nseg, c0, R, rnorm_bits,
+                                                          bnorm_bits, skip, tc.err, tc.polls);
+  }
   return true;
 }
 

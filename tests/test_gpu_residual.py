@@ -2,7 +2,8 @@
 
 r = b - A x of the FP32 LU forms is computed, by default, from exact products of 8-bit digits of A (scaled per
 row over 32-column segments) and of x (scaled per column) on the bf16 tensor path, the exact level sums combined
-in double-float (REFEFF_FMS_OPT_RESIDUAL_TENSOR = 1); option 0 runs the Dot2 residual on the CUDA cores.  Both
+in double-float, one pass per 16 right-hand sides (REFEFF_FMS_OPT_RESIDUAL_TENSOR = 1); option 0 runs the Dot2
+residual on the CUDA cores.  Both
 must carry the FP32 LU to the FP64 answer: on dense systems whose entries span many orders of magnitude inside
 each row (so the segment scales differ along a row) with right-hand sides of unequal size, on column counts that
 leave the 16-column slots partly empty, on orders that leave the last 128-row tile and the last 32-column segment
@@ -37,7 +38,7 @@ def _dense_case(n, m, seed):
     return A, A @ X
 
 
-@pytest.mark.parametrize("n,m", [(64, 1), (200, 9), (333, 13), (688, 16), (1100, 16)])
+@pytest.mark.parametrize("n,m", [(64, 1), (200, 9), (333, 13), (688, 16), (1100, 16), (700, 25), (300, 32)])
 def test_tensor_residual_refines_to_fp64(n, m):
     A, B = _dense_case(n, m, 13 * n + m)
     out = {}
