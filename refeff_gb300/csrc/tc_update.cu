@@ -28,10 +28,10 @@ namespace {
 constexpr int BM = kTcBM;         // 128 rows per tile (MMA M)
 constexpr int BN = kTcBN;         // 64 columns per tile (MMA N)
 // Operand rows of kRowBytes bytes with the matching swizzle (128 or 64): with
-// 128-byte rows a K chunk holds KC = 32 TF32 values per row.  64-byte rows
-// (half the chunk, twice the ring depth) measured slower: the update is bound
-// by the tensor pipe, not by the depth of the operand ring.
-constexpr int kRowBytes = 128;
+// 64-byte rows a K chunk holds KC = 16 TF32 values per row (56 KB of planes),
+// and four chunks are in flight; 128-byte rows (112 KB chunks, two in flight)
+// measured 2% slower with the paired-N MMAs (and faster before them).
+constexpr int kRowBytes = 64;
 constexpr int KC = kRowBytes / 4;          // K elements per chunk
 constexpr int A_PLANE = BM * kRowBytes;    // bytes per A plane per chunk (16 KB)
 constexpr int B_PLANE = BN * kRowBytes;    // bytes per B plane per chunk (8 KB)
@@ -112,7 +112,7 @@ __device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// operand images: A[b][bm][chunk][plane] (16 KB), B[b][bn][chunk][plane] (8 KB), chunks of KC = 32
+// operand images: A[b][bm][chunk][plane] (8 KB), B[b][bn][chunk][plane] (4 KB), chunks of KC = 16
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) tc_split_a_kernel(BatchLayout lay, int k, int kb, const float2* __restrict__ M,
                                                          uint8_t* __restrict__ img, int nbm) {
@@ -181,9 +181,9 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
 // ---------------------------------------------------------------------------
 // One CTA per SM walks the tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...
 // (t -> matrix b, row tile bm, column tile bn, bn fastest).  Roles:
-//   warp 0   producer: bulk-copies each K-chunk (112 KB of planes) into a
-//            two-stage ring, waiting for the stage to be released;
-//   warp 1   MMA: 24 tcgen05.mma (N = 128: [Cr | Ci]) per chunk into one of four TMEM accumulators
+//   warp 0   producer: bulk-copies each K-chunk (56 KB of planes) into a
+//            four-stage ring, waiting for the stage to be released;
+//   warp 1   MMA: 12 tcgen05.mma (N = 128: [Cr | Ci]) per chunk into one of four TMEM accumulators
 //            (128 columns each), releasing the stage with tcgen05.commit and
 //            signalling the tile's accumulator the same way;
 //   warps 2-17   four epilogue groups of four warps, group g taking the tiles
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256) tc_split_b_kernel(BatchLayout lay, int k,
 // the error flag and a shared abort flag that ends every role's loop, then
 // the producer waits (bounded) for its copies still in flight and the MMA
 // thread for its MMAs before the tensor memory is freed.
-constexpr int kPStages = 2;                    // operand ring depth (2 x 112 KB)
+constexpr int kPStages = 4;                    // operand ring depth (4 x 56 KB)
 constexpr int kPGroups = 4;                     // epilogue groups of 4 warps, one accumulator each
 constexpr int kPThreads = 64 + kPGroups * 128;  // producer warp, MMA warp, epilogue groups
 constexpr uint32_t kPTmemCols = 512;  // kPGroups * 128 columns, rounded up to a power of two
