@@ -353,36 +353,58 @@ __global__ void __launch_bounds__(256) rhs_lower_tile_kernel(BatchLayout lay, in
   const int kb = min(NB, lay.n - k);
   extern __shared__ float2 lt_sm[];
   float2* Li = lt_sm;               // [NB][NB]: Li[i + NB * j] = (L11^-1)(i, j)
-  float2* Bt = lt_sm + NB * NB;     // [2 NB][kLtN]: the moves' staging, then the panel rows [NB][kLtN]
+  float2* Bt = lt_sm + NB * NB;     // [NB][kLtN]: the block rows (after the moves)
+  float2* Bw = Bt + NB * kLtN;      // [NB][kLtN]: rows moved below the block, then U12 of the pair's first block
   float2* Mb = M + size_t(b) * lay.stride;
   const size_t lda = size_t(lay.lda);
   const int tid = threadIdx.x;
-  // the block's composed row moves on these columns
+  // The block's composed row moves (dst, src; every dst >= k) on these columns.  Each block row is read
+  // straight from its source row; a row moved below the block is staged and written back.  At most NB rows
+  // land below the block: each of the block's NB pivot steps moves at most one row out of it.
+  __shared__ int src_of[NB];     // source row of block row i, or -1 when the row stays
+  __shared__ int2 below[NB];     // (dst, src) of the moves with dst >= k + kb
+  __shared__ int nbelow;
   const size_t pidx = size_t(b) * w.npanels + k / NB;
   const int np = w.nperm[pidx];
   const int2* pm = w.perm + pidx * (2 * NB);
-  for (int idx = tid; idx < np * ncols; idx += 256) {
-    const int i = idx % np, c = idx / np;
-    Bt[i * kLtN + c] = Mb[size_t(pm[i].y) + lda * size_t(cb + c)];
-  }
+  for (int i = tid; i < NB; i += 256) src_of[i] = -1;
+  if (tid == 0) nbelow = 0;
   const float4* src = reinterpret_cast<const float4*>(linv + size_t(b) * NB * NB);
   if (kprev < 0)
     for (int idx = tid; idx < NB * NB / 2; idx += 256) reinterpret_cast<float4*>(Li)[idx] = src[idx];
   __syncthreads();
-  for (int idx = tid; idx < np * ncols; idx += 256) {
-    const int i = idx % np, c = idx / np;
-    Mb[size_t(pm[i].x) + lda * size_t(cb + c)] = Bt[i * kLtN + c];
+  for (int i = tid; i < np; i += 256) {
+    const int2 mv = pm[i];
+    if (mv.x < k + kb) {
+      src_of[mv.x - k] = mv.y;
+    } else {
+      const int q = atomicAdd(&nbelow, 1);
+      if (q < NB) below[q] = mv;
+    }
   }
   __syncthreads();
+  const int nbw = min(nbelow, NB);
   for (int idx = tid; idx < NB * kLtN; idx += 256) {
     const int i = idx % NB, c = idx / NB;
-    Bt[i * kLtN + c] = (i < kb && c < ncols) ? Mb[size_t(k + i) + lda * size_t(cb + c)] : make_float2(0.f, 0.f);
+    const int sr = i < kb ? (src_of[i] >= 0 ? src_of[i] : k + i) : -1;
+    Bt[i * kLtN + c] = (sr >= 0 && c < ncols) ? Mb[size_t(sr) + lda * size_t(cb + c)] : make_float2(0.f, 0.f);
+  }
+  for (int idx = tid; idx < nbw * ncols; idx += 256) {
+    const int q = idx % nbw, c = idx / nbw;
+    Bw[q * kLtN + c] = Mb[size_t(below[q].y) + lda * size_t(cb + c)];
+  }
+  __syncthreads();  // every source is read before any row is written
+  for (int idx = tid; idx < nbw * ncols; idx += 256) {
+    const int q = idx % nbw, c = idx / nbw;
+    Mb[size_t(below[q].x) + lda * size_t(cb + c)] = Bw[q * kLtN + c];
   }
   // rows r0 .. r0 + 7 of column `col`
   const int col = tid & 31, r0 = (tid >> 5) * 8;
   if (kprev >= 0) {
-    // the deferred update by the pair's first block: Li <- L21prev, Bt rows [NB, 2 NB) <- U12prev
-    float2* Up = Bt + NB * kLtN;
+    // the deferred update by the pair's first block: Li <- L21prev, Bw <- U12prev (once the rows moved
+    // below the block have left it)
+    __syncthreads();
+    float2* Up = Bw;
     for (int idx = tid; idx < NB * NB; idx += 256) {
       const int i = idx % NB, j = idx / NB;
       Li[i + NB * j] = i < kb ? Mb[size_t(k + i) + lda * size_t(kprev + j)] : make_float2(0.f, 0.f);
