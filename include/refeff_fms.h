@@ -158,8 +158,9 @@ unsigned long long refeff_fms_kernel_launches(void);
  *     products of 8-bit digits of A and x on the bf16 path, summed in
  *     double-float, one pass per 16 right-hand sides; with the tensor-core
  *     update on);
- *     0 in double-float on the FP32 CUDA cores.  Both reach about 2^-46 of
- *     sum |a||x|.  A residual whose bounded wait gives up sends the call's
+ *     0 in double-float on the FP32 CUDA cores.  The tensor-core residual
+ *     reaches about 2^-48 of ||a_row||_1 ||x||_inf (2^-43 of sum |a||x|
+ *     componentwise), the double-float one about 2^-47 of sum |a||x|.  A residual whose bounded wait gives up sends the call's
  *     energies to the FP64 LU. */
 #define REFEFF_FMS_OPT_RESIDUAL_TENSOR 9
 int refeff_fms_context_set_option(refeff_fms_context* ctx, int option, long long value);

@@ -1,8 +1,11 @@
 // Refinement residual R = B - A X on the 5th-generation tensor cores.
 //
-// The refinement of the FP32 LU form needs r = b - A x to about 2^-46 of
-// sum |a| |x| (A and B are stored as hi/lo FP32 pairs, X in FP64).  The
-// products are made exact on the bf16 tensor path by an error-free splitting
+// The refinement of the FP32 LU form needs r = b - A x to well below its
+// stopping tolerance times |A| |x| (A and B are stored as hi/lo FP32 pairs
+// exact to 2^-48, X in FP64).  This residual reaches about 2^-48 of
+// ||a_row||_1 ||x||_inf (each digit cut is exact to 2^-48 of its power-of-two
+// scale); componentwise, where a row's large entries meet small entries of x,
+// about 2^-43 of sum |a| |x|.  The products are made exact on the bf16 tensor path by an error-free splitting
 // after Ozaki, Ogita, Oishi and Rump, "Error-free transformations of matrix
 // multiplication by using fast routines of matrix multiplication and its
 // applications", Numer. Algorithms 59 (2012):
