@@ -5,10 +5,10 @@
 // exact to 2^-48, X in FP64).  This residual reaches about 2^-48 of
 // ||a_row||_1 ||x||_inf (each digit cut is exact to 2^-48 of its power-of-two
 // scale); componentwise, where a row's large entries meet small entries of x,
-// about 2^-43 of sum |a| |x|.  The products are made exact on the bf16 tensor path by an error-free splitting
-// after Ozaki, Ogita, Oishi and Rump, "Error-free transformations of matrix
-// multiplication by using fast routines of matrix multiplication and its
-// applications", Numer. Algorithms 59 (2012):
+// about 2^-43 of sum |a| |x|.  The products are made exact on the bf16 tensor
+// path by an error-free splitting after Ozaki, Ogita, Oishi and Rump,
+// "Error-free transformations of matrix multiplication by using fast routines
+// of matrix multiplication and its applications", Numer. Algorithms 59 (2012):
 //
 //   * every entry of A is scaled by a power of two shared by its row over a
 //     32-column segment, and every column of X by a power of two shared by the
