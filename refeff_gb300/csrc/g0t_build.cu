@@ -596,8 +596,15 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
     return dfc_mul(eph4[p * (4 * L + 1) + (m2 - m1 + 2 * L)], make_float4(sx.hi, sy.hi, sx.lo, sy.lo));
   };
   const int total = nrow * ncol;
-  for (int idx = tid; idx < total; idx += nthr) {
-    const int v = idx % nrow, cc = idx / nrow;
+  // element idx is (row v, column cc) with idx = v + nrow cc; (v, cc) follow idx without a division
+  auto advance = [&](int& v, int& cc) {
+    v += nthr;
+    while (v >= nrow) {
+      v -= nrow;
+      ++cc;
+    }
+  };
+  for (int idx = tid, v = tid % nrow, cc = tid / nrow; idx < total; idx += nthr, advance(v, cc)) {
     const int4 ri = rowinfo[v];
     const int4 ci = colinfo[cc];
     const int rp = ri.x >> 2, rs = ri.x & 3;
