@@ -495,13 +495,24 @@ __global__ void __launch_bounds__(256) build_system_kernel(PlanDev P, const doub
       if (sp == 0) flag[p] = ok;
     }
   }
+  __shared__ int gdec[(kMaxL + 1) * (kMaxL + 1) * (kMaxL + 1)];
+  for (int q = tid; q < L1 * L1 * L1; q += nthr) gdec[q] = (q % L1) | (((q / L1) % L1) << 8) | ((q / (L1 * L1)) << 16);
   __syncthreads();
   // ---- z-axis propagator g(l1, l2, mu) per (pair, spin) (xgllm) ----
+  // entry t = rem + gsz ps of the table, rem = l1 + L1 (l2 + L1 mu); (ps, rem) follow t without a
+  // division, (l1, l2, mu) come from the decode table
   const int gsz = L1 * L1 * L1;
-  for (int t = tid; t < RA * nsp * gsz; t += nthr) {
-    const int ps = t / gsz, rem = t % gsz;
-    const int p = ps / nsp;
-    const int l1 = rem % L1, l2 = (rem / L1) % L1, mu = rem / (L1 * L1);
+  auto advance_g = [&](int& ps, int& rem) {
+    rem += nthr;
+    while (rem >= gsz) {
+      rem -= gsz;
+      ++ps;
+    }
+  };
+  for (int t = tid, ps = tid / gsz, rem = tid % gsz; t < RA * nsp * gsz; t += nthr, advance_g(ps, rem)) {
+    const int p = nsp == 2 ? ps >> 1 : ps;
+    const int dec = gdec[rem];
+    const int l1 = dec & 0xFF, l2 = (dec >> 8) & 0xFF, mu = dec >> 16;
     if constexpr (kMode == 1) {
       // g in double-float: gamtl = c(l1, nu) (2 l1 + 1) / xnlm, gam = c(l2, mu + nu) (-1)^mu xnlm, summed,
       // times the pair prefactor
