@@ -548,6 +548,26 @@ int refeff_ff2x_xscorr(int ne, int ne1, int fermi_index, int ispec, const refeff
                        const refeff_complex128* path_chi, double real_correction, double electronic_temperature_ev,
                        refeff_complex128* cchi_out);
 
+/* FEFF xsect.dat, XSPH's cross-section table, read and handed to FF2X the way
+ * FEFF's rdxbin does (parse_xsect_dat and xsect_dat_ff2x_handoff,
+ * crates/refeff-io/src/xsect_dat.rs:394-760, 268-309): energies from eV to
+ * Hartree, omega = Re(E) - edge + emu, the signed wave number of Re(E) - edge
+ * (sqrt(2|x|) with the sign of x), and the effective S02 = the file's value when
+ * mbconv > 0 or current_s02 <= 0.1, else current_s02.  The arrays feed
+ * refeff_ff2x_xanes_mu / _thermal (energy, omega, cross_section, background).
+ *   counts_out[4]: rows (nxsec), ne1, fermi_index (zero-based ik0 - 1), titles.
+ *   scalars_out[7]: effective s02, the file's s02, erelax, wp, edge, emu
+ *                   (both in Hartree as written), gamach in Hartree.
+ *   energy_out, omega_out, wave_number_out, background_out, cross_section_out:
+ *                   capacity rows each.
+ * With capacity 0 only counts_out is written.  Errors: INVALID_ARGUMENT (file,
+ * record or layout errors, ik0 outside 1..ne1, capacity below the row count),
+ * NONFINITE_INPUT; the reason is in refeff_ff2x_xsect_last_error.  Host only. */
+int refeff_ff2x_read_xsect_dat(const char* path, double current_s02, int mbconv, int capacity, int32_t* counts_out,
+                               double* scalars_out, refeff_complex128* energy_out, double* omega_out,
+                               double* wave_number_out, double* background_out, refeff_complex128* cross_section_out);
+const char* refeff_ff2x_xsect_last_error(void);
+
 /* FEFF conv (crates/refeff-core/src/convolution/lorentzian.rs:32-100): the
  * piecewise-linear spectrum (n >= 2 points over increasing omega) broadened by
  * a Lorentzian of half width `width`, divided by single-precision pi as FEFF

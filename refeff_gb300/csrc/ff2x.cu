@@ -13,10 +13,15 @@
 //   conv1 / conv                           crates/refeff-core/src/convolution/lorentzian.rs:4-100
 //   sig_gk Debye factor on chi            ff2x_xanes_xmu_dat_from_components 3388-3397
 //                                          (refeff_ff2x_debye_factor, after the mu(E) step)
-// The thermal xscorr (4643-) is not restated.
+//   xscorr at a finite temperature         ff2x_thermal_xscorr                4643-5050
+//   xsect.dat reader and rdxbin handoff    crates/refeff-io/src/xsect_dat.rs  268-309, 394-760
 #include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <complex>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -584,6 +589,279 @@ extern "C" int refeff_ff2x_debye_factor(int n, const double* wave_number, double
       chi[r] *= std::exp(-(x * x));
     }
     if (mu && mu0) mu[r] = mu0[r] + chi[r];
+  }
+  return REFEFF_FMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// xsect.dat: XSPH's cross-section table and FEFF's rdxbin handoff to FF2X
+// ---------------------------------------------------------------------------
+// The text format (crates/refeff-io/src/xsect_dat.rs): title records up to a
+// dashed rdhead separator (characters 4-11 all '-'), a method record (s02,
+// erelax, wp, edge, emu; edge and emu in Hartree), a gamach record (the core-hole
+// width in eV, ne1, ik0), a label naming em, xsnorm and xsec, and one row per
+// energy (Re em, Im em in eV, xsnorm, Re xsec, Im xsec).  A leading '#' of any
+// record is skipped, blank lines are ignored, and a record may carry trailing
+// words after its numbers.
+namespace {
+
+std::string g_xsect_error;
+
+int xsect_fail(int code, const std::string& msg) {
+  g_xsect_error = msg;
+  return code;
+}
+
+// Rust str::lines: split on '\n', one trailing '\r' dropped per line
+std::vector<std::string> text_lines(const std::string& text) {
+  std::vector<std::string> out;
+  size_t start = 0;
+  while (start < text.size()) {
+    size_t end = text.find('\n', start);
+    if (end == std::string::npos) end = text.size();
+    std::string line = text.substr(start, end - start);
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    out.push_back(line);
+    start = end + 1;
+  }
+  return out;
+}
+
+bool is_blank(const std::string& s) {
+  for (char ch : s)
+    if (!std::isspace(static_cast<unsigned char>(ch))) return false;
+  return true;
+}
+
+// the record without a leading '#' (and the blanks around it)
+std::string record_body(const std::string& line) {
+  size_t i = 0;
+  while (i < line.size() && std::isspace(static_cast<unsigned char>(line[i]))) ++i;
+  if (i < line.size() && line[i] == '#') {
+    ++i;
+    while (i < line.size() && std::isspace(static_cast<unsigned char>(line[i]))) ++i;
+  }
+  return line.substr(i);
+}
+
+std::vector<std::string> record_tokens(const std::string& line) {
+  std::vector<std::string> out;
+  const std::string body = record_body(line);
+  size_t i = 0;
+  while (i < body.size()) {
+    while (i < body.size() && std::isspace(static_cast<unsigned char>(body[i]))) ++i;
+    size_t j = i;
+    while (j < body.size() && !std::isspace(static_cast<unsigned char>(body[j]))) ++j;
+    if (j > i) out.push_back(body.substr(i, j - i));
+    i = j;
+  }
+  return out;
+}
+
+// A decimal float token as Rust's f64 parser takes it: [+-] digits [. digits] [(e|E) [+-] digits], at least
+// one digit in the mantissa, or inf / infinity / nan in any case.
+bool parse_real_token(const std::string& t, double& v) {
+  size_t i = 0, n = t.size();
+  if (i < n && (t[i] == '+' || t[i] == '-')) ++i;
+  std::string rest = t.substr(i);
+  std::string low;
+  for (char ch : rest) low.push_back(char(std::tolower(static_cast<unsigned char>(ch))));
+  if (low == "inf" || low == "infinity" || low == "nan") {
+    v = low == "nan" ? std::nan("") : (t[0] == '-' ? -HUGE_VAL : HUGE_VAL);
+    return true;
+  }
+  size_t digits = 0;
+  while (i < n && std::isdigit(static_cast<unsigned char>(t[i]))) ++i, ++digits;
+  if (i < n && t[i] == '.') {
+    ++i;
+    while (i < n && std::isdigit(static_cast<unsigned char>(t[i]))) ++i, ++digits;
+  }
+  if (digits == 0) return false;
+  if (i < n && (t[i] == 'e' || t[i] == 'E')) {
+    ++i;
+    if (i < n && (t[i] == '+' || t[i] == '-')) ++i;
+    size_t ed = 0;
+    while (i < n && std::isdigit(static_cast<unsigned char>(t[i]))) ++i, ++ed;
+    if (ed == 0) return false;
+  }
+  if (i != n) return false;
+  v = std::strtod(t.c_str(), nullptr);
+  return true;
+}
+
+// An unsigned integer token as Rust's usize parser takes it: [+] digits.
+bool parse_count_token(const std::string& t, long long& v) {
+  size_t i = t.size() > 0 && t[0] == '+' ? 1 : 0;
+  if (i == t.size()) return false;
+  long long x = 0;
+  for (; i < t.size(); ++i) {
+    if (!std::isdigit(static_cast<unsigned char>(t[i]))) return false;
+    if (x > (1LL << 50)) return false;
+    x = 10 * x + (t[i] - '0');
+  }
+  v = x;
+  return true;
+}
+
+bool is_rdhead_separator(const std::string& line) {
+  if (line.size() < 11) return false;
+  for (size_t k = 3; k < 11; ++k)
+    if (line[k] != '-') return false;
+  return true;
+}
+
+struct XsectDat {
+  int titles = 0;
+  double s02 = 0, erelax = 0, wp = 0, edge = 0, emu = 0, gamach_ev = 0;
+  long long ne1 = 0, ik0 = 0;
+  std::vector<cd> em;
+  std::vector<double> xsnorm;
+  std::vector<cd> xsec;
+};
+
+// parse_xsect_dat, crates/refeff-io/src/xsect_dat.rs:394-429 (the record reader 620-760)
+int parse_xsect_dat(const std::string& text, XsectDat& d) {
+  const std::vector<std::string> lines = text_lines(text);
+  size_t i = 0;
+  bool separator = false;
+  for (; i < lines.size(); ++i) {
+    if (is_rdhead_separator(lines[i])) {
+      separator = true;
+      ++i;
+      break;
+    }
+    if (!is_blank(lines[i])) ++d.titles;
+  }
+  if (!separator) return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat: missing the rdhead separator");
+  auto next_record = [&](const char* field, size_t& line_no) -> const std::string* {
+    for (; i < lines.size(); ++i)
+      if (!is_blank(lines[i])) {
+        line_no = i + 1;
+        return &lines[i++];
+      }
+    g_xsect_error = std::string("xsect.dat: missing the ") + field + " record";
+    return nullptr;
+  };
+  auto reals = [&](const std::string& line, size_t line_no, const char* field, int count, double* out) -> int {
+    const std::vector<std::string> tok = record_tokens(line);
+    if (int(tok.size()) < count)
+      return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat line " + std::to_string(line_no) + ": " + field +
+                                                             " record has " + std::to_string(tok.size()) +
+                                                             " fields, " + std::to_string(count) + " expected");
+    for (int k = 0; k < count; ++k)
+      if (!parse_real_token(tok[size_t(k)], out[k]))
+        return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat line " + std::to_string(line_no) + ": " +
+                                                               field + " field '" + tok[size_t(k)] + "' is not a number");
+    return REFEFF_FMS_OK;
+  };
+  size_t ln = 0;
+  const std::string* method = next_record("method", ln);
+  if (!method) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  double mv[5];
+  if (int rc = reals(*method, ln, "method", 5, mv)) return rc;
+  d.s02 = mv[0], d.erelax = mv[1], d.wp = mv[2], d.edge = mv[3], d.emu = mv[4];
+  const std::string* gam = next_record("gamach", ln);
+  if (!gam) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  {
+    const std::vector<std::string> tok = record_tokens(*gam);
+    if (tok.size() < 3)
+      return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT,
+                        "xsect.dat line " + std::to_string(ln) + ": gamach record has " + std::to_string(tok.size()) +
+                            " fields, 3 expected");
+    if (!parse_real_token(tok[0], d.gamach_ev) || !parse_count_token(tok[1], d.ne1) ||
+        !parse_count_token(tok[2], d.ik0))
+      return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT,
+                        "xsect.dat line " + std::to_string(ln) + ": gamach record is not 'gamach ne1 ik0'");
+  }
+  const std::string* label = next_record("label", ln);
+  if (!label) return REFEFF_FMS_ERR_INVALID_ARGUMENT;
+  {
+    std::string low = record_body(*label);
+    for (char& ch : low) ch = char(std::tolower(static_cast<unsigned char>(ch)));
+    if (low.find("em") == std::string::npos || low.find("xsnorm") == std::string::npos ||
+        low.find("xsec") == std::string::npos)
+      return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat line " + std::to_string(ln) + ": unexpected label");
+  }
+  for (; i < lines.size(); ++i) {
+    if (is_blank(lines[i])) continue;
+    double row[5];
+    if (int rc = reals(lines[i], i + 1, "row", 5, row)) return rc;
+    d.em.emplace_back(row[0], row[1]);
+    d.xsnorm.push_back(row[2]);
+    d.xsec.emplace_back(row[3], row[4]);
+  }
+  // validate_xsect_dat (xsect_dat.rs:443-491): rows, ne1 in 1..=rows, ne1 and ik0 within FEFF's i7 fields,
+  // every value finite
+  const long long rows = (long long)d.em.size();
+  if (rows == 0) return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat: at least one energy row is required");
+  if (d.ne1 < 1 || d.ne1 > rows)
+    return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat: ne1 " + std::to_string(d.ne1) + " must be in 1.." +
+                                                           std::to_string(rows));
+  if (d.ne1 > 9999999 || d.ik0 > 9999999)
+    return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat: ne1 or ik0 does not fit FEFF's i7 field");
+  const double sc[6] = {d.s02, d.erelax, d.wp, d.edge, d.emu, d.gamach_ev};
+  for (double v : sc)
+    if (!std::isfinite(v)) return xsect_fail(REFEFF_FMS_ERR_NONFINITE_INPUT, "xsect.dat: a scalar is not finite");
+  for (long long r = 0; r < rows; ++r)
+    if (!std::isfinite(d.em[size_t(r)].real()) || !std::isfinite(d.em[size_t(r)].imag()) ||
+        !std::isfinite(d.xsnorm[size_t(r)]) || !std::isfinite(d.xsec[size_t(r)].real()) ||
+        !std::isfinite(d.xsec[size_t(r)].imag()))
+      return xsect_fail(REFEFF_FMS_ERR_NONFINITE_INPUT, "xsect.dat: row " + std::to_string(r + 1) + " is not finite");
+  return REFEFF_FMS_OK;
+}
+
+}  // namespace
+
+extern "C" const char* refeff_ff2x_xsect_last_error(void) { return g_xsect_error.c_str(); }
+
+// xsect_dat_ff2x_handoff, crates/refeff-io/src/xsect_dat.rs:268-309
+extern "C" int refeff_ff2x_read_xsect_dat(const char* path, double current_s02, int mbconv, int capacity,
+                                          int32_t* counts_out, double* scalars_out, refeff_complex128* energy_out,
+                                          double* omega_out, double* wave_number_out, double* background_out,
+                                          refeff_complex128* cross_section_out) {
+  g_xsect_error.clear();
+  if (!path || !counts_out || capacity < 0) return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "null path or counts");
+  std::FILE* f = std::fopen(path, "rb");
+  if (!f) return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, std::string("cannot open ") + path);
+  std::string text;
+  char buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, got);
+  std::fclose(f);
+  XsectDat d;
+  if (int rc = parse_xsect_dat(text, d)) return rc;
+  if (!std::isfinite(current_s02)) return xsect_fail(REFEFF_FMS_ERR_NONFINITE_INPUT, "s02 must be finite");
+  if (d.ik0 < 1 || d.ik0 > d.ne1)
+    return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "xsect.dat: Fermi index " + std::to_string(d.ik0) +
+                                                           " must be in 1.." + std::to_string(d.ne1));
+  const int rows = int(d.em.size());
+  counts_out[0] = rows;
+  counts_out[1] = int32_t(d.ne1);
+  counts_out[2] = int32_t(d.ik0 - 1);
+  counts_out[3] = d.titles;
+  if (capacity == 0) return REFEFF_FMS_OK;
+  if (capacity < rows || !scalars_out || !energy_out || !omega_out || !wave_number_out || !background_out ||
+      !cross_section_out)
+    return xsect_fail(REFEFF_FMS_ERR_INVALID_ARGUMENT, "capacity below the row count, or a null output");
+  // FEFF takes the file's S02 when mbconv > 0 or the current S02 is at most 0.1
+  scalars_out[0] = (mbconv > 0 || current_s02 <= 0.1) ? d.s02 : current_s02;
+  scalars_out[1] = d.s02;
+  scalars_out[2] = d.erelax;
+  scalars_out[3] = d.wp;
+  scalars_out[4] = d.edge;
+  scalars_out[5] = d.emu;
+  scalars_out[6] = d.gamach_ev / kHartreeEv;
+  for (int r = 0; r < rows; ++r) {
+    const cd e = d.em[size_t(r)] / kHartreeEv;
+    energy_out[r].re = e.real();
+    energy_out[r].im = e.imag();
+    omega_out[r] = e.real() - d.edge + d.emu;
+    const double x = e.real() - d.edge;  // signed wave number (crates/refeff-core/src/grid/radial.rs:7-10)
+    const double mag = std::sqrt(std::fabs(2.0 * x));
+    wave_number_out[r] = x < 0.0 ? -mag : mag;
+    background_out[r] = d.xsnorm[size_t(r)];
+    cross_section_out[r].re = d.xsec[size_t(r)].real();
+    cross_section_out[r].im = d.xsec[size_t(r)].imag();
   }
   return REFEFF_FMS_OK;
 }

@@ -165,6 +165,8 @@ def load(build_if_missing: bool = True):
         "refeff_fms_plan_get_tuning": ([_p, _p, _p], _i),
         "refeff_fms_write_geom_dat": ([C.c_char_p, C.c_char_p], _i),
         "refeff_fms_feff_inp_last_error": ([], C.c_char_p),
+        "refeff_ff2x_read_xsect_dat": ([C.c_char_p, C.c_double, _i, _i, _p, _p, _p, _p, _p, _p, _p], _i),
+        "refeff_ff2x_xsect_last_error": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -757,6 +759,32 @@ def geometry_from_feff_inp(path):
     if rc:
         raise FmsError(rc, lib.refeff_fms_feff_inp_last_error().decode())
     return xyz, ipot, model
+
+
+def ff2x_read_xsect_dat(path, s02=1.0, mbconv=0) -> dict:
+    """XSPH's xsect.dat handed to FF2X as FEFF's rdxbin does (refeff_ff2x_read_xsect_dat): energies in Hartree,
+    omega, signed wave numbers, background (xsnorm), cross section, ne1, the zero-based Fermi index and the
+    effective S02 (the file's when mbconv > 0 or s02 <= 0.1)."""
+    lib = load()
+    b = str(path).encode()
+    counts = np.zeros(4, np.int32)
+    rc = lib.refeff_ff2x_read_xsect_dat(b, float(s02), int(mbconv), 0, _ptr(counts), None, None, None, None, None,
+                                        None)
+    if rc:
+        raise FmsError(rc, lib.refeff_ff2x_xsect_last_error().decode())
+    n = int(counts[0])
+    sc = np.zeros(7)
+    energy = np.zeros(n, np.complex128)
+    omega, wave, background = np.zeros(n), np.zeros(n), np.zeros(n)
+    xsec = np.zeros(n, np.complex128)
+    rc = lib.refeff_ff2x_read_xsect_dat(b, float(s02), int(mbconv), n, _ptr(counts), _ptr(sc), _ptr(energy),
+                                        _ptr(omega), _ptr(wave), _ptr(background), _ptr(xsec))
+    if rc:
+        raise FmsError(rc, lib.refeff_ff2x_xsect_last_error().decode())
+    return {"rows": n, "ne1": int(counts[1]), "fermi_index": int(counts[2]), "titles": int(counts[3]),
+            "s02": sc[0], "file_s02": sc[1], "erelax": sc[2], "wp": sc[3], "edge": sc[4], "emu": sc[5],
+            "core_hole_width": sc[6], "energy": energy, "omega": omega, "wave_number": wave,
+            "background": background, "cross_section": xsec}
 
 
 def write_geom_dat(feff_inp, geom_dat) -> None:

@@ -23,6 +23,7 @@ XSCORR = "crates/refeff-core/src/xscorr.rs"
 RECIP = "crates/refeff-core/src/fms/tests/reciprocal.rs"
 CONV = "crates/refeff-core/src/convolution/tests.rs"
 FF2X_TESTS = "crates/refeff-engine/src/ff2x/tests.rs"
+XSECT_DAT = "crates/refeff-io/src/xsect_dat.rs"
 
 
 def c(re_, im_, src):
@@ -288,6 +289,43 @@ KATS = {
         "temperature_ev": r(0.5, f"{FF2X_TESTS}:1166"),
         "corrected_im": r([2.585850230196276, 5.000003995527989, 7.414157694791554], f"{FF2X_TESTS}:1170-1173"),
         "tolerance": r(1.0e-11, f"{FF2X_TESTS}:1176"),
+    },
+    # FEFF xsect.dat: the comment-prefixed records of the codec's parse test and what they parse to.
+    "xsect_dat_parse": {
+        "text": {"text": "# Cu crystal\n#  -----------------------------------------------------------------------\n"
+                         "#   8.50000E-01  1.50000E-01  2.40000E+00  9.1000000E+00 -4.0000000E-01 method to calculate xsect\n"
+                         "#   1.2300000E+00      2      1 gamach in eV, # of points on horizontal axis\n"
+                         "#       em              xsnorm            xsec  \n"
+                         "  1.250000000E+00  1.00000E-02  2.00000E+00  3.00000E+00 -4.00000E-01\n"
+                         "  1.500000000E+00  2.00000E-02  2.50000E+00  3.50000E+00 -5.00000E-01\n",
+                 "src": f"{XSECT_DAT}:920"},
+        "main_energy_count": r(2, f"{XSECT_DAT}:923"),
+        "fermi_index": r(1, f"{XSECT_DAT}:924"),
+        "energy_0": c(1.25, 0.01, f"{XSECT_DAT}:926"),
+        "cross_section_1": c(3.5, -0.5, f"{XSECT_DAT}:927"),
+    },
+    # FEFF rdxbin handoff (xsect_dat_ff2x_handoff) of the codec's three-row sample: eV -> Hartree energies,
+    # omega = Re(E) - edge + emu, the signed wave number of Re(E) - edge, and FEFF's S02 rule.
+    "xsect_ff2x_handoff": {
+        "scalars": r([0.85, 0.15, 2.4, 9.1, -0.4], f"{XSECT_DAT}:1202-1206"),
+        "core_hole_width_ev": r(1.23, f"{XSECT_DAT}:1208"),
+        "ne1": r(2, f"{XSECT_DAT}:1209"),
+        "ik0": r(1, f"{XSECT_DAT}:1210"),
+        "energy_ev": [c(1.25, 0.01, f"{XSECT_DAT}:1212"), c(1.5, 0.02, f"{XSECT_DAT}:1213"),
+                      c(10.0, 0.03, f"{XSECT_DAT}:1214")],
+        "background": r([2.0, 2.5, 3.0], f"{XSECT_DAT}:1216"),
+        "cross_section": [c(3.0, -0.4, f"{XSECT_DAT}:1218"), c(3.5, -0.5, f"{XSECT_DAT}:1219"),
+                          c(4.0, -0.6, f"{XSECT_DAT}:1220")],
+        "s02_args": r([0.05, 0], f"{XSECT_DAT}:959"),
+        "core_hole_width_hartree": r(0.04520165007337367, f"{XSECT_DAT}:969"),
+        "energy_hartree": [c(0.045936636253428524, 0.0003674930900274282, f"{XSECT_DAT}:977"),
+                           c(0.05512396350411423, 0.0007349861800548564, f"{XSECT_DAT}:978"),
+                           c(0.3674930900274282, 0.0011024792700822846, f"{XSECT_DAT}:979")],
+        "omega_hartree": r([-9.454063363746572, -9.444876036495886, -9.132506909972571], f"{XSECT_DAT}:982-984"),
+        "wave_number": r([-4.255364464707241, -4.253204917822767, -4.1791163922467085], f"{XSECT_DAT}:987-989"),
+        "s02_keep": {"args": r([0.9, 0], f"{XSECT_DAT}:1039"), "want": r(0.9, f"{XSECT_DAT}:1040")},
+        "s02_file": {"args": r([0.9, 1], f"{XSECT_DAT}:1043"), "want": r(0.85, f"{XSECT_DAT}:1044")},
+        "tolerance": r(1.0e-14, f"{XSECT_DAT}:1227"),
     },
     # FEFF conv1 / conv on the convolution fixture (omega, spectrum), width 0.2, tolerance 1e-12.
     "lorentz_conv": {

@@ -237,3 +237,95 @@ def test_thermal_xscorr_rejects_short_layouts_and_bad_temperatures():
     with pytest.raises(fms.FmsError):
         fms.ff2x_xscorr(energy=f["energy"], ne1=3, fermi_index=1, cross_section=f["xsec"], background=f["bg"],
                         path_chi=np.zeros(ne), electronic_temperature=-0.1)
+
+
+# ---- xsect.dat reader and the rdxbin handoff (crates/refeff-io/src/xsect_dat.rs) ----
+
+def _xsect_text(scalars, gamach_ev, ne1, ik0, energy, background, cross_section, title="Cu crystal"):
+    """xsect.dat records in FEFF's layout (the reader takes any decimal field, so full precision is kept)."""
+    out = [f"# {title}", "#  " + "-" * 71]
+    out.append("# " + "".join(f" {v:.17e}" for v in scalars) + " method to calculate xsect")
+    out.append(f"#  {gamach_ev:.17e} {ne1:6d} {ik0:6d} gamach in eV, # of points on horizontal axis")
+    out.append("#       em              xsnorm            xsec  ")
+    for e, b, x in zip(energy, background, cross_section):
+        out.append(f"  {e.real:.17e} {e.imag:.17e} {b:.17e} {x.real:.17e} {x.imag:.17e}")
+    return "\n".join(out) + "\n"
+
+
+def _close(a, b, tol):
+    return abs(a - b) <= tol * max(1.0, abs(b))
+
+
+def test_xsect_dat_parses_reference_records(tmp_path):
+    """The codec's comment-prefixed records parse to what the reference's parse test asserts."""
+    k = KAT["xsect_dat_parse"]
+    p = tmp_path / "xsect.dat"
+    p.write_text(k["text"]["text"])
+    d = fms.ff2x_read_xsect_dat(p, s02=0.05)
+    assert d["rows"] == 2 and d["titles"] == 1
+    assert d["ne1"] == k["main_energy_count"]["value"]
+    assert d["fermi_index"] == k["fermi_index"]["value"] - 1
+    e0 = d["energy"][0] * 27.211396
+    assert _close(e0.real, k["energy_0"]["value"][0], 1e-14) and _close(e0.imag, k["energy_0"]["value"][1], 1e-14)
+    assert d["cross_section"][1] == complex(*k["cross_section_1"]["value"])
+    assert d["s02"] == 0.85 and d["file_s02"] == 0.85
+
+
+def test_xsect_dat_ff2x_handoff_matches_reference(tmp_path):
+    """Energies in Hartree, omega, signed wave numbers and the core-hole width of the reference's three-row
+    handoff test, to its 1e-14 tolerance; S02 follows FEFF's rule."""
+    k = KAT["xsect_ff2x_handoff"]
+    energy = [complex(*v["value"]) for v in k["energy_ev"]]
+    xsec = [complex(*v["value"]) for v in k["cross_section"]]
+    p = tmp_path / "xsect.dat"
+    p.write_text(_xsect_text(k["scalars"]["value"], k["core_hole_width_ev"]["value"], k["ne1"]["value"],
+                             k["ik0"]["value"], energy, k["background"]["value"], xsec))
+    s02, mbconv = k["s02_args"]["value"]
+    d = fms.ff2x_read_xsect_dat(p, s02=s02, mbconv=mbconv)
+    tol = k["tolerance"]["value"]
+    assert d["rows"] == 3 and d["ne1"] == 2 and d["fermi_index"] == 0
+    assert _close(d["core_hole_width"], k["core_hole_width_hartree"]["value"], tol)
+    assert _close(d["s02"], 0.85, tol) and _close(d["edge"], 9.1, tol) and _close(d["emu"], -0.4, tol)
+    for r in range(3):
+        want = k["energy_hartree"][r]["value"]
+        assert _close(d["energy"][r].real, want[0], tol) and _close(d["energy"][r].imag, want[1], tol), r
+        assert _close(d["omega"][r], k["omega_hartree"]["value"][r], tol), r
+        assert _close(d["wave_number"][r], k["wave_number"]["value"][r], tol), r
+        assert d["cross_section"][r] == xsec[r] and d["background"][r] == k["background"]["value"][r]
+    for case in ("s02_keep", "s02_file"):
+        cur, mb = k[case]["args"]["value"]
+        assert _close(fms.ff2x_read_xsect_dat(p, s02=cur, mbconv=mb)["s02"], k[case]["want"]["value"], tol)
+
+
+def test_xsect_dat_feeds_the_xanes_step(tmp_path):
+    """The handoff arrays run FF2X's XANES step as they come out of the reader."""
+    ne, ne1 = 30, 20
+    grid = np.linspace(-5.0, 40.0, ne1)
+    energy = [complex(x, 0.1) for x in grid] + [complex(0.0, 0.1 + 0.5 * j) for j in range(ne - ne1)]
+    background = [1.0 + 0.01 * j for j in range(ne)]
+    xsec = [complex(0.5 + 0.02 * j, 0.01) for j in range(ne)]
+    p = tmp_path / "xsect.dat"
+    p.write_text(_xsect_text([0.9, 0.0, 0.0, 0.0, 0.0], 1.5, ne1, 8, energy, background, xsec))
+    d = fms.ff2x_read_xsect_dat(p, s02=0.9)
+    assert d["rows"] == ne and d["ne1"] == ne1 and d["fermi_index"] == 7
+    assert np.allclose(d["energy"] * 27.211396, energy, rtol=1e-15, atol=1e-15)
+    assert np.all(np.diff(d["omega"][:ne1]) > 0)
+    assert np.array_equal(np.sign(d["wave_number"][:ne1]), np.sign(d["energy"][:ne1].real))
+
+
+@pytest.mark.parametrize("text,fragment", [
+    ("# Cu\n# title without separator\n", "separator"),
+    ("# Cu\n#  -----------------------------------------------------------------------\n# nope\n", "method"),
+    ("# Cu\n#  --------\n# 1 2 3 4 5\n# 1.0 1 1\n# nothing here\n 1 2 3 4 5\n", "label"),
+    ("# Cu\n#  --------\n# 1 2 3 4 5\n# 1.0 2 1\n# em xsnorm xsec\n 1 2 3 4 5\n", "ne1"),
+    ("# Cu\n#  --------\n# 1 2 3 4 5\n# 1.0 1 0\n# em xsnorm xsec\n 1 2 3 4 5\n", "Fermi index"),
+    ("# Cu\n#  --------\n# 1 2 3 4 5\n# 1.0 1 1\n# em xsnorm xsec\n 1 2 3 4\n", "fields"),
+    ("# Cu\n#  --------\n# 1 2 3 4 5\n# 1.0 1 1\n# em xsnorm xsec\n 1 2 3 4 1.0D+00\n", "not a number"),
+    ("# Cu\n#  --------\n# 1 2 3 4 5\n# 1.0 1 1\n# em xsnorm xsec\n", "at least one"),
+])
+def test_xsect_dat_rejects_bad_records(tmp_path, text, fragment):
+    p = tmp_path / "xsect.dat"
+    p.write_text(text)
+    with pytest.raises(fms.FmsError) as err:
+        fms.ff2x_read_xsect_dat(p)
+    assert fragment in str(err.value), str(err.value)
