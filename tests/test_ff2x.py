@@ -298,19 +298,33 @@ def test_xsect_dat_ff2x_handoff_matches_reference(tmp_path):
 
 
 def test_xsect_dat_feeds_the_xanes_step(tmp_path):
-    """The handoff arrays run FF2X's XANES step as they come out of the reader."""
-    ne, ne1 = 30, 20
-    grid = np.linspace(-5.0, 40.0, ne1)
-    energy = [complex(x, 0.1) for x in grid] + [complex(0.0, 0.1 + 0.5 * j) for j in range(ne - ne1)]
-    background = [1.0 + 0.01 * j for j in range(ne)]
-    xsec = [complex(0.5 + 0.02 * j, 0.01) for j in range(ne)]
+    """Seeded XANES rows written as an xsect.dat (energies in eV, edge 0 and emu set so that omega is the rows'
+    photon energies), read back and handed to FF2X: mu(E) from the file equals mu(E) from the rows themselves,
+    and both equal the oracle's."""
+    d = xanes_inputs(np.random.default_rng(3))
+    emu = float(d["omega"][0] - d["energy"][0].real)
     p = tmp_path / "xsect.dat"
-    p.write_text(_xsect_text([0.9, 0.0, 0.0, 0.0, 0.0], 1.5, ne1, 8, energy, background, xsec))
-    d = fms.ff2x_read_xsect_dat(p, s02=0.9)
-    assert d["rows"] == ne and d["ne1"] == ne1 and d["fermi_index"] == 7
-    assert np.allclose(d["energy"] * 27.211396, energy, rtol=1e-15, atol=1e-15)
-    assert np.all(np.diff(d["omega"][:ne1]) > 0)
-    assert np.array_equal(np.sign(d["wave_number"][:ne1]), np.sign(d["energy"][:ne1].real))
+    p.write_text(_xsect_text([0.9, 0.0, 0.0, 0.0, emu], 1.5, d["ne1"], d["fermi"] + 1,
+                             d["energy"] * 27.211396, d["bg"], d["xsec"]))
+    h = fms.ff2x_read_xsect_dat(p, s02=0.9)
+    assert h["rows"] == d["energy"].shape[0] and h["ne1"] == d["ne1"] and h["fermi_index"] == d["fermi"]
+    assert np.allclose(h["energy"], d["energy"], rtol=1e-15, atol=1e-17)
+    assert np.allclose(h["omega"][:d["ne1"]], d["omega"], rtol=1e-14, atol=0)
+    kw = dict(ne1=h["ne1"], fermi_index=h["fermi_index"], trace=d["trace"], s02=h["s02"],
+              fermi_photon_energy=d["fermi_photon"])
+    got = fms.ff2x_xanes_mu(energy=h["energy"], omega=h["omega"][:h["ne1"]], cross_section=h["cross_section"],
+                            background=h["background"], **kw)
+    direct = fms.ff2x_xanes_mu(energy=d["energy"], omega=d["omega"], cross_section=d["xsec"], background=d["bg"],
+                               **kw)
+    want = fo.xanes_mu(energy=list(h["energy"]), ne1=h["ne1"], fermi=h["fermi_index"],
+                       omega=list(h["omega"][:h["ne1"]]), cross_section=list(h["cross_section"]),
+                       background=list(h["background"]), trace=list(d["trace"]), s02=h["s02"],
+                       fermi_photon_energy=d["fermi_photon"])
+    for g, r, w in zip(got, direct, want):
+        w = np.asarray(w)
+        scale = max(np.abs(w).max(), 1.0)
+        assert np.abs(g - r).max() <= 1e-12 * scale
+        assert np.abs(g - w).max() <= 1e-12 * scale
 
 
 @pytest.mark.parametrize("text,fragment", [
