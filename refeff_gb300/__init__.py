@@ -14,7 +14,9 @@ from .fms import (  # noqa: F401
     PrecondModel,
     complex_lu_solve_batched,
     debye_sigma2_table,
+    ff2x_read_xsect_dat,
     ff2x_xanes_mu,
+    ff2x_xscorr,
     fms_full_scattering_spectrum,
     fms_real_space_plan,
     fms_real_space_spectrum,
@@ -40,7 +42,7 @@ from .fms import (  # noqa: F401
 
 __all__ = [
     "FORM_BICGSTAB", "FORM_FP32_REFINED", "FORM_FP64_LU", "Context", "FmsError", "FmsRealSpacePlan", "PrecondModel", "complex_lu_solve_batched",
-    "debye_sigma2_table", "ff2x_xanes_mu", "fms_full_scattering_spectrum",
+    "debye_sigma2_table", "ff2x_read_xsect_dat", "ff2x_xanes_mu", "ff2x_xscorr", "fms_full_scattering_spectrum",
     "fms_real_space_plan", "fms_real_space_spectrum", "fms_real_space_spectrum_device", "fms_real_space_spectrum_multi",
     "fms_yprep_cluster",
     "gg_section", "load", "mkgtr_trace", "mkgtr_trace_device", "read_phase_bin", "reciprocal_core_hole",
